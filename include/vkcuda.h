@@ -1,0 +1,190 @@
+/*
+ * vkcuda: the GB300 (sm_103a) kernel backend of the verkehrt array language, behind a C ABI.
+ *
+ * The reference interpreter (antiguru/verkehrt, Rust) resolves one entry per kernel from its
+ * kernel table (src/kernels.rs:302, KernelTable; src/kernels.rs:632-644, Registry::resolve)
+ * and calls it through Dispatch (src/kernels/dispatch.rs:25-268). This library is the entry
+ * set of a new `cuda` ISA slot in that table. Each function below names the reference
+ * interface it replaces. Arrays are device-resident handles, so bindings stay in HBM between
+ * statements and host<->device copies happen only at vkc_array_upload / vkc_array_download.
+ *
+ * Conventions
+ *  - Every function that can fail returns a vkc_status. On VKC_RUNTIME the message of
+ *    vkc_last_error() is byte-identical to the reference kernel's `Err(String)`.
+ *  - Input handles are borrowed and never mutated (arrays are immutable, src/value.rs:215).
+ *    Output handles are new references owned by the caller (release with vkc_array_release).
+ *  - Calls are synchronous from the caller's view: a returned scalar is final and a returned
+ *    array may be read or passed to the next call at once (same context stream).
+ *  - A context is used by one host thread at a time.
+ */
+#ifndef VKCUDA_H
+#define VKCUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define VKC_API __attribute__((visibility("default")))
+#else
+#define VKC_API
+#endif
+
+/* Status codes. src/error.rs:1-40 has one runtime kind; the split below tells the caller
+ * whether the message is a kernel error (RUNTIME, formatted like the reference) or a failure
+ * of the backend itself. */
+typedef enum {
+    VKC_OK = 0,
+    VKC_RUNTIME = 1, /* kernel error, reference message text in vkc_last_error */
+    VKC_ALLOC = 2,   /* device allocation failed ("cannot allocate ..." message) */
+    VKC_TIMEOUT = 3, /* a bounded device-side wait gave up; the context stays usable */
+    VKC_DEVICE = 4,  /* CUDA runtime error */
+    VKC_USAGE = 5    /* bad kernel id, arity, kind or handle */
+} vkc_status;
+
+/* Element types, src/value.rs:7-19 (ScalarType) restricted to ARRAY_TYPES (:23-31). Bool is
+ * stored as one byte holding 0 or 1. */
+typedef enum {
+    VKC_F64 = 0,
+    VKC_F32 = 1,
+    VKC_I64 = 2,
+    VKC_U64 = 3,
+    VKC_I32 = 4,
+    VKC_U8 = 5,
+    VKC_BOOL = 6
+} vkc_type;
+
+/* Kernel classes, src/kernels.rs:336-343 (KernelClass). */
+typedef enum {
+    VKC_ELEMENTWISE = 0,
+    VKC_REDUCTION = 1,
+    VKC_SELECTION = 2,
+    VKC_SCAN = 3,
+    VKC_WHOLE = 4
+} vkc_class;
+
+typedef struct vkc_ctx vkc_ctx;
+typedef struct vkc_array vkc_array;
+typedef struct vkc_reducer vkc_reducer;
+typedef struct vkc_scanner vkc_scanner;
+typedef struct vkc_builder vkc_builder;
+
+/* A scalar, src/value.rs (Scalar): the type and the value's bits in the low bytes of `bits`
+ * (little-endian, f64 as its IEEE bits, bool as 0/1). */
+typedef struct {
+    vkc_type type;
+    uint64_t bits;
+} vkc_scalar;
+
+/* A value, src/value.rs:640 (Value) and :464 (Arg): an array handle or a scalar. Arg::Rows is
+ * kind VKC_VALUE_ARRAY, Arg::Splat is VKC_VALUE_SCALAR. */
+typedef enum { VKC_VALUE_ARRAY = 0, VKC_VALUE_SCALAR = 1 } vkc_value_kind;
+typedef struct {
+    vkc_value_kind kind;
+    vkc_array *array;
+    vkc_scalar scalar;
+} vkc_value;
+
+/* ------------------------------------------------------------------ context */
+
+/* Opens a context on CUDA device `device`: one stream, one scratch arena. Replaces the
+ * per-interpreter Registry::resolve (src/kernels.rs:632-644) for the `cuda` ISA; the level
+ * check of features::runnable (src/kernels/features.rs:198-212) becomes "a device is
+ * present", which this call reports as VKC_DEVICE when it is not. */
+VKC_API vkc_status vkc_open(int device, vkc_ctx **out);
+VKC_API void vkc_close(vkc_ctx *ctx);
+/* The message of the last failed call on this context (empty string when none). */
+VKC_API const char *vkc_last_error(const vkc_ctx *ctx);
+/* Waits for all work of the context. */
+VKC_API vkc_status vkc_synchronize(vkc_ctx *ctx);
+/* Runs the context's work on `stream` (a cudaStream_t) instead of its own stream. */
+VKC_API vkc_status vkc_set_stream(vkc_ctx *ctx, void *stream);
+VKC_API void *vkc_get_stream(const vkc_ctx *ctx);
+/* Number of kernels this library launched on the context since it was opened. */
+VKC_API uint64_t vkc_launch_count(const vkc_ctx *ctx);
+/* CUDA-event timing on the context stream: start, then stop returns milliseconds. */
+VKC_API vkc_status vkc_timer_start(vkc_ctx *ctx);
+VKC_API vkc_status vkc_timer_stop(vkc_ctx *ctx, float *ms);
+
+/* ------------------------------------------------------------------ arrays */
+
+/* A new zeroed array of `len` rows of `type`, src/value.rs:326-336 (Array::try_build). Fails
+ * with "array of N elements is too large" (value.rs:285-289) or "cannot allocate an array of
+ * N elements" (value.rs:297-307). */
+VKC_API vkc_status vkc_array_new(vkc_ctx *ctx, vkc_type type, int64_t len, vkc_array **out);
+/* Copies `len` rows from host memory into a new device array (program inputs). */
+VKC_API vkc_status vkc_array_upload(vkc_ctx *ctx, vkc_type type, const void *host, int64_t len,
+                            vkc_array **out);
+/* Copies the array's rows into host memory, `capacity` rows at most (print and exports). */
+VKC_API vkc_status vkc_array_download(vkc_ctx *ctx, const vkc_array *a, void *host, int64_t capacity);
+/* A zero-copy view of rows start..start+len, src/value.rs:245-259 (Array::slice) and
+ * src/kernels/scalar/index.rs:76-93 (slice_T). */
+VKC_API vkc_status vkc_array_slice(vkc_ctx *ctx, const vkc_array *a, int64_t start, int64_t len,
+                           vkc_array **out);
+VKC_API int64_t vkc_array_len(const vkc_array *a);
+VKC_API vkc_type vkc_array_type(const vkc_array *a);
+/* Device address of row 0 of the view. */
+VKC_API void *vkc_array_device_ptr(const vkc_array *a);
+VKC_API void vkc_array_retain(vkc_array *a);
+VKC_API void vkc_array_release(vkc_array *a);
+
+/* ------------------------------------------------------------------ kernel table */
+
+/* The kernels with a `cuda` entry, named as in the reference registry (src/kernels.rs:471-482,
+ * Registry::new; names from src/kernels/scalar/*::register). Ids are dense, 0..count-1. */
+VKC_API int vkc_kernel_count(void);
+VKC_API const char *vkc_kernel_name(int id);
+/* Registry::by_name, src/kernels.rs:620-622: the id, or -1. */
+VKC_API int vkc_kernel_lookup(const char *name);
+VKC_API vkc_class vkc_kernel_class(int id);
+VKC_API int vkc_kernel_arity(int id);
+/* KernelDef::cost, src/kernels.rs:417-418: bytes moved per element. */
+VKC_API uint64_t vkc_kernel_cost(int id);
+
+/* ------------------------------------------------------------------ entries */
+
+/* Dispatch::call, src/kernels/dispatch.rs:56-142: runs kernel `id` over whole arguments. It
+ * unifies array lengths first ("length mismatch: a vs b"), then an elementwise kernel gets
+ * its output allocated, a reduction is updated once with all rows (never on empty input), a
+ * scan is updated once, a selection runs with base 0, and a whole kernel checks its own
+ * arguments. On success `*out` holds the result value. */
+VKC_API vkc_status vkc_call(vkc_ctx *ctx, int id, const vkc_value *args, int nargs, vkc_value *out);
+
+/* Reducer (src/kernels.rs:48-63) for tile-fed callers, handed out by Dispatch::reducer
+ * (src/kernels/dispatch.rs:156-163). Every update but the last has a multiple of 16 rows;
+ * the canonical float state carries across updates, so any such split gives the bits of one
+ * update (Split::Free, src/kernels.rs:158-170). finish consumes the reducer. */
+VKC_API vkc_status vkc_reducer_new(vkc_ctx *ctx, int id, vkc_reducer **out);
+VKC_API vkc_status vkc_reducer_update(vkc_reducer *r, const vkc_value *args, int nargs);
+VKC_API vkc_status vkc_reducer_finish(vkc_reducer *r, vkc_scalar *out);
+VKC_API void vkc_reducer_free(vkc_reducer *r);
+
+/* Scanner (src/kernels.rs:65-88) for tile-fed callers, Dispatch::scanner
+ * (src/kernels/dispatch.rs:177-185). update writes exactly the tile's output rows into `out`
+ * (a caller-owned array of the tile's length); the state carries to the next update. */
+VKC_API vkc_status vkc_scanner_new(vkc_ctx *ctx, int id, vkc_scanner **out);
+VKC_API vkc_status vkc_scanner_update(vkc_scanner *s, const vkc_value *args, int nargs, vkc_array *out);
+VKC_API void vkc_scanner_free(vkc_scanner *s);
+
+/* ArrayBuilder (src/value.rs:471-600): an appendable device array for selections. */
+VKC_API vkc_status vkc_builder_new(vkc_ctx *ctx, vkc_type type, vkc_builder **out);
+VKC_API vkc_status vkc_builder_finish(vkc_builder *b, vkc_array **out);
+VKC_API void vkc_builder_free(vkc_builder *b);
+
+/* Dispatch::select_tile, src/kernels/dispatch.rs:236-265: appends the selected rows of one
+ * tile whose first row is row `base` of the whole array. */
+VKC_API vkc_status vkc_select_tile(vkc_ctx *ctx, int id, const vkc_value *args, int nargs, int64_t base,
+                           vkc_builder *out);
+
+/* Dispatch::elementwise_tile, src/kernels/dispatch.rs:192-229: writes the tile's rows into
+ * `out`, whose length must equal every array argument's. */
+VKC_API vkc_status vkc_elementwise_tile(vkc_ctx *ctx, int id, const vkc_value *args, int nargs,
+                                vkc_array *out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

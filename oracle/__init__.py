@@ -1,0 +1,342 @@
+"""The CPU oracle: TEST INFRASTRUCTURE ONLY.
+
+numpy-facing ctypes wrapper over liboracle.so, the plain-C restatement of the reference's
+scalar kernel entries (oracle.c cites the reference file:line of each). Only tests/,
+__graft_entry__.smoke() and bench.py's CPU-baseline leg use it; the CUDA library never does.
+Functions that fail raise OracleError with the reference's message text.
+"""
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+_lib = None
+ERR_LEN = 256
+CMPS = {"eq": 0, "ne": 1, "lt": 2, "le": 3, "gt": 4, "ge": 5}
+
+
+class OracleError(Exception):
+    pass
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _build.build()
+        _lib = ctypes.CDLL(path)
+        L = _lib
+        P, I64, D, U64 = ctypes.c_void_p, ctypes.c_int64, ctypes.c_double, ctypes.c_uint64
+        L.orc_splitmix64.restype = U64
+        L.orc_splitmix64.argtypes = [U64]
+        L.orc_rand_f64.argtypes = [I64, I64, P]
+        L.orc_rand_i64.argtypes = [I64, I64, P]
+        for name in ("orc_reduce_add_f64", "orc_reduce_mul_f64", "orc_sumsq_f64", "orc_neumaier_sum"):
+            getattr(L, name).restype = D
+            getattr(L, name).argtypes = [P, I64]
+        L.orc_dot_f64.restype = D
+        L.orc_dot_f64.argtypes = [P, P, I64]
+        L.orc_count_cmp_f64.restype = I64
+        L.orc_count_cmp_f64.argtypes = [P, I64, ctypes.c_int, D]
+        L.orc_condsum_cmp_f64.restype = D
+        L.orc_condsum_cmp_f64.argtypes = [P, I64, ctypes.c_int, D, D]
+        L.orc_filter_cmp_f64.restype = I64
+        L.orc_filter_cmp_f64.argtypes = [P, I64, ctypes.c_int, D, P]
+        L.orc_reduce_minmax_f64.argtypes = [P, I64, ctypes.c_int, P, ctypes.c_char_p]
+        L.orc_argext_f64.argtypes = [P, I64, ctypes.c_int, P, ctypes.c_char_p]
+        L.orc_reduce_minmax_i64.argtypes = [P, I64, ctypes.c_int, P, ctypes.c_char_p]
+        L.orc_argext_i64.argtypes = [P, I64, ctypes.c_int, P, ctypes.c_char_p]
+        L.orc_reduce_add_i64.restype = I64
+        L.orc_reduce_add_i64.argtypes = [P, I64]
+        L.orc_compress.restype = I64
+        L.orc_compress.argtypes = [P, ctypes.c_int, P, I64, P]
+        L.orc_where.restype = I64
+        L.orc_where.argtypes = [P, I64, I64, P]
+        L.orc_scan_add_i64.argtypes = [P, I64, P]
+        L.orc_scan_by_add_i64.argtypes = [P, P, I64, P]
+        L.orc_prev_i64.argtypes = [P, I64, I64, P]
+        L.orc_gather.argtypes = [P, ctypes.c_int, I64, P, I64, P, ctypes.c_char_p]
+        L.orc_histogram.argtypes = [P, I64, I64, P, ctypes.c_char_p]
+        L.orc_reduce_into_add_i64.argtypes = [P, P, I64, I64, P, ctypes.c_char_p]
+        L.orc_argsort_i64.argtypes = [P, I64, P, ctypes.c_char_p]
+        L.orc_argsort_reference_i64.argtypes = [P, I64, P]
+        L.orc_group_id_i64.argtypes = [P, I64, P, ctypes.c_char_p]
+        L.orc_group_id2_i64_i64.argtypes = [P, P, I64, P, ctypes.c_char_p]
+        L.orc_mul_f64.argtypes = [P, P, I64, P]
+        L.orc_cmp_f64.argtypes = [P, P, I64, ctypes.c_int, P]
+        L.orc_select_f64.argtypes = [P, P, P, I64, P]
+        L.orc_dd_sum.argtypes = [P, I64, P, P]
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _f64(x):
+    return np.ascontiguousarray(x, dtype=np.float64)
+
+
+def _i64(x):
+    return np.ascontiguousarray(x, dtype=np.int64)
+
+
+def _u8(x):
+    return np.ascontiguousarray(np.asarray(x).astype(np.uint8))
+
+
+def _err(rc, buf):
+    if rc:
+        raise OracleError(buf.value.decode())
+
+
+def splitmix64(x):
+    return int(lib().orc_splitmix64(x & 0xFFFFFFFFFFFFFFFF))
+
+
+def rand_f64(n, seed):
+    out = np.empty(n, dtype=np.float64)
+    lib().orc_rand_f64(n, seed, _p(out))
+    return out
+
+
+def rand_i64(n, seed):
+    out = np.empty(n, dtype=np.int64)
+    lib().orc_rand_i64(n, seed, _p(out))
+    return out
+
+
+def reduce_add_f64(x):
+    x = _f64(x)
+    return lib().orc_reduce_add_f64(_p(x), len(x))
+
+
+def reduce_mul_f64(x):
+    x = _f64(x)
+    return lib().orc_reduce_mul_f64(_p(x), len(x))
+
+
+def dot_f64(x, y):
+    x, y = _f64(x), _f64(y)
+    return lib().orc_dot_f64(_p(x), _p(y), len(x))
+
+
+def sumsq_f64(x):
+    x = _f64(x)
+    return lib().orc_sumsq_f64(_p(x), len(x))
+
+
+def count_cmp_f64(x, cmp, c):
+    x = _f64(x)
+    return int(lib().orc_count_cmp_f64(_p(x), len(x), CMPS[cmp], c))
+
+
+def condsum_cmp_f64(x, cmp, c, e):
+    x = _f64(x)
+    return lib().orc_condsum_cmp_f64(_p(x), len(x), CMPS[cmp], c, e)
+
+
+def filter_cmp_f64(x, cmp, c):
+    x = _f64(x)
+    out = np.empty(len(x), dtype=np.float64)
+    k = lib().orc_filter_cmp_f64(_p(x), len(x), CMPS[cmp], c, _p(out))
+    return out[:k].copy()
+
+
+def _ext(fn, x, is_max, dtype):
+    out = np.zeros(1, dtype=dtype)
+    buf = ctypes.create_string_buffer(ERR_LEN)
+    _err(fn(_p(x), len(x), int(is_max), _p(out), buf), buf)
+    return out[0]
+
+
+def reduce_min_f64(x):
+    return float(_ext(lib().orc_reduce_minmax_f64, _f64(x), False, np.float64))
+
+
+def reduce_max_f64(x):
+    return float(_ext(lib().orc_reduce_minmax_f64, _f64(x), True, np.float64))
+
+
+def argmin_f64(x):
+    return int(_ext(lib().orc_argext_f64, _f64(x), False, np.int64))
+
+
+def argmax_f64(x):
+    return int(_ext(lib().orc_argext_f64, _f64(x), True, np.int64))
+
+
+def reduce_min_i64(x):
+    return int(_ext(lib().orc_reduce_minmax_i64, _i64(x), False, np.int64))
+
+
+def reduce_max_i64(x):
+    return int(_ext(lib().orc_reduce_minmax_i64, _i64(x), True, np.int64))
+
+
+def argmin_i64(x):
+    return int(_ext(lib().orc_argext_i64, _i64(x), False, np.int64))
+
+
+def argmax_i64(x):
+    return int(_ext(lib().orc_argext_i64, _i64(x), True, np.int64))
+
+
+def reduce_add_i64(x):
+    x = _i64(x)
+    return int(lib().orc_reduce_add_i64(_p(x), len(x)))
+
+
+def compress(x, mask):
+    x = np.ascontiguousarray(x)
+    m = _u8(mask)
+    out = np.empty_like(x)
+    k = lib().orc_compress(_p(x), x.dtype.itemsize, _p(m), len(x), _p(out))
+    return out[:k].copy()
+
+
+def where(mask, base=0):
+    m = _u8(mask)
+    out = np.empty(len(m), dtype=np.int64)
+    k = lib().orc_where(_p(m), len(m), base, _p(out))
+    return out[:k].copy()
+
+
+def scan_add_i64(x):
+    x = _i64(x)
+    out = np.empty(len(x), dtype=np.int64)
+    lib().orc_scan_add_i64(_p(x), len(x), _p(out))
+    return out
+
+
+def scan_by_add_i64(x, starts):
+    x, s = _i64(x), _u8(starts)
+    out = np.empty(len(x), dtype=np.int64)
+    lib().orc_scan_by_add_i64(_p(x), _p(s), len(x), _p(out))
+    return out
+
+
+def prev_i64(x, fill):
+    x = _i64(x)
+    out = np.empty(len(x), dtype=np.int64)
+    lib().orc_prev_i64(_p(x), len(x), fill, _p(out))
+    return out
+
+
+def gather(src, idx):
+    src = np.ascontiguousarray(src)
+    idx = _i64(idx)
+    out = np.empty(len(idx), dtype=src.dtype)
+    buf = ctypes.create_string_buffer(ERR_LEN)
+    _err(lib().orc_gather(_p(src), src.dtype.itemsize, len(src), _p(idx), len(idx), _p(out), buf), buf)
+    return out
+
+
+def _huge_buckets(keys, buckets):
+    """The errors of a bucket count too large to allocate here (index.rs:116-130, then
+    value.rs:285-307): a negative count, the first key out of range, the size cap, then the
+    allocation failure."""
+    if buckets < 0:
+        raise OracleError("negative bucket count %d" % buckets)
+    bad = np.nonzero(keys.view(np.uint64) >= np.uint64(buckets))[0]
+    if len(bad):
+        raise OracleError("bucket key %d out of range for %d buckets" % (keys[bad[0]], buckets))
+    if buckets > (1 << 63) // 8 - 1:
+        raise OracleError("array of %d elements is too large" % buckets)
+    raise OracleError("cannot allocate an array of %d elements" % buckets)
+
+
+def histogram(keys, buckets):
+    keys = _i64(keys)
+    if buckets > 1 << 28:
+        _huge_buckets(keys, buckets)
+    out = np.empty(max(0, min(buckets, 1 << 28)), dtype=np.int64)
+    buf = ctypes.create_string_buffer(ERR_LEN)
+    _err(lib().orc_histogram(_p(keys), len(keys), buckets, _p(out), buf), buf)
+    return out
+
+
+def reduce_into_add_i64(keys, vals, buckets):
+    keys, vals = _i64(keys), _i64(vals)
+    if len(keys) != len(vals):
+        # index.rs:203-210: the key check comes first, then the length mismatch.
+        buf = ctypes.create_string_buffer(ERR_LEN)
+        tmp = np.empty(max(0, min(buckets, 1 << 20)), dtype=np.int64)
+        if buckets >= 0 and buckets <= (1 << 20):
+            _err(lib().orc_histogram(_p(keys), len(keys), buckets, _p(tmp), buf), buf)
+        raise OracleError("length mismatch: %d keys for %d values" % (len(keys), len(vals)))
+    if buckets > 1 << 28:
+        _huge_buckets(keys, buckets)
+    out = np.empty(max(0, min(buckets, 1 << 28)), dtype=np.int64)
+    buf = ctypes.create_string_buffer(ERR_LEN)
+    _err(lib().orc_reduce_into_add_i64(_p(keys), _p(vals), len(keys), buckets, _p(out), buf), buf)
+    return out
+
+
+def argsort_i64(x):
+    x = _i64(x)
+    out = np.empty(len(x), dtype=np.int64)
+    buf = ctypes.create_string_buffer(ERR_LEN)
+    _err(lib().orc_argsort_i64(_p(x), len(x), _p(out), buf), buf)
+    return out
+
+
+def argsort_reference_i64(x):
+    x = _i64(x)
+    out = np.empty(len(x), dtype=np.int64)
+    lib().orc_argsort_reference_i64(_p(x), len(x), _p(out))
+    return out
+
+
+def group_id_i64(x):
+    x = _i64(x)
+    out = np.empty(len(x), dtype=np.int64)
+    buf = ctypes.create_string_buffer(ERR_LEN)
+    _err(lib().orc_group_id_i64(_p(x), len(x), _p(out), buf), buf)
+    return out
+
+
+def group_id2_i64_i64(x, y):
+    x, y = _i64(x), _i64(y)
+    if len(x) != len(y):
+        raise OracleError("length mismatch: %d vs %d" % (len(x), len(y)))
+    out = np.empty(len(x), dtype=np.int64)
+    buf = ctypes.create_string_buffer(ERR_LEN)
+    _err(lib().orc_group_id2_i64_i64(_p(x), _p(y), len(x), _p(out), buf), buf)
+    return out
+
+
+def mul_f64(x, y):
+    x, y = _f64(x), _f64(y)
+    out = np.empty(len(x), dtype=np.float64)
+    lib().orc_mul_f64(_p(x), _p(y), len(x), _p(out))
+    return out
+
+
+def cmp_f64(x, y, cmp):
+    x, y = _f64(x), _f64(y)
+    out = np.empty(len(x), dtype=np.uint8)
+    lib().orc_cmp_f64(_p(x), _p(y), len(x), CMPS[cmp], _p(out))
+    return out
+
+
+def select_f64(m, a, b):
+    m, a, b = _u8(m), _f64(a), _f64(b)
+    out = np.empty(len(m), dtype=np.float64)
+    lib().orc_select_f64(_p(m), _p(a), _p(b), len(m), _p(out))
+    return out
+
+
+def neumaier_sum(x):
+    x = _f64(x)
+    return lib().orc_neumaier_sum(_p(x), len(x))
+
+
+def dd_sum(x):
+    x = _f64(x)
+    hi, lo = ctypes.c_double(), ctypes.c_double()
+    lib().orc_dd_sum(_p(x), len(x), ctypes.byref(hi), ctypes.byref(lo))
+    return hi.value, lo.value

@@ -1,0 +1,252 @@
+// Index kernels: gather_T, histogram, reduce_into_add_i64 (src/kernels/scalar/index.rs:31-155,
+// :194-222).
+//
+// The reference checks every index before it writes a row and reports the first offending
+// value in index order (first_out_of_range, index.rs:102-111). Here the check is fused into
+// the kernel: each offending row does an atomicMin of its row number into the status word,
+// and the host reports the value at that row and discards the output.
+#include "reduce_common.h"
+
+namespace vkc {
+
+// ------------------------------------------------------------------ gather
+
+template <int W> struct GWord;
+template <> struct GWord<8> { using T = unsigned long long; };
+template <> struct GWord<4> { using T = unsigned; };
+template <> struct GWord<1> { using T = unsigned char; };
+
+template <int W>
+__global__ void __launch_bounds__(256) gather_kernel(const typename GWord<W>::T *__restrict__ src, uint64_t nsrc,
+                                                     const long long *__restrict__ idx, int64_t n,
+                                                     typename GWord<W>::T *__restrict__ out, DevStatus *status) {
+    int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    unsigned long long bad = ~0ull;
+    int64_t head = (reinterpret_cast<uintptr_t>(idx) & 15) ? 1 : 0;
+    if (head > n) head = n;
+    int64_t tid = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    auto one = [&](int64_t i, long long k) {
+        if (static_cast<uint64_t>(k) < nsrc) out[i] = __ldg(src + k);
+        else if (static_cast<unsigned long long>(i) < bad) bad = static_cast<unsigned long long>(i);
+    };
+    if (head && tid == 0) one(0, idx[0]);
+    const longlong2 *i2 = reinterpret_cast<const longlong2 *>(idx + head);
+    int64_t n2 = (n - head) >> 1;
+    for (int64_t p = tid; p < n2; p += stride) {
+        longlong2 k = __ldcs(i2 + p);
+        one(head + 2 * p, k.x);
+        one(head + 2 * p + 1, k.y);
+    }
+    if (((n - head) & 1) && tid == 0) one(n - 1, idx[n - 1]);
+    if (bad != ~0ull) atomicMin(&status->first_bad, bad);
+}
+
+// Reads the value at `row` of an i64 device array.
+static vkc_status read_i64(vkc_ctx *ctx, const void *base, uint64_t row, int64_t *out) {
+    void *h;
+    vkc_status st = pinned(ctx, 8, &h);
+    if (st) return st;
+    VKC_CUDA(ctx, cudaMemcpyAsync(h, static_cast<const long long *>(base) + row, 8, cudaMemcpyDeviceToHost,
+                                  ctx->stream));
+    VKC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    *out = *static_cast<long long *>(h);
+    return VKC_OK;
+}
+
+// index.rs:40-73 (Gather::checked, run).
+template <vkc_type T> static vkc_status gather(vkc_ctx *ctx, const vkc_value *args, int nargs, vkc_value *out) {
+    vkc_status st;
+    if (nargs != 2) return fail(ctx, VKC_RUNTIME, arity_error(2, nargs));
+    if (!array_arg(ctx, args[0], T, &st) || !array_arg(ctx, args[1], VKC_I64, &st)) return st;
+    const vkc_array *xs = args[0].array, *ix = args[1].array;
+    int64_t n = ix->len;
+    vkc_array *o;
+    if ((st = new_array(ctx, T, n, false, &o))) return st;
+    if (n > 0) {
+        int grid = stream_grid(ctx, (n + 1) / 2, 256, 8, 512);
+        const auto *idx = static_cast<const long long *>(ix->data());
+        switch (type_width(T)) {
+        case 8: gather_kernel<8><<<grid, 256, 0, ctx->stream>>>(static_cast<const unsigned long long *>(xs->data()), xs->len, idx, n, static_cast<unsigned long long *>(o->data()), ctx->status); break;
+        case 4: gather_kernel<4><<<grid, 256, 0, ctx->stream>>>(static_cast<const unsigned *>(xs->data()), xs->len, idx, n, static_cast<unsigned *>(o->data()), ctx->status); break;
+        default: gather_kernel<1><<<grid, 256, 0, ctx->stream>>>(static_cast<const unsigned char *>(xs->data()), xs->len, idx, n, static_cast<unsigned char *>(o->data()), ctx->status); break;
+        }
+        if ((st = launched(ctx, "gather"))) {
+            vkc_array_release(o);
+            return st;
+        }
+        DevStatus ds;
+        if ((st = read_status(ctx, &ds))) {
+            vkc_array_release(o);
+            return st;
+        }
+        if (ds.first_bad != ~0ull) {
+            vkc_array_release(o);
+            int64_t v;
+            if ((st = read_i64(ctx, ix->data(), ds.first_bad, &v))) return st;
+            return fail(ctx, VKC_RUNTIME, "gather index " + std::to_string(v) + " out of range for length " +
+                                              std::to_string(static_cast<uint64_t>(xs->len)));
+        }
+    }
+    out->kind = VKC_VALUE_ARRAY;
+    out->array = o;
+    return VKC_OK;
+}
+
+// ------------------------------------------------------------------ histogram, reduce_into
+
+// Bounds only: the first key outside [0, nb).
+__global__ void __launch_bounds__(256) keys_check_kernel(const long long *__restrict__ keys, int64_t n,
+                                                         uint64_t nb, DevStatus *status) {
+    int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    unsigned long long bad = ~0ull;
+    for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride)
+        if (static_cast<uint64_t>(__ldcs(keys + i)) >= nb && static_cast<unsigned long long>(i) < bad)
+            bad = static_cast<unsigned long long>(i);
+    if (bad != ~0ull) atomicMin(&status->first_bad, bad);
+}
+
+// Per-bucket wrapping sums (vals) or counts (vals == nullptr). Buckets up to SMEM_BINS are
+// accumulated in shared memory per block first.
+constexpr int SMEM_BINS = 4096;
+
+template <bool SMEM, bool COUNT>
+__global__ void __launch_bounds__(256) bucket_kernel(const long long *__restrict__ keys,
+                                                     const unsigned long long *__restrict__ vals, int64_t n,
+                                                     uint64_t nb, unsigned long long *__restrict__ out,
+                                                     DevStatus *status) {
+    __shared__ unsigned long long bins[SMEM ? SMEM_BINS : 1];
+    if (SMEM) {
+        for (int b = threadIdx.x; b < static_cast<int>(nb); b += blockDim.x) bins[b] = 0;
+        __syncthreads();
+    }
+    int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    unsigned long long bad = ~0ull;
+    for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride) {
+        long long k = __ldcs(keys + i);
+        if (static_cast<uint64_t>(k) >= nb) {
+            if (static_cast<unsigned long long>(i) < bad) bad = static_cast<unsigned long long>(i);
+            continue;
+        }
+        unsigned long long v = COUNT ? 1ull : __ldcs(vals + i);
+        if (SMEM) atomicAdd(&bins[k], v);
+        else atomicAdd(out + k, v);
+    }
+    if (bad != ~0ull) atomicMin(&status->first_bad, bad);
+    if (SMEM) {
+        __syncthreads();
+        for (int b = threadIdx.x; b < static_cast<int>(nb); b += blockDim.x)
+            if (bins[b]) atomicAdd(out + b, bins[b]);
+    }
+}
+
+// index.rs:116-130 (checked_keys) then the result allocation (value.rs:285-307). The key check
+// precedes allocation errors; a length mismatch of reduce_into follows it (index.rs:203-210).
+static vkc_status run_buckets(vkc_ctx *ctx, const vkc_array *keys, const vkc_array *vals, int64_t nb,
+                              vkc_value *out) {
+    vkc_status st;
+    if (nb < 0) return fail(ctx, VKC_RUNTIME, "negative bucket count " + std::to_string(nb));
+    int64_t n = keys->len;
+    const auto *k = static_cast<const long long *>(keys->data());
+    auto key_error = [&](bool *found) -> vkc_status {
+        *found = false;
+        if (n == 0) return VKC_OK;
+        int grid = stream_grid(ctx, n, 256, 8, 4096);
+        keys_check_kernel<<<grid, 256, 0, ctx->stream>>>(k, n, static_cast<uint64_t>(nb), ctx->status);
+        vkc_status s2 = launched(ctx, "keys_check");
+        if (s2) return s2;
+        DevStatus ds;
+        if ((s2 = read_status(ctx, &ds))) return s2;
+        if (ds.first_bad == ~0ull) return VKC_OK;
+        int64_t v;
+        if ((s2 = read_i64(ctx, k, ds.first_bad, &v))) return s2;
+        *found = true;
+        return fail(ctx, VKC_RUNTIME, "bucket key " + std::to_string(v) + " out of range for " +
+                                          std::to_string(nb) + " buckets");
+    };
+    bool found;
+    if (vals && vals->len != n) {
+        if ((st = key_error(&found))) return st;
+        return fail(ctx, VKC_RUNTIME, "length mismatch: " + std::to_string(n) + " keys for " +
+                                          std::to_string(vals->len) + " values");
+    }
+    vkc_array *o;
+    st = new_array(ctx, VKC_I64, nb, true, &o);
+    if (st) {
+        std::string msg = ctx->err;
+        vkc_status kst = key_error(&found);
+        if (kst) return kst;
+        return fail(ctx, st, msg);
+    }
+    if (n > 0) {
+        int grid = stream_grid(ctx, n, 256, 8, 8192);
+        auto *ov = static_cast<unsigned long long *>(o->data());
+        const auto *vv = vals ? static_cast<const unsigned long long *>(vals->data()) : nullptr;
+        bool smem = nb <= SMEM_BINS;
+        if (smem && !vals) bucket_kernel<true, true><<<grid, 256, 0, ctx->stream>>>(k, vv, n, nb, ov, ctx->status);
+        else if (smem) bucket_kernel<true, false><<<grid, 256, 0, ctx->stream>>>(k, vv, n, nb, ov, ctx->status);
+        else if (!vals) bucket_kernel<false, true><<<grid, 256, 0, ctx->stream>>>(k, vv, n, nb, ov, ctx->status);
+        else bucket_kernel<false, false><<<grid, 256, 0, ctx->stream>>>(k, vv, n, nb, ov, ctx->status);
+        if ((st = launched(ctx, "buckets"))) {
+            vkc_array_release(o);
+            return st;
+        }
+        DevStatus ds;
+        if ((st = read_status(ctx, &ds))) {
+            vkc_array_release(o);
+            return st;
+        }
+        if (ds.first_bad != ~0ull) {
+            vkc_array_release(o);
+            int64_t v;
+            if ((st = read_i64(ctx, k, ds.first_bad, &v))) return st;
+            return fail(ctx, VKC_RUNTIME, "bucket key " + std::to_string(v) + " out of range for " +
+                                              std::to_string(nb) + " buckets");
+        }
+    }
+    out->kind = VKC_VALUE_ARRAY;
+    out->array = o;
+    return VKC_OK;
+}
+
+// index.rs:138-155 (Histogram).
+static vkc_status histogram(vkc_ctx *ctx, const vkc_value *args, int nargs, vkc_value *out) {
+    vkc_status st;
+    if (nargs != 2) return fail(ctx, VKC_RUNTIME, arity_error(2, nargs));
+    int64_t nb;
+    if (!array_arg(ctx, args[0], VKC_I64, &st) || !i64_arg(ctx, args[1], &nb, &st)) return st;
+    return run_buckets(ctx, args[0].array, nullptr, nb, out);
+}
+
+// index.rs:194-222 (ReduceInto with ScanSum<i64>): values kinds first, then checked_keys.
+static vkc_status reduce_into_add(vkc_ctx *ctx, const vkc_value *args, int nargs, vkc_value *out) {
+    vkc_status st;
+    if (nargs != 3) return fail(ctx, VKC_RUNTIME, arity_error(3, nargs));
+    if (!array_arg(ctx, args[1], VKC_I64, &st)) return st;
+    int64_t nb;
+    if (!array_arg(ctx, args[0], VKC_I64, &st) || !i64_arg(ctx, args[2], &nb, &st)) return st;
+    return run_buckets(ctx, args[0].array, args[1].array, nb, out);
+}
+
+void register_index(std::vector<KernelDef> &t) {
+    struct G { vkc_type t; WholeFn f; };
+    const G gs[] = {{VKC_F64, gather<VKC_F64>}, {VKC_F32, gather<VKC_F32>}, {VKC_I64, gather<VKC_I64>},
+                    {VKC_U64, gather<VKC_U64>}, {VKC_I32, gather<VKC_I32>}, {VKC_U8, gather<VKC_U8>},
+                    {VKC_BOOL, gather<VKC_BOOL>}};
+    for (const G &g : gs) {
+        // index.rs:255-270: cost 8 + 2 widths.
+        KernelDef d{std::string("gather_") + type_name(g.t), VKC_WHOLE,
+                    {InSpec{IN_ARRAY, g.t}, InSpec{IN_ARRAY, VKC_I64}}, true, g.t,
+                    static_cast<uint64_t>(8 + 2 * type_width(g.t))};
+        d.whole = g.f;
+        t.push_back(d);
+    }
+    InSpec ia{IN_ARRAY, VKC_I64}, is{IN_SCALAR, VKC_I64};
+    KernelDef d{"histogram", VKC_WHOLE, {ia, is}, true, VKC_I64, 24};
+    d.whole = histogram;
+    t.push_back(d);
+    d = KernelDef{"reduce_into_add_i64", VKC_WHOLE, {ia, ia, is}, true, VKC_I64, 32};
+    d.whole = reduce_into_add;
+    t.push_back(d);
+}
+
+}  // namespace vkc

@@ -1,0 +1,419 @@
+// Reductions: count_<cmp>_f64, count, reduce_min/max and argmin/argmax on f64 and i64, and
+// reduce_add_i64 (src/kernels/scalar/reduce.rs:331-468, src/kernels/scalar/fused.rs:145-179).
+// The canonical float sums live in k_canon.cu.
+//
+// Each reducer keeps its running state in a small device buffer. An update is one kernel: every
+// block folds its rows, and the last block to finish (last-block-done) folds the block
+// partials into the state, so the only host sync is the download at finish.
+#include <cmath>
+#include <cstring>
+
+#include "kcommon.cuh"
+#include "reduce_common.h"
+
+namespace vkc {
+
+// ------------------------------------------------------------------ comparison ranges
+
+CmpRange cmp_range(int cmp, double c) {
+    CmpRange r{1, 0, 0};  // empty
+    if (std::isnan(c)) {
+        r.negate = cmp == 1;  // ne is true on everything, the others on nothing
+        return r;
+    }
+    unsigned long long pz = 0, nz = 0x8000000000000000ull, cb;
+    memcpy(&cb, &c, 8);
+    const bool zero = c == 0.0;
+    auto key = [](unsigned long long b) { return key_of_bits(b); };
+    switch (cmp) {
+    case 0:  // eq
+    case 1:  // ne
+        r.lo = zero ? key(nz) : key(cb);
+        r.hi = zero ? key(pz) : key(cb);
+        r.negate = cmp == 1;
+        break;
+    case 2:  // lt: keys below c, with -0 standing for both zeros
+        r.lo = KEY_NEG_INF;
+        r.hi = (zero ? key(nz) : key(cb)) - 1;
+        break;
+    case 3:  // le
+        r.lo = KEY_NEG_INF;
+        r.hi = zero ? key(pz) : key(cb);
+        break;
+    case 4:  // gt: keys above c, with +0 standing for both zeros
+        r.lo = (zero ? key(pz) : key(cb)) + 1;
+        r.hi = KEY_POS_INF;
+        break;
+    default:  // ge
+        r.lo = zero ? key(nz) : key(cb);
+        r.hi = KEY_POS_INF;
+        break;
+    }
+    return r;
+}
+
+// ------------------------------------------------------------------ count
+
+// Counts rows with x <cmp> c (as a key range) or, for `count` over bool, nonzero bytes.
+template <bool BOOL>
+__global__ void __launch_bounds__(256) count_kernel(const void *__restrict__ xv, int64_t n,
+                                                    CmpRange r, unsigned long long *partials,
+                                                    unsigned *done, unsigned long long *state) {
+    unsigned long long c = 0;
+    int64_t tid = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    if (BOOL) {
+        const uint8_t *x = static_cast<const uint8_t *>(xv);
+        int64_t head = (16 - (reinterpret_cast<uintptr_t>(x) & 15)) & 15;
+        if (head > n) head = n;
+        for (int64_t i = tid; i < head; i += stride) c += x[i] != 0;
+        const uint4 *x16 = reinterpret_cast<const uint4 *>(x + head);
+        int64_t n16 = (n - head) >> 4;
+        for (int64_t i = tid; i < n16; i += stride) {
+            uint4 v = __ldcs(&x16[i]);
+            unsigned w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                // A byte is nonzero when any of its bits is set.
+                unsigned t = w[j] | (w[j] >> 4);
+                t |= t >> 2;
+                t |= t >> 1;
+                c += __popc(t & 0x01010101u);
+            }
+        }
+        for (int64_t i = head + (n16 << 4) + tid; i < n; i += stride) c += x[i] != 0;
+    } else {
+        const unsigned long long *x = static_cast<const unsigned long long *>(xv);
+        int64_t head = (reinterpret_cast<uintptr_t>(x) & 15) ? 1 : 0;
+        if (head > n) head = n;
+        if (head && tid == 0) c += in_range(r, x[0]);
+        const ulonglong2 *x2 = reinterpret_cast<const ulonglong2 *>(x + head);
+        int64_t n2 = (n - head) >> 1;
+        for (int64_t i = tid; i < n2; i += stride) {
+            ulonglong2 v = __ldcs(&x2[i]);
+            c += in_range(r, v.x);
+            c += in_range(r, v.y);
+        }
+        if (((n - head) & 1) && tid == 0) c += in_range(r, x[n - 1]);
+    }
+    c = warp_sum(c);
+    __shared__ unsigned long long ws[8];
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = c;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long s = 0;
+        for (int w = 0; w < 8; ++w) s += ws[w];
+        partials[blockIdx.x] = s;
+    }
+    if (last_block(done) && threadIdx.x < 32) {
+        unsigned long long s = 0;
+        for (unsigned b = threadIdx.x; b < gridDim.x; b += 32) s += partials[b];
+        s = warp_sum(s);
+        if (threadIdx.x == 0) *state += s;
+    }
+}
+
+struct CountReducer : DevReducer {
+    int cmp;  // -1 for `count` over bool
+    vkc_status update(vkc_ctx *ctx, const Arg *args, int nargs) override {
+        vkc_status st;
+        if (cmp < 0) {
+            if (nargs != 1) return fail(ctx, VKC_RUNTIME, arity_error(1, nargs));
+            if (!rows_arg(ctx, args[0], VKC_BOOL, &st)) return st;
+        } else {
+            if (nargs != 2) return fail(ctx, VKC_RUNTIME, arity_error(2, nargs));
+            if (!rows_arg(ctx, args[0], VKC_F64, &st) || !splat_arg(ctx, args[1], VKC_F64, &st))
+                return st;
+        }
+        int64_t n = args[0].len();
+        if (n == 0) return VKC_OK;
+        int grid = stream_grid(ctx, n, 256, 8, cmp < 0 ? 16384 : 4096);
+        void *part;
+        if ((st = scratch(ctx, sizeof(unsigned long long) * grid, &part))) return st;
+        auto *s = static_cast<unsigned long long *>(state);
+        if (cmp < 0)
+            count_kernel<true><<<grid, 256, 0, ctx->stream>>>(args[0].a->data(), n, CmpRange{},
+                static_cast<unsigned long long *>(part), ctx->counters + 1, s);
+        else
+            count_kernel<false><<<grid, 256, 0, ctx->stream>>>(args[0].a->data(), n,
+                cmp_range(cmp, args[1].f64()), static_cast<unsigned long long *>(part),
+                ctx->counters + 1, s);
+        return launched(ctx, "count");
+    }
+    vkc_status finish(vkc_ctx *ctx, vkc_scalar *out) override {
+        unsigned long long v;
+        vkc_status st = download(ctx, &v, sizeof v);
+        if (st) return st;
+        *out = scalar_i64(static_cast<int64_t>(v));
+        return VKC_OK;
+    }
+};
+
+// ------------------------------------------------------------------ extremes
+
+// State of reduce_min / reduce_max / argmin / argmax: the best key and its row, the first NaN
+// row, and whether any row was seen.
+struct ExtState {
+    long long key;
+    unsigned long long idx;
+    unsigned long long nan_idx;  // ~0 when no NaN
+    unsigned long long seen;
+};
+
+// Combines two candidates: for MAX the larger key, else the smaller, ties to the earlier row.
+template <bool MAX>
+__device__ __forceinline__ void better(long long &k, unsigned long long &i, long long k2,
+                                       unsigned long long i2) {
+    bool b = MAX ? (k2 > k || (k2 == k && i2 < i)) : (k2 < k || (k2 == k && i2 < i));
+    if (b) {
+        k = k2;
+        i = i2;
+    }
+}
+
+// One pass over x[0, n) at global row offset `base`. F64 rows are keyed; NaN rows only
+// record their first position, which decides argmin/argmax and makes min/max NaN.
+template <bool MAX, bool F64>
+__global__ void __launch_bounds__(256) extreme_kernel(const long long *__restrict__ x, int64_t n,
+                                                      unsigned long long base, ExtState *partials,
+                                                      unsigned *done, ExtState *state) {
+    long long bk = MAX ? LLONG_MIN : LLONG_MAX;
+    unsigned long long bi = ~0ull, nan = ~0ull;
+    int64_t tid = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    auto visit = [&](long long v, int64_t i) {
+        if (F64) {
+            unsigned long long b = static_cast<unsigned long long>(v);
+            if ((b & 0x7fffffffffffffffull) > 0x7ff0000000000000ull) {
+                if (static_cast<unsigned long long>(i) < nan) nan = static_cast<unsigned long long>(i);
+                return;
+            }
+            v = f64_key(b);
+        }
+        better<MAX>(bk, bi, v, static_cast<unsigned long long>(i));
+    };
+    int64_t head = (reinterpret_cast<uintptr_t>(x) & 15) ? 1 : 0;
+    if (head > n) head = n;
+    if (head && tid == 0) visit(x[0], 0);
+    const longlong2 *x2 = reinterpret_cast<const longlong2 *>(x + head);
+    int64_t n2 = (n - head) >> 1;
+    for (int64_t i = tid; i < n2; i += stride) {
+        longlong2 v = __ldcs(&x2[i]);
+        visit(v.x, head + 2 * i);
+        visit(v.y, head + 2 * i + 1);
+    }
+    if (((n - head) & 1) && tid == 0) visit(x[n - 1], n - 1);
+    // Warp, then block.
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        long long k2 = __shfl_xor_sync(FULL, bk, o);
+        unsigned long long i2 = __shfl_xor_sync(FULL, bi, o);
+        unsigned long long n2v = __shfl_xor_sync(FULL, nan, o);
+        better<MAX>(bk, bi, k2, i2);
+        nan = n2v < nan ? n2v : nan;
+    }
+    __shared__ ExtState ws[8];
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = ExtState{bk, bi, nan, 0};
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < 8; ++w) {
+            better<MAX>(bk, bi, ws[w].key, ws[w].idx);
+            if (ws[w].nan_idx < nan) nan = ws[w].nan_idx;
+        }
+        partials[blockIdx.x] = ExtState{bk, bi, nan, 0};
+    }
+    if (last_block(done) && threadIdx.x == 0) {
+        ExtState s = *state;
+        long long k = s.seen ? s.key : (MAX ? LLONG_MIN : LLONG_MAX);
+        unsigned long long i = s.seen ? s.idx : ~0ull, nn = s.nan_idx;
+        for (unsigned b = 0; b < gridDim.x; ++b) {
+            ExtState p = partials[b];
+            if (p.idx != ~0ull) better<MAX>(k, i, p.key, p.idx + base);
+            if (p.nan_idx != ~0ull && p.nan_idx + base < nn) nn = p.nan_idx + base;
+        }
+        *state = ExtState{k, i, nn, 1};
+    }
+}
+
+struct ExtremeReducer : DevReducer {
+    bool max, arg;
+    vkc_type type;
+    unsigned long long consumed = 0;
+    vkc_status init(vkc_ctx *ctx) {
+        ExtState s{0, ~0ull, ~0ull, 0};
+        return upload(ctx, &s, sizeof s);
+    }
+    vkc_status update(vkc_ctx *ctx, const Arg *args, int nargs) override {
+        vkc_status st;
+        if (nargs != 1) return fail(ctx, VKC_RUNTIME, arity_error(1, nargs));
+        if (!rows_arg(ctx, args[0], type, &st)) return st;
+        int64_t n = args[0].len();
+        if (n == 0) return VKC_OK;
+        int grid = stream_grid(ctx, n, 256, 8, 4096);
+        void *part;
+        if ((st = scratch(ctx, sizeof(ExtState) * grid, &part))) return st;
+        auto *p = static_cast<ExtState *>(part);
+        auto *s = static_cast<ExtState *>(state);
+        const long long *x = static_cast<const long long *>(args[0].a->data());
+        bool f = type == VKC_F64;
+        if (max && f) extreme_kernel<true, true><<<grid, 256, 0, ctx->stream>>>(x, n, consumed, p, ctx->counters + 1, s);
+        else if (max) extreme_kernel<true, false><<<grid, 256, 0, ctx->stream>>>(x, n, consumed, p, ctx->counters + 1, s);
+        else if (f) extreme_kernel<false, true><<<grid, 256, 0, ctx->stream>>>(x, n, consumed, p, ctx->counters + 1, s);
+        else extreme_kernel<false, false><<<grid, 256, 0, ctx->stream>>>(x, n, consumed, p, ctx->counters + 1, s);
+        consumed += static_cast<unsigned long long>(n);
+        return launched(ctx, "extreme");
+    }
+    // reduce.rs:401-411 and :454-467: empty input is an error; a NaN decides the result.
+    vkc_status finish(vkc_ctx *ctx, vkc_scalar *out) override {
+        ExtState s;
+        vkc_status st = download(ctx, &s, sizeof s);
+        if (st) return st;
+        if (!s.seen) {
+            std::string what = arg ? (max ? "argmax" : "argmin") : (max ? "reduce_max" : "reduce_min");
+            return fail(ctx, VKC_RUNTIME, what + " of an empty array");
+        }
+        if (arg) {
+            unsigned long long i = s.nan_idx != ~0ull ? s.nan_idx : s.idx;
+            *out = scalar_i64(static_cast<int64_t>(i));
+        } else if (type == VKC_F64) {
+            if (s.nan_idx != ~0ull) *out = scalar_f64(NAN);
+            else {
+                out->type = VKC_F64;
+                out->bits = bits_of_key(s.key);
+            }
+        } else {
+            *out = scalar_i64(s.key);
+        }
+        return VKC_OK;
+    }
+};
+
+// ------------------------------------------------------------------ integer sum
+
+__global__ void __launch_bounds__(256) isum_kernel(const unsigned long long *__restrict__ x, int64_t n,
+                                                   unsigned long long *partials, unsigned *done,
+                                                   unsigned long long *state) {
+    unsigned long long c = 0;
+    int64_t tid = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    int64_t head = (reinterpret_cast<uintptr_t>(x) & 15) ? 1 : 0;
+    if (head > n) head = n;
+    if (head && tid == 0) c += x[0];
+    const ulonglong2 *x2 = reinterpret_cast<const ulonglong2 *>(x + head);
+    int64_t n2 = (n - head) >> 1;
+    for (int64_t i = tid; i < n2; i += stride) {
+        ulonglong2 v = __ldcs(&x2[i]);
+        c += v.x + v.y;
+    }
+    if (((n - head) & 1) && tid == 0) c += x[n - 1];
+    c = warp_sum(c);
+    __shared__ unsigned long long ws[8];
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = c;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long s = 0;
+        for (int w = 0; w < 8; ++w) s += ws[w];
+        partials[blockIdx.x] = s;
+    }
+    if (last_block(done) && threadIdx.x < 32) {
+        unsigned long long s = 0;
+        for (unsigned b = threadIdx.x; b < gridDim.x; b += 32) s += partials[b];
+        s = warp_sum(s);
+        if (threadIdx.x == 0) *state += s;
+    }
+}
+
+// reduce.rs:331-377 (IntSum<i64>): wrapping, so any grouping gives the same bits.
+struct IntSumReducer : DevReducer {
+    vkc_status update(vkc_ctx *ctx, const Arg *args, int nargs) override {
+        vkc_status st;
+        if (nargs != 1) return fail(ctx, VKC_RUNTIME, arity_error(1, nargs));
+        if (!rows_arg(ctx, args[0], VKC_I64, &st)) return st;
+        int64_t n = args[0].len();
+        if (n == 0) return VKC_OK;
+        int grid = stream_grid(ctx, n, 256, 8, 4096);
+        void *part;
+        if ((st = scratch(ctx, sizeof(unsigned long long) * grid, &part))) return st;
+        isum_kernel<<<grid, 256, 0, ctx->stream>>>(
+            static_cast<const unsigned long long *>(args[0].a->data()), n,
+            static_cast<unsigned long long *>(part), ctx->counters + 1,
+            static_cast<unsigned long long *>(state));
+        return launched(ctx, "isum");
+    }
+    vkc_status finish(vkc_ctx *ctx, vkc_scalar *out) override {
+        unsigned long long v;
+        vkc_status st = download(ctx, &v, sizeof v);
+        if (st) return st;
+        *out = scalar_i64(static_cast<int64_t>(v));
+        return VKC_OK;
+    }
+};
+
+// ------------------------------------------------------------------ registration
+
+template <class R> static R *alloc_reducer(vkc_ctx *ctx, size_t bytes) {
+    R *r = new R;
+    if (r->alloc(ctx, bytes)) {
+        delete r;
+        return nullptr;
+    }
+    return r;
+}
+
+static const char *CMP_NAMES[6] = {"eq", "ne", "lt", "le", "gt", "ge"};
+
+template <int C> static ReducerImpl *make_count(vkc_ctx *ctx) {
+    auto *r = alloc_reducer<CountReducer>(ctx, 8);
+    if (r) r->cmp = C;
+    return r;
+}
+
+template <bool MAX, bool ARG, vkc_type T> static ReducerImpl *make_ext(vkc_ctx *ctx) {
+    auto *r = alloc_reducer<ExtremeReducer>(ctx, sizeof(ExtState));
+    if (!r) return nullptr;
+    r->max = MAX;
+    r->arg = ARG;
+    r->type = T;
+    if (r->init(ctx)) {
+        delete r;
+        return nullptr;
+    }
+    return r;
+}
+
+static ReducerImpl *make_isum(vkc_ctx *ctx) { return alloc_reducer<IntSumReducer>(ctx, 8); }
+
+void register_reduce(std::vector<KernelDef> &t) {
+    InSpec xa{IN_ARRAY, VKC_F64}, xs{IN_SCALAR, VKC_F64};
+    ReducerMake counts[6] = {make_count<0>, make_count<1>, make_count<2>,
+                             make_count<3>, make_count<4>, make_count<5>};
+    for (int c = 0; c < 6; ++c) {
+        // fused.rs:293-306: count_<cmp>_f64, cost 1 width.
+        KernelDef d{std::string("count_") + CMP_NAMES[c] + "_f64", VKC_REDUCTION, {xa, xs}, false, VKC_I64, 8};
+        d.red = counts[c];
+        t.push_back(d);
+    }
+    KernelDef d{"count", VKC_REDUCTION, {InSpec{IN_ARRAY, VKC_BOOL}}, false, VKC_I64, 1};
+    d.red = make_count<-1>;
+    t.push_back(d);
+    struct E { const char *name; ReducerMake make; vkc_type in, out; };
+    const E ext[] = {
+        {"reduce_min_f64", make_ext<false, false, VKC_F64>, VKC_F64, VKC_F64},
+        {"reduce_max_f64", make_ext<true, false, VKC_F64>, VKC_F64, VKC_F64},
+        {"argmin_f64", make_ext<false, true, VKC_F64>, VKC_F64, VKC_I64},
+        {"argmax_f64", make_ext<true, true, VKC_F64>, VKC_F64, VKC_I64},
+        {"reduce_min_i64", make_ext<false, false, VKC_I64>, VKC_I64, VKC_I64},
+        {"reduce_max_i64", make_ext<true, false, VKC_I64>, VKC_I64, VKC_I64},
+        {"argmin_i64", make_ext<false, true, VKC_I64>, VKC_I64, VKC_I64},
+        {"argmax_i64", make_ext<true, true, VKC_I64>, VKC_I64, VKC_I64},
+        {"reduce_add_i64", make_isum, VKC_I64, VKC_I64},
+    };
+    for (const E &e : ext) {
+        KernelDef k{e.name, VKC_REDUCTION, {InSpec{IN_ARRAY, e.in}}, false, e.out, 8};
+        k.red = e.make;
+        t.push_back(k);
+    }
+    register_canon(t);
+}
+
+}  // namespace vkc

@@ -1,0 +1,257 @@
+// Scans: scan_add_i64 and scan_by_add_i64 (src/kernels/scalar/scan.rs:284-326), plus prev_i64
+// (scan.rs:16-48).
+//
+// One pass with decoupled lookback over 4096-row tiles. scan_by uses the segmented operator
+// on (starts-a-segment, sum): (f1, v1) then (f2, v2) = (f1 | f2, f2 ? v2 : v1 + v2). Row 0 of
+// the array always starts a segment; a later update continues the segment of the previous
+// one unless its first start byte says otherwise, as Scan::update does.
+#include "lookback.cuh"
+#include "reduce_common.h"
+
+namespace vkc {
+
+constexpr int SC_THREADS = 256;
+constexpr int SC_ITEMS = 16;
+constexpr int SC_TILE = SC_THREADS * SC_ITEMS;
+
+// A segmented partial: `start` when a segment starts inside it, `sum` since the last start.
+struct Seg {
+    unsigned long long sum;
+    unsigned long long start;
+};
+
+__device__ __forceinline__ Seg seg_op(Seg a, Seg b) {
+    return Seg{b.start ? b.sum : a.sum + b.sum, a.start | b.start};
+}
+
+// The carried state of a scanner: the last output and whether any row was seen.
+struct ScanState {
+    unsigned long long last;
+    unsigned long long seen;
+};
+
+template <bool BY, bool ALIGNED>
+__global__ void __launch_bounds__(SC_THREADS) scan_kernel(const unsigned long long *__restrict__ x,
+                                                          const unsigned char *__restrict__ starts,
+                                                          unsigned long long *__restrict__ out, int64_t n,
+                                                          int tiles, LookbackTiles<Seg> lb, unsigned epoch,
+                                                          ScanState *state, unsigned *counters,
+                                                          DevStatus *status) {
+    // The carried state is read once, before this block publishes anything; the block that
+    // finishes last rewrites it, after every block has read it.
+    const bool seen = state->seen != 0;
+    const unsigned long long carried = state->last;
+    const int tile = take_ticket(counters);
+    const int64_t row0 = static_cast<int64_t>(tile) * SC_TILE + threadIdx.x * SC_ITEMS;
+    unsigned long long v[SC_ITEMS];
+    unsigned fl = 0;  // bit j: row row0 + j starts a segment
+    if (ALIGNED && row0 + SC_ITEMS <= n) {
+        const ulonglong2 *q = reinterpret_cast<const ulonglong2 *>(x + row0);
+#pragma unroll
+        for (int j = 0; j < SC_ITEMS / 2; ++j) {
+            ulonglong2 u = __ldcs(q + j);
+            v[2 * j] = u.x;
+            v[2 * j + 1] = u.y;
+        }
+        if (BY) {
+            uint4 m = __ldcs(reinterpret_cast<const uint4 *>(starts + row0));
+            unsigned w[4] = {m.x, m.y, m.z, m.w};
+#pragma unroll
+            for (int j = 0; j < SC_ITEMS; ++j)
+                if ((w[j >> 2] >> (8 * (j & 3))) & 0xffu) fl |= 1u << j;
+        }
+    } else {
+#pragma unroll
+        for (int j = 0; j < SC_ITEMS; ++j) {
+            bool in = row0 + j < n;
+            v[j] = in ? x[row0 + j] : 0ull;
+            if (BY && in && starts[row0 + j]) fl |= 1u << j;
+        }
+    }
+    // Row 0 of the array starts a segment whatever its byte (scan.rs:300-308).
+    if (row0 == 0 && !seen) fl |= 1u;
+    // Thread-local inclusive scan.
+    Seg agg{0, 0};
+#pragma unroll
+    for (int j = 0; j < SC_ITEMS; ++j) {
+        bool s = BY ? ((fl >> j) & 1u) : (j == 0 && row0 == 0 && !seen);
+        agg = seg_op(agg, Seg{v[j], s});
+        v[j] = agg.sum;
+    }
+    // Block-wide exclusive scan of the thread partials (segmented), by warps then across warps.
+    __shared__ Seg s_warp[SC_THREADS / 32];
+    __shared__ Seg s_prefix;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    Seg inc = agg;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        Seg y{__shfl_up_sync(FULL, inc.sum, o), __shfl_up_sync(FULL, inc.start, o)};
+        if (lane >= o) inc = seg_op(y, inc);
+    }
+    if (lane == 31) s_warp[w] = inc;
+    Seg excl{__shfl_up_sync(FULL, inc.sum, 1), __shfl_up_sync(FULL, inc.start, 1)};
+    bool has_excl = lane > 0;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        Seg wp{0, 0}, tile_agg{0, 0};
+        for (int i = 0; i < SC_THREADS / 32; ++i) {
+            Seg t = s_warp[i];
+            s_warp[i] = wp;  // exclusive over warps
+            wp = i ? seg_op(wp, t) : t;
+        }
+        tile_agg = wp;
+        Seg init{carried, 0};
+        s_prefix = lookback_exclusive<Seg>(lb, tile, tile_agg, init, epoch, seg_op, status);
+    }
+    __syncthreads();
+    // prefix before this thread = tile prefix, then warps before, then lanes before.
+    Seg pre = s_prefix;
+    if (w > 0) pre = seg_op(pre, s_warp[w]);
+    if (has_excl) pre = seg_op(pre, excl);
+    // Rows up to the thread's first start add the carried prefix.
+    unsigned first = BY ? (fl ? __ffs(fl) - 1 : SC_ITEMS) : ((row0 == 0 && !seen) ? 0 : SC_ITEMS);
+#pragma unroll
+    for (int j = 0; j < SC_ITEMS; ++j)
+        if (static_cast<unsigned>(j) < first) v[j] += pre.sum;
+    if (ALIGNED && row0 + SC_ITEMS <= n) {
+        ulonglong2 *q = reinterpret_cast<ulonglong2 *>(out + row0);
+#pragma unroll
+        for (int j = 0; j < SC_ITEMS / 2; ++j) __stcs(q + j, make_ulonglong2(v[2 * j], v[2 * j + 1]));
+    } else {
+#pragma unroll
+        for (int j = 0; j < SC_ITEMS; ++j)
+            if (row0 + j < n) out[row0 + j] = v[j];
+    }
+    // The last row's output, the last tile's inclusive value, is the carried state.
+    if (release_ticket_last(counters, tiles) && threadIdx.x == 0) {
+        state->last = ld_relaxed64(&lb.inc[tiles - 1].sum);
+        state->seen = 1;
+    }
+}
+
+struct ScanImpl : ScannerImpl {
+    bool by;
+    ScanState *state = nullptr;
+    cudaStream_t stream = nullptr;
+    ~ScanImpl() override {
+        if (state) cudaFreeAsync(state, stream);
+    }
+    // scan.rs:228-282 (tile_rows): arity, kinds, then destination rows.
+    vkc_status update(vkc_ctx *ctx, const Arg *args, int nargs, vkc_array *out) override {
+        vkc_status st;
+        int want = by ? 2 : 1;
+        if (nargs != want) return fail(ctx, VKC_RUNTIME, arity_error(want, nargs));
+        if (!rows_arg(ctx, args[0], VKC_I64, &st)) return st;
+        if (by && !rows_arg(ctx, args[1], VKC_BOOL, &st)) return st;
+        if (out->type != VKC_I64) return fail(ctx, VKC_RUNTIME, "bad destination");
+        int64_t n = args[0].len();
+        if (out->len != n || (by && args[1].len() != n))
+            return fail(ctx, VKC_RUNTIME, "length mismatch: " + std::to_string(n) +
+                                              " rows for a destination of " + std::to_string(out->len) +
+                                              " rows");
+        if (n == 0) return VKC_OK;
+        int tiles = static_cast<int>((n + SC_TILE - 1) / SC_TILE);
+        void *p;
+        unsigned *flags;
+        if ((st = scratch(ctx, 2 * sizeof(Seg) * static_cast<size_t>(tiles), &p))) return st;
+        if ((st = flag_arena(ctx, static_cast<size_t>(tiles), &flags))) return st;
+        Seg *vals = static_cast<Seg *>(p);
+        LookbackTiles<Seg> lb{flags, vals, vals + tiles};
+        unsigned epoch = next_epoch(ctx);
+        const auto *x = args[0].ptr<unsigned long long>();
+        const unsigned char *s = by ? args[1].ptr<unsigned char>() : nullptr;
+        auto *o = static_cast<unsigned long long *>(out->data());
+        bool aligned = (reinterpret_cast<uintptr_t>(x) & 15) == 0 && (reinterpret_cast<uintptr_t>(o) & 15) == 0 &&
+                       (reinterpret_cast<uintptr_t>(s) & 15) == 0;
+        if (by && aligned) scan_kernel<true, true><<<tiles, SC_THREADS, 0, ctx->stream>>>(x, s, o, n, tiles, lb, epoch, state, ctx->counters, ctx->status);
+        else if (by) scan_kernel<true, false><<<tiles, SC_THREADS, 0, ctx->stream>>>(x, s, o, n, tiles, lb, epoch, state, ctx->counters, ctx->status);
+        else if (aligned) scan_kernel<false, true><<<tiles, SC_THREADS, 0, ctx->stream>>>(x, s, o, n, tiles, lb, epoch, state, ctx->counters, ctx->status);
+        else scan_kernel<false, false><<<tiles, SC_THREADS, 0, ctx->stream>>>(x, s, o, n, tiles, lb, epoch, state, ctx->counters, ctx->status);
+        return launched(ctx, "scan");
+    }
+};
+
+template <bool BY> static ScannerImpl *make_scan(vkc_ctx *ctx) {
+    auto *s = new ScanImpl;
+    s->by = BY;
+    s->stream = ctx->stream;
+    if (cudaMallocAsync(reinterpret_cast<void **>(&s->state), sizeof(ScanState), ctx->stream) != cudaSuccess ||
+        cudaMemsetAsync(s->state, 0, sizeof(ScanState), ctx->stream) != cudaSuccess) {
+        cudaGetLastError();
+        s->state = nullptr;
+        delete s;
+        return nullptr;
+    }
+    return s;
+}
+
+// ------------------------------------------------------------------ prev
+
+__global__ void prev_kernel(const unsigned long long *__restrict__ x, unsigned long long *__restrict__ out,
+                            int64_t n, unsigned long long fill, const ScanState *state) {
+    int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride)
+        out[i] = i == 0 ? (state->seen ? state->last : fill) : __ldcs(x + i - 1);
+}
+
+__global__ void prev_carry(const unsigned long long *x, int64_t n, ScanState *state) {
+    state->last = x[n - 1];
+    state->seen = 1;
+}
+
+// scan.rs:16-48 (Prev): row 0 is the fill on the first update, else the previous update's
+// last row.
+struct PrevImpl : ScannerImpl {
+    ScanState *state = nullptr;
+    cudaStream_t stream = nullptr;
+    ~PrevImpl() override {
+        if (state) cudaFreeAsync(state, stream);
+    }
+    vkc_status update(vkc_ctx *ctx, const Arg *args, int nargs, vkc_array *out) override {
+        vkc_status st;
+        if (nargs != 2) return fail(ctx, VKC_RUNTIME, arity_error(2, nargs));
+        if (!rows_arg(ctx, args[0], VKC_I64, &st) || !splat_arg(ctx, args[1], VKC_I64, &st)) return st;
+        int64_t n = args[0].len();
+        if (out->len != n)
+            return fail(ctx, VKC_RUNTIME, "length mismatch: " + std::to_string(n) +
+                                              " rows for a destination of " + std::to_string(out->len) +
+                                              " rows");
+        if (n == 0) return VKC_OK;
+        const auto *x = args[0].ptr<unsigned long long>();
+        int grid = stream_grid(ctx, n, 256, 8, 2048);
+        prev_kernel<<<grid, 256, 0, ctx->stream>>>(x, static_cast<unsigned long long *>(out->data()), n,
+                                                  args[1].s.bits, state);
+        if ((st = launched(ctx, "prev"))) return st;
+        prev_carry<<<1, 1, 0, ctx->stream>>>(x, n, state);
+        return launched(ctx, "prev_carry");
+    }
+};
+
+static ScannerImpl *make_prev(vkc_ctx *ctx) {
+    auto *s = new PrevImpl;
+    s->stream = ctx->stream;
+    if (cudaMallocAsync(reinterpret_cast<void **>(&s->state), sizeof(ScanState), ctx->stream) != cudaSuccess ||
+        cudaMemsetAsync(s->state, 0, sizeof(ScanState), ctx->stream) != cudaSuccess) {
+        cudaGetLastError();
+        s->state = nullptr;
+        delete s;
+        return nullptr;
+    }
+    return s;
+}
+
+void register_scan(std::vector<KernelDef> &t) {
+    InSpec ia{IN_ARRAY, VKC_I64};
+    // scan.rs:336-352: cost = input + output width (+1 for the starts byte).
+    KernelDef d{"scan_add_i64", VKC_SCAN, {ia}, true, VKC_I64, 16};
+    d.scan = make_scan<false>;
+    t.push_back(d);
+    d = KernelDef{"scan_by_add_i64", VKC_SCAN, {ia, InSpec{IN_ARRAY, VKC_BOOL}}, true, VKC_I64, 17};
+    d.scan = make_scan<true>;
+    t.push_back(d);
+    d = KernelDef{"prev_i64", VKC_SCAN, {ia, InSpec{IN_SCALAR, VKC_I64}}, true, VKC_I64, 16};
+    d.scan = make_prev;
+    t.push_back(d);
+}
+
+}  // namespace vkc

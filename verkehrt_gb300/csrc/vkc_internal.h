@@ -1,0 +1,138 @@
+// Internal declarations shared by the runtime (runtime.cu) and the kernel families (k_*.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cstdint>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/vkcuda.h"
+
+namespace vkc {
+
+// Bytes per row of each element type (src/value.rs:47-55, ScalarType::width).
+inline int type_width(vkc_type t) {
+    switch (t) {
+    case VKC_F64: case VKC_I64: case VKC_U64: return 8;
+    case VKC_F32: case VKC_I32: return 4;
+    default: return 1;
+    }
+}
+
+// ScalarType::name, src/value.rs:57-71.
+inline const char *type_name(vkc_type t) {
+    switch (t) {
+    case VKC_F64: return "f64";
+    case VKC_F32: return "f32";
+    case VKC_I64: return "i64";
+    case VKC_U64: return "u64";
+    case VKC_I32: return "i32";
+    case VKC_U8: return "u8";
+    default: return "bool";
+    }
+}
+
+// A device allocation shared by an array and its views. Freed stream-ordered on the stream of
+// the context that allocated it.
+struct Buffer {
+    void *ptr = nullptr;
+    size_t bytes = 0;
+    cudaStream_t stream = nullptr;
+    ~Buffer();
+};
+
+}  // namespace vkc
+
+struct vkc_array {
+    std::atomic<int> refs{1};
+    std::shared_ptr<vkc::Buffer> buf;
+    int64_t offset = 0;  // rows into buf
+    int64_t len = 0;
+    vkc_type type = VKC_F64;
+    void *data() const {
+        return buf && buf->ptr ? static_cast<char *>(buf->ptr) + offset * vkc::type_width(type)
+                               : nullptr;
+    }
+};
+
+namespace vkc {
+
+// Lookback and reduction scratch. One arena per context: kernels on the context stream run
+// one after another, so consecutive launches may reuse it.
+struct Scratch {
+    void *ptr = nullptr;
+    size_t bytes = 0;
+};
+
+// Device-side status word, written by kernels on a detected error (an out-of-range index, a
+// wait that ran out). Positions are row indices of the offending input element.
+struct DevStatus {
+    unsigned long long first_bad;  // min offending row, ~0 when none
+    unsigned int timeout;          // a bounded spin gave up
+    unsigned int pad;
+};
+
+}  // namespace vkc
+
+struct vkc_ctx {
+    int device = 0;
+    int sms = 0;
+    cudaStream_t stream = nullptr;
+    cudaStream_t own_stream = nullptr;
+    cudaEvent_t ev_start = nullptr, ev_stop = nullptr;
+    std::string err;
+    uint64_t launches = 0;
+    // Epoch tag of lookback flags: a flag word written by an earlier launch never matches.
+    uint32_t epoch = 0;
+    vkc::Scratch scratch;
+    // Lookback flag words, written only as epoch<<2 | state, so a word from another launch
+    // never reads as ready.
+    vkc::Scratch flags;
+    // Device status and the counters that last-block-done reductions reset on exit.
+    vkc::DevStatus *status = nullptr;
+    unsigned int *counters = nullptr;  // [0] ticket, [1] done; zero between launches
+    // Pinned host staging for small results.
+    void *pinned = nullptr;
+    size_t pinned_bytes = 0;
+};
+
+namespace vkc {
+
+constexpr int kCounterSlots = 64;
+
+// Status helpers. `fail` records the message and returns the status.
+vkc_status fail(vkc_ctx *ctx, vkc_status st, const std::string &msg);
+vkc_status cuda_fail(vkc_ctx *ctx, cudaError_t e, const char *what);
+#define VKC_CUDA(ctx, call)                                          \
+    do {                                                             \
+        cudaError_t e_ = (call);                                     \
+        if (e_ != cudaSuccess) return ::vkc::cuda_fail(ctx, e_, #call); \
+    } while (0)
+
+// Scratch of at least `bytes`, 256-byte aligned. The pointer stays valid until the next call.
+vkc_status scratch(vkc_ctx *ctx, size_t bytes, void **out);
+// `count` epoch-tagged lookback flag words (see vkc_ctx::flags).
+vkc_status flag_arena(vkc_ctx *ctx, size_t count, unsigned **out);
+// Pinned host staging of at least `bytes`.
+vkc_status pinned(vkc_ctx *ctx, size_t bytes, void **out);
+// Next lookback epoch (1..2^30-1). Wraps by clearing the scratch arena.
+uint32_t next_epoch(vkc_ctx *ctx);
+// Reads and clears the device status after the stream's work completes.
+vkc_status read_status(vkc_ctx *ctx, DevStatus *out);
+// Checks a kernel launch and counts it.
+vkc_status launched(vkc_ctx *ctx, const char *what);
+
+// New array of `len` rows (uninitialised unless `zero`). Message texts follow
+// src/value.rs:285-307.
+vkc_status new_array(vkc_ctx *ctx, vkc_type t, int64_t len, bool zero, vkc_array **out);
+// Shrinks an array's logical length (the allocation stays).
+inline void set_len(vkc_array *a, int64_t len) { a->len = len; }
+
+// Grid size for a streaming kernel: a multiple of the SM count, at most enough blocks to give
+// every block `min_items` items.
+int stream_grid(const vkc_ctx *ctx, int64_t items, int block, int per_sm, int64_t min_items);
+
+}  // namespace vkc
