@@ -124,12 +124,18 @@ static vkc_status run_select(vkc_ctx *ctx, SelArgs a, int64_t n, Builder *b) {
     else
         select_kernel<KIND, W, false><<<tiles, SEL_THREADS, 0, ctx->stream>>>(a, tiles, lb, epoch, ctx->counters, ctx->status);
     if ((st = launched(ctx, "select"))) return st;
+    DevStatus ds;
+    if ((st = read_status(ctx, &ds))) return st;
     void *h;
     if ((st = pinned(ctx, 8, &h))) return st;
     VKC_CUDA(ctx, cudaMemcpyAsync(h, a.total, 8, cudaMemcpyDeviceToHost, ctx->stream));
-    DevStatus ds;
-    if ((st = read_status(ctx, &ds))) return st;
-    b->len += static_cast<int64_t>(*static_cast<unsigned long long *>(h));
+    VKC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    unsigned long long k = *static_cast<unsigned long long *>(h);
+    // The count can only be at most the rows reserved; anything else is a broken launch.
+    if (k > static_cast<unsigned long long>(n))
+        return fail(ctx, VKC_DEVICE, "selection returned " + std::to_string(k) + " rows for " +
+                                         std::to_string(n) + " input rows");
+    b->len += static_cast<int64_t>(k);
     return VKC_OK;
 }
 

@@ -87,13 +87,10 @@ uint32_t next_epoch(vkc_ctx *ctx) {
 }
 
 vkc_status read_status(vkc_ctx *ctx, DevStatus *out) {
-    void *h;
-    vkc_status st = pinned(ctx, sizeof(DevStatus), &h);
-    if (st) return st;
-    VKC_CUDA(ctx, cudaMemcpyAsync(h, ctx->status, sizeof(DevStatus), cudaMemcpyDeviceToHost,
-                                  ctx->stream));
+    VKC_CUDA(ctx, cudaMemcpyAsync(ctx->status_host, ctx->status, sizeof(DevStatus),
+                                  cudaMemcpyDeviceToHost, ctx->stream));
     VKC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    memcpy(out, h, sizeof(DevStatus));
+    memcpy(out, ctx->status_host, sizeof(DevStatus));
     if (out->first_bad != ~0ull || out->timeout) {
         DevStatus clean{~0ull, 0, 0};
         VKC_CUDA(ctx, cudaMemcpyAsync(ctx->status, &clean, sizeof clean, cudaMemcpyHostToDevice,
@@ -375,6 +372,12 @@ vkc_status vkc_open(int device, vkc_ctx **out) {
         return VKC_DEVICE;
     }
     ctx->status = static_cast<DevStatus *>(p);
+    if (cudaMallocHost(reinterpret_cast<void **>(&ctx->status_host), sizeof(DevStatus)) != cudaSuccess) {
+        cudaGetLastError();
+        cudaFree(p);
+        delete ctx;
+        return VKC_DEVICE;
+    }
     ctx->counters = reinterpret_cast<unsigned *>(static_cast<char *>(p) + sizeof(DevStatus));
     DevStatus clean{~0ull, 0, 0};
     cudaMemcpy(ctx->status, &clean, sizeof clean, cudaMemcpyHostToDevice);
@@ -392,6 +395,7 @@ void vkc_close(vkc_ctx *ctx) {
     cudaStreamSynchronize(ctx->stream);
     if (ctx->status) cudaFree(ctx->status);
     if (ctx->pinned) cudaFreeHost(ctx->pinned);
+    if (ctx->status_host) cudaFreeHost(ctx->status_host);
     cudaEventDestroy(ctx->ev_start);
     cudaEventDestroy(ctx->ev_stop);
     cudaStreamDestroy(ctx->own_stream);

@@ -94,6 +94,8 @@ struct vkc_ctx {
     // Device status and the counters that last-block-done reductions reset on exit.
     vkc::DevStatus *status = nullptr;
     unsigned int *counters = nullptr;  // [0] ticket, [1] done; zero between launches
+    // Pinned host copy of the status word (its own buffer: never shared with results).
+    vkc::DevStatus *status_host = nullptr;
     // Pinned host staging for small results.
     void *pinned = nullptr;
     size_t pinned_bytes = 0;
