@@ -1,0 +1,448 @@
+#!/usr/bin/env python3
+"""Benchmark of the verkehrt kernel-table primitives on GB300 (the `cuda` ISA).
+
+Workload: the primitive sweep at n = 2^28 rows (the reference's headline "HBM GB/s per kernel"
+sweep at its largest size): reduce_add/dot/min/max/argmin/argmax over f64 uniform [0,1),
+count_gt and filter_gt at 1%/50%/99% selectivity, gather_i64 with indices uniform in [0,n),
+scan_add_i64 over values uniform in [-2^20, 2^20), and the unfused dot (mul_f64 then
+reduce_add_f64), which must give the fused bits. One step runs every primitive once as a plain
+per-statement call through the C ABI.
+
+value   algorithmic bytes of the step / device time of the step (GB/s, inputs resident in HBM,
+        every array 2 GiB, larger than the 126 MB L2, so no flush is needed)
+e2e     the same bytes / time of the step through the C ABI with host buffers: the step's inputs
+        uploaded from pinned host memory and its array results downloaded, every step
+roofline  the dominant kernel's algorithmic GB/s against the measured HBM copy bandwidth
+cpu_baseline  the oracle port of the reference's scalar entries (single thread, like the
+        reference) on a bounded sample of the same workload, on this machine's host
+
+--impl reference times that CPU implementation as the reference arm. With N > 1 ranks (torchrun)
+every rank runs an independent replica ("replicas only": the primitives have no exchange step).
+"""
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "HBM GB/s per kernel vs peak; batched/served req/s and p99 vs plain GPU path"
+UNIT = "GB/s"
+SELECTIVITY = (0.99, 0.5, 0.01)  # thresholds of count_gt/filter_gt: 1%, 50%, 99% kept
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def committed_traffic():
+    """Per-launch DRAM bytes of the dominant kernels from the committed ncu captures."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            return json.load(f)
+    return {}
+
+
+# ---------------------------------------------------------------------------- clocks
+
+
+class ClockSampler:
+    """Samples nvidia-smi every 200 ms during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, ValueError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for name, val in zip(names, f[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------- the sweep
+
+
+def sweep_plan(n):
+    """(label, kernel, argument names, extra scalars, fixed algorithmic bytes)."""
+    plan = [
+        ("reduce_add_f64", "reduce_add_f64", ["x"], [], 8 * n),
+        ("dot_f64", "dot_f64", ["x", "y"], [], 16 * n),
+        ("reduce_min_f64", "reduce_min_f64", ["x"], [], 8 * n),
+        ("reduce_max_f64", "reduce_max_f64", ["x"], [], 8 * n),
+        ("argmin_f64", "argmin_f64", ["x"], [], 8 * n),
+        ("argmax_f64", "argmax_f64", ["x"], [], 8 * n),
+    ]
+    for c in SELECTIVITY:
+        plan.append(("count_gt_f64@%g" % c, "count_gt_f64", ["x"], [c], 8 * n))
+    for c in SELECTIVITY:
+        plan.append(("filter_gt_f64@%g" % c, "filter_gt_f64", ["x"], [c], 8 * n))  # + 8k
+    plan += [
+        ("gather_i64", "gather_i64", ["src", "idx"], [], 24 * n),
+        ("scan_add_i64", "scan_add_i64", ["v"], [], 16 * n),
+        ("mul_f64", "mul_f64", ["x", "y"], [], 24 * n),
+        ("reduce_add_f64(mul)", "reduce_add_f64", ["xy"], [], 8 * n),
+    ]
+    return plan
+
+
+def make_inputs(ctx, n):
+    """Seeded inputs generated on the device with the reference's rand_* kernels."""
+    assert n & (n - 1) == 0, "n must be a power of two (indices are rand mod n)"
+    x = ctx.call("rand_f64", n, 1)
+    y = ctx.call("rand_f64", n, 2)
+    src = ctx.call("rand_i64", n, 3)
+    idx = ctx.call("and_i64", ctx.call("rand_i64", n, 4), n - 1)
+    v = ctx.call("sub_i64", ctx.call("and_i64", ctx.call("rand_i64", n, 5), (1 << 21) - 1), 1 << 20)
+    ctx.synchronize()
+    return {"x": x, "y": y, "src": src, "idx": idx, "v": v}
+
+
+def run_step(ctx, n, inputs, events, host_out=None):
+    """One pass of the sweep. Returns {label: (ms, bytes)} measured with CUDA events on the
+    library's stream, the step's device time, and the results."""
+    import torch
+
+    plan = sweep_plan(n)
+    marks = []
+    results = {}
+    env = dict(inputs)
+    stream = events["stream"]
+    with torch.cuda.stream(stream):
+        start = torch.cuda.Event(enable_timing=True)
+        start.record(stream)
+        for label, kernel, names, extra, nbytes in plan:
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            out = ctx.call(kernel, *[env[a] for a in names], *extra)
+            e1.record(stream)
+            if kernel == "filter_gt_f64":
+                nbytes += 8 * len(out)
+            if kernel == "mul_f64":
+                env["xy"] = out
+            results[label] = out
+            marks.append((label, e0, e1, nbytes))
+        stop = torch.cuda.Event(enable_timing=True)
+        stop.record(stream)
+    stop.synchronize()
+    per = {label: (e0.elapsed_time(e1), b) for label, e0, e1, b in marks}
+    return per, start.elapsed_time(stop), results
+
+
+def check_results(results):
+    """The unfused dot must give the fused bits (fused-equals-unfused on device)."""
+    a = results["dot_f64"]
+    b = results["reduce_add_f64(mul)"]
+    if np.float64(a).view(np.uint64) != np.float64(b).view(np.uint64):
+        raise SystemExit("fused dot %r != unfused %r" % (a, b))
+
+
+# ---------------------------------------------------------------------------- e2e
+
+
+class HostInputs:
+    """The step's inputs in pinned host memory, and pinned buffers for the array results."""
+
+    def __init__(self, ctx, inputs, n):
+        import torch
+
+        self.n = n
+        self.host = {}
+        for name, arr in inputs.items():
+            t = torch.empty(n, dtype=torch.float64 if arr.type == "f64" else torch.int64, pin_memory=True)
+            ctx.download_ptr(arr, t.data_ptr(), n)
+            self.host[name] = (t, arr.type)
+        self.out = torch.empty(n, dtype=torch.int64, pin_memory=True)
+
+    def upload(self, ctx):
+        return {name: ctx.upload_ptr(t.data_ptr(), self.n, ty) for name, (t, ty) in self.host.items()}
+
+
+def run_e2e_step(ctx, n, hin):
+    """Upload the inputs from pinned host memory, run the sweep, download the array results.
+    Returns (seconds, h2d bytes, d2h bytes)."""
+    t0 = time.perf_counter()
+    inputs = hin.upload(ctx)
+    h2d = sum(8 * n for _ in inputs)
+    env = dict(inputs)
+    d2h = 0
+    for label, kernel, names, extra, _ in sweep_plan(n):
+        out = ctx.call(kernel, *[env[a] for a in names], *extra)
+        if kernel == "mul_f64":
+            env["xy"] = out
+        if hasattr(out, "handle"):
+            if kernel != "mul_f64":
+                ctx.download_ptr(out, hin.out.data_ptr(), n)
+                d2h += 8 * len(out)
+        else:
+            d2h += 8  # the scalar result
+    ctx.synchronize()
+    return time.perf_counter() - t0, h2d, d2h
+
+
+# ---------------------------------------------------------------------------- CPU baseline
+
+
+def cpu_baseline(n_sample, budget_s=12.0):
+    """Times the oracle port of the reference's scalar entries (one thread, as the reference
+    runs) over the same sweep at a sample size. Returns (GB/s, description)."""
+    import oracle
+
+    x, y = oracle.rand_f64(n_sample, 1), oracle.rand_f64(n_sample, 2)
+    src = oracle.rand_i64(n_sample, 3)
+    idx = (oracle.rand_i64(n_sample, 4) & (n_sample - 1)).astype(np.int64)
+    v = (oracle.rand_i64(n_sample, 5) & ((1 << 21) - 1)) - (1 << 20)
+    n = n_sample
+    steps = [
+        (lambda: oracle.reduce_add_f64(x), 8 * n),
+        (lambda: oracle.dot_f64(x, y), 16 * n),
+        (lambda: oracle.reduce_min_f64(x), 8 * n),
+        (lambda: oracle.reduce_max_f64(x), 8 * n),
+        (lambda: oracle.argmin_f64(x), 8 * n),
+        (lambda: oracle.argmax_f64(x), 8 * n),
+    ]
+    for c in SELECTIVITY:
+        steps.append((lambda c=c: oracle.count_cmp_f64(x, "gt", c), 8 * n))
+    for c in SELECTIVITY:
+        steps.append((lambda c=c: oracle.filter_cmp_f64(x, "gt", c), None))
+    steps += [
+        (lambda: oracle.gather(src, idx), 24 * n),
+        (lambda: oracle.scan_add_i64(v), 16 * n),
+        (lambda: oracle.reduce_add_f64(oracle.mul_f64(x, y)), 32 * n),
+    ]
+    total_b, total_t, passes = 0, 0.0, 0
+    t_start = time.perf_counter()
+    while passes < 2 or (time.perf_counter() - t_start < budget_s and passes < 50):
+        for fn, b in steps:
+            t0 = time.perf_counter()
+            r = fn()
+            total_t += time.perf_counter() - t0
+            total_b += b if b is not None else 8 * n + 8 * len(r)
+        passes += 1
+    return total_b / total_t / 1e9, passes
+
+
+# ---------------------------------------------------------------------------- main
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("gloo", rank=rank, world_size=world)
+    return world, rank, local
+
+
+def reduce_max(value, world):
+    """Max over ranks (the slowest replica sets the aggregate time)."""
+    if world == 1:
+        return value
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([value], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def aggregate(bytes_per_step, steps, max_total_ms, world):
+    """Whole-job GB/s: every replica moves bytes_per_step per step; the slowest sets the time."""
+    return world * bytes_per_step * steps / (max_total_ms / 1e3) / 1e9
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--n", type=int, default=1 << 28)
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--cpu-sample", type=int, default=1 << 23)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    world, rank, local = dist_setup()
+    n = args.n
+    config = {"workload": "primitive sweep, n=2^%d rows per array (f64 uniform [0,1), i64 gather "
+                          "indices uniform in [0,n), i64 scan values uniform in [-2^20,2^20))"
+                          % (n.bit_length() - 1),
+              "n": n, "kernels": [p[0] for p in sweep_plan(n)],
+              "l2": "inputs larger than L2 (2 GiB arrays), no flush",
+              "parallelism": "replicas" if world > 1 else "single GPU"}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        gbs, passes = cpu_baseline(args.cpu_sample, budget_s=max(3.0, 2.0 * args.steps))
+        sample = "oracle port of the scalar entries, sweep at n=2^%d, %d passes" % (
+            args.cpu_sample.bit_length() - 1, passes)
+        line = {"impl": "reference", "metric": METRIC, "value": round(gbs, 3), "unit": UNIT,
+                "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64+i64",
+                "data": "synthetic (seeded rand_f64/rand_i64, the reference generators)",
+                "config": config,
+                "cpu_baseline": {"value": round(gbs, 3), "unit": UNIT, "cores": 1, "kind": "port",
+                                 "sample": sample},
+                "e2e": {"value": round(gbs, 3), "unit": UNIT, "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
+
+    import torch
+
+    import verkehrt_gb300 as vk
+    from verkehrt_gb300 import build as vbuild
+
+    vbuild.build()
+    torch.cuda.set_device(local)
+    ctx = vk.Context(local)
+    stream = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", local))
+    events = {"stream": stream}
+    inputs = make_inputs(ctx, n)
+
+    for _ in range(args.warmup):
+        _, _, res = run_step(ctx, n, inputs, events)
+        check_results(res)
+
+    clocks = ClockSampler(local)
+    barrier(world)
+    clocks.start()
+    launches0 = ctx.launch_count()
+    per_label = {}
+    step_ms = []
+    for _ in range(args.steps):
+        per, ms, res = run_step(ctx, n, inputs, events)
+        step_ms.append(ms)
+        for label, (t, b) in per.items():
+            acc = per_label.setdefault(label, [0.0, 0, 0])
+            acc[0] += t
+            acc[1] += b
+            acc[2] += 1
+    launches = ctx.launch_count() - launches0
+    torch.cuda.synchronize()
+    barrier(world)
+    clk = clocks.stop()
+    check_results(res)
+
+    bytes_per_step = sum(v[1] for v in per_label.values()) / args.steps
+    total_ms = reduce_max(sum(step_ms), world)
+    value = aggregate(bytes_per_step, args.steps, total_ms, world)
+
+    # Dominant kernel: the largest share of the step's kernel time.
+    dom = max(per_label, key=lambda k: per_label[k][0])
+    dom_ms = per_label[dom][0] / per_label[dom][2]
+    dom_bytes = per_label[dom][1] / per_label[dom][2]
+    achieved = dom_bytes / (dom_ms / 1e3) / 1e9
+    peak, peak_kind = measured_peaks()
+    traffic = committed_traffic().get(dom.split("@")[0])
+    kernels = {k: {"ms": round(v[0] / v[2], 4), "GB/s": round(v[1] / v[2] / (v[0] / v[2] / 1e3) / 1e9, 1),
+                   "frac": round(v[1] / v[2] / (v[0] / v[2] / 1e3) / 1e9 / peak, 3)}
+               for k, v in per_label.items()}
+
+    # e2e through the C ABI with pinned host buffers.
+    hin = HostInputs(ctx, inputs, n)
+    e2e = []
+    for _ in range(max(1, args.e2e_steps)):
+        e2e.append(run_e2e_step(ctx, n, hin))
+    e2e_s = reduce_max(sum(t for t, _, _ in e2e), world)
+    e2e_value = world * bytes_per_step * len(e2e) / e2e_s / 1e9
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        gbs, passes = cpu_baseline(args.cpu_sample)
+        cpu = {"value": round(gbs, 3), "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": "oracle port of the scalar entries (one thread, as the reference), the sweep "
+                         "at n=2^%d, %d passes" % (args.cpu_sample.bit_length() - 1, passes)}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(total_ms / args.steps, 4), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64+i64",
+            "data": "synthetic (seeded rand_f64/rand_i64 generated on device, the reference generators)",
+            "config": config,
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1),
+                         "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
+                         "traffic": traffic, "peak_kind": peak_kind},
+            "cpu_baseline": cpu,
+            "e2e": {"value": round(e2e_value, 3), "unit": UNIT,
+                    "h2d_bytes_per_step": e2e[0][1], "d2h_bytes_per_step": e2e[0][2]},
+            "clocks": clk,
+            "gpu_launches": launches,
+            "kernels": kernels,
+        }
+        print(json.dumps(line), flush=True)
+    ctx.close()
+
+
+if __name__ == "__main__":
+    main()

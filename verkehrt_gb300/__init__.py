@@ -265,6 +265,16 @@ class Context:
                                           len(a), ctypes.byref(h)))
         return Array(self, h.value)
 
+    def upload_ptr(self, ptr, n, type_name):
+        """Uploads n rows from host address `ptr` (pinned memory for full-speed copies)."""
+        h = _P()
+        self._check(_lib.vkc_array_upload(self.handle, TYPES[type_name], ptr, n, ctypes.byref(h)))
+        return Array(self, h.value)
+
+    def download_ptr(self, arr, ptr, capacity):
+        """Copies up to `capacity` rows of `arr` to host address `ptr`; waits for the copy."""
+        self._check(_lib.vkc_array_download(self.handle, arr.handle, ptr, capacity))
+
     def new_array(self, type_name, n):
         h = _P()
         self._check(_lib.vkc_array_new(self.handle, TYPES[type_name], n, ctypes.byref(h)))

@@ -22,10 +22,10 @@ template <class T> __device__ __forceinline__ T get(const Opnd &o, int64_t i) {
     return v;
 }
 
+// Comparisons come last: an op at or after EW_EQ produces bool.
 enum EwOp {
-    EW_ADD, EW_SUB, EW_MUL, EW_MIN, EW_MAX,
-    EW_EQ, EW_NE, EW_LT, EW_LE, EW_GT, EW_GE,
-    EW_AND, EW_OR, EW_NOT, EW_SELECT
+    EW_ADD, EW_SUB, EW_MUL, EW_MIN, EW_MAX, EW_AND, EW_OR, EW_XOR, EW_NOT,
+    EW_EQ, EW_NE, EW_LT, EW_LE, EW_GT, EW_GE
 };
 
 // IEEE 754-2019 minimum/maximum, elementwise.rs:412-440.
@@ -70,6 +70,9 @@ template <int OP> struct Bin<long long, OP> {
         case EW_MUL: return static_cast<long long>(ua * ub);
         case EW_MIN: return a < b ? a : b;
         case EW_MAX: return a > b ? a : b;
+        case EW_AND: return a & b;
+        case EW_OR: return a | b;
+        case EW_XOR: return a ^ b;
         case EW_EQ: return a == b;
         case EW_NE: return a != b;
         case EW_LT: return a < b;
@@ -188,6 +191,9 @@ void register_elementwise(std::vector<KernelDef> &t) {
         {"mul_i64", {ie, ie}, VKC_I64, 24, run_binary<long long, EW_MUL>},
         {"min_i64", {ie, ie}, VKC_I64, 24, run_binary<long long, EW_MIN>},
         {"max_i64", {ie, ie}, VKC_I64, 24, run_binary<long long, EW_MAX>},
+        {"and_i64", {ie, ie}, VKC_I64, 24, run_binary<long long, EW_AND>},
+        {"or_i64", {ie, ie}, VKC_I64, 24, run_binary<long long, EW_OR>},
+        {"xor_i64", {ie, ie}, VKC_I64, 24, run_binary<long long, EW_XOR>},
         {"eq_i64", {ie, ie}, VKC_BOOL, 17, run_binary<long long, EW_EQ>},
         {"ne_i64", {ie, ie}, VKC_BOOL, 17, run_binary<long long, EW_NE>},
         {"lt_i64", {ie, ie}, VKC_BOOL, 17, run_binary<long long, EW_LT>},
