@@ -184,6 +184,23 @@ VKC_API vkc_status vkc_select_tile(vkc_ctx *ctx, int id, const vkc_value *args, 
 VKC_API vkc_status vkc_elementwise_tile(vkc_ctx *ctx, int id, const vkc_value *args, int nargs,
                                 vkc_array *out);
 
+/* ------------------------------------------------------------------ allocation-free entry */
+
+/* scan_add_i64 (the inclusive wrapping prefix sum of `n` rows of `in` into `out`, both device
+ * pointers) for callers that cannot allocate device memory: an embedding host that gives this
+ * library only its own buffers (an interpreter's arena, a pool with a fixed budget), or a
+ * serving loop that must not take the allocator's lock or latency per request. It has no
+ * counterpart in the reference, whose kernels run on the host. It needs no vkc_ctx and calls
+ * no allocator: its lookback scratch is a 2.5 MiB array in the library's device image, so n
+ * may be at most 2^28 rows (larger n is rejected with VKC_USAGE and a message). The first call
+ * on a device looks up the array's device address (once per device); make that first call
+ * before any stream capture. Every call shares the array: calls that overlap on the GPU race,
+ * so run them on one stream or one after another. Work runs on `stream` (a cudaStream_t, NULL
+ * for the legacy default stream) and the call returns when the scan is complete. On failure a
+ * message is written to `err` (`err_len` bytes, may be NULL). */
+VKC_API vkc_status vkc_scan_add_i64_noalloc(int device, const int64_t *in, int64_t *out, int64_t n,
+                                            void *stream, char *err, size_t err_len);
+
 #ifdef __cplusplus
 }
 #endif

@@ -91,6 +91,8 @@ _SIGNATURES = {
                                        ctypes.c_int64, _P]),
     "vkc_elementwise_tile": (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(_Value), ctypes.c_int,
                                             _P]),
+    "vkc_scan_add_i64_noalloc": (ctypes.c_int, [ctypes.c_int, _P, _P, ctypes.c_int64, _P,
+                                                ctypes.c_char_p, ctypes.c_size_t]),
 }
 
 _lib = None

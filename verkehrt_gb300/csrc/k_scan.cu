@@ -5,6 +5,9 @@
 // on (starts-a-segment, sum): (f1, v1) then (f2, v2) = (f1 | f2, f2 ? v2 : v1 + v2). Row 0 of
 // the array always starts a segment; a later update continues the segment of the previous
 // one unless its first start byte says otherwise, as Scan::update does.
+#include <cstring>
+#include <mutex>
+
 #include "lookback.cuh"
 #include "reduce_common.h"
 
@@ -255,3 +258,122 @@ void register_scan(std::vector<KernelDef> &t) {
 }
 
 }  // namespace vkc
+
+// ------------------------------------------------------------------ allocation-free scan_add_i64
+//
+// vkc_scan_add_i64_noalloc: scan_add_i64 for callers that cannot allocate device memory. An
+// embedding host that hands this library only its own buffers (an interpreter's arena or a
+// memory pool with a fixed budget), or a serving loop that must not take the allocator's lock
+// or latency while it answers a request, cannot use the entries above, which take their
+// lookback scratch from a context arena that grows with cudaMallocAsync. This entry needs no
+// context and allocates nothing: the lookback records live in the file-scope array below, whose
+// address is looked up once per device. Every call shares the array and finds it as the last
+// call left it, so each call clears the words that must start at zero (the ticket counters,
+// the tile flags, the carried state and the status). Calls that overlap on the GPU race on the
+// array: issue them on one stream, or wait for one to finish before the next starts.
+namespace vkc {
+
+// Header (ticket counters, status, carried state), the tile flags, then the tile aggregates
+// and inclusive prefixes. 2.5 MiB holds the 65,536 tiles of 2^28 rows.
+constexpr int64_t NOALLOC_MAX_ROWS = int64_t(1) << 28;
+constexpr int64_t NOALLOC_MAX_TILES = NOALLOC_MAX_ROWS / SC_TILE;
+constexpr size_t NOALLOC_HEADER = 512;
+constexpr size_t NOALLOC_FLAGS = NOALLOC_MAX_TILES * sizeof(unsigned);
+constexpr size_t NOALLOC_BYTES = NOALLOC_HEADER + NOALLOC_FLAGS + 2 * NOALLOC_MAX_TILES * sizeof(Seg);
+
+static __device__ __align__(256) unsigned char g_scan_scratch[NOALLOC_BYTES];
+
+constexpr int NOALLOC_MAX_DEVICES = 64;
+static std::mutex g_noalloc_mu;
+static unsigned char *g_noalloc_ptr[NOALLOC_MAX_DEVICES];
+
+static void noalloc_msg(char *err, size_t err_len, const std::string &msg) {
+    if (err && err_len) {
+        size_t k = msg.size() < err_len - 1 ? msg.size() : err_len - 1;
+        memcpy(err, msg.data(), k);
+        err[k] = 0;
+    }
+}
+
+}  // namespace vkc
+
+extern "C" vkc_status vkc_scan_add_i64_noalloc(int device, const int64_t *in, int64_t *out, int64_t n,
+                                               void *stream, char *err, size_t err_len) {
+    using namespace vkc;
+    noalloc_msg(err, err_len, "");
+    if (n < 0 || n > NOALLOC_MAX_ROWS) {
+        noalloc_msg(err, err_len, "vkc_scan_add_i64_noalloc: " + std::to_string(n) +
+                                      " rows is more than its maximum of 268435456 rows (2^28)");
+        return VKC_USAGE;
+    }
+    if (device < 0 || device >= NOALLOC_MAX_DEVICES) {
+        noalloc_msg(err, err_len, "vkc_scan_add_i64_noalloc: device " + std::to_string(device) +
+                                      " is out of range");
+        return VKC_USAGE;
+    }
+    if (n == 0) return VKC_OK;
+    int prev = 0;
+    if (cudaGetDevice(&prev) != cudaSuccess || cudaSetDevice(device) != cudaSuccess) {
+        cudaGetLastError();
+        noalloc_msg(err, err_len, "vkc_scan_add_i64_noalloc: cannot make device " + std::to_string(device) +
+                                      " current");
+        return VKC_DEVICE;
+    }
+    auto done = [&](vkc_status st, const std::string &msg) {
+        if (st != VKC_OK) noalloc_msg(err, err_len, msg);
+        cudaSetDevice(prev);
+        return st;
+    };
+    unsigned char *base;
+    {
+        // Set-up, once per device: the device address of the scratch array. On the first call on
+        // a device this runs inside that call.
+        std::lock_guard<std::mutex> lock(g_noalloc_mu);
+        if (!g_noalloc_ptr[device]) {
+            void *p = nullptr;
+            cudaError_t e = cudaGetSymbolAddress(&p, g_scan_scratch);
+            if (e != cudaSuccess || !p) {
+                cudaGetLastError();
+                return done(VKC_DEVICE, std::string("vkc_scan_add_i64_noalloc: cudaGetSymbolAddress failed: ") +
+                                            cudaGetErrorString(e));
+            }
+            g_noalloc_ptr[device] = static_cast<unsigned char *>(p);
+        }
+        base = g_noalloc_ptr[device];
+    }
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    int tiles = static_cast<int>((n + SC_TILE - 1) / SC_TILE);
+    unsigned *counters = reinterpret_cast<unsigned *>(base);
+    DevStatus *status = reinterpret_cast<DevStatus *>(base + 256);
+    ScanState *state = reinterpret_cast<ScanState *>(base + 256 + sizeof(DevStatus));
+    unsigned *flags = reinterpret_cast<unsigned *>(base + NOALLOC_HEADER);
+    Seg *agg = reinterpret_cast<Seg *>(base + NOALLOC_HEADER + NOALLOC_FLAGS);
+    LookbackTiles<Seg> lb{flags, agg, agg + NOALLOC_MAX_TILES};
+    // The header and the flags of this call's tiles start at zero; with clean flags one epoch
+    // value serves every call.
+    cudaError_t e = cudaMemsetAsync(base, 0, NOALLOC_HEADER, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(flags, 0, static_cast<size_t>(tiles) * sizeof(unsigned), s);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return done(VKC_DEVICE, std::string("vkc_scan_add_i64_noalloc: ") + cudaGetErrorString(e));
+    }
+    const auto *x = reinterpret_cast<const unsigned long long *>(in);
+    auto *o = reinterpret_cast<unsigned long long *>(out);
+    bool aligned = (reinterpret_cast<uintptr_t>(x) & 15) == 0 && (reinterpret_cast<uintptr_t>(o) & 15) == 0;
+    if (aligned)
+        scan_kernel<false, true><<<tiles, SC_THREADS, 0, s>>>(x, nullptr, o, n, tiles, lb, 1u, state, counters, status);
+    else
+        scan_kernel<false, false><<<tiles, SC_THREADS, 0, s>>>(x, nullptr, o, n, tiles, lb, 1u, state, counters, status);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return done(VKC_DEVICE, std::string("vkc_scan_add_i64_noalloc: ") + cudaGetErrorString(e));
+    // Synchronous, like the other entries: read the status word into host memory.
+    DevStatus hs{};
+    e = cudaMemcpyAsync(&hs, status, sizeof hs, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return done(VKC_DEVICE, std::string("vkc_scan_add_i64_noalloc: ") + cudaGetErrorString(e));
+    }
+    if (hs.timeout) return done(VKC_TIMEOUT, "vkc_scan_add_i64_noalloc: a device-side wait gave up");
+    return done(VKC_OK, "");
+}
