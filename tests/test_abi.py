@@ -51,6 +51,8 @@ HOT_PATH = [
     "histogram", "reduce_into_add_i64",
     # unfused plans
     "mul_f64", "gt_f64", "select_f64",
+    # sort and group-by
+    "argsort_i64", "group_id_i64", "group_id2_i64_i64", "prev_i64", "iota",
 ]
 
 
