@@ -38,9 +38,9 @@
 namespace vkc {
 
 constexpr int CT_THREADS = 256;
-constexpr int CT_SEGS = 32;        // segments per tile
-constexpr int CT_SEG_BLOCKS = 16;  // 16-row blocks per segment
-constexpr int CT_BLOCKS = CT_SEGS * CT_SEG_BLOCKS;  // 512 blocks = 8192 rows per tile
+constexpr int CT_SEGS = 32;       // segments per tile
+constexpr int CT_SEG_BLOCKS = 8;  // 16-row blocks per segment
+constexpr int CT_BLOCKS = CT_SEGS * CT_SEG_BLOCKS;  // 256 blocks = 4096 rows per tile
 constexpr unsigned long long MANT = 0xfffffffffffffull;
 constexpr unsigned long long ONE52 = 1ull << 52;
 constexpr unsigned long long SAT = 1ull << 60;
@@ -163,15 +163,6 @@ __device__ __forceinline__ int binade(double v) {
     return static_cast<int>(as_bits(v) >> 52) - 1023;
 }
 
-// Lookback records of one launch, in the context scratch arena.
-struct CanonScratch {
-    unsigned *flag1;           // approx: epoch<<2 | 1 aggregate, 2 inclusive
-    unsigned *flag2;           // exact
-    double *agg1, *inc1;       // [tiles][16]
-    unsigned long long *agg2;  // [tiles][16][3]: E+1024 (0 = invalid), d0, d1
-    unsigned long long *inc2;  // [tiles][16] lane state bits
-};
-
 // Reducer state on the device.
 struct CanonState {
     unsigned long long lanes[16];
@@ -179,31 +170,29 @@ struct CanonState {
     unsigned long long result;
 };
 
+// Per-launch work arrays, in the context scratch arena. T = number of 4096-row tiles.
+struct CanonWork {
+    float *apx;                // [T][16] approximate lane sums of each tile
+    int *cand;                 // [T][16][2] candidate binades (NO_E when absent)
+    int *recE;                 // [16][T][2] binade of each tile transfer function (NO_E: none)
+    TF *recD;                  // [16][T][2]
+    int *chunkE;               // [16][C] binade of each 32-tile chunk's transfer function
+    TF *chunkD;                // [16][C]
+};
+
+__device__ __forceinline__ TF shfl_tf(TF v, int src) {
+    return TF{__shfl_sync(FULL, v.d0, src), __shfl_sync(FULL, v.d1, src)};
+}
+__device__ __forceinline__ TF shfl_up_tf(TF v, int o) {
+    return TF{__shfl_up_sync(FULL, v.d0, o), __shfl_up_sync(FULL, v.d1, o)};
+}
+
+// Loads the thread's 8 blocks x 2 lanes of tile `tile` and computes the row values. Rows past
+// the last block read as +0.0, which leaves every lane state unchanged (a lane is never -0).
 template <int OP, bool ALIGNED>
-__global__ void __launch_bounds__(CT_THREADS, 2)
-canon_kernel(RowArgs args, int64_t nb, int tiles, CanonScratch sc, unsigned epoch,
-             CanonState *state, unsigned *counters, DevStatus *status) {
-    extern __shared__ unsigned long long s_vals[];  // [512 blocks][16 lanes], staged on demand
-    __shared__ float s_apx[CT_SEGS][16];
-    __shared__ int s_E[16][2];
-    __shared__ TF s_tf[2][CT_SEGS][16];
-    __shared__ unsigned char s_ok[2][CT_SEGS][16];
-    __shared__ unsigned long long s_start[16];
-    __shared__ int s_stage;
-    __shared__ unsigned s_tile;
-
-    const int t = threadIdx.x;
-    const int lp = t & 7, seg = t >> 3;
-    if (t == 0) {
-        s_tile = atomicAdd(&counters[0], 1u);
-        s_stage = 0;
-    }
-    __syncthreads();
-    const int tile = static_cast<int>(s_tile);
+__device__ __forceinline__ void load_tile(const RowArgs &args, int64_t nb, int tile, int lp, int seg,
+                                          unsigned long long (&v)[CT_SEG_BLOCKS][2]) {
     const int64_t blk0 = static_cast<int64_t>(tile) * CT_BLOCKS;
-
-    // 1. Load the segment's rows (two lanes per thread) and compute the row values.
-    unsigned long long v[CT_SEG_BLOCKS][2];
 #pragma unroll
     for (int i = 0; i < CT_SEG_BLOCKS; ++i) {
         int64_t b = blk0 + seg * CT_SEG_BLOCKS + i;
@@ -230,216 +219,275 @@ canon_kernel(RowArgs args, int64_t nb, int tiles, CanonScratch sc, unsigned epoc
             v[i][0] = row_value<OP>(args, x0, y0);
             v[i][1] = row_value<OP>(args, x1, y1);
         } else {
-            // Past the last block: +0.0 leaves every lane state unchanged (a lane is never -0).
             v[i][0] = 0;
             v[i][1] = 0;
         }
     }
+}
 
-    // 2. Approximate lane sums of the tile.
-    {
-        float a0 = 0.f, a1 = 0.f;
+// K1: the approximate lane sums of every tile (float sums of float images, one read).
+template <int OP, bool ALIGNED>
+__global__ void __launch_bounds__(CT_THREADS) canon_apx_kernel(RowArgs args, int64_t nb, CanonWork wk) {
+    __shared__ float s_apx[CT_SEGS][16];
+    const int t = threadIdx.x, lp = t & 7, seg = t >> 3;
+    const int tile = blockIdx.x;
+    unsigned long long v[CT_SEG_BLOCKS][2];
+    load_tile<OP, ALIGNED>(args, nb, tile, lp, seg, v);
+    float a0 = 0.f, a1 = 0.f;
 #pragma unroll
-        for (int i = 0; i < CT_SEG_BLOCKS; ++i) {
-            a0 += approx_f32(v[i][0]);
-            a1 += approx_f32(v[i][1]);
-        }
-        s_apx[seg][2 * lp] = a0;
-        s_apx[seg][2 * lp + 1] = a1;
+    for (int i = 0; i < CT_SEG_BLOCKS; ++i) {
+        a0 += approx_f32(v[i][0]);
+        a1 += approx_f32(v[i][1]);
     }
+    s_apx[seg][2 * lp] = a0;
+    s_apx[seg][2 * lp + 1] = a1;
     __syncthreads();
-
-    // 3. Lookback 1 (approximate prefix), one thread per lane in warp 0.
     if (t < 16) {
-        double A = 0;
-        for (int s = 0; s < CT_SEGS; ++s) A += static_cast<double>(s_apx[s][t]);
-        sc.agg1[tile * 16 + t] = A;
-        __threadfence();
-        __syncwarp(0xffffu);
-        if (t == 0) st_release(&sc.flag1[tile], (epoch << 2) | 1u);
-        double excl = 0;
-        bool found = false;
-        for (int tp = tile - 1; tp >= 0 && !found; --tp) {
-            unsigned f = 0, it = 0;
-            while (((f = ld_acquire(&sc.flag1[tp])) >> 2) != epoch) {
-                if (++it > SPIN_LIMIT) {
-                    set_timeout(status);
-                    found = true;
-                    break;
-                }
-                backoff(it);
-            }
-            if (found) break;
-            if ((f & 3u) == 2u) {
-                excl += sc.inc1[tp * 16 + t];
-                found = true;
-            } else {
-                excl += sc.agg1[tp * 16 + t];
-            }
-        }
-        if (!found) excl += as_f64(state->lanes[t]);
-        sc.inc1[tile * 16 + t] = excl + A;
-        __threadfence();
-        __syncwarp(0xffffu);
-        if (t == 0) st_release(&sc.flag1[tile], (epoch << 2) | 2u);
-        // Candidate binades: the range [start, end] widened by 2^-12 on each side.
-        double lo = excl < excl + A ? excl : excl + A;
-        double hi = excl < excl + A ? excl + A : excl;
-        int elo = binade(lo * (1.0 - 0x1p-12)), ehi = binade(hi * (1.0 + 0x1p-12));
-        int e0 = NO_E, e1 = NO_E;
-        if (elo != NO_E && ehi != NO_E && elo >= -959) {
-            if (ehi == elo) e0 = elo;
-            else if (ehi == elo + 1) {
-                e0 = elo;
-                e1 = ehi;
-            }
-        }
-        s_E[t][0] = e0;
-        s_E[t][1] = e1;
+        float A = 0.f;
+        for (int s = 0; s < CT_SEGS; ++s) A += s_apx[s][t];
+        wk.apx[tile * 16 + t] = A;
     }
-    __syncthreads();
+}
 
-    // 4. Segment transfer functions for each candidate binade.
+// K2: per lane (one block each), the exclusive prefix of the approximate sums over tiles,
+// from the lane's exact state, and each tile's candidate binades: the range [start, end]
+// widened by 2^-12 on each side must lie in one binade or two adjacent ones.
+__global__ void __launch_bounds__(1024) canon_cand_kernel(int T, CanonWork wk, const CanonState *state) {
+    __shared__ double s_tot[1024];
+    const int L = blockIdx.x, t = threadIdx.x;
+    const int per = (T + 1023) / 1024;
+    const int t0 = t * per, t1 = min(T, t0 + per);
+    double sum = 0;
+    for (int k = t0; k < t1; ++k) sum += static_cast<double>(wk.apx[k * 16 + L]);
+    s_tot[t] = sum;
+    __syncthreads();
+    // Block exclusive scan of the thread sums (Hillis-Steele over shared memory).
+    for (int o = 1; o < 1024; o <<= 1) {
+        double add = t >= o ? s_tot[t - o] : 0.0;
+        __syncthreads();
+        s_tot[t] += add;
+        __syncthreads();
+    }
+    double pre = (t ? s_tot[t - 1] : 0.0) + as_f64(state->lanes[L]);
+    for (int k = t0; k < t1; ++k) {
+        double A = static_cast<double>(wk.apx[k * 16 + L]);
+        double lo = A < 0 ? pre + A : pre, hi = A < 0 ? pre : pre + A;
+        int elo = binade(lo * (1.0 - 0x1p-12)), ehi = binade(hi * (1.0 + 0x1p-12));
+        int c0 = NO_E, c1 = NO_E;
+        if (elo != NO_E && ehi != NO_E && elo >= -959) {
+            if (ehi == elo) c0 = elo;
+            else if (ehi == elo + 1) {
+                c0 = elo;
+                c1 = ehi;
+            }
+        }
+        wk.cand[(k * 16 + L) * 2] = c0;
+        wk.cand[(k * 16 + L) * 2 + 1] = c1;
+        pre += A;
+    }
+}
+
+// K3: each tile's transfer function per lane and candidate binade (NO_E when a segment does
+// not take the integer step in that binade).
+template <int OP, bool ALIGNED>
+__global__ void __launch_bounds__(CT_THREADS) canon_tf_kernel(RowArgs args, int64_t nb, int T, CanonWork wk) {
+    __shared__ TF s_tf[2][CT_SEGS][16];
+    __shared__ unsigned char s_ok[2][CT_SEGS][16];
+    __shared__ int s_E[16][2];
+    const int t = threadIdx.x, lp = t & 7, seg = t >> 3;
+    const int tile = blockIdx.x;
+    if (t < 32) (&s_E[0][0])[t] = wk.cand[tile * 32 + t];
+    unsigned long long v[CT_SEG_BLOCKS][2];
+    load_tile<OP, ALIGNED>(args, nb, tile, lp, seg, v);
+    __syncthreads();
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
-        const int lane = 2 * lp + h;
+        const int L = 2 * lp + h;
         for (int c = 0; c < 2; ++c) {
-            int E = s_E[lane][c];
+            int E = s_E[L][c];
             TF f{0, 0};
             bool ok = E != NO_E && seg_tf(v, h, 1023 + E, &f);
-            s_tf[c][seg][lane] = f;
-            s_ok[c][seg][lane] = ok;
+            s_tf[c][seg][L] = f;
+            s_ok[c][seg][L] = ok;
         }
     }
     __syncthreads();
-
-    // 5. Publish the tile's transfer function per lane (single-binade lanes only), then
-    //    lookback 2 for the exact start state.
-    TF tile_tf{0, 0};
-    int tile_E = NO_E;
-    if (t < 16) {
-        if (s_E[t][0] != NO_E && s_E[t][1] == NO_E) {
-            bool ok = true;
-            for (int s = 0; s < CT_SEGS; ++s) {
-                ok = ok && s_ok[0][s][t];
-                tile_tf = compose(tile_tf, s_tf[0][s][t]);
-            }
-            if (ok) tile_E = s_E[t][0];
+    if (t < 32) {
+        const int L = t >> 1, c = t & 1;
+        int E = s_E[L][c];
+        TF f{0, 0};
+        bool ok = E != NO_E;
+        for (int s = 0; s < CT_SEGS && ok; ++s) {
+            ok = s_ok[c][s][L];
+            f = compose(f, s_tf[c][s][L]);
         }
-        unsigned long long *rec = sc.agg2 + (static_cast<int64_t>(tile) * 16 + t) * 3;
-        rec[0] = tile_E == NO_E ? 0ull : static_cast<unsigned long long>(tile_E + 1024);
-        rec[1] = tile_tf.d0;
-        rec[2] = tile_tf.d1;
-        __threadfence();
-        __syncwarp(0xffffu);
-        if (t == 0) st_release(&sc.flag2[tile], (epoch << 2) | 1u);
-
-        // Walk back over aggregates of one binade to the nearest exact state.
-        TF acc{0, 0};
-        int accE = NO_E;
-        bool have_acc = false, done = false, timed_out = false;
-        unsigned long long base = 0, start = 0;
-        for (int tp = tile - 1; tp >= 0 && !done; --tp) {
-            unsigned f = 0, it = 0;
-            for (;;) {
-                f = ld_acquire(&sc.flag2[tp]);
-                if ((f >> 2) == epoch) {
-                    if ((f & 3u) == 2u) break;
-                    const unsigned long long *r = sc.agg2 + (static_cast<int64_t>(tp) * 16 + t) * 3;
-                    int e = r[0] ? static_cast<int>(r[0]) - 1024 : NO_E;
-                    if (e != NO_E && (!have_acc || e == accE)) break;
-                }
-                // An unusable aggregate: wait for that tile's exact state.
-                if (++it > SPIN_LIMIT) {
-                    set_timeout(status);
-                    timed_out = true;
-                    break;
-                }
-                backoff(it);
-            }
-            if (timed_out) break;
-            if ((f & 3u) == 2u) {
-                base = sc.inc2[tp * 16 + t];
-                done = true;
-            } else {
-                const unsigned long long *r = sc.agg2 + (static_cast<int64_t>(tp) * 16 + t) * 3;
-                TF g{r[1], r[2]};
-                accE = static_cast<int>(r[0]) - 1024;
-                acc = have_acc ? compose(g, acc) : g;
-                have_acc = true;
-            }
-        }
-        if (!done) base = state->lanes[t];
-        start = base;
-        if (have_acc && !timed_out && !apply(base, accE, acc, &start)) {
-            // The composed aggregates do not hold from that state: wait for the previous
-            // tile's exact state.
-            unsigned f = 0, it = 0;
-            while ((((f = ld_acquire(&sc.flag2[tile - 1])) >> 2) != epoch) || (f & 3u) != 2u) {
-                if (++it > SPIN_LIMIT) {
-                    set_timeout(status);
-                    break;
-                }
-                backoff(it);
-            }
-            start = sc.inc2[(tile - 1) * 16 + t];
-        }
-        s_start[t] = start;
-        // Stage the rows when the tile's own transfer function does not carry the lane.
-        unsigned long long end;
-        if (!(tile_E != NO_E && apply(start, tile_E, tile_tf, &end))) s_stage = 1;
+        const int64_t at = (static_cast<int64_t>(L) * T + tile) * 2 + c;
+        wk.recE[at] = ok ? E : NO_E;
+        wk.recD[at] = f;
     }
-    __syncthreads();
-    if (s_stage) {
+}
+
+// The transfer function of tile `tp` for lane L in binade E, if it has one.
+__device__ __forceinline__ bool tile_tf(const CanonWork &wk, int T, int L, int tp, int E, TF *f) {
+    const int64_t at = (static_cast<int64_t>(L) * T + tp) * 2;
+    if (E == NO_E) return false;
+    if (wk.recE[at] == E) {
+        *f = wk.recD[at];
+        return true;
+    }
+    if (wk.recE[at + 1] == E) {
+        *f = wk.recD[at + 1];
+        return true;
+    }
+    return false;
+}
+
+// K4a: per lane and 32-tile chunk (one warp each), the composed transfer function when every
+// tile of the chunk has one in the same binade (the binade of candidate 0 of the chunk's
+// first tile).
+__global__ void __launch_bounds__(256) canon_chunk_kernel(int T, int C, CanonWork wk) {
+    const int lane = threadIdx.x & 31;
+    const int64_t gw = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    if (gw >= static_cast<int64_t>(16) * C) return;
+    const int L = static_cast<int>(gw / C), k = static_cast<int>(gw % C);
+    const int tp = k * 32 + lane;
+    const int E = __shfl_sync(FULL, tp < T ? wk.recE[(static_cast<int64_t>(L) * T + tp) * 2] : NO_E, 0);
+    TF f{0, 0};
+    bool ok = tp >= T || tile_tf(wk, T, L, tp, E, &f);
+    if (!__all_sync(FULL, ok) || E == NO_E) {
+        if (lane == 0) wk.chunkE[static_cast<int64_t>(L) * C + k] = NO_E;
+        return;
+    }
+    // Ordered composition: lane i holds tile 32k + i, the lower lane is the earlier tile.
 #pragma unroll
-        for (int i = 0; i < CT_SEG_BLOCKS; ++i)
-            *reinterpret_cast<ulonglong2 *>(&s_vals[(seg * CT_SEG_BLOCKS + i) * 16 + 2 * lp]) =
-                make_ulonglong2(v[i][0], v[i][1]);
+    for (int o = 1; o < 32; o <<= 1) {
+        TF other = TF{__shfl_down_sync(FULL, f.d0, o), __shfl_down_sync(FULL, f.d1, o)};
+        if (lane + o < 32) f = compose(f, other);
     }
-    __syncthreads();
+    if (lane == 0) {
+        wk.chunkE[static_cast<int64_t>(L) * C + k] = E;
+        wk.chunkD[static_cast<int64_t>(L) * C + k] = f;
+    }
+}
 
-    // 6. Walk the lane's segments from the exact start.
-    if (t < 16) {
-        unsigned long long s = s_start[t], end;
-        if (tile_E != NO_E && apply(s, tile_E, tile_tf, &end)) {
-            s = end;
+__device__ __forceinline__ int state_binade(unsigned long long s) {
+    unsigned long long e = s >> 52;  // sign bit included: a negative state has none
+    return (e >= 1 && e <= 2046) ? static_cast<int>(e) - 1023 : NO_E;
+}
+
+// Inclusive ordered prefix composition over the warp (lane 0 first), then the number of
+// leading lanes whose prefix applies to state s (usable and inside the binade). Returns that
+// count and, in *out, the state after them.
+__device__ __forceinline__ int apply_prefix(TF f, bool usable, unsigned long long s, int E,
+                                            unsigned long long *out) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        TF y = shfl_up_tf(f, o);
+        if (lane >= o) f = compose(y, f);
+    }
+    unsigned long long r = 0;
+    const bool ok = usable && apply(s, E, f, &r);
+    const unsigned bad = __ballot_sync(FULL, !ok);
+    const int m = bad ? __ffs(bad) - 1 : 32;
+    if (m > 0) *out = __shfl_sync(FULL, r, m - 1);
+    return m;
+}
+
+// Resolves tile `tp` for lane L from the state s: the warp recomputes the tile's 32 segment
+// transfer functions from the rows (lane j = segment j) for the state's binade and the next,
+// applies them in order, and adds the rows of any segment they do not carry one by one.
+template <int OP>
+__device__ unsigned long long resolve_tile(const RowArgs &args, int64_t nb, int tp, int L, unsigned long long s) {
+    const int lane = threadIdx.x & 31;
+    unsigned long long v[CT_SEG_BLOCKS][2];
+    const int64_t blk0 = static_cast<int64_t>(tp) * CT_BLOCKS + lane * CT_SEG_BLOCKS;
+#pragma unroll
+    for (int i = 0; i < CT_SEG_BLOCKS; ++i) {
+        int64_t b = blk0 + i;
+        unsigned long long xv = 0, yv = 0;
+        if (b < nb) {
+            xv = args.x[b * 16 + L];
+            if (OP == ROW_DOT) yv = args.y[b * 16 + L];
+            v[i][0] = row_value<OP>(args, xv, yv);
         } else {
-            for (int sg = 0; sg < CT_SEGS; ++sg) {
-                bool ok = false;
-                for (int c = 0; c < 2 && !ok; ++c)
-                    if (s_E[t][c] != NO_E && s_ok[c][sg][t])
-                        ok = apply(s, s_E[t][c], s_tf[c][sg][t], &s);
-                if (!ok) {
-                    double d = as_f64(s);
-                    for (int i = 0; i < CT_SEG_BLOCKS; ++i)
-                        d = __dadd_rn(d, as_f64(s_vals[(sg * CT_SEG_BLOCKS + i) * 16 + t]));
-                    s = as_bits(d);
-                }
+            v[i][0] = 0;
+        }
+        v[i][1] = 0;
+    }
+    int seg = 0;
+    while (seg < CT_SEGS) {
+        const int E = state_binade(s);
+        if (E != NO_E && E >= -959) {
+            TF f{0, 0};
+            bool ok = lane >= seg && seg_tf(v, 0, 1023 + E, &f);
+            if (lane < seg) {
+                f = TF{0, 0};
+                ok = true;  // already consumed: identity
+            }
+            unsigned long long r = s;
+            int m = apply_prefix(f, ok, s, E, &r);
+            if (m > seg) {
+                s = r;
+                seg = m;
+                continue;
             }
         }
-        sc.inc2[tile * 16 + t] = s;
-        __threadfence();
-        __syncwarp(0xffffu);
-        if (t == 0) st_release(&sc.flag2[tile], (epoch << 2) | 2u);
-    }
-
-    // The block that finishes last stores the end states (no block reads the start states
-    // any more) and resets the ticket for the next launch.
-    __shared__ int s_last;
-    if (t == 0) {
-        __threadfence();
-        unsigned prev = atomicAdd(&counters[1], 1u);
-        s_last = prev == static_cast<unsigned>(tiles) - 1;
-    }
-    __syncthreads();
-    if (s_last) {
-        __threadfence();
-        if (t < 16) state->lanes[t] = ld_relaxed64(&sc.inc2[(tiles - 1) * 16 + t]);
-        if (t == 0) {
-            counters[0] = 0;
-            counters[1] = 0;
+        // Segment `seg` is not carried: its owner adds its rows one by one.
+        unsigned long long r = 0;
+        if (lane == seg) {
+            double d = as_f64(s);
+#pragma unroll
+            for (int i = 0; i < CT_SEG_BLOCKS; ++i) d = __dadd_rn(d, as_f64(v[i][0]));
+            r = as_bits(d);
         }
+        s = __shfl_sync(FULL, r, seg);
+        ++seg;
     }
+    return s;
+}
+
+// K4b: one warp per lane walks the tiles from the lane's exact state: whole 32-tile chunks
+// while their transfer function holds, then single tiles, and resolves the tiles that none
+// carries (binade crossings, negative or special rows, the first rows of the lane).
+template <int OP>
+__global__ void __launch_bounds__(512) canon_walk_kernel(RowArgs args, int64_t nb, int T, int C, CanonWork wk,
+                                                         CanonState *state) {
+    const int lane = threadIdx.x & 31, L = threadIdx.x >> 5;
+    unsigned long long s = state->lanes[L];
+    int k = 0;  // next chunk
+    while (k < C) {
+        // Whole chunks k .. k+31.
+        const int E = state_binade(s);
+        const int kc = k + lane;
+        int ce = kc < C ? wk.chunkE[static_cast<int64_t>(L) * C + kc] : NO_E;
+        TF f = (ce != NO_E && ce == E) ? wk.chunkD[static_cast<int64_t>(L) * C + kc] : TF{0, 0};
+        unsigned long long r = s;
+        int m = E == NO_E ? 0 : apply_prefix(f, kc < C && ce != NO_E && ce == E, s, E, &r);
+        if (m > 0) {
+            s = r;
+            k += m;
+            continue;
+        }
+        // Chunk k, tile by tile.
+        int tp = k * 32, end = min(T, tp + 32);
+        while (tp < end) {
+            const int Et = state_binade(s);
+            const int tl = tp + lane;
+            TF g{0, 0};
+            bool usable = tl < end && tile_tf(wk, T, L, tl, Et, &g);
+            int mt = Et == NO_E ? 0 : apply_prefix(g, usable, s, Et, &r);
+            if (mt > 0) {
+                s = r;
+                tp += mt;
+            } else {
+                s = resolve_tile<OP>(args, nb, tp, L, s);
+                ++tp;
+            }
+        }
+        ++k;
+    }
+    if (lane == 0) state->lanes[L] = s;
 }
 
 // Stores the row values of the rest rows (fewer than 16) as the pending tail.
@@ -464,17 +512,20 @@ __global__ void canon_finish(CanonState *state, int tail_len) {
 }
 
 template <int OP, bool ALIGNED>
-static void launch_canon(vkc_ctx *ctx, const RowArgs &a, int64_t nb, int tiles, CanonScratch sc,
-                         unsigned epoch, CanonState *state) {
-    const size_t smem = sizeof(unsigned long long) * CT_BLOCKS * 16;
-    static bool configured = false;
-    if (!configured) {
-        cudaFuncSetAttribute(canon_kernel<OP, ALIGNED>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             static_cast<int>(smem));
-        configured = true;
-    }
-    canon_kernel<OP, ALIGNED><<<tiles, CT_THREADS, smem, ctx->stream>>>(a, nb, tiles, sc, epoch, state,
-                                                                       ctx->counters, ctx->status);
+static vkc_status launch_canon(vkc_ctx *ctx, const RowArgs &a, int64_t nb, int T, int C, const CanonWork &wk,
+                               CanonState *state) {
+    vkc_status st;
+    canon_apx_kernel<OP, ALIGNED><<<T, CT_THREADS, 0, ctx->stream>>>(a, nb, wk);
+    if ((st = launched(ctx, "canon_apx"))) return st;
+    canon_cand_kernel<<<16, 1024, 0, ctx->stream>>>(T, wk, state);
+    if ((st = launched(ctx, "canon_cand"))) return st;
+    canon_tf_kernel<OP, ALIGNED><<<T, CT_THREADS, 0, ctx->stream>>>(a, nb, T, wk);
+    if ((st = launched(ctx, "canon_tf"))) return st;
+    int warps = 16 * C;
+    canon_chunk_kernel<<<(warps + 7) / 8, 256, 0, ctx->stream>>>(T, C, wk);
+    if ((st = launched(ctx, "canon_chunk"))) return st;
+    canon_walk_kernel<OP><<<1, 512, 0, ctx->stream>>>(a, nb, T, C, wk, state);
+    return launched(ctx, "canon_walk");
 }
 
 // The canonical reducer of one row operation.
@@ -486,7 +537,6 @@ struct CanonReducer : DevReducer {
     vkc_status update(vkc_ctx *ctx, const Arg *args, int nargs) override {
         vkc_status st;
         RowArgs a{};
-        int64_t n = 0;
         // Argument checks in the order of each reducer's update (fused.rs:77-203, reduce.rs:612-617).
         switch (op) {
         case ROW_SUM:
@@ -512,49 +562,41 @@ struct CanonReducer : DevReducer {
             break;
         }
         a.x = args[0].ptr<unsigned long long>();
-        n = args[0].len();
+        const int64_t n = args[0].len();
         // reduce.rs:297-303: rows may only follow whole blocks.
         if (tail_len != 0) return fail(ctx, VKC_RUNTIME, "canonical update after a partial block");
-        int64_t nb = n / 16;
-        int rest = static_cast<int>(n % 16);
+        const int64_t nb = n / 16;
+        const int rest = static_cast<int>(n % 16);
         auto *cs = static_cast<CanonState *>(state);
         if (nb > 0) {
-            int64_t tiles64 = (nb + CT_BLOCKS - 1) / CT_BLOCKS;
-            if (tiles64 > INT_MAX / 2) return fail(ctx, VKC_USAGE, "array too long for one update");
-            int tiles = static_cast<int>(tiles64);
-            size_t t16 = static_cast<size_t>(tiles) * 16;
-            size_t off_inc1 = t16 * 8;
-            size_t off_agg2 = off_inc1 + t16 * 8;
-            size_t off_inc2 = off_agg2 + t16 * 24;
-            size_t total = off_inc2 + t16 * 8;
+            const int64_t T64 = (nb + CT_BLOCKS - 1) / CT_BLOCKS;
+            if (T64 > (int64_t(1) << 26)) return fail(ctx, VKC_USAGE, "array too long for one update");
+            const int T = static_cast<int>(T64), C = (T + 31) / 32;
+            const size_t t16 = static_cast<size_t>(T) * 16, c16 = static_cast<size_t>(C) * 16;
+            const size_t o_cand = (t16 * 4 + 255) & ~size_t(255);
+            const size_t o_recE = o_cand + ((t16 * 8 + 255) & ~size_t(255));
+            const size_t o_recD = o_recE + ((t16 * 8 + 255) & ~size_t(255));
+            const size_t o_chE = o_recD + t16 * 2 * sizeof(TF);
+            const size_t o_chD = o_chE + ((c16 * 4 + 255) & ~size_t(255));
+            const size_t total = o_chD + c16 * sizeof(TF);
             void *p;
-            unsigned *flags;
             if ((st = scratch(ctx, total, &p))) return st;
-            if ((st = flag_arena(ctx, static_cast<size_t>(tiles) * 2, &flags))) return st;
-            char *base = static_cast<char *>(p);
-            CanonScratch sc{flags, flags + tiles,
-                            reinterpret_cast<double *>(base), reinterpret_cast<double *>(base + off_inc1),
-                            reinterpret_cast<unsigned long long *>(base + off_agg2),
-                            reinterpret_cast<unsigned long long *>(base + off_inc2)};
-            unsigned epoch = next_epoch(ctx);
-            bool aligned = (reinterpret_cast<uintptr_t>(a.x) & 15) == 0 &&
-                           (op != ROW_DOT || (reinterpret_cast<uintptr_t>(a.y) & 15) == 0);
-#define CANON_CASE(OPV)                                                              \
-    case OPV:                                                                        \
-        if (aligned) launch_canon<OPV, true>(ctx, a, nb, tiles, sc, epoch, cs);      \
-        else launch_canon<OPV, false>(ctx, a, nb, tiles, sc, epoch, cs);             \
-        break;
+            char *b = static_cast<char *>(p);
+            CanonWork wk{reinterpret_cast<float *>(b), reinterpret_cast<int *>(b + o_cand),
+                         reinterpret_cast<int *>(b + o_recE), reinterpret_cast<TF *>(b + o_recD),
+                         reinterpret_cast<int *>(b + o_chE), reinterpret_cast<TF *>(b + o_chD)};
+            const bool aligned = (reinterpret_cast<uintptr_t>(a.x) & 15) == 0 &&
+                                 (op != ROW_DOT || (reinterpret_cast<uintptr_t>(a.y) & 15) == 0);
             switch (op) {
-                CANON_CASE(ROW_SUM)
-                CANON_CASE(ROW_DOT)
-                CANON_CASE(ROW_SUMSQ)
-                CANON_CASE(ROW_CONDSUM)
+            case ROW_SUM: st = aligned ? launch_canon<ROW_SUM, true>(ctx, a, nb, T, C, wk, cs) : launch_canon<ROW_SUM, false>(ctx, a, nb, T, C, wk, cs); break;
+            case ROW_DOT: st = aligned ? launch_canon<ROW_DOT, true>(ctx, a, nb, T, C, wk, cs) : launch_canon<ROW_DOT, false>(ctx, a, nb, T, C, wk, cs); break;
+            case ROW_SUMSQ: st = aligned ? launch_canon<ROW_SUMSQ, true>(ctx, a, nb, T, C, wk, cs) : launch_canon<ROW_SUMSQ, false>(ctx, a, nb, T, C, wk, cs); break;
+            default: st = aligned ? launch_canon<ROW_CONDSUM, true>(ctx, a, nb, T, C, wk, cs) : launch_canon<ROW_CONDSUM, false>(ctx, a, nb, T, C, wk, cs); break;
             }
-#undef CANON_CASE
-            if ((st = launched(ctx, "canon"))) return st;
+            if (st) return st;
         }
         if (rest > 0) {
-            int64_t first = nb * 16;
+            const int64_t first = nb * 16;
             switch (op) {
             case ROW_SUM: canon_tail<ROW_SUM><<<1, 16, 0, ctx->stream>>>(a, first, rest, cs); break;
             case ROW_DOT: canon_tail<ROW_DOT><<<1, 16, 0, ctx->stream>>>(a, first, rest, cs); break;
@@ -572,8 +614,6 @@ struct CanonReducer : DevReducer {
         canon_finish<<<1, 1, 0, ctx->stream>>>(cs, tail_len);
         vkc_status st = launched(ctx, "canon_finish");
         if (st) return st;
-        DevStatus ds;
-        if ((st = read_status(ctx, &ds))) return st;
         out->type = VKC_F64;
         return download(ctx, &out->bits, 8, offsetof(CanonState, result));
     }

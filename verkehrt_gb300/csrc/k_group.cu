@@ -115,9 +115,10 @@ __global__ void __launch_bounds__(GI_THREADS) gi_number_kernel(const unsigned *_
     }
     unsigned long long c = __popc(keep), tile_count;
     unsigned long long off = block_exclusive_sum<unsigned long long>(c, &tile_count);
-    if (threadIdx.x == 0) {
+    if (threadIdx.x < 32) {
         auto add = [](unsigned long long p, unsigned long long q) { return p + q; };
-        s_prefix = lookback_exclusive<unsigned long long>(lb, tile, tile_count, 0ull, epoch, add, st);
+        unsigned long long pre = warp_lookback<unsigned long long>(lb, tile, tile_count, 0ull, 0ull, epoch, add, st);
+        if (threadIdx.x == 0) s_prefix = pre;
     }
     __syncthreads();
     unsigned r = static_cast<unsigned>(s_prefix + off);

@@ -32,10 +32,28 @@ __global__ void __launch_bounds__(256) gather_kernel(const typename GWord<W>::T 
     if (head && tid == 0) one(0, idx[0]);
     const longlong2 *i2 = reinterpret_cast<const longlong2 *>(idx + head);
     int64_t n2 = (n - head) >> 1;
-    for (int64_t p = tid; p < n2; p += stride) {
-        longlong2 k = __ldcs(i2 + p);
-        one(head + 2 * p, k.x);
-        one(head + 2 * p + 1, k.y);
+    // Eight random source loads per thread in flight: the index loads of four strides first,
+    // then every gather load, then the stores.
+    for (int64_t p = tid; p < n2; p += 4 * stride) {
+        longlong2 k[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) k[u] = p + u * stride < n2 ? __ldcs(i2 + p + u * stride) : make_longlong2(-1, -1);
+        typename GWord<W>::T g[4][2];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            g[u][0] = static_cast<uint64_t>(k[u].x) < nsrc ? __ldg(src + k[u].x) : 0;
+            g[u][1] = static_cast<uint64_t>(k[u].y) < nsrc ? __ldg(src + k[u].y) : 0;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            int64_t q = p + u * stride;
+            if (q >= n2) break;
+            int64_t i = head + 2 * q;
+            if (static_cast<uint64_t>(k[u].x) < nsrc) out[i] = g[u][0];
+            else if (static_cast<unsigned long long>(i) < bad) bad = static_cast<unsigned long long>(i);
+            if (static_cast<uint64_t>(k[u].y) < nsrc) out[i + 1] = g[u][1];
+            else if (static_cast<unsigned long long>(i + 1) < bad) bad = static_cast<unsigned long long>(i + 1);
+        }
     }
     if (((n - head) & 1) && tid == 0) one(n - 1, idx[n - 1]);
     if (bad != ~0ull) atomicMin(&status->first_bad, bad);

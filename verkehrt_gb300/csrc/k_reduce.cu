@@ -89,10 +89,15 @@ __global__ void __launch_bounds__(256) count_kernel(const void *__restrict__ xv,
         if (head && tid == 0) c += in_range(r, x[0]);
         const ulonglong2 *x2 = reinterpret_cast<const ulonglong2 *>(x + head);
         int64_t n2 = (n - head) >> 1;
-        for (int64_t i = tid; i < n2; i += stride) {
-            ulonglong2 v = __ldcs(&x2[i]);
-            c += in_range(r, v.x);
-            c += in_range(r, v.y);
+        // Four independent 16-byte loads per thread in flight.
+        for (int64_t i = tid; i < n2; i += 4 * stride) {
+            ulonglong2 v[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                v[u] = i + u * stride < n2 ? __ldcs(&x2[i + u * stride]) : make_ulonglong2(~0ull, ~0ull);
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                if (i + u * stride < n2) c += in_range(r, v[u].x) + in_range(r, v[u].y);
         }
         if (((n - head) & 1) && tid == 0) c += in_range(r, x[n - 1]);
     }
@@ -197,10 +202,19 @@ __global__ void __launch_bounds__(256) extreme_kernel(const long long *__restric
     if (head && tid == 0) visit(x[0], 0);
     const longlong2 *x2 = reinterpret_cast<const longlong2 *>(x + head);
     int64_t n2 = (n - head) >> 1;
-    for (int64_t i = tid; i < n2; i += stride) {
-        longlong2 v = __ldcs(&x2[i]);
-        visit(v.x, head + 2 * i);
-        visit(v.y, head + 2 * i + 1);
+    // Four independent 16-byte loads per thread in flight; rows of a thread still arrive in
+    // increasing order, which the first-index tie rule relies on.
+    for (int64_t i = tid; i < n2; i += 4 * stride) {
+        longlong2 v[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+            if (i + u * stride < n2) v[u] = __ldcs(&x2[i + u * stride]);
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+            if (i + u * stride < n2) {
+                visit(v[u].x, head + 2 * (i + u * stride));
+                visit(v[u].y, head + 2 * (i + u * stride) + 1);
+            }
     }
     if (((n - head) & 1) && tid == 0) visit(x[n - 1], n - 1);
     // Warp, then block.
@@ -301,9 +315,12 @@ __global__ void __launch_bounds__(256) isum_kernel(const unsigned long long *__r
     if (head && tid == 0) c += x[0];
     const ulonglong2 *x2 = reinterpret_cast<const ulonglong2 *>(x + head);
     int64_t n2 = (n - head) >> 1;
-    for (int64_t i = tid; i < n2; i += stride) {
-        ulonglong2 v = __ldcs(&x2[i]);
-        c += v.x + v.y;
+    for (int64_t i = tid; i < n2; i += 4 * stride) {
+        ulonglong2 v[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) v[u] = i + u * stride < n2 ? __ldcs(&x2[i + u * stride]) : make_ulonglong2(0, 0);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) c += v[u].x + v[u].y;
     }
     if (((n - head) & 1) && tid == 0) c += x[n - 1];
     c = warp_sum(c);

@@ -33,6 +33,18 @@ struct ScanState {
     unsigned long long seen;
 };
 
+__device__ __forceinline__ Seg shfl_down_v(Seg v, int o) {
+    return Seg{__shfl_down_sync(FULL, v.sum, o), __shfl_down_sync(FULL, v.start, o)};
+}
+__device__ __forceinline__ Seg __shfl_sync_v(Seg v, int src) {
+    return Seg{__shfl_sync(FULL, v.sum, src), __shfl_sync(FULL, v.start, src)};
+}
+
+// Per warp, 4 rows of 128 consecutive rows of the input: lane l holds rows 4l..4l+3 of each
+// (one 32-byte load), so loads and stores are coalesced and row order is (row, lane, item).
+constexpr int SC_VEC = 4;
+constexpr int SC_ROWS = SC_ITEMS / SC_VEC;
+
 template <bool BY, bool ALIGNED>
 __global__ void __launch_bounds__(SC_THREADS) scan_kernel(const unsigned long long *__restrict__ x,
                                                           const unsigned char *__restrict__ starts,
@@ -44,86 +56,107 @@ __global__ void __launch_bounds__(SC_THREADS) scan_kernel(const unsigned long lo
     // finishes last rewrites it, after every block has read it.
     const bool seen = state->seen != 0;
     const unsigned long long carried = state->last;
-    const int tile = take_ticket(counters);
-    const int64_t row0 = static_cast<int64_t>(tile) * SC_TILE + threadIdx.x * SC_ITEMS;
-    unsigned long long v[SC_ITEMS];
-    unsigned fl = 0;  // bit j: row row0 + j starts a segment
-    if (ALIGNED && row0 + SC_ITEMS <= n) {
-        const ulonglong2 *q = reinterpret_cast<const ulonglong2 *>(x + row0);
-#pragma unroll
-        for (int j = 0; j < SC_ITEMS / 2; ++j) {
-            ulonglong2 u = __ldcs(q + j);
-            v[2 * j] = u.x;
-            v[2 * j + 1] = u.y;
-        }
-        if (BY) {
-            uint4 m = __ldcs(reinterpret_cast<const uint4 *>(starts + row0));
-            unsigned w[4] = {m.x, m.y, m.z, m.w};
-#pragma unroll
-            for (int j = 0; j < SC_ITEMS; ++j)
-                if ((w[j >> 2] >> (8 * (j & 3))) & 0xffu) fl |= 1u << j;
-        }
-    } else {
-#pragma unroll
-        for (int j = 0; j < SC_ITEMS; ++j) {
-            bool in = row0 + j < n;
-            v[j] = in ? x[row0 + j] : 0ull;
-            if (BY && in && starts[row0 + j]) fl |= 1u << j;
-        }
-    }
-    // Row 0 of the array starts a segment whatever its byte (scan.rs:300-308).
-    if (row0 == 0 && !seen) fl |= 1u;
-    // Thread-local inclusive scan.
-    Seg agg{0, 0};
-#pragma unroll
-    for (int j = 0; j < SC_ITEMS; ++j) {
-        bool s = BY ? ((fl >> j) & 1u) : (j == 0 && row0 == 0 && !seen);
-        agg = seg_op(agg, Seg{v[j], s});
-        v[j] = agg.sum;
-    }
-    // Block-wide exclusive scan of the thread partials (segmented), by warps then across warps.
     __shared__ Seg s_warp[SC_THREADS / 32];
     __shared__ Seg s_prefix;
+    const int tile = take_ticket(counters);
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    Seg inc = agg;
+    const int64_t wbase = static_cast<int64_t>(tile) * SC_TILE + static_cast<int64_t>(w) * (32 * SC_ITEMS);
+
+    unsigned long long v[SC_ROWS][SC_VEC];
+    unsigned has = 0;  // bit 4r+k: a segment start at or before item k of row r within the warp slice
+    Seg carry{0, 0};   // the warp slice so far
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        Seg y{__shfl_up_sync(FULL, inc.sum, o), __shfl_up_sync(FULL, inc.start, o)};
-        if (lane >= o) inc = seg_op(y, inc);
-    }
-    if (lane == 31) s_warp[w] = inc;
-    Seg excl{__shfl_up_sync(FULL, inc.sum, 1), __shfl_up_sync(FULL, inc.start, 1)};
-    bool has_excl = lane > 0;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        Seg wp{0, 0}, tile_agg{0, 0};
-        for (int i = 0; i < SC_THREADS / 32; ++i) {
-            Seg t = s_warp[i];
-            s_warp[i] = wp;  // exclusive over warps
-            wp = i ? seg_op(wp, t) : t;
+    for (int r = 0; r < SC_ROWS; ++r) {
+        const int64_t i0 = wbase + r * (32 * SC_VEC) + lane * SC_VEC;
+        unsigned f = 0;
+        if (ALIGNED && i0 + SC_VEC <= n) {
+            ulonglong4_32a u = *reinterpret_cast<const ulonglong4_32a *>(x + i0);
+            v[r][0] = u.x;
+            v[r][1] = u.y;
+            v[r][2] = u.z;
+            v[r][3] = u.w;
+            if (BY) {
+                unsigned m = *reinterpret_cast<const unsigned *>(starts + i0);
+#pragma unroll
+                for (int k = 0; k < SC_VEC; ++k)
+                    if ((m >> (8 * k)) & 0xffu) f |= 1u << k;
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < SC_VEC; ++k) {
+                bool in = i0 + k < n;
+                v[r][k] = in ? x[i0 + k] : 0ull;
+                if (BY && in && starts[i0 + k]) f |= 1u << k;
+            }
         }
-        tile_agg = wp;
-        Seg init{carried, 0};
-        s_prefix = lookback_exclusive<Seg>(lb, tile, tile_agg, init, epoch, seg_op, status);
+        // Row 0 of the array starts a segment whatever its byte (scan.rs:300-308).
+        if (i0 == 0 && !seen) f |= 1u;
+        // Lane-local inclusive segmented scan of the 4 items.
+        Seg loc{0, 0};
+#pragma unroll
+        for (int k = 0; k < SC_VEC; ++k) {
+            loc = seg_op(loc, Seg{v[r][k], (f >> k) & 1u});
+            v[r][k] = loc.sum;
+        }
+        // Warp inclusive scan of the lane partials.
+        Seg inc = loc;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            Seg y{__shfl_up_sync(FULL, inc.sum, o), __shfl_up_sync(FULL, inc.start, o)};
+            if (lane >= o) inc = seg_op(y, inc);
+        }
+        Seg ex{__shfl_up_sync(FULL, inc.sum, 1), __shfl_up_sync(FULL, inc.start, 1)};
+        if (lane == 0) ex = Seg{0, 0};
+        Seg pre = seg_op(carry, ex);  // the warp slice before this lane's items
+        // Items before the lane's first start add the prefix; `has` records whether the
+        // warp slice has a start at or before the item.
+        unsigned first = f ? __ffs(f) - 1 : SC_VEC;
+#pragma unroll
+        for (int k = 0; k < SC_VEC; ++k) {
+            if (static_cast<unsigned>(k) < first) v[r][k] += pre.sum;
+            if (static_cast<unsigned>(k) >= first || pre.start) has |= 1u << (r * SC_VEC + k);
+        }
+        Seg row_total = __shfl_sync_v(inc, 31);
+        carry = seg_op(carry, row_total);
+    }
+    if (lane == 0) s_warp[w] = carry;
+    __syncthreads();
+    if (w == 0) {
+        // Exclusive segmented scan over the warps, then the lookback over tiles.
+        Seg c = lane < SC_THREADS / 32 ? s_warp[lane] : Seg{0, 0}, inc = c;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            Seg y{__shfl_up_sync(FULL, inc.sum, o), __shfl_up_sync(FULL, inc.start, o)};
+            if (lane >= o) inc = seg_op(y, inc);
+        }
+        Seg ex{__shfl_up_sync(FULL, inc.sum, 1), __shfl_up_sync(FULL, inc.start, 1)};
+        if (lane == 0) ex = Seg{0, 0};
+        Seg tile_agg = __shfl_sync_v(inc, SC_THREADS / 32 - 1);
+        if (lane < SC_THREADS / 32) s_warp[lane] = ex;
+        Seg pre = warp_lookback<Seg>(lb, tile, tile_agg, Seg{carried, 0}, Seg{0, 0}, epoch, seg_op, status);
+        if (lane == 0) s_prefix = pre;
     }
     __syncthreads();
-    // prefix before this thread = tile prefix, then warps before, then lanes before.
-    Seg pre = s_prefix;
-    if (w > 0) pre = seg_op(pre, s_warp[w]);
-    if (has_excl) pre = seg_op(pre, excl);
-    // Rows up to the thread's first start add the carried prefix.
-    unsigned first = BY ? (fl ? __ffs(fl) - 1 : SC_ITEMS) : ((row0 == 0 && !seen) ? 0 : SC_ITEMS);
+    // The prefix before the warp slice: the tile's exclusive prefix, then the earlier warps.
+    const Seg before = seg_op(s_prefix, s_warp[w]);
 #pragma unroll
-    for (int j = 0; j < SC_ITEMS; ++j)
-        if (static_cast<unsigned>(j) < first) v[j] += pre.sum;
-    if (ALIGNED && row0 + SC_ITEMS <= n) {
-        ulonglong2 *q = reinterpret_cast<ulonglong2 *>(out + row0);
+    for (int r = 0; r < SC_ROWS; ++r) {
 #pragma unroll
-        for (int j = 0; j < SC_ITEMS / 2; ++j) __stcs(q + j, make_ulonglong2(v[2 * j], v[2 * j + 1]));
-    } else {
+        for (int k = 0; k < SC_VEC; ++k)
+            if (!((has >> (r * SC_VEC + k)) & 1u)) v[r][k] += before.sum;
+        const int64_t i0 = wbase + r * (32 * SC_VEC) + lane * SC_VEC;
+        if (ALIGNED && i0 + SC_VEC <= n) {
+            ulonglong4_32a u;
+            u.x = v[r][0];
+            u.y = v[r][1];
+            u.z = v[r][2];
+            u.w = v[r][3];
+            *reinterpret_cast<ulonglong4_32a *>(out + i0) = u;
+        } else {
 #pragma unroll
-        for (int j = 0; j < SC_ITEMS; ++j)
-            if (row0 + j < n) out[row0 + j] = v[j];
+            for (int k = 0; k < SC_VEC; ++k)
+                if (i0 + k < n) out[i0 + k] = v[r][k];
+        }
     }
     // The last row's output, the last tile's inclusive value, is the carried state.
     if (release_ticket_last(counters, tiles) && threadIdx.x == 0) {
@@ -164,8 +197,8 @@ struct ScanImpl : ScannerImpl {
         const auto *x = args[0].ptr<unsigned long long>();
         const unsigned char *s = by ? args[1].ptr<unsigned char>() : nullptr;
         auto *o = static_cast<unsigned long long *>(out->data());
-        bool aligned = (reinterpret_cast<uintptr_t>(x) & 15) == 0 && (reinterpret_cast<uintptr_t>(o) & 15) == 0 &&
-                       (reinterpret_cast<uintptr_t>(s) & 15) == 0;
+        bool aligned = (reinterpret_cast<uintptr_t>(x) & 31) == 0 && (reinterpret_cast<uintptr_t>(o) & 31) == 0 &&
+                       (reinterpret_cast<uintptr_t>(s) & 3) == 0;
         if (by && aligned) scan_kernel<true, true><<<tiles, SC_THREADS, 0, ctx->stream>>>(x, s, o, n, tiles, lb, epoch, state, ctx->counters, ctx->status);
         else if (by) scan_kernel<true, false><<<tiles, SC_THREADS, 0, ctx->stream>>>(x, s, o, n, tiles, lb, epoch, state, ctx->counters, ctx->status);
         else if (aligned) scan_kernel<false, true><<<tiles, SC_THREADS, 0, ctx->stream>>>(x, s, o, n, tiles, lb, epoch, state, ctx->counters, ctx->status);
@@ -359,7 +392,7 @@ extern "C" vkc_status vkc_scan_add_i64_noalloc(int device, const int64_t *in, in
     }
     const auto *x = reinterpret_cast<const unsigned long long *>(in);
     auto *o = reinterpret_cast<unsigned long long *>(out);
-    bool aligned = (reinterpret_cast<uintptr_t>(x) & 15) == 0 && (reinterpret_cast<uintptr_t>(o) & 15) == 0;
+    bool aligned = (reinterpret_cast<uintptr_t>(x) & 31) == 0 && (reinterpret_cast<uintptr_t>(o) & 31) == 0;
     if (aligned)
         scan_kernel<false, true><<<tiles, SC_THREADS, 0, s>>>(x, nullptr, o, n, tiles, lb, 1u, state, counters, status);
     else

@@ -31,26 +31,13 @@ struct SelArgs {
     unsigned long long *total;  // survivor count of the launch
 };
 
-// Loads 16 consecutive items starting at item `row` (16-byte aligned when ALIGNED).
-template <int W, bool ALIGNED>
-__device__ __forceinline__ void load16(const void *p, int64_t row, int64_t n,
-                                       typename Word<W>::T (&v)[SEL_ITEMS]) {
-    using T = typename Word<W>::T;
-    const T *src = static_cast<const T *>(p) + row;
-    if (ALIGNED && row + SEL_ITEMS <= n) {
-        const uint4 *q = reinterpret_cast<const uint4 *>(src);
-#pragma unroll
-        for (int j = 0; j < SEL_ITEMS * W / 16; ++j) {
-            uint4 u = __ldcs(q + j);
-            const T *e = reinterpret_cast<const T *>(&u);
-#pragma unroll
-            for (int k = 0; k < 16 / W; ++k) v[j * (16 / W) + k] = e[k];
-        }
-    } else {
-#pragma unroll
-        for (int j = 0; j < SEL_ITEMS; ++j) v[j] = row + j < n ? src[j] : T(0);
-    }
-}
+// Per thread, ITEMS items in ROWS rows of the warp's 512-item slice: in row r the warp reads
+// 32 * VEC consecutive items, VEC per lane (one 16-byte load), so every load is coalesced and
+// item order is (row, lane, element).
+template <int W> struct SelShape {
+    static constexpr int VEC = 16 / W;
+    static constexpr int ROWS = SEL_ITEMS / VEC;
+};
 
 template <int KIND, int W, bool ALIGNED>
 __global__ void __launch_bounds__(SEL_THREADS) select_kernel(SelArgs a, int tiles,
@@ -59,45 +46,93 @@ __global__ void __launch_bounds__(SEL_THREADS) select_kernel(SelArgs a, int tile
                                                              DevStatus *status) {
     using T = typename Word<W>::T;
     using O = typename Word<KIND == SEL_WHERE ? 8 : W>::T;
-    __shared__ O s_out[SEL_TILE];
-    __shared__ unsigned long long s_prefix, s_count;
+    constexpr int VEC = SelShape<W>::VEC, ROWS = SelShape<W>::ROWS;
+    __shared__ unsigned s_warp[SEL_THREADS / 32];
+    __shared__ unsigned long long s_prefix;
     const int tile = take_ticket(counters);
-    const int64_t row0 = static_cast<int64_t>(tile) * SEL_TILE + threadIdx.x * SEL_ITEMS;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const unsigned lt = (1u << lane) - 1;
+    const int64_t wbase = static_cast<int64_t>(tile) * SEL_TILE + static_cast<int64_t>(w) * (32 * SEL_ITEMS);
 
-    T v[SEL_ITEMS];
-    unsigned keep = 0;
-    if (KIND != SEL_WHERE) load16<W, ALIGNED>(a.x, row0, a.n, v);
-    if (KIND == SEL_FILTER) {
+    T v[ROWS][VEC];
+    unsigned keep[ROWS];       // VEC bits per row
+    unsigned rank[ROWS];       // survivors before this lane's first item in the row
+    unsigned row_off[ROWS];    // survivors of the warp before the row
+    unsigned total = 0;
 #pragma unroll
-        for (int j = 0; j < SEL_ITEMS; ++j)
-            if (row0 + j < a.n && in_range(a.r, static_cast<unsigned long long>(v[j]))) keep |= 1u << j;
-    } else {
-        unsigned char m[SEL_ITEMS];
-        load16<1, ALIGNED>(a.m, row0, a.n, m);
+    for (int r = 0; r < ROWS; ++r) {
+        const int64_t i0 = wbase + r * (32 * VEC) + lane * VEC;
+        if (KIND != SEL_WHERE) {
+            if (ALIGNED && i0 + VEC <= a.n) {
+                uint4 u = __ldcs(reinterpret_cast<const uint4 *>(static_cast<const T *>(a.x) + i0));
+                const T *e = reinterpret_cast<const T *>(&u);
 #pragma unroll
-        for (int j = 0; j < SEL_ITEMS; ++j)
-            if (m[j]) keep |= 1u << j;
-    }
-    unsigned long long c = __popc(keep), tile_count;
-    unsigned long long off = block_exclusive_sum<unsigned long long>(c, &tile_count);
-    // Compact into shared memory in row order.
-    int r = static_cast<int>(off);
+                for (int k = 0; k < VEC; ++k) v[r][k] = e[k];
+            } else {
 #pragma unroll
-    for (int j = 0; j < SEL_ITEMS; ++j)
-        if (keep & (1u << j)) {
-            if (KIND == SEL_WHERE) s_out[r] = static_cast<O>(a.base + row0 + j);
-            else s_out[r] = static_cast<O>(v[j]);
-            ++r;
+                for (int k = 0; k < VEC; ++k) v[r][k] = i0 + k < a.n ? static_cast<const T *>(a.x)[i0 + k] : T(0);
+            }
         }
-    if (threadIdx.x == 0) {
+        unsigned bits = 0;
+        if (KIND == SEL_FILTER) {
+#pragma unroll
+            for (int k = 0; k < VEC; ++k)
+                if (i0 + k < a.n && in_range(a.r, static_cast<unsigned long long>(v[r][k]))) bits |= 1u << k;
+        } else if (ALIGNED && VEC == 16 && i0 + 16 <= a.n) {
+            uint4 u = __ldcs(reinterpret_cast<const uint4 *>(a.m + i0));
+            unsigned wd[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+            for (int k = 0; k < 16; ++k)
+                if ((wd[k >> 2] >> (8 * (k & 3))) & 0xffu) bits |= 1u << k;
+        } else {
+#pragma unroll
+            for (int k = 0; k < VEC; ++k)
+                if (i0 + k < a.n && a.m[i0 + k]) bits |= 1u << k;
+        }
+        keep[r] = bits;
+        // In-order ranks: the lanes before this one, element by element.
+        unsigned before = 0, row_total = 0;
+#pragma unroll
+        for (int k = 0; k < VEC; ++k) {
+            unsigned m = __ballot_sync(FULL, (bits >> k) & 1u);
+            before += __popc(m & lt);
+            row_total += __popc(m);
+        }
+        rank[r] = before;
+        row_off[r] = total;
+        total += row_total;
+    }
+    if (lane == 0) s_warp[w] = total;
+    __syncthreads();
+    if (w == 0) {
+        unsigned c = lane < SEL_THREADS / 32 ? s_warp[lane] : 0u, x = c;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            unsigned y = __shfl_up_sync(FULL, x, o);
+            if (lane >= o) x += y;
+        }
+        unsigned long long tile_count = __shfl_sync(FULL, x, SEL_THREADS / 32 - 1);
+        if (lane < SEL_THREADS / 32) s_warp[lane] = x - c;  // exclusive over warps
         auto add = [](unsigned long long p, unsigned long long q) { return p + q; };
-        s_prefix = lookback_exclusive<unsigned long long>(lb, tile, tile_count, 0ull, epoch, add, status);
-        s_count = tile_count;
-        if (tile == tiles - 1) *a.total = s_prefix + tile_count;
+        unsigned long long pre = warp_lookback<unsigned long long>(lb, tile, tile_count, 0ull, 0ull, epoch, add, status);
+        if (lane == 0) {
+            s_prefix = pre;
+            if (tile == tiles - 1) *a.total = pre + tile_count;
+        }
     }
     __syncthreads();
-    O *out = static_cast<O *>(a.out) + s_prefix;
-    for (int i = threadIdx.x; i < static_cast<int>(s_count); i += SEL_THREADS) out[i] = s_out[i];
+    O *out = static_cast<O *>(a.out) + s_prefix + s_warp[w];
+#pragma unroll
+    for (int r = 0; r < ROWS; ++r) {
+        unsigned p = row_off[r] + rank[r];
+        const int64_t i0 = wbase + r * (32 * VEC) + lane * VEC;
+#pragma unroll
+        for (int k = 0; k < VEC; ++k)
+            if ((keep[r] >> k) & 1u) {
+                out[p] = KIND == SEL_WHERE ? static_cast<O>(a.base + i0 + k) : static_cast<O>(v[r][k]);
+                ++p;
+            }
+    }
     release_ticket(counters, tiles);
 }
 

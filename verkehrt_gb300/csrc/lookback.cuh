@@ -51,6 +51,73 @@ __device__ V lookback_exclusive(LookbackTiles<V> lb, int tile, V agg, V init, un
     return excl;
 }
 
+// Warp shuffles of lookback values.
+__device__ __forceinline__ unsigned long long shfl_down_v(unsigned long long v, int o) {
+    return __shfl_down_sync(FULL, v, o);
+}
+__device__ __forceinline__ unsigned long long __shfl_sync_v(unsigned long long v, int src) {
+    return __shfl_sync(FULL, v, src);
+}
+
+// Warp-parallel decoupled lookback, run by all 32 lanes of one warp: publishes the tile's
+// aggregate, then reads the flags of 32 predecessor tiles per step (lane i reads tile
+// hi - i), combines every aggregate up to the closest inclusive value in one ordered warp
+// reduction, and stops at that inclusive value (or at `init` before tile 0). Publishes the
+// inclusive value and returns the exclusive prefix in every lane. `ident` is the identity of
+// `op`. On a wait that runs out it records a timeout and returns `init`.
+template <class V, class Op>
+__device__ V warp_lookback(LookbackTiles<V> lb, int tile, V agg, V init, V ident, unsigned epoch, Op op,
+                           DevStatus *status) {
+    const int lane = threadIdx.x & 31;
+    if (lane == 0) {
+        lb.agg[tile] = agg;
+        __threadfence();
+        st_release(&lb.flag[tile], (epoch << 2) | 1u);
+    }
+    __syncwarp();
+    V excl = ident;
+    bool have = false;
+    for (int hi = tile - 1;; hi -= 32) {
+        int tp = hi - lane;
+        unsigned f = 0;
+        bool bad = false;
+        if (tp >= 0) {
+            unsigned it = 0;
+            while (((f = ld_acquire(&lb.flag[tp])) >> 2) != epoch) {
+                if (++it > SPIN_LIMIT) {
+                    set_timeout(status);
+                    bad = true;
+                    break;
+                }
+                backoff(it);
+            }
+        }
+        if (__any_sync(FULL, bad)) return init;
+        bool incl = tp < 0 || (f & 3u) == 2u;
+        unsigned m = __ballot_sync(FULL, incl);
+        int k = m ? __ffs(m) - 1 : 32;
+        V v = ident;
+        if (lane < k) v = lb.agg[tp];
+        else if (lane == k) v = tp >= 0 ? lb.inc[tp] : init;
+        // Lane i holds tile hi - i, so the higher lane is the earlier tile.
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            V other = shfl_down_v(v, o);
+            if (lane + o < 32) v = op(other, v);
+        }
+        V window = __shfl_sync_v(v, 0);
+        excl = have ? op(window, excl) : window;
+        have = true;
+        if (k < 32) break;
+    }
+    if (lane == 0) {
+        lb.inc[tile] = op(excl, agg);
+        __threadfence();
+        st_release(&lb.flag[tile], (epoch << 2) | 2u);
+    }
+    return excl;
+}
+
 // Block-wide exclusive sum of one value per thread (blockDim.x a multiple of 32, at most 1024).
 // Returns the exclusive prefix; *total gets the block sum.
 template <class V> __device__ __forceinline__ V block_exclusive_sum(V v, V *total) {
