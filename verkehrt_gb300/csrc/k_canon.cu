@@ -106,21 +106,22 @@ __device__ __forceinline__ bool apply(unsigned long long s, int E, TF f, unsigne
 __device__ __forceinline__ bool seg_tf(const unsigned long long (&v)[CT_SEG_BLOCKS][2], int h,
                                        int KE, TF *out) {
     unsigned long long D = 0;
-    int kmin = 64;
+    int exmax = 0;
     bool tie = false;
 #pragma unroll
     for (int i = 0; i < CT_SEG_BLOCKS; ++i) {
         unsigned long long b = v[i][h];
-        int ex = static_cast<int>(b >> 52);  // the sign bit makes negative rows fail k >= 1
-        int k = KE - ex;
-        kmin = min(kmin, k);
-        k = min(max(k, 1), 63);  // zero and subnormal rows have k >= 64: increment 0, no tie
+        int ex = static_cast<int>(b >> 52);  // the sign bit makes negative rows fail ex < KE
+        exmax = max(exmax, ex);
+        // k = KE - ex in [1, 63]: zero and subnormal rows have k >= 64 (increment 0, no tie);
+        // a row with ex >= KE wraps to a large unsigned k and fails the exmax check below.
+        unsigned k = min(static_cast<unsigned>(KE - ex), 63u);
         unsigned long long M = (b & MANT) | ONE52;
         unsigned long long w = M + (1ull << (k - 1));
         D += w >> k;
         tie |= (w << (64 - k)) == 0;
     }
-    if (kmin < 1) return false;
+    if (exmax >= KE) return false;
     if (!tie) {
         *out = TF{D, D};
         return true;
@@ -130,7 +131,7 @@ __device__ __forceinline__ bool seg_tf(const unsigned long long (&v)[CT_SEG_BLOC
     unsigned long long d0 = 0, d1 = 0;
     for (int i = 0; i < CT_SEG_BLOCKS; ++i) {
         unsigned long long b = v[i][h];
-        int k = min(max(KE - static_cast<int>(b >> 52), 1), 63);
+        unsigned k = min(static_cast<unsigned>(KE - static_cast<int>(b >> 52)), 63u);
         unsigned long long M = (b & MANT) | ONE52;
         unsigned long long w = M + (1ull << (k - 1));
         unsigned long long inc = w >> k;
@@ -172,7 +173,7 @@ struct CanonState {
 
 // Per-launch work arrays, in the context scratch arena. T = number of 4096-row tiles.
 struct CanonWork {
-    float *apx;                // [T][16] approximate lane sums of each tile
+    float *apx;                // [16][T] approximate lane sums of each tile
     int *cand;                 // [T][16][2] candidate binades (NO_E when absent)
     int *recE;                 // [16][T][2] binade of each tile transfer function (NO_E: none)
     TF *recD;                  // [16][T][2]
@@ -227,7 +228,7 @@ __device__ __forceinline__ void load_tile(const RowArgs &args, int64_t nb, int t
 
 // K1: the approximate lane sums of every tile (float sums of float images, one read).
 template <int OP, bool ALIGNED>
-__global__ void __launch_bounds__(CT_THREADS) canon_apx_kernel(RowArgs args, int64_t nb, CanonWork wk) {
+__global__ void __launch_bounds__(CT_THREADS) canon_apx_kernel(RowArgs args, int64_t nb, int T, CanonWork wk) {
     __shared__ float s_apx[CT_SEGS][16];
     const int t = threadIdx.x, lp = t & 7, seg = t >> 3;
     const int tile = blockIdx.x;
@@ -245,7 +246,7 @@ __global__ void __launch_bounds__(CT_THREADS) canon_apx_kernel(RowArgs args, int
     if (t < 16) {
         float A = 0.f;
         for (int s = 0; s < CT_SEGS; ++s) A += s_apx[s][t];
-        wk.apx[tile * 16 + t] = A;
+        wk.apx[static_cast<int64_t>(t) * T + tile] = A;
     }
 }
 
@@ -253,24 +254,36 @@ __global__ void __launch_bounds__(CT_THREADS) canon_apx_kernel(RowArgs args, int
 // from the lane's exact state, and each tile's candidate binades: the range [start, end]
 // widened by 2^-12 on each side must lie in one binade or two adjacent ones.
 __global__ void __launch_bounds__(1024) canon_cand_kernel(int T, CanonWork wk, const CanonState *state) {
-    __shared__ double s_tot[1024];
     const int L = blockIdx.x, t = threadIdx.x;
+    const float *a = wk.apx + static_cast<int64_t>(L) * T;
     const int per = (T + 1023) / 1024;
-    const int t0 = t * per, t1 = min(T, t0 + per);
+    const int t0 = min(T, t * per), t1 = min(T, t0 + per);
     double sum = 0;
-    for (int k = t0; k < t1; ++k) sum += static_cast<double>(wk.apx[k * 16 + L]);
-    s_tot[t] = sum;
-    __syncthreads();
-    // Block exclusive scan of the thread sums (Hillis-Steele over shared memory).
-    for (int o = 1; o < 1024; o <<= 1) {
-        double add = t >= o ? s_tot[t - o] : 0.0;
-        __syncthreads();
-        s_tot[t] += add;
-        __syncthreads();
+    for (int k = t0; k < t1; ++k) sum += static_cast<double>(a[k]);
+    // Block inclusive scan of the thread sums: warps, then across warps.
+    const int lane = t & 31, w = t >> 5;
+    double x = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        double y = __shfl_up_sync(FULL, x, o);
+        if (lane >= o) x += y;
     }
-    double pre = (t ? s_tot[t - 1] : 0.0) + as_f64(state->lanes[L]);
+    __shared__ double s_w[32];
+    if (lane == 31) s_w[w] = x;
+    __syncthreads();
+    if (w == 0) {
+        double z = s_w[lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            double y = __shfl_up_sync(FULL, z, o);
+            if (lane >= o) z += y;
+        }
+        s_w[lane] = z;
+    }
+    __syncthreads();
+    double pre = (w ? s_w[w - 1] : 0.0) + x - sum + as_f64(state->lanes[L]);
     for (int k = t0; k < t1; ++k) {
-        double A = static_cast<double>(wk.apx[k * 16 + L]);
+        double A = static_cast<double>(a[k]);
         double lo = A < 0 ? pre + A : pre, hi = A < 0 ? pre : pre + A;
         int elo = binade(lo * (1.0 - 0x1p-12)), ehi = binade(hi * (1.0 + 0x1p-12));
         int c0 = NO_E, c1 = NO_E;
@@ -281,8 +294,7 @@ __global__ void __launch_bounds__(1024) canon_cand_kernel(int T, CanonWork wk, c
                 c1 = ehi;
             }
         }
-        wk.cand[(k * 16 + L) * 2] = c0;
-        wk.cand[(k * 16 + L) * 2 + 1] = c1;
+        *reinterpret_cast<int2 *>(&wk.cand[(k * 16 + L) * 2]) = make_int2(c0, c1);
         pre += A;
     }
 }
@@ -447,21 +459,86 @@ __device__ unsigned long long resolve_tile(const RowArgs &args, int64_t nb, int 
     return s;
 }
 
-// K4b: one warp per lane walks the tiles from the lane's exact state: whole 32-tile chunks
-// while their transfer function holds, then single tiles, and resolves the tiles that none
-// carries (binade crossings, negative or special rows, the first rows of the lane).
+// K4b: one block per lane. The block first copies the lane's chunk records, and the tile
+// records of the chunks without one ("mixed"), into shared memory; then warp 0 walks the tiles
+// from the lane's exact state: whole 32-tile chunks while their transfer function holds, single
+// tiles inside mixed chunks, and resolves from the rows the tiles that none carries (binade
+// crossings, negative or special rows, the first rows of the lane).
+constexpr int WK_THREADS = 256;
+constexpr int WK_MAX_CHUNKS = 4096;  // chunk records held in shared memory
+constexpr int WK_MAX_MIXED = 48;     // mixed chunks whose tile records are held there
+
+struct WalkSmem {
+    int chunkE[WK_MAX_CHUNKS];
+    TF chunkD[WK_MAX_CHUNKS];
+    short mixed_of[WK_MAX_CHUNKS];
+    int chunk_of[WK_MAX_MIXED];
+    int mE[WK_MAX_MIXED][32][2];
+    TF mD[WK_MAX_MIXED][32][2];
+    int nmixed;
+};
+
 template <int OP>
-__global__ void __launch_bounds__(512) canon_walk_kernel(RowArgs args, int64_t nb, int T, int C, CanonWork wk,
-                                                         CanonState *state) {
-    const int lane = threadIdx.x & 31, L = threadIdx.x >> 5;
+__global__ void __launch_bounds__(WK_THREADS) canon_walk_kernel(RowArgs args, int64_t nb, int T, int C, CanonWork wk,
+                                                                CanonState *state) {
+    extern __shared__ __align__(16) unsigned char walk_smem[];
+    WalkSmem &sm = *reinterpret_cast<WalkSmem *>(walk_smem);
+    const int L = blockIdx.x, t = threadIdx.x;
+    const bool held = C <= WK_MAX_CHUNKS;
+    const int *gE = wk.chunkE + static_cast<int64_t>(L) * C;
+    const TF *gD = wk.chunkD + static_cast<int64_t>(L) * C;
+    if (t == 0) sm.nmixed = 0;
+    __syncthreads();
+    if (held) {
+        for (int c = t; c < C; c += WK_THREADS) {
+            int e = gE[c];
+            sm.chunkE[c] = e;
+            sm.chunkD[c] = gD[c];
+            short slot = -1;
+            if (e == NO_E) {
+                int k = atomicAdd(&sm.nmixed, 1);
+                if (k < WK_MAX_MIXED) {
+                    slot = static_cast<short>(k);
+                    sm.chunk_of[k] = c;
+                }
+            }
+            sm.mixed_of[c] = slot;
+        }
+    }
+    __syncthreads();
+    if (held) {
+        // Tile records of the mixed chunks with a slot: 32 tiles x 2 candidates each.
+        const int nm = min(sm.nmixed, WK_MAX_MIXED);
+        for (int idx = t; idx < nm * 64; idx += WK_THREADS) {
+            const int slot = idx >> 6, j = (idx >> 1) & 31, cand = idx & 1;
+            const int tp = sm.chunk_of[slot] * 32 + j;
+            int e = NO_E;
+            TF d{0, 0};
+            if (tp < T) {
+                const int64_t at = (static_cast<int64_t>(L) * T + tp) * 2 + cand;
+                e = wk.recE[at];
+                d = wk.recD[at];
+            }
+            sm.mE[slot][j][cand] = e;
+            sm.mD[slot][j][cand] = d;
+        }
+    }
+    __syncthreads();
+    if (t >= 32) return;
+
+    const int lane = t;
     unsigned long long s = state->lanes[L];
     int k = 0;  // next chunk
     while (k < C) {
         // Whole chunks k .. k+31.
         const int E = state_binade(s);
         const int kc = k + lane;
-        int ce = kc < C ? wk.chunkE[static_cast<int64_t>(L) * C + kc] : NO_E;
-        TF f = (ce != NO_E && ce == E) ? wk.chunkD[static_cast<int64_t>(L) * C + kc] : TF{0, 0};
+        int ce = NO_E;
+        TF f{0, 0};
+        if (kc < C) {
+            ce = held ? sm.chunkE[kc] : gE[kc];
+            if (ce != NO_E && ce == E) f = held ? sm.chunkD[kc] : gD[kc];
+        }
         unsigned long long r = s;
         int m = E == NO_E ? 0 : apply_prefix(f, kc < C && ce != NO_E && ce == E, s, E, &r);
         if (m > 0) {
@@ -470,12 +547,28 @@ __global__ void __launch_bounds__(512) canon_walk_kernel(RowArgs args, int64_t n
             continue;
         }
         // Chunk k, tile by tile.
-        int tp = k * 32, end = min(T, tp + 32);
+        const int slot = held ? sm.mixed_of[k] : -1;
+        int tp = k * 32;
+        const int end = min(T, tp + 32);
         while (tp < end) {
             const int Et = state_binade(s);
             const int tl = tp + lane;
             TF g{0, 0};
-            bool usable = tl < end && tile_tf(wk, T, L, tl, Et, &g);
+            bool usable = false;
+            if (tl < end && Et != NO_E) {
+                if (slot >= 0) {
+                    const int j = tl - k * 32;
+                    if (sm.mE[slot][j][0] == Et) {
+                        g = sm.mD[slot][j][0];
+                        usable = true;
+                    } else if (sm.mE[slot][j][1] == Et) {
+                        g = sm.mD[slot][j][1];
+                        usable = true;
+                    }
+                } else {
+                    usable = tile_tf(wk, T, L, tl, Et, &g);
+                }
+            }
             int mt = Et == NO_E ? 0 : apply_prefix(g, usable, s, Et, &r);
             if (mt > 0) {
                 s = r;
@@ -515,7 +608,7 @@ template <int OP, bool ALIGNED>
 static vkc_status launch_canon(vkc_ctx *ctx, const RowArgs &a, int64_t nb, int T, int C, const CanonWork &wk,
                                CanonState *state) {
     vkc_status st;
-    canon_apx_kernel<OP, ALIGNED><<<T, CT_THREADS, 0, ctx->stream>>>(a, nb, wk);
+    canon_apx_kernel<OP, ALIGNED><<<T, CT_THREADS, 0, ctx->stream>>>(a, nb, T, wk);
     if ((st = launched(ctx, "canon_apx"))) return st;
     canon_cand_kernel<<<16, 1024, 0, ctx->stream>>>(T, wk, state);
     if ((st = launched(ctx, "canon_cand"))) return st;
@@ -524,7 +617,13 @@ static vkc_status launch_canon(vkc_ctx *ctx, const RowArgs &a, int64_t nb, int T
     int warps = 16 * C;
     canon_chunk_kernel<<<(warps + 7) / 8, 256, 0, ctx->stream>>>(T, C, wk);
     if ((st = launched(ctx, "canon_chunk"))) return st;
-    canon_walk_kernel<OP><<<1, 512, 0, ctx->stream>>>(a, nb, T, C, wk, state);
+    static bool configured = false;
+    if (!configured) {
+        cudaFuncSetAttribute(canon_walk_kernel<OP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             static_cast<int>(sizeof(WalkSmem)));
+        configured = true;
+    }
+    canon_walk_kernel<OP><<<16, WK_THREADS, sizeof(WalkSmem), ctx->stream>>>(a, nb, T, C, wk, state);
     return launched(ctx, "canon_walk");
 }
 

@@ -98,8 +98,7 @@ __global__ void __launch_bounds__(GI_THREADS) gi_insert_kernel(const long long *
 // Numbers the first occurrences in row order (a compaction of the rows whose slot's smallest
 // row is themselves) and stores each group's id in its slot.
 __global__ void __launch_bounds__(GI_THREADS) gi_number_kernel(const unsigned *__restrict__ slot_of, int64_t n,
-                                                               GroupTable t, int tiles,
-                                                               LookbackTiles<unsigned long long> lb,
+                                                               GroupTable t, int tiles, unsigned long long *words,
                                                                unsigned epoch, unsigned *counters,
                                                                DevStatus *st) {
     __shared__ unsigned long long s_prefix;
@@ -116,8 +115,7 @@ __global__ void __launch_bounds__(GI_THREADS) gi_number_kernel(const unsigned *_
     unsigned long long c = __popc(keep), tile_count;
     unsigned long long off = block_exclusive_sum<unsigned long long>(c, &tile_count);
     if (threadIdx.x < 32) {
-        auto add = [](unsigned long long p, unsigned long long q) { return p + q; };
-        unsigned long long pre = warp_lookback<unsigned long long>(lb, tile, tile_count, 0ull, 0ull, epoch, add, st);
+        unsigned long long pre = warp_lookback_count<4>(words, tile, tile_count, epoch, st);
         if (threadIdx.x == 0) s_prefix = pre;
     }
     __syncthreads();
@@ -184,16 +182,14 @@ static vkc_status run_group(vkc_ctx *ctx, const vkc_array *xa, const vkc_array *
         return st;
     }
     int tiles = static_cast<int>((n + GI_TILE - 1) / GI_TILE);
-    void *p;
     unsigned *flags;
-    if ((st = scratch(ctx, 16 * static_cast<size_t>(tiles), &p)) || (st = flag_arena(ctx, tiles, &flags))) {
+    if ((st = flag_arena(ctx, 2 * static_cast<size_t>(tiles), &flags))) {
         cleanup();
         vkc_array_release(o);
         return st;
     }
-    auto *vals = static_cast<unsigned long long *>(p);
-    LookbackTiles<unsigned long long> lb{flags, vals, vals + tiles};
-    gi_number_kernel<<<tiles, GI_THREADS, 0, ctx->stream>>>(slot_of, n, t, tiles, lb, next_epoch(ctx), ctx->counters, ctx->status);
+    gi_number_kernel<<<tiles, GI_THREADS, 0, ctx->stream>>>(slot_of, n, t, tiles, reinterpret_cast<unsigned long long *>(flags),
+                                                           next_epoch(ctx), ctx->counters, ctx->status);
     if ((st = launched(ctx, "gi_number"))) {
         cleanup();
         vkc_array_release(o);

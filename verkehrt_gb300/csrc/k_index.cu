@@ -49,9 +49,9 @@ __global__ void __launch_bounds__(256) gather_kernel(const typename GWord<W>::T 
             int64_t q = p + u * stride;
             if (q >= n2) break;
             int64_t i = head + 2 * q;
-            if (static_cast<uint64_t>(k[u].x) < nsrc) out[i] = g[u][0];
+            if (static_cast<uint64_t>(k[u].x) < nsrc) __stcs(out + i, g[u][0]);
             else if (static_cast<unsigned long long>(i) < bad) bad = static_cast<unsigned long long>(i);
-            if (static_cast<uint64_t>(k[u].y) < nsrc) out[i + 1] = g[u][1];
+            if (static_cast<uint64_t>(k[u].y) < nsrc) __stcs(out + i + 1, g[u][1]);
             else if (static_cast<unsigned long long>(i + 1) < bad) bad = static_cast<unsigned long long>(i + 1);
         }
     }

@@ -176,54 +176,104 @@ __device__ __forceinline__ void better(long long &k, unsigned long long &i, long
     }
 }
 
-// One pass over x[0, n) at global row offset `base`. F64 rows are keyed; NaN rows only
-// record their first position, which decides argmin/argmax and makes min/max NaN.
-template <bool MAX, bool F64>
+// One pass over x[0, n) at global row offset `base`. F64 rows are compared as order keys;
+// NaN rows only record their first position, which decides argmin/argmax and makes min/max
+// NaN. A thread visits its rows in increasing order, four 16-byte loads per step, so within a
+// thread a strict comparison keeps the first index of the extreme, and a thread's position is
+// kept as (step * 8 + slot) until the end.
+template <bool MAX, bool F64, bool ARG>
 __global__ void __launch_bounds__(256) extreme_kernel(const long long *__restrict__ x, int64_t n,
                                                       unsigned long long base, ExtState *partials,
                                                       unsigned *done, ExtState *state) {
     long long bk = MAX ? LLONG_MIN : LLONG_MAX;
-    unsigned long long bi = ~0ull, nan = ~0ull;
-    int64_t tid = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
-    auto visit = [&](long long v, int64_t i) {
-        if (F64) {
-            unsigned long long b = static_cast<unsigned long long>(v);
-            if ((b & 0x7fffffffffffffffull) > 0x7ff0000000000000ull) {
-                if (static_cast<unsigned long long>(i) < nan) nan = static_cast<unsigned long long>(i);
-                return;
-            }
-            v = f64_key(b);
-        }
-        better<MAX>(bk, bi, v, static_cast<unsigned long long>(i));
-    };
-    int64_t head = (reinterpret_cast<uintptr_t>(x) & 15) ? 1 : 0;
-    if (head > n) head = n;
-    if (head && tid == 0) visit(x[0], 0);
+    unsigned bpos = ~0u, npos = ~0u;  // best and first-NaN positions (step * 8 + slot)
+    unsigned long long maxabs = 0;     // min/max only: NaN when above +inf's bits
+    const int64_t tid = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    const int64_t head = ((reinterpret_cast<uintptr_t>(x) & 15) && n > 0) ? 1 : 0;
     const longlong2 *x2 = reinterpret_cast<const longlong2 *>(x + head);
-    int64_t n2 = (n - head) >> 1;
-    // Four independent 16-byte loads per thread in flight; rows of a thread still arrive in
-    // increasing order, which the first-index tie rule relies on.
-    for (int64_t i = tid; i < n2; i += 4 * stride) {
+    const int64_t n2 = (n - head) >> 1;
+    unsigned step = 0;
+    bool any = false;
+    for (int64_t i = tid; i < n2; i += 4 * stride, ++step) {
         longlong2 v[4];
 #pragma unroll
-        for (int u = 0; u < 4; ++u)
-            if (i + u * stride < n2) v[u] = __ldcs(&x2[i + u * stride]);
+        for (int u = 0; u < 4; ++u) v[u] = i + u * stride < n2 ? __ldcs(&x2[i + u * stride]) : make_longlong2(0, 0);
 #pragma unroll
-        for (int u = 0; u < 4; ++u)
-            if (i + u * stride < n2) {
-                visit(v[u].x, head + 2 * (i + u * stride));
-                visit(v[u].y, head + 2 * (i + u * stride) + 1);
+        for (int u = 0; u < 4; ++u) {
+            if (i + u * stride >= n2) break;  // the slots after it are past the end too
+            any = true;
+            long long e[2] = {v[u].x, v[u].y};
+#pragma unroll
+            for (int j = 0; j < 2; ++j) {
+                long long k = e[j];
+                if (F64) {
+                    const unsigned long long b = static_cast<unsigned long long>(k);
+                    if (!ARG) {
+                        maxabs = max(maxabs, b & 0x7fffffffffffffffull);
+                        k = f64_key(b);
+                    } else {
+                        if ((b & 0x7fffffffffffffffull) > 0x7ff0000000000000ull) {
+                            npos = min(npos, step * 8 + u * 2 + j);
+                            continue;
+                        }
+                        k = f64_key(b);
+                    }
+                }
+                if (ARG) {
+                    if (MAX ? k > bk : k < bk) {
+                        bk = k;
+                        bpos = step * 8 + u * 2 + j;
+                    }
+                } else {
+                    bk = MAX ? max(bk, k) : min(bk, k);
+                }
             }
+        }
     }
-    if (((n - head) & 1) && tid == 0) visit(x[n - 1], n - 1);
+    // Rows: position (step, slot) of this thread is row head + 2 * (tid + (step*4 + slot/2) * stride) + slot%2.
+    auto row_of = [&](unsigned p) -> unsigned long long {
+        const int64_t q = tid + (static_cast<int64_t>(p >> 3) * 4 + ((p >> 1) & 3)) * stride;
+        return static_cast<unsigned long long>(head + 2 * q + (p & 1));
+    };
+    unsigned long long bi = ~0ull, nan = ~0ull;
+    if (ARG) {
+        if (bpos != ~0u) bi = row_of(bpos);
+        if (npos != ~0u) nan = row_of(npos);
+    } else {
+        if (any) bi = 0;  // a row was seen
+        if (maxabs > 0x7ff0000000000000ull) nan = 0;
+    }
+    // The head and tail rows (views that start or end off the 16-byte grid).
+    auto visit = [&](int64_t r) {
+        const unsigned long long b = static_cast<unsigned long long>(x[r]);
+        long long k = static_cast<long long>(b);
+        if (F64) {
+            if ((b & 0x7fffffffffffffffull) > 0x7ff0000000000000ull) {
+                nan = ARG ? min(nan, static_cast<unsigned long long>(r)) : 0;
+                return;
+            }
+            k = f64_key(b);
+        }
+        if (ARG) better<MAX>(bk, bi, k, static_cast<unsigned long long>(r));
+        else {
+            bk = MAX ? max(bk, k) : min(bk, k);
+            bi = 0;
+        }
+    };
+    if (tid == 0 && head) visit(0);
+    if (tid == 0 && ((n - head) & 1)) visit(n - 1);
     // Warp, then block.
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         long long k2 = __shfl_xor_sync(FULL, bk, o);
         unsigned long long i2 = __shfl_xor_sync(FULL, bi, o);
         unsigned long long n2v = __shfl_xor_sync(FULL, nan, o);
-        better<MAX>(bk, bi, k2, i2);
+        if (ARG) better<MAX>(bk, bi, k2, i2);
+        else if (i2 != ~0ull) {
+            bk = MAX ? max(bk, k2) : min(bk, k2);
+            bi = 0;
+        }
         nan = n2v < nan ? n2v : nan;
     }
     __shared__ ExtState ws[8];
@@ -231,7 +281,11 @@ __global__ void __launch_bounds__(256) extreme_kernel(const long long *__restric
     __syncthreads();
     if (threadIdx.x == 0) {
         for (int w = 1; w < 8; ++w) {
-            better<MAX>(bk, bi, ws[w].key, ws[w].idx);
+            if (ARG) better<MAX>(bk, bi, ws[w].key, ws[w].idx);
+            else if (ws[w].idx != ~0ull) {
+                bk = MAX ? max(bk, ws[w].key) : min(bk, ws[w].key);
+                bi = 0;
+            }
             if (ws[w].nan_idx < nan) nan = ws[w].nan_idx;
         }
         partials[blockIdx.x] = ExtState{bk, bi, nan, 0};
@@ -242,7 +296,13 @@ __global__ void __launch_bounds__(256) extreme_kernel(const long long *__restric
         unsigned long long i = s.seen ? s.idx : ~0ull, nn = s.nan_idx;
         for (unsigned b = 0; b < gridDim.x; ++b) {
             ExtState p = partials[b];
-            if (p.idx != ~0ull) better<MAX>(k, i, p.key, p.idx + base);
+            if (p.idx != ~0ull) {
+                if (ARG) better<MAX>(k, i, p.key, p.idx + base);
+                else {
+                    k = (i == ~0ull) ? p.key : (MAX ? max(k, p.key) : min(k, p.key));
+                    i = 0;
+                }
+            }
             if (p.nan_idx != ~0ull && p.nan_idx + base < nn) nn = p.nan_idx + base;
         }
         *state = ExtState{k, i, nn, 1};
@@ -270,10 +330,19 @@ struct ExtremeReducer : DevReducer {
         auto *s = static_cast<ExtState *>(state);
         const long long *x = static_cast<const long long *>(args[0].a->data());
         bool f = type == VKC_F64;
-        if (max && f) extreme_kernel<true, true><<<grid, 256, 0, ctx->stream>>>(x, n, consumed, p, ctx->counters + 1, s);
-        else if (max) extreme_kernel<true, false><<<grid, 256, 0, ctx->stream>>>(x, n, consumed, p, ctx->counters + 1, s);
-        else if (f) extreme_kernel<false, true><<<grid, 256, 0, ctx->stream>>>(x, n, consumed, p, ctx->counters + 1, s);
-        else extreme_kernel<false, false><<<grid, 256, 0, ctx->stream>>>(x, n, consumed, p, ctx->counters + 1, s);
+#define EXT_LAUNCH(MX, F, A) extreme_kernel<MX, F, A><<<grid, 256, 0, ctx->stream>>>(x, n, consumed, p, ctx->counters + 1, s)
+        if (arg) {
+            if (max && f) EXT_LAUNCH(true, true, true);
+            else if (max) EXT_LAUNCH(true, false, true);
+            else if (f) EXT_LAUNCH(false, true, true);
+            else EXT_LAUNCH(false, false, true);
+        } else {
+            if (max && f) EXT_LAUNCH(true, true, false);
+            else if (max) EXT_LAUNCH(true, false, false);
+            else if (f) EXT_LAUNCH(false, true, false);
+            else EXT_LAUNCH(false, false, false);
+        }
+#undef EXT_LAUNCH
         consumed += static_cast<unsigned long long>(n);
         return launched(ctx, "extreme");
     }

@@ -1,7 +1,7 @@
 // Scans: scan_add_i64 and scan_by_add_i64 (src/kernels/scalar/scan.rs:284-326), plus prev_i64
 // (scan.rs:16-48).
 //
-// One pass with decoupled lookback over 4096-row tiles. scan_by uses the segmented operator
+// One pass with decoupled lookback over 8192-row tiles. scan_by uses the segmented operator
 // on (starts-a-segment, sum): (f1, v1) then (f2, v2) = (f1 | f2, f2 ? v2 : v1 + v2). Row 0 of
 // the array always starts a segment; a later update continues the segment of the previous
 // one unless its first start byte says otherwise, as Scan::update does.
@@ -13,7 +13,7 @@
 
 namespace vkc {
 
-constexpr int SC_THREADS = 256;
+constexpr int SC_THREADS = 512;
 constexpr int SC_ITEMS = 16;
 constexpr int SC_TILE = SC_THREADS * SC_ITEMS;
 
@@ -46,7 +46,7 @@ constexpr int SC_VEC = 4;
 constexpr int SC_ROWS = SC_ITEMS / SC_VEC;
 
 template <bool BY, bool ALIGNED>
-__global__ void __launch_bounds__(SC_THREADS) scan_kernel(const unsigned long long *__restrict__ x,
+__global__ void __launch_bounds__(SC_THREADS, 2) scan_kernel(const unsigned long long *__restrict__ x,
                                                           const unsigned char *__restrict__ starts,
                                                           unsigned long long *__restrict__ out, int64_t n,
                                                           int tiles, LookbackTiles<Seg> lb, unsigned epoch,
@@ -56,47 +56,62 @@ __global__ void __launch_bounds__(SC_THREADS) scan_kernel(const unsigned long lo
     // finishes last rewrites it, after every block has read it.
     const bool seen = state->seen != 0;
     const unsigned long long carried = state->last;
+    constexpr int SLICE = 32 * SC_ITEMS;  // rows of one warp
+    // Each warp stages its slice's partial results (sums since the slice start or the last
+    // segment start) and whether a segment started at or before each row, so no row value
+    // waits in registers while the block waits for its prefix.
+    extern __shared__ __align__(16) unsigned char scan_smem[];
+    unsigned long long *s_val = reinterpret_cast<unsigned long long *>(scan_smem);
+    unsigned char *s_has = scan_smem + sizeof(unsigned long long) * SC_TILE;
     __shared__ Seg s_warp[SC_THREADS / 32];
     __shared__ Seg s_prefix;
     const int tile = take_ticket(counters);
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int64_t wbase = static_cast<int64_t>(tile) * SC_TILE + static_cast<int64_t>(w) * (32 * SC_ITEMS);
+    const int64_t wbase = static_cast<int64_t>(tile) * SC_TILE + static_cast<int64_t>(w) * SLICE;
 
-    unsigned long long v[SC_ROWS][SC_VEC];
-    unsigned has = 0;  // bit 4r+k: a segment start at or before item k of row r within the warp slice
-    Seg carry{0, 0};   // the warp slice so far
+    // Every row's load is issued before any is used: the loads of a thread are all in flight.
+    unsigned long long vv[SC_ROWS][SC_VEC];
+    unsigned ff = 0;  // start flags, 4 bits per row
 #pragma unroll
     for (int r = 0; r < SC_ROWS; ++r) {
         const int64_t i0 = wbase + r * (32 * SC_VEC) + lane * SC_VEC;
-        unsigned f = 0;
         if (ALIGNED && i0 + SC_VEC <= n) {
             ulonglong4_32a u = *reinterpret_cast<const ulonglong4_32a *>(x + i0);
-            v[r][0] = u.x;
-            v[r][1] = u.y;
-            v[r][2] = u.z;
-            v[r][3] = u.w;
+            vv[r][0] = u.x;
+            vv[r][1] = u.y;
+            vv[r][2] = u.z;
+            vv[r][3] = u.w;
             if (BY) {
                 unsigned m = *reinterpret_cast<const unsigned *>(starts + i0);
 #pragma unroll
                 for (int k = 0; k < SC_VEC; ++k)
-                    if ((m >> (8 * k)) & 0xffu) f |= 1u << k;
+                    if ((m >> (8 * k)) & 0xffu) ff |= 1u << (r * SC_VEC + k);
             }
         } else {
 #pragma unroll
             for (int k = 0; k < SC_VEC; ++k) {
                 bool in = i0 + k < n;
-                v[r][k] = in ? x[i0 + k] : 0ull;
-                if (BY && in && starts[i0 + k]) f |= 1u << k;
+                vv[r][k] = in ? x[i0 + k] : 0ull;
+                if (BY && in && starts[i0 + k]) ff |= 1u << (r * SC_VEC + k);
             }
         }
+    }
+    Seg carry{0, 0};  // the warp slice so far
+#pragma unroll
+    for (int r = 0; r < SC_ROWS; ++r) {
+        const int64_t i0 = wbase + r * (32 * SC_VEC) + lane * SC_VEC;
+        unsigned long long v[SC_VEC];
+#pragma unroll
+        for (int k = 0; k < SC_VEC; ++k) v[k] = vv[r][k];
+        unsigned f = (ff >> (r * SC_VEC)) & 0xfu;
         // Row 0 of the array starts a segment whatever its byte (scan.rs:300-308).
         if (i0 == 0 && !seen) f |= 1u;
-        // Lane-local inclusive segmented scan of the 4 items.
+        // Lane-local inclusive segmented scan of the 4 rows.
         Seg loc{0, 0};
 #pragma unroll
         for (int k = 0; k < SC_VEC; ++k) {
-            loc = seg_op(loc, Seg{v[r][k], (f >> k) & 1u});
-            v[r][k] = loc.sum;
+            loc = seg_op(loc, Seg{v[k], (f >> k) & 1u});
+            v[k] = loc.sum;
         }
         // Warp inclusive scan of the lane partials.
         Seg inc = loc;
@@ -107,17 +122,23 @@ __global__ void __launch_bounds__(SC_THREADS) scan_kernel(const unsigned long lo
         }
         Seg ex{__shfl_up_sync(FULL, inc.sum, 1), __shfl_up_sync(FULL, inc.start, 1)};
         if (lane == 0) ex = Seg{0, 0};
-        Seg pre = seg_op(carry, ex);  // the warp slice before this lane's items
-        // Items before the lane's first start add the prefix; `has` records whether the
-        // warp slice has a start at or before the item.
-        unsigned first = f ? __ffs(f) - 1 : SC_VEC;
+        const Seg pre = seg_op(carry, ex);  // the warp slice before this lane's rows
+        const unsigned first = f ? __ffs(f) - 1 : SC_VEC;
+        const int j0 = w * SLICE + r * (32 * SC_VEC) + lane * SC_VEC;
+        unsigned hasw = 0;
 #pragma unroll
         for (int k = 0; k < SC_VEC; ++k) {
-            if (static_cast<unsigned>(k) < first) v[r][k] += pre.sum;
-            if (static_cast<unsigned>(k) >= first || pre.start) has |= 1u << (r * SC_VEC + k);
+            if (static_cast<unsigned>(k) < first) v[k] += pre.sum;
+            if (static_cast<unsigned>(k) >= first || pre.start) hasw |= 1u << (8 * k);
         }
-        Seg row_total = __shfl_sync_v(inc, 31);
-        carry = seg_op(carry, row_total);
+        ulonglong4_32a sv;
+        sv.x = v[0];
+        sv.y = v[1];
+        sv.z = v[2];
+        sv.w = v[3];
+        *reinterpret_cast<ulonglong4_32a *>(s_val + j0) = sv;
+        *reinterpret_cast<unsigned *>(s_has + j0) = hasw;
+        carry = seg_op(carry, __shfl_sync_v(inc, 31));
     }
     if (lane == 0) s_warp[w] = carry;
     __syncthreads();
@@ -132,30 +153,30 @@ __global__ void __launch_bounds__(SC_THREADS) scan_kernel(const unsigned long lo
         Seg ex{__shfl_up_sync(FULL, inc.sum, 1), __shfl_up_sync(FULL, inc.start, 1)};
         if (lane == 0) ex = Seg{0, 0};
         Seg tile_agg = __shfl_sync_v(inc, SC_THREADS / 32 - 1);
+        Seg pre = warp_lookback<4, Seg>(lb, tile, tile_agg, Seg{carried, 0}, Seg{0, 0}, epoch, seg_op, status);
         if (lane < SC_THREADS / 32) s_warp[lane] = ex;
-        Seg pre = warp_lookback<Seg>(lb, tile, tile_agg, Seg{carried, 0}, Seg{0, 0}, epoch, seg_op, status);
         if (lane == 0) s_prefix = pre;
     }
     __syncthreads();
-    // The prefix before the warp slice: the tile's exclusive prefix, then the earlier warps.
-    const Seg before = seg_op(s_prefix, s_warp[w]);
+    // Rows without a segment start before them in their warp slice add the slice's prefix.
+    const unsigned long long before = seg_op(s_prefix, s_warp[w]).sum;
 #pragma unroll
     for (int r = 0; r < SC_ROWS; ++r) {
-#pragma unroll
-        for (int k = 0; k < SC_VEC; ++k)
-            if (!((has >> (r * SC_VEC + k)) & 1u)) v[r][k] += before.sum;
+        const int j0 = w * SLICE + r * (32 * SC_VEC) + lane * SC_VEC;
         const int64_t i0 = wbase + r * (32 * SC_VEC) + lane * SC_VEC;
+        ulonglong4_32a u = *reinterpret_cast<const ulonglong4_32a *>(s_val + j0);
+        const unsigned hasw = *reinterpret_cast<const unsigned *>(s_has + j0);
+        if (!(hasw & 0xffu)) u.x += before;
+        if (!(hasw & 0xff00u)) u.y += before;
+        if (!(hasw & 0xff0000u)) u.z += before;
+        if (!(hasw & 0xff000000u)) u.w += before;
         if (ALIGNED && i0 + SC_VEC <= n) {
-            ulonglong4_32a u;
-            u.x = v[r][0];
-            u.y = v[r][1];
-            u.z = v[r][2];
-            u.w = v[r][3];
             *reinterpret_cast<ulonglong4_32a *>(out + i0) = u;
         } else {
+            unsigned long long e[4] = {u.x, u.y, u.z, u.w};
 #pragma unroll
             for (int k = 0; k < SC_VEC; ++k)
-                if (i0 + k < n) out[i0 + k] = v[r][k];
+                if (i0 + k < n) out[i0 + k] = e[k];
         }
     }
     // The last row's output, the last tile's inclusive value, is the carried state.
@@ -165,13 +186,22 @@ __global__ void __launch_bounds__(SC_THREADS) scan_kernel(const unsigned long lo
     }
 }
 
+// Dynamic shared memory of scan_kernel: the staged rows and their start flags.
+constexpr size_t SC_SMEM = (sizeof(unsigned long long) + 1) * SC_TILE;
+
+template <bool BY, bool ALIGNED> static void scan_configure() {
+    static bool configured = false;
+    if (!configured) {
+        cudaFuncSetAttribute(scan_kernel<BY, ALIGNED>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             static_cast<int>(SC_SMEM));
+        configured = true;
+    }
+}
+
 struct ScanImpl : ScannerImpl {
     bool by;
     ScanState *state = nullptr;
-    cudaStream_t stream = nullptr;
-    ~ScanImpl() override {
-        if (state) cudaFreeAsync(state, stream);
-    }
+    DeviceMem mem;  // owns `state`
     // scan.rs:228-282 (tile_rows): arity, kinds, then destination rows.
     vkc_status update(vkc_ctx *ctx, const Arg *args, int nargs, vkc_array *out) override {
         vkc_status st;
@@ -199,22 +229,34 @@ struct ScanImpl : ScannerImpl {
         auto *o = static_cast<unsigned long long *>(out->data());
         bool aligned = (reinterpret_cast<uintptr_t>(x) & 31) == 0 && (reinterpret_cast<uintptr_t>(o) & 31) == 0 &&
                        (reinterpret_cast<uintptr_t>(s) & 3) == 0;
-        if (by && aligned) scan_kernel<true, true><<<tiles, SC_THREADS, 0, ctx->stream>>>(x, s, o, n, tiles, lb, epoch, state, ctx->counters, ctx->status);
-        else if (by) scan_kernel<true, false><<<tiles, SC_THREADS, 0, ctx->stream>>>(x, s, o, n, tiles, lb, epoch, state, ctx->counters, ctx->status);
-        else if (aligned) scan_kernel<false, true><<<tiles, SC_THREADS, 0, ctx->stream>>>(x, s, o, n, tiles, lb, epoch, state, ctx->counters, ctx->status);
-        else scan_kernel<false, false><<<tiles, SC_THREADS, 0, ctx->stream>>>(x, s, o, n, tiles, lb, epoch, state, ctx->counters, ctx->status);
+        if (by && aligned) scan_configure<true, true>(), scan_kernel<true, true><<<tiles, SC_THREADS, SC_SMEM, ctx->stream>>>(x, s, o, n, tiles, lb, epoch, state, ctx->counters, ctx->status);
+        else if (by) scan_configure<true, false>(), scan_kernel<true, false><<<tiles, SC_THREADS, SC_SMEM, ctx->stream>>>(x, s, o, n, tiles, lb, epoch, state, ctx->counters, ctx->status);
+        else if (aligned) scan_configure<false, true>(), scan_kernel<false, true><<<tiles, SC_THREADS, SC_SMEM, ctx->stream>>>(x, s, o, n, tiles, lb, epoch, state, ctx->counters, ctx->status);
+        else scan_configure<false, false>(), scan_kernel<false, false><<<tiles, SC_THREADS, SC_SMEM, ctx->stream>>>(x, s, o, n, tiles, lb, epoch, state, ctx->counters, ctx->status);
         return launched(ctx, "scan");
     }
 };
 
+// A zeroed ScanState on the context's stream, owned by `mem`.
+static bool alloc_scan_state(vkc_ctx *ctx, ScanState **state, DeviceMem *mem) {
+    if (cudaMallocAsync(reinterpret_cast<void **>(state), sizeof(ScanState), ctx->stream) != cudaSuccess) {
+        cudaGetLastError();
+        *state = nullptr;
+        return false;
+    }
+    mem->ptr = *state;
+    mem->box = ctx->box;
+    if (cudaMemsetAsync(*state, 0, sizeof(ScanState), ctx->stream) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return true;
+}
+
 template <bool BY> static ScannerImpl *make_scan(vkc_ctx *ctx) {
     auto *s = new ScanImpl;
     s->by = BY;
-    s->stream = ctx->stream;
-    if (cudaMallocAsync(reinterpret_cast<void **>(&s->state), sizeof(ScanState), ctx->stream) != cudaSuccess ||
-        cudaMemsetAsync(s->state, 0, sizeof(ScanState), ctx->stream) != cudaSuccess) {
-        cudaGetLastError();
-        s->state = nullptr;
+    if (!alloc_scan_state(ctx, &s->state, &s->mem)) {
         delete s;
         return nullptr;
     }
@@ -239,10 +281,7 @@ __global__ void prev_carry(const unsigned long long *x, int64_t n, ScanState *st
 // last row.
 struct PrevImpl : ScannerImpl {
     ScanState *state = nullptr;
-    cudaStream_t stream = nullptr;
-    ~PrevImpl() override {
-        if (state) cudaFreeAsync(state, stream);
-    }
+    DeviceMem mem;  // owns `state`
     vkc_status update(vkc_ctx *ctx, const Arg *args, int nargs, vkc_array *out) override {
         vkc_status st;
         if (nargs != 2) return fail(ctx, VKC_RUNTIME, arity_error(2, nargs));
@@ -265,11 +304,7 @@ struct PrevImpl : ScannerImpl {
 
 static ScannerImpl *make_prev(vkc_ctx *ctx) {
     auto *s = new PrevImpl;
-    s->stream = ctx->stream;
-    if (cudaMallocAsync(reinterpret_cast<void **>(&s->state), sizeof(ScanState), ctx->stream) != cudaSuccess ||
-        cudaMemsetAsync(s->state, 0, sizeof(ScanState), ctx->stream) != cudaSuccess) {
-        cudaGetLastError();
-        s->state = nullptr;
+    if (!alloc_scan_state(ctx, &s->state, &s->mem)) {
         delete s;
         return nullptr;
     }
@@ -307,7 +342,7 @@ void register_scan(std::vector<KernelDef> &t) {
 namespace vkc {
 
 // Header (ticket counters, status, carried state), the tile flags, then the tile aggregates
-// and inclusive prefixes. 2.5 MiB holds the 65,536 tiles of 2^28 rows.
+// and inclusive prefixes. 1.13 MiB holds the 32,768 tiles of 2^28 rows.
 constexpr int64_t NOALLOC_MAX_ROWS = int64_t(1) << 28;
 constexpr int64_t NOALLOC_MAX_TILES = NOALLOC_MAX_ROWS / SC_TILE;
 constexpr size_t NOALLOC_HEADER = 512;
@@ -393,10 +428,13 @@ extern "C" vkc_status vkc_scan_add_i64_noalloc(int device, const int64_t *in, in
     const auto *x = reinterpret_cast<const unsigned long long *>(in);
     auto *o = reinterpret_cast<unsigned long long *>(out);
     bool aligned = (reinterpret_cast<uintptr_t>(x) & 31) == 0 && (reinterpret_cast<uintptr_t>(o) & 31) == 0;
-    if (aligned)
-        scan_kernel<false, true><<<tiles, SC_THREADS, 0, s>>>(x, nullptr, o, n, tiles, lb, 1u, state, counters, status);
-    else
-        scan_kernel<false, false><<<tiles, SC_THREADS, 0, s>>>(x, nullptr, o, n, tiles, lb, 1u, state, counters, status);
+    if (aligned) {
+        scan_configure<false, true>();
+        scan_kernel<false, true><<<tiles, SC_THREADS, SC_SMEM, s>>>(x, nullptr, o, n, tiles, lb, 1u, state, counters, status);
+    } else {
+        scan_configure<false, false>();
+        scan_kernel<false, false><<<tiles, SC_THREADS, SC_SMEM, s>>>(x, nullptr, o, n, tiles, lb, 1u, state, counters, status);
+    }
     e = cudaGetLastError();
     if (e != cudaSuccess) return done(VKC_DEVICE, std::string("vkc_scan_add_i64_noalloc: ") + cudaGetErrorString(e));
     // Synchronous, like the other entries: read the status word into host memory.

@@ -1,7 +1,7 @@
 // Selections: filter_<cmp>_f64, compress_T and where (src/kernels/scalar/select.rs:81-104,
 // src/kernels/scalar/fused.rs:225-236).
 //
-// One pass: each 4096-row tile computes its keep flags, the tile's survivor count goes through
+// One pass: each 8192-row tile computes its keep flags, the tile's survivor count goes through
 // a decoupled lookback for the tile's output offset, and the survivors are compacted in shared
 // memory and written out contiguously. The output is the rows in input order, so it does not
 // depend on the tiling (select.rs:36-57 writes the same rows).
@@ -10,7 +10,7 @@
 
 namespace vkc {
 
-constexpr int SEL_THREADS = 256;
+constexpr int SEL_THREADS = 512;
 constexpr int SEL_ITEMS = 16;
 constexpr int SEL_TILE = SEL_THREADS * SEL_ITEMS;
 
@@ -40,44 +40,53 @@ template <int W> struct SelShape {
 };
 
 template <int KIND, int W, bool ALIGNED>
-__global__ void __launch_bounds__(SEL_THREADS) select_kernel(SelArgs a, int tiles,
-                                                             LookbackTiles<unsigned long long> lb,
+__global__ void __launch_bounds__(SEL_THREADS) select_kernel(SelArgs a, int tiles, unsigned long long *words,
                                                              unsigned epoch, unsigned *counters,
                                                              DevStatus *status) {
     using T = typename Word<W>::T;
     using O = typename Word<KIND == SEL_WHERE ? 8 : W>::T;
     constexpr int VEC = SelShape<W>::VEC, ROWS = SelShape<W>::ROWS;
+    constexpr int SLICE = 32 * SEL_ITEMS;  // rows of one warp
+    // Each warp compacts its survivors into its own slice of shared memory row by row, so no
+    // row value waits in registers while the block waits for its offset.
+    extern __shared__ __align__(16) unsigned char sel_smem[];
     __shared__ unsigned s_warp[SEL_THREADS / 32];
-    __shared__ unsigned long long s_prefix;
+    __shared__ unsigned long long s_prefix, s_count;
     const int tile = take_ticket(counters);
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    O *s_out = reinterpret_cast<O *>(sel_smem) + w * SLICE;
     const unsigned lt = (1u << lane) - 1;
-    const int64_t wbase = static_cast<int64_t>(tile) * SEL_TILE + static_cast<int64_t>(w) * (32 * SEL_ITEMS);
+    const int64_t wbase = static_cast<int64_t>(tile) * SEL_TILE + static_cast<int64_t>(w) * SLICE;
 
-    T v[ROWS][VEC];
-    unsigned keep[ROWS];       // VEC bits per row
-    unsigned rank[ROWS];       // survivors before this lane's first item in the row
-    unsigned row_off[ROWS];    // survivors of the warp before the row
-    unsigned total = 0;
+    // Every row's load is issued before any is used: the loads of a thread are all in flight.
+    T vv[ROWS][VEC];
+    if (KIND != SEL_WHERE) {
 #pragma unroll
-    for (int r = 0; r < ROWS; ++r) {
-        const int64_t i0 = wbase + r * (32 * VEC) + lane * VEC;
-        if (KIND != SEL_WHERE) {
+        for (int r = 0; r < ROWS; ++r) {
+            const int64_t i0 = wbase + r * (32 * VEC) + lane * VEC;
             if (ALIGNED && i0 + VEC <= a.n) {
                 uint4 u = __ldcs(reinterpret_cast<const uint4 *>(static_cast<const T *>(a.x) + i0));
                 const T *e = reinterpret_cast<const T *>(&u);
 #pragma unroll
-                for (int k = 0; k < VEC; ++k) v[r][k] = e[k];
+                for (int k = 0; k < VEC; ++k) vv[r][k] = e[k];
             } else {
 #pragma unroll
-                for (int k = 0; k < VEC; ++k) v[r][k] = i0 + k < a.n ? static_cast<const T *>(a.x)[i0 + k] : T(0);
+                for (int k = 0; k < VEC; ++k) vv[r][k] = i0 + k < a.n ? static_cast<const T *>(a.x)[i0 + k] : T(0);
             }
         }
+    }
+    unsigned total = 0;
+#pragma unroll
+    for (int r = 0; r < ROWS; ++r) {
+        const int64_t i0 = wbase + r * (32 * VEC) + lane * VEC;
+        T v[VEC];
+#pragma unroll
+        for (int k = 0; k < VEC; ++k) v[k] = KIND != SEL_WHERE ? vv[r][k] : T(0);
         unsigned bits = 0;
         if (KIND == SEL_FILTER) {
 #pragma unroll
             for (int k = 0; k < VEC; ++k)
-                if (i0 + k < a.n && in_range(a.r, static_cast<unsigned long long>(v[r][k]))) bits |= 1u << k;
+                if (i0 + k < a.n && in_range(a.r, static_cast<unsigned long long>(v[k]))) bits |= 1u << k;
         } else if (ALIGNED && VEC == 16 && i0 + 16 <= a.n) {
             uint4 u = __ldcs(reinterpret_cast<const uint4 *>(a.m + i0));
             unsigned wd[4] = {u.x, u.y, u.z, u.w};
@@ -89,7 +98,6 @@ __global__ void __launch_bounds__(SEL_THREADS) select_kernel(SelArgs a, int tile
             for (int k = 0; k < VEC; ++k)
                 if (i0 + k < a.n && a.m[i0 + k]) bits |= 1u << k;
         }
-        keep[r] = bits;
         // In-order ranks: the lanes before this one, element by element.
         unsigned before = 0, row_total = 0;
 #pragma unroll
@@ -98,8 +106,13 @@ __global__ void __launch_bounds__(SEL_THREADS) select_kernel(SelArgs a, int tile
             before += __popc(m & lt);
             row_total += __popc(m);
         }
-        rank[r] = before;
-        row_off[r] = total;
+        unsigned p = total + before;
+#pragma unroll
+        for (int k = 0; k < VEC; ++k)
+            if ((bits >> k) & 1u) {
+                s_out[p] = KIND == SEL_WHERE ? static_cast<O>(a.base + i0 + k) : static_cast<O>(v[k]);
+                ++p;
+            }
         total += row_total;
     }
     if (lane == 0) s_warp[w] = total;
@@ -111,28 +124,19 @@ __global__ void __launch_bounds__(SEL_THREADS) select_kernel(SelArgs a, int tile
             unsigned y = __shfl_up_sync(FULL, x, o);
             if (lane >= o) x += y;
         }
-        unsigned long long tile_count = __shfl_sync(FULL, x, SEL_THREADS / 32 - 1);
+        const unsigned long long tile_count = __shfl_sync(FULL, x, SEL_THREADS / 32 - 1);
+        unsigned long long pre = warp_lookback_count<4>(words, tile, tile_count, epoch, status);
         if (lane < SEL_THREADS / 32) s_warp[lane] = x - c;  // exclusive over warps
-        auto add = [](unsigned long long p, unsigned long long q) { return p + q; };
-        unsigned long long pre = warp_lookback<unsigned long long>(lb, tile, tile_count, 0ull, 0ull, epoch, add, status);
         if (lane == 0) {
             s_prefix = pre;
+            s_count = tile_count;
             if (tile == tiles - 1) *a.total = pre + tile_count;
         }
     }
     __syncthreads();
+    // Each warp writes its slice's survivors after those of the warps before it.
     O *out = static_cast<O *>(a.out) + s_prefix + s_warp[w];
-#pragma unroll
-    for (int r = 0; r < ROWS; ++r) {
-        unsigned p = row_off[r] + rank[r];
-        const int64_t i0 = wbase + r * (32 * VEC) + lane * VEC;
-#pragma unroll
-        for (int k = 0; k < VEC; ++k)
-            if ((keep[r] >> k) & 1u) {
-                out[p] = KIND == SEL_WHERE ? static_cast<O>(a.base + i0 + k) : static_cast<O>(v[r][k]);
-                ++p;
-            }
-    }
+    for (unsigned i = lane; i < total; i += 32) out[i] = s_out[i];
     release_ticket(counters, tiles);
 }
 
@@ -143,21 +147,28 @@ static vkc_status run_select(vkc_ctx *ctx, SelArgs a, int64_t n, Builder *b) {
     void *p;
     unsigned *flags;
     vkc_status st;
-    if ((st = scratch(ctx, 16 * static_cast<size_t>(tiles) + 256, &p))) return st;
-    if ((st = flag_arena(ctx, static_cast<size_t>(tiles), &flags))) return st;
-    auto *vals = static_cast<unsigned long long *>(p);
-    LookbackTiles<unsigned long long> lb{flags, vals, vals + tiles};
-    a.total = vals + 2 * static_cast<size_t>(tiles);
+    if ((st = scratch(ctx, 256, &p))) return st;
+    if ((st = flag_arena(ctx, 2 * static_cast<size_t>(tiles), &flags))) return st;
+    auto *words = reinterpret_cast<unsigned long long *>(flags);
+    a.total = static_cast<unsigned long long *>(p);
     void *at;
     if ((st = b->reserve(n, &at))) return st;
     a.out = at;
     unsigned epoch = next_epoch(ctx);
     bool aligned = (reinterpret_cast<uintptr_t>(a.x) & 15) == 0 &&
                    (reinterpret_cast<uintptr_t>(a.m) & 15) == 0;
+    using O = typename Word<KIND == SEL_WHERE ? 8 : W>::T;
+    const size_t smem = sizeof(O) * SEL_TILE;
+    static bool configured = false;
+    if (!configured) {
+        cudaFuncSetAttribute(select_kernel<KIND, W, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+        cudaFuncSetAttribute(select_kernel<KIND, W, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+        configured = true;
+    }
     if (aligned)
-        select_kernel<KIND, W, true><<<tiles, SEL_THREADS, 0, ctx->stream>>>(a, tiles, lb, epoch, ctx->counters, ctx->status);
+        select_kernel<KIND, W, true><<<tiles, SEL_THREADS, smem, ctx->stream>>>(a, tiles, words, epoch, ctx->counters, ctx->status);
     else
-        select_kernel<KIND, W, false><<<tiles, SEL_THREADS, 0, ctx->stream>>>(a, tiles, lb, epoch, ctx->counters, ctx->status);
+        select_kernel<KIND, W, false><<<tiles, SEL_THREADS, smem, ctx->stream>>>(a, tiles, words, epoch, ctx->counters, ctx->status);
     if ((st = launched(ctx, "select"))) return st;
     DevStatus ds;
     if ((st = read_status(ctx, &ds))) return st;

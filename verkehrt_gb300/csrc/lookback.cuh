@@ -60,12 +60,15 @@ __device__ __forceinline__ unsigned long long __shfl_sync_v(unsigned long long v
 }
 
 // Warp-parallel decoupled lookback, run by all 32 lanes of one warp: publishes the tile's
-// aggregate, then reads the flags of 32 predecessor tiles per step (lane i reads tile
-// hi - i), combines every aggregate up to the closest inclusive value in one ordered warp
-// reduction, and stops at that inclusive value (or at `init` before tile 0). Publishes the
-// inclusive value and returns the exclusive prefix in every lane. `ident` is the identity of
-// `op`. On a wait that runs out it records a timeout and returns `init`.
-template <class V, class Op>
+// aggregate, then reads the flags of 32*P predecessor tiles per step (lane i reads tiles
+// hi - P*i - j, j < P), combines every aggregate up to the closest inclusive value in one
+// ordered warp reduction, and stops at that inclusive value (or at `init` before tile 0).
+// Publishes the inclusive value and returns the exclusive prefix in every lane. `ident` is
+// the identity of `op`. On a wait that runs out it records a timeout and returns `init`.
+//
+// A step costs two L2 round trips (the flags, then the values), and a tile waits for the
+// tiles before it in launch order, so the window width is what bounds the tile rate.
+template <int P, class V, class Op>
 __device__ V warp_lookback(LookbackTiles<V> lb, int tile, V agg, V init, V ident, unsigned epoch, Op op,
                            DevStatus *status) {
     const int lane = threadIdx.x & 31;
@@ -77,29 +80,50 @@ __device__ V warp_lookback(LookbackTiles<V> lb, int tile, V agg, V init, V ident
     __syncwarp();
     V excl = ident;
     bool have = false;
-    for (int hi = tile - 1;; hi -= 32) {
-        int tp = hi - lane;
-        unsigned f = 0;
+    for (int hi = tile - 1;; hi -= 32 * P) {
+        unsigned f[P];
         bool bad = false;
-        if (tp >= 0) {
-            unsigned it = 0;
-            while (((f = ld_acquire(&lb.flag[tp])) >> 2) != epoch) {
-                if (++it > SPIN_LIMIT) {
-                    set_timeout(status);
-                    bad = true;
-                    break;
+#pragma unroll
+        for (int j = 0; j < P; ++j) {
+            const int tp = hi - P * lane - j;
+            f[j] = 0;
+            if (tp >= 0) {
+                unsigned it = 0;
+                while (((f[j] = ld_acquire(&lb.flag[tp])) >> 2) != epoch) {
+                    if (++it > SPIN_LIMIT) {
+                        set_timeout(status);
+                        bad = true;
+                        break;
+                    }
+                    backoff(it);
                 }
-                backoff(it);
             }
         }
         if (__any_sync(FULL, bad)) return init;
-        bool incl = tp < 0 || (f & 3u) == 2u;
-        unsigned m = __ballot_sync(FULL, incl);
-        int k = m ? __ffs(m) - 1 : 32;
+        // The lane's closest inclusive item, and the warp's.
+        int jin = P;
+#pragma unroll
+        for (int j = P - 1; j >= 0; --j) {
+            const int tp = hi - P * lane - j;
+            if (tp < 0 || (f[j] & 3u) == 2u) jin = j;
+        }
+        const unsigned m = __ballot_sync(FULL, jin < P);
+        const int kl = m ? __ffs(m) - 1 : 32;  // first lane holding an inclusive item
+        // Lane value: its items from the earliest used one to the latest, in order.
         V v = ident;
-        if (lane < k) v = lb.agg[tp];
-        else if (lane == k) v = tp >= 0 ? lb.inc[tp] : init;
-        // Lane i holds tile hi - i, so the higher lane is the earlier tile.
+        if (lane <= kl) {
+            const int jmax = lane == kl ? jin : P - 1;
+#pragma unroll
+            for (int j = P - 1; j >= 0; --j) {
+                if (j > jmax) continue;
+                const int tp = hi - P * lane - j;
+                V x;
+                if (lane == kl && j == jin) x = tp >= 0 ? lb.inc[tp] : init;
+                else x = lb.agg[tp];
+                v = (j == jmax) ? x : op(v, x);
+            }
+        }
+        // Lane i holds later tiles than lane i + 1.
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
             V other = shfl_down_v(v, o);
@@ -108,13 +132,68 @@ __device__ V warp_lookback(LookbackTiles<V> lb, int tile, V agg, V init, V ident
         V window = __shfl_sync_v(v, 0);
         excl = have ? op(window, excl) : window;
         have = true;
-        if (k < 32) break;
+        if (kl < 32) break;
     }
     if (lane == 0) {
         lb.inc[tile] = op(excl, agg);
         __threadfence();
         st_release(&lb.flag[tile], (epoch << 2) | 2u);
     }
+    return excl;
+}
+
+// Counts in one word: epoch (24 bits) | state (2 bits) | count (38 bits), so a lookback step
+// is a single L2 round trip. Counts must stay below 2^38.
+__device__ __forceinline__ unsigned long long packed_word(unsigned epoch, unsigned state, unsigned long long c) {
+    return (static_cast<unsigned long long>(epoch & 0xffffffu) << 40) | (static_cast<unsigned long long>(state) << 38) | c;
+}
+
+// warp_lookback for additive counts in packed words: `words` holds one word per tile.
+template <int P>
+__device__ unsigned long long warp_lookback_count(unsigned long long *words, int tile, unsigned long long agg,
+                                                  unsigned epoch, DevStatus *status) {
+    const int lane = threadIdx.x & 31;
+    const unsigned long long ep = epoch & 0xffffffu;
+    if (lane == 0) st_release64(words + tile, packed_word(epoch, 1, agg));
+    __syncwarp();
+    unsigned long long excl = 0;
+    for (int hi = tile - 1;; hi -= 32 * P) {
+        unsigned long long w[P];
+        bool bad = false;
+#pragma unroll
+        for (int j = 0; j < P; ++j) {
+            const int tp = hi - P * lane - j;
+            w[j] = packed_word(epoch, 2, 0);  // before tile 0: inclusive zero
+            if (tp >= 0) {
+                unsigned it = 0;
+                while (((w[j] = ld_acquire64(words + tp)) >> 40) != ep) {
+                    if (++it > SPIN_LIMIT) {
+                        set_timeout(status);
+                        bad = true;
+                        break;
+                    }
+                    backoff(it);
+                }
+            }
+        }
+        if (__any_sync(FULL, bad)) return 0;
+        int jin = P;
+#pragma unroll
+        for (int j = P - 1; j >= 0; --j)
+            if (((w[j] >> 38) & 3u) == 2u) jin = j;
+        const unsigned m = __ballot_sync(FULL, jin < P);
+        const int kl = m ? __ffs(m) - 1 : 32;
+        unsigned long long v = 0;
+        if (lane <= kl) {
+            const int jmax = lane == kl ? jin : P - 1;
+#pragma unroll
+            for (int j = 0; j < P; ++j)
+                if (j <= jmax) v += w[j] & ((1ull << 38) - 1);
+        }
+        excl += warp_sum(v);
+        if (kl < 32) break;
+    }
+    if (lane == 0) st_release64(words + tile, packed_word(epoch, 2, excl + agg));
     return excl;
 }
 

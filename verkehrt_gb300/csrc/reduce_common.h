@@ -12,15 +12,13 @@ namespace vkc {
 struct DevReducer : ReducerImpl {
     void *state = nullptr;
     size_t bytes = 0;
-    cudaStream_t stream = nullptr;
-    ~DevReducer() override {
-        if (state) cudaFreeAsync(state, stream);
-    }
+    DeviceMem mem;  // frees `state` on the context's stream, even after the context closed
     // Allocates the zeroed state.
     vkc_status alloc(vkc_ctx *ctx, size_t n) {
-        stream = ctx->stream;
         bytes = n;
         VKC_CUDA(ctx, cudaMallocAsync(&state, n, ctx->stream));
+        mem.ptr = state;
+        mem.box = ctx->box;
         VKC_CUDA(ctx, cudaMemsetAsync(state, 0, n, ctx->stream));
         return VKC_OK;
     }

@@ -11,8 +11,60 @@
 
 namespace vkc {
 
+// Cached free blocks at most this many bytes; frees beyond it go back to the pool.
+constexpr size_t kCacheLimit = size_t(48) << 30;
+
+StreamBox::~StreamBox() {
+    if (stream) {
+        int prev = 0;
+        cudaGetDevice(&prev);
+        cudaSetDevice(device);
+        for (auto &kv : free_blocks) cudaFreeAsync(kv.second, stream);
+        free_blocks.clear();
+        cudaStreamSynchronize(stream);
+        cudaStreamDestroy(stream);
+        cudaSetDevice(prev);
+    }
+}
+
+void *StreamBox::take(size_t bytes, size_t *cls) {
+    *cls = size_class(bytes);
+    std::lock_guard<std::mutex> lock(mu);
+    // The smallest cached block of the class or up to a quarter larger.
+    auto it = free_blocks.lower_bound(*cls);
+    if (it == free_blocks.end() || it->first > *cls + *cls / 4) return nullptr;
+    void *p = it->second;
+    *cls = it->first;
+    cached -= it->first;
+    free_blocks.erase(it);
+    return p;
+}
+
+void StreamBox::release_all() {
+    std::lock_guard<std::mutex> lock(mu);
+    for (auto &kv : free_blocks) cudaFreeAsync(kv.second, stream);
+    free_blocks.clear();
+    cached = 0;
+}
+
+void StreamBox::give(void *p, size_t cls) {
+    {
+        std::lock_guard<std::mutex> lock(mu);
+        if (cached + cls <= kCacheLimit) {
+            free_blocks.emplace(cls, p);
+            cached += cls;
+            return;
+        }
+    }
+    cudaFreeAsync(p, stream);
+}
+
+DeviceMem::~DeviceMem() {
+    if (ptr && box) cudaFreeAsync(ptr, box->stream);
+}
+
 Buffer::~Buffer() {
-    if (ptr) cudaFreeAsync(ptr, stream);
+    if (ptr && box) box->give(ptr, bytes);
 }
 
 vkc_status fail(vkc_ctx *ctx, vkc_status st, const std::string &msg) {
@@ -77,7 +129,8 @@ vkc_status pinned(vkc_ctx *ctx, size_t bytes, void **out) {
 }
 
 uint32_t next_epoch(vkc_ctx *ctx) {
-    ctx->epoch = (ctx->epoch + 1) & 0x3fffffffu;
+    // 24 bits: packed lookback words keep the epoch in their top 24 bits.
+    ctx->epoch = (ctx->epoch + 1) & 0xffffffu;
     if (ctx->epoch == 0) {
         if (ctx->flags.ptr)
             cudaMemsetAsync(ctx->flags.ptr, 0, ctx->flags.bytes, ctx->stream);
@@ -119,20 +172,30 @@ vkc_status new_array(vkc_ctx *ctx, vkc_type t, int64_t len, bool zero, vkc_array
                                           " elements is too large");
     size_t bytes = static_cast<size_t>(len) * w;
     auto buf = std::make_shared<Buffer>();
-    buf->stream = ctx->stream;
+    buf->box = ctx->box;
     if (bytes) {
-        // Rounded up so that vector kernels may read the last 16 bytes of any allocation.
-        size_t alloc = (bytes + 255) & ~size_t(255);
-        cudaError_t e = cudaMallocAsync(&buf->ptr, alloc, ctx->stream);
-        if (e != cudaSuccess) {
-            cudaGetLastError();
-            buf->ptr = nullptr;
-            // value.rs:297-307 (try_zeroed).
-            return fail(ctx, VKC_ALLOC,
-                        "cannot allocate an array of " + std::to_string(len) + " elements");
+        // Whole size classes, so vector kernels may read the last 16 bytes of any allocation.
+        size_t cls = 0;
+        buf->ptr = ctx->box->take(bytes, &cls);
+        if (!buf->ptr) {
+            cudaError_t e = cudaMallocAsync(&buf->ptr, cls, ctx->stream);
+            if (e != cudaSuccess) {
+                // Give the cached blocks back to the pool and try once more.
+                cudaGetLastError();
+                ctx->box->release_all();
+                cudaStreamSynchronize(ctx->stream);
+                e = cudaMallocAsync(&buf->ptr, cls, ctx->stream);
+            }
+            if (e != cudaSuccess) {
+                cudaGetLastError();
+                buf->ptr = nullptr;
+                // value.rs:297-307 (try_zeroed).
+                return fail(ctx, VKC_ALLOC,
+                            "cannot allocate an array of " + std::to_string(len) + " elements");
+            }
         }
-        buf->bytes = alloc;
-        if (zero) VKC_CUDA(ctx, cudaMemsetAsync(buf->ptr, 0, alloc, ctx->stream));
+        buf->bytes = cls;
+        if (zero) VKC_CUDA(ctx, cudaMemsetAsync(buf->ptr, 0, cls, ctx->stream));
     }
     vkc_array *a = new vkc_array;
     a->buf = std::move(buf);
@@ -359,6 +422,9 @@ vkc_status vkc_open(int device, vkc_ctx **out) {
         return VKC_DEVICE;
     }
     ctx->stream = ctx->own_stream;
+    ctx->box = std::make_shared<StreamBox>();
+    ctx->box->stream = ctx->own_stream;
+    ctx->box->device = device;
     // Freed blocks stay in the device pool, so per-statement allocations are cheap.
     cudaMemPool_t pool;
     if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
@@ -398,7 +464,8 @@ void vkc_close(vkc_ctx *ctx) {
     if (ctx->status_host) cudaFreeHost(ctx->status_host);
     cudaEventDestroy(ctx->ev_start);
     cudaEventDestroy(ctx->ev_stop);
-    cudaStreamDestroy(ctx->own_stream);
+    // The stream goes with the last allocation that still refers to it.
+    ctx->box.reset();
     delete ctx;
 }
 

@@ -5,7 +5,9 @@
 
 #include <atomic>
 #include <cstdint>
+#include <map>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -35,12 +37,44 @@ inline const char *type_name(vkc_type t) {
     }
 }
 
-// A device allocation shared by an array and its views. Freed stream-ordered on the stream of
-// the context that allocated it.
+// The context's own stream, shared by the context and every allocation freed on it, so the
+// stream outlives the context while arrays, reducers or scanners of that context live on. It
+// also caches freed array blocks by size class: every use of a block is ordered on this one
+// stream, so a block freed by one statement can serve the next without a driver call or a new
+// mapping of pages.
+struct StreamBox {
+    cudaStream_t stream = nullptr;
+    int device = 0;
+    std::multimap<size_t, void *> free_blocks;  // size class -> block
+    size_t cached = 0;
+    std::mutex mu;
+    ~StreamBox();
+    // A block of at least `bytes` (its class size in *cls), or nullptr.
+    void *take(size_t bytes, size_t *cls);
+    // Returns a block of class size `cls` to the cache (or frees it past the cache limit).
+    void give(void *p, size_t cls);
+    // Frees every cached block.
+    void release_all();
+};
+
+// The size class of an allocation: 256-byte multiples below 1 MiB, then 2 MiB multiples.
+inline size_t size_class(size_t bytes) {
+    if (bytes < (size_t(1) << 20)) return (bytes + 255) & ~size_t(255);
+    return (bytes + (size_t(2) << 20) - 1) & ~((size_t(2) << 20) - 1);
+}
+
+// A device allocation freed stream-ordered on its context's stream, whenever it goes.
+struct DeviceMem {
+    void *ptr = nullptr;
+    std::shared_ptr<StreamBox> box;
+    ~DeviceMem();
+};
+
+// A device allocation shared by an array and its views.
 struct Buffer {
     void *ptr = nullptr;
     size_t bytes = 0;
-    cudaStream_t stream = nullptr;
+    std::shared_ptr<StreamBox> box;
     ~Buffer();
 };
 
@@ -82,6 +116,7 @@ struct vkc_ctx {
     int sms = 0;
     cudaStream_t stream = nullptr;
     cudaStream_t own_stream = nullptr;
+    std::shared_ptr<vkc::StreamBox> box;  // owns own_stream
     cudaEvent_t ev_start = nullptr, ev_stop = nullptr;
     std::string err;
     uint64_t launches = 0;
@@ -120,7 +155,7 @@ vkc_status scratch(vkc_ctx *ctx, size_t bytes, void **out);
 vkc_status flag_arena(vkc_ctx *ctx, size_t count, unsigned **out);
 // Pinned host staging of at least `bytes`.
 vkc_status pinned(vkc_ctx *ctx, size_t bytes, void **out);
-// Next lookback epoch (1..2^30-1). Wraps by clearing the scratch arena.
+// Next lookback epoch (1..2^24-1). Wraps by clearing the flag arena.
 uint32_t next_epoch(vkc_ctx *ctx);
 // Reads and clears the device status after the stream's work completes.
 vkc_status read_status(vkc_ctx *ctx, DevStatus *out);
