@@ -115,7 +115,7 @@ __global__ void __launch_bounds__(GI_THREADS) gi_number_kernel(const unsigned *_
     unsigned long long c = __popc(keep), tile_count;
     unsigned long long off = block_exclusive_sum<unsigned long long>(c, &tile_count);
     if (threadIdx.x < 32) {
-        unsigned long long pre = warp_lookback_count<4>(words, tile, tile_count, epoch, st);
+        unsigned long long pre = lookback_publish<4, CountRec>(words, tile, tile_count, 0ull, epoch, st);
         if (threadIdx.x == 0) s_prefix = pre;
     }
     __syncthreads();

@@ -1,21 +1,26 @@
 // Scans: scan_add_i64 and scan_by_add_i64 (src/kernels/scalar/scan.rs:284-326), plus prev_i64
 // (scan.rs:16-48).
 //
-// One pass with decoupled lookback over 8192-row tiles. scan_by uses the segmented operator
-// on (starts-a-segment, sum): (f1, v1) then (f2, v2) = (f1 | f2, f2 ? v2 : v1 + v2). Row 0 of
-// the array always starts a segment; a later update continues the segment of the previous
-// one unless its first start byte says otherwise, as Scan::update does.
+// One persistent pass (tilepass.cuh) over 4096-row tiles: a tile's aggregate is taken while it
+// streams from HBM, the decoupled lookback gives its prefix, and the scanned rows are written
+// when the tile is read again, from L2. scan_by uses the segmented operator on
+// (starts-a-segment, sum): (f1, v1) then (f2, v2) = (f1 | f2, f2 ? v2 : v1 + v2). Row 0 of the
+// array always starts a segment; a later update continues the segment of the previous one
+// unless its first start byte says otherwise, as Scan::update does.
 #include <cstring>
 #include <mutex>
 
-#include "lookback.cuh"
 #include "reduce_common.h"
+#include "tilepass.cuh"
 
 namespace vkc {
 
-constexpr int SC_THREADS = 512;
-constexpr int SC_ITEMS = 16;
-constexpr int SC_TILE = SC_THREADS * SC_ITEMS;
+constexpr int SC_THREADS = 256;
+constexpr int SC_TILE = 4096;
+constexpr int SC_SLICE = SC_TILE / (SC_THREADS / 32);  // rows per warp
+constexpr int SC_VEC = 4;                              // rows per lane per step (one 32-byte load)
+constexpr int SC_STEPS = SC_SLICE / (32 * SC_VEC);
+constexpr int SC_WINDOW = 4;
 
 // A segmented partial: `start` when a segment starts inside it, `sum` since the last start.
 struct Seg {
@@ -33,169 +38,209 @@ struct ScanState {
     unsigned long long seen;
 };
 
-__device__ __forceinline__ Seg shfl_down_v(Seg v, int o) {
-    return Seg{__shfl_down_sync(FULL, v.sum, o), __shfl_down_sync(FULL, v.start, o)};
+__device__ __forceinline__ ulonglong2 ld_relaxed128(const ulonglong2 *p) {
+    ulonglong2 v;
+    asm volatile("ld.relaxed.gpu.global.v2.u64 {%0, %1}, [%2];" : "=l"(v.x), "=l"(v.y) : "l"(p) : "memory");
+    return v;
 }
-__device__ __forceinline__ Seg __shfl_sync_v(Seg v, int src) {
-    return Seg{__shfl_sync(FULL, v.sum, src), __shfl_sync(FULL, v.start, src)};
+__device__ __forceinline__ void st_relaxed128(ulonglong2 *p, ulonglong2 v) {
+    asm volatile("st.relaxed.gpu.global.v2.u64 [%0], {%1, %2};" ::"l"(p), "l"(v.x), "l"(v.y) : "memory");
 }
 
-// Per warp, 4 rows of 128 consecutive rows of the input: lane l holds rows 4l..4l+3 of each
-// (one 32-byte load), so loads and stores are coalesced and row order is (row, lane, item).
-constexpr int SC_VEC = 4;
-constexpr int SC_ROWS = SC_ITEMS / SC_VEC;
+// A 32-byte load marked evict-first (the last read of these rows).
+__device__ __forceinline__ ulonglong4_32a ldcs256(const unsigned long long *p) {
+    ulonglong4_32a v;
+    asm volatile("ld.global.cs.v4.u64 {%0, %1, %2, %3}, [%4];" : "=l"(v.x), "=l"(v.y), "=l"(v.z), "=l"(v.w) : "l"(p));
+    return v;
+}
 
-template <bool BY, bool ALIGNED>
-__global__ void __launch_bounds__(SC_THREADS, 2) scan_kernel(const unsigned long long *__restrict__ x,
-                                                          const unsigned char *__restrict__ starts,
-                                                          unsigned long long *__restrict__ out, int64_t n,
-                                                          int tiles, LookbackTiles<Seg> lb, unsigned epoch,
-                                                          ScanState *state, unsigned *counters,
-                                                          DevStatus *status) {
-    // The carried state is read once, before this block publishes anything; the block that
-    // finishes last rewrites it, after every block has read it.
-    const bool seen = state->seen != 0;
-    const unsigned long long carried = state->last;
-    constexpr int SLICE = 32 * SC_ITEMS;  // rows of one warp
-    // Each warp stages its slice's partial results (sums since the slice start or the last
-    // segment start) and whether a segment started at or before each row, so no row value
-    // waits in registers while the block waits for its prefix.
-    extern __shared__ __align__(16) unsigned char scan_smem[];
-    unsigned long long *s_val = reinterpret_cast<unsigned long long *>(scan_smem);
-    unsigned char *s_has = scan_smem + sizeof(unsigned long long) * SC_TILE;
-    __shared__ Seg s_warp[SC_THREADS / 32];
-    __shared__ Seg s_prefix;
-    const int tile = take_ticket(counters);
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int64_t wbase = static_cast<int64_t>(tile) * SC_TILE + static_cast<int64_t>(w) * SLICE;
+// Lookback record of a Seg in two words, each carrying the epoch and the state: the start
+// flag and the high half of the sum in one, the low half in the other. Each word is read or
+// written whole, so a record read in the middle of its update from aggregate to inclusive
+// shows two states and is polled again.
+struct SegRec {
+    using V = Seg;
+    using W = ulonglong2;
+    __device__ static V ident() { return Seg{0, 0}; }
+    __device__ static V op(V a, V b) { return seg_op(a, b); }
+    __device__ static W make(unsigned ep, unsigned state, V v) {
+        const unsigned long long tag = (static_cast<unsigned long long>(ep & 0xffffffu) << 40) |
+                                       (static_cast<unsigned long long>(state) << 38);
+        return W{tag | ((v.start & 1ull) << 37) | (v.sum >> 32), tag | (v.sum & 0xffffffffull)};
+    }
+    __device__ static bool ready(W w, unsigned ep) {
+        const unsigned long long e = ep & 0xffffffu;
+        return (w.x >> 40) == e && (w.y >> 40) == e && ((w.x >> 38) & 3u) == ((w.y >> 38) & 3u);
+    }
+    __device__ static unsigned state(W w) { return static_cast<unsigned>(w.x >> 38) & 3u; }
+    __device__ static V value(W w) {
+        return Seg{((w.x & 0xffffffffull) << 32) | (w.y & 0xffffffffull), (w.x >> 37) & 1ull};
+    }
+    __device__ static W load(const W *p) { return ld_relaxed128(p); }
+    __device__ static void store(W *p, W w) { st_relaxed128(p, w); }
+    __device__ static V shfl_up(V v, int o) {
+        return Seg{__shfl_up_sync(FULL, v.sum, o), __shfl_up_sync(FULL, v.start, o)};
+    }
+    __device__ static V shfl(V v, int src) { return Seg{__shfl_sync(FULL, v.sum, src), __shfl_sync(FULL, v.start, src)}; }
+    __device__ static V shfl_down(V v, int o) {
+        return Seg{__shfl_down_sync(FULL, v.sum, o), __shfl_down_sync(FULL, v.start, o)};
+    }
+};
 
-    // Every row's load is issued before any is used: the loads of a thread are all in flight.
-    unsigned long long vv[SC_ROWS][SC_VEC];
-    unsigned ff = 0;  // start flags, 4 bits per row
-#pragma unroll
-    for (int r = 0; r < SC_ROWS; ++r) {
-        const int64_t i0 = wbase + r * (32 * SC_VEC) + lane * SC_VEC;
+// A scan as a tile pass. A warp's slice is SC_SLICE consecutive rows, read in SC_STEPS steps of
+// 128 rows; in a step lane l holds rows 4l..4l+3 (one 32-byte load), so loads and stores are
+// coalesced and row order is (step, lane, item).
+template <bool BY, bool ALIGNED> struct ScanPass {
+    static constexpr int THREADS = SC_THREADS;
+    using R = SegRec;
+    using V = Seg;
+
+    const unsigned long long *x;
+    const unsigned char *starts;
+    unsigned long long *out;
+    int64_t n;
+    bool seen;  // an earlier update saw rows: row 0 continues its segment
+
+    // The rows of one step and their start flags (bit k: row 4l + k). Row 0 of the array
+    // starts a segment whatever its byte (scan.rs:300-308).
+    __device__ __forceinline__ void load(int64_t i0, unsigned long long (&v)[SC_VEC], unsigned &f, bool stream) const {
+        f = 0;
         if (ALIGNED && i0 + SC_VEC <= n) {
-            ulonglong4_32a u = *reinterpret_cast<const ulonglong4_32a *>(x + i0);
-            vv[r][0] = u.x;
-            vv[r][1] = u.y;
-            vv[r][2] = u.z;
-            vv[r][3] = u.w;
+            const ulonglong4_32a u = stream ? ldcs256(x + i0) : *reinterpret_cast<const ulonglong4_32a *>(x + i0);
+            v[0] = u.x;
+            v[1] = u.y;
+            v[2] = u.z;
+            v[3] = u.w;
             if (BY) {
-                unsigned m = *reinterpret_cast<const unsigned *>(starts + i0);
+                const unsigned m = *reinterpret_cast<const unsigned *>(starts + i0);
 #pragma unroll
                 for (int k = 0; k < SC_VEC; ++k)
-                    if ((m >> (8 * k)) & 0xffu) ff |= 1u << (r * SC_VEC + k);
+                    if ((m >> (8 * k)) & 0xffu) f |= 1u << k;
             }
         } else {
 #pragma unroll
             for (int k = 0; k < SC_VEC; ++k) {
-                bool in = i0 + k < n;
-                vv[r][k] = in ? x[i0 + k] : 0ull;
-                if (BY && in && starts[i0 + k]) ff |= 1u << (r * SC_VEC + k);
+                const bool in = i0 + k < n;
+                v[k] = in ? x[i0 + k] : 0ull;
+                if (BY && in && starts[i0 + k]) f |= 1u << k;
             }
         }
+        if (BY && i0 == 0 && !seen) f |= 1u;
     }
-    Seg carry{0, 0};  // the warp slice so far
+
+    // The slice aggregate: the sum of the rows from the slice's last segment start on (of all
+    // rows when none starts), which needs no ordered combination across lanes.
+    __device__ Seg count(int tile) const {
+        const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+        const int64_t base = static_cast<int64_t>(tile) * SC_TILE + static_cast<int64_t>(w) * SC_SLICE;
+        unsigned long long v[SC_STEPS][SC_VEC];
+        unsigned f[SC_STEPS];
 #pragma unroll
-    for (int r = 0; r < SC_ROWS; ++r) {
-        const int64_t i0 = wbase + r * (32 * SC_VEC) + lane * SC_VEC;
-        unsigned long long v[SC_VEC];
+        for (int s = 0; s < SC_STEPS; ++s) load(base + s * (32 * SC_VEC) + lane * SC_VEC, v[s], f[s], false);
+        if (!BY) {
+            unsigned long long t = 0;
 #pragma unroll
-        for (int k = 0; k < SC_VEC; ++k) v[k] = vv[r][k];
-        unsigned f = (ff >> (r * SC_VEC)) & 0xfu;
-        // Row 0 of the array starts a segment whatever its byte (scan.rs:300-308).
-        if (i0 == 0 && !seen) f |= 1u;
-        // Lane-local inclusive segmented scan of the 4 rows.
-        Seg loc{0, 0};
+            for (int s = 0; s < SC_STEPS; ++s)
 #pragma unroll
-        for (int k = 0; k < SC_VEC; ++k) {
-            loc = seg_op(loc, Seg{v[k], (f >> k) & 1u});
-            v[k] = loc.sum;
+                for (int k = 0; k < SC_VEC; ++k) t += v[s][k];
+            return Seg{warp_sum(t), 0};
         }
-        // Warp inclusive scan of the lane partials.
-        Seg inc = loc;
+        // The last start in the slice, as a position in row order (0 = none).
+        unsigned last = 0;
 #pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            Seg y{__shfl_up_sync(FULL, inc.sum, o), __shfl_up_sync(FULL, inc.start, o)};
-            if (lane >= o) inc = seg_op(y, inc);
-        }
-        Seg ex{__shfl_up_sync(FULL, inc.sum, 1), __shfl_up_sync(FULL, inc.start, 1)};
-        if (lane == 0) ex = Seg{0, 0};
-        const Seg pre = seg_op(carry, ex);  // the warp slice before this lane's rows
-        const unsigned first = f ? __ffs(f) - 1 : SC_VEC;
-        const int j0 = w * SLICE + r * (32 * SC_VEC) + lane * SC_VEC;
-        unsigned hasw = 0;
-#pragma unroll
-        for (int k = 0; k < SC_VEC; ++k) {
-            if (static_cast<unsigned>(k) < first) v[k] += pre.sum;
-            if (static_cast<unsigned>(k) >= first || pre.start) hasw |= 1u << (8 * k);
-        }
-        ulonglong4_32a sv;
-        sv.x = v[0];
-        sv.y = v[1];
-        sv.z = v[2];
-        sv.w = v[3];
-        *reinterpret_cast<ulonglong4_32a *>(s_val + j0) = sv;
-        *reinterpret_cast<unsigned *>(s_has + j0) = hasw;
-        carry = seg_op(carry, __shfl_sync_v(inc, 31));
-    }
-    if (lane == 0) s_warp[w] = carry;
-    __syncthreads();
-    if (w == 0) {
-        // Exclusive segmented scan over the warps, then the lookback over tiles.
-        Seg c = lane < SC_THREADS / 32 ? s_warp[lane] : Seg{0, 0}, inc = c;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            Seg y{__shfl_up_sync(FULL, inc.sum, o), __shfl_up_sync(FULL, inc.start, o)};
-            if (lane >= o) inc = seg_op(y, inc);
-        }
-        Seg ex{__shfl_up_sync(FULL, inc.sum, 1), __shfl_up_sync(FULL, inc.start, 1)};
-        if (lane == 0) ex = Seg{0, 0};
-        Seg tile_agg = __shfl_sync_v(inc, SC_THREADS / 32 - 1);
-        Seg pre = warp_lookback<4, Seg>(lb, tile, tile_agg, Seg{carried, 0}, Seg{0, 0}, epoch, seg_op, status);
-        if (lane < SC_THREADS / 32) s_warp[lane] = ex;
-        if (lane == 0) s_prefix = pre;
-    }
-    __syncthreads();
-    // Rows without a segment start before them in their warp slice add the slice's prefix.
-    const unsigned long long before = seg_op(s_prefix, s_warp[w]).sum;
-#pragma unroll
-    for (int r = 0; r < SC_ROWS; ++r) {
-        const int j0 = w * SLICE + r * (32 * SC_VEC) + lane * SC_VEC;
-        const int64_t i0 = wbase + r * (32 * SC_VEC) + lane * SC_VEC;
-        ulonglong4_32a u = *reinterpret_cast<const ulonglong4_32a *>(s_val + j0);
-        const unsigned hasw = *reinterpret_cast<const unsigned *>(s_has + j0);
-        if (!(hasw & 0xffu)) u.x += before;
-        if (!(hasw & 0xff00u)) u.y += before;
-        if (!(hasw & 0xff0000u)) u.z += before;
-        if (!(hasw & 0xff000000u)) u.w += before;
-        if (ALIGNED && i0 + SC_VEC <= n) {
-            *reinterpret_cast<ulonglong4_32a *>(out + i0) = u;
-        } else {
-            unsigned long long e[4] = {u.x, u.y, u.z, u.w};
+        for (int s = 0; s < SC_STEPS; ++s)
 #pragma unroll
             for (int k = 0; k < SC_VEC; ++k)
-                if (i0 + k < n) out[i0 + k] = e[k];
+                if ((f[s] >> k) & 1u) last = (s * 32 + lane) * SC_VEC + k + 1;
+        last = __reduce_max_sync(FULL, last);
+        unsigned long long t = 0;
+#pragma unroll
+        for (int s = 0; s < SC_STEPS; ++s)
+#pragma unroll
+            for (int k = 0; k < SC_VEC; ++k)
+                if (static_cast<unsigned>((s * 32 + lane) * SC_VEC + k + 1) >= last) t += v[s][k];
+        return Seg{warp_sum(t), last != 0};
+    }
+
+    __device__ void write(int tile, Seg carry) const {
+        const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+        const int64_t base = static_cast<int64_t>(tile) * SC_TILE + static_cast<int64_t>(w) * SC_SLICE;
+        unsigned long long v[SC_STEPS][SC_VEC];
+        unsigned f[SC_STEPS];
+#pragma unroll
+        for (int s = 0; s < SC_STEPS; ++s) load(base + s * (32 * SC_VEC) + lane * SC_VEC, v[s], f[s], true);
+#pragma unroll
+        for (int s = 0; s < SC_STEPS; ++s) {
+            const int64_t i0 = base + s * (32 * SC_VEC) + lane * SC_VEC;
+            // Lane-local inclusive segmented scan of the 4 rows.
+            Seg loc{0, 0};
+#pragma unroll
+            for (int k = 0; k < SC_VEC; ++k) {
+                loc = seg_op(loc, Seg{v[s][k], (f[s] >> k) & 1u});
+                v[s][k] = loc.sum;
+            }
+            const Seg inc = warp_inclusive<SegRec>(loc);
+            Seg ex = SegRec::shfl_up(inc, 1);
+            if (lane == 0) ex = Seg{0, 0};
+            const Seg pre = seg_op(carry, ex);  // everything before this lane's rows
+            const unsigned first = f[s] ? __ffs(f[s]) - 1 : SC_VEC;
+#pragma unroll
+            for (int k = 0; k < SC_VEC; ++k)
+                if (static_cast<unsigned>(k) < first) v[s][k] += pre.sum;
+            if (ALIGNED && i0 + SC_VEC <= n) {
+                ulonglong4_32a u;
+                u.x = v[s][0];
+                u.y = v[s][1];
+                u.z = v[s][2];
+                u.w = v[s][3];
+                *reinterpret_cast<ulonglong4_32a *>(out + i0) = u;
+            } else {
+#pragma unroll
+                for (int k = 0; k < SC_VEC; ++k)
+                    if (i0 + k < n) out[i0 + k] = v[s][k];
+            }
+            carry = seg_op(carry, SegRec::shfl(inc, 31));
         }
     }
+
+    __device__ void last_tile(Seg) const {}
+};
+
+template <bool BY, bool ALIGNED>
+__global__ void __launch_bounds__(SC_THREADS, 3) scan_kernel(const unsigned long long *__restrict__ x,
+                                                             const unsigned char *__restrict__ starts,
+                                                             unsigned long long *__restrict__ out, int64_t n,
+                                                             int tiles, ulonglong2 *recs, unsigned epoch,
+                                                             ScanState *state, unsigned *counters,
+                                                             DevStatus *status) {
+    // The carried state is read once, before this block publishes anything; the block that
+    // finishes last rewrites it, after every block has read it.
+    const bool seen = state->seen != 0;
+    const unsigned long long carried = state->last;
+    ScanPass<BY, ALIGNED> p{x, starts, out, n, seen};
     // The last row's output, the last tile's inclusive value, is the carried state.
-    if (release_ticket_last(counters, tiles) && threadIdx.x == 0) {
-        state->last = ld_relaxed64(&lb.inc[tiles - 1].sum);
+    if (tile_pass<SC_WINDOW>(p, recs, tiles, epoch, counters, status, Seg{carried, 0}) && threadIdx.x == 0) {
+        state->last = SegRec::value(ld_relaxed128(recs + tiles - 1)).sum;
         state->seen = 1;
     }
 }
 
-// Dynamic shared memory of scan_kernel: the staged rows and their start flags.
-constexpr size_t SC_SMEM = (sizeof(unsigned long long) + 1) * SC_TILE;
-
-template <bool BY, bool ALIGNED> static void scan_configure() {
-    static bool configured = false;
-    if (!configured) {
-        cudaFuncSetAttribute(scan_kernel<BY, ALIGNED>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             static_cast<int>(SC_SMEM));
-        configured = true;
+// Launches a scan on `stream` with the tile records at `recs` (one 16-byte record per tile).
+template <bool BY>
+static void launch_scan(int sms, cudaStream_t stream, const unsigned long long *x, const unsigned char *s,
+                        unsigned long long *o, int64_t n, int tiles, ulonglong2 *recs, unsigned epoch,
+                        ScanState *state, unsigned *counters, DevStatus *status) {
+    const bool aligned = (reinterpret_cast<uintptr_t>(x) & 31) == 0 && (reinterpret_cast<uintptr_t>(o) & 31) == 0 &&
+                         (reinterpret_cast<uintptr_t>(s) & 3) == 0;
+    auto kernel = aligned ? scan_kernel<BY, true> : scan_kernel<BY, false>;
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, SC_THREADS, 0) != cudaSuccess || per_sm < 1) {
+        cudaGetLastError();
+        per_sm = 1;
     }
+    const long long g = static_cast<long long>(per_sm) * sms;
+    const int grid = static_cast<int>(g < tiles ? g : tiles);
+    kernel<<<grid, SC_THREADS, 0, stream>>>(x, s, o, n, tiles, recs, epoch, state, counters, status);
 }
 
 struct ScanImpl : ScannerImpl {
@@ -216,23 +261,15 @@ struct ScanImpl : ScannerImpl {
                                               " rows for a destination of " + std::to_string(out->len) +
                                               " rows");
         if (n == 0) return VKC_OK;
-        int tiles = static_cast<int>((n + SC_TILE - 1) / SC_TILE);
-        void *p;
+        const int tiles = static_cast<int>((n + SC_TILE - 1) / SC_TILE);
         unsigned *flags;
-        if ((st = scratch(ctx, 2 * sizeof(Seg) * static_cast<size_t>(tiles), &p))) return st;
-        if ((st = flag_arena(ctx, static_cast<size_t>(tiles), &flags))) return st;
-        Seg *vals = static_cast<Seg *>(p);
-        LookbackTiles<Seg> lb{flags, vals, vals + tiles};
-        unsigned epoch = next_epoch(ctx);
+        if ((st = flag_arena(ctx, 4 * static_cast<size_t>(tiles), &flags))) return st;
+        const unsigned epoch = next_epoch(ctx);
         const auto *x = args[0].ptr<unsigned long long>();
         const unsigned char *s = by ? args[1].ptr<unsigned char>() : nullptr;
         auto *o = static_cast<unsigned long long *>(out->data());
-        bool aligned = (reinterpret_cast<uintptr_t>(x) & 31) == 0 && (reinterpret_cast<uintptr_t>(o) & 31) == 0 &&
-                       (reinterpret_cast<uintptr_t>(s) & 3) == 0;
-        if (by && aligned) scan_configure<true, true>(), scan_kernel<true, true><<<tiles, SC_THREADS, SC_SMEM, ctx->stream>>>(x, s, o, n, tiles, lb, epoch, state, ctx->counters, ctx->status);
-        else if (by) scan_configure<true, false>(), scan_kernel<true, false><<<tiles, SC_THREADS, SC_SMEM, ctx->stream>>>(x, s, o, n, tiles, lb, epoch, state, ctx->counters, ctx->status);
-        else if (aligned) scan_configure<false, true>(), scan_kernel<false, true><<<tiles, SC_THREADS, SC_SMEM, ctx->stream>>>(x, s, o, n, tiles, lb, epoch, state, ctx->counters, ctx->status);
-        else scan_configure<false, false>(), scan_kernel<false, false><<<tiles, SC_THREADS, SC_SMEM, ctx->stream>>>(x, s, o, n, tiles, lb, epoch, state, ctx->counters, ctx->status);
+        if (by) launch_scan<true>(ctx->sms, ctx->stream, x, s, o, n, tiles, reinterpret_cast<ulonglong2 *>(flags), epoch, state, ctx->counters, ctx->status);
+        else launch_scan<false>(ctx->sms, ctx->stream, x, s, o, n, tiles, reinterpret_cast<ulonglong2 *>(flags), epoch, state, ctx->counters, ctx->status);
         return launched(ctx, "scan");
     }
 };
@@ -337,23 +374,23 @@ void register_scan(std::vector<KernelDef> &t) {
 // context and allocates nothing: the lookback records live in the file-scope array below, whose
 // address is looked up once per device. Every call shares the array and finds it as the last
 // call left it, so each call clears the words that must start at zero (the ticket counters,
-// the tile flags, the carried state and the status). Calls that overlap on the GPU race on the
+// the tile records, the carried state and the status). Calls that overlap on the GPU race on the
 // array: issue them on one stream, or wait for one to finish before the next starts.
 namespace vkc {
 
-// Header (ticket counters, status, carried state), the tile flags, then the tile aggregates
-// and inclusive prefixes. 1.13 MiB holds the 32,768 tiles of 2^28 rows.
+// Header (ticket counters, status, carried state), then one 16-byte lookback record per tile.
+// 1 MiB and 512 bytes hold the 65,536 tiles of 2^28 rows.
 constexpr int64_t NOALLOC_MAX_ROWS = int64_t(1) << 28;
 constexpr int64_t NOALLOC_MAX_TILES = NOALLOC_MAX_ROWS / SC_TILE;
 constexpr size_t NOALLOC_HEADER = 512;
-constexpr size_t NOALLOC_FLAGS = NOALLOC_MAX_TILES * sizeof(unsigned);
-constexpr size_t NOALLOC_BYTES = NOALLOC_HEADER + NOALLOC_FLAGS + 2 * NOALLOC_MAX_TILES * sizeof(Seg);
+constexpr size_t NOALLOC_BYTES = NOALLOC_HEADER + NOALLOC_MAX_TILES * sizeof(ulonglong2);
 
 static __device__ __align__(256) unsigned char g_scan_scratch[NOALLOC_BYTES];
 
 constexpr int NOALLOC_MAX_DEVICES = 64;
 static std::mutex g_noalloc_mu;
 static unsigned char *g_noalloc_ptr[NOALLOC_MAX_DEVICES];
+static int g_noalloc_sms[NOALLOC_MAX_DEVICES];
 
 static void noalloc_msg(char *err, size_t err_len, const std::string &msg) {
     if (err && err_len) {
@@ -393,6 +430,7 @@ extern "C" vkc_status vkc_scan_add_i64_noalloc(int device, const int64_t *in, in
         return st;
     };
     unsigned char *base;
+    int sms;
     {
         // Set-up, once per device: the device address of the scratch array. On the first call on
         // a device this runs inside that call.
@@ -405,36 +443,35 @@ extern "C" vkc_status vkc_scan_add_i64_noalloc(int device, const int64_t *in, in
                 return done(VKC_DEVICE, std::string("vkc_scan_add_i64_noalloc: cudaGetSymbolAddress failed: ") +
                                             cudaGetErrorString(e));
             }
+            int sms = 0;
+            e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+            if (e != cudaSuccess || sms < 1) {
+                cudaGetLastError();
+                return done(VKC_DEVICE, std::string("vkc_scan_add_i64_noalloc: cannot read the SM count: ") +
+                                            cudaGetErrorString(e));
+            }
+            g_noalloc_sms[device] = sms;
             g_noalloc_ptr[device] = static_cast<unsigned char *>(p);
         }
         base = g_noalloc_ptr[device];
+        sms = g_noalloc_sms[device];
     }
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     int tiles = static_cast<int>((n + SC_TILE - 1) / SC_TILE);
     unsigned *counters = reinterpret_cast<unsigned *>(base);
     DevStatus *status = reinterpret_cast<DevStatus *>(base + 256);
     ScanState *state = reinterpret_cast<ScanState *>(base + 256 + sizeof(DevStatus));
-    unsigned *flags = reinterpret_cast<unsigned *>(base + NOALLOC_HEADER);
-    Seg *agg = reinterpret_cast<Seg *>(base + NOALLOC_HEADER + NOALLOC_FLAGS);
-    LookbackTiles<Seg> lb{flags, agg, agg + NOALLOC_MAX_TILES};
-    // The header and the flags of this call's tiles start at zero; with clean flags one epoch
-    // value serves every call.
+    auto *recs = reinterpret_cast<ulonglong2 *>(base + NOALLOC_HEADER);
+    // The header and the records of this call's tiles start at zero; with clean records one
+    // epoch value serves every call.
     cudaError_t e = cudaMemsetAsync(base, 0, NOALLOC_HEADER, s);
-    if (e == cudaSuccess) e = cudaMemsetAsync(flags, 0, static_cast<size_t>(tiles) * sizeof(unsigned), s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(recs, 0, static_cast<size_t>(tiles) * sizeof(ulonglong2), s);
     if (e != cudaSuccess) {
         cudaGetLastError();
         return done(VKC_DEVICE, std::string("vkc_scan_add_i64_noalloc: ") + cudaGetErrorString(e));
     }
-    const auto *x = reinterpret_cast<const unsigned long long *>(in);
-    auto *o = reinterpret_cast<unsigned long long *>(out);
-    bool aligned = (reinterpret_cast<uintptr_t>(x) & 31) == 0 && (reinterpret_cast<uintptr_t>(o) & 31) == 0;
-    if (aligned) {
-        scan_configure<false, true>();
-        scan_kernel<false, true><<<tiles, SC_THREADS, SC_SMEM, s>>>(x, nullptr, o, n, tiles, lb, 1u, state, counters, status);
-    } else {
-        scan_configure<false, false>();
-        scan_kernel<false, false><<<tiles, SC_THREADS, SC_SMEM, s>>>(x, nullptr, o, n, tiles, lb, 1u, state, counters, status);
-    }
+    launch_scan<false>(sms, s, reinterpret_cast<const unsigned long long *>(in), nullptr,
+                       reinterpret_cast<unsigned long long *>(out), n, tiles, recs, 1u, state, counters, status);
     e = cudaGetLastError();
     if (e != cudaSuccess) return done(VKC_DEVICE, std::string("vkc_scan_add_i64_noalloc: ") + cudaGetErrorString(e));
     // Synchronous, like the other entries: read the status word into host memory.

@@ -1,24 +1,27 @@
 // Selections: filter_<cmp>_f64, compress_T and where (src/kernels/scalar/select.rs:81-104,
 // src/kernels/scalar/fused.rs:225-236).
 //
-// One pass: each 8192-row tile computes its keep flags, the tile's survivor count goes through
-// a decoupled lookback for the tile's output offset, and the survivors are compacted in shared
-// memory and written out contiguously. The output is the rows in input order, so it does not
-// depend on the tiling (select.rs:36-57 writes the same rows).
-#include "lookback.cuh"
+// One persistent pass (tilepass.cuh): a tile's survivor count is taken while the tile streams
+// from HBM, its output offset comes from the decoupled lookback, and the survivors are written
+// when the tile is read a second time, from L2. The output is the rows in input order, so it
+// does not depend on the tiling (select.rs:36-57 writes the same rows).
 #include "reduce_common.h"
+#include "tilepass.cuh"
 
 namespace vkc {
 
-constexpr int SEL_THREADS = 512;
-constexpr int SEL_ITEMS = 16;
-constexpr int SEL_TILE = SEL_THREADS * SEL_ITEMS;
+constexpr int SEL_THREADS = 256;
+constexpr int SEL_TILE = 4096;                             // rows per tile
+constexpr int SEL_SLICE = SEL_TILE / (SEL_THREADS / 32);   // rows per warp
+constexpr int SEL_WINDOW = 4;                              // lookback: 32 * 4 tiles per step
 
 enum SelKind { SEL_FILTER = 0, SEL_COMPRESS = 1, SEL_WHERE = 2 };
 
 template <int W> struct Word;
+template <> struct Word<16> { using T = uint4; };
 template <> struct Word<8> { using T = unsigned long long; };
 template <> struct Word<4> { using T = unsigned; };
+template <> struct Word<2> { using T = unsigned short; };
 template <> struct Word<1> { using T = unsigned char; };
 
 struct SelArgs {
@@ -31,144 +34,193 @@ struct SelArgs {
     unsigned long long *total;  // survivor count of the launch
 };
 
-// Per thread, ITEMS items in ROWS rows of the warp's 512-item slice: in row r the warp reads
-// 32 * VEC consecutive items, VEC per lane (one 16-byte load), so every load is coalesced and
-// item order is (row, lane, element).
-template <int W> struct SelShape {
-    static constexpr int VEC = 16 / W;
-    static constexpr int ROWS = SEL_ITEMS / VEC;
+// Nonzero bytes of a 32-bit word.
+__device__ __forceinline__ unsigned nonzero_bytes(unsigned v) {
+    const unsigned t = ~(((v & 0x7f7f7f7fu) + 0x7f7f7f7fu) | v | 0x7f7f7f7fu);  // 0x80 per zero byte
+    return 4u - __popc(t);
+}
+
+// A selection as a tile pass. A warp's slice of a tile is SEL_SLICE consecutive rows. The
+// count reads the keys (the values of a filter, the mask otherwise) with 16-byte loads; the
+// write reads, per step, VV rows per lane (16 bytes of values, and the mask bytes of the same
+// rows), ranks the kept rows with ballots and compacts them into the warp's slice of shared
+// memory, which it then copies out with consecutive lanes on consecutive rows.
+template <int KIND, int W, bool ALIGNED> struct SelectPass {
+    static constexpr int THREADS = SEL_THREADS;
+    using R = CountRec;
+    using V = unsigned long long;
+    using T = typename Word<W>::T;
+    using O = typename Word<KIND == SEL_WHERE ? 8 : W>::T;
+    static constexpr int VK = KIND == SEL_FILTER ? 2 : 16;  // keys per lane per count step
+    static constexpr int SK = SEL_SLICE / (32 * VK);
+    static constexpr int VV = KIND == SEL_WHERE ? 16 : 16 / W;  // rows per lane per write step
+    static constexpr int SV = SEL_SLICE / (32 * VV);
+    static_assert(SK >= 1 && SV >= 1, "a slice holds whole steps");
+
+    SelArgs a;
+    O *stage;  // SEL_SLICE outputs per warp
+
+    __device__ __forceinline__ bool keep_filter(unsigned long long v) const { return in_range(a.r, v); }
+
+    __device__ V count(int tile) const {
+        const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+        const int64_t base = static_cast<int64_t>(tile) * SEL_TILE + static_cast<int64_t>(w) * SEL_SLICE;
+        unsigned c = 0;
+        if (KIND == SEL_FILTER) {
+            const auto *x = static_cast<const unsigned long long *>(a.x);
+            ulonglong2 u[SK];
+#pragma unroll
+            for (int s = 0; s < SK; ++s) {
+                const int64_t i0 = base + s * 64 + lane * 2;
+                if (ALIGNED && i0 + 2 <= a.n) {
+                    u[s] = *reinterpret_cast<const ulonglong2 *>(x + i0);
+                } else {
+                    u[s].x = i0 < a.n ? x[i0] : 0ull;
+                    u[s].y = i0 + 1 < a.n ? x[i0 + 1] : 0ull;
+                }
+            }
+#pragma unroll
+            for (int s = 0; s < SK; ++s) {
+                const int64_t i0 = base + s * 64 + lane * 2;
+                c += (i0 < a.n && keep_filter(u[s].x)) + (i0 + 1 < a.n && keep_filter(u[s].y));
+            }
+        } else {
+#pragma unroll
+            for (int s = 0; s < SK; ++s) {
+                const int64_t i0 = base + s * 512 + lane * 16;
+                if (ALIGNED && i0 + 16 <= a.n) {
+                    const uint4 u = *reinterpret_cast<const uint4 *>(a.m + i0);
+                    c += nonzero_bytes(u.x) + nonzero_bytes(u.y) + nonzero_bytes(u.z) + nonzero_bytes(u.w);
+                } else {
+                    for (int k = 0; k < 16; ++k)
+                        if (i0 + k < a.n && a.m[i0 + k]) ++c;
+                }
+            }
+        }
+        return warp_sum(c);
+    }
+
+    __device__ void write(int tile, V pre) const {
+        const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+        const unsigned lt = (1u << lane) - 1;
+        const int64_t base = static_cast<int64_t>(tile) * SEL_TILE + static_cast<int64_t>(w) * SEL_SLICE;
+        O *st = stage + w * SEL_SLICE;
+        // Every step's loads are issued before any is used.
+        T v[SV][KIND == SEL_WHERE ? 1 : VV];
+        unsigned bits[SV];
+#pragma unroll
+        for (int s = 0; s < SV; ++s) {
+            const int64_t i0 = base + s * (32 * VV) + lane * VV;
+            bits[s] = 0;
+            if (KIND != SEL_WHERE) {
+                const T *x = static_cast<const T *>(a.x) + i0;
+                if (ALIGNED && i0 + VV <= a.n) {
+                    const uint4 u = __ldcs(reinterpret_cast<const uint4 *>(x));
+                    const T *e = reinterpret_cast<const T *>(&u);
+#pragma unroll
+                    for (int k = 0; k < VV; ++k) v[s][k] = e[k];
+                } else {
+#pragma unroll
+                    for (int k = 0; k < VV; ++k) v[s][k] = i0 + k < a.n ? x[k] : T(0);
+                }
+            }
+            if (KIND != SEL_FILTER) {
+                const unsigned char *m = a.m + i0;
+                if (ALIGNED && i0 + VV <= a.n) {
+                    if (VV == 16) {
+                        const uint4 u = __ldcs(reinterpret_cast<const uint4 *>(m));
+                        const unsigned wd[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+                        for (int k = 0; k < 16; ++k)
+                            if ((wd[k >> 2] >> (8 * (k & 3))) & 0xffu) bits[s] |= 1u << k;
+                    } else {
+                        const unsigned wd = VV == 4 ? __ldcs(reinterpret_cast<const unsigned *>(m))
+                                                    : __ldcs(reinterpret_cast<const unsigned short *>(m));
+#pragma unroll
+                        for (int k = 0; k < VV; ++k)
+                            if ((wd >> (8 * k)) & 0xffu) bits[s] |= 1u << k;
+                    }
+                } else {
+#pragma unroll
+                    for (int k = 0; k < VV; ++k)
+                        if (i0 + k < a.n && m[k]) bits[s] |= 1u << k;
+                }
+            }
+        }
+        unsigned total = 0;
+#pragma unroll
+        for (int s = 0; s < SV; ++s) {
+            const int64_t i0 = base + s * (32 * VV) + lane * VV;
+            unsigned b = bits[s];
+            if (KIND == SEL_FILTER) {
+#pragma unroll
+                for (int k = 0; k < VV; ++k)
+                    if (i0 + k < a.n && keep_filter(static_cast<unsigned long long>(v[s][k]))) b |= 1u << k;
+            }
+            // In-order ranks: the lanes before this one, element by element.
+            unsigned before = 0, step_total = 0;
+#pragma unroll
+            for (int k = 0; k < VV; ++k) {
+                const unsigned m = __ballot_sync(FULL, (b >> k) & 1u);
+                before += __popc(m & lt);
+                step_total += __popc(m);
+            }
+            unsigned p = total + before;
+#pragma unroll
+            for (int k = 0; k < VV; ++k)
+                if ((b >> k) & 1u) {
+                    if (KIND == SEL_WHERE) st[p] = static_cast<O>(a.base + i0 + k);
+                    else st[p] = static_cast<O>(v[s][KIND == SEL_WHERE ? 0 : k]);
+                    ++p;
+                }
+            total += step_total;
+        }
+        __syncwarp();
+        O *out = static_cast<O *>(a.out) + pre;
+        for (unsigned i = lane; i < total; i += 32) out[i] = st[i];
+        __syncwarp();  // the slice of shared memory is free again
+    }
+
+    __device__ void last_tile(V inclusive) const { *a.total = inclusive; }
 };
 
 template <int KIND, int W, bool ALIGNED>
-__global__ void __launch_bounds__(SEL_THREADS) select_kernel(SelArgs a, int tiles, unsigned long long *words,
+__global__ void __launch_bounds__(SEL_THREADS, 4) select_kernel(SelArgs a, int tiles, unsigned long long *recs,
                                                              unsigned epoch, unsigned *counters,
                                                              DevStatus *status) {
-    using T = typename Word<W>::T;
-    using O = typename Word<KIND == SEL_WHERE ? 8 : W>::T;
-    constexpr int VEC = SelShape<W>::VEC, ROWS = SelShape<W>::ROWS;
-    constexpr int SLICE = 32 * SEL_ITEMS;  // rows of one warp
-    // Each warp compacts its survivors into its own slice of shared memory row by row, so no
-    // row value waits in registers while the block waits for its offset.
+    using P = SelectPass<KIND, W, ALIGNED>;
     extern __shared__ __align__(16) unsigned char sel_smem[];
-    __shared__ unsigned s_warp[SEL_THREADS / 32];
-    __shared__ unsigned long long s_prefix, s_count;
-    const int tile = take_ticket(counters);
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    O *s_out = reinterpret_cast<O *>(sel_smem) + w * SLICE;
-    const unsigned lt = (1u << lane) - 1;
-    const int64_t wbase = static_cast<int64_t>(tile) * SEL_TILE + static_cast<int64_t>(w) * SLICE;
-
-    // Every row's load is issued before any is used: the loads of a thread are all in flight.
-    T vv[ROWS][VEC];
-    if (KIND != SEL_WHERE) {
-#pragma unroll
-        for (int r = 0; r < ROWS; ++r) {
-            const int64_t i0 = wbase + r * (32 * VEC) + lane * VEC;
-            if (ALIGNED && i0 + VEC <= a.n) {
-                uint4 u = __ldcs(reinterpret_cast<const uint4 *>(static_cast<const T *>(a.x) + i0));
-                const T *e = reinterpret_cast<const T *>(&u);
-#pragma unroll
-                for (int k = 0; k < VEC; ++k) vv[r][k] = e[k];
-            } else {
-#pragma unroll
-                for (int k = 0; k < VEC; ++k) vv[r][k] = i0 + k < a.n ? static_cast<const T *>(a.x)[i0 + k] : T(0);
-            }
-        }
-    }
-    unsigned total = 0;
-#pragma unroll
-    for (int r = 0; r < ROWS; ++r) {
-        const int64_t i0 = wbase + r * (32 * VEC) + lane * VEC;
-        T v[VEC];
-#pragma unroll
-        for (int k = 0; k < VEC; ++k) v[k] = KIND != SEL_WHERE ? vv[r][k] : T(0);
-        unsigned bits = 0;
-        if (KIND == SEL_FILTER) {
-#pragma unroll
-            for (int k = 0; k < VEC; ++k)
-                if (i0 + k < a.n && in_range(a.r, static_cast<unsigned long long>(v[k]))) bits |= 1u << k;
-        } else if (ALIGNED && VEC == 16 && i0 + 16 <= a.n) {
-            uint4 u = __ldcs(reinterpret_cast<const uint4 *>(a.m + i0));
-            unsigned wd[4] = {u.x, u.y, u.z, u.w};
-#pragma unroll
-            for (int k = 0; k < 16; ++k)
-                if ((wd[k >> 2] >> (8 * (k & 3))) & 0xffu) bits |= 1u << k;
-        } else {
-#pragma unroll
-            for (int k = 0; k < VEC; ++k)
-                if (i0 + k < a.n && a.m[i0 + k]) bits |= 1u << k;
-        }
-        // In-order ranks: the lanes before this one, element by element.
-        unsigned before = 0, row_total = 0;
-#pragma unroll
-        for (int k = 0; k < VEC; ++k) {
-            unsigned m = __ballot_sync(FULL, (bits >> k) & 1u);
-            before += __popc(m & lt);
-            row_total += __popc(m);
-        }
-        unsigned p = total + before;
-#pragma unroll
-        for (int k = 0; k < VEC; ++k)
-            if ((bits >> k) & 1u) {
-                s_out[p] = KIND == SEL_WHERE ? static_cast<O>(a.base + i0 + k) : static_cast<O>(v[k]);
-                ++p;
-            }
-        total += row_total;
-    }
-    if (lane == 0) s_warp[w] = total;
-    __syncthreads();
-    if (w == 0) {
-        unsigned c = lane < SEL_THREADS / 32 ? s_warp[lane] : 0u, x = c;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            unsigned y = __shfl_up_sync(FULL, x, o);
-            if (lane >= o) x += y;
-        }
-        const unsigned long long tile_count = __shfl_sync(FULL, x, SEL_THREADS / 32 - 1);
-        unsigned long long pre = warp_lookback_count<4>(words, tile, tile_count, epoch, status);
-        if (lane < SEL_THREADS / 32) s_warp[lane] = x - c;  // exclusive over warps
-        if (lane == 0) {
-            s_prefix = pre;
-            s_count = tile_count;
-            if (tile == tiles - 1) *a.total = pre + tile_count;
-        }
-    }
-    __syncthreads();
-    // Each warp writes its slice's survivors after those of the warps before it.
-    O *out = static_cast<O *>(a.out) + s_prefix + s_warp[w];
-    for (unsigned i = lane; i < total; i += 32) out[i] = s_out[i];
-    release_ticket(counters, tiles);
+    P p{a, reinterpret_cast<typename P::O *>(sel_smem)};
+    tile_pass<SEL_WINDOW>(p, recs, tiles, epoch, counters, status, 0ull);
 }
 
 template <int KIND, int W>
 static vkc_status run_select(vkc_ctx *ctx, SelArgs a, int64_t n, Builder *b) {
-    int64_t tiles64 = (n + SEL_TILE - 1) / SEL_TILE;
-    int tiles = static_cast<int>(tiles64);
+    if (n >= (int64_t(1) << 38)) return fail(ctx, VKC_USAGE, "selection of 2^38 rows or more");
+    const int64_t tiles64 = (n + SEL_TILE - 1) / SEL_TILE;
+    const int tiles = static_cast<int>(tiles64);
     void *p;
     unsigned *flags;
     vkc_status st;
     if ((st = scratch(ctx, 256, &p))) return st;
     if ((st = flag_arena(ctx, 2 * static_cast<size_t>(tiles), &flags))) return st;
-    auto *words = reinterpret_cast<unsigned long long *>(flags);
+    auto *recs = reinterpret_cast<unsigned long long *>(flags);
     a.total = static_cast<unsigned long long *>(p);
     void *at;
     if ((st = b->reserve(n, &at))) return st;
     a.out = at;
-    unsigned epoch = next_epoch(ctx);
-    bool aligned = (reinterpret_cast<uintptr_t>(a.x) & 15) == 0 &&
-                   (reinterpret_cast<uintptr_t>(a.m) & 15) == 0;
-    using O = typename Word<KIND == SEL_WHERE ? 8 : W>::T;
+    const unsigned epoch = next_epoch(ctx);
+    const bool aligned = (reinterpret_cast<uintptr_t>(a.x) & 15) == 0 &&
+                         (reinterpret_cast<uintptr_t>(a.m) & 15) == 0;
+    using O = typename SelectPass<KIND, W, true>::O;
     const size_t smem = sizeof(O) * SEL_TILE;
-    static bool configured = false;
-    if (!configured) {
-        cudaFuncSetAttribute(select_kernel<KIND, W, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-        cudaFuncSetAttribute(select_kernel<KIND, W, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-        configured = true;
+    if (aligned) {
+        const int grid = tile_pass_grid(ctx, select_kernel<KIND, W, true>, SEL_THREADS, smem, tiles);
+        select_kernel<KIND, W, true><<<grid, SEL_THREADS, smem, ctx->stream>>>(a, tiles, recs, epoch, ctx->counters, ctx->status);
+    } else {
+        const int grid = tile_pass_grid(ctx, select_kernel<KIND, W, false>, SEL_THREADS, smem, tiles);
+        select_kernel<KIND, W, false><<<grid, SEL_THREADS, smem, ctx->stream>>>(a, tiles, recs, epoch, ctx->counters, ctx->status);
     }
-    if (aligned)
-        select_kernel<KIND, W, true><<<tiles, SEL_THREADS, smem, ctx->stream>>>(a, tiles, words, epoch, ctx->counters, ctx->status);
-    else
-        select_kernel<KIND, W, false><<<tiles, SEL_THREADS, smem, ctx->stream>>>(a, tiles, words, epoch, ctx->counters, ctx->status);
     if ((st = launched(ctx, "select"))) return st;
     DevStatus ds;
     if ((st = read_status(ctx, &ds))) return st;
@@ -176,7 +228,7 @@ static vkc_status run_select(vkc_ctx *ctx, SelArgs a, int64_t n, Builder *b) {
     if ((st = pinned(ctx, 8, &h))) return st;
     VKC_CUDA(ctx, cudaMemcpyAsync(h, a.total, 8, cudaMemcpyDeviceToHost, ctx->stream));
     VKC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    unsigned long long k = *static_cast<unsigned long long *>(h);
+    const unsigned long long k = *static_cast<unsigned long long *>(h);
     // The count can only be at most the rows reserved; anything else is a broken launch.
     if (k > static_cast<unsigned long long>(n))
         return fail(ctx, VKC_DEVICE, "selection returned " + std::to_string(k) + " rows for " +
