@@ -191,7 +191,7 @@ VKC_API vkc_status vkc_elementwise_tile(vkc_ctx *ctx, int id, const vkc_value *a
  * library only its own buffers (an interpreter's arena, a pool with a fixed budget), or a
  * serving loop that must not take the allocator's lock or latency per request. It has no
  * counterpart in the reference, whose kernels run on the host. It needs no vkc_ctx and calls
- * no allocator: its lookback scratch is a 1.13 MiB array in the library's device image, so n
+ * no allocator: its lookback scratch is a 4 MiB array in the library's device image, so n
  * may be at most 2^28 rows (larger n is rejected with VKC_USAGE and a message). The first call
  * on a device looks up the array's device address (once per device); make that first call
  * before any stream capture. Every call shares the array: calls that overlap on the GPU race,

@@ -36,6 +36,18 @@ def test_filter_selectivity_large(ctx, sel):
     assert same_rows(got, oracle.filter_cmp_f64(x, "gt", sel))
 
 
+def test_filter_large_many_tiles(ctx):
+    # Far more tiles than resident blocks, so every block takes tickets after its first ring.
+    n = (1 << 26) + 3
+    dx = ctx.call("rand_f64", n, 6)
+    x = oracle.rand_f64(n, 6)
+    got = ctx.call("filter_gt_f64", dx, 0.5).numpy()
+    assert len(got) == ctx.call("count_gt_f64", dx, 0.5)
+    assert same_rows(got, x[x > 0.5])
+    m = x < 0.25
+    assert same_rows(ctx.call("where", ctx.upload(m)).numpy(), np.flatnonzero(m).astype(np.int64))
+
+
 @pytest.mark.parametrize("t", ["f64", "i64", "u64", "i32", "f32", "u8", "bool"])
 def test_compress_types(ctx, t):
     for n in LENGTHS + GPU_LENGTHS:

@@ -182,14 +182,14 @@ static vkc_status run_group(vkc_ctx *ctx, const vkc_array *xa, const vkc_array *
         return st;
     }
     int tiles = static_cast<int>((n + GI_TILE - 1) / GI_TILE);
-    unsigned *flags;
-    if ((st = flag_arena(ctx, 2 * static_cast<size_t>(tiles), &flags))) {
+    unsigned long long *recs;
+    if ((st = rec_arena(ctx, tiles, &recs))) {
         cleanup();
         vkc_array_release(o);
         return st;
     }
-    gi_number_kernel<<<tiles, GI_THREADS, 0, ctx->stream>>>(slot_of, n, t, tiles, reinterpret_cast<unsigned long long *>(flags),
-                                                           next_epoch(ctx), ctx->counters, ctx->status);
+    gi_number_kernel<<<tiles, GI_THREADS, 0, ctx->stream>>>(slot_of, n, t, tiles, recs, next_epoch(ctx), ctx->counters,
+                                                           ctx->status);
     if ((st = launched(ctx, "gi_number"))) {
         cleanup();
         vkc_array_release(o);

@@ -1,9 +1,9 @@
 // Scans: scan_add_i64 and scan_by_add_i64 (src/kernels/scalar/scan.rs:284-326), plus prev_i64
 // (scan.rs:16-48).
 //
-// One persistent pass (tilepass.cuh) over 4096-row tiles: a tile's aggregate is taken while it
-// streams from HBM, the decoupled lookback gives its prefix, and the scanned rows are written
-// when the tile is read again, from L2. scan_by uses the segmented operator on
+// One persistent pass (tilepass.cuh) over 8192-row tiles: a tile's aggregate is taken while it
+// streams from HBM, the tile is read again from L2 and scanned into shared memory while the
+// decoupled lookback finds its prefix, and the scanned rows are written with the prefix added. scan_by uses the segmented operator on
 // (starts-a-segment, sum): (f1, v1) then (f2, v2) = (f1 | f2, f2 ? v2 : v1 + v2). Row 0 of the
 // array always starts a segment; a later update continues the segment of the previous one
 // unless its first start byte says otherwise, as Scan::update does.
@@ -15,12 +15,14 @@
 
 namespace vkc {
 
-constexpr int SC_THREADS = 256;
-constexpr int SC_TILE = 4096;
+constexpr int SC_THREADS = 512;  // compute threads (+ 2 warps)
+constexpr int SC_TILE = 8192;
 constexpr int SC_SLICE = SC_TILE / (SC_THREADS / 32);  // rows per warp
 constexpr int SC_VEC = 4;                              // rows per lane per step (one 32-byte load)
 constexpr int SC_STEPS = SC_SLICE / (32 * SC_VEC);
 constexpr int SC_WINDOW = 4;
+constexpr int SC_SLOTS = 3;   // tile ring: 1 copy in flight
+constexpr int SC_BLOCKS = 1;  // blocks per SM
 
 // A segmented partial: `start` when a segment starts inside it, `sum` since the last start.
 struct Seg {
@@ -45,13 +47,6 @@ __device__ __forceinline__ ulonglong2 ld_relaxed128(const ulonglong2 *p) {
 }
 __device__ __forceinline__ void st_relaxed128(ulonglong2 *p, ulonglong2 v) {
     asm volatile("st.relaxed.gpu.global.v2.u64 [%0], {%1, %2};" ::"l"(p), "l"(v.x), "l"(v.y) : "memory");
-}
-
-// A 32-byte load marked evict-first (the last read of these rows).
-__device__ __forceinline__ ulonglong4_32a ldcs256(const unsigned long long *p) {
-    ulonglong4_32a v;
-    asm volatile("ld.global.cs.v4.u64 {%0, %1, %2, %3}, [%4];" : "=l"(v.x), "=l"(v.y), "=l"(v.z), "=l"(v.w) : "l"(p));
-    return v;
 }
 
 // Lookback record of a Seg in two words, each carrying the epoch and the state: the start
@@ -87,32 +82,50 @@ struct SegRec {
     }
 };
 
-// A scan as a tile pass. A warp's slice is SC_SLICE consecutive rows, read in SC_STEPS steps of
-// 128 rows; in a step lane l holds rows 4l..4l+3 (one 32-byte load), so loads and stores are
-// coalesced and row order is (step, lane, item).
-template <bool BY, bool ALIGNED> struct ScanPass {
+// A scan as a tile pass. A slot holds the tile's values (scanned in place by the stage) and
+// one byte per row: the start flags of scan_by as copied, then whether a segment starts at or
+// before the row in its warp slice. A compute warp's slice is SC_SLICE consecutive rows, read in
+// SC_STEPS steps of 128 rows; in a step lane l holds rows 4l..4l+3, so global stores are
+// coalesced and row order is (step, lane, item). A tile that is not whole, or not aligned, is
+// read from global memory instead of the slot.
+template <bool BY> struct ScanPass {
     static constexpr int THREADS = SC_THREADS;
+    static constexpr int VAL_BYTES = 8 * SC_TILE;
+    static constexpr int SLOT_BYTES = VAL_BYTES + SC_TILE;
+    static constexpr int SLOTS = SC_SLOTS;
     using R = SegRec;
     using V = Seg;
+    struct Staged {};
 
     const unsigned long long *x;
     const unsigned char *starts;
     unsigned long long *out;
     int64_t n;
-    bool seen;  // an earlier update saw rows: row 0 continues its segment
+    bool seen;     // an earlier update saw rows: row 0 continues its segment
+    bool aligned;  // x, out (32 bytes) and starts (16 bytes) aligned: whole tiles go by TMA
 
-    // The rows of one step and their start flags (bit k: row 4l + k). Row 0 of the array
-    // starts a segment whatever its byte (scan.rs:300-308).
-    __device__ __forceinline__ void load(int64_t i0, unsigned long long (&v)[SC_VEC], unsigned &f, bool stream) const {
+    __device__ bool whole(int tile) const { return aligned && static_cast<int64_t>(tile + 1) * SC_TILE <= n; }
+    __device__ unsigned bulk_bytes(int tile) const { return whole(tile) ? VAL_BYTES + (BY ? SC_TILE : 0) : 0u; }
+    __device__ void load(int tile, unsigned char *slot, unsigned long long *bar) const {
+        const int64_t r0 = static_cast<int64_t>(tile) * SC_TILE;
+        bulk_load(slot, x + r0, VAL_BYTES, bar);
+        if (BY) bulk_load(slot + VAL_BYTES, starts + r0, SC_TILE, bar);
+    }
+
+    // The rows of one step and their start flags (bit k: row 4l + k), from the slot or from
+    // global memory. Row 0 of the array starts a segment whatever its byte (scan.rs:300-308).
+    __device__ __forceinline__ void load_step(bool sm, const unsigned char *slot, int j, int64_t i0,
+                                              unsigned long long (&v)[SC_VEC], unsigned &f) const {
         f = 0;
-        if (ALIGNED && i0 + SC_VEC <= n) {
-            const ulonglong4_32a u = stream ? ldcs256(x + i0) : *reinterpret_cast<const ulonglong4_32a *>(x + i0);
-            v[0] = u.x;
-            v[1] = u.y;
-            v[2] = u.z;
-            v[3] = u.w;
+        if (sm) {
+            const ulonglong2 *p = reinterpret_cast<const ulonglong2 *>(reinterpret_cast<const unsigned long long *>(slot) + j);
+            const ulonglong2 u0 = p[0], u1 = p[1];
+            v[0] = u0.x;
+            v[1] = u0.y;
+            v[2] = u1.x;
+            v[3] = u1.y;
             if (BY) {
-                const unsigned m = *reinterpret_cast<const unsigned *>(starts + i0);
+                const unsigned m = *reinterpret_cast<const unsigned *>(slot + VAL_BYTES + j);
 #pragma unroll
                 for (int k = 0; k < SC_VEC; ++k)
                     if ((m >> (8 * k)) & 0xffu) f |= 1u << k;
@@ -130,30 +143,32 @@ template <bool BY, bool ALIGNED> struct ScanPass {
 
     // The slice aggregate: the sum of the rows from the slice's last segment start on (of all
     // rows when none starts), which needs no ordered combination across lanes.
-    __device__ Seg count(int tile) const {
+    __device__ Seg count(int tile, unsigned char *slot) const {
         const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-        const int64_t base = static_cast<int64_t>(tile) * SC_TILE + static_cast<int64_t>(w) * SC_SLICE;
+        const int64_t r0 = static_cast<int64_t>(tile) * SC_TILE;
+        const bool sm = whole(tile);
+        unsigned long long t = 0;
+        unsigned last = 0;  // the last start in the slice, as a position in row order + 1 (0: none)
         unsigned long long v[SC_STEPS][SC_VEC];
         unsigned f[SC_STEPS];
 #pragma unroll
-        for (int s = 0; s < SC_STEPS; ++s) load(base + s * (32 * SC_VEC) + lane * SC_VEC, v[s], f[s], false);
+        for (int s = 0; s < SC_STEPS; ++s) {
+            const int j = w * SC_SLICE + s * (32 * SC_VEC) + lane * SC_VEC;
+            load_step(sm, slot, j, r0 + j, v[s], f[s]);
+        }
         if (!BY) {
-            unsigned long long t = 0;
 #pragma unroll
             for (int s = 0; s < SC_STEPS; ++s)
 #pragma unroll
                 for (int k = 0; k < SC_VEC; ++k) t += v[s][k];
             return Seg{warp_sum(t), 0};
         }
-        // The last start in the slice, as a position in row order (0 = none).
-        unsigned last = 0;
 #pragma unroll
         for (int s = 0; s < SC_STEPS; ++s)
 #pragma unroll
             for (int k = 0; k < SC_VEC; ++k)
                 if ((f[s] >> k) & 1u) last = (s * 32 + lane) * SC_VEC + k + 1;
         last = __reduce_max_sync(FULL, last);
-        unsigned long long t = 0;
 #pragma unroll
         for (int s = 0; s < SC_STEPS; ++s)
 #pragma unroll
@@ -162,85 +177,120 @@ template <bool BY, bool ALIGNED> struct ScanPass {
         return Seg{warp_sum(t), last != 0};
     }
 
-    __device__ void write(int tile, Seg carry) const {
+    // Scans the slice from its own start, in place in the slot, with the has-a-start bytes
+    // over the start flags; a lane reads back only what it wrote itself.
+    __device__ Staged stage(int tile, unsigned char *slot) const {
         const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-        const int64_t base = static_cast<int64_t>(tile) * SC_TILE + static_cast<int64_t>(w) * SC_SLICE;
-        unsigned long long v[SC_STEPS][SC_VEC];
-        unsigned f[SC_STEPS];
-#pragma unroll
-        for (int s = 0; s < SC_STEPS; ++s) load(base + s * (32 * SC_VEC) + lane * SC_VEC, v[s], f[s], true);
+        const int64_t r0 = static_cast<int64_t>(tile) * SC_TILE;
+        const bool sm = whole(tile);
+        Seg carry{0, 0};  // the slice so far
 #pragma unroll
         for (int s = 0; s < SC_STEPS; ++s) {
-            const int64_t i0 = base + s * (32 * SC_VEC) + lane * SC_VEC;
+            const int j = w * SC_SLICE + s * (32 * SC_VEC) + lane * SC_VEC;
+            unsigned long long v[SC_VEC];
+            unsigned f;
+            load_step(sm, slot, j, r0 + j, v, f);
             // Lane-local inclusive segmented scan of the 4 rows.
             Seg loc{0, 0};
 #pragma unroll
             for (int k = 0; k < SC_VEC; ++k) {
-                loc = seg_op(loc, Seg{v[s][k], (f[s] >> k) & 1u});
-                v[s][k] = loc.sum;
+                loc = seg_op(loc, Seg{v[k], (f >> k) & 1u});
+                v[k] = loc.sum;
             }
             const Seg inc = warp_inclusive<SegRec>(loc);
             Seg ex = SegRec::shfl_up(inc, 1);
             if (lane == 0) ex = Seg{0, 0};
-            const Seg pre = seg_op(carry, ex);  // everything before this lane's rows
-            const unsigned first = f[s] ? __ffs(f[s]) - 1 : SC_VEC;
+            const Seg pre = seg_op(carry, ex);  // the slice before this lane's rows
+            const unsigned first = f ? __ffs(f) - 1 : SC_VEC;
+            unsigned has = 0;
+#pragma unroll
+            for (int k = 0; k < SC_VEC; ++k) {
+                if (static_cast<unsigned>(k) < first) v[k] += pre.sum;
+                if (static_cast<unsigned>(k) >= first || pre.start) has |= 1u << (8 * k);
+            }
+            ulonglong2 *p = reinterpret_cast<ulonglong2 *>(reinterpret_cast<unsigned long long *>(slot) + j);
+            p[0] = ulonglong2{v[0], v[1]};
+            p[1] = ulonglong2{v[2], v[3]};
+            *reinterpret_cast<unsigned *>(slot + VAL_BYTES + j) = has;
+            carry = seg_op(carry, SegRec::shfl(inc, 31));
+        }
+        return Staged{};
+    }
+
+    __device__ void flush(int tile, Seg pre, Staged, unsigned char *slot) const {
+        const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+        const int64_t r0 = static_cast<int64_t>(tile) * SC_TILE;
+#pragma unroll
+        for (int s = 0; s < SC_STEPS; ++s) {
+            const int j = w * SC_SLICE + s * (32 * SC_VEC) + lane * SC_VEC;
+            const int64_t i0 = r0 + j;
+            const ulonglong2 *p = reinterpret_cast<const ulonglong2 *>(reinterpret_cast<const unsigned long long *>(slot) + j);
+            const ulonglong2 u0 = p[0], u1 = p[1];
+            unsigned long long e[4] = {u0.x, u0.y, u1.x, u1.y};
+            const unsigned has = *reinterpret_cast<const unsigned *>(slot + VAL_BYTES + j);
 #pragma unroll
             for (int k = 0; k < SC_VEC; ++k)
-                if (static_cast<unsigned>(k) < first) v[s][k] += pre.sum;
-            if (ALIGNED && i0 + SC_VEC <= n) {
+                if (!((has >> (8 * k)) & 0xffu)) e[k] += pre.sum;
+            if (aligned && i0 + SC_VEC <= n) {
                 ulonglong4_32a u;
-                u.x = v[s][0];
-                u.y = v[s][1];
-                u.z = v[s][2];
-                u.w = v[s][3];
+                u.x = e[0];
+                u.y = e[1];
+                u.z = e[2];
+                u.w = e[3];
                 *reinterpret_cast<ulonglong4_32a *>(out + i0) = u;
             } else {
 #pragma unroll
                 for (int k = 0; k < SC_VEC; ++k)
-                    if (i0 + k < n) out[i0 + k] = v[s][k];
+                    if (i0 + k < n) out[i0 + k] = e[k];
             }
-            carry = seg_op(carry, SegRec::shfl(inc, 31));
         }
     }
 
     __device__ void last_tile(Seg) const {}
 };
 
-template <bool BY, bool ALIGNED>
-__global__ void __launch_bounds__(SC_THREADS, 3) scan_kernel(const unsigned long long *__restrict__ x,
-                                                             const unsigned char *__restrict__ starts,
-                                                             unsigned long long *__restrict__ out, int64_t n,
-                                                             int tiles, ulonglong2 *recs, unsigned epoch,
-                                                             ScanState *state, unsigned *counters,
-                                                             DevStatus *status) {
+template <bool BY>
+__global__ void __launch_bounds__(SC_THREADS + 64, SC_BLOCKS) scan_kernel(const unsigned long long *__restrict__ x,
+                                                                  const unsigned char *__restrict__ starts,
+                                                                  unsigned long long *__restrict__ out, int64_t n,
+                                                                  bool aligned, int tiles, ulonglong2 *recs,
+                                                                  unsigned epoch, ScanState *state,
+                                                                  unsigned *counters, DevStatus *status) {
     // The carried state is read once, before this block publishes anything; the block that
     // finishes last rewrites it, after every block has read it.
     const bool seen = state->seen != 0;
     const unsigned long long carried = state->last;
-    ScanPass<BY, ALIGNED> p{x, starts, out, n, seen};
+    ScanPass<BY> p{x, starts, out, n, seen, aligned};
     // The last row's output, the last tile's inclusive value, is the carried state.
     if (tile_pass<SC_WINDOW>(p, recs, tiles, epoch, counters, status, Seg{carried, 0}) && threadIdx.x == 0) {
-        state->last = SegRec::value(ld_relaxed128(recs + tiles - 1)).sum;
+        state->last = SegRec::value(ld_relaxed128(rec_at<SegRec>(recs, tiles - 1))).sum;
         state->seen = 1;
     }
 }
 
-// Launches a scan on `stream` with the tile records at `recs` (one 16-byte record per tile).
+// Launches a scan on `stream` with the tile records at `recs` (REC_STRIDE bytes per tile).
 template <bool BY>
 static void launch_scan(int sms, cudaStream_t stream, const unsigned long long *x, const unsigned char *s,
                         unsigned long long *o, int64_t n, int tiles, ulonglong2 *recs, unsigned epoch,
                         ScanState *state, unsigned *counters, DevStatus *status) {
     const bool aligned = (reinterpret_cast<uintptr_t>(x) & 31) == 0 && (reinterpret_cast<uintptr_t>(o) & 31) == 0 &&
-                         (reinterpret_cast<uintptr_t>(s) & 3) == 0;
-    auto kernel = aligned ? scan_kernel<BY, true> : scan_kernel<BY, false>;
+                         (reinterpret_cast<uintptr_t>(s) & 15) == 0;
+    constexpr size_t smem = SC_SLOTS * ScanPass<BY>::SLOT_BYTES;
+    static const bool configured = [] {
+        cudaFuncSetAttribute(scan_kernel<BY>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+        return true;
+    }();
+    (void)configured;
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, SC_THREADS, 0) != cudaSuccess || per_sm < 1) {
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, scan_kernel<BY>, SC_THREADS + 64, smem) != cudaSuccess ||
+        per_sm < 1) {
         cudaGetLastError();
         per_sm = 1;
     }
     const long long g = static_cast<long long>(per_sm) * sms;
     const int grid = static_cast<int>(g < tiles ? g : tiles);
-    kernel<<<grid, SC_THREADS, 0, stream>>>(x, s, o, n, tiles, recs, epoch, state, counters, status);
+    scan_kernel<BY><<<grid, SC_THREADS + 64, smem, stream>>>(x, s, o, n, aligned, tiles, recs, epoch, state, counters,
+                                                             status);
 }
 
 struct ScanImpl : ScannerImpl {
@@ -262,14 +312,14 @@ struct ScanImpl : ScannerImpl {
                                               " rows");
         if (n == 0) return VKC_OK;
         const int tiles = static_cast<int>((n + SC_TILE - 1) / SC_TILE);
-        unsigned *flags;
-        if ((st = flag_arena(ctx, 4 * static_cast<size_t>(tiles), &flags))) return st;
+        ulonglong2 *recs;
+        if ((st = rec_arena(ctx, tiles, &recs))) return st;
         const unsigned epoch = next_epoch(ctx);
         const auto *x = args[0].ptr<unsigned long long>();
         const unsigned char *s = by ? args[1].ptr<unsigned char>() : nullptr;
         auto *o = static_cast<unsigned long long *>(out->data());
-        if (by) launch_scan<true>(ctx->sms, ctx->stream, x, s, o, n, tiles, reinterpret_cast<ulonglong2 *>(flags), epoch, state, ctx->counters, ctx->status);
-        else launch_scan<false>(ctx->sms, ctx->stream, x, s, o, n, tiles, reinterpret_cast<ulonglong2 *>(flags), epoch, state, ctx->counters, ctx->status);
+        if (by) launch_scan<true>(ctx->sms, ctx->stream, x, s, o, n, tiles, recs, epoch, state, ctx->counters, ctx->status);
+        else launch_scan<false>(ctx->sms, ctx->stream, x, s, o, n, tiles, recs, epoch, state, ctx->counters, ctx->status);
         return launched(ctx, "scan");
     }
 };
@@ -378,12 +428,12 @@ void register_scan(std::vector<KernelDef> &t) {
 // array: issue them on one stream, or wait for one to finish before the next starts.
 namespace vkc {
 
-// Header (ticket counters, status, carried state), then one 16-byte lookback record per tile.
-// 1 MiB and 512 bytes hold the 65,536 tiles of 2^28 rows.
+// Header (ticket counters, status, carried state), then one lookback record per tile, REC_STRIDE
+// (128) bytes apart. 4 MiB and 512 bytes hold the 32,768 tiles of 2^28 rows.
 constexpr int64_t NOALLOC_MAX_ROWS = int64_t(1) << 28;
 constexpr int64_t NOALLOC_MAX_TILES = NOALLOC_MAX_ROWS / SC_TILE;
 constexpr size_t NOALLOC_HEADER = 512;
-constexpr size_t NOALLOC_BYTES = NOALLOC_HEADER + NOALLOC_MAX_TILES * sizeof(ulonglong2);
+constexpr size_t NOALLOC_BYTES = NOALLOC_HEADER + NOALLOC_MAX_TILES * REC_STRIDE;
 
 static __device__ __align__(256) unsigned char g_scan_scratch[NOALLOC_BYTES];
 
@@ -465,7 +515,7 @@ extern "C" vkc_status vkc_scan_add_i64_noalloc(int device, const int64_t *in, in
     // The header and the records of this call's tiles start at zero; with clean records one
     // epoch value serves every call.
     cudaError_t e = cudaMemsetAsync(base, 0, NOALLOC_HEADER, s);
-    if (e == cudaSuccess) e = cudaMemsetAsync(recs, 0, static_cast<size_t>(tiles) * sizeof(ulonglong2), s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(recs, 0, static_cast<size_t>(tiles) * REC_STRIDE, s);
     if (e != cudaSuccess) {
         cudaGetLastError();
         return done(VKC_DEVICE, std::string("vkc_scan_add_i64_noalloc: ") + cudaGetErrorString(e));

@@ -1,27 +1,27 @@
 // Selections: filter_<cmp>_f64, compress_T and where (src/kernels/scalar/select.rs:81-104,
 // src/kernels/scalar/fused.rs:225-236).
 //
-// One persistent pass (tilepass.cuh): a tile's survivor count is taken while the tile streams
-// from HBM, its output offset comes from the decoupled lookback, and the survivors are written
-// when the tile is read a second time, from L2. The output is the rows in input order, so it
-// does not depend on the tiling (select.rs:36-57 writes the same rows).
+// One persistent pass (tilepass.cuh): each tile is copied into shared memory by TMA, its
+// survivor count goes to the decoupled lookback, its survivors are compacted in place while
+// the lookback runs, and then written out at the tile's offset. The output is the rows in
+// input order, so it does not depend on the tiling (select.rs:36-57 writes the same rows).
 #include "reduce_common.h"
 #include "tilepass.cuh"
 
 namespace vkc {
 
-constexpr int SEL_THREADS = 256;
-constexpr int SEL_TILE = 4096;                             // rows per tile
-constexpr int SEL_SLICE = SEL_TILE / (SEL_THREADS / 32);   // rows per warp
+constexpr int SEL_THREADS = 512;                           // compute threads (+ 2 warps)
+constexpr int SEL_TILE = 8192;                             // rows per tile
+constexpr int SEL_SLICE = SEL_TILE / (SEL_THREADS / 32);   // rows per compute warp
 constexpr int SEL_WINDOW = 4;                              // lookback: 32 * 4 tiles per step
+constexpr int SEL_SLOTS = 3;                               // tile ring: 1 copy in flight
+constexpr int SEL_BLOCKS = 1;                              // blocks per SM
 
 enum SelKind { SEL_FILTER = 0, SEL_COMPRESS = 1, SEL_WHERE = 2 };
 
 template <int W> struct Word;
-template <> struct Word<16> { using T = uint4; };
 template <> struct Word<8> { using T = unsigned long long; };
 template <> struct Word<4> { using T = unsigned; };
-template <> struct Word<2> { using T = unsigned short; };
 template <> struct Word<1> { using T = unsigned char; };
 
 struct SelArgs {
@@ -32,6 +32,7 @@ struct SelArgs {
     int64_t base;           // where: global row of row 0
     void *out;
     unsigned long long *total;  // survivor count of the launch
+    bool aligned;           // values and mask start on 16-byte boundaries: whole tiles go by TMA
 };
 
 // Nonzero bytes of a 32-bit word.
@@ -40,157 +41,234 @@ __device__ __forceinline__ unsigned nonzero_bytes(unsigned v) {
     return 4u - __popc(t);
 }
 
-// A selection as a tile pass. A warp's slice of a tile is SEL_SLICE consecutive rows. The
-// count reads the keys (the values of a filter, the mask otherwise) with 16-byte loads; the
-// write reads, per step, VV rows per lane (16 bytes of values, and the mask bytes of the same
-// rows), ranks the kept rows with ballots and compacts them into the warp's slice of shared
-// memory, which it then copies out with consecutive lanes on consecutive rows.
-template <int KIND, int W, bool ALIGNED> struct SelectPass {
+// A selection as a tile pass. A slot holds the tile's values (filter, compress) and mask
+// (compress, where); the survivors are compacted into the values in place, or for `where`
+// (8-byte row numbers from 1-byte mask rows) into an output area after the mask. A compute
+// warp's slice is SEL_SLICE consecutive rows, read in steps of VV rows per lane (16 bytes of
+// values, or of mask for `where`), ranked with ballots, and copied out with consecutive lanes
+// on consecutive rows. A filter's count keeps its ballots in the slot, so the stage touches
+// only the steps and rows that survive. A tile that is not whole, or not 16-byte aligned, is
+// read from global memory instead of the slot.
+template <int KIND, int W> struct SelectPass {
     static constexpr int THREADS = SEL_THREADS;
     using R = CountRec;
     using V = unsigned long long;
     using T = typename Word<W>::T;
     using O = typename Word<KIND == SEL_WHERE ? 8 : W>::T;
+    static constexpr int VAL_BYTES = KIND == SEL_WHERE ? 0 : W * SEL_TILE;
+    static constexpr int MASK_BYTES = KIND == SEL_FILTER ? 0 : SEL_TILE;
+    static constexpr int OUT_BYTES = KIND == SEL_WHERE ? 8 * SEL_TILE : 0;
     static constexpr int VK = KIND == SEL_FILTER ? 2 : 16;  // keys per lane per count step
     static constexpr int SK = SEL_SLICE / (32 * VK);
-    static constexpr int VV = KIND == SEL_WHERE ? 16 : 16 / W;  // rows per lane per write step
+    static constexpr int BALLOT_BYTES = KIND == SEL_FILTER ? (SEL_THREADS / 32) * SK * 8 : 0;
+    static constexpr int SLOT_BYTES = VAL_BYTES + MASK_BYTES + OUT_BYTES + BALLOT_BYTES;
+    static constexpr int SLOTS = SEL_SLOTS;
+    static constexpr int VV = KIND == SEL_WHERE ? 16 : 16 / W;  // rows per lane per stage step
     static constexpr int SV = SEL_SLICE / (32 * VV);
     static_assert(SK >= 1 && SV >= 1, "a slice holds whole steps");
+    static_assert(KIND != SEL_FILTER || SK <= 32, "one lane stores each step's ballots");
+    using Staged = unsigned;  // survivors compacted in the warp's slice
 
     SelArgs a;
-    O *stage;  // SEL_SLICE outputs per warp
 
-    __device__ __forceinline__ bool keep_filter(unsigned long long v) const { return in_range(a.r, v); }
+    __device__ bool whole(int tile) const {
+        return a.aligned && static_cast<int64_t>(tile + 1) * SEL_TILE <= a.n;
+    }
+    __device__ unsigned bulk_bytes(int tile) const { return whole(tile) ? VAL_BYTES + MASK_BYTES : 0u; }
+    __device__ void load(int tile, unsigned char *slot, unsigned long long *bar) const {
+        const int64_t r0 = static_cast<int64_t>(tile) * SEL_TILE;
+        if (VAL_BYTES) bulk_load(slot, static_cast<const T *>(a.x) + r0, VAL_BYTES, bar);
+        if (MASK_BYTES) bulk_load(slot + VAL_BYTES, a.m + r0, MASK_BYTES, bar);
+    }
+    __device__ bool keep_filter(unsigned long long v) const { return in_range(a.r, v); }
 
-    __device__ V count(int tile) const {
+    // The slice's keys from `keys` (the slot, or global memory at the tile's first row).
+    template <class K> __device__ unsigned count_keys(const K *keys, int64_t r0) const {
         const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-        const int64_t base = static_cast<int64_t>(tile) * SEL_TILE + static_cast<int64_t>(w) * SEL_SLICE;
+        const int j = w * SEL_SLICE + lane * VK;  // row in the tile
         unsigned c = 0;
         if (KIND == SEL_FILTER) {
-            const auto *x = static_cast<const unsigned long long *>(a.x);
             ulonglong2 u[SK];
 #pragma unroll
-            for (int s = 0; s < SK; ++s) {
-                const int64_t i0 = base + s * 64 + lane * 2;
-                if (ALIGNED && i0 + 2 <= a.n) {
-                    u[s] = *reinterpret_cast<const ulonglong2 *>(x + i0);
-                } else {
-                    u[s].x = i0 < a.n ? x[i0] : 0ull;
-                    u[s].y = i0 + 1 < a.n ? x[i0 + 1] : 0ull;
-                }
-            }
+            for (int s = 0; s < SK; ++s) u[s] = *reinterpret_cast<const ulonglong2 *>(keys + j + s * 64);
 #pragma unroll
-            for (int s = 0; s < SK; ++s) {
-                const int64_t i0 = base + s * 64 + lane * 2;
-                c += (i0 < a.n && keep_filter(u[s].x)) + (i0 + 1 < a.n && keep_filter(u[s].y));
-            }
+            for (int s = 0; s < SK; ++s) c += keep_filter(u[s].x) + keep_filter(u[s].y);
         } else {
 #pragma unroll
             for (int s = 0; s < SK; ++s) {
-                const int64_t i0 = base + s * 512 + lane * 16;
-                if (ALIGNED && i0 + 16 <= a.n) {
-                    const uint4 u = *reinterpret_cast<const uint4 *>(a.m + i0);
-                    c += nonzero_bytes(u.x) + nonzero_bytes(u.y) + nonzero_bytes(u.z) + nonzero_bytes(u.w);
-                } else {
-                    for (int k = 0; k < 16; ++k)
-                        if (i0 + k < a.n && a.m[i0 + k]) ++c;
-                }
+                const uint4 u = *reinterpret_cast<const uint4 *>(keys + j + s * 512);
+                c += nonzero_bytes(u.x) + nonzero_bytes(u.y) + nonzero_bytes(u.z) + nonzero_bytes(u.w);
+            }
+        }
+        return c;
+    }
+
+    // The filter's ballots of the warp's slice: step s, element e in [s].(x, y).
+    __device__ uint2 *ballots(unsigned char *slot) const {
+        return reinterpret_cast<uint2 *>(slot + VAL_BYTES + MASK_BYTES + OUT_BYTES) + (threadIdx.x >> 5) * SK;
+    }
+
+    __device__ V count(int tile, unsigned char *slot) const {
+        const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+        const int64_t r0 = static_cast<int64_t>(tile) * SEL_TILE;
+        unsigned c = 0;
+        if (KIND == SEL_FILTER && whole(tile)) {
+            const auto *k = reinterpret_cast<const unsigned long long *>(slot) + w * SEL_SLICE + lane * 2;
+            uint2 *mb = ballots(slot);
+            ulonglong2 u[SK];
+#pragma unroll
+            for (int s = 0; s < SK; ++s) u[s] = *reinterpret_cast<const ulonglong2 *>(k + s * 64);
+#pragma unroll
+            for (int s = 0; s < SK; ++s) {
+                const unsigned m0 = __ballot_sync(FULL, keep_filter(u[s].x));
+                const unsigned m1 = __ballot_sync(FULL, keep_filter(u[s].y));
+                if (lane == s) mb[s] = make_uint2(m0, m1);
+                c += __popc(m0) + __popc(m1);
+            }
+            return c;
+        }
+        if (whole(tile)) {
+            c = KIND == SEL_FILTER ? count_keys(reinterpret_cast<const unsigned long long *>(slot), r0)
+                                   : count_keys(slot + VAL_BYTES, r0);
+        } else {
+            // Row by row from global memory.
+            for (int i = lane; i < SEL_SLICE; i += 32) {
+                const int64_t r = r0 + w * SEL_SLICE + i;
+                if (r >= a.n) break;
+                if (KIND == SEL_FILTER) c += keep_filter(static_cast<const unsigned long long *>(a.x)[r]);
+                else c += a.m[r] != 0;
             }
         }
         return warp_sum(c);
     }
 
-    __device__ void write(int tile, V pre) const {
+    __device__ unsigned stage(int tile, unsigned char *slot) const {
         const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
         const unsigned lt = (1u << lane) - 1;
-        const int64_t base = static_cast<int64_t>(tile) * SEL_TILE + static_cast<int64_t>(w) * SEL_SLICE;
-        O *st = stage + w * SEL_SLICE;
-        // Every step's loads are issued before any is used.
-        T v[SV][KIND == SEL_WHERE ? 1 : VV];
-        unsigned bits[SV];
-#pragma unroll
+        const int64_t r0 = static_cast<int64_t>(tile) * SEL_TILE;
+        const bool sm = whole(tile);
+        if (KIND == SEL_FILTER && sm) {
+            // From the count's ballots: steps with no survivor are skipped, and a lane reads
+            // its two rows only when one survives.
+            unsigned long long *st = reinterpret_cast<unsigned long long *>(slot) + w * SEL_SLICE;
+            const uint2 *mb = ballots(slot);
+            unsigned total = 0;
+            __syncwarp();
+#pragma unroll 4
+            for (int s = 0; s < SK; ++s) {
+                const uint2 m = mb[s];
+                if ((m.x | m.y) == 0) continue;
+                const unsigned b = ((m.x >> lane) & 1u) | (((m.y >> lane) & 1u) << 1);
+                ulonglong2 u = make_ulonglong2(0, 0);
+                if (b) u = *reinterpret_cast<const ulonglong2 *>(st + s * 64 + lane * 2);
+                unsigned q = total + __popc(m.x & lt) + __popc(m.y & lt);
+                __syncwarp();  // the step is read before any of it is overwritten
+                if (b & 1u) st[q++] = u.x;
+                if (b & 2u) st[q] = u.y;
+                total += __popc(m.x) + __popc(m.y);
+            }
+            return total;
+        }
+        O *st = reinterpret_cast<O *>(slot + VAL_BYTES + MASK_BYTES) + w * SEL_SLICE;  // where
+        if (KIND != SEL_WHERE) st = reinterpret_cast<O *>(slot) + w * SEL_SLICE;          // in place
+        unsigned total = 0;
+#pragma unroll 2
         for (int s = 0; s < SV; ++s) {
-            const int64_t i0 = base + s * (32 * VV) + lane * VV;
-            bits[s] = 0;
-            if (KIND != SEL_WHERE) {
-                const T *x = static_cast<const T *>(a.x) + i0;
-                if (ALIGNED && i0 + VV <= a.n) {
-                    const uint4 u = __ldcs(reinterpret_cast<const uint4 *>(x));
+            const int j = w * SEL_SLICE + s * (32 * VV) + lane * VV;  // row in the tile
+            const int64_t i0 = r0 + j;
+            T v[KIND == SEL_WHERE ? 1 : VV];
+            unsigned bits = 0;
+            if (sm) {
+                if (KIND != SEL_WHERE) {
+                    const uint4 u = *reinterpret_cast<const uint4 *>(reinterpret_cast<const T *>(slot) + j);
                     const T *e = reinterpret_cast<const T *>(&u);
 #pragma unroll
-                    for (int k = 0; k < VV; ++k) v[s][k] = e[k];
-                } else {
-#pragma unroll
-                    for (int k = 0; k < VV; ++k) v[s][k] = i0 + k < a.n ? x[k] : T(0);
+                    for (int k = 0; k < VV; ++k) v[k] = e[k];
                 }
-            }
-            if (KIND != SEL_FILTER) {
-                const unsigned char *m = a.m + i0;
-                if (ALIGNED && i0 + VV <= a.n) {
+                if (KIND != SEL_FILTER) {
+                    const unsigned char *m = slot + VAL_BYTES + j;
                     if (VV == 16) {
-                        const uint4 u = __ldcs(reinterpret_cast<const uint4 *>(m));
+                        const uint4 u = *reinterpret_cast<const uint4 *>(m);
                         const unsigned wd[4] = {u.x, u.y, u.z, u.w};
 #pragma unroll
                         for (int k = 0; k < 16; ++k)
-                            if ((wd[k >> 2] >> (8 * (k & 3))) & 0xffu) bits[s] |= 1u << k;
+                            if ((wd[k >> 2] >> (8 * (k & 3))) & 0xffu) bits |= 1u << k;
                     } else {
-                        const unsigned wd = VV == 4 ? __ldcs(reinterpret_cast<const unsigned *>(m))
-                                                    : __ldcs(reinterpret_cast<const unsigned short *>(m));
+                        const unsigned wd = VV == 4 ? *reinterpret_cast<const unsigned *>(m)
+                                                    : *reinterpret_cast<const unsigned short *>(m);
 #pragma unroll
                         for (int k = 0; k < VV; ++k)
-                            if ((wd >> (8 * k)) & 0xffu) bits[s] |= 1u << k;
+                            if ((wd >> (8 * k)) & 0xffu) bits |= 1u << k;
                     }
-                } else {
+                }
+            } else {
 #pragma unroll
-                    for (int k = 0; k < VV; ++k)
-                        if (i0 + k < a.n && m[k]) bits[s] |= 1u << k;
+                for (int k = 0; k < VV; ++k) {
+                    const bool in = i0 + k < a.n;
+                    if (KIND != SEL_WHERE) v[k] = in ? static_cast<const T *>(a.x)[i0 + k] : T(0);
+                    if (KIND != SEL_FILTER && in && a.m[i0 + k]) bits |= 1u << k;
                 }
             }
-        }
-        unsigned total = 0;
-#pragma unroll
-        for (int s = 0; s < SV; ++s) {
-            const int64_t i0 = base + s * (32 * VV) + lane * VV;
-            unsigned b = bits[s];
             if (KIND == SEL_FILTER) {
 #pragma unroll
                 for (int k = 0; k < VV; ++k)
-                    if (i0 + k < a.n && keep_filter(static_cast<unsigned long long>(v[s][k]))) b |= 1u << k;
+                    if ((sm || i0 + k < a.n) && keep_filter(static_cast<unsigned long long>(v[k]))) bits |= 1u << k;
             }
             // In-order ranks: the lanes before this one, element by element.
             unsigned before = 0, step_total = 0;
 #pragma unroll
             for (int k = 0; k < VV; ++k) {
-                const unsigned m = __ballot_sync(FULL, (b >> k) & 1u);
+                const unsigned m = __ballot_sync(FULL, (bits >> k) & 1u);
                 before += __popc(m & lt);
                 step_total += __popc(m);
             }
-            unsigned p = total + before;
+            __syncwarp();  // the step is read before any of it is overwritten
+            unsigned q = total + before;
 #pragma unroll
             for (int k = 0; k < VV; ++k)
-                if ((b >> k) & 1u) {
-                    if (KIND == SEL_WHERE) st[p] = static_cast<O>(a.base + i0 + k);
-                    else st[p] = static_cast<O>(v[s][KIND == SEL_WHERE ? 0 : k]);
-                    ++p;
+                if ((bits >> k) & 1u) {
+                    if (KIND == SEL_WHERE) st[q] = static_cast<O>(a.base + i0 + k);
+                    else st[q] = static_cast<O>(v[KIND == SEL_WHERE ? 0 : k]);
+                    ++q;
                 }
             total += step_total;
         }
+        return total;
+    }
+
+    __device__ void flush(int, V pre, unsigned total, unsigned char *slot) const {
+        const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+        const O *st = KIND == SEL_WHERE ? reinterpret_cast<const O *>(slot + VAL_BYTES + MASK_BYTES) + w * SEL_SLICE
+                                        : reinterpret_cast<const O *>(slot) + w * SEL_SLICE;
         __syncwarp();
         O *out = static_cast<O *>(a.out) + pre;
-        for (unsigned i = lane; i < total; i += 32) out[i] = st[i];
-        __syncwarp();  // the slice of shared memory is free again
+        unsigned i0 = 0;
+        if (sizeof(O) == 8) {
+            // Pairs of rows as aligned 16-byte stores, after a single row when the output does
+            // not start on a 16-byte boundary.
+            const unsigned mis = (reinterpret_cast<uintptr_t>(out) & 15) ? 1u : 0u;
+            const unsigned head = mis < total ? mis : total;
+            if (head && lane == 0) out[0] = st[0];
+            const unsigned pairs = (total - head) >> 1;
+            for (unsigned i = lane; i < pairs; i += 32) {
+                ulonglong2 u;
+                u.x = static_cast<unsigned long long>(st[head + 2 * i]);
+                u.y = static_cast<unsigned long long>(st[head + 2 * i + 1]);
+                *reinterpret_cast<ulonglong2 *>(out + head + 2 * i) = u;
+            }
+            i0 = head + 2 * pairs;
+        }
+        for (unsigned i = i0 + lane; i < total; i += 32) out[i] = st[i];
     }
 
     __device__ void last_tile(V inclusive) const { *a.total = inclusive; }
 };
 
-template <int KIND, int W, bool ALIGNED>
-__global__ void __launch_bounds__(SEL_THREADS, 4) select_kernel(SelArgs a, int tiles, unsigned long long *recs,
-                                                             unsigned epoch, unsigned *counters,
-                                                             DevStatus *status) {
-    using P = SelectPass<KIND, W, ALIGNED>;
-    extern __shared__ __align__(16) unsigned char sel_smem[];
-    P p{a, reinterpret_cast<typename P::O *>(sel_smem)};
+template <int KIND, int W>
+__global__ void __launch_bounds__(SEL_THREADS + 64, SEL_BLOCKS) select_kernel(SelArgs a, int tiles, unsigned long long *recs,
+                                                                     unsigned epoch, unsigned *counters,
+                                                                     DevStatus *status) {
+    SelectPass<KIND, W> p{a};
     tile_pass<SEL_WINDOW>(p, recs, tiles, epoch, counters, status, 0ull);
 }
 
@@ -200,27 +278,24 @@ static vkc_status run_select(vkc_ctx *ctx, SelArgs a, int64_t n, Builder *b) {
     const int64_t tiles64 = (n + SEL_TILE - 1) / SEL_TILE;
     const int tiles = static_cast<int>(tiles64);
     void *p;
-    unsigned *flags;
+    unsigned long long *recs;
     vkc_status st;
     if ((st = scratch(ctx, 256, &p))) return st;
-    if ((st = flag_arena(ctx, 2 * static_cast<size_t>(tiles), &flags))) return st;
-    auto *recs = reinterpret_cast<unsigned long long *>(flags);
+    if ((st = rec_arena(ctx, tiles, &recs))) return st;
     a.total = static_cast<unsigned long long *>(p);
     void *at;
     if ((st = b->reserve(n, &at))) return st;
     a.out = at;
     const unsigned epoch = next_epoch(ctx);
-    const bool aligned = (reinterpret_cast<uintptr_t>(a.x) & 15) == 0 &&
-                         (reinterpret_cast<uintptr_t>(a.m) & 15) == 0;
-    using O = typename SelectPass<KIND, W, true>::O;
-    const size_t smem = sizeof(O) * SEL_TILE;
-    if (aligned) {
-        const int grid = tile_pass_grid(ctx, select_kernel<KIND, W, true>, SEL_THREADS, smem, tiles);
-        select_kernel<KIND, W, true><<<grid, SEL_THREADS, smem, ctx->stream>>>(a, tiles, recs, epoch, ctx->counters, ctx->status);
-    } else {
-        const int grid = tile_pass_grid(ctx, select_kernel<KIND, W, false>, SEL_THREADS, smem, tiles);
-        select_kernel<KIND, W, false><<<grid, SEL_THREADS, smem, ctx->stream>>>(a, tiles, recs, epoch, ctx->counters, ctx->status);
-    }
+    a.aligned = (reinterpret_cast<uintptr_t>(a.x) & 15) == 0 && (reinterpret_cast<uintptr_t>(a.m) & 15) == 0;
+    constexpr size_t smem = SEL_SLOTS * SelectPass<KIND, W>::SLOT_BYTES;
+    static const bool configured = [] {
+        cudaFuncSetAttribute(select_kernel<KIND, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+        return true;
+    }();
+    (void)configured;
+    const int grid = tile_pass_grid(ctx, select_kernel<KIND, W>, SEL_THREADS + 64, smem, tiles);
+    select_kernel<KIND, W><<<grid, SEL_THREADS + 64, smem, ctx->stream>>>(a, tiles, recs, epoch, ctx->counters, ctx->status);
     if ((st = launched(ctx, "select"))) return st;
     DevStatus ds;
     if ((st = read_status(ctx, &ds))) return st;

@@ -12,10 +12,10 @@ template <int P, class R>
 __device__ typename R::V lookback_publish(typename R::W *recs, int tile, typename R::V agg, typename R::V init,
                                           unsigned epoch, DevStatus *status) {
     const int lane = threadIdx.x & 31;
-    if (lane == 0) R::store(recs + tile, R::make(epoch, 1u, agg));
+    if (lane == 0) R::store(rec_at<R>(recs, tile), R::make(epoch, 1u, agg));
     __syncwarp();
     const typename R::V pre = tile_lookback<P, R>(recs, tile, init, epoch, status);
-    if (lane == 0) R::store(recs + tile, R::make(epoch, 2u, R::op(pre, agg)));
+    if (lane == 0) R::store(rec_at<R>(recs, tile), R::make(epoch, 2u, R::op(pre, agg)));
     return pre;
 }
 
