@@ -373,8 +373,9 @@ def main():
         check_results(res)
 
     clocks = ClockSampler(local)
-    barrier(world)
     clocks.start()
+    time.sleep(1.0)  # nvidia-smi's start-up stalls the GPU briefly: keep it out of the timed steps
+    barrier(world)
     launches0 = ctx.launch_count()
     per_label = {}
     step_ms = []

@@ -196,13 +196,17 @@ __global__ void __launch_bounds__(256) extreme_kernel(const long long *__restric
     unsigned step = 0;
     bool any = false;
     for (int64_t i = tid; i < n2; i += 4 * stride, ++step) {
+        any = true;
         longlong2 v[4];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) v[u] = i + u * stride < n2 ? __ldcs(&x2[i + u * stride]) : make_longlong2(0, 0);
+        bool ok[4];
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
-            if (i + u * stride >= n2) break;  // the slots after it are past the end too
-            any = true;
+            ok[u] = i + u * stride < n2;
+            v[u] = ok[u] ? __ldcs(&x2[i + u * stride]) : make_longlong2(0, 0);
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            if (!ok[u]) continue;
             long long e[2] = {v[u].x, v[u].y};
 #pragma unroll
             for (int j = 0; j < 2; ++j) {
@@ -290,22 +294,40 @@ __global__ void __launch_bounds__(256) extreme_kernel(const long long *__restric
         }
         partials[blockIdx.x] = ExtState{bk, bi, nan, 0};
     }
-    if (last_block(done) && threadIdx.x == 0) {
-        ExtState s = *state;
-        long long k = s.seen ? s.key : (MAX ? LLONG_MIN : LLONG_MAX);
-        unsigned long long i = s.seen ? s.idx : ~0ull, nn = s.nan_idx;
-        for (unsigned b = 0; b < gridDim.x; ++b) {
-            ExtState p = partials[b];
-            if (p.idx != ~0ull) {
-                if (ARG) better<MAX>(k, i, p.key, p.idx + base);
+    if (last_block(done)) {
+        // The block's threads combine the partials (strided), then the warps, then warp 0 with
+        // the carried state. (key, row) is a total order, so the grouping does not matter.
+        long long k = MAX ? LLONG_MIN : LLONG_MAX;
+        unsigned long long i = ~0ull, nn = ~0ull;
+        auto take = [&](long long k2, unsigned long long i2, unsigned long long n2) {
+            if (i2 != ~0ull) {
+                if (ARG) better<MAX>(k, i, k2, i2);
                 else {
-                    k = (i == ~0ull) ? p.key : (MAX ? max(k, p.key) : min(k, p.key));
+                    k = (i == ~0ull) ? k2 : (MAX ? max(k, k2) : min(k, k2));
                     i = 0;
                 }
             }
-            if (p.nan_idx != ~0ull && p.nan_idx + base < nn) nn = p.nan_idx + base;
+            if (n2 < nn) nn = n2;
+        };
+        for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x) {
+            const ExtState q = partials[b];
+            take(q.key, q.idx == ~0ull ? ~0ull : q.idx + base, q.nan_idx == ~0ull ? ~0ull : q.nan_idx + base);
         }
-        *state = ExtState{k, i, nn, 1};
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const long long k2 = __shfl_xor_sync(FULL, k, o);
+            const unsigned long long i2 = __shfl_xor_sync(FULL, i, o), n2 = __shfl_xor_sync(FULL, nn, o);
+            take(k2, i2, n2);
+        }
+        __syncthreads();
+        if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = ExtState{k, i, nn, 0};
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            for (int w = 1; w < 8; ++w) take(ws[w].key, ws[w].idx, ws[w].nan_idx);
+            const ExtState s = *state;
+            if (s.seen) take(s.key, s.idx, s.nan_idx);
+            *state = ExtState{k, i, nn, 1};
+        }
     }
 }
 
