@@ -194,6 +194,108 @@ def check_results(results):
         raise SystemExit("fused dot %r != unfused %r" % (a, b))
 
 
+# ---------------------------------------------------------------------------- config 3
+
+
+def splitmix64_np(x):
+    """splitmix64 of uint64 counters (the generator behind rand_i64), vectorised."""
+    with np.errstate(over="ignore"):
+        z = x + np.uint64(0x9E3779B97F4A7C15)
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        return z ^ (z >> np.uint64(31))
+
+
+def zipf_keys(n, s=1.1, distinct=1 << 20, seed=11):
+    """Keys with Zipf(s) frequencies over `distinct` ranks: inverse CDF of a host table driven
+    by a seeded splitmix stream; key = splitmix64(rank), so keys span the full 64 bits."""
+    w = np.arange(1, distinct + 1, dtype=np.float64) ** -s
+    cdf = np.cumsum(w)
+    cdf /= cdf[-1]
+    out = np.empty(n, dtype=np.int64)
+    chunk = 1 << 24
+    for a in range(0, n, chunk):
+        b = min(n, a + chunk)
+        u = (splitmix64_np(np.arange(seed + a, seed + b, dtype=np.uint64)) >> np.uint64(11)).astype(np.float64) * 2.0 ** -53
+        rank = np.minimum(np.searchsorted(cdf, u, side="right"), distinct - 1).astype(np.uint64)
+        out[a:b] = splitmix64_np(rank).view(np.int64)
+    return out
+
+
+def config3_plan(n, nb):
+    """(label, algorithmic bytes) of the sorted and hashed group-by pipelines."""
+    return [("argsort_i64", 16 * n), ("gather_i64(keys)", 24 * n), ("gather_f64(vals)", 24 * n),
+            ("gather_i64(vals)", 24 * n), ("prev_i64", 16 * n), ("ne_i64", 17 * n),
+            ("scan_by_add_i64", 17 * n), ("group_id_i64", 16 * n), ("reduce_max_i64", 8 * n),
+            ("reduce_into_add_i64", 16 * n + 8 * nb), ("histogram", 8 * n + 8 * nb)]
+
+
+def config3_step(ctx, keys, vf, vi, stream):
+    """Stable argsort, values gathered by the permutation, scan_by add over the sorted runs, and
+    group-by sum/count through group_id. Returns ({label: ms}, results)."""
+    import torch
+
+    marks, res = [], {}
+
+    def timed(label, fn):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        out = fn()
+        e1.record(stream)
+        marks.append((label, e0, e1))
+        res[label] = out
+        return out
+
+    with torch.cuda.stream(stream):
+        perm = timed("argsort_i64", lambda: ctx.call("argsort_i64", keys))
+        sk = timed("gather_i64(keys)", lambda: ctx.call("gather_i64", keys, perm))
+        timed("gather_f64(vals)", lambda: ctx.call("gather_f64", vf, perm))
+        sv = timed("gather_i64(vals)", lambda: ctx.call("gather_i64", vi, perm))
+        pk = timed("prev_i64", lambda: ctx.call("prev_i64", sk, 0))
+        starts = timed("ne_i64", lambda: ctx.call("ne_i64", sk, pk))
+        timed("scan_by_add_i64", lambda: ctx.call("scan_by_add_i64", sv, starts))
+        g = timed("group_id_i64", lambda: ctx.call("group_id_i64", keys))
+        nb = timed("reduce_max_i64", lambda: ctx.call("reduce_max_i64", g)) + 1
+        timed("reduce_into_add_i64", lambda: ctx.call("reduce_into_add_i64", g, vi, nb))
+        timed("histogram", lambda: ctx.call("histogram", g, nb))
+    torch.cuda.current_stream().synchronize()
+    stream.synchronize()
+    return {label: e0.elapsed_time(e1) for label, e0, e1 in marks}, res
+
+
+def run_config3(ctx, n, stream, steps, warmup):
+    """Config 3 at n rows for both key distributions: per-kernel ms, GB/s and rows/s."""
+    out = {}
+    vf = ctx.call("rand_f64", n, 21)
+    vi = ctx.call("sub_i64", ctx.call("and_i64", ctx.call("rand_i64", n, 22), (1 << 21) - 1), 1 << 20)
+    for dist in ("uniform32", "zipf1.1"):
+        if dist == "uniform32":
+            keys = ctx.call("and_i64", ctx.call("rand_i64", n, 23), (1 << 32) - 1)
+        else:
+            keys = ctx.upload(zipf_keys(n))
+        for _ in range(warmup):
+            config3_step(ctx, keys, vf, vi, stream)
+        acc = {}
+        for _ in range(steps):
+            per, res = config3_step(ctx, keys, vf, vi, stream)
+            for k, v in per.items():
+                acc[k] = acc.get(k, 0.0) + v
+        nb = res["reduce_max_i64"] + 1
+        groups = {}
+        for label, nbytes in config3_plan(n, nb):
+            ms = acc[label] / steps
+            groups[label] = {"ms": round(ms, 4), "GB/s": round(nbytes / (ms / 1e3) / 1e9, 1),
+                             "Grows/s": round(n / (ms / 1e3) / 1e9, 3)}
+        total = sum(acc.values()) / steps
+        out[dist] = {"groups": int(nb), "pipeline_ms": round(total, 3), "kernels": groups}
+        del keys
+    return {"workload": "n=2^%d i64 keys (uniform over [0,2^32); Zipf s=1.1 over 2^20 keys, "
+                        "key = splitmix64(rank)), f64 and i64 values; stable argsort, gathers by "
+                        "the permutation, scan_by add over sorted runs, group_id + reduce_into + "
+                        "histogram" % (n.bit_length() - 1), "steps": steps, "warmup": warmup, **out}
+
+
 # ---------------------------------------------------------------------------- e2e
 
 
@@ -328,6 +430,7 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--cpu-sample", type=int, default=1 << 23)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--config3-n", type=int, default=1 << 27, help="0 skips the argsort/group-by section")
     args = ap.parse_args()
     world, rank, local = dist_setup()
     n = args.n
@@ -423,6 +526,12 @@ def main():
                "sample": "oracle port of the scalar entries (one thread, as the reference), the sweep "
                          "at n=2^%d, %d passes" % (args.cpu_sample.bit_length() - 1, passes)}
 
+    # Config 3 (argsort and group-by), reported beside the headline sweep, not in it.
+    c3 = None
+    if args.config3_n > 0:
+        del inputs, hin, res
+        c3 = run_config3(ctx, args.config3_n, stream, steps=3, warmup=1)
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world,
@@ -440,6 +549,7 @@ def main():
             "clocks": clk,
             "gpu_launches": launches,
             "kernels": kernels,
+            "config3": c3,
         }
         print(json.dumps(line), flush=True)
     ctx.close()

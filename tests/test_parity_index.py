@@ -67,6 +67,20 @@ def test_histogram_and_reduce_into(ctx):
                                   oracle.reduce_into_add_i64(keys, v, nb)), (n, nb)
 
 
+def test_histogram_and_reduce_into_skewed(ctx):
+    # Most rows on a few buckets, in runs and scattered: the warp-combined atomics.
+    n = 300_001
+    r = oracle.rand_i64(n, 77).view(np.uint64)
+    for nb in (7, 4096, 4097, 1 << 20):
+        hot = (r % np.uint64(3)).astype(np.int64)
+        cold = (r % np.uint64(nb)).astype(np.int64)
+        for keys in (np.where(r % np.uint64(100) == 0, cold, hot), np.sort(cold), np.zeros(n, np.int64)):
+            v = oracle.rand_i64(n, 78)
+            assert np.array_equal(ctx.call("histogram", ctx.upload(keys), nb).numpy(), oracle.histogram(keys, nb)), nb
+            assert np.array_equal(ctx.call("reduce_into_add_i64", ctx.upload(keys), ctx.upload(v), nb).numpy(),
+                                  oracle.reduce_into_add_i64(keys, v, nb)), nb
+
+
 def test_bucket_errors(ctx):
     # src/kernels/tests.rs:1576-1620
     for keys, nb in (([0, 3], 3), ([0, -1], 3), ([0, 0], 0), ([], -1), ([0], 1 << 62), ([0], 1 << 50),

@@ -100,38 +100,51 @@ __global__ void __launch_bounds__(256) keys_check_kernel(const long long *__rest
     if (bad != ~0ull) atomicMin(&status->first_bad, bad);
 }
 
-// Per-bucket wrapping sums (vals) or counts (vals == nullptr). Buckets up to SMEM_BINS are
-// accumulated in shared memory per block first.
+// Per-bucket wrapping sums (vals) or counts (vals == nullptr). Buckets below SMEM_BINS are
+// accumulated in shared memory per block and added to the output once per block; the others
+// go to global atomics. Small keys are where the contention is: group ids number groups by first
+// occurrence, so frequent groups get small ids (under a Zipf(1.1) key distribution the first
+// 4096 ids hold about three quarters of the rows).
 constexpr int SMEM_BINS = 4096;
+constexpr int BK_ROWS = 4;  // rows per thread in flight
 
-template <bool SMEM, bool COUNT>
+template <bool COUNT>
 __global__ void __launch_bounds__(256) bucket_kernel(const long long *__restrict__ keys,
                                                      const unsigned long long *__restrict__ vals, int64_t n,
                                                      uint64_t nb, unsigned long long *__restrict__ out,
                                                      DevStatus *status) {
-    __shared__ unsigned long long bins[SMEM ? SMEM_BINS : 1];
-    if (SMEM) {
-        for (int b = threadIdx.x; b < static_cast<int>(nb); b += blockDim.x) bins[b] = 0;
-        __syncthreads();
-    }
-    int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    __shared__ unsigned long long bins[SMEM_BINS];
+    const int sb = nb < static_cast<uint64_t>(SMEM_BINS) ? static_cast<int>(nb) : SMEM_BINS;
+    for (int b = threadIdx.x; b < sb; b += blockDim.x) bins[b] = 0;
+    __syncthreads();
+    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
     unsigned long long bad = ~0ull;
-    for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride) {
-        long long k = __ldcs(keys + i);
-        if (static_cast<uint64_t>(k) >= nb) {
-            if (static_cast<unsigned long long>(i) < bad) bad = static_cast<unsigned long long>(i);
-            continue;
+    for (int64_t i0 = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i0 < n; i0 += BK_ROWS * stride) {
+        long long k[BK_ROWS];
+        unsigned long long v[BK_ROWS];
+#pragma unroll
+        for (int r = 0; r < BK_ROWS; ++r) {
+            const int64_t i = i0 + r * stride;
+            k[r] = i < n ? __ldcs(keys + i) : 0;
+            v[r] = (!COUNT && i < n) ? __ldcs(vals + i) : 1ull;
         }
-        unsigned long long v = COUNT ? 1ull : __ldcs(vals + i);
-        if (SMEM) atomicAdd(&bins[k], v);
-        else atomicAdd(out + k, v);
+#pragma unroll
+        for (int r = 0; r < BK_ROWS; ++r) {
+            const int64_t i = i0 + r * stride;
+            if (i >= n) break;
+            if (static_cast<uint64_t>(k[r]) >= nb) {
+                if (static_cast<unsigned long long>(i) < bad) bad = static_cast<unsigned long long>(i);
+            } else if (k[r] < SMEM_BINS) {
+                atomicAdd(&bins[k[r]], v[r]);
+            } else {
+                atomicAdd(out + k[r], v[r]);
+            }
+        }
     }
     if (bad != ~0ull) atomicMin(&status->first_bad, bad);
-    if (SMEM) {
-        __syncthreads();
-        for (int b = threadIdx.x; b < static_cast<int>(nb); b += blockDim.x)
-            if (bins[b]) atomicAdd(out + b, bins[b]);
-    }
+    __syncthreads();
+    for (int b = threadIdx.x; b < sb; b += blockDim.x)
+        if (bins[b]) atomicAdd(out + b, bins[b]);
 }
 
 // index.rs:116-130 (checked_keys) then the result allocation (value.rs:285-307). The key check
@@ -173,14 +186,13 @@ static vkc_status run_buckets(vkc_ctx *ctx, const vkc_array *keys, const vkc_arr
         return fail(ctx, st, msg);
     }
     if (n > 0) {
+        // Every block adds its shared bins to the output once: at most 8 blocks per SM, and at
+        // least 8192 rows per block.
         int grid = stream_grid(ctx, n, 256, 8, 8192);
         auto *ov = static_cast<unsigned long long *>(o->data());
         const auto *vv = vals ? static_cast<const unsigned long long *>(vals->data()) : nullptr;
-        bool smem = nb <= SMEM_BINS;
-        if (smem && !vals) bucket_kernel<true, true><<<grid, 256, 0, ctx->stream>>>(k, vv, n, nb, ov, ctx->status);
-        else if (smem) bucket_kernel<true, false><<<grid, 256, 0, ctx->stream>>>(k, vv, n, nb, ov, ctx->status);
-        else if (!vals) bucket_kernel<false, true><<<grid, 256, 0, ctx->stream>>>(k, vv, n, nb, ov, ctx->status);
-        else bucket_kernel<false, false><<<grid, 256, 0, ctx->stream>>>(k, vv, n, nb, ov, ctx->status);
+        if (!vals) bucket_kernel<true><<<grid, 256, 0, ctx->stream>>>(k, vv, n, nb, ov, ctx->status);
+        else bucket_kernel<false><<<grid, 256, 0, ctx->stream>>>(k, vv, n, nb, ov, ctx->status);
         if ((st = launched(ctx, "buckets"))) {
             vkc_array_release(o);
             return st;

@@ -6,10 +6,12 @@
 //  * one histogram kernel counts all 8 digits in one read (radix.rs:199-202);
 //  * a digit that is equal in every row leaves the order unchanged and its pass is skipped
 //    (radix.rs:203-211);
-//  * each remaining digit is one "onesweep" pass: a 4096-row tile ranks its rows stably by
-//    digit (warp match + ballot in row order), finds each digit's offset among the earlier
-//    tiles with a decoupled lookback per digit, and scatters. The first pass reads the keys,
-//    the last writes the positions as i64.
+//  * each remaining digit is one reduce-then-scan pass over 4096-row tiles: `up` counts each
+//    tile's digits into a digit-major table, one exclusive scan of that table gives every
+//    (digit, tile) its first output row, and `down` ranks the tile's rows stably by digit
+//    (warp match + ballot in row order) and scatters them. The first pass reads the keys, the
+//    last writes the positions as i64. (A single-pass lookback per digit was slower here: the
+//    lookback of 256 digits per tile advances a few tiles per L2 round trip.)
 // Stability makes the output the reference's, which the comparison sort of short inputs
 // (radix.rs:140-151) also gives, so one path serves every length.
 #include <algorithm>
@@ -48,25 +50,117 @@ __global__ void __launch_bounds__(256) rs_hist_kernel(const long long *__restric
     }
 }
 
-// Lookback word of one (tile, digit): epoch << 34 | state << 32 | count (n < 2^32).
-__device__ __forceinline__ unsigned long long rs_word(unsigned epoch, unsigned state, unsigned count) {
-    return (static_cast<unsigned long long>(epoch) << 34) | (static_cast<unsigned long long>(state) << 32) | count;
+// Up: the digit counts of every tile, digit-major: counts[d * tiles + tile]. Rows are
+// warp-striped (row = base + j*32 + lane) as in `down`.
+template <bool FIRST>
+__global__ void __launch_bounds__(RS_THREADS) rs_up_kernel(const long long *__restrict__ keys_in,
+                                                           const unsigned long long *__restrict__ img_in, int64_t n,
+                                                           int shift, int tiles, unsigned *__restrict__ counts) {
+    __shared__ unsigned s_cnt[RS_WARPS][RADIX];
+    const int tile = blockIdx.x;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int i = threadIdx.x; i < RS_WARPS * RADIX; i += RS_THREADS) (&s_cnt[0][0])[i] = 0;
+    __syncthreads();
+    const int64_t base = static_cast<int64_t>(tile) * RS_TILE + static_cast<int64_t>(w) * (32 * RS_ITEMS);
+    unsigned long long img[RS_ITEMS];
+#pragma unroll
+    for (int j = 0; j < RS_ITEMS; ++j) {
+        const int64_t r = base + j * 32 + lane;
+        img[j] = r < n ? (FIRST ? image_of(__ldcs(keys_in + r)) : __ldcs(img_in + r)) : 0ull;
+    }
+#pragma unroll
+    for (int j = 0; j < RS_ITEMS; ++j) {
+        const bool in = base + j * 32 + lane < n;
+        const unsigned d = static_cast<unsigned>(img[j] >> shift) & 0xffu;
+        const unsigned active = __ballot_sync(FULL, in);
+        const unsigned peers = __match_any_sync(FULL, in ? d : 0x100u + lane) & active;
+        // One leader per digit adds its peers; leaders of one warp hold distinct digits.
+        if (in && (peers & ((1u << lane) - 1)) == 0) s_cnt[w][d] += __popc(peers);
+        __syncwarp();
+    }
+    __syncthreads();
+    const int d = threadIdx.x;  // RS_THREADS == RADIX
+    unsigned total = 0;
+#pragma unroll
+    for (int ww = 0; ww < RS_WARPS; ++ww) total += s_cnt[ww][d];
+    counts[static_cast<int64_t>(d) * tiles + tile] = total;
 }
 
-// One pass over digit `shift`. FIRST reads the i64 keys (positions are the row numbers);
-// LAST writes only the positions, as i64.
+// Exclusive scan of `m` u32 counts (n < 2^32, so sums fit) in SCAN_CHUNK-element blocks:
+// block sums, one block scanning the sums, then each block scanning its chunk from its base.
+constexpr int SCAN_THREADS = 256;
+constexpr int SCAN_ITEMS = 16;
+constexpr int SCAN_CHUNK = SCAN_THREADS * SCAN_ITEMS;
+
+__global__ void __launch_bounds__(SCAN_THREADS) rs_scan_sums(const unsigned *__restrict__ c, int64_t m,
+                                                              unsigned *__restrict__ sums) {
+    const int64_t b0 = static_cast<int64_t>(blockIdx.x) * SCAN_CHUNK;
+    unsigned t = 0;
+#pragma unroll
+    for (int j = 0; j < SCAN_ITEMS; ++j) {
+        const int64_t i = b0 + j * SCAN_THREADS + threadIdx.x;
+        if (i < m) t += c[i];
+    }
+    unsigned total;
+    block_exclusive_sum<unsigned>(t, &total);
+    if (threadIdx.x == 0) sums[blockIdx.x] = total;
+}
+
+// One block: exclusive scan of `k` block sums in place.
+__global__ void __launch_bounds__(1024) rs_scan_top(unsigned *sums, int k) {
+    __shared__ unsigned carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int b0 = 0; b0 < k; b0 += 1024) {
+        const int i = b0 + threadIdx.x;
+        const unsigned v = i < k ? sums[i] : 0u;
+        unsigned total;
+        const unsigned ex = block_exclusive_sum<unsigned>(v, &total);
+        if (i < k) sums[i] = carry + ex;
+        __syncthreads();
+        if (threadIdx.x == 0) carry += total;
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) rs_scan_apply(const unsigned *__restrict__ c, int64_t m,
+                                                               const unsigned *__restrict__ sums,
+                                                               unsigned *__restrict__ out) {
+    // Thread t holds the chunk's rows t*SCAN_ITEMS .. +SCAN_ITEMS-1 (contiguous), so a block
+    // exclusive sum of the thread totals orders them.
+    const int64_t b0 = static_cast<int64_t>(blockIdx.x) * SCAN_CHUNK + static_cast<int64_t>(threadIdx.x) * SCAN_ITEMS;
+    unsigned v[SCAN_ITEMS], t = 0;
+#pragma unroll
+    for (int j = 0; j < SCAN_ITEMS; ++j) {
+        v[j] = b0 + j < m ? c[b0 + j] : 0u;
+        t += v[j];
+    }
+    unsigned total;
+    unsigned run = sums[blockIdx.x] + block_exclusive_sum<unsigned>(t, &total);
+#pragma unroll
+    for (int j = 0; j < SCAN_ITEMS; ++j) {
+        if (b0 + j < m) out[b0 + j] = run;
+        run += v[j];
+    }
+}
+
+// Down: one pass over digit `shift` with the tile's first output row per digit in
+// offsets[d * tiles + tile]. FIRST reads the i64 keys (positions are the row numbers); LAST
+// writes only the positions, as i64.
 template <bool FIRST, bool LAST>
-__global__ void __launch_bounds__(RS_THREADS) rs_pass_kernel(
+__global__ void __launch_bounds__(RS_THREADS) rs_down_kernel(
     const long long *__restrict__ keys_in, const unsigned long long *__restrict__ img_in,
     const unsigned *__restrict__ pos_in, unsigned long long *__restrict__ img_out,
-    unsigned *__restrict__ pos_out, long long *__restrict__ out, int64_t n, int shift,
-    const unsigned *__restrict__ bucket_base, unsigned long long *status, int tiles, unsigned epoch,
-    unsigned *counters, DevStatus *st) {
+    unsigned *__restrict__ pos_out, long long *__restrict__ out, int64_t n, int shift, int tiles,
+    const unsigned *__restrict__ offsets) {
     __shared__ unsigned short s_wcnt[RS_WARPS][RADIX];  // per-warp digit counts, then offsets
-    __shared__ unsigned s_tile_excl[RADIX];
-    const int tile = take_ticket(counters);
+    __shared__ unsigned s_tile_excl[RADIX];             // the digit's first output row
+    __shared__ unsigned s_dstart[RADIX];                // the digit's first row in the sorted tile
+    extern __shared__ __align__(16) unsigned char rs_smem[];
+    const int tile = blockIdx.x;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     for (int i = threadIdx.x; i < RS_WARPS * RADIX; i += RS_THREADS) (&s_wcnt[0][0])[i] = 0;
+    s_tile_excl[threadIdx.x] = offsets[static_cast<int64_t>(threadIdx.x) * tiles + tile];  // RS_THREADS == RADIX
     __syncthreads();
 
     // Rows of this warp: warp-striped, row = base + j*32 + lane, so (j, lane) is row order.
@@ -78,8 +172,8 @@ __global__ void __launch_bounds__(RS_THREADS) rs_pass_kernel(
     const unsigned lt = (1u << lane) - 1;
 #pragma unroll
     for (int j = 0; j < RS_ITEMS; ++j) {
-        int64_t r = base + j * 32 + lane;
-        bool in = r < n;
+        const int64_t r = base + j * 32 + lane;
+        const bool in = r < n;
         if (FIRST) {
             img[j] = in ? image_of(__ldcs(keys_in + r)) : ~0ull;
             pos[j] = static_cast<unsigned>(r);
@@ -87,12 +181,16 @@ __global__ void __launch_bounds__(RS_THREADS) rs_pass_kernel(
             img[j] = in ? __ldcs(img_in + r) : ~0ull;
             pos[j] = in ? __ldcs(pos_in + r) : 0u;
         }
-        unsigned d = static_cast<unsigned>(img[j] >> shift) & 0xffu;
+    }
+#pragma unroll
+    for (int j = 0; j < RS_ITEMS; ++j) {
+        const bool in = base + j * 32 + lane < n;
+        const unsigned d = static_cast<unsigned>(img[j] >> shift) & 0xffu;
         dig[j] = static_cast<unsigned char>(d);
         // Rank among this warp's earlier rows with the same digit.
-        unsigned active = __ballot_sync(FULL, in);
-        unsigned peers = __match_any_sync(FULL, in ? d : 0x100u + lane) & active;
-        unsigned short before = s_wcnt[w][d];
+        const unsigned active = __ballot_sync(FULL, in);
+        const unsigned peers = __match_any_sync(FULL, in ? d : 0x100u + lane) & active;
+        const unsigned short before = s_wcnt[w][d];
         __syncwarp();
         if (in) {
             rank[j] = static_cast<unsigned short>(before + __popc(peers & lt));
@@ -101,53 +199,51 @@ __global__ void __launch_bounds__(RS_THREADS) rs_pass_kernel(
         __syncwarp();
     }
     __syncthreads();
-    // Per digit: tile count, per-warp exclusive offsets, and the lookback over earlier tiles.
+    // Per digit: exclusive offsets of the warps within the digit, and the digit's first row in
+    // the tile sorted by digit.
     {
-        const int d = threadIdx.x;  // RS_THREADS == RADIX
+        const int d = threadIdx.x;
         unsigned total = 0;
 #pragma unroll
         for (int ww = 0; ww < RS_WARPS; ++ww) {
-            unsigned c = s_wcnt[ww][d];
+            const unsigned c = s_wcnt[ww][d];
             s_wcnt[ww][d] = static_cast<unsigned short>(total);
             total += c;
         }
-        unsigned long long *my = status + static_cast<int64_t>(tile) * RADIX + d;
-        st_release64(my, rs_word(epoch, 1, total));
-        unsigned excl = 0;
-        for (int tp = tile - 1; tp >= 0; --tp) {
-            unsigned long long v;
-            unsigned it = 0;
-            while (((v = ld_acquire64(status + static_cast<int64_t>(tp) * RADIX + d)) >> 34) != epoch) {
-                if (++it > SPIN_LIMIT) {
-                    set_timeout(st);
-                    break;
-                }
-                backoff(it);
-            }
-            if ((v >> 34) != epoch) break;
-            excl += static_cast<unsigned>(v);
-            if (((v >> 32) & 3u) == 2u) break;
-        }
-        st_release64(my, rs_word(epoch, 2, excl + total));
-        s_tile_excl[d] = bucket_base[d] + excl;
+        unsigned tile_total;
+        s_dstart[d] = block_exclusive_sum<unsigned>(total, &tile_total);
     }
     __syncthreads();
+    // The tile sorted by digit (stable) in shared memory, then written out with consecutive
+    // threads on consecutive rows of each digit's run, so the stores coalesce.
+    unsigned long long *s_img = reinterpret_cast<unsigned long long *>(rs_smem);
+    unsigned *s_pos = reinterpret_cast<unsigned *>(rs_smem + sizeof(unsigned long long) * RS_TILE);
 #pragma unroll
     for (int j = 0; j < RS_ITEMS; ++j) {
-        int64_t r = base + j * 32 + lane;
-        if (r < n) {
-            unsigned d = dig[j];
-            unsigned dst = s_tile_excl[d] + s_wcnt[w][d] + rank[j];
-            if (LAST) {
-                out[dst] = static_cast<long long>(pos[j]);
-            } else {
-                img_out[dst] = img[j];
-                pos_out[dst] = pos[j];
-            }
+        if (base + j * 32 + lane < n) {
+            const unsigned d = dig[j];
+            const unsigned l = s_dstart[d] + s_wcnt[w][d] + rank[j];
+            s_img[l] = img[j];
+            s_pos[l] = pos[j];
         }
     }
-    release_ticket(counters, tiles);
+    __syncthreads();
+    const int rows = static_cast<int>(n - static_cast<int64_t>(tile) * RS_TILE < RS_TILE ? n - static_cast<int64_t>(tile) * RS_TILE : RS_TILE);
+    for (int l = threadIdx.x; l < rows; l += RS_THREADS) {
+        const unsigned long long im = s_img[l];
+        const unsigned d = static_cast<unsigned>(im >> shift) & 0xffu;
+        const unsigned dst = s_tile_excl[d] + (static_cast<unsigned>(l) - s_dstart[d]);
+        if (LAST) {
+            out[dst] = static_cast<long long>(s_pos[l]);
+        } else {
+            img_out[dst] = im;
+            pos_out[dst] = s_pos[l];
+        }
+    }
 }
+
+// Dynamic shared memory of rs_down_kernel: the tile's images and positions sorted by digit.
+constexpr size_t RS_DOWN_SMEM = (sizeof(unsigned long long) + sizeof(unsigned)) * RS_TILE;
 
 __global__ void rs_iota_kernel(long long *out, int64_t n) {
     int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
@@ -177,9 +273,8 @@ static vkc_status argsort_i64(vkc_ctx *ctx, const vkc_value *args, int nargs, vk
     const auto *keys = static_cast<const long long *>(xs->data());
     // Histogram of every digit.
     void *p;
-    if ((st = scratch(ctx, 8 * RADIX * sizeof(unsigned) * 2, &p))) return release(st);
+    if ((st = scratch(ctx, 8 * RADIX * sizeof(unsigned), &p))) return release(st);
     auto *hist = static_cast<unsigned *>(p);
-    auto *bases = hist + 8 * RADIX;
     VKC_CUDA(ctx, cudaMemsetAsync(hist, 0, 8 * RADIX * sizeof(unsigned), ctx->stream));
     rs_hist_kernel<<<stream_grid(ctx, n, 256, 4, 16384), 256, 0, ctx->stream>>>(keys, n, hist);
     if ((st = launched(ctx, "rs_hist"))) return release(st);
@@ -190,20 +285,12 @@ static vkc_status argsort_i64(vkc_ctx *ctx, const vkc_value *args, int nargs, vk
     VKC_CUDA(ctx, cudaMemcpyAsync(hh, hist, 8 * RADIX * sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream));
     VKC_CUDA(ctx, cudaMemcpyAsync(first, keys, 8, cudaMemcpyDeviceToHost, ctx->stream));
     VKC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    // Active digits (radix.rs:203-211) and each pass's exclusive bucket offsets.
+    // Active digits (radix.rs:203-211): a digit whose bucket of the first row holds every row.
     unsigned long long first_img = static_cast<unsigned long long>(*first) ^ 0x8000000000000000ull;
     int active[8], passes = 0;
-    unsigned *hb = hh + 8 * RADIX;
     for (int pss = 0; pss < 8; ++pss) {
         unsigned fd = static_cast<unsigned>(first_img >> (8 * pss)) & 0xffu;
-        if (hh[pss * RADIX + fd] != static_cast<unsigned>(n)) {
-            unsigned sum = 0;
-            for (int d = 0; d < RADIX; ++d) {
-                hb[passes * RADIX + d] = sum;
-                sum += hh[pss * RADIX + d];
-            }
-            active[passes++] = pss;
-        }
+        if (hh[pss * RADIX + fd] != static_cast<unsigned>(n)) active[passes++] = pss;
     }
     auto *oo = static_cast<long long *>(o->data());
     if (passes == 0) {
@@ -213,12 +300,11 @@ static vkc_status argsort_i64(vkc_ctx *ctx, const vkc_value *args, int nargs, vk
         out->array = o;
         return VKC_OK;
     }
-    VKC_CUDA(ctx, cudaMemcpyAsync(bases, hb, static_cast<size_t>(passes) * RADIX * sizeof(unsigned),
-                                  cudaMemcpyHostToDevice, ctx->stream));
     // Ping-pong buffers of (image, position), as radix.rs:224-232.
-    vkc_array *ia = nullptr, *ib = nullptr, *pa = nullptr, *pb = nullptr;
+    vkc_array *ia = nullptr, *ib = nullptr, *pa = nullptr, *pb = nullptr, *ca = nullptr, *oa = nullptr,
+              *sa = nullptr;
     auto cleanup = [&]() {
-        for (vkc_array *a : {ia, ib, pa, pb})
+        for (vkc_array *a : {ia, ib, pa, pb, ca, oa, sa})
             if (a) vkc_array_release(a);
     };
     if (passes > 1) {
@@ -231,32 +317,48 @@ static vkc_status argsort_i64(vkc_ctx *ctx, const vkc_value *args, int nargs, vk
             return release(fail(ctx, VKC_ALLOC, "cannot allocate argsort scratch for " + std::to_string(n) + " rows"));
         }
     }
-    int tiles = static_cast<int>((n + RS_TILE - 1) / RS_TILE);
-    unsigned *flags;
-    if ((st = flag_arena(ctx, static_cast<size_t>(tiles) * RADIX * 2, &flags))) {
+    // Digit-major tile counts, their exclusive scan, and the scan's block sums.
+    const int tiles = static_cast<int>((n + RS_TILE - 1) / RS_TILE);
+    const int64_t m = static_cast<int64_t>(RADIX) * tiles;
+    const int chunks = static_cast<int>((m + SCAN_CHUNK - 1) / SCAN_CHUNK);
+    if ((st = new_array(ctx, VKC_I32, m, false, &ca)) || (st = new_array(ctx, VKC_I32, m, false, &oa)) ||
+        (st = new_array(ctx, VKC_I32, chunks, false, &sa))) {
         cleanup();
-        return release(st);
+        return release(fail(ctx, VKC_ALLOC, "cannot allocate argsort scratch for " + std::to_string(n) + " rows"));
     }
-    auto *status = reinterpret_cast<unsigned long long *>(flags);
+    auto *counts = static_cast<unsigned *>(ca->data());
+    auto *offs = static_cast<unsigned *>(oa->data());
+    auto *sums = static_cast<unsigned *>(sa->data());
     unsigned long long *img[2] = {ia ? static_cast<unsigned long long *>(ia->data()) : nullptr,
                                   ib ? static_cast<unsigned long long *>(ib->data()) : nullptr};
     unsigned *pos[2] = {pa ? static_cast<unsigned *>(pa->data()) : nullptr,
                         pb ? static_cast<unsigned *>(pb->data()) : nullptr};
     int cur = 0;
+    static const bool configured = [] {
+        cudaFuncSetAttribute(rs_down_kernel<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(RS_DOWN_SMEM));
+        cudaFuncSetAttribute(rs_down_kernel<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(RS_DOWN_SMEM));
+        cudaFuncSetAttribute(rs_down_kernel<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(RS_DOWN_SMEM));
+        cudaFuncSetAttribute(rs_down_kernel<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(RS_DOWN_SMEM));
+        return true;
+    }();
+    (void)configured;
     for (int a = 0; a < passes; ++a) {
         bool fst = a == 0, lst = a == passes - 1;
         int shift = 8 * active[a];
-        unsigned epoch = next_epoch(ctx);
-        const unsigned *bb = bases + a * RADIX;
         int src = cur, dst = passes > 2 ? 1 - cur : 0;
+        if (fst) rs_up_kernel<true><<<tiles, RS_THREADS, 0, ctx->stream>>>(keys, nullptr, n, shift, tiles, counts);
+        else rs_up_kernel<false><<<tiles, RS_THREADS, 0, ctx->stream>>>(nullptr, img[src], n, shift, tiles, counts);
+        rs_scan_sums<<<chunks, SCAN_THREADS, 0, ctx->stream>>>(counts, m, sums);
+        rs_scan_top<<<1, 1024, 0, ctx->stream>>>(sums, chunks);
+        rs_scan_apply<<<chunks, SCAN_THREADS, 0, ctx->stream>>>(counts, m, sums, offs);
         if (fst && lst)
-            rs_pass_kernel<true, true><<<tiles, RS_THREADS, 0, ctx->stream>>>(keys, nullptr, nullptr, nullptr, nullptr, oo, n, shift, bb, status, tiles, epoch, ctx->counters, ctx->status);
+            rs_down_kernel<true, true><<<tiles, RS_THREADS, RS_DOWN_SMEM, ctx->stream>>>(keys, nullptr, nullptr, nullptr, nullptr, oo, n, shift, tiles, offs);
         else if (fst)
-            rs_pass_kernel<true, false><<<tiles, RS_THREADS, 0, ctx->stream>>>(keys, nullptr, nullptr, img[0], pos[0], nullptr, n, shift, bb, status, tiles, epoch, ctx->counters, ctx->status);
+            rs_down_kernel<true, false><<<tiles, RS_THREADS, RS_DOWN_SMEM, ctx->stream>>>(keys, nullptr, nullptr, img[0], pos[0], nullptr, n, shift, tiles, offs);
         else if (lst)
-            rs_pass_kernel<false, true><<<tiles, RS_THREADS, 0, ctx->stream>>>(nullptr, img[src], pos[src], nullptr, nullptr, oo, n, shift, bb, status, tiles, epoch, ctx->counters, ctx->status);
+            rs_down_kernel<false, true><<<tiles, RS_THREADS, RS_DOWN_SMEM, ctx->stream>>>(nullptr, img[src], pos[src], nullptr, nullptr, oo, n, shift, tiles, offs);
         else
-            rs_pass_kernel<false, false><<<tiles, RS_THREADS, 0, ctx->stream>>>(nullptr, img[src], pos[src], img[dst], pos[dst], nullptr, n, shift, bb, status, tiles, epoch, ctx->counters, ctx->status);
+            rs_down_kernel<false, false><<<tiles, RS_THREADS, RS_DOWN_SMEM, ctx->stream>>>(nullptr, img[src], pos[src], img[dst], pos[dst], nullptr, n, shift, tiles, offs);
         if ((st = launched(ctx, "rs_pass"))) {
             cleanup();
             return release(st);
