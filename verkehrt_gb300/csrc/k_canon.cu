@@ -17,16 +17,22 @@
 //    RNE(x/u) depends on S only through its parity when x/u is exactly halfway. So the effect
 //    of a run of rows on S is a pair of integer increments (d0, d1) for even and odd S: a
 //    "transfer function". Transfer functions compose associatively.
-//  * Each 8192-row tile (512 blocks of 16 rows) computes, per lane and per 256-row segment,
-//    the transfer functions for the one or two binades its running sum can be in. The binade
-//    comes from an approximate prefix of the lane sums found by a first decoupled lookback
-//    over the tiles (float sums, with a 2^-12 relative margin).
-//  * A second decoupled lookback composes the predecessors' tile transfer functions until
-//    it reaches a published exact lane state; the tile then walks its segments from its exact
-//    start, applying each transfer function whose binade and bound check out, and adding the
-//    rows of any other segment one by one with IEEE f64 adds (the reference's own operation).
-//    Negative, infinite or NaN rows, the first rows of a lane and binade crossings take this
-//    sequential path, so the result is the reference's in every case.
+//  * The rows are cut into 4096-row tiles (256 blocks of 16 rows, 256 rows per lane, in 32
+//    segments of 8 blocks), and five kernels, none of which waits on another block, find the
+//    exact lane states:
+//      K1  the approximate (float) lane sums of every tile, in one read of the rows;
+//      K2  per lane, their exclusive prefix over the tiles from the lane's exact state, and each
+//          tile's candidate binades (the approximate range widened by 2^-12 must lie in one
+//          binade or two adjacent ones);
+//      K3  each tile's transfer function per lane and candidate binade, in a second read;
+//      K4a per lane and 32-tile chunk, the composed transfer function when the chunk's tiles
+//          share one;
+//      K4b per lane, a walk from the exact state: whole chunks while their transfer function
+//          holds, single tiles in mixed chunks, and the tiles none carries (binade crossings,
+//          negative, infinite or NaN rows, the first rows of a lane) resolved from the rows by
+//          a warp that recomputes their segments' transfer functions and adds the rows of any
+//          segment without one one by one with IEEE f64 adds (the reference's own operation).
+//    So the result is the reference's in every case.
 //
 // All of the per-row work is integer arithmetic: GB300 executes FP64 adds at about 1/66 of
 // its integer op rate, so an FP64 tree would be compute-bound well below the HBM roofline.
