@@ -185,7 +185,10 @@ struct CanonWork {
     TF *recD;                  // [16][T][2]
     int *chunkE;               // [16][C] binade of each 32-tile chunk's transfer function
     TF *chunkD;                // [16][C]
+    double *gsum;              // [16][G] approximate sum of each group of CAND_GROUP tiles
 };
+
+constexpr int CAND_GROUP = 1024;  // tiles per K2 block
 
 __device__ __forceinline__ TF shfl_tf(TF v, int src) {
     return TF{__shfl_sync(FULL, v.d0, src), __shfl_sync(FULL, v.d1, src)};
@@ -256,53 +259,94 @@ __global__ void __launch_bounds__(CT_THREADS) canon_apx_kernel(RowArgs args, int
     }
 }
 
-// K2: per lane (one block each), the exclusive prefix of the approximate sums over tiles,
-// from the lane's exact state, and each tile's candidate binades: the range [start, end]
-// widened by 2^-12 on each side must lie in one binade or two adjacent ones.
-__global__ void __launch_bounds__(1024) canon_cand_kernel(int T, CanonWork wk, const CanonState *state) {
-    const int L = blockIdx.x, t = threadIdx.x;
-    const float *a = wk.apx + static_cast<int64_t>(L) * T;
-    const int per = (T + 1023) / 1024;
-    const int t0 = min(T, t * per), t1 = min(T, t0 + per);
-    double sum = 0;
-    for (int k = t0; k < t1; ++k) sum += static_cast<double>(a[k]);
-    // Block inclusive scan of the thread sums: warps, then across warps.
-    const int lane = t & 31, w = t >> 5;
-    double x = sum;
+// Block-wide sum and exclusive prefix of one double per thread (blockDim.x a multiple of 32).
+__device__ double block_sum_f64(double v) {
+    __shared__ double s_w[32];
+    __shared__ double s_total;
+    v = warp_sum(v);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    __syncthreads();
+    if (lane == 0) s_w[w] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0;
+        for (int i = 0; i < nw; ++i) t += s_w[i];
+        s_total = t;
+    }
+    __syncthreads();
+    return s_total;
+}
+__device__ double block_exclusive_f64(double v, double *total) {
+    __shared__ double s_w[32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    double x = v;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-        double y = __shfl_up_sync(FULL, x, o);
+        const double y = __shfl_up_sync(FULL, x, o);
         if (lane >= o) x += y;
     }
-    __shared__ double s_w[32];
+    __syncthreads();
     if (lane == 31) s_w[w] = x;
     __syncthreads();
     if (w == 0) {
-        double z = s_w[lane];
+        double z = lane < nw ? s_w[lane] : 0.0;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-            double y = __shfl_up_sync(FULL, z, o);
+            const double y = __shfl_up_sync(FULL, z, o);
             if (lane >= o) z += y;
         }
         s_w[lane] = z;
     }
     __syncthreads();
-    double pre = (w ? s_w[w - 1] : 0.0) + x - sum + as_f64(state->lanes[L]);
-    for (int k = t0; k < t1; ++k) {
-        double A = static_cast<double>(a[k]);
-        double lo = A < 0 ? pre + A : pre, hi = A < 0 ? pre : pre + A;
-        int elo = binade(lo * (1.0 - 0x1p-12)), ehi = binade(hi * (1.0 + 0x1p-12));
-        int c0 = NO_E, c1 = NO_E;
-        if (elo != NO_E && ehi != NO_E && elo >= -959) {
-            if (ehi == elo) c0 = elo;
-            else if (ehi == elo + 1) {
-                c0 = elo;
-                c1 = ehi;
-            }
-        }
-        *reinterpret_cast<int2 *>(&wk.cand[(k * 16 + L) * 2]) = make_int2(c0, c1);
-        pre += A;
+    *total = s_w[nw - 1];
+    return (w ? s_w[w - 1] : 0.0) + x - v;
+}
+
+// K2a: per lane and group of CAND_GROUP tiles (one block each), the approximate sum of the
+// group's tiles.
+__global__ void __launch_bounds__(256) canon_gsum_kernel(int T, int G, CanonWork wk) {
+    const int L = blockIdx.x / G, g = blockIdx.x % G;
+    const float *a = wk.apx + static_cast<int64_t>(L) * T;
+    double s = 0;
+    for (int k = g * CAND_GROUP + threadIdx.x; k < min(T, (g + 1) * CAND_GROUP); k += 256) s += static_cast<double>(a[k]);
+    s = warp_sum(s);
+    __shared__ double s_w[8];
+    if ((threadIdx.x & 31) == 0) s_w[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0;
+        for (int w = 0; w < 8; ++w) t += s_w[w];
+        wk.gsum[L * G + g] = t;
     }
+}
+
+// K2b: per lane and group (one block each, one thread per tile), the exclusive prefix of the
+// approximate sums over the lane's tiles from its exact state, and each tile's candidate
+// binades: the range [start, end] widened by 2^-12 on each side must lie in one binade or two
+// adjacent ones.
+__global__ void __launch_bounds__(CAND_GROUP) canon_cand_kernel(int T, int G, CanonWork wk, const CanonState *state) {
+    const int L = blockIdx.x / G, g = blockIdx.x % G, t = threadIdx.x;
+    const int k = g * CAND_GROUP + t;
+    const double A = k < T ? static_cast<double>(wk.apx[static_cast<int64_t>(L) * T + k]) : 0.0;
+    // The groups before this one (at most G values), then this group's exclusive prefix.
+    double before = t < g ? wk.gsum[L * G + t] : 0.0;
+    for (int i = t + CAND_GROUP; i < g; i += CAND_GROUP) before += wk.gsum[L * G + i];
+    double ex_total;
+    const double base = block_sum_f64(before);
+    const double ex = block_exclusive_f64(A, &ex_total);
+    if (k >= T) return;
+    const double pre = as_f64(state->lanes[L]) + base + ex;
+    const double lo = A < 0 ? pre + A : pre, hi = A < 0 ? pre : pre + A;
+    const int elo = binade(lo * (1.0 - 0x1p-12)), ehi = binade(hi * (1.0 + 0x1p-12));
+    int c0 = NO_E, c1 = NO_E;
+    if (elo != NO_E && ehi != NO_E && elo >= -959) {
+        if (ehi == elo) c0 = elo;
+        else if (ehi == elo + 1) {
+            c0 = elo;
+            c1 = ehi;
+        }
+    }
+    *reinterpret_cast<int2 *>(&wk.cand[(static_cast<int64_t>(k) * 16 + L) * 2]) = make_int2(c0, c1);
 }
 
 // K3: each tile's transfer function per lane and candidate binade (NO_E when a segment does
@@ -616,7 +660,10 @@ static vkc_status launch_canon(vkc_ctx *ctx, const RowArgs &a, int64_t nb, int T
     vkc_status st;
     canon_apx_kernel<OP, ALIGNED><<<T, CT_THREADS, 0, ctx->stream>>>(a, nb, T, wk);
     if ((st = launched(ctx, "canon_apx"))) return st;
-    canon_cand_kernel<<<16, 1024, 0, ctx->stream>>>(T, wk, state);
+    const int G = (T + CAND_GROUP - 1) / CAND_GROUP;
+    canon_gsum_kernel<<<16 * G, 256, 0, ctx->stream>>>(T, G, wk);
+    if ((st = launched(ctx, "canon_gsum"))) return st;
+    canon_cand_kernel<<<16 * G, CAND_GROUP, 0, ctx->stream>>>(T, G, wk, state);
     if ((st = launched(ctx, "canon_cand"))) return st;
     canon_tf_kernel<OP, ALIGNED><<<T, CT_THREADS, 0, ctx->stream>>>(a, nb, T, wk);
     if ((st = launched(ctx, "canon_tf"))) return st;
@@ -683,13 +730,16 @@ struct CanonReducer : DevReducer {
             const size_t o_recD = o_recE + ((t16 * 8 + 255) & ~size_t(255));
             const size_t o_chE = o_recD + t16 * 2 * sizeof(TF);
             const size_t o_chD = o_chE + ((c16 * 4 + 255) & ~size_t(255));
-            const size_t total = o_chD + c16 * sizeof(TF);
+            const size_t g16 = static_cast<size_t>((T + CAND_GROUP - 1) / CAND_GROUP) * 16;
+            const size_t o_gs = o_chD + ((c16 * sizeof(TF) + 255) & ~size_t(255));
+            const size_t total = o_gs + g16 * sizeof(double);
             void *p;
             if ((st = scratch(ctx, total, &p))) return st;
             char *b = static_cast<char *>(p);
             CanonWork wk{reinterpret_cast<float *>(b), reinterpret_cast<int *>(b + o_cand),
                          reinterpret_cast<int *>(b + o_recE), reinterpret_cast<TF *>(b + o_recD),
-                         reinterpret_cast<int *>(b + o_chE), reinterpret_cast<TF *>(b + o_chD)};
+                         reinterpret_cast<int *>(b + o_chE), reinterpret_cast<TF *>(b + o_chD),
+                         reinterpret_cast<double *>(b + o_gs)};
             const bool aligned = (reinterpret_cast<uintptr_t>(a.x) & 15) == 0 &&
                                  (op != ROW_DOT || (reinterpret_cast<uintptr_t>(a.y) & 15) == 0);
             switch (op) {
