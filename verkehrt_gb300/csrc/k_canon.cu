@@ -352,7 +352,7 @@ __global__ void __launch_bounds__(CAND_GROUP) canon_cand_kernel(int T, int G, Ca
 // K3: each tile's transfer function per lane and candidate binade (NO_E when a segment does
 // not take the integer step in that binade).
 template <int OP, bool ALIGNED>
-__global__ void __launch_bounds__(CT_THREADS) canon_tf_kernel(RowArgs args, int64_t nb, int T, CanonWork wk) {
+__global__ void __launch_bounds__(CT_THREADS, 4) canon_tf_kernel(RowArgs args, int64_t nb, int T, CanonWork wk) {
     __shared__ TF s_tf[2][CT_SEGS][16];
     __shared__ unsigned char s_ok[2][CT_SEGS][16];
     __shared__ int s_E[16][2];
@@ -374,18 +374,30 @@ __global__ void __launch_bounds__(CT_THREADS) canon_tf_kernel(RowArgs args, int6
         }
     }
     __syncthreads();
-    if (t < 32) {
-        const int L = t >> 1, c = t & 1;
-        int E = s_E[L][c];
-        TF f{0, 0};
-        bool ok = E != NO_E;
-        for (int s = 0; s < CT_SEGS && ok; ++s) {
-            ok = s_ok[c][s][L];
-            f = compose(f, s_tf[c][s][L]);
+    // The 32 (lane, candidate) pairs, four per warp: lane s of the warp holds segment s, and an
+    // ordered scan (earlier segments on the left) composes them.
+    static_assert(CT_SEGS == 32 && CT_THREADS == 256, "one warp lane per segment, four pairs per warp");
+    const int sl = t & 31, wp = t >> 5;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int pair = wp * 4 + q, L = pair >> 1, c = pair & 1;
+        const int E = s_E[L][c];
+        if (E == NO_E) {
+            if (sl == 0) wk.recE[(static_cast<int64_t>(L) * T + tile) * 2 + c] = NO_E;
+            continue;
         }
-        const int64_t at = (static_cast<int64_t>(L) * T + tile) * 2 + c;
-        wk.recE[at] = ok ? E : NO_E;
-        wk.recD[at] = f;
+        TF f = s_tf[c][sl][L];
+        const bool ok = __all_sync(FULL, s_ok[c][sl][L] != 0);
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const TF y = shfl_up_tf(f, o);
+            if (sl >= o) f = compose(y, f);
+        }
+        if (sl == 31) {
+            const int64_t at = (static_cast<int64_t>(L) * T + tile) * 2 + c;
+            wk.recE[at] = ok ? E : NO_E;
+            wk.recD[at] = f;
+        }
     }
 }
 
