@@ -55,7 +55,7 @@ CmpRange cmp_range(int cmp, double c) {
 // ------------------------------------------------------------------ count
 
 // Counts rows with x <cmp> c (as a key range) or, for `count` over bool, nonzero bytes.
-template <bool BOOL>
+template <bool BOOL, bool POS>
 __global__ void __launch_bounds__(256) count_kernel(const void *__restrict__ xv, int64_t n,
                                                     CmpRange r, unsigned long long *partials,
                                                     unsigned *done, unsigned long long *state) {
@@ -86,7 +86,7 @@ __global__ void __launch_bounds__(256) count_kernel(const void *__restrict__ xv,
         const unsigned long long *x = static_cast<const unsigned long long *>(xv);
         int64_t head = (reinterpret_cast<uintptr_t>(x) & 15) ? 1 : 0;
         if (head > n) head = n;
-        if (head && tid == 0) c += in_range(r, x[0]);
+        if (head && tid == 0) c += in_range_t<POS>(r, x[0]);
         const ulonglong2 *x2 = reinterpret_cast<const ulonglong2 *>(x + head);
         int64_t n2 = (n - head) >> 1;
         // Four independent 16-byte loads per thread in flight.
@@ -97,9 +97,9 @@ __global__ void __launch_bounds__(256) count_kernel(const void *__restrict__ xv,
                 v[u] = i + u * stride < n2 ? __ldcs(&x2[i + u * stride]) : make_ulonglong2(~0ull, ~0ull);
 #pragma unroll
             for (int u = 0; u < 4; ++u)
-                if (i + u * stride < n2) c += in_range(r, v[u].x) + in_range(r, v[u].y);
+                if (i + u * stride < n2) c += in_range_t<POS>(r, v[u].x) + in_range_t<POS>(r, v[u].y);
         }
-        if (((n - head) & 1) && tid == 0) c += in_range(r, x[n - 1]);
+        if (((n - head) & 1) && tid == 0) c += in_range_t<POS>(r, x[n - 1]);
     }
     c = warp_sum(c);
     __shared__ unsigned long long ws[8];
@@ -136,13 +136,14 @@ struct CountReducer : DevReducer {
         void *part;
         if ((st = scratch(ctx, sizeof(unsigned long long) * grid, &part))) return st;
         auto *s = static_cast<unsigned long long *>(state);
-        if (cmp < 0)
-            count_kernel<true><<<grid, 256, 0, ctx->stream>>>(args[0].a->data(), n, CmpRange{},
-                static_cast<unsigned long long *>(part), ctx->counters + 1, s);
-        else
-            count_kernel<false><<<grid, 256, 0, ctx->stream>>>(args[0].a->data(), n,
-                cmp_range(cmp, args[1].f64()), static_cast<unsigned long long *>(part),
-                ctx->counters + 1, s);
+        auto *pp = static_cast<unsigned long long *>(part);
+        if (cmp < 0) {
+            count_kernel<true, false><<<grid, 256, 0, ctx->stream>>>(args[0].a->data(), n, CmpRange{}, pp, ctx->counters + 1, s);
+        } else {
+            const CmpRange r = cmp_range(cmp, args[1].f64());
+            if (pos_range(r)) count_kernel<false, true><<<grid, 256, 0, ctx->stream>>>(args[0].a->data(), n, r, pp, ctx->counters + 1, s);
+            else count_kernel<false, false><<<grid, 256, 0, ctx->stream>>>(args[0].a->data(), n, r, pp, ctx->counters + 1, s);
+        }
         return launched(ctx, "count");
     }
     vkc_status finish(vkc_ctx *ctx, vkc_scalar *out) override {

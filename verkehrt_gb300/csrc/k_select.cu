@@ -49,7 +49,7 @@ __device__ __forceinline__ unsigned nonzero_bytes(unsigned v) {
 // on consecutive rows. A filter's count keeps its ballots in the slot, so the stage touches
 // only the steps and rows that survive. A tile that is not whole, or not 16-byte aligned, is
 // read from global memory instead of the slot.
-template <int KIND, int W> struct SelectPass {
+template <int KIND, int W, bool POS = false> struct SelectPass {
     static constexpr int THREADS = SEL_THREADS;
     using R = CountRec;
     using V = unsigned long long;
@@ -80,7 +80,7 @@ template <int KIND, int W> struct SelectPass {
         if (VAL_BYTES) bulk_load(slot, static_cast<const T *>(a.x) + r0, VAL_BYTES, bar);
         if (MASK_BYTES) bulk_load(slot + VAL_BYTES, a.m + r0, MASK_BYTES, bar);
     }
-    __device__ bool keep_filter(unsigned long long v) const { return in_range(a.r, v); }
+    __device__ bool keep_filter(unsigned long long v) const { return in_range_t<POS>(a.r, v); }
 
     // The slice's keys from `keys` (the slot, or global memory at the tile's first row).
     template <class K> __device__ unsigned count_keys(const K *keys, int64_t r0) const {
@@ -264,11 +264,11 @@ template <int KIND, int W> struct SelectPass {
     __device__ void last_tile(V inclusive) const { *a.total = inclusive; }
 };
 
-template <int KIND, int W>
+template <int KIND, int W, bool POS>
 __global__ void __launch_bounds__(SEL_THREADS + 64, SEL_BLOCKS) select_kernel(SelArgs a, int tiles, unsigned long long *recs,
                                                                      unsigned epoch, unsigned *counters,
                                                                      DevStatus *status) {
-    SelectPass<KIND, W> p{a};
+    SelectPass<KIND, W, POS> p{a};
     tile_pass<SEL_WINDOW>(p, recs, tiles, epoch, counters, status, 0ull);
 }
 
@@ -290,12 +290,24 @@ static vkc_status run_select(vkc_ctx *ctx, SelArgs a, int64_t n, Builder *b) {
     a.aligned = (reinterpret_cast<uintptr_t>(a.x) & 15) == 0 && (reinterpret_cast<uintptr_t>(a.m) & 15) == 0;
     constexpr size_t smem = SEL_SLOTS * SelectPass<KIND, W>::SLOT_BYTES;
     static const bool configured = [] {
-        cudaFuncSetAttribute(select_kernel<KIND, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+        cudaFuncSetAttribute(select_kernel<KIND, W, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+        if constexpr (KIND == SEL_FILTER)
+            cudaFuncSetAttribute(select_kernel<KIND, W, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
         return true;
     }();
     (void)configured;
-    const int grid = tile_pass_grid(ctx, select_kernel<KIND, W>, SEL_THREADS + 64, smem, tiles);
-    select_kernel<KIND, W><<<grid, SEL_THREADS + 64, smem, ctx->stream>>>(a, tiles, recs, epoch, ctx->counters, ctx->status);
+    bool launched_pos = false;
+    if constexpr (KIND == SEL_FILTER) {
+        if (pos_range(a.r)) {
+            const int grid = tile_pass_grid(ctx, select_kernel<KIND, W, true>, SEL_THREADS + 64, smem, tiles);
+            select_kernel<KIND, W, true><<<grid, SEL_THREADS + 64, smem, ctx->stream>>>(a, tiles, recs, epoch, ctx->counters, ctx->status);
+            launched_pos = true;
+        }
+    }
+    if (!launched_pos) {
+        const int grid = tile_pass_grid(ctx, select_kernel<KIND, W, false>, SEL_THREADS + 64, smem, tiles);
+        select_kernel<KIND, W, false><<<grid, SEL_THREADS + 64, smem, ctx->stream>>>(a, tiles, recs, epoch, ctx->counters, ctx->status);
+    }
     if ((st = launched(ctx, "select"))) return st;
     DevStatus ds;
     if ((st = read_status(ctx, &ds))) return st;

@@ -45,6 +45,17 @@ __device__ __forceinline__ bool in_range(const CmpRange &r, unsigned long long b
     return in != static_cast<bool>(r.negate);
 }
 
+// in_range for a non-empty, non-negated range of non-negative keys (pos_range): there a key is
+// the value's bits, and a negative value's bits, read unsigned, lie above every such range, so
+// one unsigned comparison decides.
+__host__ __device__ __forceinline__ bool pos_range(const CmpRange &r) { return r.lo >= 0 && r.lo <= r.hi && !r.negate; }
+__device__ __forceinline__ bool in_pos_range(const CmpRange &r, unsigned long long bits) {
+    return bits - static_cast<unsigned long long>(r.lo) <= static_cast<unsigned long long>(r.hi - r.lo);
+}
+template <bool POS> __device__ __forceinline__ bool in_range_t(const CmpRange &r, unsigned long long bits) {
+    return POS ? in_pos_range(r, bits) : in_range(r, bits);
+}
+
 // ------------------------------------------------------------------ lookback flags
 
 __device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
