@@ -183,6 +183,31 @@ template <bool BY> struct ScanPass {
         const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
         const int64_t r0 = static_cast<int64_t>(tile) * SC_TILE;
         const bool sm = whole(tile);
+        if constexpr (!BY) {
+            // Without segments: a plain wrapping add scan of the slice, in place.
+            unsigned long long carry = 0;
+#pragma unroll
+            for (int s = 0; s < SC_STEPS; ++s) {
+                const int j = w * SC_SLICE + s * (32 * SC_VEC) + lane * SC_VEC;
+                unsigned long long v[SC_VEC];
+                unsigned f;
+                load_step(sm, slot, j, r0 + j, v, f);
+#pragma unroll
+                for (int k = 1; k < SC_VEC; ++k) v[k] += v[k - 1];
+                unsigned long long inc = v[SC_VEC - 1];
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const unsigned long long y = __shfl_up_sync(FULL, inc, o);
+                    if (lane >= o) inc += y;
+                }
+                const unsigned long long pre = carry + inc - v[SC_VEC - 1];
+                ulonglong2 *p = reinterpret_cast<ulonglong2 *>(reinterpret_cast<unsigned long long *>(slot) + j);
+                p[0] = ulonglong2{v[0] + pre, v[1] + pre};
+                p[1] = ulonglong2{v[2] + pre, v[3] + pre};
+                carry += __shfl_sync(FULL, inc, 31);
+            }
+            return Staged{};
+        }
         Seg carry{0, 0};  // the slice so far
 #pragma unroll
         for (int s = 0; s < SC_STEPS; ++s) {
@@ -227,10 +252,15 @@ template <bool BY> struct ScanPass {
             const ulonglong2 *p = reinterpret_cast<const ulonglong2 *>(reinterpret_cast<const unsigned long long *>(slot) + j);
             const ulonglong2 u0 = p[0], u1 = p[1];
             unsigned long long e[4] = {u0.x, u0.y, u1.x, u1.y};
-            const unsigned has = *reinterpret_cast<const unsigned *>(slot + VAL_BYTES + j);
+            if constexpr (BY) {
+                const unsigned has = *reinterpret_cast<const unsigned *>(slot + VAL_BYTES + j);
 #pragma unroll
-            for (int k = 0; k < SC_VEC; ++k)
-                if (!((has >> (8 * k)) & 0xffu)) e[k] += pre.sum;
+                for (int k = 0; k < SC_VEC; ++k)
+                    if (!((has >> (8 * k)) & 0xffu)) e[k] += pre.sum;
+            } else {
+#pragma unroll
+                for (int k = 0; k < SC_VEC; ++k) e[k] += pre.sum;
+            }
             if (aligned && i0 + SC_VEC <= n) {
                 ulonglong4_32a u;
                 u.x = e[0];
