@@ -201,6 +201,42 @@ VKC_API vkc_status vkc_elementwise_tile(vkc_ctx *ctx, int id, const vkc_value *a
 VKC_API vkc_status vkc_scan_add_i64_noalloc(int device, const int64_t *in, int64_t *out, int64_t n,
                                             void *stream, char *err, size_t err_len);
 
+/* ------------------------------------------------------------------ batches and graphs */
+
+/* A batch: many arrays of one element type that run the same planned statement. The
+ * reference's executor (src/exec.rs:162-231, Strategy :77-91) runs a statement once per array;
+ * a batch runs it once for all of them, as one persistent launch, with no host synchronisation
+ * inside the batch entries, so a sequence of them can be captured in a graph (below) and
+ * replayed. These entries have no counterpart in the reference's kernel table. The batch
+ * retains its arrays. vkc_batch_new copies the array table to the device (and waits for it). */
+typedef struct vkc_batch vkc_batch;
+VKC_API vkc_status vkc_batch_new(vkc_ctx *ctx, int n, vkc_array *const *arrays, vkc_batch **out);
+VKC_API void vkc_batch_free(vkc_batch *b);
+VKC_API int vkc_batch_len(const vkc_batch *b);
+
+/* For every f64 array i of the batch, sums[i] = reduce_add_f64(filter_<cmp>_f64(array i, c)),
+ * bit for bit (the reference's canonical order over the compacted rows). cmp: 0 eq, 1 ne, 2 lt,
+ * 3 le, 4 gt, 5 ge (the reference's Cmp, src/kernels/scalar/fused.rs:45-54). `sums` is an f64
+ * array of the batch's length. */
+VKC_API vkc_status vkc_batch_filter_sum_f64(vkc_ctx *ctx, vkc_batch *b, int cmp, double c, vkc_array *sums);
+
+/* For every i64 array i of `keys`, the stable ascending positions (argsort_i64) into the i64
+ * array i of `outs` (same lengths). key_digits: bit d set when byte d of the keys' sign-flipped
+ * image varies (0: all eight); a caller that knows its key range saves the passes of constant
+ * bytes. The first call on a (keys, outs) pair allocates scratch: make it before capturing, and
+ * give key_digits when capturing. */
+VKC_API vkc_status vkc_batch_argsort_i64(vkc_ctx *ctx, vkc_batch *keys, const vkc_batch *outs,
+                                         unsigned key_digits);
+
+/* A CUDA graph of the work the library enqueues on ctx's stream between vkc_graph_begin and
+ * vkc_graph_end (stream capture; only enqueue-only entries, such as the batch entries above,
+ * may run in between), replayed by vkc_graph_launch. */
+typedef struct vkc_graph vkc_graph;
+VKC_API vkc_status vkc_graph_begin(vkc_ctx *ctx);
+VKC_API vkc_status vkc_graph_end(vkc_ctx *ctx, vkc_graph **out);
+VKC_API vkc_status vkc_graph_launch(vkc_ctx *ctx, vkc_graph *g);
+VKC_API void vkc_graph_free(vkc_graph *g);
+
 #ifdef __cplusplus
 }
 #endif

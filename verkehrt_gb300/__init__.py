@@ -93,6 +93,15 @@ _SIGNATURES = {
                                             _P]),
     "vkc_scan_add_i64_noalloc": (ctypes.c_int, [ctypes.c_int, _P, _P, ctypes.c_int64, _P,
                                                 ctypes.c_char_p, ctypes.c_size_t]),
+    "vkc_batch_new": (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(_P), ctypes.POINTER(_P)]),
+    "vkc_batch_free": (None, [_P]),
+    "vkc_batch_len": (ctypes.c_int, [_P]),
+    "vkc_batch_filter_sum_f64": (ctypes.c_int, [_P, _P, ctypes.c_int, ctypes.c_double, _P]),
+    "vkc_batch_argsort_i64": (ctypes.c_int, [_P, _P, _P, ctypes.c_uint]),
+    "vkc_graph_begin": (ctypes.c_int, [_P]),
+    "vkc_graph_end": (ctypes.c_int, [_P, ctypes.POINTER(_P)]),
+    "vkc_graph_launch": (ctypes.c_int, [_P, _P]),
+    "vkc_graph_free": (None, [_P]),
 }
 
 _lib = None
@@ -353,6 +362,27 @@ class Context:
     def stream(self):
         return _lib.vkc_get_stream(self.handle)
 
+    # ---------------------------------------------------------------- batches and graphs
+
+    def batch(self, arrays):
+        return Batch(self, arrays)
+
+    def batch_filter_sum(self, batch, cmp, c, sums):
+        """sums[i] = reduce_add_f64(filter_<cmp>_f64(batch[i], c)) for every array (enqueued)."""
+        self._check(_lib.vkc_batch_filter_sum_f64(self.handle, batch.handle, CMPS.index(cmp), c, sums.handle))
+
+    def batch_argsort(self, keys, outs, key_digits=0):
+        """outs[i] = argsort_i64(keys[i]) for every array (enqueued)."""
+        self._check(_lib.vkc_batch_argsort_i64(self.handle, keys.handle, outs.handle, key_digits))
+
+    def graph_begin(self):
+        self._check(_lib.vkc_graph_begin(self.handle))
+
+    def graph_end(self):
+        h = _P()
+        self._check(_lib.vkc_graph_end(self.handle, ctypes.byref(h)))
+        return Graph(self, h.value)
+
 
 class Reducer:
     """Dispatch::reducer: tile-fed reduction state (every update but the last has a multiple
@@ -415,3 +445,40 @@ class Builder:
     def __del__(self):
         if getattr(self, "handle", None) and _lib is not None:
             _lib.vkc_builder_free(self.handle)
+
+
+CMPS = ["eq", "ne", "lt", "le", "gt", "ge"]
+
+
+class Batch:
+    """Many arrays of one type that run the same statement (vkc_batch); keeps them alive."""
+
+    def __init__(self, ctx, arrays):
+        self.ctx = ctx
+        self.arrays = list(arrays)
+        handles = (_P * max(1, len(self.arrays)))(*[a.handle for a in self.arrays])
+        h = _P()
+        ctx._check(_lib.vkc_batch_new(ctx.handle, len(self.arrays), handles, ctypes.byref(h)))
+        self.handle = h.value
+
+    def __len__(self):
+        return len(self.arrays)
+
+    def __del__(self):
+        if getattr(self, "handle", None) and _lib is not None:
+            _lib.vkc_batch_free(self.handle)
+
+
+class Graph:
+    """A captured CUDA graph of enqueued library work (vkc_graph)."""
+
+    def __init__(self, ctx, handle):
+        self.ctx = ctx
+        self.handle = handle
+
+    def launch(self):
+        self.ctx._check(_lib.vkc_graph_launch(self.ctx.handle, self.handle))
+
+    def __del__(self):
+        if getattr(self, "handle", None) and _lib is not None:
+            _lib.vkc_graph_free(self.handle)

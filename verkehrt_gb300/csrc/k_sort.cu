@@ -375,6 +375,45 @@ static vkc_status argsort_i64(vkc_ctx *ctx, const vkc_value *args, int nargs, vk
     return VKC_OK;
 }
 
+// Stable LSD passes over (image, position) pairs that are already in img[0] / pos[0], one per
+// entry of `shifts`, ping-ponging between the two buffers; *which gets the buffer that holds
+// the result. counts and offs hold RADIX * ceil(n / RS_TILE) words and sums
+// ceil(that / SCAN_CHUNK). Enqueue only: no host synchronisation and no allocation.
+vkc_status radix_pairs(vkc_ctx *ctx, unsigned long long *img[2], unsigned *pos[2], int64_t n, const int *shifts,
+                       int npasses, unsigned *counts, unsigned *offs, unsigned *sums, int *which) {
+    vkc_status st;
+    const int tiles = static_cast<int>((n + RS_TILE - 1) / RS_TILE);
+    const int64_t m = static_cast<int64_t>(RADIX) * tiles;
+    const int chunks = static_cast<int>((m + SCAN_CHUNK - 1) / SCAN_CHUNK);
+    static const bool configured = [] {
+        cudaFuncSetAttribute(rs_down_kernel<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             static_cast<int>(RS_DOWN_SMEM));
+        return true;
+    }();
+    (void)configured;
+    int cur = 0;
+    for (int a = 0; a < npasses; ++a) {
+        const int shift = shifts[a];
+        rs_up_kernel<false><<<tiles, RS_THREADS, 0, ctx->stream>>>(nullptr, img[cur], n, shift, tiles, counts);
+        rs_scan_sums<<<chunks, SCAN_THREADS, 0, ctx->stream>>>(counts, m, sums);
+        rs_scan_top<<<1, 1024, 0, ctx->stream>>>(sums, chunks);
+        rs_scan_apply<<<chunks, SCAN_THREADS, 0, ctx->stream>>>(counts, m, sums, offs);
+        rs_down_kernel<false, false><<<tiles, RS_THREADS, RS_DOWN_SMEM, ctx->stream>>>(
+            nullptr, img[cur], pos[cur], img[1 - cur], pos[1 - cur], nullptr, n, shift, tiles, offs);
+        if ((st = launched(ctx, "radix_pairs"))) return st;
+        cur = 1 - cur;
+    }
+    *which = cur;
+    return VKC_OK;
+}
+
+// Words of the radix_pairs scratch for n rows: counts/offs each, and sums.
+void radix_pairs_scratch(int64_t n, int64_t *count_words, int64_t *sum_words) {
+    const int64_t tiles = (n + RS_TILE - 1) / RS_TILE;
+    *count_words = static_cast<int64_t>(RADIX) * tiles;
+    *sum_words = (*count_words + SCAN_CHUNK - 1) / SCAN_CHUNK;
+}
+
 void register_sort(std::vector<KernelDef> &t) {
     // index.rs:241-255: cost = key width + 8.
     KernelDef d{"argsort_i64", VKC_WHOLE, {InSpec{IN_ARRAY, VKC_I64}}, true, VKC_I64, 16};
