@@ -296,6 +296,85 @@ def run_config3(ctx, n, stream, steps, warmup):
                         "histogram" % (n.bit_length() - 1), "steps": steps, "warmup": warmup, **out}
 
 
+# ---------------------------------------------------------------------------- config 4
+
+
+def config4_lengths(count, lo, hi, seed=13):
+    """Lengths floor(2^U), U uniform in [lo, hi], from a seeded splitmix stream."""
+    u = (splitmix64_np(np.arange(seed, seed + count, dtype=np.uint64)) >> np.uint64(11)).astype(np.float64) * 2.0 ** -53
+    return np.floor(2.0 ** (lo + (hi - lo) * u)).astype(np.int64)
+
+
+def run_config4(ctx, count=4096, lo=10, hi=18, reps=2):
+    """Config 4: `count` independent arrays, each running filter_gt(0.9) -> sum on f64 values and
+    argsort of i64 keys below 2^16, three ways: the plain per-array GPU path (one synchronous
+    call per statement, as the reference executor runs them), the batched entries (one
+    persistent launch for the filter-sum, one batched radix sort), and a captured CUDA graph of
+    the batch replayed. Each timed run includes reading the sums back to the host."""
+    lens = config4_lengths(count, lo, hi)
+    xs = [ctx.call("rand_f64", int(n), 100 + i) for i, n in enumerate(lens)]
+    ks = [ctx.call("and_i64", ctx.call("rand_i64", int(n), 50_000 + i), 0xFFFF) for i, n in enumerate(lens)]
+    ctx.synchronize()
+
+    def plain():
+        sums, perms = [], []
+        for x, k in zip(xs, ks):
+            sums.append(ctx.call("reduce_add_f64", ctx.call("filter_gt_f64", x, 0.9)))
+            perms.append(ctx.call("argsort_i64", k))
+        ctx.synchronize()
+        return sums, perms
+
+    xb, kb = ctx.batch(xs), ctx.batch(ks)
+    outs = [ctx.new_array("i64", int(n)) for n in lens]
+    ob = ctx.batch(outs)
+    sums_arr = ctx.new_array("f64", count)
+    ctx.batch_argsort(kb, ob, key_digits=0b11)  # first call: scratch
+    ctx.synchronize()
+
+    def batched():
+        ctx.batch_filter_sum(xb, "gt", 0.9, sums_arr)
+        ctx.batch_argsort(kb, ob, key_digits=0b11)
+        return sums_arr.numpy()
+
+    ctx.graph_begin()
+    ctx.batch_filter_sum(xb, "gt", 0.9, sums_arr)
+    ctx.batch_argsort(kb, ob, key_digits=0b11)
+    graph = ctx.graph_end()
+
+    def replay():
+        graph.launch()
+        return sums_arr.numpy()
+
+    def timed(fn):
+        fn()  # warm-up
+        best = None
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            out = fn()
+            dt = time.perf_counter() - t0
+            best = dt if best is None else min(best, dt)
+        return best, out
+
+    t_plain, (psums, pperms) = timed(plain)
+    t_batch, bsums = timed(batched)
+    t_graph, gsums = timed(replay)
+    want = np.array(psums, dtype=np.float64).view(np.uint64)
+    exact = bool(np.array_equal(bsums.view(np.uint64), want) and np.array_equal(gsums.view(np.uint64), want))
+    sample = range(0, count, max(1, count // 64))
+    perms_ok = all(np.array_equal(outs[i].numpy(), pperms[i].numpy()) for i in sample)
+    rows = int(lens.sum())
+
+    def line(t):
+        return {"s": round(t, 4), "arrays_per_s": round(count / t, 1), "rows_per_s": round(rows / t, 1)}
+
+    return {"workload": "%d arrays, lengths floor(2^U) with U uniform in [%d, %d] (%d rows, %.2f GiB of f64 "
+                        "values and i64 keys); per array filter_gt_f64(0.9) -> reduce_add_f64 and "
+                        "argsort_i64 of keys below 2^16" % (count, lo, hi, rows, 16 * rows / 2 ** 30),
+            "plain": line(t_plain), "batched": line(t_batch), "graph": line(t_graph),
+            "speedup_batched": round(t_plain / t_batch, 2), "speedup_graph": round(t_plain / t_graph, 2),
+            "sums_bit_exact": exact, "argsort_sample_equal": bool(perms_ok)}
+
+
 # ---------------------------------------------------------------------------- e2e
 
 
@@ -431,6 +510,7 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=1 << 23)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--config3-n", type=int, default=1 << 27, help="0 skips the argsort/group-by section")
+    ap.add_argument("--config4-arrays", type=int, default=4096, help="0 skips the batched section")
     args = ap.parse_args()
     world, rank, local = dist_setup()
     n = args.n
@@ -528,9 +608,10 @@ def main():
 
     # Config 3 (argsort and group-by), reported beside the headline sweep, not in it.
     c3 = None
+    del inputs, hin, res
     if args.config3_n > 0:
-        del inputs, hin, res
         c3 = run_config3(ctx, args.config3_n, stream, steps=3, warmup=1)
+    c4 = run_config4(ctx, args.config4_arrays) if args.config4_arrays > 0 else None
 
     if rank == 0:
         line = {
@@ -550,6 +631,7 @@ def main():
             "gpu_launches": launches,
             "kernels": kernels,
             "config3": c3,
+            "config4": c4,
         }
         print(json.dumps(line), flush=True)
     ctx.close()
