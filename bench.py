@@ -375,6 +375,52 @@ def run_config4(ctx, count=4096, lo=10, hi=18, reps=2):
             "sums_bit_exact": exact, "argsort_sample_equal": bool(perms_ok)}
 
 
+# ---------------------------------------------------------------------------- config 5
+
+
+def run_config5(ctx, rates=(100, 400, 1600, 6400), count=300, slots=4, budget=150e9, p99_bound_ms=100.0):
+    """Config 5: Poisson arrivals of programs drawn from {dot, filter_gt + length, argsort,
+    group-by sum} with n = floor(10^U), U uniform in [3, 8], inputs generated on the device;
+    the plain GPU path (one request at a time, one synchronous call per statement) against the
+    server (continuous batching over `slots` streams, same-kind coalescing, admission by a
+    150 GB HBM budget). Latency is arrival to answer."""
+    import verkehrt_gb300 as vk
+    from verkehrt_gb300 import serve
+
+    ctx.set_cache_limit(16 << 30)
+    workers = [vk.Context(ctx.device) for _ in range(slots)]
+    for w in workers:
+        w.set_cache_limit(16 << 30)
+    # Warm-up of both paths on a short mix.
+    serve.serve([ctx], serve.poisson_requests(16, 1e4, seed=1, n_hi=1e5), budget, batching=False)
+    serve.serve(workers, serve.poisson_requests(16, 1e4, seed=1, n_hi=1e5), budget)
+    out = []
+    for rate in rates:
+        plain = serve.poisson_requests(count, rate, seed=rate)
+        wall_p = serve.serve([ctx], plain, budget, batching=False)
+        served = serve.poisson_requests(count, rate, seed=rate)
+        wall_s = serve.serve(workers, served, budget)
+        same = all(a.result == b.result for a, b in zip(plain, served) if a.kind in ("dot", "filter_len"))
+        out.append({"offered_req_per_s": rate, "plain": serve.summary(plain, wall_p),
+                    "served": serve.summary(served, wall_s), "scalar_results_equal": bool(same)})
+        del plain, served
+    for w in workers:
+        w.close()
+
+    def best(mode):
+        ok = [r[mode]["req_per_s"] for r in out if r[mode]["p99_ms"] <= p99_bound_ms]
+        return max(ok) if ok else None
+
+    at_bound = {"p99_bound_ms": p99_bound_ms, "plain_req_per_s": best("plain"), "served_req_per_s": best("served")}
+    if at_bound["plain_req_per_s"] and at_bound["served_req_per_s"]:
+        at_bound["ratio"] = round(at_bound["served_req_per_s"] / at_bound["plain_req_per_s"], 2)
+    return {"at_equal_p99": at_bound,
+            "workload": "%d requests per rate, kinds uniform over dot_f64 / filter_gt_f64+length / "
+                        "argsort_i64 / group-by sum, n = floor(10^U) with U uniform in [3, 8], seeded "
+                        "inputs generated on the device; server: %d streams, requests up to 2^20 rows "
+                        "coalesced per kind, 150 GB admission budget" % (count, slots), "rates": out}
+
+
 # ---------------------------------------------------------------------------- e2e
 
 
@@ -511,6 +557,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--config3-n", type=int, default=1 << 27, help="0 skips the argsort/group-by section")
     ap.add_argument("--config4-arrays", type=int, default=4096, help="0 skips the batched section")
+    ap.add_argument("--config5-requests", type=int, default=300, help="0 skips the served section")
     args = ap.parse_args()
     world, rank, local = dist_setup()
     n = args.n
@@ -612,6 +659,7 @@ def main():
     if args.config3_n > 0:
         c3 = run_config3(ctx, args.config3_n, stream, steps=3, warmup=1)
     c4 = run_config4(ctx, args.config4_arrays) if args.config4_arrays > 0 else None
+    c5 = run_config5(ctx, count=args.config5_requests) if args.config5_requests > 0 else None
 
     if rank == 0:
         line = {
@@ -632,6 +680,7 @@ def main():
             "kernels": kernels,
             "config3": c3,
             "config4": c4,
+            "config5": c5,
         }
         print(json.dumps(line), flush=True)
     ctx.close()

@@ -100,6 +100,10 @@ VKC_API void vkc_close(vkc_ctx *ctx);
 VKC_API const char *vkc_last_error(const vkc_ctx *ctx);
 /* Waits for all work of the context. */
 VKC_API vkc_status vkc_synchronize(vkc_ctx *ctx);
+/* Freed array blocks are kept for reuse by the context, up to `bytes` (48 GiB by default);
+ * lowering it releases the cache at once. Several contexts on one GPU (one per stream of a
+ * server) share the device, so each keeps a smaller cache. */
+VKC_API vkc_status vkc_set_cache_limit(vkc_ctx *ctx, size_t bytes);
 /* Runs the context's work on `stream` (a cudaStream_t) instead of its own stream. */
 VKC_API vkc_status vkc_set_stream(vkc_ctx *ctx, void *stream);
 VKC_API void *vkc_get_stream(const vkc_ctx *ctx);
@@ -219,6 +223,16 @@ VKC_API int vkc_batch_len(const vkc_batch *b);
  * 3 le, 4 gt, 5 ge (the reference's Cmp, src/kernels/scalar/fused.rs:45-54). `sums` is an f64
  * array of the batch's length. */
 VKC_API vkc_status vkc_batch_filter_sum_f64(vkc_ctx *ctx, vkc_batch *b, int cmp, double c, vkc_array *sums);
+
+/* For every f64 array i of the batch, counts[i] = length(filter_<cmp>_f64(array i, c)), i.e. the
+ * rows with x <cmp> c (count_<cmp>_f64, src/kernels/scalar/fused.rs:150-179). `counts` is an i64
+ * array of the batch's length. */
+VKC_API vkc_status vkc_batch_count_f64(vkc_ctx *ctx, vkc_batch *b, int cmp, double c, vkc_array *counts);
+
+/* sums[i] = dot_f64(xs[i], ys[i]) for every pair (equal lengths), bit for bit: fl(x*y) in the
+ * canonical order (src/kernels/scalar/fused.rs:73-106). One block per pair: meant for short
+ * arrays (a lane adds n/16 rows in sequence). `sums` is an f64 array of the batch's length. */
+VKC_API vkc_status vkc_batch_dot_f64(vkc_ctx *ctx, vkc_batch *xs, vkc_batch *ys, vkc_array *sums);
 
 /* For every i64 array i of `keys`, the stable ascending positions (argsort_i64) into the i64
  * array i of `outs` (same lengths). key_digits: bit d set when byte d of the keys' sign-flipped

@@ -81,3 +81,19 @@ def test_batch_graph_replay(ctx):
         assert np.array_equal(f64bits(sums.numpy()), want)
         for k, o in zip(keys, outs):
             assert np.array_equal(o.numpy(), oracle.argsort_i64(k))
+
+
+def test_batch_count_and_dot(ctx):
+    xs = [with_specials(n, 200 + i) for i, n in enumerate(LENGTHS)]
+    ys = [oracle.rand_f64(n, 300 + i) - 0.5 for i, n in enumerate(LENGTHS)]
+    xb, yb = ctx.batch([ctx.upload(x) for x in xs]), ctx.batch([ctx.upload(y) for y in ys])
+    counts = ctx.new_array("i64", len(xs))
+    ctx.batch_count(xb, "gt", 0.99, counts)
+    assert list(counts.numpy()) == [oracle.count_cmp_f64(x, "gt", 0.99) for x in xs]
+    ctx.batch_count(xb, "le", 0.0, counts)
+    assert list(counts.numpy()) == [oracle.count_cmp_f64(x, "le", 0.0) for x in xs]
+    sums = ctx.new_array("f64", len(xs))
+    ctx.batch_dot(xb, yb, sums)
+    got = sums.numpy()
+    want = np.array([oracle.dot_f64(x, y) for x, y in zip(xs, ys)])
+    assert ((f64bits(got) == f64bits(want)) | (np.isnan(got) & np.isnan(want))).all()

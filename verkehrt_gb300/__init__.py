@@ -55,6 +55,7 @@ _SIGNATURES = {
     "vkc_close": (None, [_P]),
     "vkc_last_error": (ctypes.c_char_p, [_P]),
     "vkc_synchronize": (ctypes.c_int, [_P]),
+    "vkc_set_cache_limit": (ctypes.c_int, [_P, ctypes.c_size_t]),
     "vkc_set_stream": (ctypes.c_int, [_P, _P]),
     "vkc_get_stream": (_P, [_P]),
     "vkc_launch_count": (ctypes.c_uint64, [_P]),
@@ -98,6 +99,8 @@ _SIGNATURES = {
     "vkc_batch_len": (ctypes.c_int, [_P]),
     "vkc_batch_filter_sum_f64": (ctypes.c_int, [_P, _P, ctypes.c_int, ctypes.c_double, _P]),
     "vkc_batch_argsort_i64": (ctypes.c_int, [_P, _P, _P, ctypes.c_uint]),
+    "vkc_batch_count_f64": (ctypes.c_int, [_P, _P, ctypes.c_int, ctypes.c_double, _P]),
+    "vkc_batch_dot_f64": (ctypes.c_int, [_P, _P, _P, _P]),
     "vkc_graph_begin": (ctypes.c_int, [_P]),
     "vkc_graph_end": (ctypes.c_int, [_P, ctypes.POINTER(_P)]),
     "vkc_graph_launch": (ctypes.c_int, [_P, _P]),
@@ -235,6 +238,7 @@ class Context:
         if st != 0:
             raise KernelError(STATUS[st], "cannot open CUDA device %d" % device)
         self.handle = h.value
+        self.device = device
         self._ids = {}
 
     def close(self):
@@ -347,6 +351,9 @@ class Context:
     def synchronize(self):
         self._check(_lib.vkc_synchronize(self.handle))
 
+    def set_cache_limit(self, nbytes):
+        self._check(_lib.vkc_set_cache_limit(self.handle, int(nbytes)))
+
     def launch_count(self):
         return int(_lib.vkc_launch_count(self.handle))
 
@@ -370,6 +377,14 @@ class Context:
     def batch_filter_sum(self, batch, cmp, c, sums):
         """sums[i] = reduce_add_f64(filter_<cmp>_f64(batch[i], c)) for every array (enqueued)."""
         self._check(_lib.vkc_batch_filter_sum_f64(self.handle, batch.handle, CMPS.index(cmp), c, sums.handle))
+
+    def batch_count(self, batch, cmp, c, counts):
+        """counts[i] = length(filter_<cmp>_f64(batch[i], c)) for every array (enqueued)."""
+        self._check(_lib.vkc_batch_count_f64(self.handle, batch.handle, CMPS.index(cmp), c, counts.handle))
+
+    def batch_dot(self, xs, ys, sums):
+        """sums[i] = dot_f64(xs[i], ys[i]) for every pair (enqueued)."""
+        self._check(_lib.vkc_batch_dot_f64(self.handle, xs.handle, ys.handle, sums.handle))
 
     def batch_argsort(self, keys, outs, key_digits=0):
         """outs[i] = argsort_i64(keys[i]) for every array (enqueued)."""

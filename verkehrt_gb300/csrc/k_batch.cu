@@ -142,6 +142,92 @@ __global__ void __launch_bounds__(BF_THREADS) batch_filter_sum_kernel(const BSeg
     }
 }
 
+// Counts of rows with x <cmp> c per array (length of filter), one block per array.
+template <bool POS>
+__global__ void __launch_bounds__(BF_THREADS) batch_count_kernel(const BSeg *__restrict__ segs, int nseg, CmpRange r,
+                                                                long long *counts, unsigned *ticket) {
+    __shared__ int s_seg;
+    const int t = threadIdx.x;
+    for (;;) {
+        if (t == 0) s_seg = static_cast<int>(atomicAdd(ticket, 1u));
+        __syncthreads();
+        const int sg = s_seg;
+        if (sg >= nseg) break;
+        const BSeg seg = segs[sg];
+        const auto *x = static_cast<const unsigned long long *>(seg.ptr);
+        unsigned long long kc = 0;
+        for (int64_t i = t; i < seg.n; i += BF_THREADS) kc += in_range_t<POS>(r, __ldg(x + i));
+        unsigned long long k;
+        block_exclusive_sum<unsigned long long>(kc, &k);
+        if (t == 0) counts[seg.index] = static_cast<long long>(k);
+        __syncthreads();
+    }
+    __syncthreads();
+    if (t == 0) {
+        const unsigned prev = atomicAdd(ticket + 1, 1u);
+        if (prev == gridDim.x - 1) {
+            ticket[0] = 0;
+            ticket[1] = 0;
+        }
+    }
+}
+
+// dot_f64 per pair of arrays (x from xs, y from ys, same index and length), one block per pair:
+// lane j (thread j < 16) adds fl(x*y) of rows j, j+16, ... below the last whole block of 16 in
+// order, the lanes combine +8, +4, +2, +1, and the tail rows are added to lane 0 in order
+// (src/kernels/scalar/fused.rs:73-106 with reduce.rs:45-91). The other threads stage the rows
+// into shared memory ahead of the lanes. Meant for short arrays: a lane's chain is n/16 adds.
+constexpr int BD_CHUNK = 4096;
+
+__global__ void __launch_bounds__(BF_THREADS) batch_dot_kernel(const BSeg *__restrict__ xs, const BSeg *__restrict__ ys,
+                                                              int nseg, unsigned long long *sums, unsigned *ticket) {
+    __shared__ double s_p[BD_CHUNK];  // the chunk's products fl(x*y)
+    __shared__ int s_seg;
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    for (;;) {
+        if (t == 0) s_seg = static_cast<int>(atomicAdd(ticket, 1u));
+        __syncthreads();
+        const int sg = s_seg;
+        if (sg >= nseg) break;
+        const BSeg sx = xs[sg];
+        const BSeg sy = ys[sg];
+        const auto *x = static_cast<const double *>(sx.ptr);
+        const auto *y = static_cast<const double *>(sy.ptr);
+        const int64_t n = sx.n, b = n - n % 16;
+        double acc = 0.0;
+        for (int64_t r0 = 0; r0 < n; r0 += BD_CHUNK) {
+            const int rows = static_cast<int>(n - r0 < BD_CHUNK ? n - r0 : BD_CHUNK);
+            for (int i = t; i < rows; i += BF_THREADS) s_p[i] = __dmul_rn(__ldg(x + r0 + i), __ldg(y + r0 + i));
+            __syncthreads();
+            if (t < 16) {
+                // r0 is a multiple of 16, so row r0 + i belongs to lane i mod 16.
+                for (int i = t; i < rows && r0 + i < b; i += 16) acc = __dadd_rn(acc, s_p[i]);
+            }
+            __syncthreads();
+        }
+        if (w == 0) {
+#pragma unroll
+            for (int step = 8; step > 0; step >>= 1) {
+                const double other = __shfl_down_sync(FULL, acc, step);
+                if (lane < step) acc = __dadd_rn(acc, other);
+            }
+            if (lane == 0) {
+                for (int64_t i = b; i < n; ++i) acc = __dadd_rn(acc, __dmul_rn(__ldg(x + i), __ldg(y + i)));
+                sums[sx.index] = static_cast<unsigned long long>(__double_as_longlong(acc));
+            }
+        }
+        __syncthreads();
+    }
+    __syncthreads();
+    if (t == 0) {
+        const unsigned prev = atomicAdd(ticket + 1, 1u);
+        if (prev == gridDim.x - 1) {
+            ticket[0] = 0;
+            ticket[1] = 0;
+        }
+    }
+}
+
 // ------------------------------------------------------------------ argsort
 
 // Images and positions of every array, in index order (array i at rows bases[i]..).
@@ -279,6 +365,44 @@ extern "C" VKC_API vkc_status vkc_batch_filter_sum_f64(vkc_ctx *ctx, vkc_batch *
     if (pos_range(r)) batch_filter_sum_kernel<true><<<grid, BF_THREADS, 0, ctx->stream>>>(tab, n, r, out, ticket);
     else batch_filter_sum_kernel<false><<<grid, BF_THREADS, 0, ctx->stream>>>(tab, n, r, out, ticket);
     return launched(ctx, "batch_filter_sum");
+}
+
+extern "C" VKC_API vkc_status vkc_batch_count_f64(vkc_ctx *ctx, vkc_batch *b, int cmp, double c, vkc_array *counts) {
+    if (!ctx || !b || !counts) return VKC_USAGE;
+    if (b->type != VKC_F64) return fail(ctx, VKC_RUNTIME, "batch count: expected f64[] arrays");
+    if (cmp < 0 || cmp > 5) return fail(ctx, VKC_USAGE, "batch count: comparison 0..5 (eq ne lt le gt ge)");
+    const int n = static_cast<int>(b->host.size());
+    if (counts->type != VKC_I64 || counts->len != n)
+        return fail(ctx, VKC_RUNTIME, "batch count: the result array must be i64[" + std::to_string(n) + "]");
+    if (n == 0) return VKC_OK;
+    const CmpRange r = cmp_range(cmp, c);
+    const int grid = std::min(n, ctx->sms * 8);
+    auto *out = static_cast<long long *>(counts->data());
+    const auto *tab = static_cast<const BSeg *>(b->table.ptr);
+    if (pos_range(r)) batch_count_kernel<true><<<grid, BF_THREADS, 0, ctx->stream>>>(tab, n, r, out, ctx->counters + 4);
+    else batch_count_kernel<false><<<grid, BF_THREADS, 0, ctx->stream>>>(tab, n, r, out, ctx->counters + 4);
+    return launched(ctx, "batch_count");
+}
+
+extern "C" VKC_API vkc_status vkc_batch_dot_f64(vkc_ctx *ctx, vkc_batch *xs, vkc_batch *ys, vkc_array *sums) {
+    if (!ctx || !xs || !ys || !sums) return VKC_USAGE;
+    if (xs->type != VKC_F64 || ys->type != VKC_F64) return fail(ctx, VKC_RUNTIME, "batch dot: expected f64[] arrays");
+    const int n = static_cast<int>(xs->host.size());
+    if (static_cast<int>(ys->host.size()) != n) return fail(ctx, VKC_RUNTIME, "batch dot: batches of different sizes");
+    // Both tables are largest first with ties kept in index order, so equal lengths pair up.
+    for (int i = 0; i < n; ++i)
+        if (xs->arrays[i]->len != ys->arrays[i]->len)
+            return fail(ctx, VKC_RUNTIME, "length mismatch: " + std::to_string(xs->arrays[i]->len) + " vs " +
+                                              std::to_string(ys->arrays[i]->len));
+    if (sums->type != VKC_F64 || sums->len != n)
+        return fail(ctx, VKC_RUNTIME, "batch dot: the result array must be f64[" + std::to_string(n) + "]");
+    if (n == 0) return VKC_OK;
+    const int grid = std::min(n, ctx->sms * 8);
+    batch_dot_kernel<<<grid, BF_THREADS, 0, ctx->stream>>>(static_cast<const BSeg *>(xs->table.ptr),
+                                                           static_cast<const BSeg *>(ys->table.ptr), n,
+                                                           static_cast<unsigned long long *>(sums->data()),
+                                                           ctx->counters + 4);
+    return launched(ctx, "batch_dot");
 }
 
 extern "C" VKC_API vkc_status vkc_batch_argsort_i64(vkc_ctx *ctx, vkc_batch *keys, const vkc_batch *outs,

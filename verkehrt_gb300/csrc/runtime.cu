@@ -11,9 +11,6 @@
 
 namespace vkc {
 
-// Cached free blocks at most this many bytes; frees beyond it go back to the pool.
-constexpr size_t kCacheLimit = size_t(48) << 30;
-
 StreamBox::~StreamBox() {
     if (stream) {
         int prev = 0;
@@ -50,7 +47,7 @@ void StreamBox::release_all() {
 void StreamBox::give(void *p, size_t cls) {
     {
         std::lock_guard<std::mutex> lock(mu);
-        if (cached + cls <= kCacheLimit) {
+        if (cached + cls <= limit) {
             free_blocks.emplace(cls, p);
             cached += cls;
             return;
@@ -470,6 +467,18 @@ void vkc_close(vkc_ctx *ctx) {
 }
 
 const char *vkc_last_error(const vkc_ctx *ctx) { return ctx ? ctx->err.c_str() : ""; }
+
+vkc_status vkc_set_cache_limit(vkc_ctx *ctx, size_t bytes) {
+    if (!ctx || !ctx->box) return VKC_USAGE;
+    bool drop;
+    {
+        std::lock_guard<std::mutex> lock(ctx->box->mu);
+        ctx->box->limit = bytes;
+        drop = ctx->box->cached > bytes;
+    }
+    if (drop) ctx->box->release_all();
+    return VKC_OK;
+}
 
 vkc_status vkc_synchronize(vkc_ctx *ctx) {
     VKC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));

@@ -47,6 +47,7 @@ struct StreamBox {
     int device = 0;
     std::multimap<size_t, void *> free_blocks;  // size class -> block
     size_t cached = 0;
+    size_t limit = size_t(48) << 30;  // cached bytes at most (vkc_set_cache_limit)
     std::mutex mu;
     ~StreamBox();
     // A block of at least `bytes` (its class size in *cls), or nullptr.
