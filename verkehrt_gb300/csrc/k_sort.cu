@@ -9,7 +9,7 @@
 //  * each remaining digit is one reduce-then-scan pass over 4096-row tiles: `up` counts each
 //    tile's digits into a digit-major table, one exclusive scan of that table gives every
 //    (digit, tile) its first output row, and `down` ranks the tile's rows stably by digit
-//    (warp match + ballot in row order) and scatters them. The first pass reads the keys, the
+//    (a ballot per digit bit, in row order) and scatters them. The first pass reads the keys, the
 //    last writes the positions as i64. (A single-pass lookback per digit was slower here: the
 //    lookback of 256 digits per tile advances a few tiles per L2 round trip.)
 // Stability makes the output the reference's, which the comparison sort of short inputs
@@ -26,6 +26,9 @@ constexpr int RS_WARPS = RS_THREADS / 32;
 constexpr int RS_ITEMS = 16;
 constexpr int RS_TILE = RS_THREADS * RS_ITEMS;
 constexpr int RADIX = 256;
+#ifndef RS_DOWN_MIN_BLOCKS
+#define RS_DOWN_MIN_BLOCKS 3  // resident blocks per SM that the down kernel's registers allow
+#endif
 
 __device__ __forceinline__ unsigned long long image_of(long long k) {
     return static_cast<unsigned long long>(k) ^ 0x8000000000000000ull;
@@ -50,8 +53,8 @@ __global__ void __launch_bounds__(256) rs_hist_kernel(const long long *__restric
     }
 }
 
-// Up: the digit counts of every tile, digit-major: counts[d * tiles + tile]. Rows are
-// warp-striped (row = base + j*32 + lane) as in `down`.
+// Up: the digit counts of every tile, digit-major: counts[d * tiles + tile]. Shared-memory
+// atomics into one histogram per warp (the order of the increments does not matter here).
 template <bool FIRST>
 __global__ void __launch_bounds__(RS_THREADS) rs_up_kernel(const long long *__restrict__ keys_in,
                                                            const unsigned long long *__restrict__ img_in, int64_t n,
@@ -62,21 +65,23 @@ __global__ void __launch_bounds__(RS_THREADS) rs_up_kernel(const long long *__re
     for (int i = threadIdx.x; i < RS_WARPS * RADIX; i += RS_THREADS) (&s_cnt[0][0])[i] = 0;
     __syncthreads();
     const int64_t base = static_cast<int64_t>(tile) * RS_TILE + static_cast<int64_t>(w) * (32 * RS_ITEMS);
-    unsigned long long img[RS_ITEMS];
+    if (base + 32 * RS_ITEMS <= n) {
+        unsigned long long img[RS_ITEMS];
 #pragma unroll
-    for (int j = 0; j < RS_ITEMS; ++j) {
-        const int64_t r = base + j * 32 + lane;
-        img[j] = r < n ? (FIRST ? image_of(__ldcs(keys_in + r)) : __ldcs(img_in + r)) : 0ull;
-    }
+        for (int j = 0; j < RS_ITEMS; ++j) {
+            const int64_t r = base + j * 32 + lane;
+            img[j] = FIRST ? image_of(__ldcs(keys_in + r)) : __ldcs(img_in + r);
+        }
 #pragma unroll
-    for (int j = 0; j < RS_ITEMS; ++j) {
-        const bool in = base + j * 32 + lane < n;
-        const unsigned d = static_cast<unsigned>(img[j] >> shift) & 0xffu;
-        const unsigned active = __ballot_sync(FULL, in);
-        const unsigned peers = __match_any_sync(FULL, in ? d : 0x100u + lane) & active;
-        // One leader per digit adds its peers; leaders of one warp hold distinct digits.
-        if (in && (peers & ((1u << lane) - 1)) == 0) s_cnt[w][d] += __popc(peers);
-        __syncwarp();
+        for (int j = 0; j < RS_ITEMS; ++j) atomicAdd(&s_cnt[w][static_cast<unsigned>(img[j] >> shift) & 0xffu], 1u);
+    } else {
+        for (int j = 0; j < RS_ITEMS; ++j) {
+            const int64_t r = base + j * 32 + lane;
+            if (r < n) {
+                const unsigned long long im = FIRST ? image_of(__ldcs(keys_in + r)) : __ldcs(img_in + r);
+                atomicAdd(&s_cnt[w][static_cast<unsigned>(im >> shift) & 0xffu], 1u);
+            }
+        }
     }
     __syncthreads();
     const int d = threadIdx.x;  // RS_THREADS == RADIX
@@ -84,6 +89,19 @@ __global__ void __launch_bounds__(RS_THREADS) rs_up_kernel(const long long *__re
 #pragma unroll
     for (int ww = 0; ww < RS_WARPS; ++ww) total += s_cnt[ww][d];
     counts[static_cast<int64_t>(d) * tiles + tile] = total;
+}
+
+// The lanes of the warp whose 8-bit digit equals this lane's, among the lanes of `valid`: one
+// ballot per digit bit, each lane keeping the lanes that agree with it on that bit.
+__device__ __forceinline__ unsigned digit_peers(unsigned d, unsigned valid) {
+    unsigned m = valid;
+#pragma unroll
+    for (int b = 0; b < 8; ++b) {
+        const bool set = (d >> b) & 1u;
+        const unsigned v = __ballot_sync(FULL, set);
+        m &= set ? v : ~v;
+    }
+    return m;
 }
 
 // Exclusive scan of `m` u32 counts (n < 2^32, so sums fit) in SCAN_CHUNK-element blocks:
@@ -148,7 +166,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) rs_scan_apply(const unsigned *__
 // offsets[d * tiles + tile]. FIRST reads the i64 keys (positions are the row numbers); LAST
 // writes only the positions, as i64.
 template <bool FIRST, bool LAST>
-__global__ void __launch_bounds__(RS_THREADS) rs_down_kernel(
+__global__ void __launch_bounds__(RS_THREADS, RS_DOWN_MIN_BLOCKS) rs_down_kernel(
     const long long *__restrict__ keys_in, const unsigned long long *__restrict__ img_in,
     const unsigned *__restrict__ pos_in, unsigned long long *__restrict__ img_out,
     unsigned *__restrict__ pos_out, long long *__restrict__ out, int64_t n, int shift, int tiles,
@@ -167,8 +185,7 @@ __global__ void __launch_bounds__(RS_THREADS) rs_down_kernel(
     const int64_t base = static_cast<int64_t>(tile) * RS_TILE + static_cast<int64_t>(w) * (32 * RS_ITEMS);
     unsigned long long img[RS_ITEMS];
     unsigned pos[RS_ITEMS];
-    unsigned short rank[RS_ITEMS];
-    unsigned char dig[RS_ITEMS];
+    unsigned rank2[RS_ITEMS / 2];  // two 16-bit ranks per word
     const unsigned lt = (1u << lane) - 1;
 #pragma unroll
     for (int j = 0; j < RS_ITEMS; ++j) {
@@ -176,7 +193,7 @@ __global__ void __launch_bounds__(RS_THREADS) rs_down_kernel(
         const bool in = r < n;
         if (FIRST) {
             img[j] = in ? image_of(__ldcs(keys_in + r)) : ~0ull;
-            pos[j] = static_cast<unsigned>(r);
+            pos[j] = 0u;  // the row number, recomputed when stored
         } else {
             img[j] = in ? __ldcs(img_in + r) : ~0ull;
             pos[j] = in ? __ldcs(pos_in + r) : 0u;
@@ -186,14 +203,13 @@ __global__ void __launch_bounds__(RS_THREADS) rs_down_kernel(
     for (int j = 0; j < RS_ITEMS; ++j) {
         const bool in = base + j * 32 + lane < n;
         const unsigned d = static_cast<unsigned>(img[j] >> shift) & 0xffu;
-        dig[j] = static_cast<unsigned char>(d);
         // Rank among this warp's earlier rows with the same digit.
-        const unsigned active = __ballot_sync(FULL, in);
-        const unsigned peers = __match_any_sync(FULL, in ? d : 0x100u + lane) & active;
+        const unsigned peers = digit_peers(d, __ballot_sync(FULL, in));
         const unsigned short before = s_wcnt[w][d];
         __syncwarp();
         if (in) {
-            rank[j] = static_cast<unsigned short>(before + __popc(peers & lt));
+            const unsigned rk = before + __popc(peers & lt);
+            rank2[j / 2] = (j & 1) ? (rank2[j / 2] | (rk << 16)) : rk;
             if ((peers & lt) == 0) s_wcnt[w][d] = static_cast<unsigned short>(before + __popc(peers));
         }
         __syncwarp();
@@ -221,10 +237,10 @@ __global__ void __launch_bounds__(RS_THREADS) rs_down_kernel(
 #pragma unroll
     for (int j = 0; j < RS_ITEMS; ++j) {
         if (base + j * 32 + lane < n) {
-            const unsigned d = dig[j];
-            const unsigned l = s_dstart[d] + s_wcnt[w][d] + rank[j];
+            const unsigned d = static_cast<unsigned>(img[j] >> shift) & 0xffu;
+            const unsigned l = s_dstart[d] + s_wcnt[w][d] + ((rank2[j / 2] >> (16 * (j & 1))) & 0xffffu);
             s_img[l] = img[j];
-            s_pos[l] = pos[j];
+            s_pos[l] = FIRST ? static_cast<unsigned>(base + j * 32 + lane) : pos[j];
         }
     }
     __syncthreads();
