@@ -110,3 +110,30 @@ def test_group_id_large(ctx):
         xs = (oracle.rand_i64(n, 5).view(np.uint64) % np.uint64(mod)).astype(np.int64)
         got = ctx.call("group_id_i64", ctx.upload(xs)).numpy()
         assert np.array_equal(got, oracle.group_id_i64(xs)), mod
+
+
+def test_group_id_free_slot_pattern_and_table_switch(ctx):
+    # The key whose bytes are all 0x80 marks a free slot of the GPU table; rows holding it take
+    # their own slot. Pairs with one such half probe like any other pair.
+    e = np.uint64(0x8080808080808080).view(np.int64)
+    xs = np.array([5, e, 5, e, -1, e, 0], dtype=np.int64)
+    assert np.array_equal(ctx.call("group_id_i64", ctx.upload(xs)).numpy(), oracle.group_id_i64(xs))
+    a = np.array([e, e, 1, e, e, 1, e], dtype=np.int64)
+    b = np.array([e, 1, e, e, 1, e, 2], dtype=np.int64)
+    got = ctx.call("group_id2_i64_i64", ctx.upload(a), ctx.upload(b)).numpy()
+    assert np.array_equal(got, oracle.group_id2_i64_i64(a, b))
+    # Above 2^20 rows: few keys stay in the small table; about 2^20 distinct keys (the small
+    # table's limit) and many distinct pairs move to the full table part-way.
+    n = (1 << 21) + 5
+    r = oracle.rand_i64(n, 21).view(np.uint64)
+    for mod in (1000, (1 << 20) - 3, (1 << 20) + 3):
+        xs = (r % np.uint64(mod)).astype(np.int64)
+        xs[::4097] = e
+        got = ctx.call("group_id_i64", ctx.upload(xs)).numpy()
+        assert np.array_equal(got, oracle.group_id_i64(xs)), mod
+    for mod in (50, 1 << 12):
+        a = (r % np.uint64(mod)).astype(np.int64)
+        b = ((r >> np.uint64(20)) % np.uint64(mod)).astype(np.int64)
+        a[::999] = e
+        got = ctx.call("group_id2_i64_i64", ctx.upload(a), ctx.upload(b)).numpy()
+        assert np.array_equal(got, oracle.group_id2_i64_i64(a, b)), mod
