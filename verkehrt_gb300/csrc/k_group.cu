@@ -2,7 +2,7 @@
 // (src/kernels/scalar/group.rs:207-301).
 //
 // The ids depend only on the order in which distinct keys first appear (group.rs:1-5), so any
-// correct table gives the reference's output. Three kernels:
+// correct table gives the reference's output. Two kernels:
 //  1. insert: open addressing with linear probing. A free slot holds the key EMPTY (the byte
 //     0x80 repeated) and is claimed by a CAS on the key itself (a 128-bit CAS for key pairs),
 //     so a probe that reads its key needs no further synchronisation. Slot 0 is never probed:
@@ -11,8 +11,7 @@
 //     row is already smaller), and each row records its slot. A thread probes four rows at once.
 //  2. number: a row is a first occurrence when its slot's smallest row is itself; a
 //     decoupled-lookback compaction over rows gives each first occurrence its rank, which is
-//     the group's id, stored in the slot.
-//  3. out: every row reads its slot's id.
+//     the group's id, stored in the slot; the same kernel writes every row's id.
 // Table size: the reference's maximum is nextpow2(2n) slots (group.rs:226-229). When that is
 // above 2^21 slots, the insert first runs on a 2^21-slot table, which stays in L2; it gives up
 // (an overflow flag) once 2^20 distinct keys or a probe of 64 slots is reached, and only then
@@ -30,10 +29,17 @@ constexpr unsigned long long GI_EMPTY = 0x8080808080808080ull;
 constexpr uint64_t GI_SMALL_SLOTS = uint64_t(1) << 21;
 constexpr unsigned GI_SMALL_PROBES = 64;
 
+// A slot is one 16-byte record (key, smallest row, id), or 32 bytes for key pairs (key a,
+// key b, smallest row, id, unused), so the probe, the claim and the row update of a key touch
+// one line of the table.
 struct GroupTable {
-    unsigned long long *keys;  // one word per slot (two for key pairs); GI_EMPTY when free
-    uint2 *meta;               // per slot: x = smallest row of the key, y = group id
-    unsigned long long mask;   // slots - 1
+    unsigned long long *words;  // W words per slot: the key (two for pairs, GI_EMPTY when free),
+                                // then uint2 {x = smallest row of the key, y = group id}
+    unsigned long long mask;    // slots - 1
+    int w;                      // words per slot: 2, or 4 for key pairs
+    __device__ __forceinline__ uint2 *meta(unsigned long long s) const {
+        return reinterpret_cast<uint2 *>(words + w * s + (w == 4 ? 2 : 1));
+    }
 };
 
 // group.rs:40-47 (mix) with a fixed odd multiplier; the ids do not depend on it.
@@ -79,12 +85,15 @@ __device__ __forceinline__ unsigned ld_relaxed32(const unsigned *p) {
 
 // SMALL: the attempt on the small table, which gives up through flags[1] (flags[0] counts the
 // distinct keys inserted). Otherwise the table has room for every key and a probe longer than
-// the table only records a timeout.
+// the table only records a timeout. Probes read the slot first and claim a free one by CAS,
+// except for single keys on the full table (many distinct keys): there one 128-bit CAS both
+// reads the slot and claims it with the row as its smallest row.
 template <bool PAIR, bool SMALL>
 __global__ void __launch_bounds__(GI_THREADS) gi_insert_kernel(const long long *__restrict__ a,
                                                                const long long *__restrict__ b, int64_t n,
                                                                GroupTable t, unsigned *__restrict__ slot_of,
                                                                unsigned *flags, DevStatus *st) {
+    constexpr bool CAS_FIRST = !SMALL && !PAIR;
     const int lane = threadIdx.x & 31;
     const int64_t step = static_cast<int64_t>(gridDim.x) * GI_THREADS * GI_ROWS;
     // The full table always has a free slot, so a probe ends within `mask` steps.
@@ -96,6 +105,7 @@ __global__ void __launch_bounds__(GI_THREADS) gi_insert_kernel(const long long *
             if (__shfl_sync(FULL, ov, 0)) return;  // the whole warp leaves together
         }
         unsigned long long ka[GI_ROWS], kb[GI_ROWS], s[GI_ROWS];
+        unsigned cur[GI_ROWS];  // the slot's smallest row as last seen (CAS_FIRST)
         unsigned pend = 0, in = 0, fresh = 0;
         bool gave_up = false;
 #pragma unroll
@@ -103,6 +113,7 @@ __global__ void __launch_bounds__(GI_THREADS) gi_insert_kernel(const long long *
             const int64_t r = base + j * GI_THREADS + threadIdx.x;
             ka[j] = kb[j] = GI_EMPTY;
             s[j] = 0;
+            cur[j] = 0xffffffffu;
             if (r < n) {
                 in |= 1u << j;
                 ka[j] = static_cast<unsigned long long>(__ldcs(a + r));
@@ -120,19 +131,34 @@ __global__ void __launch_bounds__(GI_THREADS) gi_insert_kernel(const long long *
             for (int j = 0; j < GI_ROWS; ++j) {
                 va[j] = vb[j] = 0;
                 if (pend & (1u << j)) {
-                    if (PAIR) ld_relaxed_pair(t.keys + 2 * s[j], va[j], vb[j]);
-                    else va[j] = ld_relaxed64(t.keys + s[j]);
+                    if (CAS_FIRST) {
+                        const unsigned long long row = static_cast<unsigned long long>(base + j * GI_THREADS + threadIdx.x);
+                        cas_pair(t.words + 2 * s[j], GI_EMPTY, ~0ull, ka[j], 0xffffffff00000000ull | row, va[j], vb[j]);
+                    } else if (PAIR) {
+                        ld_relaxed_pair(t.words + 4 * s[j], va[j], vb[j]);
+                    } else {
+                        va[j] = ld_relaxed64(t.words + 2 * s[j]);
+                    }
                 }
             }
 #pragma unroll
             for (int j = 0; j < GI_ROWS; ++j) {
                 if (!(pend & (1u << j))) continue;
                 bool done = false;
-                if (!PAIR) {
+                if (CAS_FIRST) {
+                    // A free slot always holds (EMPTY, all ones), so an EMPTY key means the CAS won.
+                    if (va[j] == GI_EMPTY) {
+                        done = true;
+                        cur[j] = 0u;  // the claim stored this row
+                    } else if (va[j] == ka[j]) {
+                        done = true;
+                        cur[j] = static_cast<unsigned>(vb[j]);
+                    }
+                } else if (!PAIR) {
                     if (va[j] == ka[j]) {
                         done = true;
                     } else if (va[j] == GI_EMPTY) {
-                        const unsigned long long old = atomicCAS(t.keys + s[j], GI_EMPTY, ka[j]);
+                        const unsigned long long old = atomicCAS(t.words + 2 * s[j], GI_EMPTY, ka[j]);
                         if (old == GI_EMPTY) ++fresh;
                         done = old == GI_EMPTY || old == ka[j];
                     }
@@ -141,7 +167,7 @@ __global__ void __launch_bounds__(GI_THREADS) gi_insert_kernel(const long long *
                     done = va[j] == ka[j] && vb[j] == kb[j];
                 } else {
                     unsigned long long oa, ob;
-                    cas_pair(t.keys + 2 * s[j], GI_EMPTY, GI_EMPTY, ka[j], kb[j], oa, ob);
+                    cas_pair(t.words + 4 * s[j], GI_EMPTY, GI_EMPTY, ka[j], kb[j], oa, ob);
                     if (oa == GI_EMPTY && ob == GI_EMPTY) ++fresh;
                     done = (oa == GI_EMPTY && ob == GI_EMPTY) || (oa == ka[j] && ob == kb[j]);
                 }
@@ -166,22 +192,31 @@ __global__ void __launch_bounds__(GI_THREADS) gi_insert_kernel(const long long *
         for (int j = 0; j < GI_ROWS; ++j) {
             if (!(in & (1u << j))) continue;
             const unsigned row = static_cast<unsigned>(base + j * GI_THREADS + threadIdx.x);
-            unsigned *m = &t.meta[s[j]].x;
-            if (ld_relaxed32(m) > row) atomicMin(m, row);
+            unsigned *m = &t.meta(s[j])->x;
+            if ((CAS_FIRST && s[j] != 0 ? cur[j] : ld_relaxed32(m)) > row) atomicMin(m, row);
             slot_of[row] = static_cast<unsigned>(s[j]);
         }
     }
 }
 
 // Numbers the first occurrences in row order (a compaction of the rows whose slot's smallest
-// row is themselves) and stores each group's id in its slot.
-__global__ void __launch_bounds__(GI_THREADS) gi_number_kernel(const unsigned *__restrict__ slot_of, int64_t n,
-                                                               GroupTable t, int tiles, unsigned long long *words,
-                                                               unsigned epoch, unsigned *counters,
-                                                               DevStatus *st) {
+// row is themselves), stores each group's id in its slot, and writes every row's id. A row
+// whose key first occurs in this tile takes its id from the tile's bitmap of first
+// occurrences; any other key first occurs in an earlier tile, which stores the id right after
+// its own lookback, so the row reads it from the slot (waiting, bounded, until it is there).
+constexpr int GI_OUT_STRIDE = GI_ITEMS + 1;  // padded rows of the staged ids (bank spread)
+
+__global__ void __launch_bounds__(GI_THREADS, 4) gi_number_kernel(const unsigned *__restrict__ slot_of, int64_t n,
+                                                                  GroupTable t, int tiles, unsigned long long *words,
+                                                                  unsigned epoch, unsigned *counters,
+                                                                  long long *__restrict__ out, DevStatus *st) {
     __shared__ unsigned long long s_prefix;
+    __shared__ unsigned s_keep[GI_TILE / 32];  // bit i of word w: row 32w + i of the tile is a first occurrence
+    __shared__ unsigned s_wpre[GI_TILE / 32];  // first occurrences of the tile before word w
+    __shared__ long long s_out[GI_THREADS * GI_OUT_STRIDE];
     const int tile = take_ticket(counters);
-    const int64_t row0 = static_cast<int64_t>(tile) * GI_TILE + threadIdx.x * GI_ITEMS;
+    const int64_t t0 = static_cast<int64_t>(tile) * GI_TILE;
+    const int64_t row0 = t0 + threadIdx.x * GI_ITEMS;
     unsigned sl[GI_ITEMS];
     if (row0 + GI_ITEMS <= n) {
         const uint4 *v = reinterpret_cast<const uint4 *>(slot_of + row0);
@@ -197,75 +232,101 @@ __global__ void __launch_bounds__(GI_THREADS) gi_number_kernel(const unsigned *_
 #pragma unroll
         for (int j = 0; j < GI_ITEMS; ++j) sl[j] = row0 + j < n ? slot_of[row0 + j] : 0u;
     }
+    int rel[GI_ITEMS];  // the key's first row relative to the tile (negative: an earlier tile)
     unsigned keep = 0;
 #pragma unroll
     for (int j = 0; j < GI_ITEMS; ++j) {
         const int64_t r = row0 + j;
-        if (r < n && t.meta[sl[j]].x == static_cast<unsigned>(r)) keep |= 1u << j;
+        rel[j] = -1;
+        if (r < n) {
+            const unsigned m = t.meta(sl[j])->x;
+            rel[j] = static_cast<int>(static_cast<int64_t>(m) - t0);
+            if (m == static_cast<unsigned>(r)) keep |= 1u << j;
+        }
     }
+    const unsigned odd = __shfl_down_sync(FULL, keep, 1);
+    if (!(threadIdx.x & 1)) s_keep[threadIdx.x >> 1] = keep | (odd << 16);
     unsigned long long c = __popc(keep), tile_count;
-    unsigned long long off = block_exclusive_sum<unsigned long long>(c, &tile_count);
+    const unsigned long long off = block_exclusive_sum<unsigned long long>(c, &tile_count);
+    if (!(threadIdx.x & 1)) s_wpre[threadIdx.x >> 1] = static_cast<unsigned>(off);
     if (threadIdx.x < 32) {
         unsigned long long pre = lookback_publish<4, CountRec>(words, tile, tile_count, 0ull, epoch, st);
         if (threadIdx.x == 0) s_prefix = pre;
     }
     __syncthreads();
-    unsigned r = static_cast<unsigned>(s_prefix + off);
+    const unsigned prefix = static_cast<unsigned>(s_prefix);
+    unsigned id = prefix + static_cast<unsigned>(off);
 #pragma unroll
     for (int j = 0; j < GI_ITEMS; ++j)
-        if (keep & (1u << j)) t.meta[sl[j]].y = r++;
+        if (keep & (1u << j)) t.meta(sl[j])->y = id++;
+#pragma unroll
+    for (int j = 0; j < GI_ITEMS; ++j) {
+        if (row0 + j >= n) continue;
+        unsigned g;
+        if (rel[j] >= 0) {
+            const int w = rel[j] >> 5, bit = rel[j] & 31;
+            g = prefix + s_wpre[w] + __popc(s_keep[w] & ((1u << bit) - 1u));
+        } else {
+            const unsigned *p = &t.meta(sl[j])->y;
+            unsigned it = 0;
+            while ((g = ld_relaxed32(p)) == 0xffffffffu) {
+                if (++it > SPIN_LIMIT) {
+                    set_timeout(st);
+                    break;
+                }
+                backoff(it);
+            }
+        }
+        s_out[threadIdx.x * GI_OUT_STRIDE + j] = static_cast<long long>(g);
+    }
+    __syncthreads();
+    const int rows = static_cast<int>(n - t0 < GI_TILE ? n - t0 : GI_TILE);
+    for (int i = threadIdx.x; i < rows; i += GI_THREADS)
+        __stcs(out + t0 + i, s_out[(i / GI_ITEMS) * GI_OUT_STRIDE + (i % GI_ITEMS)]);
     release_ticket(counters, tiles);
 }
 
-// Four rows per thread: one 16-byte load of their slots, four id loads, two 16-byte stores.
-__global__ void __launch_bounds__(256) gi_out_kernel(const unsigned *__restrict__ slot_of, int64_t n,
-                                                     const uint2 *__restrict__ meta, long long *__restrict__ out) {
-    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x * 4;
-    for (int64_t i = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) * 4; i < n; i += stride) {
-        if (i + 4 <= n) {
-            const uint4 sl = __ldcs(reinterpret_cast<const uint4 *>(slot_of + i));
-            const longlong2 lo = make_longlong2(meta[sl.x].y, meta[sl.y].y);
-            const longlong2 hi = make_longlong2(meta[sl.z].y, meta[sl.w].y);
-            __stcs(reinterpret_cast<longlong2 *>(out + i), lo);
-            __stcs(reinterpret_cast<longlong2 *>(out + i) + 1, hi);
-        } else {
-            for (int64_t r = i; r < n; ++r) out[r] = static_cast<long long>(meta[slot_of[r]].y);
-        }
-    }
+// Every slot free: keys GI_EMPTY, smallest row and id all ones.
+__global__ void __launch_bounds__(256) gi_clear_kernel(ulonglong2 *__restrict__ p, int64_t pairs, int w) {
+    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    const ulonglong2 key = make_ulonglong2(GI_EMPTY, w == 4 ? GI_EMPTY : ~0ull);
+    const ulonglong2 rest = make_ulonglong2(~0ull, ~0ull);
+    for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < pairs; i += stride)
+        p[i] = (w == 2 || (i & 1) == 0) ? key : rest;
 }
 
 struct GroupScratch {
-    vkc_array *keys = nullptr, *meta = nullptr;
+    vkc_array *words = nullptr;
     void release() {
-        if (keys) vkc_array_release(keys);
-        if (meta) vkc_array_release(meta);
-        keys = meta = nullptr;
+        if (words) vkc_array_release(words);
+        words = nullptr;
     }
 };
 
 // A table of `slots` slots (slot 0 included), every slot free.
 static vkc_status new_table(vkc_ctx *ctx, uint64_t slots, bool pair, GroupScratch *g, GroupTable *t) {
-    const int64_t words = static_cast<int64_t>(pair ? 2 * slots : slots);
-    if (new_array(ctx, VKC_U64, words, false, &g->keys) ||
-        new_array(ctx, VKC_U64, static_cast<int64_t>(slots), false, &g->meta)) {
-        g->release();
-        return VKC_ALLOC;
-    }
-    VKC_CUDA(ctx, cudaMemsetAsync(g->keys->data(), 0x80, static_cast<size_t>(words) * 8, ctx->stream));
-    VKC_CUDA(ctx, cudaMemsetAsync(g->meta->data(), 0xff, static_cast<size_t>(slots) * 8, ctx->stream));
-    *t = GroupTable{static_cast<unsigned long long *>(g->keys->data()), static_cast<uint2 *>(g->meta->data()),
-                    slots - 1};
-    return VKC_OK;
+    const int w = pair ? 4 : 2;
+    const int64_t words = static_cast<int64_t>(w * slots);
+    if (new_array(ctx, VKC_U64, words, false, &g->words)) return VKC_ALLOC;
+    gi_clear_kernel<<<stream_grid(ctx, words / 2, 256, 8, 2048), 256, 0, ctx->stream>>>(
+        static_cast<ulonglong2 *>(g->words->data()), words / 2, w);
+    *t = GroupTable{static_cast<unsigned long long *>(g->words->data()), slots - 1, w};
+    return launched(ctx, "gi_clear");
 }
 
+// One wave of resident blocks (the grid-stride loop gives every block the same share, so a
+// second, partial wave would run at a fraction of the occupancy).
 template <bool PAIR>
 static void launch_insert(vkc_ctx *ctx, bool small, const long long *a, const long long *b, int64_t n,
                           const GroupTable &t, unsigned *slot_of, unsigned *flags) {
-    const int grid = stream_grid(ctx, n, GI_THREADS, 8, GI_THREADS * GI_ROWS);
-    if (small)
-        gi_insert_kernel<PAIR, true><<<grid, GI_THREADS, 0, ctx->stream>>>(a, b, n, t, slot_of, flags, ctx->status);
-    else
-        gi_insert_kernel<PAIR, false><<<grid, GI_THREADS, 0, ctx->stream>>>(a, b, n, t, slot_of, flags, ctx->status);
+    static int resident[2] = {0, 0};
+    auto kern = small ? gi_insert_kernel<PAIR, true> : gi_insert_kernel<PAIR, false>;
+    int &per_sm = resident[small ? 1 : 0];
+    if (per_sm == 0 && (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, GI_THREADS, 0) != cudaSuccess ||
+                        per_sm < 1))
+        per_sm = 1;
+    const int grid = stream_grid(ctx, n, GI_THREADS, per_sm, GI_THREADS * GI_ROWS);
+    kern<<<grid, GI_THREADS, 0, ctx->stream>>>(a, b, n, t, slot_of, flags, ctx->status);
 }
 
 static vkc_status run_group(vkc_ctx *ctx, const vkc_array *xa, const vkc_array *xb, vkc_value *out) {
@@ -305,7 +366,12 @@ static vkc_status run_group(vkc_ctx *ctx, const vkc_array *xa, const vkc_array *
     GroupTable t{};
     bool done = false;
     if (slots > GI_SMALL_SLOTS) {
-        if (new_table(ctx, GI_SMALL_SLOTS, xb != nullptr, &small, &t)) return alloc_fail();
+        if ((st = new_table(ctx, GI_SMALL_SLOTS, xb != nullptr, &small, &t))) {
+            if (st == VKC_ALLOC) return alloc_fail();
+            cleanup();
+            vkc_array_release(o);
+            return st;
+        }
         if (xb) launch_insert<true>(ctx, true, a, b, n, t, slot_of, flags);
         else launch_insert<false>(ctx, true, a, b, n, t, slot_of, flags);
         if ((st = launched(ctx, "gi_insert"))) {
@@ -325,7 +391,12 @@ static vkc_status run_group(vkc_ctx *ctx, const vkc_array *xa, const vkc_array *
         if (!done) small.release();
     }
     if (!done) {
-        if (new_table(ctx, slots, xb != nullptr, &full, &t)) return alloc_fail();
+        if ((st = new_table(ctx, slots, xb != nullptr, &full, &t))) {
+            if (st == VKC_ALLOC) return alloc_fail();
+            cleanup();
+            vkc_array_release(o);
+            return st;
+        }
         if (xb) launch_insert<true>(ctx, false, a, b, n, t, slot_of, flags);
         else launch_insert<false>(ctx, false, a, b, n, t, slot_of, flags);
         if ((st = launched(ctx, "gi_insert"))) {
@@ -342,15 +413,8 @@ static vkc_status run_group(vkc_ctx *ctx, const vkc_array *xa, const vkc_array *
         return st;
     }
     gi_number_kernel<<<tiles, GI_THREADS, 0, ctx->stream>>>(slot_of, n, t, tiles, recs, next_epoch(ctx), ctx->counters,
-                                                           ctx->status);
+                                                           static_cast<long long *>(o->data()), ctx->status);
     if ((st = launched(ctx, "gi_number"))) {
-        cleanup();
-        vkc_array_release(o);
-        return st;
-    }
-    gi_out_kernel<<<stream_grid(ctx, n, 256, 8, 1024), 256, 0, ctx->stream>>>(slot_of, n, t.meta,
-                                                                               static_cast<long long *>(o->data()));
-    if ((st = launched(ctx, "gi_out"))) {
         cleanup();
         vkc_array_release(o);
         return st;
