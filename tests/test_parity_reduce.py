@@ -21,6 +21,12 @@ DATASETS = {
         oracle.rand_i64(n, s + 5) % 3, [1.0 + 2.0 ** -33, 1.0 + 3 * 2.0 ** -33, 1.0])),
     "small_then_big": lambda n, s=0: np.where(np.arange(n) < n // 2, 1e-300, 1e300) * uniform(n, s + 3),
     "negative": lambda n, s=0: -uniform(n, s + 4),
+    # Quarters below 16: rows with few mantissa bits, so the quick no-tie test fails on most
+    # segments and the exact test decides (no row is halfway: the lane sums stay far below
+    # 2^51). On lanes that start at 2^53 (spacing 2) a quarter k/4 is halfway when k = 4 mod 8.
+    "quarters": lambda n, s=0: (oracle.rand_i64(n, s + 8).view(np.uint64) % np.uint64(64)).astype(np.float64) / 4,
+    "quarters_on_2^53": lambda n, s=0: np.where(np.arange(n) < 16, 2.0 ** 53, (
+        oracle.rand_i64(n, s + 9).view(np.uint64) % np.uint64(64)).astype(np.float64) / 4),
     "zeros": lambda n, s=0: np.where(oracle.rand_i64(n, s + 6) % 3 == 0, 0.0, uniform(n, s + 6)),
 }
 

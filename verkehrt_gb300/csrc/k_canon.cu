@@ -21,8 +21,8 @@
 //    segments of 8 blocks), and five kernels, none of which waits on another block, find the
 //    exact lane states:
 //      K1  the approximate (float) lane sums of every tile, in one read of the rows;
-//      K2  per lane, their exclusive prefix over the tiles from the lane's exact state, and each
-//          tile's candidate binades (the approximate range widened by 2^-12 must lie in one
+//      K2  per lane, their exclusive prefix over the tiles from the lane's exact state (group
+//          sums, then a scan inside each group), and each tile's candidate binades (the approximate range widened by 2^-12 must lie in one
 //          binade or two adjacent ones);
 //      K3  each tile's transfer function per lane and candidate binade, in a second read;
 //      K4a per lane and 32-tile chunk, the composed transfer function when the chunk's tiles
@@ -39,6 +39,7 @@
 #include <climits>
 #include <cmath>
 
+#include "lookback.cuh"
 #include "reduce_common.h"
 
 namespace vkc {
@@ -111,23 +112,46 @@ __device__ __forceinline__ bool apply(unsigned long long s, int E, TF f, unsigne
 // RNE(x/u) = (M + 2^(k-1)) >> k unless M mod 2^k is exactly 2^(k-1) (a tie).
 __device__ __forceinline__ bool seg_tf(const unsigned long long (&v)[CT_SEG_BLOCKS][2], int h,
                                        int KE, TF *out) {
+    unsigned exmax = 0;
+#pragma unroll
+    for (int i = 0; i < CT_SEG_BLOCKS; ++i) exmax = max(exmax, static_cast<unsigned>(v[i][h] >> 52));
+    // The sign bit makes a negative row's exponent field at least 2048, above any KE.
+    if (exmax >= static_cast<unsigned>(KE)) return false;
+    // Every row has k = KE - ex >= kmin >= 1. With t = floor(M / 2^(k-1)) (the quotient with
+    // one more bit), round-half-up gives (t + 1) >> 1, so the sum of the increments is
+    // (sum of t + number of odd t) / 2. That is RNE unless a row is exactly halfway: k <= 53 and
+    // no bit of M below the half bit (k - 1); bits 0 .. kmin - 2 are among those bits, so a
+    // row with one of them set is no tie. Zero and subnormal rows have k = 63: t = 0, no tie.
+    const unsigned kmin = static_cast<unsigned>(KE) - exmax;
+    const unsigned low = kmin > 32 ? 0xffffffffu : (1u << (kmin - 1)) - 1u;
+    unsigned long long tsum = 0;
+    unsigned odd = 0;
+    bool maybe_tie = false;
+#pragma unroll
+    for (int i = 0; i < CT_SEG_BLOCKS; ++i) {
+        const unsigned long long b = v[i][h];
+        const unsigned k = min(static_cast<unsigned>(KE) - static_cast<unsigned>(b >> 52), 63u);
+        const unsigned long long t = ((b & MANT) | ONE52) >> (k - 1);
+        tsum += t;
+        odd += static_cast<unsigned>(t) & 1u;
+        maybe_tie |= (k <= 53u) & ((static_cast<unsigned>(b) & low) == 0u);
+    }
+    if (!maybe_tie) {
+        const unsigned long long D = (tsum + odd) >> 1;
+        *out = TF{D, D};
+        return true;
+    }
     unsigned long long D = 0;
-    int exmax = 0;
     bool tie = false;
 #pragma unroll
     for (int i = 0; i < CT_SEG_BLOCKS; ++i) {
         unsigned long long b = v[i][h];
-        int ex = static_cast<int>(b >> 52);  // the sign bit makes negative rows fail ex < KE
-        exmax = max(exmax, ex);
-        // k = KE - ex in [1, 63]: zero and subnormal rows have k >= 64 (increment 0, no tie);
-        // a row with ex >= KE wraps to a large unsigned k and fails the exmax check below.
-        unsigned k = min(static_cast<unsigned>(KE - ex), 63u);
+        unsigned k = min(static_cast<unsigned>(KE - static_cast<int>(b >> 52)), 63u);
         unsigned long long M = (b & MANT) | ONE52;
         unsigned long long w = M + (1ull << (k - 1));
         D += w >> k;
         tie |= (w << (64 - k)) == 0;
     }
-    if (exmax >= KE) return false;
     if (!tie) {
         *out = TF{D, D};
         return true;
@@ -235,19 +259,53 @@ __device__ __forceinline__ void load_tile(const RowArgs &args, int64_t nb, int t
     }
 }
 
+// The float image of a row value: products are taken of the float images (the sums only
+// choose the candidate binades, so their error costs time, never exactness).
+template <int OP>
+__device__ __forceinline__ float approx_row(const RowArgs &a, unsigned long long xv, unsigned long long yv) {
+    if (OP == ROW_DOT) return approx_f32(xv) * approx_f32(yv);
+    if (OP == ROW_SUMSQ) {
+        const float f = approx_f32(xv);
+        return f * f;
+    }
+    if (OP == ROW_CONDSUM) return approx_f32(in_range(a.r, xv) ? xv : a.e);
+    return approx_f32(xv);
+}
+
 // K1: the approximate lane sums of every tile (float sums of float images, one read).
 template <int OP, bool ALIGNED>
 __global__ void __launch_bounds__(CT_THREADS) canon_apx_kernel(RowArgs args, int64_t nb, int T, CanonWork wk) {
     __shared__ float s_apx[CT_SEGS][16];
     const int t = threadIdx.x, lp = t & 7, seg = t >> 3;
     const int tile = blockIdx.x;
-    unsigned long long v[CT_SEG_BLOCKS][2];
-    load_tile<OP, ALIGNED>(args, nb, tile, lp, seg, v);
     float a0 = 0.f, a1 = 0.f;
+    const int64_t blk0 = static_cast<int64_t>(tile) * CT_BLOCKS;
 #pragma unroll
     for (int i = 0; i < CT_SEG_BLOCKS; ++i) {
-        a0 += approx_f32(v[i][0]);
-        a1 += approx_f32(v[i][1]);
+        const int64_t b = blk0 + seg * CT_SEG_BLOCKS + i;
+        if (b < nb) {
+            const int64_t r = b * 16 + 2 * lp;
+            unsigned long long x0, x1, y0 = 0, y1 = 0;
+            if (ALIGNED) {
+                const ulonglong2 xv = __ldcs(reinterpret_cast<const ulonglong2 *>(args.x + r));
+                x0 = xv.x;
+                x1 = xv.y;
+                if (OP == ROW_DOT) {
+                    const ulonglong2 yv = __ldcs(reinterpret_cast<const ulonglong2 *>(args.y + r));
+                    y0 = yv.x;
+                    y1 = yv.y;
+                }
+            } else {
+                x0 = __ldcs(args.x + r);
+                x1 = __ldcs(args.x + r + 1);
+                if (OP == ROW_DOT) {
+                    y0 = __ldcs(args.y + r);
+                    y1 = __ldcs(args.y + r + 1);
+                }
+            }
+            a0 += approx_row<OP>(args, x0, y0);
+            a1 += approx_row<OP>(args, x1, y1);
+        }
     }
     s_apx[seg][2 * lp] = a0;
     s_apx[seg][2 * lp + 1] = a1;
@@ -257,49 +315,6 @@ __global__ void __launch_bounds__(CT_THREADS) canon_apx_kernel(RowArgs args, int
         for (int s = 0; s < CT_SEGS; ++s) A += s_apx[s][t];
         wk.apx[static_cast<int64_t>(t) * T + tile] = A;
     }
-}
-
-// Block-wide sum and exclusive prefix of one double per thread (blockDim.x a multiple of 32).
-__device__ double block_sum_f64(double v) {
-    __shared__ double s_w[32];
-    __shared__ double s_total;
-    v = warp_sum(v);
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    __syncthreads();
-    if (lane == 0) s_w[w] = v;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double t = 0;
-        for (int i = 0; i < nw; ++i) t += s_w[i];
-        s_total = t;
-    }
-    __syncthreads();
-    return s_total;
-}
-__device__ double block_exclusive_f64(double v, double *total) {
-    __shared__ double s_w[32];
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    double x = v;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const double y = __shfl_up_sync(FULL, x, o);
-        if (lane >= o) x += y;
-    }
-    __syncthreads();
-    if (lane == 31) s_w[w] = x;
-    __syncthreads();
-    if (w == 0) {
-        double z = lane < nw ? s_w[lane] : 0.0;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const double y = __shfl_up_sync(FULL, z, o);
-            if (lane >= o) z += y;
-        }
-        s_w[lane] = z;
-    }
-    __syncthreads();
-    *total = s_w[nw - 1];
-    return (w ? s_w[w - 1] : 0.0) + x - v;
 }
 
 // K2a: per lane and group of CAND_GROUP tiles (one block each), the approximate sum of the
@@ -320,33 +335,54 @@ __global__ void __launch_bounds__(256) canon_gsum_kernel(int T, int G, CanonWork
     }
 }
 
-// K2b: per lane and group (one block each, one thread per tile), the exclusive prefix of the
-// approximate sums over the lane's tiles from its exact state, and each tile's candidate
-// binades: the range [start, end] widened by 2^-12 on each side must lie in one binade or two
-// adjacent ones.
-__global__ void __launch_bounds__(CAND_GROUP) canon_cand_kernel(int T, int G, CanonWork wk, const CanonState *state) {
+// K2b: per lane and group (one block each, CAND_PER tiles per thread), the exclusive prefix
+// of the approximate sums over the lane's tiles from its exact state, and each tile's
+// candidate binades: the range [start, end] widened by 2^-12 on each side must lie in one
+// binade or two adjacent ones. The prefix inside the group is a float scan (its error, a few
+// float roundings, is far inside the margin); the groups before it and the state are added in
+// double.
+constexpr int CAND_THREADS = 256;
+constexpr int CAND_PER = CAND_GROUP / CAND_THREADS;
+
+__global__ void __launch_bounds__(CAND_THREADS) canon_cand_kernel(int T, int G, CanonWork wk, const CanonState *state) {
+    __shared__ double s_base;
     const int L = blockIdx.x / G, g = blockIdx.x % G, t = threadIdx.x;
-    const int k = g * CAND_GROUP + t;
-    const double A = k < T ? static_cast<double>(wk.apx[static_cast<int64_t>(L) * T + k]) : 0.0;
-    // The groups before this one (at most G values), then this group's exclusive prefix.
-    double before = t < g ? wk.gsum[L * G + t] : 0.0;
-    for (int i = t + CAND_GROUP; i < g; i += CAND_GROUP) before += wk.gsum[L * G + i];
-    double ex_total;
-    const double base = block_sum_f64(before);
-    const double ex = block_exclusive_f64(A, &ex_total);
-    if (k >= T) return;
-    const double pre = as_f64(state->lanes[L]) + base + ex;
-    const double lo = A < 0 ? pre + A : pre, hi = A < 0 ? pre : pre + A;
-    const int elo = binade(lo * (1.0 - 0x1p-12)), ehi = binade(hi * (1.0 + 0x1p-12));
-    int c0 = NO_E, c1 = NO_E;
-    if (elo != NO_E && ehi != NO_E && elo >= -959) {
-        if (ehi == elo) c0 = elo;
-        else if (ehi == elo + 1) {
-            c0 = elo;
-            c1 = ehi;
-        }
+    const int k0 = g * CAND_GROUP + t * CAND_PER;
+    const float *apx = wk.apx + static_cast<int64_t>(L) * T;
+    float a[CAND_PER], tot = 0.f;
+#pragma unroll
+    for (int j = 0; j < CAND_PER; ++j) {
+        a[j] = k0 + j < T ? apx[k0 + j] : 0.f;
+        tot += a[j];
     }
-    *reinterpret_cast<int2 *>(&wk.cand[(static_cast<int64_t>(k) * 16 + L) * 2]) = make_int2(c0, c1);
+    if (t < 32) {
+        double b = 0.0;
+        for (int i = t; i < g; i += 32) b += wk.gsum[L * G + i];
+        b = warp_sum(b);
+        if (t == 0) s_base = as_f64(state->lanes[L]) + b;
+    }
+    float total;
+    float run = block_exclusive_sum<float>(tot, &total);  // synchronises the block
+    const double start = s_base;
+#pragma unroll
+    for (int j = 0; j < CAND_PER; ++j) {
+        const int k = k0 + j;
+        if (k >= T) break;
+        const double A = static_cast<double>(a[j]);
+        const double pre = start + static_cast<double>(run);
+        run += a[j];
+        const double lo = A < 0 ? pre + A : pre, hi = A < 0 ? pre : pre + A;
+        const int elo = binade(lo * (1.0 - 0x1p-12)), ehi = binade(hi * (1.0 + 0x1p-12));
+        int c0 = NO_E, c1 = NO_E;
+        if (elo != NO_E && ehi != NO_E && elo >= -959) {
+            if (ehi == elo) c0 = elo;
+            else if (ehi == elo + 1) {
+                c0 = elo;
+                c1 = ehi;
+            }
+        }
+        *reinterpret_cast<int2 *>(&wk.cand[(static_cast<int64_t>(k) * 16 + L) * 2]) = make_int2(c0, c1);
+    }
 }
 
 // K3: each tile's transfer function per lane and candidate binade (NO_E when a segment does
@@ -675,7 +711,7 @@ static vkc_status launch_canon(vkc_ctx *ctx, const RowArgs &a, int64_t nb, int T
     const int G = (T + CAND_GROUP - 1) / CAND_GROUP;
     canon_gsum_kernel<<<16 * G, 256, 0, ctx->stream>>>(T, G, wk);
     if ((st = launched(ctx, "canon_gsum"))) return st;
-    canon_cand_kernel<<<16 * G, CAND_GROUP, 0, ctx->stream>>>(T, G, wk, state);
+    canon_cand_kernel<<<16 * G, CAND_THREADS, 0, ctx->stream>>>(T, G, wk, state);
     if ((st = launched(ctx, "canon_cand"))) return st;
     canon_tf_kernel<OP, ALIGNED><<<T, CT_THREADS, 0, ctx->stream>>>(a, nb, T, wk);
     if ((st = launched(ctx, "canon_tf"))) return st;
