@@ -6,7 +6,7 @@
 //  * one histogram kernel counts all 8 digits in one read (radix.rs:199-202);
 //  * a digit that is equal in every row leaves the order unchanged and its pass is skipped
 //    (radix.rs:203-211);
-//  * each remaining digit is one reduce-then-scan pass over 4096-row tiles: `up` counts each
+//  * each remaining digit is one reduce-then-scan pass over 3072-row tiles: `up` counts each
 //    tile's digits into a digit-major table, one exclusive scan of that table gives every
 //    (digit, tile) its first output row, and `down` ranks the tile's rows stably by digit
 //    (a ballot per digit bit, in row order) and scatters them. The first pass reads the keys, the
@@ -21,13 +21,17 @@
 
 namespace vkc {
 
+#ifndef RS_ITEMS_PER_THREAD
+#define RS_ITEMS_PER_THREAD 12  // rows per thread in a radix pass (even: ranks are packed in pairs)
+#endif
 constexpr int RS_THREADS = 256;
 constexpr int RS_WARPS = RS_THREADS / 32;
-constexpr int RS_ITEMS = 16;
+constexpr int RS_ITEMS = RS_ITEMS_PER_THREAD;
+static_assert(RS_ITEMS % 2 == 0, "ranks are packed two per word");
 constexpr int RS_TILE = RS_THREADS * RS_ITEMS;
 constexpr int RADIX = 256;
 #ifndef RS_DOWN_MIN_BLOCKS
-#define RS_DOWN_MIN_BLOCKS 3  // resident blocks per SM that the down kernel's registers allow
+#define RS_DOWN_MIN_BLOCKS 4  // resident blocks per SM that the down kernel's registers allow
 #endif
 
 __device__ __forceinline__ unsigned long long image_of(long long k) {
