@@ -69,6 +69,12 @@ def lib():
         L.orc_cmp_f64.argtypes = [P, P, I64, ctypes.c_int, P]
         L.orc_select_f64.argtypes = [P, P, P, I64, P]
         L.orc_dd_sum.argtypes = [P, I64, P, P]
+        C, INT = ctypes.c_char_p, ctypes.c_int
+        L.orc_ew_binary.argtypes = [C, INT, P, INT, P, INT, I64, P]
+        L.orc_ew_unary.argtypes = [C, INT, P, I64, P]
+        L.orc_ew_select.argtypes = [INT, P, INT, P, INT, P, INT, I64, P]
+        L.orc_ew_cast.argtypes = [INT, INT, P, I64, P]
+        L.orc_ew_div_const.argtypes = [INT, P, P, I64, P, C]
     return _lib
 
 
@@ -340,3 +346,61 @@ def dd_sum(x):
     hi, lo = ctypes.c_double(), ctypes.c_double()
     lib().orc_dd_sum(_p(x), len(x), ctypes.byref(hi), ctypes.byref(lo))
     return hi.value, lo.value
+
+
+# ---------------------------------------------------------------- elementwise, every array type
+
+EW_TYPES = {"f64": 0, "f32": 1, "i64": 2, "u64": 3, "i32": 4, "u8": 5, "bool": 6}
+EW_DTYPES = {"f64": np.float64, "f32": np.float32, "i64": np.int64, "u64": np.uint64, "i32": np.int32,
+             "u8": np.uint8, "bool": np.uint8}
+EW_BOOL_OUT = ("lt", "le", "gt", "ge", "eq", "ne")
+
+
+def _ew_operand(x, t):
+    """(contiguous array, is_splat) of operand x of element type t."""
+    a = np.ascontiguousarray(np.atleast_1d(np.asarray(x)).astype(EW_DTYPES[t], copy=False))
+    return a, np.ndim(x) == 0
+
+
+def ew_binary(op, t, a, b):
+    """elementwise.rs binary `op` on type t; a or b may be a scalar (a splat row)."""
+    (xa, sa), (xb, sb) = _ew_operand(a, t), _ew_operand(b, t)
+    n = max(1 if sa else len(xa), 1 if sb else len(xb)) if (sa and sb) else (len(xb) if sa else len(xa))
+    out = np.empty(n, dtype=np.uint8 if (op in EW_BOOL_OUT or t == "bool") else EW_DTYPES[t])
+    if lib().orc_ew_binary(op.encode(), EW_TYPES[t], _p(xa), int(sa), _p(xb), int(sb), n, _p(out)) != 0:
+        raise OracleError("no %s on %s" % (op, t))
+    return out
+
+
+def ew_unary(op, t, a):
+    x, _ = _ew_operand(a, t)
+    out = np.empty(len(x), dtype=EW_DTYPES[t])
+    if lib().orc_ew_unary(op.encode(), EW_TYPES[t], _p(x), len(x), _p(out)) != 0:
+        raise OracleError("no %s on %s" % (op, t))
+    return out
+
+
+def ew_select(t, m, a, b):
+    (xm, sm), (xa, sa), (xb, sb) = _ew_operand(m, "bool"), _ew_operand(a, t), _ew_operand(b, t)
+    n = max(len(v) for v, s in ((xm, sm), (xa, sa), (xb, sb)) if not s) if not (sm and sa and sb) else 1
+    out = np.empty(n, dtype=EW_DTYPES[t])
+    lib().orc_ew_select(out.itemsize, _p(xm), int(sm), _p(xa), int(sa), _p(xb), int(sb), n, _p(out))
+    return out
+
+
+def ew_cast(src, dst, a):
+    x, _ = _ew_operand(a, src)
+    out = np.empty(len(x), dtype=EW_DTYPES[dst])
+    if lib().orc_ew_cast(EW_TYPES[src], EW_TYPES[dst], _p(x), len(x), _p(out)) != 0:
+        raise OracleError("no cast %s -> %s" % (src, dst))
+    return out
+
+
+def ew_div_const(t, a, d):
+    x, _ = _ew_operand(a, t)
+    dv, _ = _ew_operand(d, t)
+    out = np.empty(len(x), dtype=EW_DTYPES[t])
+    err = ctypes.create_string_buffer(256)
+    if lib().orc_ew_div_const(EW_TYPES[t], _p(x), _p(dv), len(x), _p(out), err) != 0:
+        raise OracleError(err.value.decode())
+    return out

@@ -10,18 +10,18 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "liboracle.so")
-SRC = os.path.join(HERE, "oracle.c")
+SRCS = [os.path.join(HERE, "oracle.c"), os.path.join(HERE, "elementwise.c")]
 HDR = os.path.join(HERE, "oracle.h")
 
 
 def build(force=False):
     if (not force and os.path.exists(LIB)
-            and os.path.getmtime(LIB) >= max(os.path.getmtime(SRC), os.path.getmtime(HDR),
+            and os.path.getmtime(LIB) >= max(max(os.path.getmtime(f) for f in SRCS), os.path.getmtime(HDR),
                                             os.path.getmtime(__file__))):
         return LIB
     cc = os.environ.get("CC", "gcc")
     tmp = LIB + ".tmp"
-    cmd = [cc, "-O3", "-ffp-contract=off", "-std=c11", "-fPIC", "-shared", "-o", tmp, SRC, "-lm"]
+    cmd = [cc, "-O3", "-ffp-contract=off", "-std=c11", "-fPIC", "-shared", "-o", tmp] + SRCS + ["-lm"]
     p = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
     if p.returncode != 0:
         raise RuntimeError("oracle build failed:\n" + p.stdout)

@@ -98,6 +98,14 @@ void orc_mul_f64(const double *x, const double *y, int64_t n, double *out);
 void orc_cmp_f64(const double *x, const double *y, int64_t n, int cmp, uint8_t *out);
 void orc_select_f64(const uint8_t *m, const double *a, const double *b, int64_t n, double *out);
 
+/* elementwise.c: every array type (type codes of vkc_type). */
+int orc_ew_binary(const char *op, int type, const void *a, int as, const void *b, int bs, int64_t n, void *out);
+int orc_ew_unary(const char *op, int type, const void *a, int64_t n, void *out);
+void orc_ew_select(int width, const uint8_t *m, int ms, const void *a, int as, const void *b, int bs, int64_t n,
+                   void *out);
+int orc_ew_cast(int src, int dst, const void *a, int64_t n, void *out);
+int orc_ew_div_const(int type, const void *a, const void *d, int64_t n, void *out, char *err);
+
 /* Accuracy helpers (not reference semantics): Neumaier's compensated sum and an exact
  * double-double accumulation, used to state error bounds. */
 double orc_neumaier_sum(const double *x, int64_t n);

@@ -1,10 +1,23 @@
-// Elementwise kernels for unfused plans and the group-by idioms: mul/add/sub/min/max on f64
-// and i64, the six comparisons on f64 and i64, select_f64/select_i64, and/or/not on bool, and
-// iota (src/kernels/scalar/elementwise.rs:378-445, :757-804; construct.rs:36-45).
-//
-// Every operand is an array or a scalar splat (InputSpec::Either). f64 arithmetic is one IEEE
-// operation per row (built with -fmad=false), so `mul_f64` then `reduce_add_f64` gives the bits
-// of `dot_f64`.
+// Elementwise kernels of every array type (src/kernels/scalar/elementwise.rs:757-873 register
+// them; the array kernels exist for the v1 array types f64, f32, i64, i32, u8, u64 and bool,
+// value.rs:23-31), and iota (construct.rs:36-45):
+//  * Num on every numeric type: add, sub, mul, min, max and the four orderings (:757-769);
+//    integers wrap, floats are one IEEE operation (built with -fmad=false), min/max are the
+//    754-2019 minimum/maximum (:403-445);
+//  * Signed (i32, i64, f32, f64): neg and abs, wrapping on integers, the sign bit on floats
+//    (:447-476); Float: div and sqrt, correctly rounded (:478-495, :777-781);
+//  * eq, ne and select on every type (:789-804); and, or, xor, not on i32, i64, u8, u64 (bits)
+//    and on bool (0/1 storage) (:806-823);
+//  * casts between every array type and every numeric array type by Rust `as` (:572-613,
+//    :858-871): float to integer truncates toward zero, saturates and maps NaN to 0;
+//  * div_const on i64, u64, i32, u8 (:615-755): truncating division by a scalar with the
+//    round-up multiply-high method of Granlund and Montgomery ("Division by invariant integers
+//    using multiplication", 1994), the divisor's constants derived once on the host; signed
+//    types divide magnitudes and fix the sign, so MIN / -1 = MIN as wrapping_div gives.
+// Every operand is an array or a scalar splat (InputSpec::Either; the divisor is a scalar).
+// One row per thread per grid-stride step; the cost of an entry is its row bytes.
+#include <type_traits>
+
 #include "reduce_common.h"
 
 namespace vkc {
@@ -22,93 +35,167 @@ template <class T> __device__ __forceinline__ T get(const Opnd &o, int64_t i) {
     return v;
 }
 
-// Comparisons come last: an op at or after EW_EQ produces bool.
-enum EwOp {
-    EW_ADD, EW_SUB, EW_MUL, EW_MIN, EW_MAX, EW_AND, EW_OR, EW_XOR, EW_NOT,
-    EW_EQ, EW_NE, EW_LT, EW_LE, EW_GT, EW_GE
-};
+// ------------------------------------------------------------------ row operations
 
-// IEEE 754-2019 minimum/maximum, elementwise.rs:412-440.
-__device__ __forceinline__ double fmin2(double a, double b) {
-    if (isnan(a) || isnan(b)) return __longlong_as_double(0x7ff8000000000000ll);
-    if (a == b) return signbit(a) ? a : b;
+template <class T> using Wide = typename std::make_unsigned<T>::type;
+
+// Arithmetic: wrapping integers (elementwise.rs:386-401), IEEE floats.
+template <class T> __device__ __forceinline__ T ew_add(T a, T b) { return static_cast<T>(static_cast<Wide<T>>(a) + static_cast<Wide<T>>(b)); }
+template <class T> __device__ __forceinline__ T ew_sub(T a, T b) { return static_cast<T>(static_cast<Wide<T>>(a) - static_cast<Wide<T>>(b)); }
+template <class T> __device__ __forceinline__ T ew_mul(T a, T b) { return static_cast<T>(static_cast<Wide<T>>(a) * static_cast<Wide<T>>(b)); }
+template <> __device__ __forceinline__ double ew_add(double a, double b) { return __dadd_rn(a, b); }
+template <> __device__ __forceinline__ double ew_sub(double a, double b) { return __dsub_rn(a, b); }
+template <> __device__ __forceinline__ double ew_mul(double a, double b) { return __dmul_rn(a, b); }
+template <> __device__ __forceinline__ float ew_add(float a, float b) { return __fadd_rn(a, b); }
+template <> __device__ __forceinline__ float ew_sub(float a, float b) { return __fsub_rn(a, b); }
+template <> __device__ __forceinline__ float ew_mul(float a, float b) { return __fmul_rn(a, b); }
+
+// min/max: Ord on integers; IEEE 754-2019 minimum/maximum on floats (elementwise.rs:413-440).
+template <class T> __device__ __forceinline__ T ew_min(T a, T b) {
+    if constexpr (std::is_floating_point<T>::value) {
+        if (a != a || b != b) return a != a ? a + b : b + a;  // a NaN operand: a NaN result
+        if (a == b) return (std::is_same<T, double>::value ? __double_as_longlong(a) < 0 : __float_as_int(a) < 0) ? a : b;
+    }
     return a < b ? a : b;
 }
-__device__ __forceinline__ double fmax2(double a, double b) {
-    if (isnan(a) || isnan(b)) return __longlong_as_double(0x7ff8000000000000ll);
-    if (a == b) return !signbit(a) ? a : b;
+template <class T> __device__ __forceinline__ T ew_max(T a, T b) {
+    if constexpr (std::is_floating_point<T>::value) {
+        if (a != a || b != b) return a != a ? a + b : b + a;
+        if (a == b) return (std::is_same<T, double>::value ? __double_as_longlong(a) < 0 : __float_as_int(a) < 0) ? b : a;
+    }
     return a > b ? a : b;
 }
 
-template <class T, int OP> struct Bin;
-template <int OP> struct Bin<double, OP> {
-    using Out = typename std::conditional<(OP >= EW_EQ), unsigned char, double>::type;
-    __device__ static Out f(double a, double b) {
-        switch (OP) {
-        case EW_ADD: return __dadd_rn(a, b);
-        case EW_SUB: return __dsub_rn(a, b);
-        case EW_MUL: return __dmul_rn(a, b);
-        case EW_MIN: return fmin2(a, b);
-        case EW_MAX: return fmax2(a, b);
-        case EW_EQ: return a == b;
-        case EW_NE: return a != b;
-        case EW_LT: return a < b;
-        case EW_LE: return a <= b;
-        case EW_GT: return a > b;
-        default: return a >= b;
+// neg/abs: wrapping on integers (:452-462), the sign bit on floats (:464-474).
+template <class T> __device__ __forceinline__ T ew_neg(T a) { return static_cast<T>(Wide<T>(0) - static_cast<Wide<T>>(a)); }
+template <> __device__ __forceinline__ double ew_neg(double a) { return __longlong_as_double(__double_as_longlong(a) ^ (1ll << 63)); }
+template <> __device__ __forceinline__ float ew_neg(float a) { return __int_as_float(__float_as_int(a) ^ static_cast<int>(0x80000000u)); }
+template <class T> __device__ __forceinline__ T ew_abs(T a) { return a < 0 ? ew_neg(a) : a; }
+template <> __device__ __forceinline__ double ew_abs(double a) { return __longlong_as_double(__double_as_longlong(a) & 0x7fffffffffffffffll); }
+template <> __device__ __forceinline__ float ew_abs(float a) { return __int_as_float(__float_as_int(a) & 0x7fffffff); }
+
+__device__ __forceinline__ double ew_div(double a, double b) { return __ddiv_rn(a, b); }
+__device__ __forceinline__ float ew_div(float a, float b) { return __fdiv_rn(a, b); }
+__device__ __forceinline__ double ew_sqrt(double a) { return __dsqrt_rn(a); }
+__device__ __forceinline__ float ew_sqrt(float a) { return __fsqrt_rn(a); }
+
+// Operation tags: f(a, b) or f(a) on storage type T, giving U.
+#define EW_BIN(NAME, EXPR)                                                                     \
+    struct NAME {                                                                              \
+        template <class T, class U> __device__ static U f(T a, T b) { return static_cast<U>(EXPR); } \
+    };
+EW_BIN(OpAdd, ew_add(a, b))
+EW_BIN(OpSub, ew_sub(a, b))
+EW_BIN(OpMul, ew_mul(a, b))
+EW_BIN(OpMin, ew_min(a, b))
+EW_BIN(OpMax, ew_max(a, b))
+EW_BIN(OpLt, a < b)
+EW_BIN(OpLe, a <= b)
+EW_BIN(OpGt, a > b)
+EW_BIN(OpGe, a >= b)
+EW_BIN(OpEq, a == b)
+EW_BIN(OpNe, a != b)
+EW_BIN(OpAnd, a & b)
+EW_BIN(OpOr, a | b)
+EW_BIN(OpXor, a ^ b)
+EW_BIN(OpDiv, ew_div(a, b))
+#undef EW_BIN
+
+#define EW_UN(NAME, EXPR)                                                                      \
+    struct NAME {                                                                              \
+        template <class T, class U> __device__ static U f(T a) { return static_cast<U>(EXPR); } \
+    };
+EW_UN(OpNeg, ew_neg(a))
+EW_UN(OpAbs, ew_abs(a))
+EW_UN(OpSqrt, ew_sqrt(a))
+EW_UN(OpBitNot, ~a)
+EW_UN(OpBoolNot, a ^ 1u)
+#undef EW_UN
+
+// Rust `as` (elementwise.rs:572-613).
+template <class S, class D> struct CastAs {
+    __device__ static D f(S x) {
+        if constexpr (std::is_floating_point<S>::value && std::is_integral<D>::value) {
+            // Truncation toward zero, saturated at D's bounds; NaN maps to 0.
+            const double v = static_cast<double>(x);
+            if (v != v) return D(0);
+            const double hi = std::is_same<D, unsigned char>::value ? 256.0
+                              : std::is_same<D, int>::value         ? 2147483648.0
+                              : std::is_same<D, long long>::value   ? 9223372036854775808.0
+                                                                    : 18446744073709551616.0;
+            const double lo = std::is_signed<D>::value ? -hi : 0.0;
+            if (v >= hi) return static_cast<D>(std::is_signed<D>::value ? (hi == 2147483648.0 ? 2147483647ll : 9223372036854775807ll)
+                                                                        : (hi == 256.0 ? 255ull : 18446744073709551615ull));
+            if (v <= lo) return std::is_signed<D>::value ? static_cast<D>(hi == 2147483648.0 ? -2147483648ll : (-9223372036854775807ll - 1)) : D(0);
+            return static_cast<D>(v);
+        } else {
+            return static_cast<D>(x);  // integer truncation or extension; to float: round to nearest even
         }
     }
 };
-template <int OP> struct Bin<long long, OP> {
-    using Out = typename std::conditional<(OP >= EW_EQ), unsigned char, long long>::type;
-    __device__ static Out f(long long a, long long b) {
-        // Integer arithmetic wraps (elementwise.rs:391-400).
-        unsigned long long ua = static_cast<unsigned long long>(a), ub = static_cast<unsigned long long>(b);
-        switch (OP) {
-        case EW_ADD: return static_cast<long long>(ua + ub);
-        case EW_SUB: return static_cast<long long>(ua - ub);
-        case EW_MUL: return static_cast<long long>(ua * ub);
-        case EW_MIN: return a < b ? a : b;
-        case EW_MAX: return a > b ? a : b;
-        case EW_AND: return a & b;
-        case EW_OR: return a | b;
-        case EW_XOR: return a ^ b;
-        case EW_EQ: return a == b;
-        case EW_NE: return a != b;
-        case EW_LT: return a < b;
-        case EW_LE: return a <= b;
-        case EW_GT: return a > b;
-        default: return a >= b;
-        }
-    }
-};
-template <int OP> struct Bin<unsigned char, OP> {
-    using Out = unsigned char;
-    __device__ static Out f(unsigned char a, unsigned char b) {
-        switch (OP) {
-        case EW_AND: return a & b;
-        case EW_OR: return a | b;
-        case EW_EQ: return a == b;
-        case EW_NE: return a != b;
-        default: return static_cast<unsigned char>(a ^ 1u);  // not
-        }
-    }
+template <class S, class D> struct OpCast {
+    template <class T, class U> __device__ static U f(T a) { return CastAs<S, D>::f(a); }
 };
 
-template <class T, int OP>
-__global__ void __launch_bounds__(256) binary_kernel(Opnd a, Opnd b, typename Bin<T, OP>::Out *__restrict__ out,
-                                                     int64_t n) {
-    int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+// ------------------------------------------------------------------ kernels
+
+template <class T, class U, class F>
+__global__ void __launch_bounds__(256) ew_binary_kernel(Opnd a, Opnd b, U *__restrict__ out, int64_t n) {
+    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
     for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride)
-        out[i] = Bin<T, OP>::f(get<T>(a, i), get<T>(b, i));
+        out[i] = F::template f<T, U>(get<T>(a, i), get<T>(b, i));
+}
+
+template <class T, class U, class F>
+__global__ void __launch_bounds__(256) ew_unary_kernel(Opnd a, U *__restrict__ out, int64_t n) {
+    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride)
+        out[i] = F::template f<T, U>(get<T>(a, i));
 }
 
 template <class T>
 __global__ void __launch_bounds__(256) select_kernel(Opnd m, Opnd a, Opnd b, T *__restrict__ out, int64_t n) {
-    int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
     for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride)
         out[i] = get<unsigned char>(m, i) ? get<T>(a, i) : get<T>(b, i);
 }
+
+// The divider of an unsigned divisor d of B bits (elementwise.rs:627-666): with l = ceil(log2 d),
+// m = floor(2^B (2^l - d) / d) + 1, t = mulhi(m, n), q = (t + ((n - t) >> min(l, 1))) >> max(l - 1, 0).
+struct Divider {
+    unsigned long long m;
+    int sh1, sh2;
+    unsigned long long dneg;  // signed types: all ones when the divisor is negative
+};
+
+__device__ __forceinline__ unsigned long long div_u(unsigned long long x, const Divider &v, int bits) {
+    unsigned long long t;
+    if (bits == 64) t = __umul64hi(v.m, x);
+    else t = (v.m * x) >> bits;  // m and x below 2^bits <= 2^32: the product fits
+    return (t + ((x - t) >> v.sh1)) >> v.sh2;
+}
+
+template <class T>
+__global__ void __launch_bounds__(256) div_const_kernel(Opnd a, Divider v, T *__restrict__ out, int64_t n) {
+    using UT = Wide<T>;
+    constexpr int B = 8 * sizeof(T);
+    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const T x = get<T>(a, i);
+        if constexpr (std::is_signed<T>::value) {
+            // Magnitudes, then the sign: MIN's magnitude 2^(B-1) divided by 1 reads back as MIN.
+            const UT xneg = static_cast<UT>(x < 0 ? ~UT(0) : UT(0));
+            const UT mag = x < 0 ? static_cast<UT>(UT(0) - static_cast<UT>(x)) : static_cast<UT>(x);
+            const UT q = static_cast<UT>(div_u(mag, v, B));
+            const UT mask = static_cast<UT>(xneg ^ static_cast<UT>(v.dneg));
+            out[i] = static_cast<T>(static_cast<UT>((q ^ mask) - mask));
+        } else {
+            out[i] = static_cast<T>(div_u(static_cast<unsigned long long>(x), v, B));
+        }
+    }
+}
+
+// ------------------------------------------------------------------ entries
 
 static Opnd opnd(const Arg &a) {
     Opnd o;
@@ -118,31 +205,59 @@ static Opnd opnd(const Arg &a) {
     return o;
 }
 
-template <class T, int OP>
-static vkc_status run_binary(vkc_ctx *ctx, const Arg *args, int nargs, int64_t n, vkc_array *out) {
+static int ew_grid(vkc_ctx *ctx, int64_t n) { return stream_grid(ctx, n, 256, 8, 2048); }
+
+template <class T, class U, class F>
+static vkc_status run_bin(vkc_ctx *ctx, const Arg *args, int nargs, int64_t n, vkc_array *out) {
     if (nargs != 2) return fail(ctx, VKC_RUNTIME, arity_error(2, nargs));
-    int grid = stream_grid(ctx, n, 256, 8, 2048);
-    binary_kernel<T, OP><<<grid, 256, 0, ctx->stream>>>(opnd(args[0]), opnd(args[1]),
-        static_cast<typename Bin<T, OP>::Out *>(out->data()), n);
-    return launched(ctx, "binary");
+    ew_binary_kernel<T, U, F><<<ew_grid(ctx, n), 256, 0, ctx->stream>>>(opnd(args[0]), opnd(args[1]),
+                                                                         static_cast<U *>(out->data()), n);
+    return launched(ctx, "elementwise");
+}
+
+template <class T, class U, class F>
+static vkc_status run_un(vkc_ctx *ctx, const Arg *args, int nargs, int64_t n, vkc_array *out) {
+    if (nargs != 1) return fail(ctx, VKC_RUNTIME, arity_error(1, nargs));
+    ew_unary_kernel<T, U, F><<<ew_grid(ctx, n), 256, 0, ctx->stream>>>(opnd(args[0]), static_cast<U *>(out->data()), n);
+    return launched(ctx, "elementwise");
 }
 
 template <class T>
 static vkc_status run_select(vkc_ctx *ctx, const Arg *args, int nargs, int64_t n, vkc_array *out) {
     if (nargs != 3) return fail(ctx, VKC_RUNTIME, arity_error(3, nargs));
-    int grid = stream_grid(ctx, n, 256, 8, 2048);
-    select_kernel<T><<<grid, 256, 0, ctx->stream>>>(opnd(args[0]), opnd(args[1]), opnd(args[2]),
-                                                    static_cast<T *>(out->data()), n);
+    select_kernel<T><<<ew_grid(ctx, n), 256, 0, ctx->stream>>>(opnd(args[0]), opnd(args[1]), opnd(args[2]),
+                                                               static_cast<T *>(out->data()), n);
     return launched(ctx, "select");
 }
 
-static vkc_status run_not(vkc_ctx *ctx, const Arg *args, int nargs, int64_t n, vkc_array *out) {
-    if (nargs != 1) return fail(ctx, VKC_RUNTIME, arity_error(1, nargs));
-    int grid = stream_grid(ctx, n, 256, 8, 2048);
-    Opnd z{nullptr, 0, 0};
-    binary_kernel<unsigned char, EW_NOT><<<grid, 256, 0, ctx->stream>>>(opnd(args[0]), z,
-        static_cast<unsigned char *>(out->data()), n);
-    return launched(ctx, "not");
+// The divider of |d| (B bits), elementwise.rs:640-656.
+static Divider make_divider(unsigned long long d, int bits) {
+    int l = 0;
+    while (l < bits && (1ull << l) < d) ++l;  // ceil(log2 d); 0 for d = 1
+    unsigned __int128 num = (static_cast<unsigned __int128>(1) << bits) *
+                            ((static_cast<unsigned __int128>(1) << l) - d);
+    const unsigned __int128 m = num / d + 1;
+    Divider v;
+    v.m = static_cast<unsigned long long>(m);
+    v.sh1 = l < 1 ? l : 1;
+    v.sh2 = l > 0 ? l - 1 : 0;
+    v.dneg = 0;
+    return v;
+}
+
+template <class T>
+static vkc_status run_div_const(vkc_ctx *ctx, const Arg *args, int nargs, int64_t n, vkc_array *out) {
+    if (nargs != 2) return fail(ctx, VKC_RUNTIME, arity_error(2, nargs));
+    T d;
+    memcpy(&d, &args[1].s.bits, sizeof(T));
+    if (d == 0) return fail(ctx, VKC_RUNTIME, "div_const: division by zero");  // elementwise.rs:725-727
+    using UT = Wide<T>;
+    const bool neg = std::is_signed<T>::value && d < 0;
+    const UT mag = neg ? static_cast<UT>(UT(0) - static_cast<UT>(d)) : static_cast<UT>(d);
+    Divider v = make_divider(static_cast<unsigned long long>(mag), 8 * sizeof(T));
+    v.dneg = neg ? ~0ull : 0ull;
+    div_const_kernel<T><<<ew_grid(ctx, n), 256, 0, ctx->stream>>>(opnd(args[0]), v, static_cast<T *>(out->data()), n);
+    return launched(ctx, "div_const");
 }
 
 __global__ void iota_kernel(long long *out, int64_t n) {
@@ -171,49 +286,136 @@ static vkc_status iota(vkc_ctx *ctx, const vkc_value *args, int nargs, vkc_value
     return VKC_OK;
 }
 
+// ------------------------------------------------------------------ registration
+
+template <class T> struct TypeOf;
+template <> struct TypeOf<double> { static constexpr vkc_type v = VKC_F64; };
+template <> struct TypeOf<float> { static constexpr vkc_type v = VKC_F32; };
+template <> struct TypeOf<long long> { static constexpr vkc_type v = VKC_I64; };
+template <> struct TypeOf<unsigned long long> { static constexpr vkc_type v = VKC_U64; };
+template <> struct TypeOf<int> { static constexpr vkc_type v = VKC_I32; };
+template <> struct TypeOf<unsigned char> { static constexpr vkc_type v = VKC_U8; };
+
+static std::string tname(vkc_type t) { return type_name(t); }
+
+// KernelDef of an elementwise entry; cost = the row bytes (elementwise.rs:272).
+static void add(std::vector<KernelDef> &t, const std::string &name, std::vector<InSpec> in, vkc_type out, ElemFn f) {
+    uint64_t cost = static_cast<uint64_t>(type_width(out));
+    for (const InSpec &s : in) cost += static_cast<uint64_t>(type_width(s.type));
+    KernelDef d{name, VKC_ELEMENTWISE, std::move(in), true, out, cost};
+    d.elem = f;
+    t.push_back(d);
+}
+
+// register_num (:757-769).
+template <class T> static void reg_num(std::vector<KernelDef> &t) {
+    const vkc_type ty = TypeOf<T>::v;
+    const std::string n = tname(ty);
+    const InSpec e{IN_EITHER, ty};
+    add(t, "add_" + n, {e, e}, ty, run_bin<T, T, OpAdd>);
+    add(t, "sub_" + n, {e, e}, ty, run_bin<T, T, OpSub>);
+    add(t, "mul_" + n, {e, e}, ty, run_bin<T, T, OpMul>);
+    add(t, "min_" + n, {e, e}, ty, run_bin<T, T, OpMin>);
+    add(t, "max_" + n, {e, e}, ty, run_bin<T, T, OpMax>);
+    add(t, "lt_" + n, {e, e}, VKC_BOOL, run_bin<T, unsigned char, OpLt>);
+    add(t, "le_" + n, {e, e}, VKC_BOOL, run_bin<T, unsigned char, OpLe>);
+    add(t, "gt_" + n, {e, e}, VKC_BOOL, run_bin<T, unsigned char, OpGt>);
+    add(t, "ge_" + n, {e, e}, VKC_BOOL, run_bin<T, unsigned char, OpGe>);
+}
+
+// register_signed (:771-775) and register_float (:777-781).
+template <class T> static void reg_signed(std::vector<KernelDef> &t) {
+    const vkc_type ty = TypeOf<T>::v;
+    const InSpec e{IN_EITHER, ty};
+    add(t, "neg_" + tname(ty), {e}, ty, run_un<T, T, OpNeg>);
+    add(t, "abs_" + tname(ty), {e}, ty, run_un<T, T, OpAbs>);
+}
+template <class T> static void reg_float(std::vector<KernelDef> &t) {
+    const vkc_type ty = TypeOf<T>::v;
+    const InSpec e{IN_EITHER, ty};
+    add(t, "div_" + tname(ty), {e, e}, ty, run_bin<T, T, OpDiv>);
+    add(t, "sqrt_" + tname(ty), {e}, ty, run_un<T, T, OpSqrt>);
+}
+
+// register_any (:789-804): eq, ne, select; `ty` is bool for the bool instantiation on u8.
+template <class T> static void reg_any(std::vector<KernelDef> &t, vkc_type ty) {
+    const std::string n = tname(ty);
+    const InSpec e{IN_EITHER, ty}, b{IN_EITHER, VKC_BOOL};
+    add(t, "eq_" + n, {e, e}, VKC_BOOL, run_bin<T, unsigned char, OpEq>);
+    add(t, "ne_" + n, {e, e}, VKC_BOOL, run_bin<T, unsigned char, OpNe>);
+    add(t, "select_" + n, {b, e, e}, ty, run_select<T>);
+}
+
+// register_bits (:806-813).
+template <class T> static void reg_bits(std::vector<KernelDef> &t) {
+    const vkc_type ty = TypeOf<T>::v;
+    const std::string n = tname(ty);
+    const InSpec e{IN_EITHER, ty};
+    add(t, "and_" + n, {e, e}, ty, run_bin<T, T, OpAnd>);
+    add(t, "or_" + n, {e, e}, ty, run_bin<T, T, OpOr>);
+    add(t, "xor_" + n, {e, e}, ty, run_bin<T, T, OpXor>);
+    add(t, "not_" + n, {e}, ty, run_un<T, T, OpBitNot>);
+}
+
+// register_div_const (:739-755): the divisor is a scalar.
+template <class T> static void reg_div_const(std::vector<KernelDef> &t) {
+    const vkc_type ty = TypeOf<T>::v;
+    add(t, "div_const_" + tname(ty), {InSpec{IN_EITHER, ty}, InSpec{IN_SCALAR, ty}}, ty, run_div_const<T>);
+}
+
+// register_casts (:858-871): one source type to every numeric array type.
+template <class S> static void reg_casts_from(std::vector<KernelDef> &t, vkc_type src) {
+    const std::string s = "cast_" + tname(src) + "_";
+    const InSpec e{IN_EITHER, src};
+    add(t, s + "f64", {e}, VKC_F64, run_un<S, double, OpCast<S, double>>);
+    add(t, s + "f32", {e}, VKC_F32, run_un<S, float, OpCast<S, float>>);
+    add(t, s + "i64", {e}, VKC_I64, run_un<S, long long, OpCast<S, long long>>);
+    add(t, s + "u64", {e}, VKC_U64, run_un<S, unsigned long long, OpCast<S, unsigned long long>>);
+    add(t, s + "i32", {e}, VKC_I32, run_un<S, int, OpCast<S, int>>);
+    add(t, s + "u8", {e}, VKC_U8, run_un<S, unsigned char, OpCast<S, unsigned char>>);
+}
+
 void register_elementwise(std::vector<KernelDef> &t) {
-    InSpec fe{IN_EITHER, VKC_F64}, ie{IN_EITHER, VKC_I64}, be{IN_EITHER, VKC_BOOL};
-    struct E { const char *name; std::vector<InSpec> in; vkc_type out; uint64_t cost; ElemFn f; };
-    const E es[] = {
-        {"add_f64", {fe, fe}, VKC_F64, 24, run_binary<double, EW_ADD>},
-        {"sub_f64", {fe, fe}, VKC_F64, 24, run_binary<double, EW_SUB>},
-        {"mul_f64", {fe, fe}, VKC_F64, 24, run_binary<double, EW_MUL>},
-        {"min_f64", {fe, fe}, VKC_F64, 24, run_binary<double, EW_MIN>},
-        {"max_f64", {fe, fe}, VKC_F64, 24, run_binary<double, EW_MAX>},
-        {"eq_f64", {fe, fe}, VKC_BOOL, 17, run_binary<double, EW_EQ>},
-        {"ne_f64", {fe, fe}, VKC_BOOL, 17, run_binary<double, EW_NE>},
-        {"lt_f64", {fe, fe}, VKC_BOOL, 17, run_binary<double, EW_LT>},
-        {"le_f64", {fe, fe}, VKC_BOOL, 17, run_binary<double, EW_LE>},
-        {"gt_f64", {fe, fe}, VKC_BOOL, 17, run_binary<double, EW_GT>},
-        {"ge_f64", {fe, fe}, VKC_BOOL, 17, run_binary<double, EW_GE>},
-        {"add_i64", {ie, ie}, VKC_I64, 24, run_binary<long long, EW_ADD>},
-        {"sub_i64", {ie, ie}, VKC_I64, 24, run_binary<long long, EW_SUB>},
-        {"mul_i64", {ie, ie}, VKC_I64, 24, run_binary<long long, EW_MUL>},
-        {"min_i64", {ie, ie}, VKC_I64, 24, run_binary<long long, EW_MIN>},
-        {"max_i64", {ie, ie}, VKC_I64, 24, run_binary<long long, EW_MAX>},
-        {"and_i64", {ie, ie}, VKC_I64, 24, run_binary<long long, EW_AND>},
-        {"or_i64", {ie, ie}, VKC_I64, 24, run_binary<long long, EW_OR>},
-        {"xor_i64", {ie, ie}, VKC_I64, 24, run_binary<long long, EW_XOR>},
-        {"eq_i64", {ie, ie}, VKC_BOOL, 17, run_binary<long long, EW_EQ>},
-        {"ne_i64", {ie, ie}, VKC_BOOL, 17, run_binary<long long, EW_NE>},
-        {"lt_i64", {ie, ie}, VKC_BOOL, 17, run_binary<long long, EW_LT>},
-        {"le_i64", {ie, ie}, VKC_BOOL, 17, run_binary<long long, EW_LE>},
-        {"gt_i64", {ie, ie}, VKC_BOOL, 17, run_binary<long long, EW_GT>},
-        {"ge_i64", {ie, ie}, VKC_BOOL, 17, run_binary<long long, EW_GE>},
-        {"and_bool", {be, be}, VKC_BOOL, 3, run_binary<unsigned char, EW_AND>},
-        {"or_bool", {be, be}, VKC_BOOL, 3, run_binary<unsigned char, EW_OR>},
-        {"eq_bool", {be, be}, VKC_BOOL, 3, run_binary<unsigned char, EW_EQ>},
-        {"ne_bool", {be, be}, VKC_BOOL, 3, run_binary<unsigned char, EW_NE>},
-        {"not_bool", {be}, VKC_BOOL, 2, run_not},
-        {"select_f64", {be, fe, fe}, VKC_F64, 25, run_select<double>},
-        {"select_i64", {be, ie, ie}, VKC_I64, 25, run_select<long long>},
-        {"select_bool", {be, be, be}, VKC_BOOL, 4, run_select<unsigned char>},
-    };
-    for (const E &e : es) {
-        KernelDef d{e.name, VKC_ELEMENTWISE, e.in, true, e.out, e.cost};
-        d.elem = e.f;
-        t.push_back(d);
-    }
+    reg_num<double>(t);
+    reg_num<float>(t);
+    reg_num<long long>(t);
+    reg_num<unsigned long long>(t);
+    reg_num<int>(t);
+    reg_num<unsigned char>(t);
+    reg_signed<double>(t);
+    reg_signed<float>(t);
+    reg_signed<long long>(t);
+    reg_signed<int>(t);
+    reg_float<double>(t);
+    reg_float<float>(t);
+    reg_div_const<long long>(t);
+    reg_div_const<unsigned long long>(t);
+    reg_div_const<int>(t);
+    reg_div_const<unsigned char>(t);
+    reg_any<double>(t, VKC_F64);
+    reg_any<float>(t, VKC_F32);
+    reg_any<long long>(t, VKC_I64);
+    reg_any<unsigned long long>(t, VKC_U64);
+    reg_any<int>(t, VKC_I32);
+    reg_any<unsigned char>(t, VKC_U8);
+    reg_any<unsigned char>(t, VKC_BOOL);
+    reg_bits<long long>(t);
+    reg_bits<unsigned long long>(t);
+    reg_bits<int>(t);
+    reg_bits<unsigned char>(t);
+    // register_bool (:815-823): on the 0/1 storage.
+    const InSpec be{IN_EITHER, VKC_BOOL};
+    add(t, "and_bool", {be, be}, VKC_BOOL, run_bin<unsigned char, unsigned char, OpAnd>);
+    add(t, "or_bool", {be, be}, VKC_BOOL, run_bin<unsigned char, unsigned char, OpOr>);
+    add(t, "xor_bool", {be, be}, VKC_BOOL, run_bin<unsigned char, unsigned char, OpXor>);
+    add(t, "not_bool", {be}, VKC_BOOL, run_un<unsigned char, unsigned char, OpBoolNot>);
+    reg_casts_from<double>(t, VKC_F64);
+    reg_casts_from<float>(t, VKC_F32);
+    reg_casts_from<long long>(t, VKC_I64);
+    reg_casts_from<unsigned long long>(t, VKC_U64);
+    reg_casts_from<int>(t, VKC_I32);
+    reg_casts_from<unsigned char>(t, VKC_U8);
+    reg_casts_from<unsigned char>(t, VKC_BOOL);
     KernelDef d{"iota", VKC_WHOLE, {InSpec{IN_SCALAR, VKC_I64}}, true, VKC_I64, 8};
     d.whole = iota;
     t.push_back(d);
