@@ -104,6 +104,15 @@ VKC_API vkc_status vkc_synchronize(vkc_ctx *ctx);
  * lowering it releases the cache at once. Several contexts on one GPU (one per stream of a
  * server) share the device, so each keeps a smaller cache. */
 VKC_API vkc_status vkc_set_cache_limit(vkc_ctx *ctx, size_t bytes);
+/* Launch shapes chosen per size class (0: n < 2^20, 1: n < 2^24, 2: larger) by the committed
+ * autotuner table (the reference fixes its tile sizes per ISA; these are this backend's):
+ * "radix_items" (rows per thread of the argsort passes: 8, 12, 16), "stream_blocks_per_sm"
+ * (count/min/max/argmin/argmax/integer sums: 2, 4, 8, 16), "gather_rows_per_thread" (1, 2, 4)
+ * and "group_first_table_log2" (group_id's first hash table, 18 .. 22). vkc_tune_set
+ * overrides one entry for this context (the autotuner measures candidates that way); results
+ * never depend on it. */
+VKC_API vkc_status vkc_tune_set(vkc_ctx *ctx, const char *knob, int size_class, int value);
+VKC_API vkc_status vkc_tune_get(const vkc_ctx *ctx, const char *knob, int size_class, int *value);
 /* Runs the context's work on `stream` (a cudaStream_t) instead of its own stream. */
 VKC_API vkc_status vkc_set_stream(vkc_ctx *ctx, void *stream);
 VKC_API void *vkc_get_stream(const vkc_ctx *ctx);

@@ -56,6 +56,8 @@ _SIGNATURES = {
     "vkc_last_error": (ctypes.c_char_p, [_P]),
     "vkc_synchronize": (ctypes.c_int, [_P]),
     "vkc_set_cache_limit": (ctypes.c_int, [_P, ctypes.c_size_t]),
+    "vkc_tune_set": (ctypes.c_int, [_P, ctypes.c_char_p, ctypes.c_int, ctypes.c_int]),
+    "vkc_tune_get": (ctypes.c_int, [_P, ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]),
     "vkc_set_stream": (ctypes.c_int, [_P, _P]),
     "vkc_get_stream": (_P, [_P]),
     "vkc_launch_count": (ctypes.c_uint64, [_P]),
@@ -353,6 +355,15 @@ class Context:
 
     def set_cache_limit(self, nbytes):
         self._check(_lib.vkc_set_cache_limit(self.handle, int(nbytes)))
+
+    def tune_set(self, knob, size_class, value):
+        """Overrides one entry of the autotuner table for this context (vkc_tune_set)."""
+        self._check(_lib.vkc_tune_set(self.handle, knob.encode(), int(size_class), int(value)))
+
+    def tune_get(self, knob, size_class):
+        v = ctypes.c_int()
+        self._check(_lib.vkc_tune_get(self.handle, knob.encode(), int(size_class), ctypes.byref(v)))
+        return v.value
 
     def launch_count(self):
         return int(_lib.vkc_launch_count(self.handle))

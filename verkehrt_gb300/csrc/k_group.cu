@@ -13,8 +13,9 @@
 //     decoupled-lookback compaction over rows gives each first occurrence its rank, which is
 //     the group's id, stored in the slot; the same kernel writes every row's id.
 // Table size: the reference's maximum is nextpow2(2n) slots (group.rs:226-229). When that is
-// above 2^21 slots, the insert first runs on a 2^21-slot table, which stays in L2; it gives up
-// (an overflow flag) once 2^20 distinct keys or a probe of 64 slots is reached, and only then
+// above the first table's size (2^group_first_table_log2 slots from the autotuner's table,
+// 2^21 by default, which stays in L2), the insert first runs on that table; it gives up (an
+// overflow flag) once half its slots hold keys or a probe of 64 slots is reached, and only then
 // is the full table filled. Inputs with few distinct keys never touch the large table.
 #include "lookback.cuh"
 #include "reduce_common.h"
@@ -26,7 +27,6 @@ constexpr int GI_ITEMS = 16;
 constexpr int GI_TILE = GI_THREADS * GI_ITEMS;
 constexpr int GI_ROWS = 4;  // rows a thread probes at once
 constexpr unsigned long long GI_EMPTY = 0x8080808080808080ull;
-constexpr uint64_t GI_SMALL_SLOTS = uint64_t(1) << 21;
 constexpr unsigned GI_SMALL_PROBES = 64;
 
 // A slot is one 16-byte record (key, smallest row, id), or 32 bytes for key pairs (key a,
@@ -365,8 +365,9 @@ static vkc_status run_group(vkc_ctx *ctx, const vkc_array *xa, const vkc_array *
     const auto *b = xb ? static_cast<const long long *>(xb->data()) : nullptr;
     GroupTable t{};
     bool done = false;
-    if (slots > GI_SMALL_SLOTS) {
-        if ((st = new_table(ctx, GI_SMALL_SLOTS, xb != nullptr, &small, &t))) {
+    const uint64_t first_slots = uint64_t(1) << tune(ctx, TK_GROUP_FIRST_LOG2, n);
+    if (slots > first_slots) {
+        if ((st = new_table(ctx, first_slots, xb != nullptr, &small, &t))) {
             if (st == VKC_ALLOC) return alloc_fail();
             cleanup();
             vkc_array_release(o);

@@ -16,19 +16,42 @@ template <> struct GWord<8> { using T = unsigned long long; };
 template <> struct GWord<4> { using T = unsigned; };
 template <> struct GWord<1> { using T = unsigned char; };
 
-// One row per thread over a grid that covers the rows once: random reads are bound by the
-// number of DRAM sectors in flight across the whole GPU, which the largest grid maximizes
-// (measured on GB300: 50 G random 8-byte reads/s, against 44 G for grid-stride loops with
-// several loads in flight per thread).
-template <int W>
+// R rows per thread (the autotuner's gather_rows_per_thread) over a grid that covers the rows
+// once: random reads are bound by the number of DRAM sectors in flight across the whole GPU,
+// which the largest grid maximizes (measured on GB300: 50 G random 8-byte reads/s with one
+// row per thread, against 44 G for grid-stride loops). Row r of thread g is g + r * (threads
+// of the grid), so each load of the R is coalesced across the warp; all R index loads, then
+// all R source loads, are in flight together.
+template <int W, int R>
 __global__ void __launch_bounds__(256) gather_kernel(const typename GWord<W>::T *__restrict__ src, uint64_t nsrc,
                                                      const long long *__restrict__ idx, int64_t n,
                                                      typename GWord<W>::T *__restrict__ out, DevStatus *status) {
-    const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const long long k = __ldcs(idx + i);
-    if (static_cast<uint64_t>(k) < nsrc) out[i] = __ldg(src + k);
-    else atomicMin(&status->first_bad, static_cast<unsigned long long>(i));
+    const int64_t g = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    const int64_t span = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    long long k[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) k[r] = g + r * span < n ? __ldcs(idx + g + r * span) : 0;
+    typename GWord<W>::T v[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[r] = (g + r * span < n && static_cast<uint64_t>(k[r]) < nsrc) ? __ldg(src + k[r]) : 0;
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        const int64_t i = g + r * span;
+        if (i >= n) break;
+        if (static_cast<uint64_t>(k[r]) < nsrc) out[i] = v[r];
+        else atomicMin(&status->first_bad, static_cast<unsigned long long>(i));
+    }
+}
+
+template <int W>
+static void launch_gather(vkc_ctx *ctx, int rows, int64_t n, const typename GWord<W>::T *src, uint64_t nsrc,
+                          const long long *idx, typename GWord<W>::T *out) {
+    const int grid = static_cast<int>((n + 256 * rows - 1) / (256 * rows));
+    switch (rows) {
+    case 2: gather_kernel<W, 2><<<grid, 256, 0, ctx->stream>>>(src, nsrc, idx, n, out, ctx->status); break;
+    case 4: gather_kernel<W, 4><<<grid, 256, 0, ctx->stream>>>(src, nsrc, idx, n, out, ctx->status); break;
+    default: gather_kernel<W, 1><<<grid, 256, 0, ctx->stream>>>(src, nsrc, idx, n, out, ctx->status); break;
+    }
 }
 
 // Reads the value at `row` of an i64 device array.
@@ -58,12 +81,12 @@ template <vkc_type T> static vkc_status gather(vkc_ctx *ctx, const vkc_value *ar
             vkc_array_release(o);
             return fail(ctx, VKC_USAGE, "gather of more than 2^39 rows");
         }
-        const int grid = static_cast<int>(g64);
+        const int rows = tune(ctx, TK_GATHER_ROWS, n);
         const auto *idx = static_cast<const long long *>(ix->data());
         switch (type_width(T)) {
-        case 8: gather_kernel<8><<<grid, 256, 0, ctx->stream>>>(static_cast<const unsigned long long *>(xs->data()), xs->len, idx, n, static_cast<unsigned long long *>(o->data()), ctx->status); break;
-        case 4: gather_kernel<4><<<grid, 256, 0, ctx->stream>>>(static_cast<const unsigned *>(xs->data()), xs->len, idx, n, static_cast<unsigned *>(o->data()), ctx->status); break;
-        default: gather_kernel<1><<<grid, 256, 0, ctx->stream>>>(static_cast<const unsigned char *>(xs->data()), xs->len, idx, n, static_cast<unsigned char *>(o->data()), ctx->status); break;
+        case 8: launch_gather<8>(ctx, rows, n, static_cast<const unsigned long long *>(xs->data()), xs->len, idx, static_cast<unsigned long long *>(o->data())); break;
+        case 4: launch_gather<4>(ctx, rows, n, static_cast<const unsigned *>(xs->data()), xs->len, idx, static_cast<unsigned *>(o->data())); break;
+        default: launch_gather<1>(ctx, rows, n, static_cast<const unsigned char *>(xs->data()), xs->len, idx, static_cast<unsigned char *>(o->data())); break;
         }
         if ((st = launched(ctx, "gather"))) {
             vkc_array_release(o);

@@ -132,7 +132,7 @@ struct CountReducer : DevReducer {
         }
         int64_t n = args[0].len();
         if (n == 0) return VKC_OK;
-        int grid = stream_grid(ctx, n, 256, 8, cmp < 0 ? 16384 : 4096);
+        int grid = stream_grid(ctx, n, 256, tune(ctx, TK_STREAM_BLOCKS, n), cmp < 0 ? 16384 : 4096);
         void *part;
         if ((st = scratch(ctx, sizeof(unsigned long long) * grid, &part))) return st;
         auto *s = static_cast<unsigned long long *>(state);
@@ -346,7 +346,7 @@ struct ExtremeReducer : DevReducer {
         if (!rows_arg(ctx, args[0], type, &st)) return st;
         int64_t n = args[0].len();
         if (n == 0) return VKC_OK;
-        int grid = stream_grid(ctx, n, 256, 8, 4096);
+        int grid = stream_grid(ctx, n, 256, tune(ctx, TK_STREAM_BLOCKS, n), 4096);
         void *part;
         if ((st = scratch(ctx, sizeof(ExtState) * grid, &part))) return st;
         auto *p = static_cast<ExtState *>(part);
@@ -440,7 +440,7 @@ struct IntSumReducer : DevReducer {
         if (!rows_arg(ctx, args[0], VKC_I64, &st)) return st;
         int64_t n = args[0].len();
         if (n == 0) return VKC_OK;
-        int grid = stream_grid(ctx, n, 256, 8, 4096);
+        int grid = stream_grid(ctx, n, 256, tune(ctx, TK_STREAM_BLOCKS, n), 4096);
         void *part;
         if ((st = scratch(ctx, sizeof(unsigned long long) * grid, &part))) return st;
         isum_kernel<<<grid, 256, 0, ctx->stream>>>(

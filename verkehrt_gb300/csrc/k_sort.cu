@@ -6,7 +6,8 @@
 //  * one histogram kernel counts all 8 digits in one read (radix.rs:199-202);
 //  * a digit that is equal in every row leaves the order unchanged and its pass is skipped
 //    (radix.rs:203-211);
-//  * each remaining digit is one reduce-then-scan pass over 3072-row tiles: `up` counts each
+//  * each remaining digit is one reduce-then-scan pass over tiles of 256 x radix_items rows (the
+//    autotuner's table; 3072 by default): `up` counts each
 //    tile's digits into a digit-major table, one exclusive scan of that table gives every
 //    (digit, tile) its first output row, and `down` ranks the tile's rows stably by digit
 //    (a ballot per digit bit, in row order) and scatters them. The first pass reads the keys, the
@@ -21,18 +22,21 @@
 
 namespace vkc {
 
-#ifndef RS_ITEMS_PER_THREAD
-#define RS_ITEMS_PER_THREAD 12  // rows per thread in a radix pass (even: ranks are packed in pairs)
-#endif
 constexpr int RS_THREADS = 256;
 constexpr int RS_WARPS = RS_THREADS / 32;
-constexpr int RS_ITEMS = RS_ITEMS_PER_THREAD;
-static_assert(RS_ITEMS % 2 == 0, "ranks are packed two per word");
-constexpr int RS_TILE = RS_THREADS * RS_ITEMS;
 constexpr int RADIX = 256;
-#ifndef RS_DOWN_MIN_BLOCKS
-#define RS_DOWN_MIN_BLOCKS 4  // resident blocks per SM that the down kernel's registers allow
-#endif
+
+// Rows per thread of a pass (the autotuner's radix_items: 8, 12 or 16; even, as ranks are
+// packed in pairs), the tile, and the resident blocks per SM that the down kernel's registers
+// allow (the best of a sweep over 3-6 per shape).
+template <int ITEMS> struct RsShape {
+    static_assert(ITEMS % 2 == 0, "ranks are packed two per word");
+    static constexpr int TILE = RS_THREADS * ITEMS;
+    static constexpr int MIN_BLOCKS = ITEMS >= 16 ? 3 : (ITEMS >= 12 ? 4 : 5);
+    // Dynamic shared memory of the down kernel: the tile's images and positions sorted by digit.
+    static constexpr size_t DOWN_SMEM = (sizeof(unsigned long long) + sizeof(unsigned)) * TILE;
+};
+constexpr int RS_MIN_TILE = RS_THREADS * 8;
 
 __device__ __forceinline__ unsigned long long image_of(long long k) {
     return static_cast<unsigned long long>(k) ^ 0x8000000000000000ull;
@@ -59,10 +63,11 @@ __global__ void __launch_bounds__(256) rs_hist_kernel(const long long *__restric
 
 // Up: the digit counts of every tile, digit-major: counts[d * tiles + tile]. Shared-memory
 // atomics into one histogram per warp (the order of the increments does not matter here).
-template <bool FIRST>
+template <int RS_ITEMS, bool FIRST>
 __global__ void __launch_bounds__(RS_THREADS) rs_up_kernel(const long long *__restrict__ keys_in,
                                                            const unsigned long long *__restrict__ img_in, int64_t n,
                                                            int shift, int tiles, unsigned *__restrict__ counts) {
+    constexpr int RS_TILE = RsShape<RS_ITEMS>::TILE;
     __shared__ unsigned s_cnt[RS_WARPS][RADIX];
     const int tile = blockIdx.x;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -169,12 +174,13 @@ __global__ void __launch_bounds__(SCAN_THREADS) rs_scan_apply(const unsigned *__
 // Down: one pass over digit `shift` with the tile's first output row per digit in
 // offsets[d * tiles + tile]. FIRST reads the i64 keys (positions are the row numbers); LAST
 // writes only the positions, as i64.
-template <bool FIRST, bool LAST>
-__global__ void __launch_bounds__(RS_THREADS, RS_DOWN_MIN_BLOCKS) rs_down_kernel(
+template <int RS_ITEMS, bool FIRST, bool LAST>
+__global__ void __launch_bounds__(RS_THREADS, RsShape<RS_ITEMS>::MIN_BLOCKS) rs_down_kernel(
     const long long *__restrict__ keys_in, const unsigned long long *__restrict__ img_in,
     const unsigned *__restrict__ pos_in, unsigned long long *__restrict__ img_out,
     unsigned *__restrict__ pos_out, long long *__restrict__ out, int64_t n, int shift, int tiles,
     const unsigned *__restrict__ offsets) {
+    constexpr int RS_TILE = RsShape<RS_ITEMS>::TILE;
     __shared__ unsigned short s_wcnt[RS_WARPS][RADIX];  // per-warp digit counts, then offsets
     __shared__ unsigned s_tile_excl[RADIX];             // the digit's first output row
     __shared__ unsigned s_dstart[RADIX];                // the digit's first row in the sorted tile
@@ -262,8 +268,43 @@ __global__ void __launch_bounds__(RS_THREADS, RS_DOWN_MIN_BLOCKS) rs_down_kernel
     }
 }
 
-// Dynamic shared memory of rs_down_kernel: the tile's images and positions sorted by digit.
-constexpr size_t RS_DOWN_SMEM = (sizeof(unsigned long long) + sizeof(unsigned)) * RS_TILE;
+// Launches of one pass's kernels for the tuned shape.
+template <bool FIRST>
+static void launch_up(vkc_ctx *ctx, int items, int tiles, const long long *keys, const unsigned long long *img,
+                      int64_t n, int shift, unsigned *counts) {
+    switch (items) {
+    case 8: rs_up_kernel<8, FIRST><<<tiles, RS_THREADS, 0, ctx->stream>>>(keys, img, n, shift, tiles, counts); break;
+    case 16: rs_up_kernel<16, FIRST><<<tiles, RS_THREADS, 0, ctx->stream>>>(keys, img, n, shift, tiles, counts); break;
+    default: rs_up_kernel<12, FIRST><<<tiles, RS_THREADS, 0, ctx->stream>>>(keys, img, n, shift, tiles, counts); break;
+    }
+}
+
+template <int ITEMS, bool FIRST, bool LAST> static void set_down_smem() {
+    cudaFuncSetAttribute(rs_down_kernel<ITEMS, FIRST, LAST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         static_cast<int>(RsShape<ITEMS>::DOWN_SMEM));
+}
+
+template <bool FIRST, bool LAST>
+static void launch_down(vkc_ctx *ctx, int items, int tiles, const long long *keys, const unsigned long long *img_in,
+                        const unsigned *pos_in, unsigned long long *img_out, unsigned *pos_out, long long *out,
+                        int64_t n, int shift, const unsigned *offs) {
+    static const bool configured = [] {
+        set_down_smem<8, FIRST, LAST>();
+        set_down_smem<12, FIRST, LAST>();
+        set_down_smem<16, FIRST, LAST>();
+        return true;
+    }();
+    (void)configured;
+#define RS_DOWN(I)                                                                                             \
+    rs_down_kernel<I, FIRST, LAST><<<tiles, RS_THREADS, RsShape<I>::DOWN_SMEM, ctx->stream>>>(                \
+        keys, img_in, pos_in, img_out, pos_out, out, n, shift, tiles, offs)
+    switch (items) {
+    case 8: RS_DOWN(8); break;
+    case 16: RS_DOWN(16); break;
+    default: RS_DOWN(12); break;
+    }
+#undef RS_DOWN
+}
 
 __global__ void rs_iota_kernel(long long *out, int64_t n) {
     int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
@@ -338,7 +379,9 @@ static vkc_status argsort_i64(vkc_ctx *ctx, const vkc_value *args, int nargs, vk
         }
     }
     // Digit-major tile counts, their exclusive scan, and the scan's block sums.
-    const int tiles = static_cast<int>((n + RS_TILE - 1) / RS_TILE);
+    const int items = tune(ctx, TK_RADIX_ITEMS, n);
+    const int64_t tile_rows = static_cast<int64_t>(RS_THREADS) * items;
+    const int tiles = static_cast<int>((n + tile_rows - 1) / tile_rows);
     const int64_t m = static_cast<int64_t>(RADIX) * tiles;
     const int chunks = static_cast<int>((m + SCAN_CHUNK - 1) / SCAN_CHUNK);
     if ((st = new_array(ctx, VKC_I32, m, false, &ca)) || (st = new_array(ctx, VKC_I32, m, false, &oa)) ||
@@ -354,31 +397,23 @@ static vkc_status argsort_i64(vkc_ctx *ctx, const vkc_value *args, int nargs, vk
     unsigned *pos[2] = {pa ? static_cast<unsigned *>(pa->data()) : nullptr,
                         pb ? static_cast<unsigned *>(pb->data()) : nullptr};
     int cur = 0;
-    static const bool configured = [] {
-        cudaFuncSetAttribute(rs_down_kernel<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(RS_DOWN_SMEM));
-        cudaFuncSetAttribute(rs_down_kernel<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(RS_DOWN_SMEM));
-        cudaFuncSetAttribute(rs_down_kernel<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(RS_DOWN_SMEM));
-        cudaFuncSetAttribute(rs_down_kernel<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(RS_DOWN_SMEM));
-        return true;
-    }();
-    (void)configured;
     for (int a = 0; a < passes; ++a) {
         bool fst = a == 0, lst = a == passes - 1;
         int shift = 8 * active[a];
         int src = cur, dst = passes > 2 ? 1 - cur : 0;
-        if (fst) rs_up_kernel<true><<<tiles, RS_THREADS, 0, ctx->stream>>>(keys, nullptr, n, shift, tiles, counts);
-        else rs_up_kernel<false><<<tiles, RS_THREADS, 0, ctx->stream>>>(nullptr, img[src], n, shift, tiles, counts);
+        if (fst) launch_up<true>(ctx, items, tiles, keys, nullptr, n, shift, counts);
+        else launch_up<false>(ctx, items, tiles, nullptr, img[src], n, shift, counts);
         rs_scan_sums<<<chunks, SCAN_THREADS, 0, ctx->stream>>>(counts, m, sums);
         rs_scan_top<<<1, 1024, 0, ctx->stream>>>(sums, chunks);
         rs_scan_apply<<<chunks, SCAN_THREADS, 0, ctx->stream>>>(counts, m, sums, offs);
         if (fst && lst)
-            rs_down_kernel<true, true><<<tiles, RS_THREADS, RS_DOWN_SMEM, ctx->stream>>>(keys, nullptr, nullptr, nullptr, nullptr, oo, n, shift, tiles, offs);
+            launch_down<true, true>(ctx, items, tiles, keys, nullptr, nullptr, nullptr, nullptr, oo, n, shift, offs);
         else if (fst)
-            rs_down_kernel<true, false><<<tiles, RS_THREADS, RS_DOWN_SMEM, ctx->stream>>>(keys, nullptr, nullptr, img[0], pos[0], nullptr, n, shift, tiles, offs);
+            launch_down<true, false>(ctx, items, tiles, keys, nullptr, nullptr, img[0], pos[0], nullptr, n, shift, offs);
         else if (lst)
-            rs_down_kernel<false, true><<<tiles, RS_THREADS, RS_DOWN_SMEM, ctx->stream>>>(nullptr, img[src], pos[src], nullptr, nullptr, oo, n, shift, tiles, offs);
+            launch_down<false, true>(ctx, items, tiles, nullptr, img[src], pos[src], nullptr, nullptr, oo, n, shift, offs);
         else
-            rs_down_kernel<false, false><<<tiles, RS_THREADS, RS_DOWN_SMEM, ctx->stream>>>(nullptr, img[src], pos[src], img[dst], pos[dst], nullptr, n, shift, tiles, offs);
+            launch_down<false, false>(ctx, items, tiles, nullptr, img[src], pos[src], img[dst], pos[dst], nullptr, n, shift, offs);
         if ((st = launched(ctx, "rs_pass"))) {
             cleanup();
             return release(st);
@@ -397,29 +432,25 @@ static vkc_status argsort_i64(vkc_ctx *ctx, const vkc_value *args, int nargs, vk
 
 // Stable LSD passes over (image, position) pairs that are already in img[0] / pos[0], one per
 // entry of `shifts`, ping-ponging between the two buffers; *which gets the buffer that holds
-// the result. counts and offs hold RADIX * ceil(n / RS_TILE) words and sums
+// the result. counts and offs hold radix_pairs_scratch's words and sums
 // ceil(that / SCAN_CHUNK). Enqueue only: no host synchronisation and no allocation.
 vkc_status radix_pairs(vkc_ctx *ctx, unsigned long long *img[2], unsigned *pos[2], int64_t n, const int *shifts,
                        int npasses, unsigned *counts, unsigned *offs, unsigned *sums, int *which) {
     vkc_status st;
-    const int tiles = static_cast<int>((n + RS_TILE - 1) / RS_TILE);
+    const int items = tune(ctx, TK_RADIX_ITEMS, n);
+    const int64_t tile_rows = static_cast<int64_t>(RS_THREADS) * items;
+    const int tiles = static_cast<int>((n + tile_rows - 1) / tile_rows);
     const int64_t m = static_cast<int64_t>(RADIX) * tiles;
     const int chunks = static_cast<int>((m + SCAN_CHUNK - 1) / SCAN_CHUNK);
-    static const bool configured = [] {
-        cudaFuncSetAttribute(rs_down_kernel<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             static_cast<int>(RS_DOWN_SMEM));
-        return true;
-    }();
-    (void)configured;
     int cur = 0;
     for (int a = 0; a < npasses; ++a) {
         const int shift = shifts[a];
-        rs_up_kernel<false><<<tiles, RS_THREADS, 0, ctx->stream>>>(nullptr, img[cur], n, shift, tiles, counts);
+        launch_up<false>(ctx, items, tiles, nullptr, img[cur], n, shift, counts);
         rs_scan_sums<<<chunks, SCAN_THREADS, 0, ctx->stream>>>(counts, m, sums);
         rs_scan_top<<<1, 1024, 0, ctx->stream>>>(sums, chunks);
         rs_scan_apply<<<chunks, SCAN_THREADS, 0, ctx->stream>>>(counts, m, sums, offs);
-        rs_down_kernel<false, false><<<tiles, RS_THREADS, RS_DOWN_SMEM, ctx->stream>>>(
-            nullptr, img[cur], pos[cur], img[1 - cur], pos[1 - cur], nullptr, n, shift, tiles, offs);
+        launch_down<false, false>(ctx, items, tiles, nullptr, img[cur], pos[cur], img[1 - cur], pos[1 - cur], nullptr, n,
+                                  shift, offs);
         if ((st = launched(ctx, "radix_pairs"))) return st;
         cur = 1 - cur;
     }
@@ -427,9 +458,10 @@ vkc_status radix_pairs(vkc_ctx *ctx, unsigned long long *img[2], unsigned *pos[2
     return VKC_OK;
 }
 
-// Words of the radix_pairs scratch for n rows: counts/offs each, and sums.
+// Words of the radix_pairs scratch for n rows: counts/offs each, and sums (for the smallest
+// tile, so any tuned shape fits).
 void radix_pairs_scratch(int64_t n, int64_t *count_words, int64_t *sum_words) {
-    const int64_t tiles = (n + RS_TILE - 1) / RS_TILE;
+    const int64_t tiles = (n + RS_MIN_TILE - 1) / RS_MIN_TILE;
     *count_words = static_cast<int64_t>(RADIX) * tiles;
     *sum_words = (*count_words + SCAN_CHUNK - 1) / SCAN_CHUNK;
 }

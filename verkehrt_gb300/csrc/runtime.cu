@@ -480,6 +480,28 @@ vkc_status vkc_set_cache_limit(vkc_ctx *ctx, size_t bytes) {
     return VKC_OK;
 }
 
+vkc_status vkc_tune_set(vkc_ctx *ctx, const char *knob, int size_class, int value) {
+    if (!ctx || !knob || size_class < 0 || size_class >= TUNE_CLASSES) return VKC_USAGE;
+    for (int k = 0; k < TK_COUNT; ++k) {
+        if (std::string(knob) != tune_knob_name(k)) continue;
+        if (!tune_allowed(k, value))
+            return fail(ctx, VKC_USAGE, std::string("value ") + std::to_string(value) + " not allowed for " + knob);
+        ctx->tuning.v[k][size_class] = value;
+        return VKC_OK;
+    }
+    return fail(ctx, VKC_USAGE, std::string("no tuning knob ") + knob);
+}
+
+vkc_status vkc_tune_get(const vkc_ctx *ctx, const char *knob, int size_class, int *value) {
+    if (!ctx || !knob || !value || size_class < 0 || size_class >= TUNE_CLASSES) return VKC_USAGE;
+    for (int k = 0; k < TK_COUNT; ++k)
+        if (std::string(knob) == tune_knob_name(k)) {
+            *value = ctx->tuning.v[k][size_class];
+            return VKC_OK;
+        }
+    return VKC_USAGE;
+}
+
 vkc_status vkc_synchronize(vkc_ctx *ctx) {
     VKC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return VKC_OK;

@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "../../include/vkcuda.h"
+#include "tuning.h"
 
 namespace vkc {
 
@@ -135,11 +136,16 @@ struct vkc_ctx {
     // Pinned host staging for small results.
     void *pinned = nullptr;
     size_t pinned_bytes = 0;
+    // Launch shapes per size class: the committed autotuner table, or overrides.
+    vkc::Tuning tuning = vkc::tune_defaults();
 };
 
 namespace vkc {
 
 constexpr int kCounterSlots = 64;
+
+// The tuned value of knob k for a call over n rows.
+inline int tune(const vkc_ctx *ctx, TuneKnob k, int64_t n) { return ctx->tuning.v[k][tune_class(n)]; }
 
 // Status helpers. `fail` records the message and returns the status.
 vkc_status fail(vkc_ctx *ctx, vkc_status st, const std::string &msg);
