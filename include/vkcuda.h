@@ -79,13 +79,15 @@ typedef struct {
     uint64_t bits;
 } vkc_scalar;
 
-/* A value, src/value.rs:640 (Value) and :464 (Arg): an array handle or a scalar. Arg::Rows is
- * kind VKC_VALUE_ARRAY, Arg::Splat is VKC_VALUE_SCALAR. */
-typedef enum { VKC_VALUE_ARRAY = 0, VKC_VALUE_SCALAR = 1 } vkc_value_kind;
+/* A value, src/value.rs:640 (Value) and :464 (Arg): an array handle, a scalar, or a string
+ * (Value::Str, the path argument of load_T). Arg::Rows is kind VKC_VALUE_ARRAY, Arg::Splat is
+ * VKC_VALUE_SCALAR; `str` is only read for VKC_VALUE_STR (a NUL-terminated UTF-8 path). */
+typedef enum { VKC_VALUE_ARRAY = 0, VKC_VALUE_SCALAR = 1, VKC_VALUE_STR = 2 } vkc_value_kind;
 typedef struct {
     vkc_value_kind kind;
     vkc_array *array;
     vkc_scalar scalar;
+    const char *str;
 } vkc_value;
 
 /* ------------------------------------------------------------------ context */
@@ -250,6 +252,17 @@ VKC_API vkc_status vkc_batch_dot_f64(vkc_ctx *ctx, vkc_batch *xs, vkc_batch *ys,
  * give key_digits when capturing. */
 VKC_API vkc_status vkc_batch_argsort_i64(vkc_ctx *ctx, vkc_batch *keys, const vkc_batch *outs,
                                          unsigned key_digits);
+
+/* Ingestion of the acceptance column files (src/columns.rs load_words, load_single_bytes): the
+ * file is streamed through pinned buffers into a new device array. Words are 8-byte
+ * little-endian rows read as `type` (VKC_I64 or VKC_U64), with bit 63 flipped when
+ * `flip_sign` (the columns the loader lists as signed); the bytes form reads `column`.ends and
+ * .bytes paths and checks that row i ends at byte i + 1. Errors are the reference's texts.
+ * load_T itself is the whole kernel load_<type> (construct.rs:78-97) through vkc_call. */
+VKC_API vkc_status vkc_load_column_words(vkc_ctx *ctx, const char *path, vkc_type type, int flip_sign,
+                                         vkc_array **out);
+VKC_API vkc_status vkc_load_column_bytes(vkc_ctx *ctx, const char *ends_path, const char *bytes_path,
+                                         const char *column, vkc_array **out);
 
 /* A CUDA graph of the work the library enqueues on ctx's stream between vkc_graph_begin and
  * vkc_graph_end (stream capture; only enqueue-only entries, such as the batch entries above,

@@ -45,7 +45,8 @@ class _Scalar(ctypes.Structure):
 
 
 class _Value(ctypes.Structure):
-    _fields_ = [("kind", ctypes.c_int), ("array", ctypes.c_void_p), ("scalar", _Scalar)]
+    _fields_ = [("kind", ctypes.c_int), ("array", ctypes.c_void_p), ("scalar", _Scalar),
+                ("str", ctypes.c_char_p)]
 
 
 # Every entry point of include/vkcuda.h with its ctypes signature.
@@ -57,6 +58,8 @@ _SIGNATURES = {
     "vkc_synchronize": (ctypes.c_int, [_P]),
     "vkc_set_cache_limit": (ctypes.c_int, [_P, ctypes.c_size_t]),
     "vkc_tune_set": (ctypes.c_int, [_P, ctypes.c_char_p, ctypes.c_int, ctypes.c_int]),
+    "vkc_load_column_words": (ctypes.c_int, [_P, ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.POINTER(_P)]),
+    "vkc_load_column_bytes": (ctypes.c_int, [_P, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(_P)]),
     "vkc_tune_get": (ctypes.c_int, [_P, ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]),
     "vkc_set_stream": (ctypes.c_int, [_P, _P]),
     "vkc_get_stream": (_P, [_P]),
@@ -302,7 +305,10 @@ class Context:
     def _values(self, args):
         vals = (_Value * max(1, len(args)))()
         for i, a in enumerate(args):
-            if isinstance(a, Array):
+            if isinstance(a, (str, os.PathLike)):
+                vals[i].kind = 2  # Value::Str: a path argument (load_T)
+                vals[i].str = os.fsencode(a)
+            elif isinstance(a, Array):
                 vals[i].kind = 0
                 vals[i].array = a.handle
             else:
@@ -355,6 +361,20 @@ class Context:
 
     def set_cache_limit(self, nbytes):
         self._check(_lib.vkc_set_cache_limit(self.handle, int(nbytes)))
+
+    def load_column_words(self, path, type_name, flip_sign=False):
+        """src/columns.rs load_words: a .u64/.ends file as i64 or u64 rows on the device."""
+        h = _P()
+        self._check(_lib.vkc_load_column_words(self.handle, os.fsencode(path), TYPES[type_name], int(flip_sign),
+                                               ctypes.byref(h)))
+        return Array(self, h.value)
+
+    def load_column_bytes(self, ends_path, bytes_path, column):
+        """src/columns.rs load_single_bytes: a one-byte-per-row string column as u8 rows."""
+        h = _P()
+        self._check(_lib.vkc_load_column_bytes(self.handle, os.fsencode(ends_path), os.fsencode(bytes_path),
+                                               column.encode(), ctypes.byref(h)))
+        return Array(self, h.value)
 
     def tune_set(self, knob, size_class, value):
         """Overrides one entry of the autotuner table for this context (vkc_tune_set)."""

@@ -21,7 +21,7 @@ struct Arg {
 };
 
 // InputSpec, src/kernels.rs:304-329.
-enum InKind { IN_ARRAY, IN_SCALAR, IN_EITHER };
+enum InKind { IN_ARRAY, IN_SCALAR, IN_EITHER, IN_STR };
 struct InSpec {
     InKind kind;
     vkc_type type;
@@ -78,6 +78,7 @@ void register_scan(std::vector<KernelDef> &t);
 void register_index(std::vector<KernelDef> &t);
 void register_sort(std::vector<KernelDef> &t);
 void register_group(std::vector<KernelDef> &t);
+void register_io(std::vector<KernelDef> &t);
 void register_elementwise(std::vector<KernelDef> &t);
 
 // Argument helpers with the reference's messages (src/kernels/scalar/elementwise.rs:172-199).

@@ -241,6 +241,7 @@ std::string value_type_name(const Arg &a) {
 }
 
 std::string value_type_name(const vkc_value &v) {
+    if (v.kind == VKC_VALUE_STR) return "str";
     return v.kind == VKC_VALUE_ARRAY ? std::string(type_name(v.array->type)) + "[]"
                                      : std::string(type_name(v.scalar.type));
 }
@@ -288,6 +289,7 @@ static const std::vector<KernelDef> &table() {
         register_sort(v);
         register_group(v);
         register_elementwise(v);
+        register_io(v);
         return v;
     }();
     return t;
@@ -302,6 +304,7 @@ static const KernelDef *def_of(int id) {
 // kind_error, src/kernels/dispatch.rs:324-330.
 static std::string kind_error(const InSpec &spec, const std::string &got) {
     switch (spec.kind) {
+    case IN_STR: return "expected str, got " + got;
     case IN_ARRAY: return std::string("expected ") + type_name(spec.type) + "[], got " + got;
     case IN_SCALAR: return std::string("expected ") + type_name(spec.type) + ", got " + got;
     default:
@@ -311,6 +314,7 @@ static std::string kind_error(const InSpec &spec, const std::string &got) {
 }
 
 static bool spec_accepts(const InSpec &spec, const vkc_value &v) {
+    if (v.kind == VKC_VALUE_STR || spec.kind == IN_STR) return v.kind == VKC_VALUE_STR && spec.kind == IN_STR;
     bool arr = v.kind == VKC_VALUE_ARRAY;
     vkc_type t = arr ? v.array->type : v.scalar.type;
     if (t != spec.type) return false;
@@ -459,6 +463,9 @@ void vkc_close(vkc_ctx *ctx) {
     if (ctx->status) cudaFree(ctx->status);
     if (ctx->pinned) cudaFreeHost(ctx->pinned);
     if (ctx->status_host) cudaFreeHost(ctx->status_host);
+    if (ctx->io_buf) cudaFreeHost(ctx->io_buf);
+    for (cudaEvent_t e : ctx->io_ev)
+        if (e) cudaEventDestroy(e);
     cudaEventDestroy(ctx->ev_start);
     cudaEventDestroy(ctx->ev_stop);
     // The stream goes with the last allocation that still refers to it.

@@ -136,6 +136,9 @@ struct vkc_ctx {
     // Pinned host staging for small results.
     void *pinned = nullptr;
     size_t pinned_bytes = 0;
+    // Pinned chunk buffers of file ingestion (two of 32 MiB) and their copy events.
+    void *io_buf = nullptr;
+    cudaEvent_t io_ev[2] = {nullptr, nullptr};
     // Launch shapes per size class: the committed autotuner table, or overrides.
     vkc::Tuning tuning = vkc::tune_defaults();
 };
