@@ -398,22 +398,79 @@ __global__ void __launch_bounds__(CT_THREADS, 4) canon_tf_kernel(RowArgs args, i
     unsigned long long v[CT_SEG_BLOCKS][2];
     load_tile<OP, ALIGNED>(args, nb, tile, lp, seg, v);
     __syncthreads();
+    TF fv[2][2];
+    int okv = 0;  // bit 2h + c: the segment takes the integer step for lane 2lp+h, candidate c
+    bool plain = true;
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
         const int L = 2 * lp + h;
+#pragma unroll
         for (int c = 0; c < 2; ++c) {
-            int E = s_E[L][c];
+            const int E = s_E[L][c];
             TF f{0, 0};
-            bool ok = E != NO_E && seg_tf(v, h, 1023 + E, &f);
-            s_tf[c][seg][L] = f;
-            s_ok[c][seg][L] = ok;
+            const bool ok = E != NO_E && seg_tf(v, h, 1023 + E, &f);
+            plain = plain && f.d0 == f.d1;
+            fv[h][c] = f;
+            okv |= static_cast<int>(ok) << (2 * h + c);
         }
     }
+    static_assert(CT_SEGS == 32 && CT_THREADS == 256, "four segments per warp, eight warps");
+    const int sl = t & 31, wp = t >> 5;
+    if (__syncthreads_and(plain)) {
+        // No segment has a halfway row: every transfer function adds one increment whatever
+        // the parity, so composing them is a saturated sum (the terms are below 2^57, their
+        // sum below 2^62). The warp's four segments combine by shuffles (lanes 8 and 16 apart
+        // hold the same lanes), the eight warps' partials through shared memory.
+        unsigned long long d[2][2];
+#pragma unroll
+        for (int h = 0; h < 2; ++h)
+#pragma unroll
+            for (int c = 0; c < 2; ++c) {
+                d[h][c] = fv[h][c].d0;
+                d[h][c] += __shfl_xor_sync(FULL, d[h][c], 8);
+                d[h][c] += __shfl_xor_sync(FULL, d[h][c], 16);
+            }
+        okv &= __shfl_xor_sync(FULL, okv, 8);
+        okv &= __shfl_xor_sync(FULL, okv, 16);
+        unsigned long long(*s_part)[32] = reinterpret_cast<unsigned long long(*)[32]>(&s_tf[0][0][0]);  // [warp][c*16 + L]
+        unsigned char(*s_pok)[32] = reinterpret_cast<unsigned char(*)[32]>(&s_ok[0][0][0]);
+        if (sl < 8) {
+#pragma unroll
+            for (int h = 0; h < 2; ++h)
+#pragma unroll
+                for (int c = 0; c < 2; ++c) {
+                    s_part[wp][c * 16 + 2 * lp + h] = d[h][c];
+                    s_pok[wp][c * 16 + 2 * lp + h] = static_cast<unsigned char>((okv >> (2 * h + c)) & 1);
+                }
+        }
+        __syncthreads();
+        if (t < 32) {
+            const int c = t >> 4, L = t & 15;
+            unsigned long long sum = 0;
+            int ok = 1;
+#pragma unroll
+            for (int w = 0; w < CT_THREADS / 32; ++w) {
+                sum += s_part[w][t];
+                ok &= s_pok[w][t];
+            }
+            const int E = s_E[L][c];
+            const int64_t at = (static_cast<int64_t>(L) * T + tile) * 2 + c;
+            wk.recE[at] = (E != NO_E && ok) ? E : NO_E;
+            sum = sum > SAT ? SAT : sum;
+            wk.recD[at] = TF{sum, sum};
+        }
+        return;
+    }
+#pragma unroll
+    for (int h = 0; h < 2; ++h)
+#pragma unroll
+        for (int c = 0; c < 2; ++c) {
+            s_tf[c][seg][2 * lp + h] = fv[h][c];
+            s_ok[c][seg][2 * lp + h] = static_cast<unsigned char>((okv >> (2 * h + c)) & 1);
+        }
     __syncthreads();
     // The 32 (lane, candidate) pairs, four per warp: lane s of the warp holds segment s, and an
     // ordered scan (earlier segments on the left) composes them.
-    static_assert(CT_SEGS == 32 && CT_THREADS == 256, "one warp lane per segment, four pairs per warp");
-    const int sl = t & 31, wp = t >> 5;
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
         const int pair = wp * 4 + q, L = pair >> 1, c = pair & 1;
