@@ -51,7 +51,7 @@ def measured_peaks():
 
 def committed_traffic():
     """Per-launch DRAM bytes of the dominant kernels from the committed ncu captures."""
-    path = os.path.join(ROOT, "profiles", "traffic.json")
+    path = os.path.join(ROOT, "profiles", "dram_traffic_sweep_n2p28.json")
     if os.path.exists(path):
         with open(path) as f:
             return json.load(f)
