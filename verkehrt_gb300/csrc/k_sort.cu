@@ -63,9 +63,9 @@ __global__ void __launch_bounds__(256) rs_hist_kernel(const long long *__restric
 
 // Up: the digit counts of every tile, digit-major: counts[d * tiles + tile]. Shared-memory
 // atomics into one histogram per warp (the order of the increments does not matter here).
-template <int RS_ITEMS, bool FIRST>
+template <int RS_ITEMS, bool FIRST, class IMG>
 __global__ void __launch_bounds__(RS_THREADS) rs_up_kernel(const long long *__restrict__ keys_in,
-                                                           const unsigned long long *__restrict__ img_in, int64_t n,
+                                                           const IMG *__restrict__ img_in, int64_t n,
                                                            int shift, int tiles, unsigned *__restrict__ counts) {
     constexpr int RS_TILE = RsShape<RS_ITEMS>::TILE;
     __shared__ unsigned s_cnt[RS_WARPS][RADIX];
@@ -75,11 +75,11 @@ __global__ void __launch_bounds__(RS_THREADS) rs_up_kernel(const long long *__re
     __syncthreads();
     const int64_t base = static_cast<int64_t>(tile) * RS_TILE + static_cast<int64_t>(w) * (32 * RS_ITEMS);
     if (base + 32 * RS_ITEMS <= n) {
-        unsigned long long img[RS_ITEMS];
+        IMG img[RS_ITEMS];
 #pragma unroll
         for (int j = 0; j < RS_ITEMS; ++j) {
             const int64_t r = base + j * 32 + lane;
-            img[j] = FIRST ? image_of(__ldcs(keys_in + r)) : __ldcs(img_in + r);
+            img[j] = FIRST ? static_cast<IMG>(image_of(__ldcs(keys_in + r))) : __ldcs(img_in + r);
         }
 #pragma unroll
         for (int j = 0; j < RS_ITEMS; ++j) atomicAdd(&s_cnt[w][static_cast<unsigned>(img[j] >> shift) & 0xffu], 1u);
@@ -87,7 +87,7 @@ __global__ void __launch_bounds__(RS_THREADS) rs_up_kernel(const long long *__re
         for (int j = 0; j < RS_ITEMS; ++j) {
             const int64_t r = base + j * 32 + lane;
             if (r < n) {
-                const unsigned long long im = FIRST ? image_of(__ldcs(keys_in + r)) : __ldcs(img_in + r);
+                const IMG im = FIRST ? static_cast<IMG>(image_of(__ldcs(keys_in + r))) : __ldcs(img_in + r);
                 atomicAdd(&s_cnt[w][static_cast<unsigned>(im >> shift) & 0xffu], 1u);
             }
         }
@@ -173,11 +173,12 @@ __global__ void __launch_bounds__(SCAN_THREADS) rs_scan_apply(const unsigned *__
 
 // Down: one pass over digit `shift` with the tile's first output row per digit in
 // offsets[d * tiles + tile]. FIRST reads the i64 keys (positions are the row numbers); LAST
-// writes only the positions, as i64.
-template <int RS_ITEMS, bool FIRST, bool LAST>
+// writes only the positions, as i64. IMG is the key image carried between passes: 64 bits, or
+// its low 32 bits when every active digit lies there.
+template <int RS_ITEMS, bool FIRST, bool LAST, class IMG>
 __global__ void __launch_bounds__(RS_THREADS, RsShape<RS_ITEMS>::MIN_BLOCKS) rs_down_kernel(
-    const long long *__restrict__ keys_in, const unsigned long long *__restrict__ img_in,
-    const unsigned *__restrict__ pos_in, unsigned long long *__restrict__ img_out,
+    const long long *__restrict__ keys_in, const IMG *__restrict__ img_in,
+    const unsigned *__restrict__ pos_in, IMG *__restrict__ img_out,
     unsigned *__restrict__ pos_out, long long *__restrict__ out, int64_t n, int shift, int tiles,
     const unsigned *__restrict__ offsets) {
     constexpr int RS_TILE = RsShape<RS_ITEMS>::TILE;
@@ -193,7 +194,7 @@ __global__ void __launch_bounds__(RS_THREADS, RsShape<RS_ITEMS>::MIN_BLOCKS) rs_
 
     // Rows of this warp: warp-striped, row = base + j*32 + lane, so (j, lane) is row order.
     const int64_t base = static_cast<int64_t>(tile) * RS_TILE + static_cast<int64_t>(w) * (32 * RS_ITEMS);
-    unsigned long long img[RS_ITEMS];
+    IMG img[RS_ITEMS];
     unsigned pos[RS_ITEMS];
     unsigned rank2[RS_ITEMS / 2];  // two 16-bit ranks per word
     const unsigned lt = (1u << lane) - 1;
@@ -202,10 +203,10 @@ __global__ void __launch_bounds__(RS_THREADS, RsShape<RS_ITEMS>::MIN_BLOCKS) rs_
         const int64_t r = base + j * 32 + lane;
         const bool in = r < n;
         if (FIRST) {
-            img[j] = in ? image_of(__ldcs(keys_in + r)) : ~0ull;
+            img[j] = in ? static_cast<IMG>(image_of(__ldcs(keys_in + r))) : static_cast<IMG>(~0ull);
             pos[j] = 0u;  // the row number, recomputed when stored
         } else {
-            img[j] = in ? __ldcs(img_in + r) : ~0ull;
+            img[j] = in ? __ldcs(img_in + r) : static_cast<IMG>(~0ull);
             pos[j] = in ? __ldcs(pos_in + r) : 0u;
         }
     }
@@ -242,8 +243,8 @@ __global__ void __launch_bounds__(RS_THREADS, RsShape<RS_ITEMS>::MIN_BLOCKS) rs_
     __syncthreads();
     // The tile sorted by digit (stable) in shared memory, then written out with consecutive
     // threads on consecutive rows of each digit's run, so the stores coalesce.
-    unsigned long long *s_img = reinterpret_cast<unsigned long long *>(rs_smem);
-    unsigned *s_pos = reinterpret_cast<unsigned *>(rs_smem + sizeof(unsigned long long) * RS_TILE);
+    IMG *s_img = reinterpret_cast<IMG *>(rs_smem);
+    unsigned *s_pos = reinterpret_cast<unsigned *>(rs_smem + sizeof(IMG) * RS_TILE);
 #pragma unroll
     for (int j = 0; j < RS_ITEMS; ++j) {
         if (base + j * 32 + lane < n) {
@@ -256,7 +257,7 @@ __global__ void __launch_bounds__(RS_THREADS, RsShape<RS_ITEMS>::MIN_BLOCKS) rs_
     __syncthreads();
     const int rows = static_cast<int>(n - static_cast<int64_t>(tile) * RS_TILE < RS_TILE ? n - static_cast<int64_t>(tile) * RS_TILE : RS_TILE);
     for (int l = threadIdx.x; l < rows; l += RS_THREADS) {
-        const unsigned long long im = s_img[l];
+        const IMG im = s_img[l];
         const unsigned d = static_cast<unsigned>(im >> shift) & 0xffu;
         const unsigned dst = s_tile_excl[d] + (static_cast<unsigned>(l) - s_dstart[d]);
         if (LAST) {
@@ -269,35 +270,35 @@ __global__ void __launch_bounds__(RS_THREADS, RsShape<RS_ITEMS>::MIN_BLOCKS) rs_
 }
 
 // Launches of one pass's kernels for the tuned shape.
-template <bool FIRST>
-static void launch_up(vkc_ctx *ctx, int items, int tiles, const long long *keys, const unsigned long long *img,
-                      int64_t n, int shift, unsigned *counts) {
+template <bool FIRST, class IMG>
+static void launch_up(vkc_ctx *ctx, int items, int tiles, const long long *keys, const IMG *img, int64_t n, int shift,
+                      unsigned *counts) {
     switch (items) {
-    case 8: rs_up_kernel<8, FIRST><<<tiles, RS_THREADS, 0, ctx->stream>>>(keys, img, n, shift, tiles, counts); break;
-    case 16: rs_up_kernel<16, FIRST><<<tiles, RS_THREADS, 0, ctx->stream>>>(keys, img, n, shift, tiles, counts); break;
-    default: rs_up_kernel<12, FIRST><<<tiles, RS_THREADS, 0, ctx->stream>>>(keys, img, n, shift, tiles, counts); break;
+    case 8: rs_up_kernel<8, FIRST, IMG><<<tiles, RS_THREADS, 0, ctx->stream>>>(keys, img, n, shift, tiles, counts); break;
+    case 16: rs_up_kernel<16, FIRST, IMG><<<tiles, RS_THREADS, 0, ctx->stream>>>(keys, img, n, shift, tiles, counts); break;
+    default: rs_up_kernel<12, FIRST, IMG><<<tiles, RS_THREADS, 0, ctx->stream>>>(keys, img, n, shift, tiles, counts); break;
     }
 }
 
-template <int ITEMS, bool FIRST, bool LAST> static void set_down_smem() {
-    cudaFuncSetAttribute(rs_down_kernel<ITEMS, FIRST, LAST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+template <int ITEMS, bool FIRST, bool LAST, class IMG> static void set_down_smem() {
+    cudaFuncSetAttribute(rs_down_kernel<ITEMS, FIRST, LAST, IMG>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          static_cast<int>(RsShape<ITEMS>::DOWN_SMEM));
 }
 
-template <bool FIRST, bool LAST>
-static void launch_down(vkc_ctx *ctx, int items, int tiles, const long long *keys, const unsigned long long *img_in,
-                        const unsigned *pos_in, unsigned long long *img_out, unsigned *pos_out, long long *out,
-                        int64_t n, int shift, const unsigned *offs) {
+template <bool FIRST, bool LAST, class IMG>
+static void launch_down(vkc_ctx *ctx, int items, int tiles, const long long *keys, const IMG *img_in,
+                        const unsigned *pos_in, IMG *img_out, unsigned *pos_out, long long *out, int64_t n, int shift,
+                        const unsigned *offs) {
     static const bool configured = [] {
-        set_down_smem<8, FIRST, LAST>();
-        set_down_smem<12, FIRST, LAST>();
-        set_down_smem<16, FIRST, LAST>();
+        set_down_smem<8, FIRST, LAST, IMG>();
+        set_down_smem<12, FIRST, LAST, IMG>();
+        set_down_smem<16, FIRST, LAST, IMG>();
         return true;
     }();
     (void)configured;
 #define RS_DOWN(I)                                                                                             \
-    rs_down_kernel<I, FIRST, LAST><<<tiles, RS_THREADS, RsShape<I>::DOWN_SMEM, ctx->stream>>>(                \
-        keys, img_in, pos_in, img_out, pos_out, out, n, shift, tiles, offs)
+    rs_down_kernel<I, FIRST, LAST, IMG><<<tiles, RS_THREADS, (sizeof(IMG) + sizeof(unsigned)) * RsShape<I>::TILE, \
+                                          ctx->stream>>>(keys, img_in, pos_in, img_out, pos_out, out, n, shift, tiles, offs)
     switch (items) {
     case 8: RS_DOWN(8); break;
     case 16: RS_DOWN(16); break;
@@ -309,6 +310,39 @@ static void launch_down(vkc_ctx *ctx, int items, int tiles, const long long *key
 __global__ void rs_iota_kernel(long long *out, int64_t n) {
     int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
     for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride) out[i] = i;
+}
+
+// The active-digit passes of argsort over (image, position) ping-pong buffers of image type IMG.
+template <class IMG>
+static vkc_status radix_argsort_passes(vkc_ctx *ctx, int items, int tiles, int64_t m, int chunks, const long long *keys,
+                                       void *const img_v[2], unsigned *const pos[2], unsigned *counts, unsigned *offs,
+                                       unsigned *sums, long long *oo, int64_t n, const int *active, int passes) {
+    IMG *img[2] = {static_cast<IMG *>(img_v[0]), static_cast<IMG *>(img_v[1])};
+    int cur = 0;
+    for (int a = 0; a < passes; ++a) {
+        const bool fst = a == 0, lst = a == passes - 1;
+        const int shift = 8 * active[a];
+        const int src = cur, dst = passes > 2 ? 1 - cur : 0;
+        if (fst) launch_up<true, IMG>(ctx, items, tiles, keys, nullptr, n, shift, counts);
+        else launch_up<false, IMG>(ctx, items, tiles, nullptr, img[src], n, shift, counts);
+        rs_scan_sums<<<chunks, SCAN_THREADS, 0, ctx->stream>>>(counts, m, sums);
+        rs_scan_top<<<1, 1024, 0, ctx->stream>>>(sums, chunks);
+        rs_scan_apply<<<chunks, SCAN_THREADS, 0, ctx->stream>>>(counts, m, sums, offs);
+        if (fst && lst)
+            launch_down<true, true, IMG>(ctx, items, tiles, keys, nullptr, nullptr, nullptr, nullptr, oo, n, shift, offs);
+        else if (fst)
+            launch_down<true, false, IMG>(ctx, items, tiles, keys, nullptr, nullptr, img[0], pos[0], nullptr, n, shift, offs);
+        else if (lst)
+            launch_down<false, true, IMG>(ctx, items, tiles, nullptr, img[src], pos[src], nullptr, nullptr, oo, n, shift, offs);
+        else
+            launch_down<false, false, IMG>(ctx, items, tiles, nullptr, img[src], pos[src], img[dst], pos[dst], nullptr, n,
+                                           shift, offs);
+        vkc_status st = launched(ctx, "rs_pass");
+        if (st) return st;
+        if (fst) cur = 0;
+        else if (!lst) cur = dst;
+    }
+    return VKC_OK;
 }
 
 // index.rs:159-173 (ArgSort::run).
@@ -368,12 +402,16 @@ static vkc_status argsort_i64(vkc_ctx *ctx, const vkc_value *args, int nargs, vk
         for (vkc_array *a : {ia, ib, pa, pb, ca, oa, sa})
             if (a) vkc_array_release(a);
     };
+    // When every active digit lies in the low 32 bits, rows with equal high halves differ only
+    // there, so the passes carry the image's low 32 bits: 16 bytes a row per pass, not 24.
+    const bool narrow = active[passes - 1] < 4;
+    const vkc_type img_type = narrow ? VKC_I32 : VKC_U64;
     if (passes > 1) {
-        if ((st = new_array(ctx, VKC_U64, n, false, &ia)) || (st = new_array(ctx, VKC_I32, n, false, &pa))) {
+        if ((st = new_array(ctx, img_type, n, false, &ia)) || (st = new_array(ctx, VKC_I32, n, false, &pa))) {
             cleanup();
             return release(fail(ctx, VKC_ALLOC, "cannot allocate argsort scratch for " + std::to_string(n) + " rows"));
         }
-        if (passes > 2 && ((st = new_array(ctx, VKC_U64, n, false, &ib)) || (st = new_array(ctx, VKC_I32, n, false, &pb)))) {
+        if (passes > 2 && ((st = new_array(ctx, img_type, n, false, &ib)) || (st = new_array(ctx, VKC_I32, n, false, &pb)))) {
             cleanup();
             return release(fail(ctx, VKC_ALLOC, "cannot allocate argsort scratch for " + std::to_string(n) + " rows"));
         }
@@ -392,34 +430,16 @@ static vkc_status argsort_i64(vkc_ctx *ctx, const vkc_value *args, int nargs, vk
     auto *counts = static_cast<unsigned *>(ca->data());
     auto *offs = static_cast<unsigned *>(oa->data());
     auto *sums = static_cast<unsigned *>(sa->data());
-    unsigned long long *img[2] = {ia ? static_cast<unsigned long long *>(ia->data()) : nullptr,
-                                  ib ? static_cast<unsigned long long *>(ib->data()) : nullptr};
+    void *img[2] = {ia ? ia->data() : nullptr, ib ? ib->data() : nullptr};
     unsigned *pos[2] = {pa ? static_cast<unsigned *>(pa->data()) : nullptr,
                         pb ? static_cast<unsigned *>(pb->data()) : nullptr};
-    int cur = 0;
-    for (int a = 0; a < passes; ++a) {
-        bool fst = a == 0, lst = a == passes - 1;
-        int shift = 8 * active[a];
-        int src = cur, dst = passes > 2 ? 1 - cur : 0;
-        if (fst) launch_up<true>(ctx, items, tiles, keys, nullptr, n, shift, counts);
-        else launch_up<false>(ctx, items, tiles, nullptr, img[src], n, shift, counts);
-        rs_scan_sums<<<chunks, SCAN_THREADS, 0, ctx->stream>>>(counts, m, sums);
-        rs_scan_top<<<1, 1024, 0, ctx->stream>>>(sums, chunks);
-        rs_scan_apply<<<chunks, SCAN_THREADS, 0, ctx->stream>>>(counts, m, sums, offs);
-        if (fst && lst)
-            launch_down<true, true>(ctx, items, tiles, keys, nullptr, nullptr, nullptr, nullptr, oo, n, shift, offs);
-        else if (fst)
-            launch_down<true, false>(ctx, items, tiles, keys, nullptr, nullptr, img[0], pos[0], nullptr, n, shift, offs);
-        else if (lst)
-            launch_down<false, true>(ctx, items, tiles, nullptr, img[src], pos[src], nullptr, nullptr, oo, n, shift, offs);
-        else
-            launch_down<false, false>(ctx, items, tiles, nullptr, img[src], pos[src], img[dst], pos[dst], nullptr, n, shift, offs);
-        if ((st = launched(ctx, "rs_pass"))) {
-            cleanup();
-            return release(st);
-        }
-        if (fst) cur = 0;
-        else if (!lst) cur = dst;
+    const vkc_status pst = narrow ? radix_argsort_passes<unsigned>(ctx, items, tiles, m, chunks, keys, img, pos, counts,
+                                                                    offs, sums, oo, n, active, passes)
+                                  : radix_argsort_passes<unsigned long long>(ctx, items, tiles, m, chunks, keys, img, pos,
+                                                                             counts, offs, sums, oo, n, active, passes);
+    if (pst) {
+        cleanup();
+        return release(pst);
     }
     DevStatus ds;
     st = read_status(ctx, &ds);
@@ -445,11 +465,11 @@ vkc_status radix_pairs(vkc_ctx *ctx, unsigned long long *img[2], unsigned *pos[2
     int cur = 0;
     for (int a = 0; a < npasses; ++a) {
         const int shift = shifts[a];
-        launch_up<false>(ctx, items, tiles, nullptr, img[cur], n, shift, counts);
+        launch_up<false, unsigned long long>(ctx, items, tiles, nullptr, img[cur], n, shift, counts);
         rs_scan_sums<<<chunks, SCAN_THREADS, 0, ctx->stream>>>(counts, m, sums);
         rs_scan_top<<<1, 1024, 0, ctx->stream>>>(sums, chunks);
         rs_scan_apply<<<chunks, SCAN_THREADS, 0, ctx->stream>>>(counts, m, sums, offs);
-        launch_down<false, false>(ctx, items, tiles, nullptr, img[cur], pos[cur], img[1 - cur], pos[1 - cur], nullptr, n,
+        launch_down<false, false, unsigned long long>(ctx, items, tiles, nullptr, img[cur], pos[cur], img[1 - cur], pos[1 - cur], nullptr, n,
                                   shift, offs);
         if ((st = launched(ctx, "radix_pairs"))) return st;
         cur = 1 - cur;
