@@ -238,7 +238,9 @@ __global__ void __launch_bounds__(RS_THREADS, RsShape<RS_ITEMS>::MIN_BLOCKS) rs_
             total += c;
         }
         unsigned tile_total;
-        s_dstart[d] = block_exclusive_sum<unsigned>(total, &tile_total);
+        const unsigned start = block_exclusive_sum<unsigned>(total, &tile_total);
+        s_dstart[d] = start;
+        s_tile_excl[d] -= start;  // from here: the output row of sorted-tile row l is s_tile_excl[d] + l
     }
     __syncthreads();
     // The tile sorted by digit (stable) in shared memory, then written out with consecutive
@@ -259,7 +261,7 @@ __global__ void __launch_bounds__(RS_THREADS, RsShape<RS_ITEMS>::MIN_BLOCKS) rs_
     for (int l = threadIdx.x; l < rows; l += RS_THREADS) {
         const IMG im = s_img[l];
         const unsigned d = static_cast<unsigned>(im >> shift) & 0xffu;
-        const unsigned dst = s_tile_excl[d] + (static_cast<unsigned>(l) - s_dstart[d]);
+        const unsigned dst = s_tile_excl[d] + static_cast<unsigned>(l);
         if (LAST) {
             out[dst] = static_cast<long long>(s_pos[l]);
         } else {
