@@ -194,7 +194,7 @@ def check_results(results):
         raise SystemExit("fused dot %r != unfused %r" % (a, b))
 
 
-# ---------------------------------------------------------------------------- config 3
+# ---------------------------------------------------------------------------- argsort and group-by
 
 
 def splitmix64_np(x):
@@ -222,7 +222,7 @@ def zipf_keys(n, s=1.1, distinct=1 << 20, seed=11):
     return out
 
 
-def config3_plan(n, nb):
+def sortgroup_plan(n, nb):
     """(label, algorithmic bytes) of the sorted and hashed group-by pipelines."""
     return [("argsort_i64", 16 * n), ("gather_i64(keys)", 24 * n), ("gather_f64(vals)", 24 * n),
             ("gather_i64(vals)", 24 * n), ("prev_i64", 16 * n), ("ne_i64", 17 * n),
@@ -230,7 +230,7 @@ def config3_plan(n, nb):
             ("reduce_into_add_i64", 16 * n + 8 * nb), ("histogram", 8 * n + 8 * nb)]
 
 
-def config3_step(ctx, keys, vf, vi, stream):
+def sortgroup_step(ctx, keys, vf, vi, stream):
     """Stable argsort, values gathered by the permutation, scan_by add over the sorted runs, and
     group-by sum/count through group_id. Returns ({label: ms}, results)."""
     import torch
@@ -264,8 +264,8 @@ def config3_step(ctx, keys, vf, vi, stream):
     return {label: e0.elapsed_time(e1) for label, e0, e1 in marks}, res
 
 
-def run_config3(ctx, n, stream, steps, warmup):
-    """Config 3 at n rows for both key distributions: per-kernel ms, GB/s and rows/s."""
+def run_sort_groupby(ctx, n, stream, steps, warmup):
+    """Argsort and group-by at n rows for both key distributions: per-kernel ms, GB/s and rows/s."""
     out = {}
     vf = ctx.call("rand_f64", n, 21)
     vi = ctx.call("sub_i64", ctx.call("and_i64", ctx.call("rand_i64", n, 22), (1 << 21) - 1), 1 << 20)
@@ -275,15 +275,15 @@ def run_config3(ctx, n, stream, steps, warmup):
         else:
             keys = ctx.upload(zipf_keys(n))
         for _ in range(warmup):
-            config3_step(ctx, keys, vf, vi, stream)
+            sortgroup_step(ctx, keys, vf, vi, stream)
         acc = {}
         for _ in range(steps):
-            per, res = config3_step(ctx, keys, vf, vi, stream)
+            per, res = sortgroup_step(ctx, keys, vf, vi, stream)
             for k, v in per.items():
                 acc[k] = acc.get(k, 0.0) + v
         nb = res["reduce_max_i64"] + 1
         groups = {}
-        for label, nbytes in config3_plan(n, nb):
+        for label, nbytes in sortgroup_plan(n, nb):
             ms = acc[label] / steps
             groups[label] = {"ms": round(ms, 4), "GB/s": round(nbytes / (ms / 1e3) / 1e9, 1),
                              "Grows/s": round(n / (ms / 1e3) / 1e9, 3)}
@@ -296,22 +296,22 @@ def run_config3(ctx, n, stream, steps, warmup):
                         "histogram" % (n.bit_length() - 1), "steps": steps, "warmup": warmup, **out}
 
 
-# ---------------------------------------------------------------------------- config 4
+# ---------------------------------------------------------------------------- batched statements
 
 
-def config4_lengths(count, lo, hi, seed=13):
+def batch_lengths(count, lo, hi, seed=13):
     """Lengths floor(2^U), U uniform in [lo, hi], from a seeded splitmix stream."""
     u = (splitmix64_np(np.arange(seed, seed + count, dtype=np.uint64)) >> np.uint64(11)).astype(np.float64) * 2.0 ** -53
     return np.floor(2.0 ** (lo + (hi - lo) * u)).astype(np.int64)
 
 
-def run_config4(ctx, count=4096, lo=10, hi=18, reps=2):
-    """Config 4: `count` independent arrays, each running filter_gt(0.9) -> sum on f64 values and
+def run_batched(ctx, count=4096, lo=10, hi=18, reps=2):
+    """Batched statements: `count` independent arrays, each running filter_gt(0.9) -> sum on f64 values and
     argsort of i64 keys below 2^16, three ways: the plain per-array GPU path (one synchronous
     call per statement, as the reference executor runs them), the batched entries (one
     persistent launch for the filter-sum, one batched radix sort), and a captured CUDA graph of
     the batch replayed. Each timed run includes reading the sums back to the host."""
-    lens = config4_lengths(count, lo, hi)
+    lens = batch_lengths(count, lo, hi)
     xs = [ctx.call("rand_f64", int(n), 100 + i) for i, n in enumerate(lens)]
     ks = [ctx.call("and_i64", ctx.call("rand_i64", int(n), 50_000 + i), 0xFFFF) for i, n in enumerate(lens)]
     ctx.synchronize()
@@ -375,11 +375,11 @@ def run_config4(ctx, count=4096, lo=10, hi=18, reps=2):
             "sums_bit_exact": exact, "argsort_sample_equal": bool(perms_ok)}
 
 
-# ---------------------------------------------------------------------------- config 5
+# ---------------------------------------------------------------------------- served requests
 
 
-def run_config5(ctx, rates=(100, 400, 1600, 6400), count=300, slots=4, budget=150e9, p99_bound_ms=100.0):
-    """Config 5: Poisson arrivals of programs drawn from {dot, filter_gt + length, argsort,
+def run_served(ctx, rates=(100, 400, 1600, 6400), count=300, slots=4, budget=150e9, p99_bound_ms=100.0):
+    """Served requests: Poisson arrivals of programs drawn from {dot, filter_gt + length, argsort,
     group-by sum} with n = floor(10^U), U uniform in [3, 8], inputs generated on the device;
     the plain GPU path (one request at a time, one synchronous call per statement) against the
     server (continuous batching over `slots` streams, same-kind coalescing, admission by a
@@ -555,9 +555,9 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--cpu-sample", type=int, default=1 << 23)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--config3-n", type=int, default=1 << 27, help="0 skips the argsort/group-by section")
-    ap.add_argument("--config4-arrays", type=int, default=4096, help="0 skips the batched section")
-    ap.add_argument("--config5-requests", type=int, default=300, help="0 skips the served section")
+    ap.add_argument("--sort-n", type=int, default=1 << 27, help="0 skips the argsort/group-by section")
+    ap.add_argument("--batch-arrays", type=int, default=4096, help="0 skips the batched section")
+    ap.add_argument("--serve-requests", type=int, default=300, help="0 skips the served section")
     args = ap.parse_args()
     world, rank, local = dist_setup()
     n = args.n
@@ -653,13 +653,13 @@ def main():
                "sample": "oracle port of the scalar entries (one thread, as the reference), the sweep "
                          "at n=2^%d, %d passes" % (args.cpu_sample.bit_length() - 1, passes)}
 
-    # Config 3 (argsort and group-by), reported beside the headline sweep, not in it.
+    # Argsort and group-by, batched statements and served requests, reported beside the headline sweep.
     c3 = None
     del inputs, hin, res
-    if args.config3_n > 0:
-        c3 = run_config3(ctx, args.config3_n, stream, steps=3, warmup=1)
-    c4 = run_config4(ctx, args.config4_arrays) if args.config4_arrays > 0 else None
-    c5 = run_config5(ctx, count=args.config5_requests) if args.config5_requests > 0 else None
+    if args.sort_n > 0:
+        c3 = run_sort_groupby(ctx, args.sort_n, stream, steps=3, warmup=1)
+    c4 = run_batched(ctx, args.batch_arrays) if args.batch_arrays > 0 else None
+    c5 = run_served(ctx, count=args.serve_requests) if args.serve_requests > 0 else None
 
     if rank == 0:
         line = {
@@ -678,9 +678,9 @@ def main():
             "clocks": clk,
             "gpu_launches": launches,
             "kernels": kernels,
-            "config3": c3,
-            "config4": c4,
-            "config5": c5,
+            "sort_groupby": c3,
+            "batched": c4,
+            "served": c5,
         }
         print(json.dumps(line), flush=True)
     ctx.close()

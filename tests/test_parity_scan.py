@@ -11,7 +11,7 @@ pytestmark = pytest.mark.gpu
 
 
 def vals(n, seed):
-    # BASELINE shape: uniform in [-2^20, 2^20).
+    # The sweep workload's scan values: uniform in [-2^20, 2^20).
     return (oracle.rand_i64(n, seed).view(np.uint64) % np.uint64(1 << 21)).astype(np.int64) - (1 << 20)
 
 

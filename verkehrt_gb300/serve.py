@@ -18,7 +18,7 @@ A request's result is the same whether it ran alone or in a mix: every entry use
 deterministic and bit-exact (the canonical sums, counts, stable argsort, first-occurrence
 group ids), so tests compare the two exactly.
 
-Program kinds (survey config 5): dot (x = rand_f64(n, s); y = rand_f64(n, s + 1); dot_f64),
+Program kinds (the served mix): dot (x = rand_f64(n, s); y = rand_f64(n, s + 1); dot_f64),
 filter_len (length(filter_gt_f64(rand_f64(n, s), 0.9))), argsort (argsort_i64(rand_i64(n, s))),
 group_sum (group-by sum of i64 values over keys below 2^16: group_id_i64, reduce_into_add_i64).
 """
