@@ -775,12 +775,11 @@ static vkc_status launch_canon(vkc_ctx *ctx, const RowArgs &a, int64_t nb, int T
     int warps = 16 * C;
     canon_chunk_kernel<<<(warps + 7) / 8, 256, 0, ctx->stream>>>(T, C, wk);
     if ((st = launched(ctx, "canon_chunk"))) return st;
-    static bool configured = false;
-    if (!configured) {
+    static std::atomic<unsigned long long> configured{0};
+    once_per_device(configured, ctx->device, [] {
         cudaFuncSetAttribute(canon_walk_kernel<OP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              static_cast<int>(sizeof(WalkSmem)));
-        configured = true;
-    }
+    });
     canon_walk_kernel<OP><<<16, WK_THREADS, sizeof(WalkSmem), ctx->stream>>>(a, nb, T, C, wk, state);
     return launched(ctx, "canon_walk");
 }

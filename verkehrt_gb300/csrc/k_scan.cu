@@ -300,17 +300,16 @@ __global__ void __launch_bounds__(SC_THREADS + 64, SC_BLOCKS) scan_kernel(const 
 
 // Launches a scan on `stream` with the tile records at `recs` (REC_STRIDE bytes per tile).
 template <bool BY>
-static void launch_scan(int sms, cudaStream_t stream, const unsigned long long *x, const unsigned char *s,
+static void launch_scan(int device, int sms, cudaStream_t stream, const unsigned long long *x, const unsigned char *s,
                         unsigned long long *o, int64_t n, int tiles, ulonglong2 *recs, unsigned epoch,
                         ScanState *state, unsigned *counters, DevStatus *status) {
     const bool aligned = (reinterpret_cast<uintptr_t>(x) & 31) == 0 && (reinterpret_cast<uintptr_t>(o) & 31) == 0 &&
                          (reinterpret_cast<uintptr_t>(s) & 15) == 0;
     constexpr size_t smem = SC_SLOTS * ScanPass<BY>::SLOT_BYTES;
-    static const bool configured = [] {
+    static std::atomic<unsigned long long> configured{0};
+    once_per_device(configured, device, [] {
         cudaFuncSetAttribute(scan_kernel<BY>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-        return true;
-    }();
-    (void)configured;
+    });
     int per_sm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, scan_kernel<BY>, SC_THREADS + 64, smem) != cudaSuccess ||
         per_sm < 1) {
@@ -348,8 +347,8 @@ struct ScanImpl : ScannerImpl {
         const auto *x = args[0].ptr<unsigned long long>();
         const unsigned char *s = by ? args[1].ptr<unsigned char>() : nullptr;
         auto *o = static_cast<unsigned long long *>(out->data());
-        if (by) launch_scan<true>(ctx->sms, ctx->stream, x, s, o, n, tiles, recs, epoch, state, ctx->counters, ctx->status);
-        else launch_scan<false>(ctx->sms, ctx->stream, x, s, o, n, tiles, recs, epoch, state, ctx->counters, ctx->status);
+        if (by) launch_scan<true>(ctx->device, ctx->sms, ctx->stream, x, s, o, n, tiles, recs, epoch, state, ctx->counters, ctx->status);
+        else launch_scan<false>(ctx->device, ctx->sms, ctx->stream, x, s, o, n, tiles, recs, epoch, state, ctx->counters, ctx->status);
         return launched(ctx, "scan");
     }
 };
@@ -550,7 +549,7 @@ extern "C" vkc_status vkc_scan_add_i64_noalloc(int device, const int64_t *in, in
         cudaGetLastError();
         return done(VKC_DEVICE, std::string("vkc_scan_add_i64_noalloc: ") + cudaGetErrorString(e));
     }
-    launch_scan<false>(sms, s, reinterpret_cast<const unsigned long long *>(in), nullptr,
+    launch_scan<false>(device, sms, s, reinterpret_cast<const unsigned long long *>(in), nullptr,
                        reinterpret_cast<unsigned long long *>(out), n, tiles, recs, 1u, state, counters, status);
     e = cudaGetLastError();
     if (e != cudaSuccess) return done(VKC_DEVICE, std::string("vkc_scan_add_i64_noalloc: ") + cudaGetErrorString(e));

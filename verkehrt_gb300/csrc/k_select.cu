@@ -289,13 +289,12 @@ static vkc_status run_select(vkc_ctx *ctx, SelArgs a, int64_t n, Builder *b) {
     const unsigned epoch = next_epoch(ctx);
     a.aligned = (reinterpret_cast<uintptr_t>(a.x) & 15) == 0 && (reinterpret_cast<uintptr_t>(a.m) & 15) == 0;
     constexpr size_t smem = SEL_SLOTS * SelectPass<KIND, W>::SLOT_BYTES;
-    static const bool configured = [] {
+    static std::atomic<unsigned long long> configured{0};
+    once_per_device(configured, ctx->device, [] {
         cudaFuncSetAttribute(select_kernel<KIND, W, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
         if constexpr (KIND == SEL_FILTER)
             cudaFuncSetAttribute(select_kernel<KIND, W, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-        return true;
-    }();
-    (void)configured;
+    });
     bool launched_pos = false;
     if constexpr (KIND == SEL_FILTER) {
         if (pos_range(a.r)) {

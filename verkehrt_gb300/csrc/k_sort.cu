@@ -291,13 +291,12 @@ template <bool FIRST, bool LAST, class IMG>
 static void launch_down(vkc_ctx *ctx, int items, int tiles, const long long *keys, const IMG *img_in,
                         const unsigned *pos_in, IMG *img_out, unsigned *pos_out, long long *out, int64_t n, int shift,
                         const unsigned *offs) {
-    static const bool configured = [] {
+    static std::atomic<unsigned long long> configured{0};
+    once_per_device(configured, ctx->device, [] {
         set_down_smem<8, FIRST, LAST, IMG>();
         set_down_smem<12, FIRST, LAST, IMG>();
         set_down_smem<16, FIRST, LAST, IMG>();
-        return true;
-    }();
-    (void)configured;
+    });
 #define RS_DOWN(I)                                                                                             \
     rs_down_kernel<I, FIRST, LAST, IMG><<<tiles, RS_THREADS, (sizeof(IMG) + sizeof(unsigned)) * RsShape<I>::TILE, \
                                           ctx->stream>>>(keys, img_in, pos_in, img_out, pos_out, out, n, shift, tiles, offs)

@@ -147,6 +147,16 @@ namespace vkc {
 
 constexpr int kCounterSlots = 64;
 
+// Runs `setup` (per-device function attributes such as the dynamic shared memory limit) the
+// first time a call site reaches it on a device. The bit is set after the setup, so a thread
+// that finds it set knows the setup is done; racing threads may both run it, which is harmless.
+template <class F> inline void once_per_device(std::atomic<unsigned long long> &seen, int device, F setup) {
+    const unsigned long long bit = 1ull << (device & 63);
+    if (seen.load(std::memory_order_acquire) & bit) return;
+    setup();
+    seen.fetch_or(bit, std::memory_order_release);
+}
+
 // The tuned value of knob k for a call over n rows.
 inline int tune(const vkc_ctx *ctx, TuneKnob k, int64_t n) { return ctx->tuning.v[k][tune_class(n)]; }
 
