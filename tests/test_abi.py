@@ -78,3 +78,15 @@ def test_open_without_a_device_fails_cleanly(lib):
         pytest.skip("a device is present")
     h = ctypes.c_void_p()
     assert lib.vkc_open(0, ctypes.byref(h)) == 4  # VKC_DEVICE
+
+
+def test_missing_library_raises_instead_of_falling_back(tmp_path, monkeypatch):
+    # The CUDA library is the only compute path: without it every entry raises.
+    import verkehrt_gb300 as vk
+
+    monkeypatch.setattr(vk, "_lib", None)
+    monkeypatch.setattr(vk, "LIB_PATH", str(tmp_path / "libvkcuda.so"))
+    with pytest.raises(RuntimeError, match="not built"):
+        vk.load()
+    with pytest.raises(RuntimeError, match="not built"):
+        vk.Context(0)
