@@ -738,6 +738,25 @@ __global__ void __launch_bounds__(WK_THREADS) canon_walk_kernel(RowArgs args, in
     if (lane == 0) state->lanes[L] = s;
 }
 
+// Short inputs: the reference's own order, each lane a chain of IEEE adds over its rows
+// (reduce.rs:45-62), from the lane states. The block first stages every row value in shared
+// memory (coalesced, all loads in flight at once); then 16 threads run the lane chains.
+constexpr int64_t CANON_SEQ_BLOCKS = 256;  // 16-row blocks (4096 rows) up to which this path runs
+
+template <int OP>
+__global__ void __launch_bounds__(256) canon_seq_kernel(RowArgs args, int nb, CanonState *state) {
+    __shared__ unsigned long long s_v[CANON_SEQ_BLOCKS * 16];
+    const int rows = nb * 16;
+    for (int i = threadIdx.x; i < rows; i += blockDim.x)
+        s_v[i] = row_value<OP>(args, args.x[i], OP == ROW_DOT ? args.y[i] : 0ull);
+    __syncthreads();
+    const int j = threadIdx.x;
+    if (j >= 16) return;
+    double s = as_f64(state->lanes[j]);
+    for (int b = 0; b < nb; ++b) s = __dadd_rn(s, as_f64(s_v[b * 16 + j]));
+    state->lanes[j] = as_bits(s);
+}
+
 // Stores the row values of the rest rows (fewer than 16) as the pending tail.
 template <int OP>
 __global__ void canon_tail(RowArgs args, int64_t first, int rest, CanonState *state) {
@@ -824,7 +843,16 @@ struct CanonReducer : DevReducer {
         const int64_t nb = n / 16;
         const int rest = static_cast<int>(n % 16);
         auto *cs = static_cast<CanonState *>(state);
-        if (nb > 0) {
+        if (nb > 0 && nb <= CANON_SEQ_BLOCKS) {
+            const int nbi = static_cast<int>(nb);
+            switch (op) {
+            case ROW_SUM: canon_seq_kernel<ROW_SUM><<<1, 256, 0, ctx->stream>>>(a, nbi, cs); break;
+            case ROW_DOT: canon_seq_kernel<ROW_DOT><<<1, 256, 0, ctx->stream>>>(a, nbi, cs); break;
+            case ROW_SUMSQ: canon_seq_kernel<ROW_SUMSQ><<<1, 256, 0, ctx->stream>>>(a, nbi, cs); break;
+            default: canon_seq_kernel<ROW_CONDSUM><<<1, 256, 0, ctx->stream>>>(a, nbi, cs); break;
+            }
+            if ((st = launched(ctx, "canon_seq"))) return st;
+        } else if (nb > 0) {
             const int64_t T64 = (nb + CT_BLOCKS - 1) / CT_BLOCKS;
             if (T64 > (int64_t(1) << 26)) return fail(ctx, VKC_USAGE, "array too long for one update");
             const int T = static_cast<int>(T64), C = (T + 31) / 32;

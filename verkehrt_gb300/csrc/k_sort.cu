@@ -313,6 +313,45 @@ __global__ void rs_iota_kernel(long long *out, int64_t n) {
     for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride) out[i] = i;
 }
 
+// Short inputs (the reference sorts up to 1024 rows by comparison, radix.rs:140-151): one
+// block sorts (image, position) pairs in shared memory with a bitonic network. The pairs are
+// distinct, so the order is total and the result is the stable order; padding pairs (all-ones
+// image, position >= n) sort after every row.
+constexpr int SMALL_SORT = 2048;
+
+__global__ void __launch_bounds__(1024) small_argsort_kernel(const long long *__restrict__ keys, int n,
+                                                              long long *__restrict__ out) {
+    __shared__ unsigned long long s_img[SMALL_SORT];
+    __shared__ unsigned s_pos[SMALL_SORT];
+    int p = 1;
+    while (p < n) p <<= 1;
+    for (int i = threadIdx.x; i < p; i += blockDim.x) {
+        s_img[i] = i < n ? image_of(keys[i]) : ~0ull;
+        s_pos[i] = static_cast<unsigned>(i);
+    }
+    __syncthreads();
+    for (int k = 2; k <= p; k <<= 1) {
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = threadIdx.x; i < p; i += blockDim.x) {
+                const int l = i ^ j;
+                if (l > i) {
+                    const unsigned long long a = s_img[i], b = s_img[l];
+                    const unsigned pa = s_pos[i], pb = s_pos[l];
+                    const bool greater = a > b || (a == b && pa > pb);
+                    if (greater == ((i & k) == 0)) {
+                        s_img[i] = b;
+                        s_img[l] = a;
+                        s_pos[i] = pb;
+                        s_pos[l] = pa;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    }
+    for (int i = threadIdx.x; i < n; i += blockDim.x) out[i] = static_cast<long long>(s_pos[i]);
+}
+
 // The active-digit passes of argsort over (image, position) ping-pong buffers of image type IMG.
 template <class IMG>
 static vkc_status radix_argsort_passes(vkc_ctx *ctx, int items, int tiles, int64_t m, int chunks, const long long *keys,
@@ -367,6 +406,13 @@ static vkc_status argsort_i64(vkc_ctx *ctx, const vkc_value *args, int nargs, vk
         return VKC_OK;
     }
     const auto *keys = static_cast<const long long *>(xs->data());
+    if (n <= SMALL_SORT) {
+        small_argsort_kernel<<<1, 1024, 0, ctx->stream>>>(keys, static_cast<int>(n), static_cast<long long *>(o->data()));
+        if ((st = launched(ctx, "small_argsort"))) return release(st);
+        out->kind = VKC_VALUE_ARRAY;
+        out->array = o;
+        return VKC_OK;
+    }
     // Histogram of every digit.
     void *p;
     if ((st = scratch(ctx, 8 * RADIX * sizeof(unsigned), &p))) return release(st);
