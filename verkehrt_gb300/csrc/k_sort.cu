@@ -106,9 +106,9 @@ __device__ __forceinline__ unsigned digit_peers(unsigned d, unsigned valid) {
     unsigned m = valid;
 #pragma unroll
     for (int b = 0; b < 8; ++b) {
-        const bool set = (d >> b) & 1u;
-        const unsigned v = __ballot_sync(FULL, set);
-        m &= set ? v : ~v;
+        const unsigned bit = (d >> b) & 1u;
+        const unsigned v = __ballot_sync(FULL, bit);
+        m &= ~(v ^ (0u - bit));  // keep the lanes whose bit b equals this lane's
     }
     return m;
 }
@@ -175,23 +175,16 @@ __global__ void __launch_bounds__(SCAN_THREADS) rs_scan_apply(const unsigned *__
 // offsets[d * tiles + tile]. FIRST reads the i64 keys (positions are the row numbers); LAST
 // writes only the positions, as i64. IMG is the key image carried between passes: 64 bits, or
 // its low 32 bits when every active digit lies there.
-template <int RS_ITEMS, bool FIRST, bool LAST, class IMG>
-__global__ void __launch_bounds__(RS_THREADS, RsShape<RS_ITEMS>::MIN_BLOCKS) rs_down_kernel(
-    const long long *__restrict__ keys_in, const IMG *__restrict__ img_in,
-    const unsigned *__restrict__ pos_in, IMG *__restrict__ img_out,
-    unsigned *__restrict__ pos_out, long long *__restrict__ out, int64_t n, int shift, int tiles,
-    const unsigned *__restrict__ offsets) {
+// The body of a down tile; WHOLE when every row of the tile is below n (all but the last
+// tile), which drops the per-row bounds checks.
+template <int RS_ITEMS, bool FIRST, bool LAST, class IMG, bool WHOLE>
+__device__ __forceinline__ void rs_down_tile(const long long *__restrict__ keys_in, const IMG *__restrict__ img_in,
+                                             const unsigned *__restrict__ pos_in, IMG *__restrict__ img_out,
+                                             unsigned *__restrict__ pos_out, long long *__restrict__ out, int64_t n,
+                                             int shift, int tile, unsigned short (*s_wcnt)[RADIX],
+                                             unsigned *s_tile_excl, unsigned *s_dstart, unsigned char *smem) {
     constexpr int RS_TILE = RsShape<RS_ITEMS>::TILE;
-    __shared__ unsigned short s_wcnt[RS_WARPS][RADIX];  // per-warp digit counts, then offsets
-    __shared__ unsigned s_tile_excl[RADIX];             // the digit's first output row
-    __shared__ unsigned s_dstart[RADIX];                // the digit's first row in the sorted tile
-    extern __shared__ __align__(16) unsigned char rs_smem[];
-    const int tile = blockIdx.x;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    for (int i = threadIdx.x; i < RS_WARPS * RADIX; i += RS_THREADS) (&s_wcnt[0][0])[i] = 0;
-    s_tile_excl[threadIdx.x] = offsets[static_cast<int64_t>(threadIdx.x) * tiles + tile];  // RS_THREADS == RADIX
-    __syncthreads();
-
     // Rows of this warp: warp-striped, row = base + j*32 + lane, so (j, lane) is row order.
     const int64_t base = static_cast<int64_t>(tile) * RS_TILE + static_cast<int64_t>(w) * (32 * RS_ITEMS);
     IMG img[RS_ITEMS];
@@ -201,7 +194,7 @@ __global__ void __launch_bounds__(RS_THREADS, RsShape<RS_ITEMS>::MIN_BLOCKS) rs_
 #pragma unroll
     for (int j = 0; j < RS_ITEMS; ++j) {
         const int64_t r = base + j * 32 + lane;
-        const bool in = r < n;
+        const bool in = WHOLE || r < n;
         if (FIRST) {
             img[j] = in ? static_cast<IMG>(image_of(__ldcs(keys_in + r))) : static_cast<IMG>(~0ull);
             pos[j] = 0u;  // the row number, recomputed when stored
@@ -212,10 +205,10 @@ __global__ void __launch_bounds__(RS_THREADS, RsShape<RS_ITEMS>::MIN_BLOCKS) rs_
     }
 #pragma unroll
     for (int j = 0; j < RS_ITEMS; ++j) {
-        const bool in = base + j * 32 + lane < n;
+        const bool in = WHOLE || base + j * 32 + lane < n;
         const unsigned d = static_cast<unsigned>(img[j] >> shift) & 0xffu;
         // Rank among this warp's earlier rows with the same digit.
-        const unsigned peers = digit_peers(d, __ballot_sync(FULL, in));
+        const unsigned peers = digit_peers(d, WHOLE ? FULL : __ballot_sync(FULL, in));
         const unsigned short before = s_wcnt[w][d];
         __syncwarp();
         if (in) {
@@ -245,11 +238,11 @@ __global__ void __launch_bounds__(RS_THREADS, RsShape<RS_ITEMS>::MIN_BLOCKS) rs_
     __syncthreads();
     // The tile sorted by digit (stable) in shared memory, then written out with consecutive
     // threads on consecutive rows of each digit's run, so the stores coalesce.
-    IMG *s_img = reinterpret_cast<IMG *>(rs_smem);
-    unsigned *s_pos = reinterpret_cast<unsigned *>(rs_smem + sizeof(IMG) * RS_TILE);
+    IMG *s_img = reinterpret_cast<IMG *>(smem);
+    unsigned *s_pos = reinterpret_cast<unsigned *>(smem + sizeof(IMG) * RS_TILE);
 #pragma unroll
     for (int j = 0; j < RS_ITEMS; ++j) {
-        if (base + j * 32 + lane < n) {
+        if (WHOLE || base + j * 32 + lane < n) {
             const unsigned d = static_cast<unsigned>(img[j] >> shift) & 0xffu;
             const unsigned l = s_dstart[d] + s_wcnt[w][d] + ((rank2[j / 2] >> (16 * (j & 1))) & 0xffffu);
             s_img[l] = img[j];
@@ -257,8 +250,7 @@ __global__ void __launch_bounds__(RS_THREADS, RsShape<RS_ITEMS>::MIN_BLOCKS) rs_
         }
     }
     __syncthreads();
-    const int rows = static_cast<int>(n - static_cast<int64_t>(tile) * RS_TILE < RS_TILE ? n - static_cast<int64_t>(tile) * RS_TILE : RS_TILE);
-    for (int l = threadIdx.x; l < rows; l += RS_THREADS) {
+    auto put = [&](int l) {
         const IMG im = s_img[l];
         const unsigned d = static_cast<unsigned>(im >> shift) & 0xffu;
         const unsigned dst = s_tile_excl[d] + static_cast<unsigned>(l);
@@ -268,7 +260,37 @@ __global__ void __launch_bounds__(RS_THREADS, RsShape<RS_ITEMS>::MIN_BLOCKS) rs_
             img_out[dst] = im;
             pos_out[dst] = s_pos[l];
         }
+    };
+    if (WHOLE) {
+#pragma unroll
+        for (int i = 0; i < RS_ITEMS; ++i) put(static_cast<int>(threadIdx.x) + i * RS_THREADS);
+    } else {
+        const int rows = static_cast<int>(n - static_cast<int64_t>(tile) * RS_TILE);
+        for (int l = threadIdx.x; l < rows; l += RS_THREADS) put(l);
     }
+}
+
+template <int RS_ITEMS, bool FIRST, bool LAST, class IMG>
+__global__ void __launch_bounds__(RS_THREADS, RsShape<RS_ITEMS>::MIN_BLOCKS) rs_down_kernel(
+    const long long *__restrict__ keys_in, const IMG *__restrict__ img_in,
+    const unsigned *__restrict__ pos_in, IMG *__restrict__ img_out,
+    unsigned *__restrict__ pos_out, long long *__restrict__ out, int64_t n, int shift, int tiles,
+    const unsigned *__restrict__ offsets) {
+    constexpr int RS_TILE = RsShape<RS_ITEMS>::TILE;
+    __shared__ unsigned short s_wcnt[RS_WARPS][RADIX];  // per-warp digit counts, then offsets
+    __shared__ unsigned s_tile_excl[RADIX];             // the digit's first output row
+    __shared__ unsigned s_dstart[RADIX];                // the digit's first row in the sorted tile
+    extern __shared__ __align__(16) unsigned char rs_smem[];
+    const int tile = blockIdx.x;
+    for (int i = threadIdx.x; i < RS_WARPS * RADIX; i += RS_THREADS) (&s_wcnt[0][0])[i] = 0;
+    s_tile_excl[threadIdx.x] = offsets[static_cast<int64_t>(threadIdx.x) * tiles + tile];  // RS_THREADS == RADIX
+    __syncthreads();
+    if (static_cast<int64_t>(tile + 1) * RS_TILE <= n)
+        rs_down_tile<RS_ITEMS, FIRST, LAST, IMG, true>(keys_in, img_in, pos_in, img_out, pos_out, out, n, shift, tile,
+                                                       s_wcnt, s_tile_excl, s_dstart, rs_smem);
+    else
+        rs_down_tile<RS_ITEMS, FIRST, LAST, IMG, false>(keys_in, img_in, pos_in, img_out, pos_out, out, n, shift, tile,
+                                                        s_wcnt, s_tile_excl, s_dstart, rs_smem);
 }
 
 // Launches of one pass's kernels for the tuned shape.
