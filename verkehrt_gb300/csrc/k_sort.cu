@@ -7,14 +7,16 @@
 //  * a digit that is equal in every row leaves the order unchanged and its pass is skipped
 //    (radix.rs:203-211);
 //  * each remaining digit is one reduce-then-scan pass over tiles of 256 x radix_items rows (the
-//    autotuner's table; 3072 by default): `up` counts each
+//    autotuner's table: 2048, 3072 or 4096 rows by size): `up` counts each
 //    tile's digits into a digit-major table, one exclusive scan of that table gives every
 //    (digit, tile) its first output row, and `down` ranks the tile's rows stably by digit
 //    (a ballot per digit bit, in row order) and scatters them. The first pass reads the keys, the
 //    last writes the positions as i64. (A single-pass lookback per digit was slower here: the
-//    lookback of 256 digits per tile advances a few tiles per L2 round trip.)
-// Stability makes the output the reference's, which the comparison sort of short inputs
-// (radix.rs:140-151) also gives, so one path serves every length.
+//    lookback of 256 digits per tile advances a few tiles per L2 round trip. A persistent
+//    `down` whose next tile arrives by TMA while it ranks the current one was no faster
+//    either: the pass is bound by instruction issue, about 3.8 warp instructions per row.)
+// Stability makes the output the reference's; inputs of at most 2048 rows are sorted in one
+// block by comparison (as the reference does below 1024 rows, radix.rs:140-151).
 #include <algorithm>
 
 #include "lookback.cuh"
