@@ -56,6 +56,36 @@ def test_gather_large_uniform(ctx):
     assert np.array_equal(got, oracle.gather(oracle.rand_i64(n, 1), idx_h))
 
 
+def test_gather_partitioned(ctx):
+    # Sources of 2^26 rows or more (four times L2) and at least half as many index rows take
+    # the partitioned path: uniform indices, indices crowded into one source region, the first
+    # and last rows, a ragged last tile, and 8-byte floats whose bits (NaN payloads) must
+    # survive.
+    nsrc = (1 << 26) + 3
+    src_h = oracle.rand_i64(nsrc, 1)
+    src = ctx.upload(src_h)
+    n = (1 << 25) + 5
+    r = oracle.rand_i64(n, 2).view(np.uint64)
+    cases = {
+        "uniform": (r % np.uint64(nsrc)).astype(np.int64),
+        "one_region": (r % np.uint64(1000)).astype(np.int64) + (nsrc - 5000),
+        "ends": np.where(r % np.uint64(2) == 0, 0, nsrc - 1).astype(np.int64),
+    }
+    for name, idx in cases.items():
+        got = ctx.call("gather_i64", src, ctx.upload(idx)).numpy()
+        assert np.array_equal(got, oracle.gather(src_h, idx)), name
+    idx = cases["uniform"]
+    got = ctx.call("gather_f64", ctx.upload(src_h.view(np.float64), "f64"), ctx.upload(idx)).numpy()
+    assert np.array_equal(got.view(np.int64), src_h[idx])
+    # The first offender in index order, and the context stays usable.
+    bad = idx.copy()
+    bad[30_000_001] = nsrc
+    bad[31_500_000] = -1
+    with pytest.raises(Exception, match="^gather index %d out of range for length %d$" % (nsrc, nsrc)):
+        ctx.call("gather_i64", src, ctx.upload(bad))
+    assert np.array_equal(ctx.call("gather_i64", src, ctx.upload(idx[:5])).numpy(), src_h[idx[:5]])
+
+
 def test_histogram_and_reduce_into(ctx):
     for n in (0, 5, 1000, 100_003):
         for nb in (1, 5, 1024, 4096, 4097, 100_000):

@@ -173,6 +173,16 @@ __global__ void __launch_bounds__(SCAN_THREADS) rs_scan_apply(const unsigned *__
     }
 }
 
+// Exclusive scan of m u32 counts into out, with sum_words(m) words of scratch in `sums`
+// (used by the partitioned gather as well as the passes below).
+int64_t scan_counts_sum_words(int64_t m) { return (m + SCAN_CHUNK - 1) / SCAN_CHUNK; }
+void scan_counts(vkc_ctx *ctx, const unsigned *c, int64_t m, unsigned *sums, unsigned *out) {
+    const int chunks = static_cast<int>(scan_counts_sum_words(m));
+    rs_scan_sums<<<chunks, SCAN_THREADS, 0, ctx->stream>>>(c, m, sums);
+    rs_scan_top<<<1, 1024, 0, ctx->stream>>>(sums, chunks);
+    rs_scan_apply<<<chunks, SCAN_THREADS, 0, ctx->stream>>>(c, m, sums, out);
+}
+
 // Down: one pass over digit `shift` with the tile's first output row per digit in
 // offsets[d * tiles + tile]. FIRST reads the i64 keys (positions are the row numbers); LAST
 // writes only the positions, as i64. IMG is the key image carried between passes: 64 bits, or
