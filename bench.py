@@ -424,42 +424,67 @@ def run_served(ctx, rates=(100, 400, 1600, 6400), count=300, slots=4, budget=150
 # ---------------------------------------------------------------------------- e2e
 
 
+# The order in which the e2e step uploads its inputs: the inputs of the calls whose results
+# come back to the host first, so that downloads start while the other inputs still arrive.
+E2E_UPLOADS = ["x", "v", "src", "idx", "y"]
+
+
 class HostInputs:
-    """The step's inputs in pinned host memory, and pinned buffers for the array results."""
+    """The step's inputs in pinned host memory, and one pinned host buffer per array result
+    (downloads of different results are in flight together)."""
 
     def __init__(self, ctx, inputs, n):
         import torch
 
         self.n = n
         self.host = {}
-        for name, arr in inputs.items():
+        for name in E2E_UPLOADS:
+            arr = inputs[name]
             t = torch.empty(n, dtype=torch.float64 if arr.type == "f64" else torch.int64, pin_memory=True)
             ctx.download_ptr(arr, t.data_ptr(), n)
             self.host[name] = (t, arr.type)
-        self.out = torch.empty(n, dtype=torch.int64, pin_memory=True)
+        outs = sum(1 for _, kernel, _, _, _ in sweep_plan(n) if kernel in ARRAY_RESULTS)
+        self.out = [torch.empty(n, dtype=torch.int64, pin_memory=True) for _ in range(outs)]
 
     def upload(self, ctx):
+        """Starts every upload (each a copy on the library's upload stream; a call that reads an
+        input waits for that input only)."""
         return {name: ctx.upload_ptr(t.data_ptr(), self.n, ty) for name, (t, ty) in self.host.items()}
 
 
+# Sweep calls whose result is an array (downloaded in the e2e step); mul_f64's product only
+# feeds the next call.
+ARRAY_RESULTS = ("filter_gt_f64", "gather_i64", "scan_add_i64")
+
+
+def e2e_order(plan):
+    """The sweep's calls, each once, ordered by the arrival of their last input (stable)."""
+    last = {name: i for i, name in enumerate(E2E_UPLOADS)}
+    return sorted(plan, key=lambda call: max(last.get(a, len(E2E_UPLOADS)) for a in call[2]))
+
+
 def run_e2e_step(ctx, n, hin):
-    """Upload the inputs from pinned host memory, run the sweep, download the array results.
-    Returns (seconds, h2d bytes, d2h bytes)."""
+    """Upload the inputs from pinned host memory, run the sweep, download the array results,
+    through the library's public calls: uploads and downloads run on its copy streams and
+    overlap each other and the kernels. Returns (seconds, h2d bytes, d2h bytes)."""
     t0 = time.perf_counter()
     inputs = hin.upload(ctx)
     h2d = sum(8 * n for _ in inputs)
     env = dict(inputs)
     d2h = 0
-    for label, kernel, names, extra, _ in sweep_plan(n):
+    copies = []
+    for label, kernel, names, extra, _ in e2e_order(sweep_plan(n)):
         out = ctx.call(kernel, *[env[a] for a in names], *extra)
         if kernel == "mul_f64":
             env["xy"] = out
         if hasattr(out, "handle"):
-            if kernel != "mul_f64":
-                ctx.download_ptr(out, hin.out.data_ptr(), n)
+            if kernel in ARRAY_RESULTS:
+                copies.append(ctx.download_start(out, hin.out[len(copies)].data_ptr(), n))
                 d2h += 8 * len(out)
         else:
             d2h += 8  # the scalar result
+    for c in copies:
+        c.wait()
     ctx.synchronize()
     return time.perf_counter() - t0, h2d, d2h
 
@@ -638,8 +663,10 @@ def main():
                    "frac": round(v[1] / v[2] / (v[0] / v[2] / 1e3) / 1e9 / peak, 3)}
                for k, v in per_label.items()}
 
-    # e2e through the C ABI with pinned host buffers.
+    # e2e through the C ABI with pinned host buffers, after one untimed step (the copy streams,
+    # the first touch of the pinned output pages).
     hin = HostInputs(ctx, inputs, n)
+    run_e2e_step(ctx, n, hin)
     e2e = []
     for _ in range(max(1, args.e2e_steps)):
         e2e.append(run_e2e_step(ctx, n, hin))

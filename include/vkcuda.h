@@ -130,11 +130,22 @@ VKC_API vkc_status vkc_timer_stop(vkc_ctx *ctx, float *ms);
  * with "array of N elements is too large" (value.rs:285-289) or "cannot allocate an array of
  * N elements" (value.rs:297-307). */
 VKC_API vkc_status vkc_array_new(vkc_ctx *ctx, vkc_type type, int64_t len, vkc_array **out);
-/* Copies `len` rows from host memory into a new device array (program inputs). */
+/* Copies `len` rows from host memory into a new device array (program inputs). Copies of at
+ * least 1 MiB run on the context's upload stream, overlapping kernels and downloads: the first
+ * call that reads the array waits for the copy, on the device. Pinned host memory must stay
+ * unchanged until then (or until vkc_synchronize). */
 VKC_API vkc_status vkc_array_upload(vkc_ctx *ctx, vkc_type type, const void *host, int64_t len,
                             vkc_array **out);
-/* Copies the array's rows into host memory, `capacity` rows at most (print and exports). */
+/* Copies the array's rows into host memory, `capacity` rows at most (print and exports), and
+ * waits for the copy. */
 VKC_API vkc_status vkc_array_download(vkc_ctx *ctx, const vkc_array *a, void *host, int64_t capacity);
+/* The same copy on the context's download stream, after the work queued so far: returns at
+ * once with a handle that vkc_copy_wait waits on (and frees). The handle holds a reference to
+ * the array; a later call that writes the array waits for the copy. */
+typedef struct vkc_copy vkc_copy;
+VKC_API vkc_status vkc_array_download_start(vkc_ctx *ctx, const vkc_array *a, void *host, int64_t capacity,
+                                            vkc_copy **out);
+VKC_API vkc_status vkc_copy_wait(vkc_ctx *ctx, vkc_copy *c);
 /* A zero-copy view of rows start..start+len, src/value.rs:245-259 (Array::slice) and
  * src/kernels/scalar/index.rs:76-93 (slice_T). */
 VKC_API vkc_status vkc_array_slice(vkc_ctx *ctx, const vkc_array *a, int64_t start, int64_t len,

@@ -69,6 +69,8 @@ _SIGNATURES = {
     "vkc_array_new": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int64, ctypes.POINTER(_P)]),
     "vkc_array_upload": (ctypes.c_int, [_P, ctypes.c_int, _P, ctypes.c_int64, ctypes.POINTER(_P)]),
     "vkc_array_download": (ctypes.c_int, [_P, _P, _P, ctypes.c_int64]),
+    "vkc_array_download_start": (ctypes.c_int, [_P, _P, _P, ctypes.c_int64, ctypes.POINTER(_P)]),
+    "vkc_copy_wait": (ctypes.c_int, [_P, _P]),
     "vkc_array_slice": (ctypes.c_int, [_P, _P, ctypes.c_int64, ctypes.c_int64, ctypes.POINTER(_P)]),
     "vkc_array_len": (ctypes.c_int64, [_P]),
     "vkc_array_type": (ctypes.c_int, [_P]),
@@ -233,6 +235,24 @@ class Array:
         return Array(self.ctx, h.value)
 
 
+class Copy:
+    """An asynchronous download in flight (Context.download_start)."""
+
+    def __init__(self, ctx, handle):
+        self.ctx, self.handle = ctx, handle
+
+    def wait(self):
+        if self.handle:
+            h, self.handle = self.handle, None
+            self.ctx._check(_lib.vkc_copy_wait(self.ctx.handle, h))
+
+    def __del__(self):
+        try:
+            self.wait()
+        except Exception:
+            pass
+
+
 class Context:
     """A device context (one stream, one scratch arena): the cuda ISA of one interpreter."""
 
@@ -294,6 +314,13 @@ class Context:
     def download_ptr(self, arr, ptr, capacity):
         """Copies up to `capacity` rows of `arr` to host address `ptr`; waits for the copy."""
         self._check(_lib.vkc_array_download(self.handle, arr.handle, ptr, capacity))
+
+    def download_start(self, arr, ptr, capacity):
+        """Starts the same copy on the download stream (after the work queued so far) and
+        returns a Copy whose wait() waits for it; uploads, kernels and other downloads overlap."""
+        h = _P()
+        self._check(_lib.vkc_array_download_start(self.handle, arr.handle, ptr, capacity, ctypes.byref(h)))
+        return Copy(self, h.value)
 
     def new_array(self, type_name, n):
         h = _P()

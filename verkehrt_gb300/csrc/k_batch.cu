@@ -310,6 +310,7 @@ extern "C" VKC_API vkc_status vkc_batch_new(vkc_ctx *ctx, int n, vkc_array *cons
     b->total = base[n];
     for (int i = 0; i < n; ++i) {
         vkc_array_retain(arrays[i]);
+        await_write(ctx, arrays[i]);  // batches are read and written on the context stream
         b->arrays.push_back(arrays[i]);
         b->host.push_back(BSeg{arrays[i]->data(), arrays[i]->len, base[i], i});
     }
@@ -359,6 +360,7 @@ extern "C" VKC_API vkc_status vkc_batch_filter_sum_f64(vkc_ctx *ctx, vkc_batch *
     if (n == 0) return VKC_OK;
     const CmpRange r = cmp_range(cmp, c);
     const int grid = std::min(n, ctx->sms * 8);
+    await_write(ctx, sums);
     auto *out = static_cast<unsigned long long *>(sums->data());
     const auto *tab = static_cast<const BSeg *>(b->table.ptr);
     unsigned *ticket = ctx->counters + 4;  // two words, zero between launches
@@ -377,6 +379,7 @@ extern "C" VKC_API vkc_status vkc_batch_count_f64(vkc_ctx *ctx, vkc_batch *b, in
     if (n == 0) return VKC_OK;
     const CmpRange r = cmp_range(cmp, c);
     const int grid = std::min(n, ctx->sms * 8);
+    await_write(ctx, counts);
     auto *out = static_cast<long long *>(counts->data());
     const auto *tab = static_cast<const BSeg *>(b->table.ptr);
     if (pos_range(r)) batch_count_kernel<true><<<grid, BF_THREADS, 0, ctx->stream>>>(tab, n, r, out, ctx->counters + 4);
@@ -398,6 +401,7 @@ extern "C" VKC_API vkc_status vkc_batch_dot_f64(vkc_ctx *ctx, vkc_batch *xs, vkc
         return fail(ctx, VKC_RUNTIME, "batch dot: the result array must be f64[" + std::to_string(n) + "]");
     if (n == 0) return VKC_OK;
     const int grid = std::min(n, ctx->sms * 8);
+    await_write(ctx, sums);
     batch_dot_kernel<<<grid, BF_THREADS, 0, ctx->stream>>>(static_cast<const BSeg *>(xs->table.ptr),
                                                            static_cast<const BSeg *>(ys->table.ptr), n,
                                                            static_cast<unsigned long long *>(sums->data()),
@@ -417,6 +421,7 @@ extern "C" VKC_API vkc_status vkc_batch_argsort_i64(vkc_ctx *ctx, vkc_batch *key
             return fail(ctx, VKC_RUNTIME, "batch argsort: output " + std::to_string(i) + " has the wrong length");
     const int64_t total = keys->total;
     if (n == 0 || total == 0) return VKC_OK;
+    for (int i = 0; i < n; ++i) await_write(ctx, outs->arrays[i]);
     if (total >= (int64_t(1) << 32)) return fail(ctx, VKC_USAGE, "batch argsort of 2^32 rows or more");
     const bool cap = capturing(ctx);
     // Scratch (first use only, never during a capture).

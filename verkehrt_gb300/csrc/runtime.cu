@@ -61,7 +61,67 @@ DeviceMem::~DeviceMem() {
 }
 
 Buffer::~Buffer() {
+    // The cached block is reused in the order of the box's stream: after the copies.
+    for (cudaEvent_t *e : {&pending, &reading})
+        if (*e) {
+            if (box) cudaStreamWaitEvent(box->stream, *e, 0);
+            cudaEventDestroy(*e);
+        }
     if (ptr && box) box->give(ptr, bytes);
+}
+
+// Makes `stream` wait for *e (once), then drops the event. Under graph capture an event from
+// outside the capture cannot be waited on by the stream, so the host waits for it instead.
+static bool stream_capturing(cudaStream_t stream);
+// A host wait for an event, allowed during this thread's stream capture.
+static void host_wait(cudaEvent_t e) {
+    cudaStreamCaptureMode mode = cudaStreamCaptureModeRelaxed;
+    cudaThreadExchangeStreamCaptureMode(&mode);
+    cudaEventSynchronize(e);
+    cudaThreadExchangeStreamCaptureMode(&mode);
+}
+static void take_event(cudaStream_t stream, cudaEvent_t *e) {
+    if (!*e) return;
+    if (stream_capturing(stream))
+        host_wait(*e);
+    else
+        cudaStreamWaitEvent(stream, *e, 0);
+    cudaEventDestroy(*e);
+    *e = nullptr;
+}
+
+void await_read(vkc_ctx *ctx, const vkc_array *a) {
+    if (a && a->buf) take_event(ctx->stream, &a->buf->pending);
+}
+
+void await_write(vkc_ctx *ctx, const vkc_array *a) {
+    if (!a || !a->buf) return;
+    take_event(ctx->stream, &a->buf->pending);
+    take_event(ctx->stream, &a->buf->reading);
+}
+
+void await_values(vkc_ctx *ctx, const vkc_value *args, int nargs) {
+    for (int i = 0; i < nargs; ++i)
+        if (args[i].kind == VKC_VALUE_ARRAY && args[i].array) await_read(ctx, args[i].array);
+}
+
+static bool stream_capturing(cudaStream_t stream) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    return cudaStreamIsCapturing(stream, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone;
+}
+
+// The copy streams, made on first use.
+static vkc_status copy_streams(vkc_ctx *ctx) {
+    if (!ctx->h2d) VKC_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->h2d, cudaStreamNonBlocking));
+    if (!ctx->d2h) VKC_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->d2h, cudaStreamNonBlocking));
+    return VKC_OK;
+}
+
+// An event recorded on `stream` now.
+static vkc_status mark(vkc_ctx *ctx, cudaStream_t stream, cudaEvent_t *e) {
+    VKC_CUDA(ctx, cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+    VKC_CUDA(ctx, cudaEventRecord(*e, stream));
+    return VKC_OK;
 }
 
 vkc_status fail(vkc_ctx *ctx, vkc_status st, const std::string &msg) {
@@ -456,6 +516,11 @@ vkc_status vkc_open(int device, vkc_ctx **out) {
 void vkc_close(vkc_ctx *ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
+    for (cudaStream_t cs : {ctx->h2d, ctx->d2h})
+        if (cs) {
+            cudaStreamSynchronize(cs);
+            cudaStreamDestroy(cs);
+        }
     cudaStreamSynchronize(ctx->stream);
     if (ctx->scratch.ptr) cudaFreeAsync(ctx->scratch.ptr, ctx->stream);
     if (ctx->flags.ptr) cudaFreeAsync(ctx->flags.ptr, ctx->stream);
@@ -511,6 +576,8 @@ vkc_status vkc_tune_get(const vkc_ctx *ctx, const char *knob, int size_class, in
 
 vkc_status vkc_synchronize(vkc_ctx *ctx) {
     VKC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (ctx->h2d) VKC_CUDA(ctx, cudaStreamSynchronize(ctx->h2d));
+    if (ctx->d2h) VKC_CUDA(ctx, cudaStreamSynchronize(ctx->d2h));
     return VKC_OK;
 }
 
@@ -543,20 +610,76 @@ vkc_status vkc_array_upload(vkc_ctx *ctx, vkc_type type, const void *host, int64
                             vkc_array **out) {
     vkc_status st = new_array(ctx, type, len, false, out);
     if (st) return st;
-    if (len)
-        VKC_CUDA(ctx, cudaMemcpyAsync((*out)->data(), host,
-                                      static_cast<size_t>(len) * type_width(type),
-                                      cudaMemcpyHostToDevice, ctx->stream));
+    const size_t bytes = static_cast<size_t>(len) * type_width(type);
+    if (bytes >= (size_t(1) << 20) && !stream_capturing(ctx->stream) && !copy_streams(ctx)) {
+        // On the upload stream, after the buffer's allocation (ordered on the context stream);
+        // the first kernel that reads the array waits for the copy's event.
+        cudaEvent_t ready;
+        if ((st = mark(ctx, ctx->stream, &ready))) return st;
+        cudaStreamWaitEvent(ctx->h2d, ready, 0);
+        cudaEventDestroy(ready);
+        VKC_CUDA(ctx, cudaMemcpyAsync((*out)->data(), host, bytes, cudaMemcpyHostToDevice, ctx->h2d));
+        return mark(ctx, ctx->h2d, &(*out)->buf->pending);
+    }
+    if (len) VKC_CUDA(ctx, cudaMemcpyAsync((*out)->data(), host, bytes, cudaMemcpyHostToDevice, ctx->stream));
     return VKC_OK;
 }
 
 vkc_status vkc_array_download(vkc_ctx *ctx, const vkc_array *a, void *host, int64_t capacity) {
     if (!a) return fail(ctx, VKC_USAGE, "null array handle");
     int64_t n = a->len < capacity ? a->len : capacity;
+    await_read(ctx, a);
     if (n > 0)
         VKC_CUDA(ctx, cudaMemcpyAsync(host, a->data(), static_cast<size_t>(n) * type_width(a->type),
                                       cudaMemcpyDeviceToHost, ctx->stream));
     VKC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return VKC_OK;
+}
+
+vkc_status vkc_array_download_start(vkc_ctx *ctx, const vkc_array *a, void *host, int64_t capacity, vkc_copy **out) {
+    if (!out) return VKC_USAGE;
+    *out = nullptr;
+    if (!a) return fail(ctx, VKC_USAGE, "null array handle");
+    if (stream_capturing(ctx->stream)) return fail(ctx, VKC_USAGE, "vkc_array_download_start during a stream capture");
+    vkc_status st;
+    if ((st = copy_streams(ctx))) return st;
+    // After the kernels queued so far (which made the array) and any upload into it.
+    cudaEvent_t ready;
+    if ((st = mark(ctx, ctx->stream, &ready))) return st;
+    cudaStreamWaitEvent(ctx->d2h, ready, 0);
+    cudaEventDestroy(ready);
+    if (a->buf && a->buf->pending) cudaStreamWaitEvent(ctx->d2h, a->buf->pending, 0);
+    const int64_t n = a->len < capacity ? a->len : capacity;
+    if (n > 0)
+        VKC_CUDA(ctx, cudaMemcpyAsync(host, a->data(), static_cast<size_t>(n) * type_width(a->type),
+                                      cudaMemcpyDeviceToHost, ctx->d2h));
+    auto *c = new vkc_copy{const_cast<vkc_array *>(a), nullptr};
+    if ((st = mark(ctx, ctx->d2h, &c->done))) {
+        delete c;
+        return st;
+    }
+    if (a->buf) {
+        // A later write to the array waits for this read (the copy stream runs in order, so
+        // the newest event covers the earlier downloads).
+        if (a->buf->reading) cudaEventDestroy(a->buf->reading);
+        if ((st = mark(ctx, ctx->d2h, &a->buf->reading))) {
+            cudaEventDestroy(c->done);
+            delete c;
+            return st;
+        }
+    }
+    vkc_array_retain(c->array);
+    *out = c;
+    return VKC_OK;
+}
+
+vkc_status vkc_copy_wait(vkc_ctx *ctx, vkc_copy *c) {
+    if (!c) return VKC_USAGE;
+    const cudaError_t e = cudaEventSynchronize(c->done);
+    cudaEventDestroy(c->done);
+    vkc_array_release(c->array);
+    delete c;
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "vkc_copy_wait");
     return VKC_OK;
 }
 
@@ -580,7 +703,11 @@ vkc_status vkc_array_slice(vkc_ctx *ctx, const vkc_array *a, int64_t start, int6
 
 int64_t vkc_array_len(const vkc_array *a) { return a ? a->len : 0; }
 vkc_type vkc_array_type(const vkc_array *a) { return a ? a->type : VKC_F64; }
-void *vkc_array_device_ptr(const vkc_array *a) { return a ? a->data() : nullptr; }
+void *vkc_array_device_ptr(const vkc_array *a) {
+    // The address may be used on any stream: an upload in flight finishes first.
+    if (a && a->buf && a->buf->pending) host_wait(a->buf->pending);
+    return a ? a->data() : nullptr;
+}
 void vkc_array_retain(vkc_array *a) {
     if (a) a->refs.fetch_add(1);
 }
@@ -616,6 +743,7 @@ vkc_status vkc_call(vkc_ctx *ctx, int id, const vkc_value *args, int nargs, vkc_
     const KernelDef *d = def_of(id);
     if (!d) return fail(ctx, VKC_USAGE, "unknown kernel id " + std::to_string(id));
     memset(out, 0, sizeof *out);
+    await_values(ctx, args, nargs);
     if (d->cls == VKC_WHOLE) {
         // Whole kernels check their arguments themselves (dispatch.rs:69-73).
         if (static_cast<int>(d->inputs.size()) != nargs)
@@ -719,6 +847,7 @@ static void to_args(const vkc_value *args, int nargs, std::vector<Arg> *call) {
 }
 
 vkc_status vkc_reducer_update(vkc_reducer *r, const vkc_value *args, int nargs) {
+    await_values(r->ctx, args, nargs);
     std::vector<Arg> call;
     to_args(args, nargs, &call);
     return r->impl->update(r->ctx, call.data(), nargs);
@@ -752,6 +881,8 @@ vkc_status vkc_scanner_update(vkc_scanner *s, const vkc_value *args, int nargs, 
     std::vector<Arg> call;
     to_args(args, nargs, &call);
     if (!out) return fail(s->ctx, VKC_USAGE, "null array handle");
+    await_values(s->ctx, args, nargs);
+    await_write(s->ctx, out);
     return s->impl->update(s->ctx, call.data(), nargs, out);
 }
 
@@ -786,6 +917,7 @@ vkc_status vkc_select_tile(vkc_ctx *ctx, int id, const vkc_value *args, int narg
     int64_t rows;
     vkc_status st = prepare(ctx, *d, args, nargs, &call, &rows);
     if (st) return st;
+    await_values(ctx, args, nargs);
     return d->sel(ctx, call.data(), nargs, base, &out->b);
 }
 
@@ -808,6 +940,8 @@ vkc_status vkc_elementwise_tile(vkc_ctx *ctx, int id, const vkc_value *args, int
                                           " rows for a destination of " + std::to_string(out->len) +
                                           " rows");
     if (rows == 0) return VKC_OK;
+    await_values(ctx, args, nargs);
+    await_write(ctx, out);
     return d->elem(ctx, call.data(), nargs, rows, out);
 }
 

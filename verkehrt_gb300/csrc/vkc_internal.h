@@ -72,11 +72,16 @@ struct DeviceMem {
     ~DeviceMem();
 };
 
-// A device allocation shared by an array and its views.
+// A device allocation shared by an array and its views. Copies on the context's copy streams
+// leave events here: `pending` until an upload has written the buffer, `reading` until an
+// asynchronous download has read it. Work on the context stream waits for them when it first
+// reads (pending) or writes (both) the buffer, and the buffer returns to the cache after them.
 struct Buffer {
     void *ptr = nullptr;
     size_t bytes = 0;
     std::shared_ptr<StreamBox> box;
+    cudaEvent_t pending = nullptr;
+    cudaEvent_t reading = nullptr;
     ~Buffer();
 };
 
@@ -92,6 +97,12 @@ struct vkc_array {
         return buf && buf->ptr ? static_cast<char *>(buf->ptr) + offset * vkc::type_width(type)
                                : nullptr;
     }
+};
+
+// An asynchronous download in flight: the array it reads and the copy's completion event.
+struct vkc_copy {
+    vkc_array *array;
+    cudaEvent_t done;
 };
 
 namespace vkc {
@@ -141,6 +152,9 @@ struct vkc_ctx {
     cudaEvent_t io_ev[2] = {nullptr, nullptr};
     // Launch shapes per size class: the committed autotuner table, or overrides.
     vkc::Tuning tuning = vkc::tune_defaults();
+    // Copy streams (made on first use): uploads of at least 1 MiB, and asynchronous downloads,
+    // so that copies in both directions overlap each other and the kernels.
+    cudaStream_t h2d = nullptr, d2h = nullptr;
 };
 
 namespace vkc {
@@ -179,6 +193,11 @@ vkc_status pinned(vkc_ctx *ctx, size_t bytes, void **out);
 uint32_t next_epoch(vkc_ctx *ctx);
 // Reads and clears the device status after the stream's work completes.
 vkc_status read_status(vkc_ctx *ctx, DevStatus *out);
+// Orders the context stream after the copies of an array's buffer: before it reads the array
+// (an upload in flight), or writes it (an upload or an asynchronous download in flight).
+void await_read(vkc_ctx *ctx, const vkc_array *a);
+void await_write(vkc_ctx *ctx, const vkc_array *a);
+void await_values(vkc_ctx *ctx, const vkc_value *args, int nargs);
 // Checks a kernel launch and counts it.
 vkc_status launched(vkc_ctx *ctx, const char *what);
 
