@@ -492,9 +492,10 @@ def run_e2e_step(ctx, n, hin):
 # ---------------------------------------------------------------------------- CPU baseline
 
 
-def cpu_baseline(n_sample, budget_s=12.0):
-    """Times the oracle port of the reference's scalar entries (one thread, as the reference
-    runs) over the same sweep at a sample size. Returns (GB/s, description)."""
+def cpu_baseline(n_sample, budget_s=12.0, barrier=None):
+    """Times the oracle port of the reference's scalar entries (one thread, as each of the
+    reference's kernels runs) over the same sweep at a sample size. Returns (GB/s, passes).
+    With `barrier`, the timing starts when every replica process has its inputs."""
     import oracle
 
     x, y = oracle.rand_f64(n_sample, 1), oracle.rand_f64(n_sample, 2)
@@ -520,6 +521,8 @@ def cpu_baseline(n_sample, budget_s=12.0):
         (lambda: oracle.reduce_add_f64(oracle.mul_f64(x, y)), 32 * n),
     ]
     total_b, total_t, passes = 0, 0.0, 0
+    if barrier is not None:
+        barrier.wait()
     t_start = time.perf_counter()
     while passes < 2 or (time.perf_counter() - t_start < budget_s and passes < 50):
         for fn, b in steps:
@@ -529,6 +532,37 @@ def cpu_baseline(n_sample, budget_s=12.0):
             total_b += b if b is not None else 8 * n + 8 * len(r)
         passes += 1
     return total_b / total_t / 1e9, passes
+
+
+def _cpu_replica(n_sample, budget_s, barrier, results):
+    sys.path.insert(0, ROOT)
+    results.put(cpu_baseline(n_sample, budget_s, barrier))
+
+
+def cpu_replicas(n_sample, budget_s, procs):
+    """The oracle port on `procs` host processes at once, each over its own copy of the sample
+    (the reference's programs are Send + Sync, so a host runs independent executions side by
+    side). Returns (aggregate GB/s, total passes)."""
+    if procs <= 1:
+        return cpu_baseline(n_sample, budget_s)
+    import multiprocessing
+
+    mp = multiprocessing.get_context("spawn")
+    barrier, results = mp.Barrier(procs), mp.Queue()
+    ps = [mp.Process(target=_cpu_replica, args=(n_sample, budget_s, barrier, results)) for _ in range(procs)]
+    for p in ps:
+        p.start()
+    got = [results.get(timeout=budget_s + 600) for _ in ps]
+    for p in ps:
+        p.join(timeout=60)
+    return sum(g for g, _ in got), sum(k for _, k in got)
+
+
+def host_cores():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
 
 
 # ---------------------------------------------------------------------------- main
@@ -579,6 +613,8 @@ def main():
     ap.add_argument("--n", type=int, default=1 << 28)
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--cpu-sample", type=int, default=1 << 23)
+    ap.add_argument("--cpu-procs", type=int, default=0,
+                    help="host processes of the reference arm (0: every core this process may use)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--sort-n", type=int, default=1 << 27, help="0 skips the argsort/group-by section")
     ap.add_argument("--batch-arrays", type=int, default=4096, help="0 skips the batched section")
@@ -596,15 +632,17 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        gbs, passes = cpu_baseline(args.cpu_sample, budget_s=max(3.0, 2.0 * args.steps))
-        sample = "oracle port of the scalar entries, sweep at n=2^%d, %d passes" % (
-            args.cpu_sample.bit_length() - 1, passes)
+        procs = args.cpu_procs or host_cores()
+        gbs, passes = cpu_replicas(args.cpu_sample, max(3.0, 2.0 * args.steps), procs)
+        sample = ("oracle port of the scalar entries, sweep at n=2^%d, %d processes side by side (one per "
+                  "host core, each its own copy of the sample), %d passes in all" % (
+                      args.cpu_sample.bit_length() - 1, procs, passes))
         line = {"impl": "reference", "metric": METRIC, "value": round(gbs, 3), "unit": UNIT,
                 "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64+i64",
                 "data": "synthetic (seeded rand_f64/rand_i64, the reference generators)",
                 "config": config,
-                "cpu_baseline": {"value": round(gbs, 3), "unit": UNIT, "cores": 1, "kind": "port",
+                "cpu_baseline": {"value": round(gbs, 3), "unit": UNIT, "cores": procs, "kind": "port",
                                  "sample": sample},
                 "e2e": {"value": round(gbs, 3), "unit": UNIT, "h2d_bytes_per_step": 0,
                         "d2h_bytes_per_step": 0}}

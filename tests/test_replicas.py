@@ -58,7 +58,7 @@ def test_reference_arm_runs_on_rank_zero_only():
     pytest.importorskip("torch")
     port = free_port()
     cmd = [sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--gpus", "2", "--steps", "1",
-           "--warmup", "3", "--cpu-sample", str(1 << 16)]
+           "--warmup", "3", "--cpu-sample", str(1 << 16), "--cpu-procs", "2"]
     procs = []
     for r in range(2):
         env = dict(os.environ, WORLD_SIZE="2", RANK=str(r), LOCAL_RANK=str(r), MASTER_ADDR="127.0.0.1",
@@ -70,5 +70,6 @@ def test_reference_arm_runs_on_rank_zero_only():
     assert len(lines) == 1
     line = json.loads(lines[0])
     assert line["impl"] == "reference" and line["n_gpus"] == 2 and line["value"] > 0
-    assert line["cpu_baseline"]["kind"] == "port" and line["e2e"]["h2d_bytes_per_step"] == 0
+    assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] == 2
+    assert line["e2e"]["h2d_bytes_per_step"] == 0
     assert not [ln for ln in outs[1][0].splitlines() if ln.strip()]
