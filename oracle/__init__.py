@@ -61,6 +61,7 @@ def lib():
         L.orc_gather.argtypes = [P, ctypes.c_int, I64, P, I64, P, ctypes.c_char_p]
         L.orc_histogram.argtypes = [P, I64, I64, P, ctypes.c_char_p]
         L.orc_reduce_into_add_i64.argtypes = [P, P, I64, I64, P, ctypes.c_char_p]
+        L.orc_reduce_into_add_f64.argtypes = [P, P, I64, I64, P, ctypes.c_char_p]
         L.orc_argsort_i64.argtypes = [P, I64, P, ctypes.c_char_p]
         L.orc_argsort_reference_i64.argtypes = [P, I64, P]
         L.orc_group_id_i64.argtypes = [P, I64, P, ctypes.c_char_p]
@@ -279,6 +280,24 @@ def reduce_into_add_i64(keys, vals, buckets):
     out = np.empty(max(0, min(buckets, 1 << 28)), dtype=np.int64)
     buf = ctypes.create_string_buffer(ERR_LEN)
     _err(lib().orc_reduce_into_add_i64(_p(keys), _p(vals), len(keys), buckets, _p(out), buf), buf)
+    return out
+
+
+def reduce_into_add_f64(keys, vals, buckets):
+    """Per-bucket float sums in the candidate stripe order of the reference's tier-2 notes,
+    with the canonical tail rule (oracle.c orc_reduce_into_add_f64)."""
+    keys, vals = _i64(keys), np.ascontiguousarray(vals, dtype=np.float64)
+    if len(keys) != len(vals):
+        buf = ctypes.create_string_buffer(ERR_LEN)
+        tmp = np.empty(max(0, min(buckets, 1 << 20)), dtype=np.int64)
+        if buckets >= 0 and buckets <= (1 << 20):
+            _err(lib().orc_histogram(_p(keys), len(keys), buckets, _p(tmp), buf), buf)
+        raise OracleError("length mismatch: %d keys for %d values" % (len(keys), len(vals)))
+    if buckets > 1 << 28:
+        _huge_buckets(keys, buckets)
+    out = np.empty(max(0, min(buckets, 1 << 28)), dtype=np.float64)
+    buf = ctypes.create_string_buffer(ERR_LEN)
+    _err(lib().orc_reduce_into_add_f64(_p(keys), _p(vals), len(keys), buckets, _p(out), buf), buf)
     return out
 
 

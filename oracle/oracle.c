@@ -362,6 +362,38 @@ int orc_reduce_into_add_i64(const int64_t *keys, const int64_t *vals, int64_t n,
     return 0;
 }
 
+/* reduce_into with f64 add: the reference has no such kernel (scan.rs:408-415). Its tier-2
+ * design notes (docs/superpowers/specs/2026-10-31-verkehrt-tier2-design.md:171-172) give the
+ * candidate order restated here: rows below b = n - n % 16 go to lane i % 16 of their bucket,
+ * each lane adds its rows in index order from +0.0, the lanes combine pairwise (+8, +4, +2, +1),
+ * and the bucket's rows from b on fold into the result in index order, the canonical sum's tail
+ * rule (reduce.rs:77-91, finish_lanes). With every key equal this is reduce_add_f64, bit for
+ * bit, the property the notes give. Empty buckets hold +0.0. */
+int orc_reduce_into_add_f64(const int64_t *keys, const double *vals, int64_t n, int64_t buckets,
+                            double *out, char *err) {
+    if (checked_keys(keys, n, buckets, err)) return 1;
+    if (check_i64_array_size(buckets, err)) return 1;
+    double *lanes = (double *)calloc((size_t)buckets * 16 + 1, sizeof(double));
+    if (!lanes) {
+        snprintf(err, ORC_ERR_LEN, "cannot allocate an array of %" PRId64 " elements", buckets * 16);
+        return 1;
+    }
+    const int64_t b = n - n % 16;
+    for (int64_t i = 0; i < b; ++i) {
+        double *l = lanes + keys[i] * 16 + (i & 15);
+        *l = *l + vals[i];
+    }
+    for (int64_t k = 0; k < buckets; ++k) {
+        double *l = lanes + k * 16;
+        for (int step = 8; step > 0; step /= 2)
+            for (int j = 0; j < step; ++j) l[j] = l[j] + l[j + step];
+        out[k] = l[0];
+    }
+    for (int64_t i = b; i < n; ++i) out[keys[i]] = out[keys[i]] + vals[i];
+    free(lanes);
+    return 0;
+}
+
 /* ---------------------------------------------------------------- argsort */
 
 typedef struct {

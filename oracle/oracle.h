@@ -80,6 +80,8 @@ int orc_gather(const void *src, int width, int64_t nsrc, const int64_t *idx, int
                void *out, char *err);
 /* index.rs:116-155 and :194-222 */
 int orc_histogram(const int64_t *keys, int64_t n, int64_t buckets, int64_t *out, char *err);
+int orc_reduce_into_add_f64(const int64_t *keys, const double *vals, int64_t n, int64_t buckets,
+                            double *out, char *err);
 int orc_reduce_into_add_i64(const int64_t *keys, const int64_t *vals, int64_t n,
                             int64_t buckets, int64_t *out, char *err);
 

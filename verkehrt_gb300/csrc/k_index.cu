@@ -395,6 +395,25 @@ __global__ void __launch_bounds__(256) bucket_kernel(const long long *__restrict
         if (bins[b]) atomicAdd(out + b, bins[b]);
 }
 
+// The reference's error for the first key outside [0, nb) (checked_keys, index.rs:116-130):
+// *found and VKC_RUNTIME with the message, or VKC_OK when every key is in range.
+vkc_status bucket_key_error(vkc_ctx *ctx, const long long *k, int64_t n, int64_t nb, bool *found) {
+    *found = false;
+    if (n == 0) return VKC_OK;
+    int grid = stream_grid(ctx, n, 256, 8, 4096);
+    keys_check_kernel<<<grid, 256, 0, ctx->stream>>>(k, n, static_cast<uint64_t>(nb), ctx->status);
+    vkc_status s2 = launched(ctx, "keys_check");
+    if (s2) return s2;
+    DevStatus ds;
+    if ((s2 = read_status(ctx, &ds))) return s2;
+    if (ds.first_bad == ~0ull) return VKC_OK;
+    int64_t v;
+    if ((s2 = read_i64(ctx, k, ds.first_bad, &v))) return s2;
+    *found = true;
+    return fail(ctx, VKC_RUNTIME, "bucket key " + std::to_string(v) + " out of range for " +
+                                      std::to_string(nb) + " buckets");
+}
+
 // index.rs:116-130 (checked_keys) then the result allocation (value.rs:285-307). The key check
 // precedes allocation errors; a length mismatch of reduce_into follows it (index.rs:203-210).
 static vkc_status run_buckets(vkc_ctx *ctx, const vkc_array *keys, const vkc_array *vals, int64_t nb,
@@ -403,22 +422,7 @@ static vkc_status run_buckets(vkc_ctx *ctx, const vkc_array *keys, const vkc_arr
     if (nb < 0) return fail(ctx, VKC_RUNTIME, "negative bucket count " + std::to_string(nb));
     int64_t n = keys->len;
     const auto *k = static_cast<const long long *>(keys->data());
-    auto key_error = [&](bool *found) -> vkc_status {
-        *found = false;
-        if (n == 0) return VKC_OK;
-        int grid = stream_grid(ctx, n, 256, 8, 4096);
-        keys_check_kernel<<<grid, 256, 0, ctx->stream>>>(k, n, static_cast<uint64_t>(nb), ctx->status);
-        vkc_status s2 = launched(ctx, "keys_check");
-        if (s2) return s2;
-        DevStatus ds;
-        if ((s2 = read_status(ctx, &ds))) return s2;
-        if (ds.first_bad == ~0ull) return VKC_OK;
-        int64_t v;
-        if ((s2 = read_i64(ctx, k, ds.first_bad, &v))) return s2;
-        *found = true;
-        return fail(ctx, VKC_RUNTIME, "bucket key " + std::to_string(v) + " out of range for " +
-                                          std::to_string(nb) + " buckets");
-    };
+    auto key_error = [&](bool *found) -> vkc_status { return bucket_key_error(ctx, k, n, nb, found); };
     bool found;
     if (vals && vals->len != n) {
         if ((st = key_error(&found))) return st;

@@ -70,6 +70,9 @@ struct KernelDef {
     WholeFn whole = nullptr;
 };
 
+// The table's entry of that name (for entries built from other entries), or nullptr.
+const KernelDef *kernel_def(const char *name);
+
 // Registration by family (called once, in this order, to build the table).
 void register_construct(std::vector<KernelDef> &t);
 void register_reduce(std::vector<KernelDef> &t);
@@ -79,6 +82,7 @@ void register_index(std::vector<KernelDef> &t);
 void register_sort(std::vector<KernelDef> &t);
 void register_group(std::vector<KernelDef> &t);
 void register_io(std::vector<KernelDef> &t);
+void register_reduce_into_f64(std::vector<KernelDef> &t);
 void register_elementwise(std::vector<KernelDef> &t);
 
 // Argument helpers with the reference's messages (src/kernels/scalar/elementwise.rs:172-199).

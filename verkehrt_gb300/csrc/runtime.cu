@@ -350,6 +350,7 @@ static const std::vector<KernelDef> &table() {
         register_group(v);
         register_elementwise(v);
         register_io(v);
+        register_reduce_into_f64(v);
         return v;
     }();
     return t;
@@ -359,6 +360,12 @@ static const KernelDef *def_of(int id) {
     const auto &t = table();
     if (id < 0 || id >= static_cast<int>(t.size())) return nullptr;
     return &t[static_cast<size_t>(id)];
+}
+
+const KernelDef *kernel_def(const char *name) {
+    for (const KernelDef &d : table())
+        if (d.name == name) return &d;
+    return nullptr;
 }
 
 // kind_error, src/kernels/dispatch.rs:324-330.
