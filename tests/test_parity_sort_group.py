@@ -112,6 +112,21 @@ def test_group_id_large(ctx):
         assert np.array_equal(got, oracle.group_id_i64(xs)), mod
 
 
+def test_group_id_region_partitioned(ctx):
+    # Many distinct single keys on 2^22 rows or more take the region-partitioned tables: keys
+    # repeated far apart (first occurrences in earlier tiles), the free-slot pattern as a key,
+    # one key in the first and the last row, and a ragged last tile.
+    n = (1 << 23) + 77
+    xs = (oracle.rand_i64(n, 15).view(np.uint64) % np.uint64(1 << 22)).astype(np.int64)
+    empty = np.uint64(0x8080808080808080).view(np.int64)
+    xs[[5, 70_000, 4_000_000, n - 2]] = empty
+    xs[0] = xs[n - 1] = 123_456_789_012
+    got = ctx.call("group_id_i64", ctx.upload(xs)).numpy()
+    assert np.array_equal(got, oracle.group_id_i64(xs))
+    u = oracle.rand_i64(1 << 22, 16)  # every key distinct (almost)
+    assert np.array_equal(ctx.call("group_id_i64", ctx.upload(u)).numpy(), oracle.group_id_i64(u))
+
+
 def test_group_id_free_slot_pattern_and_table_switch(ctx):
     # The key whose bytes are all 0x80 marks a free slot of the GPU table; rows holding it take
     # their own slot. Pairs with one such half probe like any other pair.

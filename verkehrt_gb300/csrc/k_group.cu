@@ -295,6 +295,291 @@ __global__ void __launch_bounds__(256) gi_clear_kernel(ulonglong2 *__restrict__ 
         p[i] = (w == 2 || (i & 1) == 0) ? key : rest;
 }
 
+// ------------------------------------------------------------------ region-partitioned tables
+//
+// Many distinct keys (the first table gave up) on a large input: a table of 2n slots is far
+// beyond L2, so each probe, claim and smallest-row update is a DRAM burst. Instead the rows are
+// put in region order by the top GR_BITS bits of their key's hash (count per tile and region,
+// one exclusive scan, a partition staged in shared memory that writes each region's runs of
+// (key, row) and each row's slot in its tile's region-sorted order), and then the regions go
+// through three sub-tables in rotation that stay in L2, one launch per region: a region's
+// sub-table is cleared, filled (claim by 128-bit CAS, smallest row by atomicMin) and read back
+// (each pair's smallest row of its key) in three consecutive launches, each of which also does
+// the other two jobs for the neighbouring regions. The smallest rows go back to row order
+// through the tiles' staged runs, and the numbering runs in row order as in gi_number_kernel,
+// except that a row whose key first occurs in an earlier tile reads its id from the output row
+// of that first occurrence (written by then, or awaited with a bounded wait).
+constexpr int GR_BITS = 8, GR_NB = 1 << GR_BITS;
+constexpr int GR_THREADS = 256, GR_ITEMS = 16, GR_TILE = GR_THREADS * GR_ITEMS;
+
+__device__ __forceinline__ unsigned gr_region(unsigned long long key) {
+    return static_cast<unsigned>(gmix(key) >> (64 - GR_BITS));
+}
+
+// Warp 0: exclusive prefix of GR_NB counts get(b) into s_start[0 .. GR_NB - 1], the total into
+// s_start[GR_NB].
+template <class Get> __device__ __forceinline__ void gr_starts(Get get, unsigned *s_start) {
+    const int lane = threadIdx.x & 31;
+    unsigned run = 0;
+#pragma unroll
+    for (int b0 = 0; b0 < GR_NB; b0 += 32) {
+        const unsigned c = get(b0 + lane);
+        unsigned x = c;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned y = __shfl_up_sync(FULL, x, o);
+            if (lane >= o) x += y;
+        }
+        s_start[b0 + lane] = run + x - c;
+        run += __shfl_sync(FULL, x, 31);
+    }
+    if (lane == 0) s_start[GR_NB] = run;
+}
+
+__device__ __forceinline__ int gr_region_of(const unsigned *s_start, unsigned v) {
+    int lo = 0, hi = GR_NB;
+#pragma unroll
+    for (int it = 0; it < GR_BITS; ++it) {
+        const int mid = (lo + hi) >> 1;
+        if (s_start[mid] <= v) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+__global__ void __launch_bounds__(GR_THREADS) gr_count_kernel(const long long *__restrict__ keys, int64_t n, int tiles,
+                                                              unsigned *__restrict__ counts) {
+    __shared__ unsigned h[GR_NB];
+    if (threadIdx.x < GR_NB) h[threadIdx.x] = 0;
+    __syncthreads();
+    const int64_t base = static_cast<int64_t>(blockIdx.x) * GR_TILE;
+#pragma unroll
+    for (int j = 0; j < GR_ITEMS; ++j) {
+        const int64_t r = base + j * GR_THREADS + threadIdx.x;
+        if (r < n) atomicAdd(&h[gr_region(static_cast<unsigned long long>(__ldcs(keys + r)))], 1u);
+    }
+    __syncthreads();
+    if (threadIdx.x < GR_NB) counts[static_cast<int64_t>(threadIdx.x) * tiles + blockIdx.x] = h[threadIdx.x];
+}
+
+__global__ void __launch_bounds__(GR_THREADS) gr_partition_kernel(const long long *__restrict__ keys, int64_t n,
+                                                                  int tiles, const unsigned *__restrict__ offs,
+                                                                  unsigned long long *__restrict__ keys_p,
+                                                                  unsigned *__restrict__ rows_p,
+                                                                  unsigned short *__restrict__ loc) {
+    __shared__ unsigned s_cnt[GR_NB], s_start[GR_NB + 1], s_goff[GR_NB];
+    __shared__ unsigned long long s_key[GR_TILE];
+    __shared__ unsigned short s_rel[GR_TILE];
+    __shared__ unsigned char s_reg[GR_TILE];
+    if (threadIdx.x < GR_NB) {
+        s_cnt[threadIdx.x] = 0;
+        s_goff[threadIdx.x] = offs[static_cast<int64_t>(threadIdx.x) * tiles + blockIdx.x];
+    }
+    __syncthreads();
+    const int64_t base = static_cast<int64_t>(blockIdx.x) * GR_TILE;
+    unsigned long long k[GR_ITEMS];
+    unsigned rk[GR_ITEMS];
+#pragma unroll
+    for (int j = 0; j < GR_ITEMS; ++j) {
+        const int64_t r = base + j * GR_THREADS + threadIdx.x;
+        k[j] = r < n ? static_cast<unsigned long long>(__ldcs(keys + r)) : 0ull;
+    }
+    // Slots within the tile's region runs, in any order: the ids do not depend on it.
+#pragma unroll
+    for (int j = 0; j < GR_ITEMS; ++j)
+        rk[j] = base + j * GR_THREADS + threadIdx.x < n ? atomicAdd(&s_cnt[gr_region(k[j])], 1u) : 0u;
+    __syncthreads();
+    if (threadIdx.x < 32) gr_starts([&](int b) { return s_cnt[b]; }, s_start);
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < GR_ITEMS; ++j) {
+        const int rel = j * GR_THREADS + threadIdx.x;
+        if (base + rel >= n) continue;
+        const unsigned b = gr_region(k[j]);
+        const unsigned l = s_start[b] + rk[j];
+        loc[base + rel] = static_cast<unsigned short>(l);
+        s_key[l] = k[j];
+        s_rel[l] = static_cast<unsigned short>(rel);
+        s_reg[l] = static_cast<unsigned char>(b);
+    }
+    __syncthreads();
+    const int rows = static_cast<int>(s_start[GR_NB]);
+    for (int l = threadIdx.x; l < rows; l += GR_THREADS) {
+        const unsigned b = s_reg[l];
+        const unsigned p = s_goff[b] + static_cast<unsigned>(l) - s_start[b];
+        keys_p[p] = s_key[l];
+        rows_p[p] = static_cast<unsigned>(base) + s_rel[l];
+    }
+}
+
+// One launch per step k of the regions' pipeline over three sub-tables: the inserts of region k
+// (into table k % 3, cleared by the previous step), the smallest rows of region k - 1 (table
+// (k - 1) % 3, whose inserts finished with the previous step) and the clearing of table
+// (k + 1) % 3 (last read by the previous step) for region k + 1. Jobs with no rows are empty.
+struct GrStep {
+    unsigned ins0, ins1;  // positions of region k
+    unsigned min0, min1;  // positions of region k - 1
+    GroupTable ins, min, clr;
+    int64_t clr_slots;  // 0: nothing to clear
+};
+
+__global__ void __launch_bounds__(256) gr_step_kernel(const unsigned long long *__restrict__ keys_p,
+                                                      const unsigned *__restrict__ rows_p,
+                                                      unsigned *__restrict__ slot_p, unsigned *__restrict__ min_p,
+                                                      GrStep s, DevStatus *st) {
+    const unsigned tid = blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned p = s.ins0 + tid;
+    if (p < s.ins1) {
+        const unsigned long long key = keys_p[p];
+        const unsigned row = rows_p[p];
+        unsigned long long sl = 0;
+        unsigned cur = 0xffffffffu;
+        if (key != GI_EMPTY) {
+            sl = gi_first(gmix(key), s.ins.mask);
+            for (unsigned long long probes = 0;; ++probes) {
+                unsigned long long va, vb;
+                cas_pair(s.ins.words + 2 * sl, GI_EMPTY, ~0ull, key, 0xffffffff00000000ull | row, va, vb);
+                if (va == GI_EMPTY) {
+                    cur = row;
+                    break;
+                }
+                if (va == key) {
+                    cur = static_cast<unsigned>(vb);
+                    break;
+                }
+                if (probes >= s.ins.mask) {
+                    set_timeout(st);
+                    break;
+                }
+                sl = gi_next(sl, s.ins.mask);
+            }
+        } else {
+            cur = ld_relaxed32(&s.ins.meta(0)->x);
+        }
+        if (cur > row) atomicMin(&s.ins.meta(sl)->x, row);
+        slot_p[p] = static_cast<unsigned>(sl);
+    }
+    const unsigned q = s.min0 + tid;
+    if (q < s.min1) min_p[q] = s.min.meta(slot_p[q])->x;
+    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    const ulonglong2 free_slot = make_ulonglong2(GI_EMPTY, ~0ull);
+    for (int64_t i = tid; i < s.clr_slots; i += stride) reinterpret_cast<ulonglong2 *>(s.clr.words)[i] = free_slot;
+}
+
+// Row order again: each tile gathers its runs of min_p into shared memory in region-sorted
+// order, then row i takes staged[loc[i]].
+__global__ void __launch_bounds__(GR_THREADS) gr_restore_kernel(const unsigned *__restrict__ min_p,
+                                                                const unsigned short *__restrict__ loc,
+                                                                const unsigned *__restrict__ counts,
+                                                                const unsigned *__restrict__ offs, int64_t n,
+                                                                int tiles, unsigned *__restrict__ minrow) {
+    __shared__ unsigned s_start[GR_NB + 1], s_goff[GR_NB];
+    __shared__ unsigned s_vals[GR_TILE];
+    if (threadIdx.x < 32) gr_starts([&](int b) { return counts[static_cast<int64_t>(b) * tiles + blockIdx.x]; }, s_start);
+    if (threadIdx.x < GR_NB) s_goff[threadIdx.x] = offs[static_cast<int64_t>(threadIdx.x) * tiles + blockIdx.x];
+    __syncthreads();
+    const int rows = static_cast<int>(s_start[GR_NB]);
+    unsigned at[GR_ITEMS];
+#pragma unroll
+    for (int j = 0; j < GR_ITEMS; ++j) {
+        const unsigned l = threadIdx.x + j * GR_THREADS;
+        const int b = l < static_cast<unsigned>(rows) ? gr_region_of(s_start, l) : 0;
+        at[j] = s_goff[b] + l - s_start[b];
+    }
+    unsigned v[GR_ITEMS];
+#pragma unroll
+    for (int j = 0; j < GR_ITEMS; ++j) v[j] = threadIdx.x + j * GR_THREADS < rows ? __ldcs(min_p + at[j]) : 0u;
+#pragma unroll
+    for (int j = 0; j < GR_ITEMS; ++j)
+        if (threadIdx.x + j * GR_THREADS < rows) s_vals[threadIdx.x + j * GR_THREADS] = v[j];
+    __syncthreads();
+    const int64_t base = static_cast<int64_t>(blockIdx.x) * GR_TILE;
+#pragma unroll
+    for (int j = 0; j < GR_ITEMS; ++j) {
+        const int64_t r = base + j * GR_THREADS + threadIdx.x;
+        if (r < n) minrow[r] = s_vals[loc[r]];
+    }
+}
+
+// The numbering of gi_number_kernel from each row's smallest row of its key: first occurrences
+// (smallest row = the row) are ranked in row order by a decoupled lookback; a repeat takes the
+// id of its first occurrence, from the tile's bitmap when that is in the same tile, else from
+// the output row of the first occurrence (out starts as all ones; a bounded wait).
+__global__ void __launch_bounds__(GI_THREADS, 4) gr_number_kernel(const unsigned *__restrict__ minrow, int64_t n,
+                                                                  int tiles, unsigned long long *words, unsigned epoch,
+                                                                  unsigned *counters, long long *out, DevStatus *st) {
+    __shared__ unsigned long long s_prefix;
+    __shared__ unsigned s_keep[GI_TILE / 32];
+    __shared__ unsigned s_wpre[GI_TILE / 32];
+    __shared__ long long s_out[GI_THREADS * GI_OUT_STRIDE];
+    const int tile = take_ticket(counters);
+    const int64_t t0 = static_cast<int64_t>(tile) * GI_TILE;
+    const int64_t row0 = t0 + threadIdx.x * GI_ITEMS;
+    unsigned mr[GI_ITEMS];
+    if (row0 + GI_ITEMS <= n) {
+        const uint4 *v = reinterpret_cast<const uint4 *>(minrow + row0);
+#pragma unroll
+        for (int q = 0; q < GI_ITEMS / 4; ++q) {
+            const uint4 w = __ldcs(v + q);
+            mr[4 * q] = w.x;
+            mr[4 * q + 1] = w.y;
+            mr[4 * q + 2] = w.z;
+            mr[4 * q + 3] = w.w;
+        }
+    } else {
+#pragma unroll
+        for (int j = 0; j < GI_ITEMS; ++j) mr[j] = row0 + j < n ? minrow[row0 + j] : 0u;
+    }
+    int rel[GI_ITEMS];
+    unsigned keep = 0;
+#pragma unroll
+    for (int j = 0; j < GI_ITEMS; ++j) {
+        const int64_t r = row0 + j;
+        rel[j] = -1;
+        if (r < n) {
+            rel[j] = static_cast<int>(static_cast<int64_t>(mr[j]) - t0);
+            if (mr[j] == static_cast<unsigned>(r)) keep |= 1u << j;
+        }
+    }
+    const unsigned odd = __shfl_down_sync(FULL, keep, 1);
+    if (!(threadIdx.x & 1)) s_keep[threadIdx.x >> 1] = keep | (odd << 16);
+    unsigned long long c = __popc(keep), tile_count;
+    const unsigned long long off = block_exclusive_sum<unsigned long long>(c, &tile_count);
+    if (!(threadIdx.x & 1)) s_wpre[threadIdx.x >> 1] = static_cast<unsigned>(off);
+    if (threadIdx.x < 32) {
+        unsigned long long pre = lookback_publish<4, CountRec>(words, tile, tile_count, 0ull, epoch, st);
+        if (threadIdx.x == 0) s_prefix = pre;
+    }
+    __syncthreads();
+    const unsigned prefix = static_cast<unsigned>(s_prefix);
+#pragma unroll
+    for (int j = 0; j < GI_ITEMS; ++j) {
+        if (row0 + j >= n) continue;
+        unsigned long long g;
+        if (rel[j] >= 0) {
+            const int w = rel[j] >> 5, bit = rel[j] & 31;
+            g = prefix + s_wpre[w] + __popc(s_keep[w] & ((1u << bit) - 1u));
+        } else {
+            const unsigned long long *p = reinterpret_cast<const unsigned long long *>(out + mr[j]);
+            unsigned it = 0;
+            while ((g = ld_relaxed64(p)) == ~0ull) {
+                if (++it > SPIN_LIMIT) {
+                    set_timeout(st);
+                    break;
+                }
+                backoff(it);
+            }
+        }
+        s_out[threadIdx.x * GI_OUT_STRIDE + j] = static_cast<long long>(g);
+    }
+    __syncthreads();
+    const int rows = static_cast<int>(n - t0 < GI_TILE ? n - t0 : GI_TILE);
+    for (int i = threadIdx.x; i < rows; i += GI_THREADS)
+        st_relaxed64(reinterpret_cast<unsigned long long *>(out + t0 + i),
+                     static_cast<unsigned long long>(s_out[(i / GI_ITEMS) * GI_OUT_STRIDE + (i % GI_ITEMS)]));
+    release_ticket(counters, tiles);
+}
+
 struct GroupScratch {
     vkc_array *words = nullptr;
     void release() {
@@ -327,6 +612,85 @@ static void launch_insert(vkc_ctx *ctx, bool small, const long long *a, const lo
         per_sm = 1;
     const int grid = stream_grid(ctx, n, GI_THREADS, per_sm, GI_THREADS * GI_ROWS);
     kern<<<grid, GI_THREADS, 0, ctx->stream>>>(a, b, n, t, slot_of, flags, ctx->status);
+}
+
+int64_t scan_counts_sum_words(int64_t m);
+void scan_counts(vkc_ctx *ctx, const unsigned *c, int64_t m, unsigned *sums, unsigned *out);
+
+// Single keys, many distinct, at least GR_MIN_ROWS rows: the region-partitioned path above.
+constexpr int64_t GR_MIN_ROWS = int64_t(1) << 22;
+
+static vkc_status run_group_partitioned(vkc_ctx *ctx, const long long *keys, int64_t n, vkc_array *o) {
+    const int tiles = static_cast<int>((n + GR_TILE - 1) / GR_TILE);
+    const int64_t m = static_cast<int64_t>(GR_NB) * tiles;
+    vkc_array *arr[10] = {};
+    auto done = [&](vkc_status st) {
+        for (vkc_array *a : arr)
+            if (a) vkc_array_release(a);
+        return st;
+    };
+    vkc_status st;
+    const int64_t sizes[9] = {m, m, scan_counts_sum_words(m), n, n, (n + 1) / 2, n, n, n};
+    const vkc_type types[9] = {VKC_I32, VKC_I32, VKC_I32, VKC_U64, VKC_I32, VKC_I32, VKC_I32, VKC_I32, VKC_I32};
+    for (int i = 0; i < 9; ++i)
+        if ((st = new_array(ctx, types[i], sizes[i], false, &arr[i]))) return done(st);
+    auto *counts = static_cast<unsigned *>(arr[0]->data());
+    auto *offs = static_cast<unsigned *>(arr[1]->data());
+    auto *keys_p = static_cast<unsigned long long *>(arr[3]->data());
+    auto *rows_p = static_cast<unsigned *>(arr[4]->data());
+    auto *loc = static_cast<unsigned short *>(arr[5]->data());  // n u16 in (n + 1) / 2 words
+    auto *slot_p = static_cast<unsigned *>(arr[6]->data());
+    auto *min_p = static_cast<unsigned *>(arr[7]->data());
+    auto *minrow = static_cast<unsigned *>(arr[8]->data());
+    gr_count_kernel<<<tiles, GR_THREADS, 0, ctx->stream>>>(keys, n, tiles, counts);
+    scan_counts(ctx, counts, m, static_cast<unsigned *>(arr[2]->data()), offs);
+    gr_partition_kernel<<<tiles, GR_THREADS, 0, ctx->stream>>>(keys, n, tiles, offs, keys_p, rows_p, loc);
+    if ((st = launched(ctx, "gr_partition"))) return done(st);
+    // Region starts (offs of each region's first tile) on the host.
+    void *h;
+    if ((st = pinned(ctx, (GR_NB + 1) * sizeof(unsigned), &h))) return done(st);
+    auto *starts = static_cast<unsigned *>(h);
+    VKC_CUDA(ctx, cudaMemcpy2DAsync(starts, sizeof(unsigned), offs, static_cast<size_t>(tiles) * sizeof(unsigned),
+                                    sizeof(unsigned), GR_NB, cudaMemcpyDeviceToHost, ctx->stream));
+    VKC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    std::vector<unsigned> start(starts, starts + GR_NB);
+    start.push_back(static_cast<unsigned>(n));
+    unsigned most = 1;
+    for (int r = 0; r < GR_NB; ++r) most = std::max(most, start[r + 1] - start[r]);
+    uint64_t slots = 2;
+    while (slots < 2ull * most) slots <<= 1;
+    if ((st = new_array(ctx, VKC_U64, static_cast<int64_t>(6 * slots), false, &arr[9]))) return done(st);
+    auto *words = static_cast<unsigned long long *>(arr[9]->data());
+    auto table = [&](int k) { return GroupTable{words + 2 * slots * static_cast<uint64_t>(k % 3), slots - 1, 2}; };
+    gi_clear_kernel<<<stream_grid(ctx, static_cast<int64_t>(slots), 256, 8, 2048), 256, 0, ctx->stream>>>(
+        reinterpret_cast<ulonglong2 *>(table(0).words), static_cast<int64_t>(slots), 2);
+    for (int k = 0; k <= GR_NB; ++k) {
+        GrStep s{};
+        if (k < GR_NB) {
+            s.ins0 = start[k];
+            s.ins1 = start[k + 1];
+        }
+        if (k > 0) {
+            s.min0 = start[k - 1];
+            s.min1 = start[k];
+        }
+        s.ins = table(k);
+        s.min = table(k + 2);  // (k - 1) % 3
+        s.clr = table(k + 1);
+        s.clr_slots = k + 1 < GR_NB ? static_cast<int64_t>(slots) : 0;
+        const unsigned rows = std::max(s.ins1 - s.ins0, s.min1 - s.min0);
+        const unsigned grid = std::max(1u, (rows + 255) / 256);
+        gr_step_kernel<<<grid, 256, 0, ctx->stream>>>(keys_p, rows_p, slot_p, min_p, s, ctx->status);
+    }
+    if ((st = launched(ctx, "gr_regions"))) return done(st);
+    gr_restore_kernel<<<tiles, GR_THREADS, 0, ctx->stream>>>(min_p, loc, counts, offs, n, tiles, minrow);
+    VKC_CUDA(ctx, cudaMemsetAsync(o->data(), 0xff, static_cast<size_t>(n) * 8, ctx->stream));
+    const int gtiles = static_cast<int>((n + GI_TILE - 1) / GI_TILE);
+    unsigned long long *recs;
+    if ((st = rec_arena(ctx, gtiles, &recs))) return done(st);
+    gr_number_kernel<<<gtiles, GI_THREADS, 0, ctx->stream>>>(minrow, n, gtiles, recs, next_epoch(ctx), ctx->counters,
+                                                            static_cast<long long *>(o->data()), ctx->status);
+    return done(launched(ctx, "gr_number"));
 }
 
 static vkc_status run_group(vkc_ctx *ctx, const vkc_array *xa, const vkc_array *xb, vkc_value *out) {
@@ -390,6 +754,22 @@ static vkc_status run_group(vkc_ctx *ctx, const vkc_array *xa, const vkc_array *
         VKC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
         done = static_cast<unsigned *>(h)[1] == 0;
         if (!done) small.release();
+        if (!done && !xb && n >= GR_MIN_ROWS) {
+            // Many distinct single keys: the region-partitioned tables.
+            st = run_group_partitioned(ctx, a, n, o);
+            if (!st) {
+                DevStatus ds;
+                st = read_status(ctx, &ds);
+            }
+            cleanup();
+            if (st) {
+                vkc_array_release(o);
+                return st;
+            }
+            out->kind = VKC_VALUE_ARRAY;
+            out->array = o;
+            return VKC_OK;
+        }
     }
     if (!done) {
         if ((st = new_table(ctx, slots, xb != nullptr, &full, &t))) {
