@@ -305,7 +305,10 @@ __global__ void __launch_bounds__(256) gi_clear_kernel(ulonglong2 *__restrict__ 
 // through three sub-tables in rotation that stay in L2, one launch per region: a region's
 // sub-table is cleared, filled (claim by 128-bit CAS, smallest row by atomicMin) and read back
 // (each pair's smallest row of its key) in three consecutive launches, each of which also does
-// the other two jobs for the neighbouring regions. The smallest rows go back to row order
+// the other two jobs for the neighbouring regions. The launches are bound by the L2's 128-bit
+// CAS operations, not by DRAM: tables at load up to 2/3 (fitting L2 better) made probes longer
+// and the call slower, and so did slots tagged with the region instead of cleared (a read
+// before each CAS). The smallest rows go back to row order
 // through the tiles' staged runs, and the numbering runs in row order as in gi_number_kernel,
 // except that a row whose key first occurs in an earlier tile reads its id from the output row
 // of that first occurrence (written by then, or awaited with a bounded wait).
