@@ -210,6 +210,7 @@ struct CanonWork {
     int *chunkE;               // [16][C] binade of each 32-tile chunk's transfer function
     TF *chunkD;                // [16][C]
     double *gsum;              // [16][G] approximate sum of each group of CAND_GROUP tiles
+    int *flags;                // [T] tiles whose transfer functions are recomputed (K3 again)
 };
 
 constexpr int CAND_GROUP = 1024;  // tiles per K2 block
@@ -272,7 +273,11 @@ __device__ __forceinline__ float approx_row(const RowArgs &a, unsigned long long
     return approx_f32(xv);
 }
 
-// K1: the approximate lane sums of every tile (float sums of float images, one read).
+// K1: the approximate lane sums of every tile (float sums of float images), from the first
+// 16-row block of each segment only (one 128-byte line in CT_SEG_BLOCKS, scaled up): the sums
+// choose K3's candidate binades, and K3's own sums check them afterwards (K2c), so an estimate
+// that sampling got wrong costs a second transfer function for that tile, never exactness.
+constexpr int CT_SAMPLE = CT_SEG_BLOCKS;
 template <int OP, bool ALIGNED>
 __global__ void __launch_bounds__(CT_THREADS) canon_apx_kernel(RowArgs args, int64_t nb, int T, CanonWork wk) {
     __shared__ float s_apx[CT_SEGS][16];
@@ -281,7 +286,7 @@ __global__ void __launch_bounds__(CT_THREADS) canon_apx_kernel(RowArgs args, int
     float a0 = 0.f, a1 = 0.f;
     const int64_t blk0 = static_cast<int64_t>(tile) * CT_BLOCKS;
 #pragma unroll
-    for (int i = 0; i < CT_SEG_BLOCKS; ++i) {
+    for (int i = 0; i < CT_SEG_BLOCKS; i += CT_SAMPLE) {
         const int64_t b = blk0 + seg * CT_SEG_BLOCKS + i;
         if (b < nb) {
             const int64_t r = b * 16 + 2 * lp;
@@ -307,8 +312,8 @@ __global__ void __launch_bounds__(CT_THREADS) canon_apx_kernel(RowArgs args, int
             a1 += approx_row<OP>(args, x1, y1);
         }
     }
-    s_apx[seg][2 * lp] = a0;
-    s_apx[seg][2 * lp + 1] = a1;
+    s_apx[seg][2 * lp] = a0 * static_cast<float>(CT_SAMPLE);
+    s_apx[seg][2 * lp + 1] = a1 * static_cast<float>(CT_SAMPLE);
     __syncthreads();
     if (t < 16) {
         float A = 0.f;
@@ -344,6 +349,9 @@ __global__ void __launch_bounds__(256) canon_gsum_kernel(int T, int G, CanonWork
 constexpr int CAND_THREADS = 256;
 constexpr int CAND_PER = CAND_GROUP / CAND_THREADS;
 
+// CHECK (K2c, after K3 and the refined sums of canon_refine_kernel): a tile whose new
+// candidates include a binade that its K3 candidates did not gets the new ones and a flag.
+template <bool CHECK>
 __global__ void __launch_bounds__(CAND_THREADS) canon_cand_kernel(int T, int G, CanonWork wk, const CanonState *state) {
     __shared__ double s_base;
     const int L = blockIdx.x / G, g = blockIdx.x % G, t = threadIdx.x;
@@ -381,19 +389,44 @@ __global__ void __launch_bounds__(CAND_THREADS) canon_cand_kernel(int T, int G, 
                 c1 = ehi;
             }
         }
-        *reinterpret_cast<int2 *>(&wk.cand[(static_cast<int64_t>(k) * 16 + L) * 2]) = make_int2(c0, c1);
+        int2 *at = reinterpret_cast<int2 *>(&wk.cand[(static_cast<int64_t>(k) * 16 + L) * 2]);
+        if (CHECK) {
+            const int2 old = *at;
+            const bool covered = (c0 == NO_E || c0 == old.x || c0 == old.y) && (c1 == NO_E || c1 == old.x || c1 == old.y);
+            if (covered) continue;
+            wk.flags[k] = 1;
+        }
+        *at = make_int2(c0, c1);
+    }
+}
+
+// K2c input: each tile's lane sum from its transfer function where K3 made one (the increment
+// in ulps of that binade is the sum to within half an ulp a row), else the sampled sum.
+__global__ void __launch_bounds__(256) canon_refine_kernel(int T, CanonWork wk) {
+    const int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= static_cast<int64_t>(16) * T) return;
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+        const int E = wk.recE[i * 2 + c];
+        if (E == NO_E) continue;
+        const double ulp = __longlong_as_double(static_cast<long long>(E - 52 + 1023) << 52);
+        const double v = __dmul_rn(__ull2double_rn(wk.recD[i * 2 + c].d0), ulp);
+        wk.apx[i] = v < 3.0e38 ? __double2float_rn(v) : 3.0e38f;
+        return;
     }
 }
 
 // K3: each tile's transfer function per lane and candidate binade (NO_E when a segment does
 // not take the integer step in that binade).
-template <int OP, bool ALIGNED>
+// FLAGGED (K3c): only the tiles that K2c flagged, with their new candidates.
+template <int OP, bool ALIGNED, bool FLAGGED>
 __global__ void __launch_bounds__(CT_THREADS, 4) canon_tf_kernel(RowArgs args, int64_t nb, int T, CanonWork wk) {
     __shared__ TF s_tf[2][CT_SEGS][16];
     __shared__ unsigned char s_ok[2][CT_SEGS][16];
     __shared__ int s_E[16][2];
     const int t = threadIdx.x, lp = t & 7, seg = t >> 3;
     const int tile = blockIdx.x;
+    if (FLAGGED && !wk.flags[tile]) return;
     if (t < 32) (&s_E[0][0])[t] = wk.cand[tile * 32 + t];
     unsigned long long v[CT_SEG_BLOCKS][2];
     load_tile<OP, ALIGNED>(args, nb, tile, lp, seg, v);
@@ -787,10 +820,18 @@ static vkc_status launch_canon(vkc_ctx *ctx, const RowArgs &a, int64_t nb, int T
     const int G = (T + CAND_GROUP - 1) / CAND_GROUP;
     canon_gsum_kernel<<<16 * G, 256, 0, ctx->stream>>>(T, G, wk);
     if ((st = launched(ctx, "canon_gsum"))) return st;
-    canon_cand_kernel<<<16 * G, CAND_THREADS, 0, ctx->stream>>>(T, G, wk, state);
+    canon_cand_kernel<false><<<16 * G, CAND_THREADS, 0, ctx->stream>>>(T, G, wk, state);
     if ((st = launched(ctx, "canon_cand"))) return st;
-    canon_tf_kernel<OP, ALIGNED><<<T, CT_THREADS, 0, ctx->stream>>>(a, nb, T, wk);
+    canon_tf_kernel<OP, ALIGNED, false><<<T, CT_THREADS, 0, ctx->stream>>>(a, nb, T, wk);
     if ((st = launched(ctx, "canon_tf"))) return st;
+    // The check of the sampled candidates: K3's sums, the prefixes again, K3 again on the tiles
+    // whose binades the first candidates missed.
+    VKC_CUDA(ctx, cudaMemsetAsync(wk.flags, 0, static_cast<size_t>(T) * sizeof(int), ctx->stream));
+    canon_refine_kernel<<<static_cast<int>((16 * static_cast<int64_t>(T) + 255) / 256), 256, 0, ctx->stream>>>(T, wk);
+    canon_gsum_kernel<<<16 * G, 256, 0, ctx->stream>>>(T, G, wk);
+    canon_cand_kernel<true><<<16 * G, CAND_THREADS, 0, ctx->stream>>>(T, G, wk, state);
+    canon_tf_kernel<OP, ALIGNED, true><<<T, CT_THREADS, 0, ctx->stream>>>(a, nb, T, wk);
+    if ((st = launched(ctx, "canon_check"))) return st;
     int warps = 16 * C;
     canon_chunk_kernel<<<(warps + 7) / 8, 256, 0, ctx->stream>>>(T, C, wk);
     if ((st = launched(ctx, "canon_chunk"))) return st;
@@ -864,14 +905,15 @@ struct CanonReducer : DevReducer {
             const size_t o_chD = o_chE + ((c16 * 4 + 255) & ~size_t(255));
             const size_t g16 = static_cast<size_t>((T + CAND_GROUP - 1) / CAND_GROUP) * 16;
             const size_t o_gs = o_chD + ((c16 * sizeof(TF) + 255) & ~size_t(255));
-            const size_t total = o_gs + g16 * sizeof(double);
+            const size_t o_fl = o_gs + ((g16 * sizeof(double) + 255) & ~size_t(255));
+            const size_t total = o_fl + static_cast<size_t>(T) * sizeof(int);
             void *p;
             if ((st = scratch(ctx, total, &p))) return st;
             char *b = static_cast<char *>(p);
             CanonWork wk{reinterpret_cast<float *>(b), reinterpret_cast<int *>(b + o_cand),
                          reinterpret_cast<int *>(b + o_recE), reinterpret_cast<TF *>(b + o_recD),
                          reinterpret_cast<int *>(b + o_chE), reinterpret_cast<TF *>(b + o_chD),
-                         reinterpret_cast<double *>(b + o_gs)};
+                         reinterpret_cast<double *>(b + o_gs), reinterpret_cast<int *>(b + o_fl)};
             const bool aligned = (reinterpret_cast<uintptr_t>(a.x) & 15) == 0 &&
                                  (op != ROW_DOT || (reinterpret_cast<uintptr_t>(a.y) & 15) == 0);
             switch (op) {
