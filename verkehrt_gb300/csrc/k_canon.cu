@@ -86,23 +86,68 @@ __device__ __forceinline__ unsigned long long sat_add(unsigned long long a, unsi
     return s > SAT ? SAT : s;
 }
 
-// a, then b.
-__device__ __forceinline__ TF compose(TF a, TF b) {
-    TF r;
-    r.d0 = sat_add(a.d0, (a.d0 & 1) ? b.d1 : b.d0);
-    r.d1 = sat_add(a.d1, (a.d1 & 1) ? b.d0 : b.d1);
-    return r;
+// Rows of both signs: a signed transfer function {up, dn | SIGNED_TF}, for rows with no tie
+// (no parity dependence): up and dn are the sums of the increments of the positive and the
+// negative rows, so the net increment is up - dn and every state between stays within
+// [S - dn, S + up]. An unsigned one without a parity dependence (d0 == d1) has the signed
+// form {d0, 0}. Saturated parts (at SAT) never apply.
+constexpr unsigned long long SIGNED_TF = 1ull << 63;
+
+__device__ __forceinline__ bool as_signed(TF f, unsigned long long *up, unsigned long long *dn) {
+    if (f.d1 & SIGNED_TF) {
+        *up = f.d0;
+        *dn = f.d1 & ~SIGNED_TF;
+        return true;
+    }
+    if (f.d0 != f.d1) return false;
+    *up = f.d0;
+    *dn = 0;
+    return true;
 }
 
-// Applies f (valid in binade E) to the lane state with bits s. Fails when s is not a
-// positive normal in binade E or when the result would leave the binade.
+// a, then b. SIGNED = false: both are known to be unsigned (the code without the signed case).
+template <bool SIGNED = true>
+__device__ __forceinline__ TF compose(TF a, TF b) {
+    if (!SIGNED || !((a.d1 | b.d1) & SIGNED_TF)) {
+        TF r;
+        r.d0 = sat_add(a.d0, (a.d0 & 1) ? b.d1 : b.d0);
+        r.d1 = sat_add(a.d1, (a.d1 & 1) ? b.d0 : b.d1);
+        return r;
+    }
+    unsigned long long au, ad, bu, bd;
+    if (!as_signed(a, &au, &ad) || !as_signed(b, &bu, &bd)) return TF{SAT, SAT | SIGNED_TF};  // never applies
+    return TF{sat_add(au, bu), sat_add(ad, bd) | SIGNED_TF};
+}
+
+// Applies f (valid in binade E) to the lane state with bits s. Fails when |s| is not a normal
+// in binade E or when a state on the way could leave the binade. A negative state is the
+// mirror image: round-to-nearest-even is symmetric, so its magnitude moves by the negated
+// increments (only for functions without a parity dependence). A signed function keeps every
+// state on the way at least one ulp above 2^E, so each exact sum lies in the binade.
+// SIGNED = false: positive states and unsigned functions only (fails otherwise).
+template <bool SIGNED = true>
 __device__ __forceinline__ bool apply(unsigned long long s, int E, TF f, unsigned long long *out) {
-    unsigned long long ef = static_cast<unsigned long long>(E + 1023);
-    if ((s >> 52) != ef) return false;
-    unsigned long long S = (s & MANT) | ONE52;
-    unsigned long long S2 = S + ((S & 1) ? f.d1 : f.d0);
-    if (S2 >= (ONE52 << 1)) return false;
-    *out = (ef << 52) | (S2 & MANT);
+    const unsigned long long ef = static_cast<unsigned long long>(E + 1023);
+    const unsigned long long neg = SIGNED ? s >> 63 : 0;
+    if (!SIGNED && (s >> 63)) return false;
+    if (((s >> 52) & 0x7ff) != ef) return false;
+    const unsigned long long S = (s & MANT) | ONE52;
+    unsigned long long S2;
+    if (!SIGNED || (!neg && !(f.d1 & SIGNED_TF))) {
+        S2 = S + ((S & 1) ? f.d1 : f.d0);
+        if (S2 >= (ONE52 << 1)) return false;
+    } else {
+        unsigned long long up, dn;
+        if (!as_signed(f, &up, &dn)) return false;
+        if (neg) {
+            const unsigned long long x = up;
+            up = dn;
+            dn = x;
+        }
+        if (up >= ONE52 || dn >= ONE52 || S + up >= (ONE52 << 1) || (dn && S - dn <= ONE52)) return false;
+        S2 = S + up - dn;
+    }
+    *out = (neg << 63) | (ef << 52) | (S2 & MANT);
     return true;
 }
 
@@ -110,13 +155,62 @@ __device__ __forceinline__ bool apply(unsigned long long s, int E, TF f, unsigne
 // when a row is negative, infinite, NaN or not below 2^E (k < 1), where the integer step does
 // not hold. For x = M * 2^(ex-1075), x/u = M / 2^k with k = KE - ex, and
 // RNE(x/u) = (M + 2^(k-1)) >> k unless M mod 2^k is exactly 2^(k-1) (a tie).
+// seg_tf of a segment with negative rows (exmax: the largest exponent field, below KE): the
+// increments of the magnitudes, positive and negative rows apart, as a signed function; a
+// segment with a halfway row has none (the walk adds it from the rows).
+__device__ __forceinline__ bool seg_tf_signed(const unsigned long long (&v)[CT_SEG_BLOCKS][2], int h, int KE,
+                                              unsigned exmax, TF *out) {
+    const unsigned kmin = static_cast<unsigned>(KE) - exmax;
+    const unsigned low = kmin > 32 ? 0xffffffffu : (1u << (kmin - 1)) - 1u;
+    unsigned long long tp = 0, tn = 0;
+    unsigned op = 0, on = 0;
+    bool maybe_tie = false;
+#pragma unroll
+    for (int i = 0; i < CT_SEG_BLOCKS; ++i) {
+        const unsigned long long b = v[i][h];
+        const unsigned k = min(static_cast<unsigned>(KE) - (static_cast<unsigned>(b >> 52) & 0x7ffu), 63u);
+        const unsigned long long t = ((b & MANT) | ONE52) >> (k - 1);
+        if (b >> 63) {
+            tn += t;
+            on += static_cast<unsigned>(t) & 1u;
+        } else {
+            tp += t;
+            op += static_cast<unsigned>(t) & 1u;
+        }
+        maybe_tie |= (k <= 53u) & ((static_cast<unsigned>(b) & low) == 0u);
+    }
+    if (!maybe_tie) {
+        *out = TF{(tp + op) >> 1, ((tn + on) >> 1) | SIGNED_TF};
+        return true;
+    }
+    unsigned long long up = 0, dn = 0;
+#pragma unroll
+    for (int i = 0; i < CT_SEG_BLOCKS; ++i) {
+        const unsigned long long b = v[i][h];
+        const unsigned k = min(static_cast<unsigned>(KE) - (static_cast<unsigned>(b >> 52) & 0x7ffu), 63u);
+        const unsigned long long w = ((b & MANT) | ONE52) + (1ull << (k - 1));
+        if ((w << (64 - k)) == 0) return false;  // a halfway row
+        if (b >> 63) dn += w >> k;
+        else up += w >> k;
+    }
+    *out = TF{up, dn | SIGNED_TF};
+    return true;
+}
+
+// SIGNED: rows of either sign (seg_tf_signed for a segment with a negative row); otherwise a
+// negative row's exponent field with its sign bit is at least 2048, above any KE, and the
+// segment has no function.
+template <bool SIGNED>
 __device__ __forceinline__ bool seg_tf(const unsigned long long (&v)[CT_SEG_BLOCKS][2], int h,
                                        int KE, TF *out) {
-    unsigned exmax = 0;
+    unsigned exmax = 0, sgn = 0;
 #pragma unroll
-    for (int i = 0; i < CT_SEG_BLOCKS; ++i) exmax = max(exmax, static_cast<unsigned>(v[i][h] >> 52));
-    // The sign bit makes a negative row's exponent field at least 2048, above any KE.
+    for (int i = 0; i < CT_SEG_BLOCKS; ++i) {
+        exmax = max(exmax, static_cast<unsigned>(v[i][h] >> 52) & (SIGNED ? 0x7ffu : 0xfffu));
+        if (SIGNED) sgn |= static_cast<unsigned>(v[i][h] >> 63);
+    }
     if (exmax >= static_cast<unsigned>(KE)) return false;
+    if (SIGNED && sgn) return seg_tf_signed(v, h, KE, exmax, out);
     // Every row has k = KE - ex >= kmin >= 1. With t = floor(M / 2^(k-1)) (the quotient with
     // one more bit), round-half-up gives (t + 1) >> 1, so the sum of the increments is
     // (sum of t + number of odd t) / 2. That is RNE unless a row is exactly halfway: k <= 53 and
@@ -210,7 +304,8 @@ struct CanonWork {
     int *chunkE;               // [16][C] binade of each 32-tile chunk's transfer function
     TF *chunkD;                // [16][C]
     double *gsum;              // [16][G] approximate sum of each group of CAND_GROUP tiles
-    int *flags;                // [T] tiles whose transfer functions are recomputed (K3 again)
+    int *flags;                // [T + 1] tiles whose transfer functions are recomputed (K3 again);
+                               // flags[T]: some tile has a negative row
 };
 
 constexpr int CAND_GROUP = 1024;  // tiles per K2 block
@@ -379,7 +474,12 @@ __global__ void __launch_bounds__(CAND_THREADS) canon_cand_kernel(int T, int G, 
         const double A = static_cast<double>(a[j]);
         const double pre = start + static_cast<double>(run);
         run += a[j];
-        const double lo = A < 0 ? pre + A : pre, hi = A < 0 ? pre : pre + A;
+        double lo = A < 0 ? pre + A : pre, hi = A < 0 ? pre : pre + A;
+        if (hi < 0) {  // a negative sum: the binades of its magnitude
+            const double m = -hi;
+            hi = -lo;
+            lo = m;
+        }
         const int elo = binade(lo * (1.0 - 0x1p-12)), ehi = binade(hi * (1.0 + 0x1p-12));
         int c0 = NO_E, c1 = NO_E;
         if (elo != NO_E && ehi != NO_E && elo >= -959) {
@@ -410,15 +510,40 @@ __global__ void __launch_bounds__(256) canon_refine_kernel(int T, CanonWork wk) 
         const int E = wk.recE[i * 2 + c];
         if (E == NO_E) continue;
         const double ulp = __longlong_as_double(static_cast<long long>(E - 52 + 1023) << 52);
-        const double v = __dmul_rn(__ull2double_rn(wk.recD[i * 2 + c].d0), ulp);
-        wk.apx[i] = v < 3.0e38 ? __double2float_rn(v) : 3.0e38f;
+        const TF f = wk.recD[i * 2 + c];
+        const double d = (f.d1 & SIGNED_TF) ? __ll2double_rn(static_cast<long long>(f.d0) -
+                                                             static_cast<long long>(f.d1 & ~SIGNED_TF))
+                                            : __ull2double_rn(f.d0);
+        const double v = __dmul_rn(d, ulp);
+        wk.apx[i] = v < 3.0e38 ? (v > -3.0e38 ? __double2float_rn(v) : -3.0e38f) : 3.0e38f;
         return;
     }
 }
 
 // K3: each tile's transfer function per lane and candidate binade (NO_E when a segment does
 // not take the integer step in that binade).
-// FLAGGED (K3c): only the tiles that K2c flagged, with their new candidates.
+// The thread's segment functions for its two lanes and both candidates.
+template <bool SIGNED>
+__device__ __forceinline__ void seg_tfs(const unsigned long long (&v)[CT_SEG_BLOCKS][2], const int (*s_E)[2], int lp,
+                                        TF (&fv)[2][2], int &okv, bool &plain) {
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const int L = 2 * lp + h;
+#pragma unroll
+        for (int c = 0; c < 2; ++c) {
+            const int E = s_E[L][c];
+            TF f{0, 0};
+            const bool ok = E != NO_E && seg_tf<SIGNED>(v, h, 1023 + E, &f);
+            plain = plain && f.d0 == f.d1;
+            fv[h][c] = f;
+            okv |= static_cast<int>(ok) << (2 * h + c);
+        }
+    }
+}
+
+// FLAGGED (K3c): only the tiles flagged by K3 (a negative row) or K2c (new candidates), with
+// the signed functions where a tile has a negative row. Otherwise (K3) a tile with a negative
+// row is only flagged, so that this kernel holds no signed code.
 template <int OP, bool ALIGNED, bool FLAGGED>
 __global__ void __launch_bounds__(CT_THREADS, 4) canon_tf_kernel(RowArgs args, int64_t nb, int T, CanonWork wk) {
     __shared__ TF s_tf[2][CT_SEGS][16];
@@ -430,22 +555,26 @@ __global__ void __launch_bounds__(CT_THREADS, 4) canon_tf_kernel(RowArgs args, i
     if (t < 32) (&s_E[0][0])[t] = wk.cand[tile * 32 + t];
     unsigned long long v[CT_SEG_BLOCKS][2];
     load_tile<OP, ALIGNED>(args, nb, tile, lp, seg, v);
-    __syncthreads();
     TF fv[2][2];
     int okv = 0;  // bit 2h + c: the segment takes the integer step for lane 2lp+h, candidate c
     bool plain = true;
+    // Tiles with a negative row take the signed functions (a separate path, so that tiles
+    // without one keep the shorter code).
+    unsigned sgn = 0;
 #pragma unroll
-    for (int h = 0; h < 2; ++h) {
-        const int L = 2 * lp + h;
-#pragma unroll
-        for (int c = 0; c < 2; ++c) {
-            const int E = s_E[L][c];
-            TF f{0, 0};
-            const bool ok = E != NO_E && seg_tf(v, h, 1023 + E, &f);
-            plain = plain && f.d0 == f.d1;
-            fv[h][c] = f;
-            okv |= static_cast<int>(ok) << (2 * h + c);
+    for (int i = 0; i < CT_SEG_BLOCKS; ++i) sgn |= static_cast<unsigned>((v[i][0] | v[i][1]) >> 63);
+    if (__syncthreads_or(sgn)) {  // also the barrier after s_E
+        if (!FLAGGED) {
+            if (t == 0) {
+                wk.flags[tile] = 2;
+                wk.flags[T] = 1;  // some tile has a negative row
+            }
+            if (t < 32) wk.recE[(static_cast<int64_t>(t & 15) * T + tile) * 2 + (t >> 4)] = NO_E;
+            return;
         }
+        seg_tfs<true>(v, s_E, lp, fv, okv, plain);
+    } else {
+        seg_tfs<false>(v, s_E, lp, fv, okv, plain);
     }
     static_assert(CT_SEGS == 32 && CT_THREADS == 256, "four segments per warp, eight warps");
     const int sl = t & 31, wp = t >> 5;
@@ -517,7 +646,7 @@ __global__ void __launch_bounds__(CT_THREADS, 4) canon_tf_kernel(RowArgs args, i
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
             const TF y = shfl_up_tf(f, o);
-            if (sl >= o) f = compose(y, f);
+            if (sl >= o) f = compose<FLAGGED>(y, f);
         }
         if (sl == 31) {
             const int64_t at = (static_cast<int64_t>(L) * T + tile) * 2 + c;
@@ -570,24 +699,26 @@ __global__ void __launch_bounds__(256) canon_chunk_kernel(int T, int C, CanonWor
     }
 }
 
+// The binade of |s| (s normal and finite), NO_E otherwise.
 __device__ __forceinline__ int state_binade(unsigned long long s) {
-    unsigned long long e = s >> 52;  // sign bit included: a negative state has none
+    const unsigned long long e = (s >> 52) & 0x7ff;
     return (e >= 1 && e <= 2046) ? static_cast<int>(e) - 1023 : NO_E;
 }
 
 // Inclusive ordered prefix composition over the warp (lane 0 first), then the number of
 // leading lanes whose prefix applies to state s (usable and inside the binade). Returns that
 // count and, in *out, the state after them.
+template <bool SIGNED = true>
 __device__ __forceinline__ int apply_prefix(TF f, bool usable, unsigned long long s, int E,
                                             unsigned long long *out) {
     const int lane = threadIdx.x & 31;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
         TF y = shfl_up_tf(f, o);
-        if (lane >= o) f = compose(y, f);
+        if (lane >= o) f = compose<SIGNED>(y, f);
     }
     unsigned long long r = 0;
-    const bool ok = usable && apply(s, E, f, &r);
+    const bool ok = usable && apply<SIGNED>(s, E, f, &r);
     const unsigned bad = __ballot_sync(FULL, !ok);
     const int m = bad ? __ffs(bad) - 1 : 32;
     if (m > 0) *out = __shfl_sync(FULL, r, m - 1);
@@ -597,7 +728,7 @@ __device__ __forceinline__ int apply_prefix(TF f, bool usable, unsigned long lon
 // Resolves tile `tp` for lane L from the state s: the warp recomputes the tile's 32 segment
 // transfer functions from the rows (lane j = segment j) for the state's binade and the next,
 // applies them in order, and adds the rows of any segment they do not carry one by one.
-template <int OP>
+template <int OP, bool SIGNED>
 __device__ unsigned long long resolve_tile(const RowArgs &args, int64_t nb, int tp, int L, unsigned long long s) {
     const int lane = threadIdx.x & 31;
     unsigned long long v[CT_SEG_BLOCKS][2];
@@ -620,13 +751,13 @@ __device__ unsigned long long resolve_tile(const RowArgs &args, int64_t nb, int 
         const int E = state_binade(s);
         if (E != NO_E && E >= -959) {
             TF f{0, 0};
-            bool ok = lane >= seg && seg_tf(v, 0, 1023 + E, &f);
+            bool ok = lane >= seg && seg_tf<SIGNED>(v, 0, 1023 + E, &f);
             if (lane < seg) {
                 f = TF{0, 0};
                 ok = true;  // already consumed: identity
             }
             unsigned long long r = s;
-            int m = apply_prefix(f, ok, s, E, &r);
+            int m = apply_prefix<SIGNED>(f, ok, s, E, &r);
             if (m > seg) {
                 s = r;
                 seg = m;
@@ -665,6 +796,68 @@ struct WalkSmem {
     TF mD[WK_MAX_MIXED][32][2];
     int nmixed;
 };
+
+// The walk of lane L from state s (warp 0 of the lane's block), with the signed functions
+// when some tile has a negative row or the state is negative (SIGNED), else the shorter code.
+template <int OP, bool SIGNED>
+__device__ __forceinline__ unsigned long long walk_lane(const RowArgs &args, int64_t nb, int T, int C, const CanonWork &wk,
+                                                        const WalkSmem &sm, bool held, const int *gE, const TF *gD,
+                                                        int L, unsigned long long s) {
+    const int lane = threadIdx.x;
+    int k = 0;  // next chunk
+    while (k < C) {
+        // Whole chunks k .. k+31.
+        const int E = state_binade(s);
+        const int kc = k + lane;
+        int ce = NO_E;
+        TF f{0, 0};
+        if (kc < C) {
+            ce = held ? sm.chunkE[kc] : gE[kc];
+            if (ce != NO_E && ce == E) f = held ? sm.chunkD[kc] : gD[kc];
+        }
+        unsigned long long r = s;
+        int m = E == NO_E ? 0 : apply_prefix<SIGNED>(f, kc < C && ce != NO_E && ce == E, s, E, &r);
+        if (m > 0) {
+            s = r;
+            k += m;
+            continue;
+        }
+        // Chunk k, tile by tile.
+        const int slot = held ? sm.mixed_of[k] : -1;
+        int tp = k * 32;
+        const int end = min(T, tp + 32);
+        while (tp < end) {
+            const int Et = state_binade(s);
+            const int tl = tp + lane;
+            TF g{0, 0};
+            bool usable = false;
+            if (tl < end && Et != NO_E) {
+                if (slot >= 0) {
+                    const int j = tl - k * 32;
+                    if (sm.mE[slot][j][0] == Et) {
+                        g = sm.mD[slot][j][0];
+                        usable = true;
+                    } else if (sm.mE[slot][j][1] == Et) {
+                        g = sm.mD[slot][j][1];
+                        usable = true;
+                    }
+                } else {
+                    usable = tile_tf(wk, T, L, tl, Et, &g);
+                }
+            }
+            int mt = Et == NO_E ? 0 : apply_prefix<SIGNED>(g, usable, s, Et, &r);
+            if (mt > 0) {
+                s = r;
+                tp += mt;
+            } else {
+                s = resolve_tile<OP, SIGNED>(args, nb, tp, L, s);
+                ++tp;
+            }
+        }
+        ++k;
+    }
+    return s;
+}
 
 template <int OP>
 __global__ void __launch_bounds__(WK_THREADS) canon_walk_kernel(RowArgs args, int64_t nb, int T, int C, CanonWork wk,
@@ -713,61 +906,10 @@ __global__ void __launch_bounds__(WK_THREADS) canon_walk_kernel(RowArgs args, in
     }
     __syncthreads();
     if (t >= 32) return;
-
     const int lane = t;
     unsigned long long s = state->lanes[L];
-    int k = 0;  // next chunk
-    while (k < C) {
-        // Whole chunks k .. k+31.
-        const int E = state_binade(s);
-        const int kc = k + lane;
-        int ce = NO_E;
-        TF f{0, 0};
-        if (kc < C) {
-            ce = held ? sm.chunkE[kc] : gE[kc];
-            if (ce != NO_E && ce == E) f = held ? sm.chunkD[kc] : gD[kc];
-        }
-        unsigned long long r = s;
-        int m = E == NO_E ? 0 : apply_prefix(f, kc < C && ce != NO_E && ce == E, s, E, &r);
-        if (m > 0) {
-            s = r;
-            k += m;
-            continue;
-        }
-        // Chunk k, tile by tile.
-        const int slot = held ? sm.mixed_of[k] : -1;
-        int tp = k * 32;
-        const int end = min(T, tp + 32);
-        while (tp < end) {
-            const int Et = state_binade(s);
-            const int tl = tp + lane;
-            TF g{0, 0};
-            bool usable = false;
-            if (tl < end && Et != NO_E) {
-                if (slot >= 0) {
-                    const int j = tl - k * 32;
-                    if (sm.mE[slot][j][0] == Et) {
-                        g = sm.mD[slot][j][0];
-                        usable = true;
-                    } else if (sm.mE[slot][j][1] == Et) {
-                        g = sm.mD[slot][j][1];
-                        usable = true;
-                    }
-                } else {
-                    usable = tile_tf(wk, T, L, tl, Et, &g);
-                }
-            }
-            int mt = Et == NO_E ? 0 : apply_prefix(g, usable, s, Et, &r);
-            if (mt > 0) {
-                s = r;
-                tp += mt;
-            } else {
-                s = resolve_tile<OP>(args, nb, tp, L, s);
-                ++tp;
-            }
-        }
-        ++k;
-    }
+    s = (wk.flags[T] != 0 || (s >> 63)) ? walk_lane<OP, true>(args, nb, T, C, wk, sm, held, gE, gD, L, s)
+                                        : walk_lane<OP, false>(args, nb, T, C, wk, sm, held, gE, gD, L, s);
     if (lane == 0) state->lanes[L] = s;
 }
 
@@ -822,11 +964,11 @@ static vkc_status launch_canon(vkc_ctx *ctx, const RowArgs &a, int64_t nb, int T
     if ((st = launched(ctx, "canon_gsum"))) return st;
     canon_cand_kernel<false><<<16 * G, CAND_THREADS, 0, ctx->stream>>>(T, G, wk, state);
     if ((st = launched(ctx, "canon_cand"))) return st;
+    VKC_CUDA(ctx, cudaMemsetAsync(wk.flags, 0, static_cast<size_t>(T + 1) * sizeof(int), ctx->stream));
     canon_tf_kernel<OP, ALIGNED, false><<<T, CT_THREADS, 0, ctx->stream>>>(a, nb, T, wk);
     if ((st = launched(ctx, "canon_tf"))) return st;
     // The check of the sampled candidates: K3's sums, the prefixes again, K3 again on the tiles
-    // whose binades the first candidates missed.
-    VKC_CUDA(ctx, cudaMemsetAsync(wk.flags, 0, static_cast<size_t>(T) * sizeof(int), ctx->stream));
+    // whose binades the first candidates missed and on the tiles with negative rows.
     canon_refine_kernel<<<static_cast<int>((16 * static_cast<int64_t>(T) + 255) / 256), 256, 0, ctx->stream>>>(T, wk);
     canon_gsum_kernel<<<16 * G, 256, 0, ctx->stream>>>(T, G, wk);
     canon_cand_kernel<true><<<16 * G, CAND_THREADS, 0, ctx->stream>>>(T, G, wk, state);
@@ -906,7 +1048,7 @@ struct CanonReducer : DevReducer {
             const size_t g16 = static_cast<size_t>((T + CAND_GROUP - 1) / CAND_GROUP) * 16;
             const size_t o_gs = o_chD + ((c16 * sizeof(TF) + 255) & ~size_t(255));
             const size_t o_fl = o_gs + ((g16 * sizeof(double) + 255) & ~size_t(255));
-            const size_t total = o_fl + static_cast<size_t>(T) * sizeof(int);
+            const size_t total = o_fl + static_cast<size_t>(T + 1) * sizeof(int);
             void *p;
             if ((st = scratch(ctx, total, &p))) return st;
             char *b = static_cast<char *>(p);
