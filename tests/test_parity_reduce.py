@@ -47,6 +47,27 @@ def test_reduce_add_f64_large_uniform(ctx):
         assert ctx.call("reduce_add_f64", ctx.upload(x), raw=True)[2] == bits(oracle.reduce_add_f64(x)), n
 
 
+def test_signed_inputs_large(ctx):
+    # Signed rows take signed transfer functions (and negative lane states their mirror image):
+    # all negative, mostly positive, mixed, magnitudes over 80 binades, and dot products of
+    # signed vectors; then a tiled reducer whose lanes turn negative before positive rows.
+    n = (1 << 22) + 13
+    u = uniform(n, 21)
+    cases = {"negative": -u, "mostly_positive": u - 0.25, "mixed": u - 0.5, "varied": varied(n, 22)}
+    for name, x in cases.items():
+        got = ctx.call("reduce_add_f64", ctx.upload(x), raw=True)[2]
+        assert got == bits(oracle.reduce_add_f64(x)), name
+    y = uniform(n, 23) - 0.75
+    dx, dy = ctx.upload(u - 0.25), ctx.upload(y)
+    assert ctx.call("dot_f64", dx, dy, raw=True)[2] == bits(oracle.dot_f64(u - 0.25, y))
+    first = -uniform(1 << 20, 24) * 8.0
+    second = uniform(1 << 21, 25)
+    r = ctx.reducer("reduce_add_f64")
+    r.update(ctx.upload(first))
+    r.update(ctx.upload(second))
+    assert r.finish(raw=True)[2] == bits(oracle.reduce_add_f64(np.concatenate([first, second])))
+
+
 def test_reduce_add_f64_device_generated_large(ctx):
     n = 1 << 24
     got = ctx.call("reduce_add_f64", ctx.call("rand_f64", n, 7), raw=True)[2]
