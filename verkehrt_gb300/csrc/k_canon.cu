@@ -304,8 +304,9 @@ struct CanonWork {
     int *chunkE;               // [16][C] binade of each 32-tile chunk's transfer function
     TF *chunkD;                // [16][C]
     double *gsum;              // [16][G] approximate sum of each group of CAND_GROUP tiles
-    int *flags;                // [T + 1] tiles whose transfer functions are recomputed (K3 again);
-                               // flags[T]: some tile has a negative row
+    int *flags;                // [T] tiles whose transfer functions are recomputed (K3 again);
+                               // [T]: some tile has a negative row; [T + 1]: the number of
+                               // flagged tiles, listed from [T + 2]
 };
 
 constexpr int CAND_GROUP = 1024;  // tiles per K2 block
@@ -545,13 +546,11 @@ __device__ __forceinline__ void seg_tfs(const unsigned long long (&v)[CT_SEG_BLO
 // the signed functions where a tile has a negative row. Otherwise (K3) a tile with a negative
 // row is only flagged, so that this kernel holds no signed code.
 template <int OP, bool ALIGNED, bool FLAGGED>
-__global__ void __launch_bounds__(CT_THREADS, 4) canon_tf_kernel(RowArgs args, int64_t nb, int T, CanonWork wk) {
+__device__ __forceinline__ void tf_tile(const RowArgs &args, int64_t nb, int T, const CanonWork &wk, int tile) {
     __shared__ TF s_tf[2][CT_SEGS][16];
     __shared__ unsigned char s_ok[2][CT_SEGS][16];
     __shared__ int s_E[16][2];
     const int t = threadIdx.x, lp = t & 7, seg = t >> 3;
-    const int tile = blockIdx.x;
-    if (FLAGGED && !wk.flags[tile]) return;
     if (t < 32) (&s_E[0][0])[t] = wk.cand[tile * 32 + t];
     unsigned long long v[CT_SEG_BLOCKS][2];
     load_tile<OP, ALIGNED>(args, nb, tile, lp, seg, v);
@@ -655,6 +654,30 @@ __global__ void __launch_bounds__(CT_THREADS, 4) canon_tf_kernel(RowArgs args, i
         }
     }
 }
+
+template <int OP, bool ALIGNED>
+__global__ void __launch_bounds__(CT_THREADS, 4) canon_tf_kernel(RowArgs args, int64_t nb, int T, CanonWork wk) {
+    tf_tile<OP, ALIGNED, false>(args, nb, T, wk, blockIdx.x);
+}
+
+// The flagged tiles in a list (any order): wk.flags[T + 1] counts them, wk.flags[T + 2 ..]
+// holds them.
+__global__ void __launch_bounds__(256) canon_flag_list_kernel(int T, CanonWork wk) {
+    const int stride = gridDim.x * blockDim.x;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < T; t += stride)
+        if (wk.flags[t]) wk.flags[T + 2 + atomicAdd(&wk.flags[T + 1], 1)] = t;
+}
+
+// K3c: persistent blocks over the list of flagged tiles.
+template <int OP, bool ALIGNED>
+__global__ void __launch_bounds__(CT_THREADS, 4) canon_tf_flagged_kernel(RowArgs args, int64_t nb, int T, CanonWork wk) {
+    const int count = wk.flags[T + 1];
+    for (int i = blockIdx.x; i < count; i += gridDim.x) {
+        __syncthreads();  // the previous tile's shared arrays are free
+        tf_tile<OP, ALIGNED, true>(args, nb, T, wk, wk.flags[T + 2 + i]);
+    }
+}
+
 
 // The transfer function of tile `tp` for lane L in binade E, if it has one.
 __device__ __forceinline__ bool tile_tf(const CanonWork &wk, int T, int L, int tp, int E, TF *f) {
@@ -964,15 +987,16 @@ static vkc_status launch_canon(vkc_ctx *ctx, const RowArgs &a, int64_t nb, int T
     if ((st = launched(ctx, "canon_gsum"))) return st;
     canon_cand_kernel<false><<<16 * G, CAND_THREADS, 0, ctx->stream>>>(T, G, wk, state);
     if ((st = launched(ctx, "canon_cand"))) return st;
-    VKC_CUDA(ctx, cudaMemsetAsync(wk.flags, 0, static_cast<size_t>(T + 1) * sizeof(int), ctx->stream));
-    canon_tf_kernel<OP, ALIGNED, false><<<T, CT_THREADS, 0, ctx->stream>>>(a, nb, T, wk);
+    VKC_CUDA(ctx, cudaMemsetAsync(wk.flags, 0, static_cast<size_t>(T + 2) * sizeof(int), ctx->stream));
+    canon_tf_kernel<OP, ALIGNED><<<T, CT_THREADS, 0, ctx->stream>>>(a, nb, T, wk);
     if ((st = launched(ctx, "canon_tf"))) return st;
     // The check of the sampled candidates: K3's sums, the prefixes again, K3 again on the tiles
     // whose binades the first candidates missed and on the tiles with negative rows.
     canon_refine_kernel<<<static_cast<int>((16 * static_cast<int64_t>(T) + 255) / 256), 256, 0, ctx->stream>>>(T, wk);
     canon_gsum_kernel<<<16 * G, 256, 0, ctx->stream>>>(T, G, wk);
     canon_cand_kernel<true><<<16 * G, CAND_THREADS, 0, ctx->stream>>>(T, G, wk, state);
-    canon_tf_kernel<OP, ALIGNED, true><<<T, CT_THREADS, 0, ctx->stream>>>(a, nb, T, wk);
+    canon_flag_list_kernel<<<std::min(T / 256 + 1, 1024), 256, 0, ctx->stream>>>(T, wk);
+    canon_tf_flagged_kernel<OP, ALIGNED><<<std::min(T, 4 * ctx->sms), CT_THREADS, 0, ctx->stream>>>(a, nb, T, wk);
     if ((st = launched(ctx, "canon_check"))) return st;
     int warps = 16 * C;
     canon_chunk_kernel<<<(warps + 7) / 8, 256, 0, ctx->stream>>>(T, C, wk);
@@ -1048,7 +1072,7 @@ struct CanonReducer : DevReducer {
             const size_t g16 = static_cast<size_t>((T + CAND_GROUP - 1) / CAND_GROUP) * 16;
             const size_t o_gs = o_chD + ((c16 * sizeof(TF) + 255) & ~size_t(255));
             const size_t o_fl = o_gs + ((g16 * sizeof(double) + 255) & ~size_t(255));
-            const size_t total = o_fl + static_cast<size_t>(T + 1) * sizeof(int);
+            const size_t total = o_fl + static_cast<size_t>(2 * T + 2) * sizeof(int);
             void *p;
             if ((st = scratch(ctx, total, &p))) return st;
             char *b = static_cast<char *>(p);
