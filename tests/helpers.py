@@ -6,7 +6,7 @@ import oracle
 
 # tests/isa_variants.rs:17 (LENGTHS) plus its TILED_LEN, LONG_LEN and lengths that cross the
 # GPU tiles (4096-row selection/scan tiles, 8192-row canonical tiles) and the end of the
-# short paths (argsort to 2048 rows, the canonical sums to 4096).
+# short paths (argsort to 2048 and to 8192 rows, the canonical sums to 4096).
 LENGTHS = [0, 1, 3, 4, 7, 8, 15, 16, 17, 31, 32, 63, 64, 65, 300, 1000, 4500]
 GPU_LENGTHS = [4095, 4096, 4097, 4111, 4112, 8191, 8192, 8193, 8192 * 3 + 17, 100_003]
 # tests/isa_variants.rs:28-30

@@ -44,7 +44,7 @@ def classes(n, seed):
 
 
 def test_argsort_classes(ctx):
-    for n in LENGTHS + [1023, 1024, 1025, 2047, 2048, 2049, 4095, 4096, 4097, 5000, 70_001]:
+    for n in LENGTHS + [1023, 1024, 1025, 2047, 2048, 2049, 4095, 4096, 4097, 5000, 8191, 8192, 8193, 70_001]:
         for name, xs in classes(n, n + 7).items():
             got = ctx.call("argsort_i64", ctx.upload(xs)).numpy()
             assert np.array_equal(got, oracle.argsort_i64(xs)), (name, n)

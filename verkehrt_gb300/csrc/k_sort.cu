@@ -16,7 +16,8 @@
 //    `down` whose next tile arrives by TMA while it ranks the current one was no faster
 //    either: the pass is bound by instruction issue, about 3.8 warp instructions per row.)
 // Stability makes the output the reference's; inputs of at most 2048 rows are sorted in one
-// block by comparison (as the reference does below 1024 rows, radix.rs:140-151).
+// block by comparison (as the reference does below 1024 rows, radix.rs:140-151), inputs of at
+// most 8192 rows by the same radix passes inside one block.
 #include <algorithm>
 
 #include "lookback.cuh"
@@ -386,6 +387,132 @@ __global__ void __launch_bounds__(1024) small_argsort_kernel(const long long *__
     for (int i = threadIdx.x; i < n; i += blockDim.x) out[i] = static_cast<long long>(s_pos[i]);
 }
 
+// Inputs of at most MID_SORT rows: one block of 1024 threads sorts (image, position) pairs in
+// shared memory by the LSD passes of the active digits (the digits not equal in every row,
+// found by a block-wide AND and OR of the images), each pass ranked stably as the down pass
+// does (per warp, a ballot per digit bit; warp w holds rows 256w .. 256w + 255), one launch and
+// no host synchronisation.
+constexpr int MID_SORT = 8192;
+constexpr int MID_THREADS = 1024, MID_ITEMS = MID_SORT / MID_THREADS, MID_WARPS = MID_THREADS / 32;
+struct MidSmem {
+    unsigned long long img[2][MID_SORT];
+    unsigned short pos[2][MID_SORT];
+    unsigned short wcnt[MID_WARPS][RADIX];  // per-warp digit counts, then offsets within the digit
+    unsigned dstart[RADIX];                 // the digit's first row
+    unsigned long long all_and[MID_WARPS], all_or[MID_WARPS];
+};
+
+__global__ void __launch_bounds__(MID_THREADS) mid_argsort_kernel(const long long *__restrict__ keys, int n,
+                                                                   long long *__restrict__ out) {
+    extern __shared__ __align__(16) unsigned char mid_smem[];
+    MidSmem &sm = *reinterpret_cast<MidSmem *>(mid_smem);
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    unsigned long long a = ~0ull, o = 0;
+    for (int i = t; i < n; i += MID_THREADS) {
+        const unsigned long long im = image_of(keys[i]);
+        sm.img[0][i] = im;
+        sm.pos[0][i] = static_cast<unsigned short>(i);
+        a &= im;
+        o |= im;
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        a &= __shfl_xor_sync(FULL, a, off);
+        o |= __shfl_xor_sync(FULL, o, off);
+    }
+    if (lane == 0) {
+        sm.all_and[w] = a;
+        sm.all_or[w] = o;
+    }
+    __syncthreads();
+    a = ~0ull;
+    o = 0;
+#pragma unroll 4
+    for (int k = 0; k < MID_WARPS; ++k) {
+        a &= sm.all_and[k];
+        o |= sm.all_or[k];
+    }
+    const unsigned long long varies = a ^ o;  // bits that differ between rows
+    int cur = 0;
+    const unsigned lt = (1u << lane) - 1;
+    for (int shift = 0; shift < 64; shift += 8) {
+        if (((varies >> shift) & 0xffu) == 0) continue;  // a constant digit leaves the order as it is
+        for (int i = t; i < MID_WARPS * RADIX; i += MID_THREADS) (&sm.wcnt[0][0])[i] = 0;
+        __syncthreads();
+        unsigned long long img[MID_ITEMS];
+        unsigned short pos[MID_ITEMS];
+        unsigned rank2[MID_ITEMS / 2];
+        const int base = w * (32 * MID_ITEMS);
+#pragma unroll
+        for (int j = 0; j < MID_ITEMS; ++j) {
+            const int r = base + j * 32 + lane;
+            img[j] = r < n ? sm.img[cur][r] : ~0ull;
+            pos[j] = r < n ? sm.pos[cur][r] : 0;
+        }
+#pragma unroll
+        for (int j = 0; j < MID_ITEMS; ++j) {
+            const bool in = base + j * 32 + lane < n;
+            const unsigned d = static_cast<unsigned>(img[j] >> shift) & 0xffu;
+            const unsigned peers = digit_peers(d, __ballot_sync(FULL, in));
+            const unsigned short before = sm.wcnt[w][d];
+            __syncwarp();
+            if (in) {
+                const unsigned rk = before + __popc(peers & lt);
+                rank2[j / 2] = (j & 1) ? (rank2[j / 2] | (rk << 16)) : rk;
+                if ((peers & lt) == 0) sm.wcnt[w][d] = static_cast<unsigned short>(before + __popc(peers));
+            }
+            __syncwarp();
+        }
+        __syncthreads();
+        // Per digit: the warps' offsets within it (threads 0..255), then the digits' first rows
+        // (warp 0, eight digits a lane).
+        unsigned total = 0;
+        if (t < RADIX) {
+#pragma unroll 4
+            for (int ww = 0; ww < MID_WARPS; ++ww) {
+                const unsigned c = sm.wcnt[ww][t];
+                sm.wcnt[ww][t] = static_cast<unsigned short>(total);
+                total += c;
+            }
+            sm.dstart[t] = total;
+        }
+        __syncthreads();
+        if (t < 32) {
+            unsigned v[8], run = 0;
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                v[k] = sm.dstart[8 * t + k];
+                run += v[k];
+            }
+            unsigned x = run;
+#pragma unroll
+            for (int off = 1; off < 32; off <<= 1) {
+                const unsigned y = __shfl_up_sync(FULL, x, off);
+                if (lane >= off) x += y;
+            }
+            unsigned ex = x - run;
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                sm.dstart[8 * t + k] = ex;
+                ex += v[k];
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int j = 0; j < MID_ITEMS; ++j) {
+            if (base + j * 32 + lane < n) {
+                const unsigned d = static_cast<unsigned>(img[j] >> shift) & 0xffu;
+                const unsigned l = sm.dstart[d] + sm.wcnt[w][d] + ((rank2[j / 2] >> (16 * (j & 1))) & 0xffffu);
+                sm.img[cur ^ 1][l] = img[j];
+                sm.pos[cur ^ 1][l] = pos[j];
+            }
+        }
+        __syncthreads();
+        cur ^= 1;
+    }
+    for (int i = t; i < n; i += MID_THREADS) out[i] = static_cast<long long>(sm.pos[cur][i]);
+}
+
 // The active-digit passes of argsort over (image, position) ping-pong buffers of image type IMG.
 template <class IMG>
 static vkc_status radix_argsort_passes(vkc_ctx *ctx, int items, int tiles, int64_t m, int chunks, const long long *keys,
@@ -443,6 +570,19 @@ static vkc_status argsort_i64(vkc_ctx *ctx, const vkc_value *args, int nargs, vk
     if (n <= SMALL_SORT) {
         small_argsort_kernel<<<1, 1024, 0, ctx->stream>>>(keys, static_cast<int>(n), static_cast<long long *>(o->data()));
         if ((st = launched(ctx, "small_argsort"))) return release(st);
+        out->kind = VKC_VALUE_ARRAY;
+        out->array = o;
+        return VKC_OK;
+    }
+    if (n <= MID_SORT) {
+        static std::atomic<unsigned long long> configured{0};
+        once_per_device(configured, ctx->device, [] {
+            cudaFuncSetAttribute(mid_argsort_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 static_cast<int>(sizeof(MidSmem)));
+        });
+        mid_argsort_kernel<<<1, MID_THREADS, sizeof(MidSmem), ctx->stream>>>(keys, static_cast<int>(n),
+                                                                              static_cast<long long *>(o->data()));
+        if ((st = launched(ctx, "mid_argsort"))) return release(st);
         out->kind = VKC_VALUE_ARRAY;
         out->array = o;
         return VKC_OK;
