@@ -3,7 +3,7 @@
 no float reduce_into). Parity is pinned by the notes' own property, checked on the oracle and on
 the GPU: with every key equal, the bucket holds exactly the bits of reduce_add_f64 (for every
 length, so the canonical tail rule is exercised). The GPU equals the oracle bit for bit (a NaN
-only has to be NaN) on both of its paths (at most 8 buckets: masked canonical sums; more: the
+only has to be NaN) on both of its paths (at most 16 buckets: masked canonical sums; more: the
 sorted stripe chains), and the errors are reduce_into_add_i64's."""
 
 import numpy as np
@@ -63,6 +63,7 @@ def keysets(n, seed):
         "three": ((u % np.uint64(3)).astype(np.int64), 4),
         "five": ((u % np.uint64(5)).astype(np.int64), 5),
         "nine": ((u % np.uint64(9)).astype(np.int64), 9),
+        "seventeen": ((u % np.uint64(17)).astype(np.int64), 17),
         "many": ((u % np.uint64(1000)).astype(np.int64), 1000),
         "skewed": (np.minimum((1.0 / (r + 1e-9)).astype(np.int64), 5000) - 1, 5000),
         "sparse": ((u % np.uint64(50)).astype(np.int64) * 1000, 60_000),
@@ -86,7 +87,7 @@ def test_gpu_equal_keys_give_reduce_add_bits(ctx):
         x = varied(n, 8)
         dx = ctx.upload(x)
         want = ctx.call("reduce_add_f64", dx, raw=True)[2]
-        for nb, k in ((1, 0), (9, 4)):  # the masked path and the sorted path
+        for nb, k in ((1, 0), (17, 4)):  # the masked path and the sorted path
             got = ctx.call("reduce_into_add_f64", ctx.upload(np.full(n, k, dtype=np.int64)), dx, nb).numpy()
             assert int(bits(got[k])) == want, (n, nb)
             assert not bits(np.delete(got, k)).any()

@@ -10,7 +10,7 @@
 // Equivalently, out[k] is the canonical sum of the rows with every row of another bucket read as
 // +0.0: a stripe starts at +0.0 and never holds -0.0 (a sum is -0.0 only when both terms are), so
 // adding +0.0 leaves it unchanged. Two paths:
-//  * few buckets (at most 8): that identity, per bucket: the masked rows, then reduce_add_f64
+//  * few buckets (at most 16): that identity, per bucket: the masked rows, then reduce_add_f64
 //    (one canonical pass each, about 1 ms per bucket at 2^27 rows);
 //  * otherwise: a stable argsort of the rows below b by (key, stripe), after which each stripe of
 //    each bucket is a contiguous chain that one warp adds in index order (32 rows per load, the
@@ -26,7 +26,7 @@ int64_t scan_counts_sum_words(int64_t m);
 void scan_counts(vkc_ctx *ctx, const unsigned *c, int64_t m, unsigned *sums, unsigned *out);
 vkc_status bucket_key_error(vkc_ctx *ctx, const long long *k, int64_t n, int64_t nb, bool *found);
 
-constexpr int64_t RIF_MASKED_BUCKETS = 8;
+constexpr int64_t RIF_MASKED_BUCKETS = 16;
 
 __device__ __forceinline__ double rif_f64(unsigned long long b) { return __longlong_as_double(static_cast<long long>(b)); }
 
