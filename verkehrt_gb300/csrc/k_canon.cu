@@ -470,20 +470,48 @@ __global__ void __launch_bounds__(CAND_THREADS) canon_cand_kernel(int T, int G, 
     float total;
     float run = block_exclusive_sum<float>(tot, &total);  // synchronises the block
     const double start = s_base;
+    // With the lane's base in a comfortable float range the prefixes are float sums (their
+    // error, a few float roundings of 2^-24, is far inside the 2^-12 margin) and the margins
+    // are tests of the exponent and mantissa bits: no FP64 arithmetic per tile, the scarce unit
+    // on this part. Otherwise double arithmetic.
+    const double as = fabs(start);
+    const bool in_float = as == 0.0 || (as > 0x1p-100 && as < 0x1p100);
+    const float sf = in_float ? __double2float_rn(start) : 0.f;
 #pragma unroll
     for (int j = 0; j < CAND_PER; ++j) {
         const int k = k0 + j;
         if (k >= T) break;
-        const double A = static_cast<double>(a[j]);
-        const double pre = start + static_cast<double>(run);
-        run += a[j];
-        double lo = A < 0 ? pre + A : pre, hi = A < 0 ? pre : pre + A;
-        if (hi < 0) {  // a negative sum: the binades of its magnitude
-            const double m = -hi;
-            hi = -lo;
-            lo = m;
+        int elo, ehi;
+        if (in_float) {
+            const float A = a[j], pre = sf + run;
+            run += A;
+            float lo = A < 0 ? pre + A : pre, hi = A < 0 ? pre : pre + A;
+            if (hi < 0) {
+                const float m = -hi;
+                hi = -lo;
+                lo = m;
+            }
+            // binade(lo (1 - 2^-12)) and binade(hi (1 + 2^-12)) of positive normal floats.
+            const unsigned bl = __float_as_uint(lo), bh = __float_as_uint(hi);
+            const unsigned xl = bl >> 23, xh = bh >> 23;  // a sign bit makes these >= 256
+            elo = (lo > 0.f && xl >= 1u && xl <= 254u) ? static_cast<int>(xl) - 127 - ((bl & 0x7fffffu) <= (1u << 11) ? 1 : 0)
+                                                        : NO_E;
+            ehi = (hi > 0.f && xh >= 1u && xh <= 254u)
+                      ? static_cast<int>(xh) - 127 + ((bh & 0x7fffffu) >= (1u << 23) - (1u << 12) ? 1 : 0)
+                      : NO_E;
+        } else {
+            const double A = static_cast<double>(a[j]);
+            const double pre = start + static_cast<double>(run);
+            run += a[j];
+            double lo = A < 0 ? pre + A : pre, hi = A < 0 ? pre : pre + A;
+            if (hi < 0) {  // a negative sum: the binades of its magnitude
+                const double m = -hi;
+                hi = -lo;
+                lo = m;
+            }
+            elo = binade(lo * (1.0 - 0x1p-12));
+            ehi = binade(hi * (1.0 + 0x1p-12));
         }
-        const int elo = binade(lo * (1.0 - 0x1p-12)), ehi = binade(hi * (1.0 + 0x1p-12));
         int c0 = NO_E, c1 = NO_E;
         if (elo != NO_E && ehi != NO_E && elo >= -959) {
             if (ehi == elo) c0 = elo;
@@ -512,13 +540,16 @@ __global__ void __launch_bounds__(256) canon_refine_kernel(int T, CanonWork wk) 
     for (int c = 0; c < 2; ++c) {
         const int E = wk.recE[i * 2 + c];
         if (E == NO_E) continue;
-        const double ulp = __longlong_as_double(static_cast<long long>(E - 52 + 1023) << 52);
         const TF f = wk.recD[i * 2 + c];
-        const double d = (f.d1 & SIGNED_TF) ? __ll2double_rn(static_cast<long long>(f.d0) -
-                                                             static_cast<long long>(f.d1 & ~SIGNED_TF))
-                                            : __ull2double_rn(f.d0);
-        const double v = __dmul_rn(d, ulp);
-        wk.apx[i] = v < 3.0e38 ? (v > -3.0e38 ? __double2float_rn(v) : -3.0e38f) : 3.0e38f;
+        const long long d = (f.d1 & SIGNED_TF) ? static_cast<long long>(f.d0) - static_cast<long long>(f.d1 & ~SIGNED_TF)
+                                               : static_cast<long long>(f.d0);
+        if (E - 52 >= -126 && E - 52 <= 40) {
+            // The sum in float: the increment below 2^62 times the ulp 2^(E-52), no FP64 unit.
+            wk.apx[i] = __ll2float_rn(d) * __uint_as_float(static_cast<unsigned>(E - 52 + 127) << 23);
+        } else {
+            const double v = __dmul_rn(__ll2double_rn(d), __longlong_as_double(static_cast<long long>(E - 52 + 1023) << 52));
+            wk.apx[i] = v < 3.0e38 ? (v > -3.0e38 ? __double2float_rn(v) : -3.0e38f) : 3.0e38f;
+        }
         return;
     }
 }
