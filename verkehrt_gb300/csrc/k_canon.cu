@@ -376,47 +376,53 @@ __device__ __forceinline__ float approx_row(const RowArgs &a, unsigned long long
 // choose K3's candidate binades, and K3's own sums check them afterwards (K2c), so an estimate
 // that sampling got wrong costs a second transfer function for that tile, never exactness.
 constexpr int CT_SAMPLE = CT_SEG_BLOCKS;
+constexpr int APX_TILES = 8;
 template <int OP, bool ALIGNED>
 __global__ void __launch_bounds__(CT_THREADS) canon_apx_kernel(RowArgs args, int64_t nb, int T, CanonWork wk) {
-    __shared__ float s_apx[CT_SEGS][16];
+    // APX_TILES tiles per block: each thread has one sampled load per tile in flight at once.
+    __shared__ float s_apx[APX_TILES][CT_SEGS][16];
     const int t = threadIdx.x, lp = t & 7, seg = t >> 3;
-    const int tile = blockIdx.x;
-    float a0 = 0.f, a1 = 0.f;
-    const int64_t blk0 = static_cast<int64_t>(tile) * CT_BLOCKS;
+    const int tile0 = blockIdx.x * APX_TILES;
+    unsigned long long x[APX_TILES][2], y[APX_TILES][2];
+    unsigned in = 0;  // bit q: the sampled block of tile q exists
 #pragma unroll
-    for (int i = 0; i < CT_SEG_BLOCKS; i += CT_SAMPLE) {
-        const int64_t b = blk0 + seg * CT_SEG_BLOCKS + i;
-        if (b < nb) {
+    for (int q = 0; q < APX_TILES; ++q) {
+        const int64_t b = static_cast<int64_t>(tile0 + q) * CT_BLOCKS + seg * CT_SEG_BLOCKS;
+        x[q][0] = x[q][1] = y[q][0] = y[q][1] = 0;
+        if (tile0 + q < T && b < nb) {
+            in |= 1u << q;
             const int64_t r = b * 16 + 2 * lp;
-            unsigned long long x0, x1, y0 = 0, y1 = 0;
             if (ALIGNED) {
                 const ulonglong2 xv = __ldcs(reinterpret_cast<const ulonglong2 *>(args.x + r));
-                x0 = xv.x;
-                x1 = xv.y;
+                x[q][0] = xv.x;
+                x[q][1] = xv.y;
                 if (OP == ROW_DOT) {
                     const ulonglong2 yv = __ldcs(reinterpret_cast<const ulonglong2 *>(args.y + r));
-                    y0 = yv.x;
-                    y1 = yv.y;
+                    y[q][0] = yv.x;
+                    y[q][1] = yv.y;
                 }
             } else {
-                x0 = __ldcs(args.x + r);
-                x1 = __ldcs(args.x + r + 1);
+                x[q][0] = __ldcs(args.x + r);
+                x[q][1] = __ldcs(args.x + r + 1);
                 if (OP == ROW_DOT) {
-                    y0 = __ldcs(args.y + r);
-                    y1 = __ldcs(args.y + r + 1);
+                    y[q][0] = __ldcs(args.y + r);
+                    y[q][1] = __ldcs(args.y + r + 1);
                 }
             }
-            a0 += approx_row<OP>(args, x0, y0);
-            a1 += approx_row<OP>(args, x1, y1);
         }
     }
-    s_apx[seg][2 * lp] = a0 * static_cast<float>(CT_SAMPLE);
-    s_apx[seg][2 * lp + 1] = a1 * static_cast<float>(CT_SAMPLE);
+#pragma unroll
+    for (int q = 0; q < APX_TILES; ++q) {
+        const bool ok = (in >> q) & 1u;
+        s_apx[q][seg][2 * lp] = ok ? approx_row<OP>(args, x[q][0], y[q][0]) * static_cast<float>(CT_SAMPLE) : 0.f;
+        s_apx[q][seg][2 * lp + 1] = ok ? approx_row<OP>(args, x[q][1], y[q][1]) * static_cast<float>(CT_SAMPLE) : 0.f;
+    }
     __syncthreads();
-    if (t < 16) {
+    if (t < 16 * APX_TILES) {
+        const int q = t >> 4, L = t & 15;
         float A = 0.f;
-        for (int s = 0; s < CT_SEGS; ++s) A += s_apx[s][t];
-        wk.apx[static_cast<int64_t>(t) * T + tile] = A;
+        for (int sg = 0; sg < CT_SEGS; ++sg) A += s_apx[q][sg][L];
+        if (tile0 + q < T) wk.apx[static_cast<int64_t>(L) * T + tile0 + q] = A;
     }
 }
 
@@ -1013,7 +1019,7 @@ template <int OP, bool ALIGNED>
 static vkc_status launch_canon(vkc_ctx *ctx, const RowArgs &a, int64_t nb, int T, int C, const CanonWork &wk,
                                CanonState *state) {
     vkc_status st;
-    canon_apx_kernel<OP, ALIGNED><<<T, CT_THREADS, 0, ctx->stream>>>(a, nb, T, wk);
+    canon_apx_kernel<OP, ALIGNED><<<(T + APX_TILES - 1) / APX_TILES, CT_THREADS, 0, ctx->stream>>>(a, nb, T, wk);
     if ((st = launched(ctx, "canon_apx"))) return st;
     const int G = (T + CAND_GROUP - 1) / CAND_GROUP;
     canon_gsum_kernel<<<16 * G, 256, 0, ctx->stream>>>(T, G, wk);
