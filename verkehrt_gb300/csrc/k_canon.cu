@@ -90,7 +90,9 @@ __device__ __forceinline__ unsigned long long sat_add(unsigned long long a, unsi
 // (no parity dependence): up and dn are the sums of the increments of the positive and the
 // negative rows, so the net increment is up - dn and every state between stays within
 // [S - dn, S + up]. An unsigned one without a parity dependence (d0 == d1) has the signed
-// form {d0, 0}. Saturated parts (at SAT) never apply.
+// form {d0, 0}. Saturated parts (at SAT) never apply. (Exact running bounds, the prefix's
+// maximum and minimum stored as rounded-up floats, were slower: a sum that wanders around
+// zero crosses binades whatever the bounds, and the encoding lengthened the walk.)
 constexpr unsigned long long SIGNED_TF = 1ull << 63;
 
 __device__ __forceinline__ bool as_signed(TF f, unsigned long long *up, unsigned long long *dn) {
