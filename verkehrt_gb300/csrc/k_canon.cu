@@ -18,13 +18,16 @@
 //    of a run of rows on S is a pair of integer increments (d0, d1) for even and odd S: a
 //    "transfer function". Transfer functions compose associatively.
 //  * The rows are cut into 4096-row tiles (256 blocks of 16 rows, 256 rows per lane, in 32
-//    segments of 8 blocks), and five kernels, none of which waits on another block, find the
+//    segments of 8 blocks), and these kernels, none of which waits on another block, find the
 //    exact lane states:
-//      K1  the approximate (float) lane sums of every tile, in one read of the rows;
+//      K1  the approximate (float) lane sums of every tile, estimated from one 16-row block
+//          per segment (an eighth of the rows);
 //      K2  per lane, their exclusive prefix over the tiles from the lane's exact state (group
-//          sums, then a scan inside each group), and each tile's candidate binades (the approximate range widened by 2^-12 must lie in one
-//          binade or two adjacent ones);
-//      K3  each tile's transfer function per lane and candidate binade, in a second read;
+//          sums, then a scan inside each group), and each tile's candidate binades (the
+//          approximate range widened by 2^-12 must lie in one binade or two adjacent ones);
+//      K3  each tile's transfer function per lane and candidate binade, in one read of the
+//          rows; then the check: K2 again on K3's own sums, and K3 again on the few tiles whose
+//          binades the sampled candidates missed or that hold negative rows;
 //      K4a per lane and 32-tile chunk, the composed transfer function when the chunk's tiles
 //          share one;
 //      K4b per lane, a walk from the exact state: whole chunks while their transfer function
