@@ -57,6 +57,8 @@ def lib():
         L.orc_where.argtypes = [P, I64, I64, P]
         L.orc_scan_add_i64.argtypes = [P, I64, P]
         L.orc_scan_by_add_i64.argtypes = [P, P, I64, P]
+        L.orc_scan_add_f64.argtypes = [P, I64, P]
+        L.orc_scan_by_add_f64.argtypes = [P, P, I64, P]
         L.orc_prev_i64.argtypes = [P, I64, I64, P]
         L.orc_gather.argtypes = [P, ctypes.c_int, I64, P, I64, P, ctypes.c_char_p]
         L.orc_histogram.argtypes = [P, I64, I64, P, ctypes.c_char_p]
@@ -280,6 +282,25 @@ def reduce_into_add_i64(keys, vals, buckets):
     out = np.empty(max(0, min(buckets, 1 << 28)), dtype=np.int64)
     buf = ctypes.create_string_buffer(ERR_LEN)
     _err(lib().orc_reduce_into_add_i64(_p(keys), _p(vals), len(keys), buckets, _p(out), buf), buf)
+    return out
+
+
+def scan_add_f64(x):
+    """Prefix canonical sums: out[i] = reduce_add_f64(x[:i + 1]) (the candidate float scan order
+    of the reference's tier-2 notes; oracle.c orc_scan_add_f64)."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    out = np.empty(len(x), dtype=np.float64)
+    lib().orc_scan_add_f64(_p(x), len(x), _p(out))
+    return out
+
+
+def scan_by_add_f64(x, starts):
+    """scan_add_f64 restarted at every set start flag (row 0 always starts)."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    s = np.ascontiguousarray(starts, dtype=np.uint8)
+    assert len(s) == len(x)
+    out = np.empty(len(x), dtype=np.float64)
+    lib().orc_scan_by_add_f64(_p(x), _p(s), len(x), _p(out))
     return out
 
 

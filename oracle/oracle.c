@@ -283,6 +283,47 @@ void orc_scan_by_add_i64(const int64_t *x, const uint8_t *starts, int64_t n, int
     }
 }
 
+/* Float scans: the reference has none (scan.rs:408-415 lists the gap). Its tier-2 design notes
+ * (docs/superpowers/specs/2026-10-31-verkehrt-tier2-design.md:172) give the candidate order
+ * restated here: out[i] is the canonical sum (reduce.rs:45-91) of the prefix x[0..=i], so
+ * out[n - 1] is reduce_add_f64 of the whole array. One pass keeps the 16 lane accumulators:
+ * before each 16-row block the lanes combine (+8, +4, +2, +1) into the prefix's base, the
+ * block's first 15 rows fold into it in order (the canonical tail), and the 16th row's prefix
+ * is the combine of the lanes after the block. scan_by restarts at every row whose start flag
+ * is set (row 0 always starts), with the lanes numbered from the segment's first row. */
+static void scan_f64_segment(const double *x, int64_t n, double *out) {
+    double lanes[LANES];
+    for (int j = 0; j < LANES; ++j) lanes[j] = 0.0;
+    double base = 0.0; /* the combine of lanes that all hold +0.0 */
+    for (int64_t b0 = 0; b0 < n; b0 += LANES) {
+        int64_t cnt = n - b0 < LANES ? n - b0 : LANES;
+        double t = base;
+        for (int64_t r = 0; r < cnt && r < LANES - 1; ++r) {
+            t = t + x[b0 + r];
+            out[b0 + r] = t;
+        }
+        if (cnt == LANES) {
+            double acc[LANES];
+            for (int j = 0; j < LANES; ++j) acc[j] = lanes[j] = lanes[j] + x[b0 + j];
+            for (int step = LANES / 2; step > 0; step /= 2)
+                for (int j = 0; j < step; ++j) acc[j] = acc[j] + acc[j + step];
+            base = acc[0];
+            out[b0 + LANES - 1] = base;
+        }
+    }
+}
+
+void orc_scan_add_f64(const double *x, int64_t n, double *out) { scan_f64_segment(x, n, out); }
+
+void orc_scan_by_add_f64(const double *x, const uint8_t *starts, int64_t n, double *out) {
+    int64_t s = 0;
+    for (int64_t i = 1; i <= n; ++i)
+        if (i == n || starts[i] != 0) {
+            scan_f64_segment(x + s, i - s, out + s);
+            s = i;
+        }
+}
+
 /* scan.rs:16-48 (Prev) */
 void orc_prev_i64(const int64_t *x, int64_t n, int64_t fill, int64_t *out) {
     for (int64_t i = 0; i < n; ++i) out[i] = i == 0 ? fill : x[i - 1];

@@ -72,6 +72,9 @@ int64_t orc_where(const uint8_t *mask, int64_t n, int64_t base, int64_t *out);
 /* scan.rs:284-326: inclusive wrapping prefix sum, and the segmented one */
 void orc_scan_add_i64(const int64_t *x, int64_t n, int64_t *out);
 void orc_scan_by_add_i64(const int64_t *x, const uint8_t *starts, int64_t n, int64_t *out);
+/* the tier-2 notes' candidate float scan order (no reference kernel): prefix canonical sums */
+void orc_scan_add_f64(const double *x, int64_t n, double *out);
+void orc_scan_by_add_f64(const double *x, const uint8_t *starts, int64_t n, double *out);
 /* scan.rs:16-48 */
 void orc_prev_i64(const int64_t *x, int64_t n, int64_t fill, int64_t *out);
 

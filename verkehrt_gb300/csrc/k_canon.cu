@@ -47,6 +47,9 @@
 
 namespace vkc {
 
+int64_t scan_counts_sum_words(int64_t m);
+void scan_counts(vkc_ctx *ctx, const unsigned *c, int64_t m, unsigned *sums, unsigned *out);
+
 constexpr int CT_THREADS = 256;
 constexpr int CT_SEGS = 32;       // segments per tile
 constexpr int CT_SEG_BLOCKS = 8;  // 16-row blocks per segment
@@ -314,6 +317,8 @@ struct CanonWork {
     int *flags;                // [T] tiles whose transfer functions are recomputed (K3 again);
                                // [T]: some tile has a negative row; [T + 1]: the number of
                                // flagged tiles, listed from [T + 2]
+    unsigned long long *tstate = nullptr;  // scans: [16][T + 1] exact lane state before each tile
+    int *whole = nullptr;                  // scans: [16][C] chunks the walk took whole
 };
 
 constexpr int CAND_GROUP = 1024;  // tiles per K2 block
@@ -777,7 +782,7 @@ __device__ __forceinline__ int state_binade(unsigned long long s) {
 // count and, in *out, the state after them.
 template <bool SIGNED = true>
 __device__ __forceinline__ int apply_prefix(TF f, bool usable, unsigned long long s, int E,
-                                            unsigned long long *out) {
+                                            unsigned long long *out, unsigned long long *mine = nullptr) {
     const int lane = threadIdx.x & 31;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -786,6 +791,7 @@ __device__ __forceinline__ int apply_prefix(TF f, bool usable, unsigned long lon
     }
     unsigned long long r = 0;
     const bool ok = usable && apply<SIGNED>(s, E, f, &r);
+    if (mine) *mine = r;  // this lane's state (valid below the returned count)
     const unsigned bad = __ballot_sync(FULL, !ok);
     const int m = bad ? __ffs(bad) - 1 : 32;
     if (m > 0) *out = __shfl_sync(FULL, r, m - 1);
@@ -864,9 +870,57 @@ struct WalkSmem {
     int nmixed;
 };
 
+// Chunk k of lane L tile by tile from state s (one warp): runs of tiles whose transfer
+// functions hold, and the tiles none carries resolved from the rows. RECORD (scans) stores the
+// exact state before each tile. sm and slot give the chunk's tile records when the walk holds
+// them in shared memory (slot >= 0).
+template <int OP, bool SIGNED, bool RECORD>
+__device__ __forceinline__ unsigned long long walk_chunk_tiles(const RowArgs &args, int64_t nb, int T, const CanonWork &wk,
+                                                               const WalkSmem *sm, int slot, int L, int k,
+                                                               unsigned long long s) {
+    const int lane = threadIdx.x & 31;
+    unsigned long long *rec = RECORD ? wk.tstate + static_cast<int64_t>(L) * (T + 1) : nullptr;
+    int tp = k * 32;
+    const int end = min(T, tp + 32);
+    while (tp < end) {
+        if (RECORD && lane == 0) rec[tp] = s;
+        const int Et = state_binade(s);
+        const int tl = tp + lane;
+        TF g{0, 0};
+        bool usable = false;
+        if (tl < end && Et != NO_E) {
+            if (slot >= 0) {
+                const int j = tl - k * 32;
+                if (sm->mE[slot][j][0] == Et) {
+                    g = sm->mD[slot][j][0];
+                    usable = true;
+                } else if (sm->mE[slot][j][1] == Et) {
+                    g = sm->mD[slot][j][1];
+                    usable = true;
+                }
+            } else {
+                usable = tile_tf(wk, T, L, tl, Et, &g);
+            }
+        }
+        unsigned long long r = s, mine = 0;
+        const int mt = Et == NO_E ? 0 : apply_prefix<SIGNED>(g, usable, s, Et, &r, RECORD ? &mine : nullptr);
+        if (mt > 0) {
+            if (RECORD && lane + 1 < mt) rec[tp + lane + 1] = mine;
+            s = r;
+            tp += mt;
+        } else {
+            s = resolve_tile<OP, SIGNED>(args, nb, tp, L, s);
+            ++tp;
+        }
+    }
+    return s;
+}
+
 // The walk of lane L from state s (warp 0 of the lane's block), with the signed functions
 // when some tile has a negative row or the state is negative (SIGNED), else the shorter code.
-template <int OP, bool SIGNED>
+// RECORD (scans) stores the state before each chunk it takes whole, marks it in wk.whole, and
+// the state before each tile of the others.
+template <int OP, bool SIGNED, bool RECORD>
 __device__ __forceinline__ unsigned long long walk_lane(const RowArgs &args, int64_t nb, int T, int C, const CanonWork &wk,
                                                         const WalkSmem &sm, bool held, const int *gE, const TF *gD,
                                                         int L, unsigned long long s) {
@@ -882,51 +936,29 @@ __device__ __forceinline__ unsigned long long walk_lane(const RowArgs &args, int
             ce = held ? sm.chunkE[kc] : gE[kc];
             if (ce != NO_E && ce == E) f = held ? sm.chunkD[kc] : gD[kc];
         }
-        unsigned long long r = s;
-        int m = E == NO_E ? 0 : apply_prefix<SIGNED>(f, kc < C && ce != NO_E && ce == E, s, E, &r);
+        unsigned long long r = s, mine = 0;
+        int m = E == NO_E ? 0
+                          : apply_prefix<SIGNED>(f, kc < C && ce != NO_E && ce == E, s, E, &r,
+                                                 RECORD ? &mine : nullptr);
         if (m > 0) {
+            if (RECORD) {
+                unsigned long long *rec = wk.tstate + static_cast<int64_t>(L) * (T + 1);
+                if (lane == 0) rec[k * 32] = s;
+                if (lane + 1 < m) rec[(k + lane + 1) * 32] = mine;
+                if (lane < m) wk.whole[static_cast<int64_t>(L) * C + kc] = 1;
+            }
             s = r;
             k += m;
             continue;
         }
         // Chunk k, tile by tile.
-        const int slot = held ? sm.mixed_of[k] : -1;
-        int tp = k * 32;
-        const int end = min(T, tp + 32);
-        while (tp < end) {
-            const int Et = state_binade(s);
-            const int tl = tp + lane;
-            TF g{0, 0};
-            bool usable = false;
-            if (tl < end && Et != NO_E) {
-                if (slot >= 0) {
-                    const int j = tl - k * 32;
-                    if (sm.mE[slot][j][0] == Et) {
-                        g = sm.mD[slot][j][0];
-                        usable = true;
-                    } else if (sm.mE[slot][j][1] == Et) {
-                        g = sm.mD[slot][j][1];
-                        usable = true;
-                    }
-                } else {
-                    usable = tile_tf(wk, T, L, tl, Et, &g);
-                }
-            }
-            int mt = Et == NO_E ? 0 : apply_prefix<SIGNED>(g, usable, s, Et, &r);
-            if (mt > 0) {
-                s = r;
-                tp += mt;
-            } else {
-                s = resolve_tile<OP, SIGNED>(args, nb, tp, L, s);
-                ++tp;
-            }
-        }
+        s = walk_chunk_tiles<OP, SIGNED, RECORD>(args, nb, T, wk, &sm, held ? sm.mixed_of[k] : -1, L, k, s);
         ++k;
     }
     return s;
 }
 
-template <int OP>
+template <int OP, bool RECORD>
 __global__ void __launch_bounds__(WK_THREADS) canon_walk_kernel(RowArgs args, int64_t nb, int T, int C, CanonWork wk,
                                                                 CanonState *state) {
     extern __shared__ __align__(16) unsigned char walk_smem[];
@@ -975,9 +1007,29 @@ __global__ void __launch_bounds__(WK_THREADS) canon_walk_kernel(RowArgs args, in
     if (t >= 32) return;
     const int lane = t;
     unsigned long long s = state->lanes[L];
-    s = (wk.flags[T] != 0 || (s >> 63)) ? walk_lane<OP, true>(args, nb, T, C, wk, sm, held, gE, gD, L, s)
-                                        : walk_lane<OP, false>(args, nb, T, C, wk, sm, held, gE, gD, L, s);
-    if (lane == 0) state->lanes[L] = s;
+    s = (wk.flags[T] != 0 || (s >> 63)) ? walk_lane<OP, true, RECORD>(args, nb, T, C, wk, sm, held, gE, gD, L, s)
+                                        : walk_lane<OP, false, RECORD>(args, nb, T, C, wk, sm, held, gE, gD, L, s);
+    if (lane == 0) {
+        state->lanes[L] = s;
+        if (RECORD) wk.tstate[static_cast<int64_t>(L) * (T + 1) + T] = s;
+    }
+}
+
+// Scans, after the walk: the state before every tile of the chunks it took whole, one warp per
+// lane and chunk, by the walk's own tile steps from the chunk's recorded state (any prefix of a
+// chunk whose composed function applied applies as well: increments only add up, and a signed
+// function's bounds cover its prefixes').
+template <int OP>
+__global__ void __launch_bounds__(256) canon_fill_kernel(RowArgs args, int64_t nb, int T, int C, CanonWork wk) {
+    const int64_t gw = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    if (gw >= static_cast<int64_t>(16) * C) return;
+    const int L = static_cast<int>(gw / C), k = static_cast<int>(gw % C);
+    if (!wk.whole[static_cast<int64_t>(L) * C + k]) return;
+    const unsigned long long s = wk.tstate[static_cast<int64_t>(L) * (T + 1) + k * 32];
+    if (wk.flags[T] != 0 || (s >> 63))
+        walk_chunk_tiles<OP, true, true>(args, nb, T, wk, nullptr, -1, L, k, s);
+    else
+        walk_chunk_tiles<OP, false, true>(args, nb, T, wk, nullptr, -1, L, k, s);
 }
 
 // Short inputs: the reference's own order, each lane a chain of IEEE adds over its rows
@@ -1020,7 +1072,8 @@ __global__ void canon_finish(CanonState *state, int tail_len) {
     state->result = as_bits(r);
 }
 
-template <int OP, bool ALIGNED>
+// RECORD (scans): the walk also stores the exact lane state before every tile in wk.tstate.
+template <int OP, bool ALIGNED, bool RECORD = false>
 static vkc_status launch_canon(vkc_ctx *ctx, const RowArgs &a, int64_t nb, int T, int C, const CanonWork &wk,
                                CanonState *state) {
     vkc_status st;
@@ -1047,11 +1100,49 @@ static vkc_status launch_canon(vkc_ctx *ctx, const RowArgs &a, int64_t nb, int T
     if ((st = launched(ctx, "canon_chunk"))) return st;
     static std::atomic<unsigned long long> configured{0};
     once_per_device(configured, ctx->device, [] {
-        cudaFuncSetAttribute(canon_walk_kernel<OP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cudaFuncSetAttribute(canon_walk_kernel<OP, RECORD>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              static_cast<int>(sizeof(WalkSmem)));
     });
-    canon_walk_kernel<OP><<<16, WK_THREADS, sizeof(WalkSmem), ctx->stream>>>(a, nb, T, C, wk, state);
-    return launched(ctx, "canon_walk");
+    if constexpr (RECORD) VKC_CUDA(ctx, cudaMemsetAsync(wk.whole, 0, static_cast<size_t>(C) * 16 * sizeof(int), ctx->stream));
+    canon_walk_kernel<OP, RECORD><<<16, WK_THREADS, sizeof(WalkSmem), ctx->stream>>>(a, nb, T, C, wk, state);
+    if ((st = launched(ctx, "canon_walk"))) return st;
+    if constexpr (RECORD) {
+        canon_fill_kernel<OP><<<(warps + 7) / 8, 256, 0, ctx->stream>>>(a, nb, T, C, wk);
+        if ((st = launched(ctx, "canon_fill"))) return st;
+    }
+    return VKC_OK;
+}
+
+// The work arrays of one canonical pass over T tiles (C chunks) in one scratch block starting
+// at b; SCAN adds the tile states, the whole-chunk marks and the pass's own lane state. Returns
+// the block's size (b == nullptr: only the size).
+static size_t canon_layout(int T, int C, bool scan, char *b, CanonWork *wk, CanonState **cs) {
+    auto up = [](size_t v) { return (v + 255) & ~size_t(255); };
+    const size_t t16 = static_cast<size_t>(T) * 16, c16 = static_cast<size_t>(C) * 16;
+    const size_t o_cand = up(t16 * sizeof(float));
+    const size_t o_recE = o_cand + up(t16 * 2 * sizeof(int));
+    const size_t o_recD = o_recE + up(t16 * 2 * sizeof(int));
+    const size_t o_chE = o_recD + up(t16 * 2 * sizeof(TF));
+    const size_t o_chD = o_chE + up(c16 * sizeof(int));
+    const size_t g16 = static_cast<size_t>((T + CAND_GROUP - 1) / CAND_GROUP) * 16;
+    const size_t o_gs = o_chD + up(c16 * sizeof(TF));
+    const size_t o_fl = o_gs + up(g16 * sizeof(double));
+    const size_t o_ts = o_fl + up(static_cast<size_t>(2 * T + 2) * sizeof(int));
+    const size_t o_wh = o_ts + up(static_cast<size_t>(T + 1) * 16 * sizeof(unsigned long long));
+    const size_t o_cs = o_wh + up(c16 * sizeof(int));
+    const size_t total = scan ? o_cs + sizeof(CanonState) : o_fl + static_cast<size_t>(2 * T + 2) * sizeof(int);
+    if (b) {
+        *wk = CanonWork{reinterpret_cast<float *>(b), reinterpret_cast<int *>(b + o_cand),
+                        reinterpret_cast<int *>(b + o_recE), reinterpret_cast<TF *>(b + o_recD),
+                        reinterpret_cast<int *>(b + o_chE), reinterpret_cast<TF *>(b + o_chD),
+                        reinterpret_cast<double *>(b + o_gs), reinterpret_cast<int *>(b + o_fl)};
+        if (scan) {
+            wk->tstate = reinterpret_cast<unsigned long long *>(b + o_ts);
+            wk->whole = reinterpret_cast<int *>(b + o_wh);
+            *cs = reinterpret_cast<CanonState *>(b + o_cs);
+        }
+    }
+    return total;
 }
 
 // The canonical reducer of one row operation.
@@ -1107,23 +1198,10 @@ struct CanonReducer : DevReducer {
             const int64_t T64 = (nb + CT_BLOCKS - 1) / CT_BLOCKS;
             if (T64 > (int64_t(1) << 26)) return fail(ctx, VKC_USAGE, "array too long for one update");
             const int T = static_cast<int>(T64), C = (T + 31) / 32;
-            const size_t t16 = static_cast<size_t>(T) * 16, c16 = static_cast<size_t>(C) * 16;
-            const size_t o_cand = (t16 * 4 + 255) & ~size_t(255);
-            const size_t o_recE = o_cand + ((t16 * 8 + 255) & ~size_t(255));
-            const size_t o_recD = o_recE + ((t16 * 8 + 255) & ~size_t(255));
-            const size_t o_chE = o_recD + t16 * 2 * sizeof(TF);
-            const size_t o_chD = o_chE + ((c16 * 4 + 255) & ~size_t(255));
-            const size_t g16 = static_cast<size_t>((T + CAND_GROUP - 1) / CAND_GROUP) * 16;
-            const size_t o_gs = o_chD + ((c16 * sizeof(TF) + 255) & ~size_t(255));
-            const size_t o_fl = o_gs + ((g16 * sizeof(double) + 255) & ~size_t(255));
-            const size_t total = o_fl + static_cast<size_t>(2 * T + 2) * sizeof(int);
             void *p;
-            if ((st = scratch(ctx, total, &p))) return st;
-            char *b = static_cast<char *>(p);
-            CanonWork wk{reinterpret_cast<float *>(b), reinterpret_cast<int *>(b + o_cand),
-                         reinterpret_cast<int *>(b + o_recE), reinterpret_cast<TF *>(b + o_recD),
-                         reinterpret_cast<int *>(b + o_chE), reinterpret_cast<TF *>(b + o_chD),
-                         reinterpret_cast<double *>(b + o_gs), reinterpret_cast<int *>(b + o_fl)};
+            if ((st = scratch(ctx, canon_layout(T, C, false, nullptr, nullptr, nullptr), &p))) return st;
+            CanonWork wk;
+            canon_layout(T, C, false, static_cast<char *>(p), &wk, nullptr);
             const bool aligned = (reinterpret_cast<uintptr_t>(a.x) & 15) == 0 &&
                                  (op != ROW_DOT || (reinterpret_cast<uintptr_t>(a.y) & 15) == 0);
             switch (op) {
@@ -1158,6 +1236,297 @@ struct CanonReducer : DevReducer {
     }
 };
 
+// ---------------------------------------------------------------------------- float scans
+// scan_add_f64 and scan_by_add_f64: the reference has no float scans (scan.rs:408-415 lists the
+// gap); its tier-2 design notes (docs/superpowers/specs/2026-10-31-verkehrt-tier2-design.md:172)
+// give the candidate order built here: out[i] is the canonical sum of the prefix x[0..=i], so
+// out[n - 1] is reduce_add_f64 of the array. With the exact lane states before each 16-row
+// block, the prefix ending at row 16k + r (r < 15) is the combine (+8, +4, +2, +1) of the lane
+// states before block k followed by rows 16k .. 16k + r in order (the canonical tail), and the
+// prefix ending at row 16k + 15 is the combine of the lane states after block k.
+//
+// The lane states before each 4096-row tile come from the canonical pass in record mode (the
+// walk, then canon_fill_kernel); one block per tile then runs the 16 lane chains over the
+// tile's blocks with IEEE adds, each block's combine and each block's tail chain. Shared rows
+// are padded to 17 doubles per 16 so that the threads of a warp, one per block, read different
+// banks.
+constexpr int SCAN_PAD = 17;
+struct ScanSmem {
+    double v[CT_BLOCKS * SCAN_PAD];         // the tile's rows, then its outputs
+    double st[(CT_BLOCKS + 1) * SCAN_PAD];  // lane states before block j, j = 0 .. 256
+    double c[CT_BLOCKS + 1];                // their combines
+};
+
+__global__ void __launch_bounds__(256) canon_scan_kernel(const unsigned long long *__restrict__ x, int64_t n, int64_t nb,
+                                                         int T, const unsigned long long *__restrict__ tstate,
+                                                         unsigned long long *__restrict__ out) {
+    extern __shared__ __align__(16) unsigned char scan_smem[];
+    ScanSmem &sm = *reinterpret_cast<ScanSmem *>(scan_smem);
+    const int t = blockIdx.x, tid = threadIdx.x;
+    const int64_t row0 = static_cast<int64_t>(t) * (CT_BLOCKS * 16);
+    const int64_t left = n - row0;
+    const int rows = left < CT_BLOCKS * 16 ? static_cast<int>(left) : CT_BLOCKS * 16;
+    for (int i = tid; i < rows; i += 256) sm.v[(i >> 4) * SCAN_PAD + (i & 15)] = as_f64(x[row0 + i]);
+    // The tile's whole blocks (all but a partial last one) feed the lanes.
+    const int64_t whole = nb - static_cast<int64_t>(t) * CT_BLOCKS;
+    const int fb = whole <= 0 ? 0 : (whole < CT_BLOCKS ? static_cast<int>(whole) : CT_BLOCKS);
+    __syncthreads();
+    if (tid < 16) {
+        double s = tstate ? as_f64(tstate[static_cast<int64_t>(tid) * (T + 1) + t]) : 0.0;
+        sm.st[tid] = s;
+        for (int j = 0; j < fb; ++j) {
+            s = __dadd_rn(s, sm.v[j * SCAN_PAD + tid]);
+            sm.st[(j + 1) * SCAN_PAD + tid] = s;
+        }
+    }
+    __syncthreads();
+    for (int j = tid; j <= fb; j += 256) {
+        double a[16];
+#pragma unroll
+        for (int q = 0; q < 16; ++q) a[q] = sm.st[j * SCAN_PAD + q];
+#pragma unroll
+        for (int step = 8; step > 0; step >>= 1)
+#pragma unroll
+            for (int q = 0; q < step; ++q) a[q] = __dadd_rn(a[q], a[q + step]);
+        sm.c[j] = a[0];
+    }
+    __syncthreads();
+    const int nbt = (rows + 15) >> 4;  // blocks in the tile, a partial last one included
+    for (int j = tid; j < nbt; j += 256) {
+        double c = sm.c[j];
+        const int cnt = min(16, rows - 16 * j);
+        double *v = sm.v + j * SCAN_PAD;
+#pragma unroll
+        for (int r = 0; r < 15; ++r) {
+            if (r < cnt) {
+                c = __dadd_rn(c, v[r]);
+                v[r] = c;
+            }
+        }
+        if (cnt == 16) v[15] = sm.c[j + 1];  // a whole block: j < fb
+    }
+    __syncthreads();
+    for (int i = tid; i < rows; i += 256) out[row0 + i] = as_bits(sm.v[(i >> 4) * SCAN_PAD + (i & 15)]);
+}
+
+// The prefix canonical sums of rows x[0 .. n) into out[0 .. n).
+static vkc_status canon_scan_rows(vkc_ctx *ctx, const unsigned long long *x, int64_t n, unsigned long long *out) {
+    if (n == 0) return VKC_OK;
+    vkc_status st;
+    const int64_t nb = n / 16;
+    const int64_t tiles = ((n + 15) / 16 + CT_BLOCKS - 1) / CT_BLOCKS;
+    if (tiles > (int64_t(1) << 26)) return fail(ctx, VKC_USAGE, "array too long for one scan");
+    const unsigned long long *tstate = nullptr;
+    int T = 0;
+    if (tiles > 1) {  // then nb >= CT_BLOCKS
+        T = static_cast<int>((nb + CT_BLOCKS - 1) / CT_BLOCKS);
+        const int C = (T + 31) / 32;
+        void *p;
+        if ((st = scratch(ctx, canon_layout(T, C, true, nullptr, nullptr, nullptr), &p))) return st;
+        CanonWork wk;
+        CanonState *cs = nullptr;
+        canon_layout(T, C, true, static_cast<char *>(p), &wk, &cs);
+        VKC_CUDA(ctx, cudaMemsetAsync(cs, 0, sizeof(CanonState), ctx->stream));
+        RowArgs a{};
+        a.x = x;
+        st = (reinterpret_cast<uintptr_t>(x) & 15) == 0 ? launch_canon<ROW_SUM, true, true>(ctx, a, nb, T, C, wk, cs)
+                                                        : launch_canon<ROW_SUM, false, true>(ctx, a, nb, T, C, wk, cs);
+        if (st) return st;
+        tstate = wk.tstate;
+    }
+    static std::atomic<unsigned long long> configured{0};
+    once_per_device(configured, ctx->device, [] {
+        cudaFuncSetAttribute(canon_scan_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             static_cast<int>(sizeof(ScanSmem)));
+    });
+    canon_scan_kernel<<<static_cast<unsigned>(tiles), 256, sizeof(ScanSmem), ctx->stream>>>(x, n, nb, T, tstate, out);
+    return launched(ctx, "canon_scan");
+}
+
+static vkc_status scan_add_f64(vkc_ctx *ctx, const vkc_value *args, int, vkc_value *out) {
+    vkc_status st;
+    if (!array_arg(ctx, args[0], VKC_F64, &st)) return st;
+    const vkc_array *xa = args[0].array;
+    vkc_array *o;
+    if ((st = new_array(ctx, VKC_F64, xa->len, false, &o))) return st;
+    st = canon_scan_rows(ctx, static_cast<const unsigned long long *>(xa->data()), xa->len,
+                         static_cast<unsigned long long *>(o->data()));
+    if (st) {
+        vkc_array_release(o);
+        return st;
+    }
+    out->kind = VKC_VALUE_ARRAY;
+    out->array = o;
+    return VKC_OK;
+}
+
+// scan_by_add_f64: each segment (from a row whose start flag is set, row 0 always, to the next)
+// is scanned with its lanes numbered from its first row. Segment heads are listed in order
+// (a count per 4096-row tile, a scan, an ordered write); one thread scans each segment of at
+// most SB_SHORT rows in registers (the 16 lanes, each block's combine and tail); longer
+// segments, listed for the host, take the tiled scan above on their rows.
+constexpr int SB_TILE = 4096;
+constexpr int64_t SB_SHORT = int64_t(1) << 16;
+
+__device__ __forceinline__ unsigned sb_heads(const unsigned char *__restrict__ starts, int64_t n, int64_t r0, unsigned *mask) {
+    unsigned m = 0;
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+        const int64_t i = r0 + j;
+        if (i < n && (i == 0 || starts[i] != 0)) m |= 1u << j;
+    }
+    *mask = m;
+    return __popc(m);
+}
+
+__global__ void __launch_bounds__(256) sb_count_kernel(const unsigned char *__restrict__ starts, int64_t n,
+                                                       unsigned *__restrict__ counts) {
+    unsigned m, total;
+    const unsigned c = sb_heads(starts, n, static_cast<int64_t>(blockIdx.x) * SB_TILE + threadIdx.x * 16, &m);
+    block_exclusive_sum<unsigned>(c, &total);
+    if (threadIdx.x == 0) counts[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(256) sb_list_kernel(const unsigned char *__restrict__ starts, int64_t n,
+                                                      const unsigned *__restrict__ offs, long long *__restrict__ heads) {
+    unsigned m, total;
+    const int64_t r0 = static_cast<int64_t>(blockIdx.x) * SB_TILE + threadIdx.x * 16;
+    const unsigned c = sb_heads(starts, n, r0, &m);
+    unsigned at = offs[blockIdx.x] + block_exclusive_sum<unsigned>(c, &total);
+    while (m) {
+        const int j = __ffs(m) - 1;
+        m &= m - 1;
+        heads[at++] = r0 + j;
+    }
+}
+
+// One segment [s, e) of at most SB_SHORT rows, in the order of the oracle's restatement.
+__device__ void sb_segment(const unsigned long long *__restrict__ x, int64_t s, int64_t e,
+                           unsigned long long *__restrict__ out) {
+    double lane[16];
+#pragma unroll
+    for (int j = 0; j < 16; ++j) lane[j] = 0.0;
+    double base = 0.0;  // the combine of the lanes before the block (+0.0 while all are +0.0)
+    for (int64_t b0 = s; b0 < e; b0 += 16) {
+        const int64_t cnt = e - b0;
+        if (cnt >= 16) {
+            double v[16];
+#pragma unroll
+            for (int j = 0; j < 16; ++j) v[j] = as_f64(x[b0 + j]);
+            double t = base;
+#pragma unroll
+            for (int r = 0; r < 15; ++r) {
+                t = __dadd_rn(t, v[r]);
+                out[b0 + r] = as_bits(t);
+            }
+            double a[16];
+#pragma unroll
+            for (int j = 0; j < 16; ++j) a[j] = lane[j] = __dadd_rn(lane[j], v[j]);
+#pragma unroll
+            for (int step = 8; step > 0; step >>= 1)
+#pragma unroll
+                for (int q = 0; q < step; ++q) a[q] = __dadd_rn(a[q], a[q + step]);
+            base = a[0];
+            out[b0 + 15] = as_bits(base);
+        } else {
+            double t = base;
+            for (int64_t i = b0; i < e; ++i) {
+                t = __dadd_rn(t, as_f64(x[i]));
+                out[i] = as_bits(t);
+            }
+        }
+    }
+}
+
+// Every segment: the short ones here, the long ones listed as (first row, rows) pairs after a
+// count in longs[0].
+__global__ void __launch_bounds__(128) sb_segment_kernel(const unsigned long long *__restrict__ x, int64_t n,
+                                                         const long long *__restrict__ heads,
+                                                         const unsigned *__restrict__ offs,
+                                                         const unsigned *__restrict__ counts, int tiles,
+                                                         unsigned long long *__restrict__ out,
+                                                         unsigned long long *__restrict__ longs) {
+    const int64_t G = static_cast<int64_t>(offs[tiles - 1]) + counts[tiles - 1];
+    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    for (int64_t g = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; g < G; g += stride) {
+        const int64_t s = heads[g], e = g + 1 < G ? heads[g + 1] : n;
+        if (e - s > SB_SHORT) {
+            const unsigned long long k = atomicAdd(longs, 1ull);
+            longs[1 + 2 * k] = static_cast<unsigned long long>(s);
+            longs[2 + 2 * k] = static_cast<unsigned long long>(e - s);
+        } else {
+            sb_segment(x, s, e, out);
+        }
+    }
+}
+
+static vkc_status scan_by_add_f64(vkc_ctx *ctx, const vkc_value *args, int, vkc_value *out) {
+    vkc_status st;
+    if (!array_arg(ctx, args[0], VKC_F64, &st) || !array_arg(ctx, args[1], VKC_BOOL, &st)) return st;
+    const vkc_array *xa = args[0].array, *sa = args[1].array;
+    const int64_t n = xa->len;
+    if (sa->len != n)
+        return fail(ctx, VKC_RUNTIME, "length mismatch: " + std::to_string(n) + " vs " + std::to_string(sa->len));
+    vkc_array *o;
+    if ((st = new_array(ctx, VKC_F64, n, false, &o))) return st;
+    if (n == 0) {
+        out->kind = VKC_VALUE_ARRAY;
+        out->array = o;
+        return VKC_OK;
+    }
+    const auto *x = static_cast<const unsigned long long *>(xa->data());
+    const auto *starts = static_cast<const unsigned char *>(sa->data());
+    auto *ov = static_cast<unsigned long long *>(o->data());
+    const int64_t tiles = (n + SB_TILE - 1) / SB_TILE;
+    const int64_t sum_words = scan_counts_sum_words(tiles);
+    const int64_t max_long = n / (SB_SHORT + 1) + 1;
+    // One i64 work array: counts and offsets (u32, tiles each), the scan's sums, the heads, the
+    // long-segment list.
+    const int64_t w_counts = (tiles + 1) / 2, w_sums = (sum_words + 1) / 2;
+    vkc_array *work;
+    if ((st = new_array(ctx, VKC_I64, 2 * w_counts + w_sums + n + 1 + 2 * max_long, false, &work))) {
+        vkc_array_release(o);
+        return st;
+    }
+    auto *w = static_cast<long long *>(work->data());
+    auto *counts = reinterpret_cast<unsigned *>(w);
+    auto *offs = reinterpret_cast<unsigned *>(w + w_counts);
+    auto *sums = reinterpret_cast<unsigned *>(w + 2 * w_counts);
+    long long *heads = w + 2 * w_counts + w_sums;
+    auto *longs = reinterpret_cast<unsigned long long *>(heads + n);
+    auto done = [&](vkc_status s2) {
+        vkc_array_release(work);
+        if (s2) {
+            vkc_array_release(o);
+            return s2;
+        }
+        out->kind = VKC_VALUE_ARRAY;
+        out->array = o;
+        return VKC_OK;
+    };
+    VKC_CUDA(ctx, cudaMemsetAsync(longs, 0, sizeof(unsigned long long), ctx->stream));
+    sb_count_kernel<<<static_cast<unsigned>(tiles), 256, 0, ctx->stream>>>(starts, n, counts);
+    if ((st = launched(ctx, "sb_count"))) return done(st);
+    scan_counts(ctx, counts, tiles, sums, offs);
+    sb_list_kernel<<<static_cast<unsigned>(tiles), 256, 0, ctx->stream>>>(starts, n, offs, heads);
+    if ((st = launched(ctx, "sb_list"))) return done(st);
+    sb_segment_kernel<<<stream_grid(ctx, n, 128, 16, 256), 128, 0, ctx->stream>>>(
+        x, n, heads, offs, counts, static_cast<int>(tiles), ov, longs);
+    if ((st = launched(ctx, "sb_segment"))) return done(st);
+    unsigned long long nlong = 0;
+    VKC_CUDA(ctx, cudaMemcpyAsync(&nlong, longs, sizeof nlong, cudaMemcpyDeviceToHost, ctx->stream));
+    VKC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (nlong > 0) {
+        std::vector<unsigned long long> list(2 * nlong);
+        VKC_CUDA(ctx, cudaMemcpyAsync(list.data(), longs + 1, list.size() * sizeof(unsigned long long),
+                                      cudaMemcpyDeviceToHost, ctx->stream));
+        VKC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        for (unsigned long long k = 0; k < nlong && !st; ++k)
+            st = canon_scan_rows(ctx, x + list[2 * k], static_cast<int64_t>(list[2 * k + 1]), ov + list[2 * k]);
+    }
+    return done(st);
+}
+
 template <int OP, int CMP> static ReducerImpl *make_canon(vkc_ctx *ctx) {
     auto *r = new CanonReducer;
     r->op = OP;
@@ -1190,6 +1559,13 @@ void register_canon(std::vector<KernelDef> &t) {
         d.red = makes[c];
         t.push_back(d);
     }
+    // Float scans (an extension: the tier-2 notes' candidate order), whole entries.
+    d = KernelDef{"scan_add_f64", VKC_WHOLE, {xa}, true, VKC_F64, 16};
+    d.whole = scan_add_f64;
+    t.push_back(d);
+    d = KernelDef{"scan_by_add_f64", VKC_WHOLE, {xa, InSpec{IN_ARRAY, VKC_BOOL}}, true, VKC_F64, 17};
+    d.whole = scan_by_add_f64;
+    t.push_back(d);
 }
 
 }  // namespace vkc
