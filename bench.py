@@ -296,6 +296,39 @@ def run_sort_groupby(ctx, n, stream, steps, warmup):
                         "histogram" % (n.bit_length() - 1), "steps": steps, "warmup": warmup, **out}
 
 
+def run_f64_scans(ctx, n, stream, steps=3, warmup=1):
+    """scan_add_f64 at n rows (uniform [0,1)) and scan_by_add_f64 at n/2 rows with segments of
+    about 128 rows (start flags set with probability 1/128): CUDA-event ms and GB/s of the
+    algorithmic bytes (read 8 + write 8 per row, plus the start flag's byte for scan_by)."""
+    import torch
+
+    x = ctx.call("rand_f64", n, 31)
+    m = n // 2
+    v = ctx.call("rand_f64", m, 32)
+    starts = ctx.call("lt_f64", ctx.call("rand_f64", m, 33), 1.0 / 128)
+    cases = (("scan_add_f64", lambda: ctx.call("scan_add_f64", x), 16 * n, n),
+             ("scan_by_add_f64", lambda: ctx.call("scan_by_add_f64", v, starts), 17 * m, m))
+    out = {}
+    with torch.cuda.stream(stream):
+        for label, fn, nbytes, rows in cases:
+            for _ in range(warmup):
+                fn()
+            ts = []
+            for _ in range(steps):
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                fn()
+                e1.record(stream)
+                stream.synchronize()
+                ts.append(e0.elapsed_time(e1))
+            ms = sorted(ts)[len(ts) // 2]
+            out[label] = {"rows": rows, "ms": round(ms, 4), "GB/s": round(nbytes / (ms / 1e3) / 1e9, 1)}
+    return {"workload": "scan_add_f64 at n=2^%d uniform [0,1); scan_by_add_f64 at n=2^%d, segments of "
+                        "about 128 rows; the candidate float scan order (prefix canonical sums)"
+                        % (n.bit_length() - 1, m.bit_length() - 1), **out}
+
+
 # ---------------------------------------------------------------------------- batched statements
 
 
@@ -617,6 +650,7 @@ def main():
                     help="host processes of the reference arm (0: every core this process may use)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--sort-n", type=int, default=1 << 27, help="0 skips the argsort/group-by section")
+    ap.add_argument("--scan-n", type=int, default=1 << 28, help="0 skips the float scan section")
     ap.add_argument("--batch-arrays", type=int, default=4096, help="0 skips the batched section")
     ap.add_argument("--serve-requests", type=int, default=300, help="0 skips the served section")
     args = ap.parse_args()
@@ -723,6 +757,7 @@ def main():
     del inputs, hin, res
     if args.sort_n > 0:
         c3 = run_sort_groupby(ctx, args.sort_n, stream, steps=3, warmup=1)
+    c6 = run_f64_scans(ctx, args.scan_n, stream) if args.scan_n > 0 else None
     c4 = run_batched(ctx, args.batch_arrays) if args.batch_arrays > 0 else None
     c5 = run_served(ctx, count=args.serve_requests) if args.serve_requests > 0 else None
 
@@ -744,6 +779,7 @@ def main():
             "gpu_launches": launches,
             "kernels": kernels,
             "sort_groupby": c3,
+            "f64_scans": c6,
             "batched": c4,
             "served": c5,
         }

@@ -13,7 +13,16 @@ import pytest
 import oracle
 from helpers import GPU_LENGTHS, LENGTHS, uniform, varied, with_specials
 
-DATA = {"uniform": uniform, "varied": varied, "specials": with_specials}
+
+def ties(n, seed=0):
+    """Rows that round exactly halfway: after a first block of 2^53 every lane holds a state in
+    [2^53, 2^54) (ulp 2), and the odd integer rows fall halfway between two states."""
+    x = (oracle.rand_i64(n, seed).view(np.uint64) % np.uint64(500)).astype(np.float64) * 2 + 1
+    x[:16] = 2.0 ** 53
+    return x
+
+
+DATA = {"uniform": uniform, "varied": varied, "specials": with_specials, "ties": ties}
 
 
 def bits(v):
@@ -76,7 +85,8 @@ def test_gpu_scan_equals_oracle(ctx, data):
 def test_gpu_scan_large(ctx):
     # Whole chunks (uniform), negative rows (the signed walk), a sum that crosses zero.
     n = (1 << 24) + 7
-    cases = {"uniform": uniform(n, 2), "negative": -uniform(n, 3), "mostly_positive": uniform(n, 4) - 0.3}
+    cases = {"uniform": uniform(n, 2), "negative": -uniform(n, 3), "mostly_positive": uniform(n, 4) - 0.3,
+             "ties": ties(n, 5)}
     for name, x in cases.items():
         dx = ctx.upload(x)
         got = ctx.call("scan_add_f64", dx).numpy()

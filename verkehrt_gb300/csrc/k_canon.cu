@@ -1,5 +1,6 @@
 // The canonical f64 sums: reduce_add_f64, dot_f64, sumsq_f64 and condsum_<cmp>_f64, bit-exact
-// to the reference's canonical order at every length.
+// to the reference's canonical order at every length; and, built on the same pass, the float
+// scans scan_add_f64 and scan_by_add_f64 (prefix canonical sums, at the end of the file).
 //
 // Reference order (src/kernels/scalar/reduce.rs:45-91, :253-323; the spec in
 // docs/superpowers/specs/2026-10-30-verkehrt-design.md:155-160): lane j (0..15) starts at +0.0
@@ -1252,11 +1253,46 @@ struct CanonReducer : DevReducer {
 // banks.
 constexpr int SCAN_PAD = 17;
 struct ScanSmem {
-    double v[CT_BLOCKS * SCAN_PAD];         // the tile's rows, then its outputs
-    double st[(CT_BLOCKS + 1) * SCAN_PAD];  // lane states before block j, j = 0 .. 256
-    double c[CT_BLOCKS + 1];                // their combines
+    unsigned long long v[CT_BLOCKS * SCAN_PAD];  // the tile's rows (bits), then its outputs
+    union {
+        unsigned long long st[(CT_BLOCKS + 1) * SCAN_PAD];  // lane states before block j, j = 0 .. 256
+        struct {
+            TF tf[16][CT_SEGS];  // each lane's segment transfer functions
+            int ok[16][CT_SEGS];
+        } seg;
+    };
+    double c[CT_BLOCKS + 1];  // the combines of st[j]
+    int serial[16];           // lanes whose segments do not all carry a transfer function
 };
 
+// fl(s + x) on bits. When s is a positive normal in binade E >= -959, x is non-negative and below
+// that binade and the sum stays in it, s = S u with u = 2^(E-52) and fl(s + x) = (S + RNE(x/u)) u
+// with ties to the even S (the integer steps of seg_tf for one row); otherwise the FP64 add.
+__device__ __forceinline__ unsigned long long add_bits(unsigned long long s, unsigned long long x) {
+    const unsigned KE = static_cast<unsigned>(s >> 52);  // with the sign bit: a negative s is above 2047
+    const unsigned ex = static_cast<unsigned>(x >> 52);  // likewise a negative x
+    if (KE >= 64u && KE <= 2046u && ex < KE) {
+        const unsigned k = min(KE - ex, 63u);  // zero and subnormal rows: k = 63, no increment
+        const unsigned long long w = ((x & MANT) | ONE52) + (1ull << (k - 1));
+        unsigned long long inc = w >> k;
+        const unsigned long long S = (s & MANT) | ONE52;
+        if ((w << (64 - k)) == 0) {  // exactly halfway: to the even neighbour
+            inc -= 1;
+            inc += (S + inc) & 1;
+        }
+        const unsigned long long S2 = S + inc;
+        if (S2 < (ONE52 << 1)) return (static_cast<unsigned long long>(KE) << 52) | (S2 & MANT);
+    }
+    return as_bits(__dadd_rn(as_f64(s), as_f64(x)));
+}
+
+// One block per tile. (1) Each (segment, lane pair) thread computes its segments' transfer
+// functions at the binade of the lane's state before the tile (K3's layout: 8 lane pairs x 32
+// segments of 8 blocks). (2) Per lane, a warp composes them in segment order from that state;
+// where all 32 apply, the states before each segment follow. (3) Each thread then adds its
+// segments' rows one at a time (add_bits) for the state after every block; a lane whose segments
+// do not all apply (a binade crossing, a negative row or state, the first tile) runs its whole
+// chain in one thread instead. (4) The combines of the states, (5) the tails, in add_bits.
 __global__ void __launch_bounds__(256) canon_scan_kernel(const unsigned long long *__restrict__ x, int64_t n, int64_t nb,
                                                          int T, const unsigned long long *__restrict__ tstate,
                                                          unsigned long long *__restrict__ out) {
@@ -1266,24 +1302,87 @@ __global__ void __launch_bounds__(256) canon_scan_kernel(const unsigned long lon
     const int64_t row0 = static_cast<int64_t>(t) * (CT_BLOCKS * 16);
     const int64_t left = n - row0;
     const int rows = left < CT_BLOCKS * 16 ? static_cast<int>(left) : CT_BLOCKS * 16;
-    for (int i = tid; i < rows; i += 256) sm.v[(i >> 4) * SCAN_PAD + (i & 15)] = as_f64(x[row0 + i]);
+    for (int i = tid; i < rows; i += 256) sm.v[(i >> 4) * SCAN_PAD + (i & 15)] = x[row0 + i];
     // The tile's whole blocks (all but a partial last one) feed the lanes.
     const int64_t whole = nb - static_cast<int64_t>(t) * CT_BLOCKS;
     const int fb = whole <= 0 ? 0 : (whole < CT_BLOCKS ? static_cast<int>(whole) : CT_BLOCKS);
     __syncthreads();
-    if (tid < 16) {
-        double s = tstate ? as_f64(tstate[static_cast<int64_t>(tid) * (T + 1) + t]) : 0.0;
-        sm.st[tid] = s;
-        for (int j = 0; j < fb; ++j) {
-            s = __dadd_rn(s, sm.v[j * SCAN_PAD + tid]);
-            sm.st[(j + 1) * SCAN_PAD + tid] = s;
+    // (1)
+    const int lp = tid & 7, seg = tid >> 3;
+    unsigned long long r[CT_SEG_BLOCKS][2];
+#pragma unroll
+    for (int i = 0; i < CT_SEG_BLOCKS; ++i) {
+        const int blk = seg * CT_SEG_BLOCKS + i;
+        r[i][0] = blk < fb ? sm.v[blk * SCAN_PAD + 2 * lp] : 0ull;
+        r[i][1] = blk < fb ? sm.v[blk * SCAN_PAD + 2 * lp + 1] : 0ull;
+    }
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const int L = 2 * lp + h;
+        const int E = tstate ? state_binade(tstate[static_cast<int64_t>(L) * (T + 1) + t]) : NO_E;
+        TF f{0, 0};
+        const bool ok = E != NO_E && E >= -959 && seg_tf<false>(r, h, 1023 + E, &f);
+        sm.seg.tf[L][seg] = f;
+        sm.seg.ok[L][seg] = ok;
+    }
+    __syncthreads();
+    // (2) warp w: lanes 2w and 2w + 1, thread `sl` of the warp = segment sl.
+    const int w = tid >> 5, sl = tid & 31;
+    unsigned long long before[2];
+    bool carried[2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const int L = 2 * w + h;
+        const unsigned long long s0 = tstate ? tstate[static_cast<int64_t>(L) * (T + 1) + t] : 0ull;
+        const int E = state_binade(s0);
+        unsigned long long after = s0, mine = 0;
+        const int m = E == NO_E ? 0 : apply_prefix<false>(sm.seg.tf[L][sl], sm.seg.ok[L][sl] != 0, s0, E, &after, &mine);
+        carried[h] = m == CT_SEGS;
+        const unsigned long long prev = __shfl_up_sync(FULL, mine, 1);
+        before[h] = sl == 0 ? s0 : prev;
+    }
+    __syncthreads();  // the segment functions are read; their space holds the states from here
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const int L = 2 * w + h;
+        if (carried[h]) sm.st[(sl * CT_SEG_BLOCKS) * SCAN_PAD + L] = before[h];
+        if (sl == 0) sm.serial[L] = !carried[h];
+    }
+    __syncthreads();
+    // (3)
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const int L = 2 * lp + h;
+        if (sm.serial[L]) continue;
+        unsigned long long st = sm.st[(seg * CT_SEG_BLOCKS) * SCAN_PAD + L];
+#pragma unroll
+        for (int i = 0; i < CT_SEG_BLOCKS; ++i) {
+            st = add_bits(st, r[i][h]);
+            // the state after the segment's last block is the next segment's, stored in (2)
+            if (i < CT_SEG_BLOCKS - 1 || seg == CT_SEGS - 1) sm.st[(seg * CT_SEG_BLOCKS + i + 1) * SCAN_PAD + L] = st;
+        }
+    }
+    if (tid < 16 && sm.serial[tid]) {
+        unsigned long long st = tstate ? tstate[static_cast<int64_t>(tid) * (T + 1) + t] : 0ull;
+        sm.st[tid] = st;
+        if (st >> 63) {  // a negative state: the integer steps do not apply
+            for (int j = 0; j < fb; ++j) {
+                st = as_bits(__dadd_rn(as_f64(st), as_f64(sm.v[j * SCAN_PAD + tid])));
+                sm.st[(j + 1) * SCAN_PAD + tid] = st;
+            }
+        } else {
+            for (int j = 0; j < fb; ++j) {
+                st = add_bits(st, sm.v[j * SCAN_PAD + tid]);
+                sm.st[(j + 1) * SCAN_PAD + tid] = st;
+            }
         }
     }
     __syncthreads();
+    // (4)
     for (int j = tid; j <= fb; j += 256) {
         double a[16];
 #pragma unroll
-        for (int q = 0; q < 16; ++q) a[q] = sm.st[j * SCAN_PAD + q];
+        for (int q = 0; q < 16; ++q) a[q] = as_f64(sm.st[j * SCAN_PAD + q]);
 #pragma unroll
         for (int step = 8; step > 0; step >>= 1)
 #pragma unroll
@@ -1291,22 +1390,23 @@ __global__ void __launch_bounds__(256) canon_scan_kernel(const unsigned long lon
         sm.c[j] = a[0];
     }
     __syncthreads();
+    // (5)
     const int nbt = (rows + 15) >> 4;  // blocks in the tile, a partial last one included
     for (int j = tid; j < nbt; j += 256) {
-        double c = sm.c[j];
+        unsigned long long c = as_bits(sm.c[j]);
         const int cnt = min(16, rows - 16 * j);
-        double *v = sm.v + j * SCAN_PAD;
+        unsigned long long *v = sm.v + j * SCAN_PAD;
 #pragma unroll
-        for (int r = 0; r < 15; ++r) {
-            if (r < cnt) {
-                c = __dadd_rn(c, v[r]);
-                v[r] = c;
+        for (int q = 0; q < 15; ++q) {
+            if (q < cnt) {
+                c = add_bits(c, v[q]);
+                v[q] = c;
             }
         }
-        if (cnt == 16) v[15] = sm.c[j + 1];  // a whole block: j < fb
+        if (cnt == 16) v[15] = as_bits(sm.c[j + 1]);  // a whole block: j < fb
     }
     __syncthreads();
-    for (int i = tid; i < rows; i += 256) out[row0 + i] = as_bits(sm.v[(i >> 4) * SCAN_PAD + (i & 15)]);
+    for (int i = tid; i < rows; i += 256) out[row0 + i] = sm.v[(i >> 4) * SCAN_PAD + (i & 15)];
 }
 
 // The prefix canonical sums of rows x[0 .. n) into out[0 .. n).
@@ -1407,21 +1507,46 @@ __device__ void sb_segment(const unsigned long long *__restrict__ x, int64_t s, 
 #pragma unroll
     for (int j = 0; j < 16; ++j) lane[j] = 0.0;
     double base = 0.0;  // the combine of the lanes before the block (+0.0 while all are +0.0)
+    // The first block's adds start from +0.0, where the integer steps never apply: FP64 adds.
     for (int64_t b0 = s; b0 < e; b0 += 16) {
         const int64_t cnt = e - b0;
-        if (cnt >= 16) {
+        if (b0 == s) {
+            double t = 0.0;
+#pragma unroll
+            for (int r = 0; r < 16; ++r) {
+                if (r < cnt) {
+                    const double v = as_f64(x[b0 + r]);
+                    if (r < 15) {
+                        t = __dadd_rn(t, v);
+                        out[b0 + r] = as_bits(t);
+                    }
+                    lane[r] = __dadd_rn(0.0, v);  // used only when the block is whole
+                }
+            }
+            if (cnt >= 16) {
+                double a[16];
+#pragma unroll
+                for (int j = 0; j < 16; ++j) a[j] = lane[j];
+#pragma unroll
+                for (int step = 8; step > 0; step >>= 1)
+#pragma unroll
+                    for (int q = 0; q < step; ++q) a[q] = __dadd_rn(a[q], a[q + step]);
+                base = a[0];
+                out[b0 + 15] = as_bits(base);
+            }
+        } else if (cnt >= 16) {
             double v[16];
 #pragma unroll
             for (int j = 0; j < 16; ++j) v[j] = as_f64(x[b0 + j]);
-            double t = base;
+            unsigned long long t = as_bits(base);
 #pragma unroll
             for (int r = 0; r < 15; ++r) {
-                t = __dadd_rn(t, v[r]);
-                out[b0 + r] = as_bits(t);
+                t = add_bits(t, as_bits(v[r]));
+                out[b0 + r] = t;
             }
             double a[16];
 #pragma unroll
-            for (int j = 0; j < 16; ++j) a[j] = lane[j] = __dadd_rn(lane[j], v[j]);
+            for (int j = 0; j < 16; ++j) a[j] = lane[j] = as_f64(add_bits(as_bits(lane[j]), as_bits(v[j])));
 #pragma unroll
             for (int step = 8; step > 0; step >>= 1)
 #pragma unroll
@@ -1429,10 +1554,10 @@ __device__ void sb_segment(const unsigned long long *__restrict__ x, int64_t s, 
             base = a[0];
             out[b0 + 15] = as_bits(base);
         } else {
-            double t = base;
+            unsigned long long t = as_bits(base);
             for (int64_t i = b0; i < e; ++i) {
-                t = __dadd_rn(t, as_f64(x[i]));
-                out[i] = as_bits(t);
+                t = add_bits(t, x[i]);
+                out[i] = t;
             }
         }
     }
