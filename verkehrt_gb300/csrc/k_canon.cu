@@ -1629,7 +1629,10 @@ static vkc_status scan_by_add_f64(vkc_ctx *ctx, const vkc_value *args, int, vkc_
         out->array = o;
         return VKC_OK;
     };
-    VKC_CUDA(ctx, cudaMemsetAsync(longs, 0, sizeof(unsigned long long), ctx->stream));
+    // CUDA errors release the arrays as well (done).
+    auto cuda = [&](cudaError_t e, const char *what) { return e == cudaSuccess ? VKC_OK : cuda_fail(ctx, e, what); };
+    if ((st = cuda(cudaMemsetAsync(longs, 0, sizeof(unsigned long long), ctx->stream), "cudaMemsetAsync")))
+        return done(st);
     sb_count_kernel<<<static_cast<unsigned>(tiles), 256, 0, ctx->stream>>>(starts, n, counts);
     if ((st = launched(ctx, "sb_count"))) return done(st);
     scan_counts(ctx, counts, tiles, sums, offs);
@@ -1639,13 +1642,15 @@ static vkc_status scan_by_add_f64(vkc_ctx *ctx, const vkc_value *args, int, vkc_
         x, n, heads, offs, counts, static_cast<int>(tiles), ov, longs);
     if ((st = launched(ctx, "sb_segment"))) return done(st);
     unsigned long long nlong = 0;
-    VKC_CUDA(ctx, cudaMemcpyAsync(&nlong, longs, sizeof nlong, cudaMemcpyDeviceToHost, ctx->stream));
-    VKC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if ((st = cuda(cudaMemcpyAsync(&nlong, longs, sizeof nlong, cudaMemcpyDeviceToHost, ctx->stream), "cudaMemcpyAsync")) ||
+        (st = cuda(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize")))
+        return done(st);
     if (nlong > 0) {
         std::vector<unsigned long long> list(2 * nlong);
-        VKC_CUDA(ctx, cudaMemcpyAsync(list.data(), longs + 1, list.size() * sizeof(unsigned long long),
-                                      cudaMemcpyDeviceToHost, ctx->stream));
-        VKC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        if ((st = cuda(cudaMemcpyAsync(list.data(), longs + 1, list.size() * sizeof(unsigned long long),
+                                       cudaMemcpyDeviceToHost, ctx->stream), "cudaMemcpyAsync")) ||
+            (st = cuda(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize")))
+            return done(st);
         for (unsigned long long k = 0; k < nlong && !st; ++k)
             st = canon_scan_rows(ctx, x + list[2 * k], static_cast<int64_t>(list[2 * k + 1]), ov + list[2 * k]);
     }
