@@ -6,6 +6,11 @@
  * of the parity tests and the "port" CPU baseline of bench.py. The CUDA library never
  * links, loads or calls it. Built with -O3 -ffp-contract=off so that no multiply-add is
  * contracted (the reference uses no FMA, docs/superpowers/specs/2026-10-30-verkehrt-design.md:162).
+ *
+ * Parity unpinned for the float extensions orc_reduce_into_add_f64, orc_scan_add_f64 and
+ * orc_scan_by_add_f64: the reference has no such kernels and no golden vectors for them; they
+ * restate the candidate orders of its tier-2 design notes and are checked against the
+ * properties those notes state.
  */
 #include "oracle.h"
 
