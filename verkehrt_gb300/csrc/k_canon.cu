@@ -1592,6 +1592,9 @@ static vkc_status scan_by_add_f64(vkc_ctx *ctx, const vkc_value *args, int, vkc_
     const int64_t n = xa->len;
     if (sa->len != n)
         return fail(ctx, VKC_RUNTIME, "length mismatch: " + std::to_string(n) + " vs " + std::to_string(sa->len));
+    // Segment heads are counted and offset in u32 (the argsort's count scan).
+    if (n >= (int64_t(1) << 32))
+        return fail(ctx, VKC_USAGE, "scan_by of " + std::to_string(n) + " rows: at most 2^32 - 1 rows per call");
     vkc_array *o;
     if ((st = new_array(ctx, VKC_F64, n, false, &o))) return st;
     if (n == 0) {
