@@ -217,7 +217,7 @@ __device__ __forceinline__ void mbar_wait(unsigned long long *bar, unsigned pari
     }
 }
 
-// ------------------------------------------------------------------ the driver
+// ------------------------------------------------------------------ the pass kernel body
 
 // Run by a block of Pass::THREADS compute threads plus two warps (producer, then lookback),
 // with Pass::SLOTS * Pass::SLOT_BYTES of dynamic shared memory (16-byte aligned slots). Tile k
