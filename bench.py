@@ -671,6 +671,13 @@ def main():
         sample = ("oracle port of the scalar entries, sweep at n=2^%d, %d processes side by side (one per "
                   "host core, each its own copy of the sample), %d passes in all" % (
                       args.cpu_sample.bit_length() - 1, procs, passes))
+        # What this arm ran: the same kernels and data distributions, at the sample size, as
+        # independent replicas on every host core.
+        config = dict(config, n=args.cpu_sample, processes=procs,
+                      workload="primitive sweep (the GPU arm's kernels and distributions) at n=2^%d rows "
+                               "per array, %d independent host processes" % (
+                                   args.cpu_sample.bit_length() - 1, procs),
+                      gpu_arm_n=n)
         line = {"impl": "reference", "metric": METRIC, "value": round(gbs, 3), "unit": UNIT,
                 "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64+i64",

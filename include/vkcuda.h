@@ -218,9 +218,13 @@ VKC_API vkc_status vkc_elementwise_tile(vkc_ctx *ctx, int id, const vkc_value *a
  * serving loop that must not take the allocator's lock or latency per request. It has no
  * counterpart in the reference, whose kernels run on the host. It needs no vkc_ctx and calls
  * no allocator: its lookback scratch is a 4 MiB array in the library's device image, so n
- * may be at most 2^28 rows (larger n is rejected with VKC_USAGE and a message). The first call
- * on a device looks up the array's device address (once per device); make that first call
- * before any stream capture. Every call shares the array: calls that overlap on the GPU race,
+ * may be at most 2^28 rows (larger n is rejected with VKC_USAGE and a message), and `in` and
+ * `out` must be device (or managed) memory of `device` (NULL or host pointers are rejected with
+ * VKC_USAGE). The first call on a device looks up the array's device address (once per device)
+ * and keeps it for the life of the process; make that first call before any stream capture.
+ * A device reset (cudaDeviceReset) reloads the library's device image and leaves that address
+ * stale, so this entry must not be called after a reset of its device. Every call shares the
+ * array: calls that overlap on the GPU race,
  * so run them on one stream or one after another. Work runs on `stream` (a cudaStream_t, NULL
  * for the legacy default stream) and the call returns when the scan is complete. On failure a
  * message is written to `err` (`err_len` bytes, may be NULL). */

@@ -60,3 +60,10 @@ def test_noalloc_scan_rejects_sizes_beyond_its_maximum(ctx):
     assert "maximum of 268435456 rows" in msg
     st, msg = noalloc(lib, ctx, None, None, 0)
     assert st == 0
+    # NULL and host pointers are refused before any launch.
+    st, msg = noalloc(lib, ctx, None, None, 16)
+    assert st == 5 and "NULL" in msg
+    host = np.zeros(16, dtype=np.int64)
+    err = ctypes.create_string_buffer(256)
+    st = lib.vkc_scan_add_i64_noalloc(0, host.ctypes.data, host.ctypes.data, 16, ctx.stream, err, len(err))
+    assert st == 5 and b"device or managed memory" in err.value

@@ -1,12 +1,16 @@
 """Builds the CUDA library libvkcuda.so in-tree, for sm_103a only.
 
 Each translation unit under csrc/ compiles in parallel with nvcc into _build/, then links into
-verkehrt_gb300/libvkcuda.so. Files are rebuilt only when a source or header is newer than the
-library. `-fmad=false` keeps every f64 multiply and add a separate IEEE operation, which the
-canonical sums and the fused-equals-unfused identity rely on.
+verkehrt_gb300/libvkcuda.so. A stamp file beside the library holds a hash of every source and
+header, of this script and of the compiler flags; the library is rebuilt whenever the stamp is
+missing or differs, so a library built from other sources (or copied from another machine) is
+never reused. `-fmad=false` keeps every f64 multiply and add a separate IEEE operation, which
+the canonical sums and the fused-equals-unfused identity rely on.
 """
 
+import hashlib
 import os
+import platform
 import subprocess
 import sys
 from concurrent.futures import ThreadPoolExecutor
@@ -16,6 +20,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libvkcuda.so")
+STAMP = LIB + ".stamp"
 
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -27,12 +32,27 @@ def _sources():
     return sorted(f for f in os.listdir(CSRC) if f.endswith(".cu"))
 
 
-def _newest_input():
-    newest = 0.0
+def source_hash():
+    """SHA-256 over the sources, headers, this script, the flags and the host machine type."""
+    h = hashlib.sha256()
+    h.update(" ".join([NVCC] + ARCH + FLAGS + [platform.machine()]).encode())
     for d in (CSRC, os.path.join(ROOT, "include")):
-        for f in os.listdir(d):
-            newest = max(newest, os.path.getmtime(os.path.join(d, f)))
-    return max(newest, os.path.getmtime(__file__))
+        for f in sorted(os.listdir(d)):
+            p = os.path.join(d, f)
+            if os.path.isfile(p):
+                h.update(f.encode())
+                with open(p, "rb") as fh:
+                    h.update(fh.read())
+    with open(__file__, "rb") as fh:
+        h.update(fh.read())
+    return h.hexdigest()
+
+
+def up_to_date():
+    if not (os.path.exists(LIB) and os.path.exists(STAMP)):
+        return False
+    with open(STAMP) as f:
+        return f.read().strip() == source_hash()
 
 
 def _run(cmd):
@@ -43,8 +63,9 @@ def _run(cmd):
 
 
 def build(force=False, verbose=False):
-    """Compiles and links libvkcuda.so unless it is up to date. Returns its path."""
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= _newest_input():
+    """Compiles and links libvkcuda.so unless its stamp matches the sources. Returns its path."""
+    digest = source_hash()
+    if not force and up_to_date():
         return LIB
     os.makedirs(BUILD, exist_ok=True)
     srcs = _sources()
@@ -63,6 +84,9 @@ def build(force=False, verbose=False):
     tmp = LIB + ".tmp"
     _run([NVCC] + ARCH + ["-shared", "-o", tmp] + objs)
     os.replace(tmp, LIB)
+    with open(STAMP + ".tmp", "w") as f:
+        f.write(digest + "\n")
+    os.replace(STAMP + ".tmp", STAMP)
     return LIB
 
 

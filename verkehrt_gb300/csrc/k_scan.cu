@@ -496,6 +496,24 @@ extern "C" vkc_status vkc_scan_add_i64_noalloc(int device, const int64_t *in, in
         return VKC_USAGE;
     }
     if (n == 0) return VKC_OK;
+    if (!in || !out) {
+        noalloc_msg(err, err_len, "vkc_scan_add_i64_noalloc: `in` and `out` must be device pointers, got NULL");
+        return VKC_USAGE;
+    }
+    // Pointers the GPU cannot address as device memory of `device` (host memory, another
+    // device's buffers) would fault the kernel: reject them before anything is launched.
+    for (const void *p : {static_cast<const void *>(in), static_cast<const void *>(out)}) {
+        cudaPointerAttributes at{};
+        cudaError_t pe = cudaPointerGetAttributes(&at, p);
+        if (pe != cudaSuccess) cudaGetLastError();
+        bool ok = pe == cudaSuccess && (at.type == cudaMemoryTypeManaged ||
+                                        (at.type == cudaMemoryTypeDevice && at.device == device));
+        if (!ok) {
+            noalloc_msg(err, err_len, "vkc_scan_add_i64_noalloc: `in` and `out` must be device or managed "
+                                      "memory of device " + std::to_string(device));
+            return VKC_USAGE;
+        }
+    }
     int prev = 0;
     if (cudaGetDevice(&prev) != cudaSuccess || cudaSetDevice(device) != cudaSuccess) {
         cudaGetLastError();
