@@ -194,6 +194,45 @@ def check_results(results):
         raise SystemExit("fused dot %r != unfused %r" % (a, b))
 
 
+# ---------------------------------------------------------------------------- parity digests
+
+
+DIGESTS = os.path.join(ROOT, "tests", "golden", "full_size_digests.json")
+
+
+def digest(value):
+    """SHA-256 (first 32 hex digits) of a result's little-endian bytes: an array's rows (bool as
+    0/1 bytes), an f64 scalar's IEEE bits, an integer scalar as an i64."""
+    import hashlib
+
+    if hasattr(value, "handle"):
+        value = value.numpy()
+    if isinstance(value, np.ndarray):
+        a = value.view(np.uint8) if value.dtype == np.bool_ else value
+        data = np.ascontiguousarray(a).tobytes()
+    elif isinstance(value, float):
+        data = np.float64(value).tobytes()
+    else:
+        data = np.int64(value).tobytes()
+    return hashlib.sha256(data).hexdigest()[:32]
+
+
+def committed_digests():
+    """The oracle's digests of the full-size workloads' outputs (tests/golden/make_full_digests.py)."""
+    if os.path.exists(DIGESTS):
+        with open(DIGESTS) as f:
+            return json.load(f)
+    return {}
+
+
+def check_digests(results, want, n, want_n):
+    """Compares every result that has a committed digest with it (outside the timed region)."""
+    if not want or want_n != n:
+        return {"parity_checked": None, "why": "no committed oracle digests at n=%d" % n}
+    bad = [label for label, d in want.items() if label not in results or digest(results[label]) != d]
+    return {"parity_checked": not bad, "outputs_checked": len(want), "mismatches": bad}
+
+
 # ---------------------------------------------------------------------------- argsort and group-by
 
 
@@ -222,50 +261,67 @@ def zipf_keys(n, s=1.1, distinct=1 << 20, seed=11):
     return out
 
 
-def sortgroup_plan(n, nb):
-    """(label, algorithmic bytes) of the sorted and hashed group-by pipelines."""
-    return [("argsort_i64", 16 * n), ("gather_i64(keys)", 24 * n), ("gather_f64(vals)", 24 * n),
-            ("gather_i64(vals)", 24 * n), ("prev_i64", 16 * n), ("ne_i64", 17 * n),
-            ("scan_by_add_i64", 17 * n), ("group_id_i64", 16 * n), ("reduce_max_i64", 8 * n),
-            ("reduce_into_add_i64", 16 * n + 8 * nb), ("histogram", 8 * n + 8 * nb)]
-
-
 def sortgroup_step(ctx, keys, vf, vi, stream):
-    """Stable argsort, values gathered by the permutation, scan_by add over the sorted runs, and
-    group-by sum/count through group_id. Returns ({label: ms}, results)."""
+    """One group-by pass at n rows, as a program of per-statement calls. The sorted idiom of the
+    reference's tests/programs/grouping.dd:12-31: stable argsort, the keys and values gathered by
+    the permutation, run starts s = (k != prev(k, 0)) | (row == 0) and ends e = (k != next(k)) |
+    (row == n - 1), scan_by add over the runs, per-group sums compress(scan_by, e) and keys
+    compress(k, s), and the same sums as reduce_into(scan(cast_i64(s)) - 1, v, count(s), add).
+    Then the hashed group-by: group_id, reduce_into add and histogram over the ids. Returns
+    ([(label, ms, algorithmic bytes)], {label: result})."""
     import torch
 
+    n = len(keys)
     marks, res = [], {}
 
-    def timed(label, fn):
+    def timed(label, fn, nbytes):
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         out = fn()
         e1.record(stream)
-        marks.append((label, e0, e1))
+        k = len(out) if hasattr(out, "handle") else 0
+        marks.append((label, e0, e1, nbytes(k) if callable(nbytes) else nbytes))
         res[label] = out
         return out
 
+    c = ctx.call
     with torch.cuda.stream(stream):
-        perm = timed("argsort_i64", lambda: ctx.call("argsort_i64", keys))
-        sk = timed("gather_i64(keys)", lambda: ctx.call("gather_i64", keys, perm))
-        timed("gather_f64(vals)", lambda: ctx.call("gather_f64", vf, perm))
-        sv = timed("gather_i64(vals)", lambda: ctx.call("gather_i64", vi, perm))
-        pk = timed("prev_i64", lambda: ctx.call("prev_i64", sk, 0))
-        starts = timed("ne_i64", lambda: ctx.call("ne_i64", sk, pk))
-        timed("scan_by_add_i64", lambda: ctx.call("scan_by_add_i64", sv, starts))
-        g = timed("group_id_i64", lambda: ctx.call("group_id_i64", keys))
-        nb = timed("reduce_max_i64", lambda: ctx.call("reduce_max_i64", g)) + 1
-        timed("reduce_into_add_i64", lambda: ctx.call("reduce_into_add_i64", g, vi, nb))
-        timed("histogram", lambda: ctx.call("histogram", g, nb))
+        perm = timed("argsort_i64", lambda: c("argsort_i64", keys), 16 * n)
+        sk = timed("gather_i64(keys)", lambda: c("gather_i64", keys, perm), 24 * n)
+        timed("gather_f64(vals)", lambda: c("gather_f64", vf, perm), 24 * n)
+        sv = timed("gather_i64(vals)", lambda: c("gather_i64", vi, perm), 24 * n)
+        io = timed("iota", lambda: c("iota", n), 8 * n)
+        pk = timed("prev_i64", lambda: c("prev_i64", sk, 0), 16 * n)
+        ne = timed("ne_i64(starts)", lambda: c("ne_i64", sk, pk), 17 * n)
+        first = timed("eq_i64(first)", lambda: c("eq_i64", io, 0), 9 * n)
+        s = timed("run_starts", lambda: c("or_bool", ne, first), 3 * n)
+        nxt = timed("add_i64(next)", lambda: c("add_i64", io, 1), 16 * n)
+        nxt = timed("min_i64(next)", lambda: c("min_i64", nxt, n - 1), 16 * n)
+        nk = timed("gather_i64(next)", lambda: c("gather_i64", sk, nxt), 24 * n)
+        ne = timed("ne_i64(ends)", lambda: c("ne_i64", sk, nk), 17 * n)
+        last = timed("eq_i64(last)", lambda: c("eq_i64", io, n - 1), 9 * n)
+        e = timed("run_ends", lambda: c("or_bool", ne, last), 3 * n)
+        sb = timed("scan_by_add_i64", lambda: c("scan_by_add_i64", sv, s), 17 * n)
+        timed("compress_i64(sums)", lambda: c("compress_i64", sb, e), lambda k: 9 * n + 8 * k)
+        timed("compress_i64(keys)", lambda: c("compress_i64", sk, s), lambda k: 9 * n + 8 * k)
+        runs = timed("count", lambda: c("count", s), n)
+        si = timed("cast_bool_i64", lambda: c("cast_bool_i64", s), 9 * n)
+        si = timed("scan_add_i64(runs)", lambda: c("scan_add_i64", si), 16 * n)
+        seg = timed("run_numbers", lambda: c("sub_i64", si, 1), 16 * n)
+        timed("reduce_into_add_i64(runs)", lambda: c("reduce_into_add_i64", seg, sv, runs), 16 * n + 8 * runs)
+        g = timed("group_id_i64", lambda: c("group_id_i64", keys), 16 * n)
+        nb = timed("reduce_max_i64", lambda: c("reduce_max_i64", g), 8 * n) + 1
+        timed("reduce_into_add_i64", lambda: c("reduce_into_add_i64", g, vi, nb), 16 * n + 8 * nb)
+        timed("histogram", lambda: c("histogram", g, nb), 8 * n + 8 * nb)
     torch.cuda.current_stream().synchronize()
     stream.synchronize()
-    return {label: e0.elapsed_time(e1) for label, e0, e1 in marks}, res
+    return [(label, e0.elapsed_time(e1), b) for label, e0, e1, b in marks], res
 
 
-def run_sort_groupby(ctx, n, stream, steps, warmup):
-    """Argsort and group-by at n rows for both key distributions: per-kernel ms, GB/s and rows/s."""
+def run_sort_groupby(ctx, n, stream, steps, warmup, digests=None):
+    """Argsort and group-by at n rows for both key distributions: per-call ms, GB/s and rows/s,
+    and the last step's outputs checked against the committed oracle digests."""
     out = {}
     vf = ctx.call("rand_f64", n, 21)
     vi = ctx.call("sub_i64", ctx.call("and_i64", ctx.call("rand_i64", n, 22), (1 << 21) - 1), 1 << 20)
@@ -278,22 +334,35 @@ def run_sort_groupby(ctx, n, stream, steps, warmup):
             sortgroup_step(ctx, keys, vf, vi, stream)
         acc = {}
         for _ in range(steps):
+            res = None  # free the previous step's outputs first
             per, res = sortgroup_step(ctx, keys, vf, vi, stream)
-            for k, v in per.items():
-                acc[k] = acc.get(k, 0.0) + v
+            for label, ms, nbytes in per:
+                a = acc.setdefault(label, [0.0, 0])
+                a[0] += ms
+                a[1] = nbytes
         nb = res["reduce_max_i64"] + 1
-        groups = {}
-        for label, nbytes in sortgroup_plan(n, nb):
-            ms = acc[label] / steps
-            groups[label] = {"ms": round(ms, 4), "GB/s": round(nbytes / (ms / 1e3) / 1e9, 1),
-                             "Grows/s": round(n / (ms / 1e3) / 1e9, 3)}
-        total = sum(acc.values()) / steps
-        out[dist] = {"groups": int(nb), "pipeline_ms": round(total, 3), "kernels": groups}
-        del keys
+        calls = {}
+        for label, (ms_sum, nbytes) in acc.items():
+            ms = ms_sum / steps
+            calls[label] = {"ms": round(ms, 4), "GB/s": round(nbytes / (ms / 1e3) / 1e9, 1),
+                            "Grows/s": round(n / (ms / 1e3) / 1e9, 3)}
+        total = sum(a[0] for a in acc.values()) / steps
+        sorted_ms = sum(a[0] for k, a in acc.items() if k not in HASHED_GROUPBY) / steps
+        out[dist] = {"groups": int(nb), "pipeline_ms": round(total, 3),
+                     "sorted_idiom_ms": round(sorted_ms, 3), "hashed_ms": round(total - sorted_ms, 3),
+                     "kernels": calls,
+                     "parity": check_digests(res, (digests or {}).get(dist), n, (digests or {}).get("n"))}
+        del keys, res
     return {"workload": "n=2^%d i64 keys (uniform over [0,2^32); Zipf s=1.1 over 2^20 keys, "
                         "key = splitmix64(rank)), f64 and i64 values; stable argsort, gathers by "
-                        "the permutation, scan_by add over sorted runs, group_id + reduce_into + "
-                        "histogram" % (n.bit_length() - 1), "steps": steps, "warmup": warmup, **out}
+                        "the permutation, the sorted group-by idiom (run starts/ends, scan_by add, "
+                        "compress of sums and keys, reduce_into over run numbers), and group_id + "
+                        "reduce_into + histogram" % (n.bit_length() - 1),
+            "steps": steps, "warmup": warmup, **out}
+
+
+# Calls of the hashed group-by in sortgroup_step (the rest is the sorted idiom).
+HASHED_GROUPBY = ("group_id_i64", "reduce_max_i64", "reduce_into_add_i64", "histogram")
 
 
 def run_f64_scans(ctx, n, stream, steps=3, warmup=1):
@@ -726,6 +795,10 @@ def main():
     barrier(world)
     clk = clocks.stop()
     check_results(res)
+    # The last timed step's outputs against the oracle's digests (outside the timed region).
+    digests = committed_digests()
+    sweep_parity = check_digests(res, digests.get("sweep", {}).get("outputs"), n,
+                                 digests.get("sweep", {}).get("n"))
 
     bytes_per_step = sum(v[1] for v in per_label.values()) / args.steps
     total_ms = reduce_max(sum(step_ms), world)
@@ -763,7 +836,8 @@ def main():
     c3 = None
     del inputs, hin, res
     if args.sort_n > 0:
-        c3 = run_sort_groupby(ctx, args.sort_n, stream, steps=3, warmup=1)
+        c3 = run_sort_groupby(ctx, args.sort_n, stream, steps=3, warmup=1,
+                              digests=digests.get("sort_groupby"))
     c6 = run_f64_scans(ctx, args.scan_n, stream) if args.scan_n > 0 else None
     c4 = run_batched(ctx, args.batch_arrays) if args.batch_arrays > 0 else None
     c5 = run_served(ctx, count=args.serve_requests) if args.serve_requests > 0 else None
@@ -784,6 +858,8 @@ def main():
                     "h2d_bytes_per_step": e2e[0][1], "d2h_bytes_per_step": e2e[0][2]},
             "clocks": clk,
             "gpu_launches": launches,
+            "parity_checked": sweep_parity["parity_checked"],
+            "parity": sweep_parity,
             "kernels": kernels,
             "sort_groupby": c3,
             "f64_scans": c6,

@@ -112,7 +112,14 @@ VKC_API vkc_status vkc_set_cache_limit(vkc_ctx *ctx, size_t bytes);
  * (count/min/max/argmin/argmax/integer sums: 2, 4, 8, 16), "gather_rows_per_thread" (1, 2, 4)
  * and "group_first_table_log2" (group_id's first hash table, 18 .. 22). vkc_tune_set
  * overrides one entry for this context (the autotuner measures candidates that way); results
- * never depend on it. */
+ * never depend on it.
+ * Two more names are test hooks of the failure paths, the same for every size class (they have
+ * no counterpart in the reference): "spin_limit" sets how many polls a kernel's wait on another
+ * block may take before it gives up and the call returns VKC_TIMEOUT (0 restores the built-in
+ * limit of 2^22 polls, about a second; waits for a block's own copies keep the built-in limit),
+ * and "fail_alloc_after" k makes the array allocation after the next k ones fail as if the
+ * device were out of memory (VKC_ALLOC with the reference's "cannot allocate ..." text; -1, the
+ * default, injects nothing). */
 VKC_API vkc_status vkc_tune_set(vkc_ctx *ctx, const char *knob, int size_class, int value);
 VKC_API vkc_status vkc_tune_get(const vkc_ctx *ctx, const char *knob, int size_class, int *value);
 /* Runs the context's work on `stream` (a cudaStream_t) instead of its own stream. */

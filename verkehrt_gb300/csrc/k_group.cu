@@ -269,8 +269,9 @@ __global__ void __launch_bounds__(GI_THREADS, 4) gi_number_kernel(const unsigned
         } else {
             const unsigned *p = &t.meta(sl[j])->y;
             unsigned it = 0;
+            const unsigned limit = wait_limit(st);
             while ((g = ld_relaxed32(p)) == 0xffffffffu) {
-                if (++it > SPIN_LIMIT) {
+                if (++it > limit) {
                     set_timeout(st);
                     break;
                 }
@@ -565,8 +566,9 @@ __global__ void __launch_bounds__(GI_THREADS, 4) gr_number_kernel(const unsigned
         } else {
             const unsigned long long *p = reinterpret_cast<const unsigned long long *>(out + mr[j]);
             unsigned it = 0;
+            const unsigned limit = wait_limit(st);
             while ((g = ld_relaxed64(p)) == ~0ull) {
-                if (++it > SPIN_LIMIT) {
+                if (++it > limit) {
                     set_timeout(st);
                     break;
                 }
@@ -722,8 +724,7 @@ static vkc_status run_group(vkc_ctx *ctx, const vkc_array *xa, const vkc_array *
         cleanup();
         vkc_array_release(o);
         // group.rs:128-137 reports a failed table allocation.
-        return fail(ctx, VKC_ALLOC, "cannot allocate a group_id table of " + std::to_string(slots) + " slots for " +
-                                        std::to_string(n) + " rows");
+        return fail(ctx, VKC_ALLOC, "cannot allocate a group_id table of " + std::to_string(slots) + " slots");
     };
     if (new_array(ctx, VKC_I32, n, false, &rows) || new_array(ctx, VKC_I32, 2, true, &flag_arr)) return alloc_fail();
     auto *slot_of = static_cast<unsigned *>(rows->data());

@@ -88,6 +88,13 @@ __device__ __forceinline__ void st_relaxed64(unsigned long long *p, unsigned lon
 // of this library can hang the GPU.
 constexpr unsigned SPIN_LIMIT = 1u << 22;
 
+// The poll budget of a wait on another block: the context's test override when set (a status
+// word's spin_limit), else SPIN_LIMIT. Waits for a block's own copies always use SPIN_LIMIT.
+__device__ __forceinline__ unsigned wait_limit(const DevStatus *st) {
+    const unsigned v = *reinterpret_cast<const volatile unsigned *>(&st->spin_limit);
+    return v ? v : SPIN_LIMIT;
+}
+
 __device__ __forceinline__ void backoff(unsigned it) {
     if (it > 64) __nanosleep(it > 4096 ? 256 : 32);
 }

@@ -202,7 +202,7 @@ vkc_status read_status(vkc_ctx *ctx, DevStatus *out) {
     VKC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     memcpy(out, ctx->status_host, sizeof(DevStatus));
     if (out->first_bad != ~0ull || out->timeout) {
-        DevStatus clean{~0ull, 0, 0};
+        DevStatus clean{~0ull, 0, ctx->spin_limit};
         VKC_CUDA(ctx, cudaMemcpyAsync(ctx->status, &clean, sizeof clean, cudaMemcpyHostToDevice,
                                       ctx->stream));
         VKC_CUDA(ctx, cudaMemsetAsync(ctx->counters, 0, kCounterSlots * sizeof(unsigned),
@@ -228,6 +228,8 @@ vkc_status new_array(vkc_ctx *ctx, vkc_type t, int64_t len, bool zero, vkc_array
         return fail(ctx, VKC_RUNTIME, "array of " + std::to_string(static_cast<uint64_t>(len)) +
                                           " elements is too large");
     size_t bytes = static_cast<size_t>(len) * w;
+    if (ctx->fail_alloc_after >= 0 && ctx->fail_alloc_after-- == 0)  // test hook: an injected failure
+        return fail(ctx, VKC_ALLOC, "cannot allocate an array of " + std::to_string(len) + " elements");
     auto buf = std::make_shared<Buffer>();
     buf->box = ctx->box;
     if (bytes) {
@@ -561,6 +563,22 @@ vkc_status vkc_set_cache_limit(vkc_ctx *ctx, size_t bytes) {
 
 vkc_status vkc_tune_set(vkc_ctx *ctx, const char *knob, int size_class, int value) {
     if (!ctx || !knob || size_class < 0 || size_class >= TUNE_CLASSES) return VKC_USAGE;
+    // Test hooks, the same for every size class.
+    if (std::string(knob) == "spin_limit") {
+        if (value < 0) return fail(ctx, VKC_USAGE, "value " + std::to_string(value) + " not allowed for spin_limit");
+        ctx->spin_limit = static_cast<unsigned>(value);
+        // The status word carries it to the kernels; a context stream is idle between calls.
+        VKC_CUDA(ctx, cudaMemcpyAsync(&ctx->status->spin_limit, &ctx->spin_limit, sizeof(unsigned),
+                                      cudaMemcpyHostToDevice, ctx->stream));
+        VKC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        return VKC_OK;
+    }
+    if (std::string(knob) == "fail_alloc_after") {
+        if (value < -1)
+            return fail(ctx, VKC_USAGE, "value " + std::to_string(value) + " not allowed for fail_alloc_after");
+        ctx->fail_alloc_after = value;
+        return VKC_OK;
+    }
     for (int k = 0; k < TK_COUNT; ++k) {
         if (std::string(knob) != tune_knob_name(k)) continue;
         if (!tune_allowed(k, value))
@@ -573,6 +591,14 @@ vkc_status vkc_tune_set(vkc_ctx *ctx, const char *knob, int size_class, int valu
 
 vkc_status vkc_tune_get(const vkc_ctx *ctx, const char *knob, int size_class, int *value) {
     if (!ctx || !knob || !value || size_class < 0 || size_class >= TUNE_CLASSES) return VKC_USAGE;
+    if (std::string(knob) == "spin_limit") {
+        *value = static_cast<int>(ctx->spin_limit);
+        return VKC_OK;
+    }
+    if (std::string(knob) == "fail_alloc_after") {
+        *value = static_cast<int>(ctx->fail_alloc_after);
+        return VKC_OK;
+    }
     for (int k = 0; k < TK_COUNT; ++k)
         if (std::string(knob) == tune_knob_name(k)) {
             *value = ctx->tuning.v[k][size_class];

@@ -88,6 +88,7 @@ __device__ typename R::V tile_lookback(typename R::W *recs, int tile, typename R
             got[j] = hi - P * lane - j < 0;
         }
         bool bad = false;
+        const unsigned limit = wait_limit(status);
         for (unsigned it = 0;;) {
 #pragma unroll
             for (int j = 0; j < P; ++j)
@@ -99,7 +100,7 @@ __device__ typename R::V tile_lookback(typename R::W *recs, int tile, typename R
                 all = all && got[j];
             }
             if (all) break;
-            if (++it > SPIN_LIMIT) {
+            if (++it > limit) {
                 set_timeout(status);
                 bad = true;
                 break;

@@ -119,7 +119,7 @@ struct Scratch {
 struct DevStatus {
     unsigned long long first_bad;  // min offending row, ~0 when none
     unsigned int timeout;          // a bounded spin gave up
-    unsigned int pad;
+    unsigned int spin_limit;       // polls of a wait on another block (0: SPIN_LIMIT)
 };
 
 }  // namespace vkc
@@ -152,6 +152,11 @@ struct vkc_ctx {
     cudaEvent_t io_ev[2] = {nullptr, nullptr};
     // Launch shapes per size class: the committed autotuner table, or overrides.
     vkc::Tuning tuning = vkc::tune_defaults();
+    // Test hooks (vkc_tune_set "spin_limit" / "fail_alloc_after"): the polls a wait on another
+    // block may take (0: the built-in limit), and the number of array allocations that succeed
+    // before the next one reports failure (-1: none fails).
+    unsigned spin_limit = 0;
+    int64_t fail_alloc_after = -1;
     // Copy streams (made on first use): uploads of at least 1 MiB, and asynchronous downloads,
     // so that copies in both directions overlap each other and the kernels.
     cudaStream_t h2d = nullptr, d2h = nullptr;
