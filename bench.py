@@ -398,6 +398,76 @@ def run_f64_scans(ctx, n, stream, steps=3, warmup=1):
                         % (n.bit_length() - 1, m.bit_length() - 1), **out}
 
 
+# ---------------------------------------------------------------------------- canonical sums on hard inputs
+
+
+def adversarial_inputs(ctx, n):
+    """Inputs whose lane sums keep leaving their binade, generated on the device: mean-centred
+    rows u - 0.5, all-negative rows -u, and signed rows over about 31 binades, (u - 0.5) * k^8
+    with k uniform in 0..15."""
+    u = ctx.call("rand_f64", n, 61)
+    k = ctx.call("cast_i64_f64", ctx.call("and_i64", ctx.call("rand_i64", n, 62), 15))
+    k2 = ctx.call("mul_f64", k, k)
+    k4 = ctx.call("mul_f64", k2, k2)
+    return {"centred": ctx.call("sub_f64", u, 0.5),
+            "negative": ctx.call("neg_f64", u),
+            "wide": ctx.call("mul_f64", ctx.call("sub_f64", u, 0.5), ctx.call("mul_f64", k4, k4))}
+
+
+def run_canon_adversarial(ctx, sizes, stream, steps=3, cpu_n=1 << 24, no_cpu=False):
+    """reduce_add_f64 on the hard inputs at each size (CUDA events, median of `steps`), beside the
+    oracle port of the reference's scalar sum (one thread, as the reference) on the same kind of
+    input at cpu_n rows, scaled to rows/s."""
+    import torch
+
+    out = {}
+    for n in sizes:
+        xs = adversarial_inputs(ctx, n)
+        for name, x in xs.items():
+            ctx.call("reduce_add_f64", x)
+            ts = []
+            with torch.cuda.stream(stream):
+                for _ in range(steps):
+                    e0 = torch.cuda.Event(enable_timing=True)
+                    e1 = torch.cuda.Event(enable_timing=True)
+                    e0.record(stream)
+                    ctx.call("reduce_add_f64", x)
+                    e1.record(stream)
+                    stream.synchronize()
+                    ts.append(e0.elapsed_time(e1))
+            ms = sorted(ts)[len(ts) // 2]
+            out.setdefault(name, {})["n=2^%d" % (n.bit_length() - 1)] = {
+                "ms": round(ms, 3), "GB/s": round(8 * n / (ms / 1e3) / 1e9, 1), "Grows/s": round(n / ms / 1e6, 3)}
+        del xs
+    cpu = None
+    if not no_cpu:
+        cpu = cpu_sum_rates(cpu_n)
+        for name, rate in cpu.items():
+            out[name]["cpu_port_1_thread_Grows/s"] = rate
+    return {"workload": "reduce_add_f64 on mean-centred (u - 0.5), all-negative (-u) and (u - 0.5) * k^8 "
+                        "(k uniform in 0..15, about 31 binades) rows; CPU: the oracle port on one host thread "
+                        "at n=2^%d"
+                        % (cpu_n.bit_length() - 1), **out}
+
+
+def cpu_sum_rates(n):
+    """Rows/s (in G) of the oracle port's canonical sum on the hard inputs, one thread."""
+    import oracle
+
+    u = oracle.rand_f64(n, 61)
+    k = (oracle.rand_i64(n, 62) & 15).astype(np.float64)
+    rates = {}
+    k4 = (k * k) * (k * k)
+    for name, x in (("centred", u - 0.5), ("negative", -u), ("wide", (u - 0.5) * (k4 * k4))):
+        oracle.reduce_add_f64(x)
+        t0 = time.perf_counter()
+        reps = 3
+        for _ in range(reps):
+            oracle.reduce_add_f64(x)
+        rates[name] = round(reps * n / (time.perf_counter() - t0) / 1e9, 3)
+    return rates
+
+
 # ---------------------------------------------------------------------------- batched statements
 
 
@@ -720,6 +790,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--sort-n", type=int, default=1 << 27, help="0 skips the argsort/group-by section")
     ap.add_argument("--scan-n", type=int, default=1 << 28, help="0 skips the float scan section")
+    ap.add_argument("--hard-sizes", default="26,28",
+                    help="log2 sizes of the canonical sums on hard inputs (empty skips the section)")
     ap.add_argument("--batch-arrays", type=int, default=4096, help="0 skips the batched section")
     ap.add_argument("--serve-requests", type=int, default=300, help="0 skips the served section")
     args = ap.parse_args()
@@ -795,10 +867,6 @@ def main():
     barrier(world)
     clk = clocks.stop()
     check_results(res)
-    # The last timed step's outputs against the oracle's digests (outside the timed region).
-    digests = committed_digests()
-    sweep_parity = check_digests(res, digests.get("sweep", {}).get("outputs"), n,
-                                 digests.get("sweep", {}).get("n"))
 
     bytes_per_step = sum(v[1] for v in per_label.values()) / args.steps
     total_ms = reduce_max(sum(step_ms), world)
@@ -832,6 +900,12 @@ def main():
                "sample": "oracle port of the scalar entries (one thread, as the reference), the sweep "
                          "at n=2^%d, %d passes" % (args.cpu_sample.bit_length() - 1, passes)}
 
+    # The last timed step's outputs against the oracle's digests (after every timed leg: the check
+    # downloads and hashes the outputs on the host).
+    digests = committed_digests()
+    sweep_parity = check_digests(res, digests.get("sweep", {}).get("outputs"), n,
+                                 digests.get("sweep", {}).get("n"))
+
     # Argsort and group-by, batched statements and served requests, reported beside the headline sweep.
     c3 = None
     del inputs, hin, res
@@ -839,7 +913,12 @@ def main():
         c3 = run_sort_groupby(ctx, args.sort_n, stream, steps=3, warmup=1,
                               digests=digests.get("sort_groupby"))
     c6 = run_f64_scans(ctx, args.scan_n, stream) if args.scan_n > 0 else None
+    hard = [1 << int(v) for v in args.hard_sizes.split(",") if v.strip()]
+    c7 = run_canon_adversarial(ctx, hard, stream, no_cpu=args.no_cpu or rank != 0) if hard else None
     c4 = run_batched(ctx, args.batch_arrays) if args.batch_arrays > 0 else None
+    # The configuration's other reading: its length range [2^10, 2^24] taken literally, with fewer
+    # arrays (512, about 14 GiB of values and keys) so that the inputs and the sort's scratch fit.
+    c4w = run_batched(ctx, 512, lo=10, hi=24) if args.batch_arrays > 0 else None
     c5 = run_served(ctx, count=args.serve_requests) if args.serve_requests > 0 else None
 
     if rank == 0:
@@ -863,7 +942,9 @@ def main():
             "kernels": kernels,
             "sort_groupby": c3,
             "f64_scans": c6,
+            "canon_adversarial": c7,
             "batched": c4,
+            "batched_wide": c4w,
             "served": c5,
         }
         print(json.dumps(line), flush=True)

@@ -16,6 +16,10 @@
  *  - Calls are synchronous from the caller's view: a returned scalar is final and a returned
  *    array may be read or passed to the next call at once (same context stream).
  *  - A context is used by one host thread at a time.
+ *  - Calls whose kernels wait on one another's blocks (scans, selections, group ids) bound every
+ *    wait. A wait that runs out inside a call that does not itself wait for the device (a scan)
+ *    is reported as VKC_TIMEOUT by the next call that does: vkc_synchronize or
+ *    vkc_array_download.
  */
 #ifndef VKCUDA_H
 #define VKCUDA_H
@@ -113,11 +117,13 @@ VKC_API vkc_status vkc_set_cache_limit(vkc_ctx *ctx, size_t bytes);
  * and "group_first_table_log2" (group_id's first hash table, 18 .. 22). vkc_tune_set
  * overrides one entry for this context (the autotuner measures candidates that way); results
  * never depend on it.
- * Two more names are test hooks of the failure paths, the same for every size class (they have
+ * Three more names are test hooks of the failure paths, the same for every size class (they have
  * no counterpart in the reference): "spin_limit" sets how many polls a kernel's wait on another
  * block may take before it gives up and the call returns VKC_TIMEOUT (0 restores the built-in
  * limit of 2^22 polls, about a second; waits for a block's own copies keep the built-in limit),
- * and "fail_alloc_after" k makes the array allocation after the next k ones fail as if the
+ * "lookback_never_ready" 1 makes every decoupled lookback poll for records that no block writes
+ * (a flag that nothing sets: with a small spin_limit, every wait on an earlier tile runs out; 0
+ * turns it off), and "fail_alloc_after" k makes the array allocation after the next k ones fail as if the
  * device were out of memory (VKC_ALLOC with the reference's "cannot allocate ..." text; -1, the
  * default, injects nothing). */
 VKC_API vkc_status vkc_tune_set(vkc_ctx *ctx, const char *knob, int size_class, int value);

@@ -444,3 +444,117 @@ def ew_div_const(t, a, d):
     if lib().orc_ew_div_const(EW_TYPES[t], _p(x), _p(dv), len(x), _p(out), err) != 0:
         raise OracleError(err.value.decode())
     return out
+
+
+# ---------------------------------------------------------------- the families on every type (families.c)
+
+FAMILY_TYPES = {"f64": 0, "f32": 1, "i64": 2, "u64": 3, "i32": 4, "u8": 5, "bool": 6}
+FOLDS = {"add": 0, "mul": 1, "min": 2, "max": 3, "and": 4, "or": 5, "xor": 6}
+NP_TYPES = {"f64": np.float64, "f32": np.float32, "i64": np.int64, "u64": np.uint64, "i32": np.int32,
+            "u8": np.uint8, "bool": np.uint8}
+WIDTH = {"f64": 8, "f32": 4, "i64": 8, "u64": 8, "i32": 4, "u8": 1, "bool": 1}
+
+
+def _fam_lib():
+    L = lib()
+    if not getattr(L, "_families", False):
+        P, I64, INT, U64 = ctypes.c_void_p, ctypes.c_int64, ctypes.c_int, ctypes.c_uint64
+        C = ctypes.c_char_p
+        L.orc_fold.argtypes = [INT, INT, P, I64, ctypes.POINTER(U64), C]
+        L.orc_argext.argtypes = [INT, INT, P, I64, ctypes.POINTER(I64), C]
+        L.orc_fused_sum.restype = U64
+        L.orc_fused_sum.argtypes = [INT, INT, INT, P, P, I64, U64, U64]
+        L.orc_count_cmp.restype = I64
+        L.orc_count_cmp.argtypes = [INT, INT, P, I64, U64]
+        L.orc_filter_cmp.restype = I64
+        L.orc_filter_cmp.argtypes = [INT, INT, P, I64, U64, P]
+        L.orc_scan.argtypes = [INT, INT, INT, P, P, I64, P]
+        L.orc_reduce_into.argtypes = [INT, INT, P, I64, P, I64, I64, P, C]
+        L._families = True
+    return L
+
+
+def sum_type(t):
+    """The result type of add (reduce.rs:559-586): i32 widens to i64, u8 to u64."""
+    return {"i32": "i64", "u8": "u64"}.get(t, t)
+
+
+def as_type(x, t):
+    return np.ascontiguousarray(np.asarray(x).astype(NP_TYPES[t]))
+
+
+def word(t, v):
+    """A scalar of type t as families.c's 64-bit word."""
+    if t == "f64":
+        return int(np.float64(v).view(np.uint64))
+    if t == "f32":
+        return int(np.float32(v).view(np.uint32))
+    if t in ("i64", "i32"):
+        return int(v) & 0xFFFFFFFFFFFFFFFF
+    return int(v) & 0xFFFFFFFFFFFFFFFF
+
+
+def word_bits(t, w):
+    """The bits of a result word in the type's width (what the device returns in its low bytes)."""
+    return int(w) & ((1 << (8 * WIDTH[t])) - 1)
+
+
+def fold(t, f, x):
+    """reduce_<f>_<t>: the result word (sum type for add), in the result type's width."""
+    x = as_type(x, t)
+    out = ctypes.c_uint64()
+    buf = ctypes.create_string_buffer(ERR_LEN)
+    _err(_fam_lib().orc_fold(FAMILY_TYPES[t], FOLDS[f], _p(x), len(x), ctypes.byref(out), buf), buf)
+    return word_bits(sum_type(t) if f == "add" else t, out.value)
+
+
+def argext(t, is_max, x):
+    x = as_type(x, t)
+    out = ctypes.c_int64()
+    buf = ctypes.create_string_buffer(ERR_LEN)
+    _err(_fam_lib().orc_argext(FAMILY_TYPES[t], int(is_max), _p(x), len(x), ctypes.byref(out), buf), buf)
+    return out.value
+
+
+def fused_sum(t, what, x, y=None, cmp="eq", c=0, e=0):
+    """dot / sumsq / condsum_<cmp> on t: the result word in the sum type's width."""
+    x = as_type(x, t)
+    y = as_type(y, t) if y is not None else x
+    w = _fam_lib().orc_fused_sum(FAMILY_TYPES[t], {"dot": 0, "sumsq": 1, "condsum": 2}[what], CMPS[cmp],
+                                 _p(x), _p(y), len(x), word(t, c), word(t, e))
+    return word_bits(sum_type(t), w)
+
+
+def count_cmp(t, cmp, x, c):
+    x = as_type(x, t)
+    return int(_fam_lib().orc_count_cmp(FAMILY_TYPES[t], CMPS[cmp], _p(x), len(x), word(t, c)))
+
+
+def filter_cmp(t, cmp, x, c):
+    x = as_type(x, t)
+    out = np.empty(len(x), dtype=NP_TYPES[t])
+    k = _fam_lib().orc_filter_cmp(FAMILY_TYPES[t], CMPS[cmp], _p(x), len(x), word(t, c), _p(out))
+    return out[:k]
+
+
+def scan(t, f, x, starts=None):
+    """scan_<f>_<t> (starts None) or scan_by_<f>_<t>: the output rows (sum type for add)."""
+    x = as_type(x, t)
+    ot = sum_type(t) if f == "add" else t
+    out = np.empty(len(x), dtype=NP_TYPES[ot])
+    s = _u8(starts) if starts is not None else np.zeros(1, np.uint8)
+    _fam_lib().orc_scan(FAMILY_TYPES[t], FOLDS[f], int(starts is not None), _p(x), _p(s), len(x), _p(out))
+    return out
+
+
+def reduce_into(t, f, keys, vals, buckets):
+    """reduce_into_<f>_<t>: the bucket rows (sum type for add), errors as the reference's."""
+    keys, vals = _i64(keys), as_type(vals, t)
+    ot = sum_type(t) if f == "add" else t
+    if buckets > 1 << 28 and len(keys) == len(vals):
+        _huge_buckets(keys, buckets)
+    out = np.empty(max(0, min(buckets, 1 << 28)), dtype=NP_TYPES[ot])
+    buf = ctypes.create_string_buffer(ERR_LEN)
+    _err(_fam_lib().orc_reduce_into(FAMILY_TYPES[t], FOLDS[f], _p(keys), len(keys), _p(vals), len(vals),
+                                    buckets, _p(out), buf), buf)
+    return out

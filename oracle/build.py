@@ -14,7 +14,7 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "liboracle.so")
 STAMP = LIB + ".stamp"
-SRCS = [os.path.join(HERE, "oracle.c"), os.path.join(HERE, "elementwise.c")]
+SRCS = [os.path.join(HERE, "oracle.c"), os.path.join(HERE, "elementwise.c"), os.path.join(HERE, "families.c")]
 HDR = os.path.join(HERE, "oracle.h")
 CFLAGS = ["-O3", "-ffp-contract=off", "-std=c11", "-fPIC", "-shared"]
 

@@ -116,6 +116,18 @@ int orc_ew_div_const(int type, const void *a, const void *d, int64_t n, void *ou
 double orc_neumaier_sum(const double *x, int64_t n);
 void orc_dd_sum(const double *x, int64_t n, double *hi, double *lo);
 
+/* families.c: the kernel families on every element type. Types are vkc_type numbers (0 f64,
+ * 1 f32, 2 i64, 3 u64, 4 i32, 5 u8, 6 bool); folds 0 add, 1 mul, 2 min, 3 max, 4 and, 5 or, 6 xor.
+ * Values are 64-bit words (i32 sign-extended, u8/bool zero-extended, f32 as its 32 bits). */
+int orc_fold(int t, int f, const void *x, int64_t n, uint64_t *out, char *err);
+int orc_argext(int t, int is_max, const void *x, int64_t n, int64_t *out, char *err);
+uint64_t orc_fused_sum(int t, int what, int cmp, const void *x, const void *y, int64_t n, uint64_t c, uint64_t e);
+int64_t orc_count_cmp(int t, int cmp, const void *x, int64_t n, uint64_t c);
+int64_t orc_filter_cmp(int t, int cmp, const void *x, int64_t n, uint64_t c, void *out);
+void orc_scan(int t, int f, int by, const void *x, const uint8_t *starts, int64_t n, void *out);
+int orc_reduce_into(int t, int f, const int64_t *keys, int64_t nk, const void *vals, int64_t nv, int64_t nb,
+                    void *out, char *err);
+
 #ifdef __cplusplus
 }
 #endif

@@ -90,3 +90,21 @@ def test_missing_library_raises_instead_of_falling_back(tmp_path, monkeypatch):
         vk.load()
     with pytest.raises(RuntimeError, match="not built"):
         vk.Context(0)
+
+
+def test_table_covers_the_reference_registry(lib):
+    # Every kernel of the reference's registry that can receive a device array has a cuda entry
+    # (tests/golden/reference_kernels.py restates the registration functions), so `select`
+    # (src/kernels.rs:342-368) never falls back to a host entry for device-resident values.
+    import sys
+
+    sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
+    import reference_kernels
+    import verkehrt_gb300 as vk
+
+    ours = {name for name, _, _, _ in vk.kernels()}
+    missing = sorted(set(reference_kernels.device_names()) - ours)
+    assert not missing, missing
+    # Beyond the reference: the float extensions of its tier-2 design notes only.
+    assert sorted(ours - set(reference_kernels.all_names())) == [
+        "reduce_into_add_f64", "scan_add_f64", "scan_by_add_f64"]

@@ -1,10 +1,13 @@
 """The failure paths, made to happen on the host or by a wait that runs out, never by a GPU fault.
 
-* A wait on another block that runs out: with the context's "spin_limit" test hook at one or
-  two polls, the decoupled lookbacks of scan_add_i64 give up while their predecessors are
-  still working. The kernel records the timeout in the status word and returns (its outputs
-  stay in bounds: a lookback that gives up uses the scan's identity as its prefix), the call
-  reports VKC_TIMEOUT, and the same context then gives the oracle's results again.
+* A wait on another block that runs out: the "lookback_never_ready" test hook makes every
+  decoupled lookback of scan_add_i64 poll for records that no block writes (a flag that
+  nothing sets), and the "spin_limit" hook bounds each wait to a few dozen polls. Each waiting
+  block records the timeout in the status word and goes on (its outputs stay in bounds: a
+  lookback that gives up uses the scan's identity as its prefix). A scan's call only enqueues
+  its kernels, so the next call that waits for the device (a download, vkc_synchronize)
+  reports VKC_TIMEOUT; a selection waits for its count and reports it itself. The same
+  context then gives the oracle's results again.
 * An allocation that fails: the "fail_alloc_after" hook makes one array allocation of the
   context report failure, as a device out of memory would. The call returns VKC_ALLOC with
   the reference's text (src/kernels/scalar/index/radix.rs:151-157 for argsort scratch,
@@ -42,18 +45,26 @@ def test_a_wait_that_runs_out_reports_a_timeout_and_the_context_recovers(fresh):
     dv = fresh.upload(v)
     want = oracle.scan_add_i64(v)
     assert np.array_equal(fresh.call("scan_add_i64", dv).numpy(), want)
-    fresh.tune_set("spin_limit", 0, 1)
-    assert fresh.tune_get("spin_limit", 0) == 1
-    timeouts = 0
-    for _ in range(8):
-        try:
-            fresh.call("scan_add_i64", dv)
-        except vk.KernelError as e:
-            assert e.status == "TIMEOUT", (e.status, e.message)
-            assert e.message == "a device-side wait gave up"
-            timeouts += 1
-    assert timeouts > 0
+    fresh.tune_set("spin_limit", 0, 64)
+    fresh.tune_set("lookback_never_ready", 0, 1)
+    assert fresh.tune_get("spin_limit", 0) == 64
+    assert fresh.tune_get("lookback_never_ready", 0) == 1
+    # A scan only enqueues its kernels: the next call that waits for the device reports it.
+    out = fresh.call("scan_add_i64", dv)
+    with pytest.raises(vk.KernelError) as e:
+        out.numpy()
+    assert (e.value.status, e.value.message) == ("TIMEOUT", "a device-side wait gave up")
+    fresh.call("scan_add_i64", dv)
+    with pytest.raises(vk.KernelError) as e:
+        fresh.synchronize()
+    assert (e.value.status, e.value.message) == ("TIMEOUT", "a device-side wait gave up")
+    # A selection waits for its count, so the call itself reports it.
+    with pytest.raises(vk.KernelError) as e:
+        fresh.call("filter_gt_f64", fresh.call("rand_f64", 1 << 24, 1), 0.5)
+    assert (e.value.status, e.value.message) == ("TIMEOUT", "a device-side wait gave up")
+    fresh.tune_set("lookback_never_ready", 0, 0)
     fresh.tune_set("spin_limit", 0, 0)
+    assert (fresh.tune_get("spin_limit", 0), fresh.tune_get("lookback_never_ready", 0)) == (0, 0)
     for _ in range(3):
         assert np.array_equal(fresh.call("scan_add_i64", dv).numpy(), want)
     assert fresh.call("reduce_add_i64", dv) == int(v.sum())
@@ -96,3 +107,5 @@ def test_hook_values_are_checked(fresh):
         fresh.tune_set("spin_limit", 0, -1)
     with pytest.raises(vk.KernelError):
         fresh.tune_set("fail_alloc_after", 0, -2)
+    with pytest.raises(vk.KernelError):
+        fresh.tune_set("lookback_never_ready", 0, 2)

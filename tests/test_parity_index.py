@@ -111,6 +111,25 @@ def test_histogram_and_reduce_into_skewed(ctx):
                                   oracle.reduce_into_add_i64(keys, v, nb)), nb
 
 
+def test_buckets_over_sorted_runs(ctx):
+    # Runs of 1 to 5000 equal keys (run numbers of a sorted group-by): runs are summed in the
+    # warp and carried across 32-row groups; keys large and small, runs split at any row.
+    lens = 1 + (oracle.rand_i64(4000, 91).view(np.uint64) % np.uint64(5000)).astype(np.int64)
+    for nb, stride in ((1 << 20, 97), (4096, 1), (5000, 1)):
+        keys = np.repeat((np.arange(len(lens)) * stride) % nb, lens).astype(np.int64)
+        v = oracle.rand_i64(len(keys), 92)
+        assert np.array_equal(ctx.call("histogram", ctx.upload(keys), nb).numpy(), oracle.histogram(keys, nb))
+        assert np.array_equal(ctx.call("reduce_into_add_i64", ctx.upload(keys), ctx.upload(v), nb).numpy(),
+                              oracle.reduce_into_add_i64(keys, v, nb))
+    # A bad key inside a long run and another later: the first one is reported.
+    keys = np.repeat(np.arange(100, dtype=np.int64), 1000)
+    keys[51_234] = -5
+    keys[70_000] = 10 ** 9
+    want = err_of(lambda: oracle.histogram(keys, 100))
+    assert want == "bucket key -5 out of range for 100 buckets"
+    assert err_of(lambda: ctx.call("histogram", ctx.upload(keys), 100)) == want
+
+
 def test_bucket_errors(ctx):
     # src/kernels/tests.rs:1576-1620
     for keys, nb in (([0, 3], 3), ([0, -1], 3), ([0, 0], 0), ([], -1), ([0], 1 << 62), ([0], 1 << 50),

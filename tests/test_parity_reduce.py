@@ -68,6 +68,29 @@ def test_signed_inputs_large(ctx):
     assert r.finish(raw=True)[2] == bits(oracle.reduce_add_f64(np.concatenate([first, second])))
 
 
+def test_sums_that_wander_at_2p26(ctx):
+    # Inputs whose lane sums keep leaving their binade: mean-centred rows (the sum wanders
+    # around zero), magnitudes as large as the sum, all negative. The walk stops after a budget
+    # of tiles and the lane chain finishes each lane; the bits are the reference order's.
+    n = 1 << 26
+    u = uniform(n, 41)
+    for name, x in (("centred", u - 0.5), ("wide", varied(n, 42)), ("negative", -u)):
+        dx = ctx.upload(x)
+        assert ctx.call("reduce_add_f64", dx, raw=True)[2] == bits(oracle.reduce_add_f64(x)), name
+        del dx
+    y = uniform(n, 43) - 0.5
+    x = u - 0.5
+    assert ctx.call("dot_f64", ctx.upload(x), ctx.upload(y), raw=True)[2] == bits(oracle.dot_f64(x, y))
+    assert ctx.call("sumsq_f64", ctx.upload(x), raw=True)[2] == bits(oracle.sumsq_f64(x))
+    assert ctx.call("condsum_gt_f64", ctx.upload(x), -0.25, 0.125, raw=True)[2] == bits(
+        oracle.condsum_cmp_f64(x, "gt", -0.25, 0.125))
+    # Tile-fed: the chain's lane states carry into the next update.
+    r = ctx.reducer("reduce_add_f64")
+    r.update(ctx.upload(x[: 1 << 25]))
+    r.update(ctx.upload(x[1 << 25:]))
+    assert r.finish(raw=True)[2] == bits(oracle.reduce_add_f64(x))
+
+
 def test_reduce_add_f64_device_generated_large(ctx):
     n = 1 << 24
     got = ctx.call("reduce_add_f64", ctx.call("rand_f64", n, 7), raw=True)[2]

@@ -320,6 +320,8 @@ struct CanonWork {
                                // flagged tiles, listed from [T + 2]
     unsigned long long *tstate = nullptr;  // scans: [16][T + 1] exact lane state before each tile
     int *whole = nullptr;                  // scans: [16][C] chunks the walk took whole
+    int *resume = nullptr;                 // reductions: [16] tile where the lane chain takes over
+                                           // from the walk (T: the walk finished the lane)
 };
 
 constexpr int CAND_GROUP = 1024;  // tiles per K2 block
@@ -858,6 +860,7 @@ __device__ unsigned long long resolve_tile(const RowArgs &args, int64_t nb, int 
 // tiles inside mixed chunks, and resolves from the rows the tiles that none carries (binade
 // crossings, negative or special rows, the first rows of the lane).
 constexpr int WK_THREADS = 256;
+constexpr int WALK_BUDGET = 1024;  // rounds of a lane's walk, plus T / 64
 constexpr int WK_MAX_CHUNKS = 4096;  // chunk records held in shared memory
 constexpr int WK_MAX_MIXED = 48;     // mixed chunks whose tile records are held there
 
@@ -875,15 +878,23 @@ struct WalkSmem {
 // functions hold, and the tiles none carries resolved from the rows. RECORD (scans) stores the
 // exact state before each tile. sm and slot give the chunk's tile records when the walk holds
 // them in shared memory (slot >= 0).
+// Without RECORD, each round of the tile loop (a run of tiles whose functions apply, or one tile
+// resolved from the rows) spends one unit of `budget`: when it runs out, *stop gets the next
+// tile and the state before it is returned (the lane chain goes on from there).
 template <int OP, bool SIGNED, bool RECORD>
 __device__ __forceinline__ unsigned long long walk_chunk_tiles(const RowArgs &args, int64_t nb, int T, const CanonWork &wk,
                                                                const WalkSmem *sm, int slot, int L, int k,
-                                                               unsigned long long s) {
+                                                               unsigned long long s, int *budget = nullptr,
+                                                               int *stop = nullptr) {
     const int lane = threadIdx.x & 31;
     unsigned long long *rec = RECORD ? wk.tstate + static_cast<int64_t>(L) * (T + 1) : nullptr;
     int tp = k * 32;
     const int end = min(T, tp + 32);
     while (tp < end) {
+        if (!RECORD && budget && --*budget < 0) {
+            *stop = tp;
+            return s;
+        }
         if (RECORD && lane == 0) rec[tp] = s;
         const int Et = state_binade(s);
         const int tl = tp + lane;
@@ -924,10 +935,19 @@ __device__ __forceinline__ unsigned long long walk_chunk_tiles(const RowArgs &ar
 template <int OP, bool SIGNED, bool RECORD>
 __device__ __forceinline__ unsigned long long walk_lane(const RowArgs &args, int64_t nb, int T, int C, const CanonWork &wk,
                                                         const WalkSmem &sm, bool held, const int *gE, const TF *gD,
-                                                        int L, unsigned long long s) {
+                                                        int L, unsigned long long s, int *stop) {
     const int lane = threadIdx.x;
+    // Rounds of the walk before the lane chain takes over (reductions only; each round costs a
+    // few microseconds of dependent loads): a growing sum's few dozen binade crossings stay in the
+    // walk; sums that wander (signed rows, magnitudes as large as the sum) go to the chain, which
+    // adds the rows at a steady rate.
+    int budget = WALK_BUDGET + T / 64;
     int k = 0;  // next chunk
     while (k < C) {
+        if (!RECORD && --budget < 0) {
+            *stop = k * 32;
+            return s;
+        }
         // Whole chunks k .. k+31.
         const int E = state_binade(s);
         const int kc = k + lane;
@@ -953,7 +973,9 @@ __device__ __forceinline__ unsigned long long walk_lane(const RowArgs &args, int
             continue;
         }
         // Chunk k, tile by tile.
-        s = walk_chunk_tiles<OP, SIGNED, RECORD>(args, nb, T, wk, &sm, held ? sm.mixed_of[k] : -1, L, k, s);
+        s = walk_chunk_tiles<OP, SIGNED, RECORD>(args, nb, T, wk, &sm, held ? sm.mixed_of[k] : -1, L, k, s,
+                                                 &budget, stop);
+        if (*stop >= 0) return s;
         ++k;
     }
     return s;
@@ -1008,11 +1030,13 @@ __global__ void __launch_bounds__(WK_THREADS) canon_walk_kernel(RowArgs args, in
     if (t >= 32) return;
     const int lane = t;
     unsigned long long s = state->lanes[L];
-    s = (wk.flags[T] != 0 || (s >> 63)) ? walk_lane<OP, true, RECORD>(args, nb, T, C, wk, sm, held, gE, gD, L, s)
-                                        : walk_lane<OP, false, RECORD>(args, nb, T, C, wk, sm, held, gE, gD, L, s);
+    int stop = -1;
+    s = (wk.flags[T] != 0 || (s >> 63)) ? walk_lane<OP, true, RECORD>(args, nb, T, C, wk, sm, held, gE, gD, L, s, &stop)
+                                        : walk_lane<OP, false, RECORD>(args, nb, T, C, wk, sm, held, gE, gD, L, s, &stop);
     if (lane == 0) {
         state->lanes[L] = s;
         if (RECORD) wk.tstate[static_cast<int64_t>(L) * (T + 1) + T] = s;
+        else wk.resume[L] = stop >= 0 ? stop : T;
     }
 }
 
@@ -1073,6 +1097,175 @@ __global__ void canon_finish(CanonState *state, int tail_len) {
     state->result = as_bits(r);
 }
 
+// ---------------------------------------------------------------------------- the lane chain
+// Reductions whose lane sums keep leaving their binade (rows of both signs whose sum wanders
+// around zero, magnitudes as large as the sum) make the walk resolve most tiles from the rows,
+// one at a time. After WALK_BUDGET such tiles the walk stops and this kernel runs each stopped
+// lane to the end from its exact state. One warp per lane; each step takes 1024 of the lane's
+// rows, 32 consecutive ones per thread, prefetched CH_SLOTS - 1 steps ahead with cp.async into
+// the thread's own row of a shared ring (each thread reads only what it copied).
+//
+// A thread's 32 rows act on the state's magnitude S (in ulps u = 2^(E-52) of its binade E) as
+// integer increments, the integer step of seg_tf: +-RNE(|x|/u) by the row's sign relative to
+// the state's, and for a row exactly halfway the even neighbour, which depends on the parity of
+// S at that row; so each thread keeps its increments for both parities of S before its rows,
+// with the lowest (mn) and highest (mx) partial sum, and a warp scan composes the parity pairs
+// in order. This is exact while every state on the way stays inside the binade: the state
+// passes every thread whose states all stay in [2^52 + 1, 2^53 - 1] ulps (the margin keeps the
+// exact sum of a downward step above 2^E); the first thread whose rows fail (a crossing, a row
+// not below 2^E or not finite) adds its rows with IEEE adds, the reference's own operation, and
+// the rest are computed again for the new state. So the result is the chain's, bit for bit.
+constexpr int CH_ROWS = 32;                  // lane rows per thread and step
+constexpr int CH_STEP = 32 * CH_ROWS;        // 16-row blocks per step
+constexpr int CH_SLOTS = 8;                  // steps in the shared ring
+constexpr int CH_PITCH = CH_ROWS + 1;        // doubles per thread row (odd: spreads the banks)
+
+__device__ __forceinline__ void cp_async8(void *dst, const void *src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N> __device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+template <int OP> constexpr size_t chain_smem() {
+    return static_cast<size_t>(CH_SLOTS) * (OP == ROW_DOT ? 2 : 1) * 32 * CH_PITCH * sizeof(unsigned long long);
+}
+
+template <int OP>
+__global__ void __launch_bounds__(32) canon_chain_kernel(RowArgs args, int64_t nb, int T, CanonWork wk,
+                                                         CanonState *state) {
+    extern __shared__ __align__(16) unsigned long long chain_smem_buf[];
+    constexpr int NA = OP == ROW_DOT ? 2 : 1;
+    const int L = blockIdx.x, j = threadIdx.x;
+    const int t0 = wk.resume[L];
+    if (t0 >= T) return;
+    const int64_t b0 = static_cast<int64_t>(t0) * CT_BLOCKS;
+    const int64_t steps = (nb - b0 + CH_STEP - 1) / CH_STEP;
+    auto row_at = [&](int64_t k, int a) {
+        return chain_smem_buf + ((k % CH_SLOTS) * NA + a) * (32 * CH_PITCH) + j * CH_PITCH;
+    };
+    // Copies of step k (an empty group past the end keeps the group count uniform).
+    auto issue = [&](int64_t k) {
+        if (k < steps) {
+            const int64_t bb = b0 + k * CH_STEP + static_cast<int64_t>(j) * CH_ROWS;
+            unsigned long long *dx = row_at(k, 0);
+            unsigned long long *dy = row_at(k, NA - 1);
+#pragma unroll 8
+            for (int i = 0; i < CH_ROWS; ++i) {
+                if (bb + i < nb) {
+                    cp_async8(dx + i, args.x + (bb + i) * 16 + L);
+                    if (OP == ROW_DOT) cp_async8(dy + i, args.y + (bb + i) * 16 + L);
+                }
+            }
+        }
+        cp_async_commit();
+    };
+    for (int k = 0; k < CH_SLOTS - 1; ++k) issue(k);
+    unsigned long long s = state->lanes[L];
+    for (int64_t k = 0; k < steps; ++k) {
+        cp_async_wait<CH_SLOTS - 2>();  // this thread's copies of step k have landed
+        unsigned long long v[CH_ROWS];
+        {
+            const int64_t bb = b0 + k * CH_STEP + static_cast<int64_t>(j) * CH_ROWS;
+            const unsigned long long *rx = row_at(k, 0);
+            const unsigned long long *ry = row_at(k, NA - 1);
+#pragma unroll
+            for (int i = 0; i < CH_ROWS; ++i)
+                v[i] = bb + i < nb ? row_value<OP>(args, rx[i], OP == ROW_DOT ? ry[i] : 0ull) : 0ull;
+        }
+        issue(k + CH_SLOTS - 1);  // into the slot of step k - 1, read by the previous step
+        if ((s & ~(1ull << 63)) > 0x7ff0000000000000ull) continue;  // NaN stays NaN
+        int cur = 0;  // threads already applied
+        // The thread's function depends on the binade and the state's sign only (in magnitude
+        // space a negative state adds the negated rows), so it is computed again only when a
+        // fallback changes either. A halfway row rounds to the even neighbour, so the function
+        // is kept for both parities of the state before the thread's rows: (P0, mn0, mx0) for an
+        // even start, (P1, mn1, mx1) for an odd one.
+        unsigned fkey = ~0u;
+        long long fP0 = 0, fP1 = 0, fmn0 = 0, fmx0 = 0, fmn1 = 0, fmx1 = 0;
+        bool fok = false;
+        while (cur < 32) {
+            const unsigned es = static_cast<unsigned>(s >> 52) & 0x7ffu;
+            const unsigned long long neg = s >> 63;
+            const bool usable = es >= 64u && es <= 2046u;
+            const unsigned key = es | static_cast<unsigned>(neg << 11);
+            if (usable && j >= cur && key != fkey) {
+                fkey = key;
+                fP0 = fP1 = 0;
+                fmn0 = fmn1 = LLONG_MAX;
+                fmx0 = fmx1 = LLONG_MIN;
+                fok = true;
+#pragma unroll
+                for (int i = 0; i < CH_ROWS; ++i) {
+                    const unsigned long long b = v[i];
+                    const unsigned ex = static_cast<unsigned>(b >> 52) & 0x7ffu;
+                    fok &= ex < es;  // below 2^E and finite
+                    const unsigned k2 = min(es - ex, 63u);
+                    const unsigned long long w = ((b & MANT) | ONE52) + (1ull << ((k2 - 1) & 63));
+                    const long long q = static_cast<long long>(w >> k2);
+                    long long i0 = q, i1 = q;
+                    if ((w << ((64 - k2) & 63)) == 0) {  // halfway: to the even magnitude
+                        const long long qf = q - 1;
+                        i0 = qf + ((fP0 + qf) & 1);
+                        i1 = qf + ((1 + fP1 + qf) & 1);
+                    }
+                    const bool down = ((b >> 63) ^ neg) != 0;  // the row moves the magnitude down
+                    fP0 += down ? -i0 : i0;
+                    fP1 += down ? -i1 : i1;
+                    fmn0 = min(fmn0, fP0);
+                    fmx0 = max(fmx0, fP0);
+                    fmn1 = min(fmn1, fP1);
+                    fmx1 = max(fmx1, fP1);
+                }
+            }
+            const bool live = j >= cur;
+            const bool ok = !live || (usable && fok);
+            // Ordered composition of the parity pairs (the state's parity after a function).
+            long long c0 = live ? fP0 : 0, c1 = live ? fP1 : 0;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const long long a0 = __shfl_up_sync(FULL, c0, o), a1 = __shfl_up_sync(FULL, c1, o);
+                if (j >= o) {
+                    const long long n0 = a0 + ((a0 & 1) ? c1 : c0);
+                    const long long n1 = a1 + (((1 + a1) & 1) ? c1 : c0);
+                    c0 = n0;
+                    c1 = n1;
+                }
+            }
+            const long long e0 = __shfl_up_sync(FULL, c0, 1), e1 = __shfl_up_sync(FULL, c1, 1);
+            const long long M = static_cast<long long>((s & MANT) | ONE52);
+            const long long p0 = M & 1;
+            const long long pre = j == 0 ? 0 : (p0 ? e1 : e0);  // increments before this thread
+            const bool odd = ((p0 + pre) & 1) != 0;
+            const long long mn = odd ? fmn1 : fmn0, mx = odd ? fmx1 : fmx0;
+            const long long lo = static_cast<long long>(ONE52) + 1, hi = static_cast<long long>(2 * ONE52) - 1;
+            bool valid = !live;
+            if (!valid && ok) valid = M + pre + mn >= lo && M + pre + mx <= hi;
+            const unsigned bad = __ballot_sync(FULL, !valid);
+            const int js = bad ? __ffs(bad) - 1 : 32;
+            if (js > cur) {
+                const long long tot = p0 ? __shfl_sync(FULL, c1, 31) : __shfl_sync(FULL, c0, 31);
+                const long long adv = js < 32 ? __shfl_sync(FULL, pre, js) : tot;
+                const unsigned long long Mn = static_cast<unsigned long long>(M + adv);
+                s = (neg << 63) | (static_cast<unsigned long long>(es) << 52) | (Mn & MANT);
+            }
+            if (js == 32) break;
+            unsigned long long r = 0;
+            if (j == js) {
+                double d = as_f64(s);
+#pragma unroll
+                for (int i = 0; i < CH_ROWS; ++i) d = __dadd_rn(d, as_f64(v[i]));
+                r = as_bits(d);
+            }
+            s = __shfl_sync(FULL, r, js);
+            cur = js + 1;
+        }
+    }
+    cp_async_wait<0>();
+    if (j == 0) state->lanes[L] = s;
+}
+
 // RECORD (scans): the walk also stores the exact lane state before every tile in wk.tstate.
 template <int OP, bool ALIGNED, bool RECORD = false>
 static vkc_status launch_canon(vkc_ctx *ctx, const RowArgs &a, int64_t nb, int T, int C, const CanonWork &wk,
@@ -1107,6 +1300,15 @@ static vkc_status launch_canon(vkc_ctx *ctx, const RowArgs &a, int64_t nb, int T
     if constexpr (RECORD) VKC_CUDA(ctx, cudaMemsetAsync(wk.whole, 0, static_cast<size_t>(C) * 16 * sizeof(int), ctx->stream));
     canon_walk_kernel<OP, RECORD><<<16, WK_THREADS, sizeof(WalkSmem), ctx->stream>>>(a, nb, T, C, wk, state);
     if ((st = launched(ctx, "canon_walk"))) return st;
+    if constexpr (!RECORD) {
+        static std::atomic<unsigned long long> chain_configured{0};
+        once_per_device(chain_configured, ctx->device, [] {
+            cudaFuncSetAttribute(canon_chain_kernel<OP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 static_cast<int>(chain_smem<OP>()));
+        });
+        canon_chain_kernel<OP><<<16, 32, chain_smem<OP>(), ctx->stream>>>(a, nb, T, wk, state);
+        if ((st = launched(ctx, "canon_chain"))) return st;
+    }
     if constexpr (RECORD) {
         canon_fill_kernel<OP><<<(warps + 7) / 8, 256, 0, ctx->stream>>>(a, nb, T, C, wk);
         if ((st = launched(ctx, "canon_fill"))) return st;
@@ -1131,12 +1333,14 @@ static size_t canon_layout(int T, int C, bool scan, char *b, CanonWork *wk, Cano
     const size_t o_ts = o_fl + up(static_cast<size_t>(2 * T + 2) * sizeof(int));
     const size_t o_wh = o_ts + up(static_cast<size_t>(T + 1) * 16 * sizeof(unsigned long long));
     const size_t o_cs = o_wh + up(c16 * sizeof(int));
-    const size_t total = scan ? o_cs + sizeof(CanonState) : o_fl + static_cast<size_t>(2 * T + 2) * sizeof(int);
+    const size_t o_rs = up(o_fl + static_cast<size_t>(2 * T + 2) * sizeof(int));
+    const size_t total = scan ? o_cs + sizeof(CanonState) : o_rs + 16 * sizeof(int);
     if (b) {
         *wk = CanonWork{reinterpret_cast<float *>(b), reinterpret_cast<int *>(b + o_cand),
                         reinterpret_cast<int *>(b + o_recE), reinterpret_cast<TF *>(b + o_recD),
                         reinterpret_cast<int *>(b + o_chE), reinterpret_cast<TF *>(b + o_chD),
                         reinterpret_cast<double *>(b + o_gs), reinterpret_cast<int *>(b + o_fl)};
+        if (!scan) wk->resume = reinterpret_cast<int *>(b + o_rs);
         if (scan) {
             wk->tstate = reinterpret_cast<unsigned long long *>(b + o_ts);
             wk->whole = reinterpret_cast<int *>(b + o_wh);

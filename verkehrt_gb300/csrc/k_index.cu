@@ -348,13 +348,19 @@ __global__ void __launch_bounds__(256) keys_check_kernel(const long long *__rest
     if (bad != ~0ull) atomicMin(&status->first_bad, bad);
 }
 
-// Per-bucket wrapping sums (vals) or counts (vals == nullptr). Buckets below SMEM_BINS are
-// accumulated in shared memory per block and added to the output once per block; the others
-// go to global atomics. Small keys are where the contention is: group ids number groups by first
+// Per-bucket wrapping sums (vals) or counts (vals == nullptr). Every warp walks chunks of
+// BK_ITEMS groups of 32 consecutive rows (one coalesced load per group and array, all groups of
+// a chunk loaded before any is added). Within a group, runs of equal keys in consecutive lanes
+// are summed by a segmented warp scan, so only the lane that ends a run adds it to a bucket; the
+// run that ends a group is carried into the next group while the key stays the same. Sorted
+// keys (run numbers, sorted group keys) thus cost about one addition per run instead of one per
+// row, which removes the contention of long runs on one bucket. Buckets below SMEM_BINS are
+// added in shared memory per block and to the output once per block; the others go to global
+// atomics. Small keys are where random contention is: group ids number groups by first
 // occurrence, so frequent groups get small ids (under a Zipf(1.1) key distribution the first
 // 4096 ids hold about three quarters of the rows).
 constexpr int SMEM_BINS = 4096;
-constexpr int BK_ROWS = 4;  // rows per thread in flight
+constexpr int BK_ITEMS = 8;  // groups of 32 rows per warp chunk, all loaded before use
 
 template <bool COUNT>
 __global__ void __launch_bounds__(256) bucket_kernel(const long long *__restrict__ keys,
@@ -365,30 +371,65 @@ __global__ void __launch_bounds__(256) bucket_kernel(const long long *__restrict
     const int sb = nb < static_cast<uint64_t>(SMEM_BINS) ? static_cast<int>(nb) : SMEM_BINS;
     for (int b = threadIdx.x; b < sb; b += blockDim.x) bins[b] = 0;
     __syncthreads();
-    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    const int lane = threadIdx.x & 31;
+    const int64_t warps = static_cast<int64_t>(gridDim.x) * (blockDim.x >> 5);
+    const int64_t chunk_rows = 32 * BK_ITEMS;
+    const int64_t chunks = (n + chunk_rows - 1) / chunk_rows;
+    const unsigned below = (1u << lane) - 1u;
+    auto add = [&](long long k, unsigned long long v) {
+        if (k < SMEM_BINS) atomicAdd(&bins[k], v);
+        else atomicAdd(out + k, v);
+    };
+    constexpr long long NONE = -1;  // a lane with no row in range: never added
     unsigned long long bad = ~0ull;
-    for (int64_t i0 = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i0 < n; i0 += BK_ROWS * stride) {
-        long long k[BK_ROWS];
-        unsigned long long v[BK_ROWS];
+    long long ckey = NONE;  // the carried run (the same in every lane)
+    unsigned long long csum = 0;
+    for (int64_t c = static_cast<int64_t>(blockIdx.x) * (blockDim.x >> 5) + (threadIdx.x >> 5); c < chunks;
+         c += warps) {
+        const int64_t base = c * chunk_rows + lane;
+        long long k[BK_ITEMS];
+        unsigned long long v[BK_ITEMS];
 #pragma unroll
-        for (int r = 0; r < BK_ROWS; ++r) {
-            const int64_t i = i0 + r * stride;
-            k[r] = i < n ? __ldcs(keys + i) : 0;
+        for (int r = 0; r < BK_ITEMS; ++r) {
+            const int64_t i = base + 32 * r;
+            k[r] = i < n ? __ldcs(keys + i) : NONE;
             v[r] = (!COUNT && i < n) ? __ldcs(vals + i) : 1ull;
         }
 #pragma unroll
-        for (int r = 0; r < BK_ROWS; ++r) {
-            const int64_t i = i0 + r * stride;
-            if (i >= n) break;
-            if (static_cast<uint64_t>(k[r]) >= nb) {
+        for (int r = 0; r < BK_ITEMS; ++r) {
+            const int64_t i = base + 32 * r;
+            long long key = k[r];
+            if (i < n && static_cast<uint64_t>(key) >= nb) {
                 if (static_cast<unsigned long long>(i) < bad) bad = static_cast<unsigned long long>(i);
-            } else if (k[r] < SMEM_BINS) {
-                atomicAdd(&bins[k[r]], v[r]);
-            } else {
-                atomicAdd(out + k[r], v[r]);
+                key = NONE;
+            }
+            unsigned long long x = key == NONE ? 0ull : v[r];
+            // Runs of equal keys: a lane heads a run when its key differs from the lane before.
+            const long long up = __shfl_up_sync(FULL, key, 1);
+            const bool head = lane == 0 || up != key;
+            const unsigned heads = __ballot_sync(FULL, head);
+            const int start = 31 - __clz(heads & (below | (1u << lane)));  // this run's first lane
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const unsigned long long t = __shfl_up_sync(FULL, x, o);
+                if (lane - o >= start) x += t;
+            }
+            const bool tail = lane == 31 || ((heads >> (lane + 1)) & 1u);
+            // Runs of the carried key join the carry; the run ending at lane 31 becomes the next
+            // carry; every other run is added now.
+            const unsigned long long join = warp_sum(tail && key == ckey ? x : 0ull);
+            csum += join;
+            const long long k31 = __shfl_sync(FULL, key, 31);
+            const unsigned long long x31 = __shfl_sync(FULL, x, 31);
+            if (tail && lane != 31 && key != ckey && key != NONE) add(key, x);
+            if (k31 != ckey) {
+                if (lane == 0 && ckey != NONE) add(ckey, csum);
+                ckey = k31;
+                csum = x31;
             }
         }
     }
+    if (lane == 0 && ckey != NONE) add(ckey, csum);
     if (bad != ~0ull) atomicMin(&status->first_bad, bad);
     __syncthreads();
     for (int b = threadIdx.x; b < sb; b += blockDim.x)

@@ -88,11 +88,17 @@ __device__ __forceinline__ void st_relaxed64(unsigned long long *p, unsigned lon
 // of this library can hang the GPU.
 constexpr unsigned SPIN_LIMIT = 1u << 22;
 
-// The poll budget of a wait on another block: the context's test override when set (a status
-// word's spin_limit), else SPIN_LIMIT. Waits for a block's own copies always use SPIN_LIMIT.
+// The poll budget of a wait on another block: the context's test override when set (the low 31
+// bits of a status word's spin_limit), else SPIN_LIMIT. Waits for a block's own copies always
+// use SPIN_LIMIT. Bit 31 is a second test hook (lookback_never_ready): lookbacks then poll for
+// records of an epoch no block writes, so every wait on another tile runs out.
+constexpr unsigned NEVER_READY = 1u << 31;
 __device__ __forceinline__ unsigned wait_limit(const DevStatus *st) {
-    const unsigned v = *reinterpret_cast<const volatile unsigned *>(&st->spin_limit);
+    const unsigned v = *reinterpret_cast<const volatile unsigned *>(&st->spin_limit) & ~NEVER_READY;
     return v ? v : SPIN_LIMIT;
+}
+__device__ __forceinline__ bool never_ready(const DevStatus *st) {
+    return (*reinterpret_cast<const volatile unsigned *>(&st->spin_limit) & NEVER_READY) != 0;
 }
 
 __device__ __forceinline__ void backoff(unsigned it) {

@@ -84,6 +84,7 @@ void register_group(std::vector<KernelDef> &t);
 void register_io(std::vector<KernelDef> &t);
 void register_reduce_into_f64(std::vector<KernelDef> &t);
 void register_elementwise(std::vector<KernelDef> &t);
+void register_families(std::vector<KernelDef> &t);
 
 // Argument helpers with the reference's messages (src/kernels/scalar/elementwise.rs:172-199).
 std::string arity_error(int want, int got);

@@ -353,6 +353,7 @@ static const std::vector<KernelDef> &table() {
         register_elementwise(v);
         register_io(v);
         register_reduce_into_f64(v);
+        register_families(v);
         return v;
     }();
     return t;
@@ -564,9 +565,13 @@ vkc_status vkc_set_cache_limit(vkc_ctx *ctx, size_t bytes) {
 vkc_status vkc_tune_set(vkc_ctx *ctx, const char *knob, int size_class, int value) {
     if (!ctx || !knob || size_class < 0 || size_class >= TUNE_CLASSES) return VKC_USAGE;
     // Test hooks, the same for every size class.
-    if (std::string(knob) == "spin_limit") {
-        if (value < 0) return fail(ctx, VKC_USAGE, "value " + std::to_string(value) + " not allowed for spin_limit");
-        ctx->spin_limit = static_cast<unsigned>(value);
+    const bool never = std::string(knob) == "lookback_never_ready";
+    if (std::string(knob) == "spin_limit" || never) {
+        if (value < 0 || (never && value > 1))
+            return fail(ctx, VKC_USAGE, "value " + std::to_string(value) + " not allowed for " + knob);
+        const unsigned flag = 1u << 31;
+        if (never) ctx->spin_limit = (ctx->spin_limit & ~flag) | (value ? flag : 0u);
+        else ctx->spin_limit = (ctx->spin_limit & flag) | static_cast<unsigned>(value);
         // The status word carries it to the kernels; a context stream is idle between calls.
         VKC_CUDA(ctx, cudaMemcpyAsync(&ctx->status->spin_limit, &ctx->spin_limit, sizeof(unsigned),
                                       cudaMemcpyHostToDevice, ctx->stream));
@@ -592,7 +597,11 @@ vkc_status vkc_tune_set(vkc_ctx *ctx, const char *knob, int size_class, int valu
 vkc_status vkc_tune_get(const vkc_ctx *ctx, const char *knob, int size_class, int *value) {
     if (!ctx || !knob || !value || size_class < 0 || size_class >= TUNE_CLASSES) return VKC_USAGE;
     if (std::string(knob) == "spin_limit") {
-        *value = static_cast<int>(ctx->spin_limit);
+        *value = static_cast<int>(ctx->spin_limit & ~(1u << 31));
+        return VKC_OK;
+    }
+    if (std::string(knob) == "lookback_never_ready") {
+        *value = static_cast<int>(ctx->spin_limit >> 31);
         return VKC_OK;
     }
     if (std::string(knob) == "fail_alloc_after") {
@@ -611,7 +620,9 @@ vkc_status vkc_synchronize(vkc_ctx *ctx) {
     VKC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     if (ctx->h2d) VKC_CUDA(ctx, cudaStreamSynchronize(ctx->h2d));
     if (ctx->d2h) VKC_CUDA(ctx, cudaStreamSynchronize(ctx->d2h));
-    return VKC_OK;
+    if (stream_capturing(ctx->stream)) return VKC_OK;
+    DevStatus ds;
+    return read_status(ctx, &ds);
 }
 
 vkc_status vkc_set_stream(vkc_ctx *ctx, void *stream) {
@@ -666,7 +677,9 @@ vkc_status vkc_array_download(vkc_ctx *ctx, const vkc_array *a, void *host, int6
         VKC_CUDA(ctx, cudaMemcpyAsync(host, a->data(), static_cast<size_t>(n) * type_width(a->type),
                                       cudaMemcpyDeviceToHost, ctx->stream));
     VKC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    return VKC_OK;
+    // A wait of earlier enqueued work that ran out (its call did not wait for the device).
+    DevStatus ds;
+    return read_status(ctx, &ds);
 }
 
 vkc_status vkc_array_download_start(vkc_ctx *ctx, const vkc_array *a, void *host, int64_t capacity, vkc_copy **out) {
