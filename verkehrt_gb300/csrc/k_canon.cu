@@ -860,9 +860,28 @@ __device__ unsigned long long resolve_tile(const RowArgs &args, int64_t nb, int 
 // tiles inside mixed chunks, and resolves from the rows the tiles that none carries (binade
 // crossings, negative or special rows, the first rows of the lane).
 constexpr int WK_THREADS = 256;
-constexpr int WALK_BUDGET = 1024;  // rounds of a lane's walk, plus T / 64
 constexpr int WK_MAX_CHUNKS = 4096;  // chunk records held in shared memory
 constexpr int WK_MAX_MIXED = 48;     // mixed chunks whose tile records are held there
+
+// The walk's progress over windows of the SM clock: a window in which it advanced fewer tiles
+// than the lane chain would (WALK_MIN_TILES in WALK_WINDOW cycles, about 2 tiles a microsecond)
+// hands the lane to the chain. A growing sum advances hundreds of tiles a microsecond between
+// its few binade crossings; a wandering one resolves tile after tile from the rows.
+constexpr long long WALK_WINDOW = 1ll << 18;
+constexpr int WALK_MIN_TILES = 256;
+struct WalkClock {
+    long long start;
+    int tile;  // the first tile of the window
+    __device__ __forceinline__ bool slower(int tp) {
+        const long long now = clock64();
+        // The first window is four times as long: the lane's first tiles cross many binades.
+        if (now - start < (tile == 0 ? 4 * WALK_WINDOW : WALK_WINDOW)) return false;
+        if (tp - tile < WALK_MIN_TILES) return true;
+        start = now;
+        tile = tp;
+        return false;
+    }
+};
 
 struct WalkSmem {
     int chunkE[WK_MAX_CHUNKS];
@@ -878,20 +897,21 @@ struct WalkSmem {
 // functions hold, and the tiles none carries resolved from the rows. RECORD (scans) stores the
 // exact state before each tile. sm and slot give the chunk's tile records when the walk holds
 // them in shared memory (slot >= 0).
-// Without RECORD, each round of the tile loop (a run of tiles whose functions apply, or one tile
-// resolved from the rows) spends one unit of `budget`: when it runs out, *stop gets the next
-// tile and the state before it is returned (the lane chain goes on from there).
+// Without RECORD, the walk stops at the first round of the tile loop (a run of tiles whose
+// functions apply, or one tile resolved from the rows) at which `clk` finds it slower than the
+// lane chain: *stop gets that tile and the state before it is returned (the chain goes on from
+// there).
 template <int OP, bool SIGNED, bool RECORD>
 __device__ __forceinline__ unsigned long long walk_chunk_tiles(const RowArgs &args, int64_t nb, int T, const CanonWork &wk,
                                                                const WalkSmem *sm, int slot, int L, int k,
-                                                               unsigned long long s, int *budget = nullptr,
+                                                               unsigned long long s, WalkClock *clk = nullptr,
                                                                int *stop = nullptr) {
     const int lane = threadIdx.x & 31;
     unsigned long long *rec = RECORD ? wk.tstate + static_cast<int64_t>(L) * (T + 1) : nullptr;
     int tp = k * 32;
     const int end = min(T, tp + 32);
     while (tp < end) {
-        if (!RECORD && budget && --*budget < 0) {
+        if (!RECORD && stop && clk->slower(tp)) {
             *stop = tp;
             return s;
         }
@@ -937,14 +957,11 @@ __device__ __forceinline__ unsigned long long walk_lane(const RowArgs &args, int
                                                         const WalkSmem &sm, bool held, const int *gE, const TF *gD,
                                                         int L, unsigned long long s, int *stop) {
     const int lane = threadIdx.x;
-    // Rounds of the walk before the lane chain takes over (reductions only; each round costs a
-    // few microseconds of dependent loads): a growing sum's few dozen binade crossings stay in the
-    // walk; sums that wander (signed rows, magnitudes as large as the sum) go to the chain, which
-    // adds the rows at a steady rate.
-    int budget = WALK_BUDGET + T / 64;
+    // Reductions only: the walk goes on while it is faster than the lane chain (WalkClock).
+    WalkClock clk{clock64(), 0};
     int k = 0;  // next chunk
     while (k < C) {
-        if (!RECORD && --budget < 0) {
+        if (!RECORD && clk.slower(k * 32)) {
             *stop = k * 32;
             return s;
         }
@@ -974,7 +991,7 @@ __device__ __forceinline__ unsigned long long walk_lane(const RowArgs &args, int
         }
         // Chunk k, tile by tile.
         s = walk_chunk_tiles<OP, SIGNED, RECORD>(args, nb, T, wk, &sm, held ? sm.mixed_of[k] : -1, L, k, s,
-                                                 &budget, stop);
+                                                 &clk, RECORD ? nullptr : stop);
         if (*stop >= 0) return s;
         ++k;
     }
@@ -1100,12 +1117,16 @@ __global__ void canon_finish(CanonState *state, int tail_len) {
 // ---------------------------------------------------------------------------- the lane chain
 // Reductions whose lane sums keep leaving their binade (rows of both signs whose sum wanders
 // around zero, magnitudes as large as the sum) make the walk resolve most tiles from the rows,
-// one at a time. After WALK_BUDGET such tiles the walk stops and this kernel runs each stopped
-// lane to the end from its exact state. One warp per lane; each step takes 1024 of the lane's
-// rows, 32 consecutive ones per thread, prefetched CH_SLOTS - 1 steps ahead with cp.async into
-// the thread's own row of a shared ring (each thread reads only what it copied).
+// one at a time. When the walk falls behind this kernel's pace (WalkClock) it stops, and this
+// kernel runs each stopped lane to the end from its exact state. One warp per lane; each step
+// takes 32 * CH_ROWS of the lane's rows, CH_ROWS consecutive ones per thread, prefetched
+// CH_SLOTS - 1 steps ahead with cp.async into the thread's own row of a shared ring (each thread
+// reads only what it copied). The cost is one warp round per binade crossing, each with CH_ROWS
+// dependent IEEE adds (63 cycles each on GB300), so the rows per thread are few (measured at
+// 2^26 mean-centred rows: 8 rows 43 ms, 32 rows 92 ms; eight warps a lane, or 32 rows in four
+// 8-row fallback units, were slower again: every crossing costs a whole round).
 //
-// A thread's 32 rows act on the state's magnitude S (in ulps u = 2^(E-52) of its binade E) as
+// A thread's CH_ROWS rows act on the state's magnitude S (in ulps u = 2^(E-52) of its binade E) as
 // integer increments, the integer step of seg_tf: +-RNE(|x|/u) by the row's sign relative to
 // the state's, and for a row exactly halfway the even neighbour, which depends on the parity of
 // S at that row; so each thread keeps its increments for both parities of S before its rows,
@@ -1115,7 +1136,7 @@ __global__ void canon_finish(CanonState *state, int tail_len) {
 // exact sum of a downward step above 2^E); the first thread whose rows fail (a crossing, a row
 // not below 2^E or not finite) adds its rows with IEEE adds, the reference's own operation, and
 // the rest are computed again for the new state. So the result is the chain's, bit for bit.
-constexpr int CH_ROWS = 32;                  // lane rows per thread and step
+constexpr int CH_ROWS = 8;                   // lane rows per thread and step
 constexpr int CH_STEP = 32 * CH_ROWS;        // 16-row blocks per step
 constexpr int CH_SLOTS = 8;                  // steps in the shared ring
 constexpr int CH_PITCH = CH_ROWS + 1;        // doubles per thread row (odd: spreads the banks)
