@@ -550,12 +550,26 @@ def run_batched(ctx, count=4096, lo=10, hi=18, reps=2):
 # ---------------------------------------------------------------------------- served requests
 
 
-def run_served(ctx, rates=(100, 400, 1600, 6400), count=300, slots=4, budget=150e9, p99_bound_ms=100.0):
+# Two request mixes: the full range of sizes, where large argsorts and group-bys keep the device
+# busy whatever the scheduling, and small requests only, where per-statement launches and
+# synchronisations dominate the plain path.
+SERVED_MIXES = {
+    "mixed": {"n_lo": 1e3, "n_hi": 1e8, "rates": (500, 1000, 1500, 2000, 2500, 3000, 4000, 6400),
+              "p99_bound_ms": 100.0},
+    "small": {"n_lo": 1e3, "n_hi": 1e5, "rates": (1000, 2500, 5000, 10000, 20000, 40000),
+              "p99_bound_ms": 20.0},
+}
+
+
+def run_served(ctx, count=3000, slots=4, budget=150e9):
     """Served requests: Poisson arrivals of programs drawn from {dot, filter_gt + length, argsort,
-    group-by sum} with n = floor(10^U), U uniform in [3, 8], inputs generated on the device;
-    the plain GPU path (one request at a time, one synchronous call per statement) against the
-    server (continuous batching over `slots` streams, same-kind coalescing, admission by a
-    150 GB HBM budget). Latency is arrival to answer."""
+    group-by sum} with n = floor(10^U), U uniform over each mix's range, inputs generated on the
+    device; the plain GPU path (one request at a time, one synchronous call per statement)
+    against the server (continuous batching over `slots` streams, same-kind coalescing,
+    admission by a 150 GB HBM budget). Latency is arrival to answer. Every rate runs `count`
+    requests. gpu_busy is the time the streams spent on requests (CUDA events around every
+    request or group) over the wall time: for the plain path's one stream, the share of the run
+    the device was working for it."""
     import verkehrt_gb300 as vk
     from verkehrt_gb300 import serve
 
@@ -566,31 +580,45 @@ def run_served(ctx, rates=(100, 400, 1600, 6400), count=300, slots=4, budget=150
     # Warm-up of both paths on a short mix.
     serve.serve([ctx], serve.poisson_requests(16, 1e4, seed=1, n_hi=1e5), budget, batching=False)
     serve.serve(workers, serve.poisson_requests(16, 1e4, seed=1, n_hi=1e5), budget)
-    out = []
-    for rate in rates:
-        plain = serve.poisson_requests(count, rate, seed=rate)
-        wall_p = serve.serve([ctx], plain, budget, batching=False)
-        served = serve.poisson_requests(count, rate, seed=rate)
-        wall_s = serve.serve(workers, served, budget)
-        same = all(a.result == b.result for a, b in zip(plain, served) if a.kind in ("dot", "filter_len"))
-        out.append({"offered_req_per_s": rate, "plain": serve.summary(plain, wall_p),
-                    "served": serve.summary(served, wall_s), "scalar_results_equal": bool(same)})
-        del plain, served
+    result = {}
+    for mix, spec in SERVED_MIXES.items():
+        out = []
+        for rate in spec["rates"]:
+            row = {"offered_req_per_s": rate}
+            runs = {}
+            for mode, ws, batching in (("plain", [ctx], False), ("served", workers, True)):
+                reqs = serve.poisson_requests(count, rate, seed=rate, n_lo=spec["n_lo"], n_hi=spec["n_hi"])
+                dev = []
+                wall = serve.serve(ws, reqs, budget, batching=batching, device_ms=dev)
+                row[mode] = serve.summary(reqs, wall)
+                row[mode]["gpu_busy"] = round(sum(dev) / 1e3 / wall, 3) if wall > 0 else None
+                runs[mode] = reqs
+            row["scalar_results_equal"] = bool(all(a.result == b.result for a, b in zip(runs["plain"], runs["served"])
+                                                   if a.kind in ("dot", "filter_len")))
+            out.append(row)
+            del runs
+        bound = spec["p99_bound_ms"]
+
+        def knee(mode):
+            ok = [r for r in out if r[mode]["p99_ms"] <= bound]
+            return max(ok, key=lambda r: r[mode]["req_per_s"]) if ok else None
+
+        kp, ks = knee("plain"), knee("served")
+        at = {"p99_bound_ms": bound, "plain_req_per_s": kp["plain"]["req_per_s"] if kp else None,
+              "served_req_per_s": ks["served"]["req_per_s"] if ks else None,
+              "plain_gpu_busy_at_knee": kp["plain"]["gpu_busy"] if kp else None}
+        if at["plain_req_per_s"] and at["served_req_per_s"]:
+            at["ratio"] = round(at["served_req_per_s"] / at["plain_req_per_s"], 2)
+        result[mix] = {"at_equal_p99": at,
+                       "workload": "%d requests per rate and path, kinds uniform over dot_f64 / filter_gt_f64+length "
+                                   "/ argsort_i64 / group-by sum, n = floor(10^U) with U uniform in [%g, %g], seeded "
+                                   "inputs generated on the device; server: %d streams, requests up to 2^20 rows "
+                                   "coalesced per kind, 150 GB admission budget"
+                                   % (count, np.log10(spec["n_lo"]), np.log10(spec["n_hi"]), slots),
+                       "rates": out}
     for w in workers:
         w.close()
-
-    def best(mode):
-        ok = [r[mode]["req_per_s"] for r in out if r[mode]["p99_ms"] <= p99_bound_ms]
-        return max(ok) if ok else None
-
-    at_bound = {"p99_bound_ms": p99_bound_ms, "plain_req_per_s": best("plain"), "served_req_per_s": best("served")}
-    if at_bound["plain_req_per_s"] and at_bound["served_req_per_s"]:
-        at_bound["ratio"] = round(at_bound["served_req_per_s"] / at_bound["plain_req_per_s"], 2)
-    return {"at_equal_p99": at_bound,
-            "workload": "%d requests per rate, kinds uniform over dot_f64 / filter_gt_f64+length / "
-                        "argsort_i64 / group-by sum, n = floor(10^U) with U uniform in [3, 8], seeded "
-                        "inputs generated on the device; server: %d streams, requests up to 2^20 rows "
-                        "coalesced per kind, 150 GB admission budget" % (count, slots), "rates": out}
+    return result
 
 
 # ---------------------------------------------------------------------------- e2e
@@ -793,7 +821,8 @@ def main():
     ap.add_argument("--hard-sizes", default="26,28",
                     help="log2 sizes of the canonical sums on hard inputs (empty skips the section)")
     ap.add_argument("--batch-arrays", type=int, default=4096, help="0 skips the batched section")
-    ap.add_argument("--serve-requests", type=int, default=300, help="0 skips the served section")
+    ap.add_argument("--serve-requests", type=int, default=3000,
+                    help="requests per rate and path in the served section (0 skips it)")
     args = ap.parse_args()
     world, rank, local = dist_setup()
     n = args.n

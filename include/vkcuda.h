@@ -192,6 +192,18 @@ VKC_API uint64_t vkc_kernel_cost(int id);
  * arguments. On success `*out` holds the result value. */
 VKC_API vkc_status vkc_call(vkc_ctx *ctx, int id, const vkc_value *args, int nargs, vkc_value *out);
 
+/* vkc_call of a reduction without a host read, so it can be captured in a graph (below): the
+ * result's bits go to row `row` of the device array `out` (of the kernel's result type) in the
+ * order of ctx's stream, and the call only enqueues work. Argument errors are reported as by
+ * vkc_call; so is an empty input where the reduction's empty result is an error (reduce_min,
+ * reduce_max, argmin, argmax: src/kernels/scalar/reduce.rs:401-411, :454-467), decided from the
+ * arguments' lengths. A device-side timeout is reported by the next call that waits for the
+ * device. The scratch arena does not grow during a capture: a call whose scratch is larger
+ * than any earlier call's fails there with VKC_USAGE, so run the sequence once before
+ * capturing it. */
+VKC_API vkc_status vkc_call_into(vkc_ctx *ctx, int id, const vkc_value *args, int nargs, vkc_array *out,
+                                 int64_t row);
+
 /* Reducer (src/kernels.rs:48-63) for tile-fed callers, handed out by Dispatch::reducer
  * (src/kernels/dispatch.rs:156-163). Every update but the last has a multiple of 16 rows;
  * the canonical float state carries across updates, so any such split gives the bits of one
@@ -281,6 +293,14 @@ VKC_API vkc_status vkc_batch_dot_f64(vkc_ctx *ctx, vkc_batch *xs, vkc_batch *ys,
 VKC_API vkc_status vkc_batch_argsort_i64(vkc_ctx *ctx, vkc_batch *keys, const vkc_batch *outs,
                                          unsigned key_digits);
 
+/* The batch's arrays concatenated in the caller's order into a new array `rows` (the batch's
+ * element type), and, when `index` is not NULL, a new i64 array naming the array of every row
+ * (0 for the rows of the first array, and so on). A statement with no batched entry
+ * (group_id2, reduce_into, scan_by, ...) then runs once for the whole batch, keyed or
+ * segmented by that column. The call allocates its outputs, so it is not for use inside a
+ * capture. */
+VKC_API vkc_status vkc_batch_concat(vkc_ctx *ctx, vkc_batch *b, vkc_array **rows, vkc_array **index);
+
 /* Ingestion of the acceptance column files (src/columns.rs load_words, load_single_bytes): the
  * file is streamed through pinned buffers into a new device array. Words are 8-byte
  * little-endian rows read as `type` (VKC_I64 or VKC_U64), with bit 63 flipped when
@@ -293,8 +313,11 @@ VKC_API vkc_status vkc_load_column_bytes(vkc_ctx *ctx, const char *ends_path, co
                                          const char *column, vkc_array **out);
 
 /* A CUDA graph of the work the library enqueues on ctx's stream between vkc_graph_begin and
- * vkc_graph_end (stream capture; only enqueue-only entries, such as the batch entries above,
- * may run in between), replayed by vkc_graph_launch. */
+ * vkc_graph_end (stream capture), replayed by vkc_graph_launch. Only enqueue-only entries may
+ * run in between: vkc_call_into (reductions into a device array), vkc_elementwise_tile (into an
+ * existing array) and the batch entries above. A statement sequence of the reference's
+ * executor (src/exec.rs:162-231) whose results stay on the device is captured once and then
+ * replayed as one launch; the arrays it reads and writes are the ones it was captured with. */
 typedef struct vkc_graph vkc_graph;
 VKC_API vkc_status vkc_graph_begin(vkc_ctx *ctx);
 VKC_API vkc_status vkc_graph_end(vkc_ctx *ctx, vkc_graph **out);

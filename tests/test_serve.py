@@ -21,7 +21,7 @@ def test_scheduler_coalesces_the_head_kind():
     group, _ = s.take()
     assert [r.rid for r in group] == [1]  # argsort, alone in the queue
     group, _ = s.take()
-    assert [r.rid for r in group] == [3]  # group_sum has no batched entry
+    assert [r.rid for r in group] == [3]  # group_sum, alone in the queue
     group, _ = s.take()
     assert [r.rid for r in group] == [4]  # large: alone
 
@@ -99,3 +99,24 @@ def test_results_same_alone_and_in_the_mix(ctx):
     assert sum(r.batched for r in mix) > 0  # small requests of one kind were coalesced
     for a, m in zip(alone, mix):
         assert _value(a) == _value(m), (a.kind, a.n)
+
+
+@pytest.mark.gpu
+def test_batched_group_sums_equal_the_plain_ones(ctx):
+    # Requests of different sizes, one empty, coalesced through the concatenation.
+    reqs = [Request(i, "group_sum", n, 500 + 3 * i) for i, n in enumerate([1000, 1, 70_000, 0, 4097, 65_536 * 3])]
+    alone = [Request(r.rid, r.kind, r.n, r.seed) for r in reqs]
+    for r in alone:
+        serve.run_one(ctx, r)
+    serve.run_batch(ctx, reqs)
+    for a, b in zip(alone, reqs):
+        assert b.batched
+        assert np.array_equal(a.result.numpy(), b.result.numpy()), a.n
+    # The concatenation and its index column.
+    arrays = [ctx.upload(np.arange(k, dtype=np.int64) * 3) for k in (5, 0, 3)]
+    rows, index = ctx.batch_concat(ctx.batch(arrays))
+    assert list(rows.numpy()) == [0, 3, 6, 9, 12, 0, 3, 6]
+    assert list(index.numpy()) == [0, 0, 0, 0, 0, 2, 2, 2]
+    big = [ctx.upload(np.full(n, i, np.uint8)) for i, n in enumerate([20_000, 8192, 8193, 1])]
+    rows = ctx.batch_concat(ctx.batch(big), index=False)
+    assert np.array_equal(rows.numpy(), np.concatenate([np.full(n, i, np.uint8) for i, n in enumerate([20_000, 8192, 8193, 1])]))

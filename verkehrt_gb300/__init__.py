@@ -85,6 +85,8 @@ _SIGNATURES = {
     "vkc_kernel_cost": (ctypes.c_uint64, [ctypes.c_int]),
     "vkc_call": (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(_Value), ctypes.c_int,
                                 ctypes.POINTER(_Value)]),
+    "vkc_call_into": (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(_Value), ctypes.c_int, _P,
+                                     ctypes.c_int64]),
     "vkc_reducer_new": (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(_P)]),
     "vkc_reducer_update": (ctypes.c_int, [_P, ctypes.POINTER(_Value), ctypes.c_int]),
     "vkc_reducer_finish": (ctypes.c_int, [_P, ctypes.POINTER(_Scalar)]),
@@ -108,6 +110,7 @@ _SIGNATURES = {
     "vkc_batch_argsort_i64": (ctypes.c_int, [_P, _P, _P, ctypes.c_uint]),
     "vkc_batch_count_f64": (ctypes.c_int, [_P, _P, ctypes.c_int, ctypes.c_double, _P]),
     "vkc_batch_dot_f64": (ctypes.c_int, [_P, _P, _P, _P]),
+    "vkc_batch_concat": (ctypes.c_int, [_P, _P, ctypes.POINTER(_P), ctypes.POINTER(_P)]),
     "vkc_graph_begin": (ctypes.c_int, [_P]),
     "vkc_graph_end": (ctypes.c_int, [_P, ctypes.POINTER(_P)]),
     "vkc_graph_launch": (ctypes.c_int, [_P, _P]),
@@ -362,6 +365,13 @@ class Context:
             return Array(self, out.array)
         return _scalar_bits_value(out.scalar) if raw else _scalar_from_c(out.scalar)
 
+    def call_into(self, name, *args, out, row=0):
+        """A reduction whose result goes to row `row` of the device array `out`, enqueued only
+        (vkc_call_into), so it can be captured in a graph."""
+        vals = self._values(args)
+        self._check(_lib.vkc_call_into(self.handle, self.kernel_id(name), vals, len(args), out.handle,
+                                       int(row)))
+
     def reducer(self, name):
         return Reducer(self, name)
 
@@ -447,6 +457,15 @@ class Context:
     def batch_argsort(self, keys, outs, key_digits=0):
         """outs[i] = argsort_i64(keys[i]) for every array (enqueued)."""
         self._check(_lib.vkc_batch_argsort_i64(self.handle, keys.handle, outs.handle, key_digits))
+
+    def batch_concat(self, batch, index=True):
+        """The batch's arrays concatenated in order, and (index=True) the i64 column naming each
+        row's array: (rows, index) or rows alone."""
+        r, ix = _P(), _P()
+        self._check(_lib.vkc_batch_concat(self.handle, batch.handle, ctypes.byref(r),
+                                          ctypes.byref(ix) if index else None))
+        rows = Array(self, r.value)
+        return (rows, Array(self, ix.value)) if index else rows
 
     def graph_begin(self):
         self._check(_lib.vkc_graph_begin(self.handle))

@@ -22,6 +22,7 @@
 #include <algorithm>
 #include <cstring>
 #include <numeric>
+#include <type_traits>
 #include <vector>
 
 #include "lookback.cuh"
@@ -51,6 +52,7 @@ struct vkc_batch {
     vkc::DeviceMem table;             // BSeg[n] on the device, largest first
     vkc::DeviceMem bases;             // int64 first rows [n + 1], index order (for the argsort)
     vkc::DeviceMem outs;              // argsort output pointers [n], index order
+    vkc::DeviceMem chunks;            // int64 [n + 1]: first concat chunk of each array, table order
     // Argsort scratch, made on first use.
     std::vector<vkc_array *> scratch;
     unsigned long long *img[2] = {nullptr, nullptr};
@@ -279,6 +281,39 @@ __global__ void __launch_bounds__(256) batch_split_kernel(const int64_t *__restr
     }
 }
 
+// ------------------------------------------------------------------ concatenation
+
+// Batched statements whose kernel has no batched form (group_id, reduce_into, scans) run once
+// over the concatenation of the batch's arrays, with an index column naming each row's array:
+// a segmented statement keyed by that column gives every array's own result. One block per
+// 8192-row chunk of one array (chunks[] gives each array's first chunk, table order).
+constexpr int BC_ROWS = 8192;
+
+template <int W>
+__global__ void __launch_bounds__(256) batch_concat_kernel(const BSeg *__restrict__ segs, int nseg,
+                                                           const int64_t *__restrict__ chunks, void *rows,
+                                                           long long *index) {
+    using U = typename std::conditional<W == 8, unsigned long long,
+                                        typename std::conditional<W == 4, unsigned, unsigned char>::type>::type;
+    const int64_t c = blockIdx.x;
+    int lo = 0, hi = nseg - 1;  // the last array whose first chunk is <= c (no chunk: empty array)
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (chunks[mid] <= c) lo = mid;
+        else hi = mid - 1;
+    }
+    const BSeg seg = segs[lo];
+    const int64_t r0 = (c - chunks[lo]) * BC_ROWS;
+    const int64_t r1 = min(seg.n, r0 + BC_ROWS);
+    const U *src = static_cast<const U *>(seg.ptr);
+    U *dst = static_cast<U *>(rows) + seg.base;
+#pragma unroll 8
+    for (int64_t r = r0 + threadIdx.x; r < r1; r += 256) {
+        dst[r] = __ldcs(src + r);
+        if (index) index[seg.base + r] = seg.index;
+    }
+}
+
 static bool capturing(vkc_ctx *ctx) {
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
     if (cudaStreamIsCapturing(ctx->stream, &cs) != cudaSuccess) {
@@ -330,8 +365,11 @@ extern "C" VKC_API vkc_status vkc_batch_new(vkc_ctx *ctx, int n, vkc_array *cons
         VKC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
         return VKC_OK;
     };
+    std::vector<int64_t> chunk(static_cast<size_t>(n) + 1, 0);
+    for (int i = 0; i < n; ++i) chunk[i + 1] = chunk[i] + (b->host[i].n + BC_ROWS - 1) / BC_ROWS;
     vkc_status st = upload(b->table, b->host.data(), sizeof(BSeg) * b->host.size());
     if (!st) st = upload(b->bases, base.data(), sizeof(int64_t) * base.size());
+    if (!st) st = upload(b->chunks, chunk.data(), sizeof(int64_t) * chunk.size());
     if (st) {
         vkc_batch_free(b);
         return st;
@@ -488,6 +526,41 @@ extern "C" VKC_API vkc_status vkc_batch_argsort_i64(vkc_ctx *ctx, vkc_batch *key
     batch_split_kernel<<<grid, 256, 0, ctx->stream>>>(bases, n, pos2[w2], static_cast<long long *const *>(keys->outs.ptr),
                                                      total);
     return launched(ctx, "batch_split");
+}
+
+extern "C" VKC_API vkc_status vkc_batch_concat(vkc_ctx *ctx, vkc_batch *b, vkc_array **rows, vkc_array **index) {
+    if (!ctx || !b || !rows) return VKC_USAGE;
+    *rows = nullptr;
+    if (index) *index = nullptr;
+    vkc_status st;
+    vkc_array *r = nullptr, *ix = nullptr;
+    if ((st = new_array(ctx, b->type, b->total, false, &r))) return st;
+    if (index && (st = new_array(ctx, VKC_I64, b->total, false, &ix))) {
+        vkc_array_release(r);
+        return st;
+    }
+    const int n = static_cast<int>(b->host.size());
+    int64_t nchunks = 0;
+    for (const BSeg &g : b->host) nchunks += (g.n + BC_ROWS - 1) / BC_ROWS;
+    if (nchunks > 0) {
+        const auto *tab = static_cast<const BSeg *>(b->table.ptr);
+        const auto *ch = static_cast<const int64_t *>(b->chunks.ptr);
+        long long *ip = ix ? static_cast<long long *>(ix->data()) : nullptr;
+        const dim3 grid(static_cast<unsigned>(nchunks));
+        switch (type_width(b->type)) {
+        case 8: batch_concat_kernel<8><<<grid, 256, 0, ctx->stream>>>(tab, n, ch, r->data(), ip); break;
+        case 4: batch_concat_kernel<4><<<grid, 256, 0, ctx->stream>>>(tab, n, ch, r->data(), ip); break;
+        default: batch_concat_kernel<1><<<grid, 256, 0, ctx->stream>>>(tab, n, ch, r->data(), ip); break;
+        }
+        if ((st = launched(ctx, "batch_concat"))) {
+            vkc_array_release(r);
+            vkc_array_release(ix);
+            return st;
+        }
+    }
+    *rows = r;
+    if (index) *index = ix;
+    return VKC_OK;
 }
 
 // ------------------------------------------------------------------ CUDA graphs

@@ -1460,6 +1460,11 @@ struct CanonReducer : DevReducer {
         out->type = VKC_F64;
         return download(ctx, &out->bits, 8, offsetof(CanonState, result));
     }
+    vkc_status finish_into(vkc_ctx *ctx, void *dst) override {
+        canon_finish<<<1, 1, 0, ctx->stream>>>(static_cast<CanonState *>(state), tail_len);
+        vkc_status st = launched(ctx, "canon_finish");
+        return st ? st : copy_out(ctx, dst, 8, offsetof(CanonState, result));
+    }
 };
 
 // ---------------------------------------------------------------------------- float scans

@@ -303,10 +303,7 @@ struct FamReducer : DevReducer {
     using Launch = void (*)(vkc_ctx *, const RowArgs &, int64_t, int, void *, u64, u64 *);
     Launch launch = nullptr;
 
-    vkc_status init(vkc_ctx *ctx, u64 id0, u64 id1) {
-        u64 h[3] = {id0, id1, 0};
-        return upload(ctx, h, sizeof h);
-    }
+    vkc_status init(vkc_ctx *ctx, u64 id0, u64 id1) { return fill(ctx, 3, id0, id1, 0); }
     vkc_status update(vkc_ctx *ctx, const Arg *args, int nargs) override {
         vkc_status st;
         if (nargs != nargs_want) return fail(ctx, VKC_RUNTIME, arity_error(nargs_want, nargs));
@@ -341,6 +338,11 @@ struct FamReducer : DevReducer {
         if (empty_error && !(arg ? h[2] : h[1])) return fail(ctx, VKC_RUNTIME, std::string(what) + " of an empty array");
         *out_s = arg ? scalar_i64(static_cast<int64_t>(h[1])) : word_scalar(out, h[0]);
         return VKC_OK;
+    }
+    vkc_status finish_into(vkc_ctx *ctx, void *dst) override {
+        if (empty_error && base == 0) return fail(ctx, VKC_RUNTIME, std::string(what) + " of an empty array");
+        // Words are little-endian: the result type's bytes are the word's low bytes.
+        return fold < 0 ? copy_out(ctx, dst, 8, 8) : copy_out(ctx, dst, static_cast<size_t>(width_of(out)));
     }
 };
 
@@ -501,6 +503,11 @@ struct ChainReducer : DevReducer {
         *out = word_scalar(in, r);
         return VKC_OK;
     }
+    vkc_status finish_into(vkc_ctx *ctx, void *dst) override {
+        fin(ctx, static_cast<u64 *>(state), tail_len);
+        vkc_status st = launched(ctx, "family_chain_finish");
+        return st ? st : copy_out(ctx, dst, static_cast<size_t>(width_of(in)), 32 * 8);
+    }
 };
 
 template <vkc_type T, int ROW, bool MUL>
@@ -524,10 +531,9 @@ template <vkc_type T, int ROW, bool MUL, int NARGS> ReducerImpl *make_chain(vkc_
     r->cmp = cmp;
     r->launch = launch_chain<T, ROW, MUL>;
     r->fin = finish_chain<T, MUL>;
-    u64 h[33];
     const u64 one = T == VKC_F64 ? 0x3ff0000000000000ull : 0x3f800000ull;
-    for (int j = 0; j < 33; ++j) h[j] = MUL ? one : 0ull;
-    if (r->upload(ctx, h, sizeof h)) {
+    const u64 v = MUL ? one : 0ull;
+    if (r->fill(ctx, 33, v, v, v, v)) {
         delete r;
         return nullptr;
     }

@@ -153,6 +153,7 @@ struct CountReducer : DevReducer {
         *out = scalar_i64(static_cast<int64_t>(v));
         return VKC_OK;
     }
+    vkc_status finish_into(vkc_ctx *ctx, void *dst) override { return copy_out(ctx, dst, 8); }
 };
 
 // ------------------------------------------------------------------ extremes
@@ -332,14 +333,18 @@ __global__ void __launch_bounds__(256) extreme_kernel(const long long *__restric
     }
 }
 
+// finish on the device: the result's bits as ExtremeReducer::finish makes them (rows seen).
+static __global__ void ext_result_kernel(const ExtState *s, bool arg, bool f64, unsigned long long *dst) {
+    if (arg) *dst = s->nan_idx != ~0ull ? s->nan_idx : s->idx;
+    else if (f64) *dst = s->nan_idx != ~0ull ? 0x7ff8000000000000ull : bits_of_key(s->key);
+    else *dst = static_cast<unsigned long long>(s->key);
+}
+
 struct ExtremeReducer : DevReducer {
     bool max, arg;
     vkc_type type;
     unsigned long long consumed = 0;
-    vkc_status init(vkc_ctx *ctx) {
-        ExtState s{0, ~0ull, ~0ull, 0};
-        return upload(ctx, &s, sizeof s);
-    }
+    vkc_status init(vkc_ctx *ctx) { return fill(ctx, 4, 0, ~0ull, ~0ull, 0); }  // ExtState{0, ~0, ~0, 0}
     vkc_status update(vkc_ctx *ctx, const Arg *args, int nargs) override {
         vkc_status st;
         if (nargs != 1) return fail(ctx, VKC_RUNTIME, arity_error(1, nargs));
@@ -391,6 +396,15 @@ struct ExtremeReducer : DevReducer {
             *out = scalar_i64(s.key);
         }
         return VKC_OK;
+    }
+    vkc_status finish_into(vkc_ctx *ctx, void *dst) override {
+        if (consumed == 0) {
+            std::string what = arg ? (max ? "argmax" : "argmin") : (max ? "reduce_max" : "reduce_min");
+            return fail(ctx, VKC_RUNTIME, what + " of an empty array");
+        }
+        ext_result_kernel<<<1, 1, 0, ctx->stream>>>(static_cast<const ExtState *>(state), arg, type == VKC_F64,
+                                                     static_cast<unsigned long long *>(dst));
+        return launched(ctx, "extreme_result");
     }
 };
 
@@ -456,6 +470,7 @@ struct IntSumReducer : DevReducer {
         *out = scalar_i64(static_cast<int64_t>(v));
         return VKC_OK;
     }
+    vkc_status finish_into(vkc_ctx *ctx, void *dst) override { return copy_out(ctx, dst, 8); }
 };
 
 // ------------------------------------------------------------------ registration

@@ -42,6 +42,11 @@ struct ReducerImpl {
     virtual ~ReducerImpl() {}
     virtual vkc_status update(vkc_ctx *ctx, const Arg *args, int nargs) = 0;
     virtual vkc_status finish(vkc_ctx *ctx, vkc_scalar *out) = 0;
+    // finish without a host read: the result's bits (the output type's width) go to the
+    // device address dst, in the order of the context's stream. The one error a finish can
+    // report, an empty input where that is an error, is decided by the rows the reducer was
+    // given, which the host knows.
+    virtual vkc_status finish_into(vkc_ctx *ctx, void *dst);
 };
 
 // Scanner (src/kernels.rs:65-88): carried state on the device.

@@ -140,9 +140,15 @@ vkc_status cuda_fail(vkc_ctx *ctx, cudaError_t e, const char *what) {
     return fail(ctx, VKC_DEVICE, buf);
 }
 
+// Arenas are freed and made again when they grow, which a captured graph could not replay: a
+// capture fails instead (growing needs a call of the same size outside the capture first).
+static const char *const GROW_IN_CAPTURE =
+    "the scratch arena would grow during a capture: make the call once before capturing";
+
 vkc_status scratch(vkc_ctx *ctx, size_t bytes, void **out) {
     bytes = (bytes + 255) & ~size_t(255);
     if (bytes > ctx->scratch.bytes) {
+        if (stream_capturing(ctx->stream)) return fail(ctx, VKC_USAGE, GROW_IN_CAPTURE);
         if (ctx->scratch.ptr) VKC_CUDA(ctx, cudaFreeAsync(ctx->scratch.ptr, ctx->stream));
         ctx->scratch.ptr = nullptr;
         ctx->scratch.bytes = 0;
@@ -157,6 +163,7 @@ vkc_status scratch(vkc_ctx *ctx, size_t bytes, void **out) {
 vkc_status flag_arena(vkc_ctx *ctx, size_t count, unsigned **out) {
     size_t bytes = (count * sizeof(unsigned) + 255) & ~size_t(255);
     if (bytes > ctx->flags.bytes) {
+        if (stream_capturing(ctx->stream)) return fail(ctx, VKC_USAGE, GROW_IN_CAPTURE);
         if (ctx->flags.ptr) VKC_CUDA(ctx, cudaFreeAsync(ctx->flags.ptr, ctx->stream));
         ctx->flags.ptr = nullptr;
         ctx->flags.bytes = 0;
@@ -899,9 +906,41 @@ vkc_status vkc_reducer_update(vkc_reducer *r, const vkc_value *args, int nargs) 
     return r->impl->update(r->ctx, call.data(), nargs);
 }
 
+vkc_status ReducerImpl::finish_into(vkc_ctx *ctx, void *) {
+    return fail(ctx, VKC_USAGE, "this reduction cannot run enqueue-only");
+}
+
 vkc_status vkc_reducer_finish(vkc_reducer *r, vkc_scalar *out) {
     vkc_status st = r->impl->finish(r->ctx, out);
     delete r->impl;
+    delete r;
+    return st;
+}
+
+vkc_status vkc_call_into(vkc_ctx *ctx, int id, const vkc_value *args, int nargs, vkc_array *out,
+                         int64_t row) {
+    const KernelDef *d = def_of(id);
+    if (!d) return fail(ctx, VKC_USAGE, "unknown kernel id " + std::to_string(id));
+    if (d->cls != VKC_REDUCTION) return fail(ctx, VKC_USAGE, d->name + " is not a reduction");
+    if (!out) return fail(ctx, VKC_USAGE, "null array handle");
+    if (out->type != d->out_type)
+        return fail(ctx, VKC_USAGE, d->name + " produces " + type_name(d->out_type) + ", got a " +
+                                        type_name(out->type) + " destination");
+    if (row < 0 || row >= out->len)
+        return fail(ctx, VKC_USAGE, "destination row " + std::to_string(row) + " out of range for length " +
+                                        std::to_string(out->len));
+    std::vector<Arg> call;
+    int64_t rows = -1;
+    vkc_status st = prepare(ctx, *d, args, nargs, &call, &rows);
+    if (st) return st;
+    if (rows < 0) return fail(ctx, VKC_USAGE, "a reduction needs an array operand");
+    await_values(ctx, args, nargs);
+    await_write(ctx, out);
+    ReducerImpl *r = d->red(ctx);
+    if (!r) return ctx->err.empty() ? fail(ctx, VKC_ALLOC, "cannot allocate a reducer") : VKC_ALLOC;
+    // As vkc_call: one update with all rows, none on empty input.
+    if (rows > 0) st = r->update(ctx, call.data(), nargs);
+    if (!st) st = r->finish_into(ctx, static_cast<char *>(out->data()) + row * type_width(out->type));
     delete r;
     return st;
 }

@@ -21,6 +21,11 @@ group ids), so tests compare the two exactly.
 Program kinds (the served mix): dot (x = rand_f64(n, s); y = rand_f64(n, s + 1); dot_f64),
 filter_len (length(filter_gt_f64(rand_f64(n, s), 0.9))), argsort (argsort_i64(rand_i64(n, s))),
 group_sum (group-by sum of i64 values over keys below 2^16: group_id_i64, reduce_into_add_i64).
+
+group_sum has no batched entry of its own: a group of them runs as one statement over the
+concatenated keys (vkc_batch_concat), keyed by (request, key) with group_id2, so each request's
+groups get consecutive ids in its own first-occurrence order, offset by the groups of the
+requests before it; one reduce_into sums them all and each request's result is its slice.
 """
 
 import collections
@@ -30,7 +35,7 @@ import time
 import numpy as np
 
 KINDS = ("dot", "filter_len", "argsort", "group_sum")
-BATCHED = ("dot", "filter_len", "argsort")  # kinds with a batched entry
+BATCHED = KINDS  # kinds that coalesce (group_sum through a concatenation)
 THRESHOLD = 0.9
 KEY_MASK = (1 << 16) - 1
 
@@ -114,12 +119,31 @@ def run_batch(ctx, reqs):
         ctx.batch_count(ctx.batch(xs), "gt", THRESHOLD, counts)
         for r, v in zip(reqs, counts.numpy()):
             r.result = int(v)
-    else:
+    elif kind == "argsort":
         ks = [ctx.call("rand_i64", r.n, r.seed) for r in reqs]
         outs = [ctx.new_array("i64", r.n) for r in reqs]
         ctx.batch_argsort(ctx.batch(ks), ctx.batch(outs))
         for r, o in zip(reqs, outs):
             r.result = o
+    else:
+        keys = [ctx.call("and_i64", ctx.call("rand_i64", r.n, r.seed), KEY_MASK) for r in reqs]
+        vals = [ctx.call("and_i64", ctx.call("rand_i64", r.n, r.seed + 1), KEY_MASK) for r in reqs]
+        kcat, index = ctx.batch_concat(ctx.batch(keys))
+        vcat = ctx.batch_concat(ctx.batch(vals), index=False)
+        g = ctx.call("group_id2_i64_i64", index, kcat)
+        nb = ctx.call("reduce_max_i64", g) + 1 if len(g) else 0
+        sums = ctx.call("reduce_into_add_i64", g, vcat, nb)
+        # The first group id of every request with rows (ids are consecutive per request).
+        starts = np.cumsum([0] + [r.n for r in reqs[:-1]])
+        live = [i for i, r in enumerate(reqs) if r.n > 0]
+        first = ctx.call("gather_i64", g, ctx.upload(starts[live].astype(np.int64))).numpy() if live else []
+        bounds = dict(zip(live, first))
+        ends = list(first[1:]) + [nb]
+        for j, i in enumerate(live):
+            reqs[i].result = sums.slice(int(bounds[i]), int(ends[j]))
+        for r in reqs:
+            if r.n == 0:
+                r.result = sums.slice(0, 0)
     ctx.synchronize()
     for r in reqs:
         r.batched = True
@@ -197,9 +221,12 @@ class Scheduler:
             self.cv.notify_all()
 
 
-def serve(contexts, requests, budget=150e9, small_rows=1 << 20, batching=True):
+def serve(contexts, requests, budget=150e9, small_rows=1 << 20, batching=True, device_ms=None):
     """Answers `requests` (sorted by arrival), released at their arrival times from now on, with
-    one worker per context. Returns the wall time from the first arrival to the last answer."""
+    one worker per context. Returns the wall time from the first arrival to the last answer.
+    With a list `device_ms`, every group appends the time its context's stream took for it
+    (CUDA events around the group): the sum over the wall time is the share of the run that the
+    device spent on requests."""
     sched = Scheduler(budget, small_rows, batching=batching)
     t0 = time.perf_counter()
     errors = []
@@ -215,10 +242,14 @@ def serve(contexts, requests, budget=150e9, small_rows=1 << 20, batching=True):
                 for r in group:
                     r.start = now
                 try:
+                    if device_ms is not None:
+                        ctx.timer_start()
                     if len(group) > 1:
                         run_batch(ctx, group)
                     else:
                         run_one(ctx, group[0])
+                    if device_ms is not None:
+                        device_ms.append(ctx.timer_stop())
                 finally:
                     done = time.perf_counter() - t0
                     for r in group:
