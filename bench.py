@@ -450,6 +450,59 @@ def run_canon_adversarial(ctx, sizes, stream, steps=3, cpu_n=1 << 24, no_cpu=Fal
                         % (cpu_n.bit_length() - 1), **out}
 
 
+def run_regions(ctx, n, stream, steps=3):
+    """Regions as one pass (vkc_region_eval, vkc_region_reduce) against their kernels run whole
+    (Tiling::Off), at n rows of rand_f64 inputs: x * y + z, sum(x * y) (the dot pattern) beside
+    dot_f64 itself, count(x * y > 0.25) and min(x * y + z). Every region value is checked
+    against whole evaluation's."""
+    import torch
+    import verkehrt_gb300 as vk
+
+    k = vk.region_kernel
+    x, y, z = (ctx.call("rand_f64", n, 71 + i) for i in range(3))
+
+    def med(fn):
+        fn()
+        ts = []
+        with torch.cuda.stream(stream):
+            for _ in range(steps):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                fn()
+                e1.record(stream)
+                stream.synchronize()
+                ts.append(e0.elapsed_time(e1))
+        return sorted(ts)[len(ts) // 2]
+
+    fma = [("mul_f64", [0, 1]), ("add_f64", [k(0), 2])]
+    out = {}
+
+    def case(name, region, whole, nbytes):
+        r = region()
+        w = whole()
+        if isinstance(r, vk.Array):
+            ok = bool(np.array_equal(r.numpy().view(np.uint64), w.numpy().view(np.uint64)))
+        else:
+            ok = r == w
+        del r, w
+        tr, tw = med(region), med(whole)
+        out[name] = {"region_ms": round(tr, 3), "whole_ms": round(tw, 3), "speedup": round(tw / tr, 2),
+                     "region_GB/s": round(nbytes / (tr / 1e3) / 1e9, 1), "equal_to_whole": ok}
+
+    case("x*y+z", lambda: ctx.region(fma, [x, y, z]),
+         lambda: ctx.call("add_f64", ctx.call("mul_f64", x, y), z), 32 * n)
+    case("sum(x*y)", lambda: ctx.region_reduce("reduce_add_f64", [k(0)], fma[:1], [x, y], raw=True),
+         lambda: ctx.call("reduce_add_f64", ctx.call("mul_f64", x, y), raw=True), 16 * n)
+    out["sum(x*y)"]["dot_f64_ms"] = round(med(lambda: ctx.call("dot_f64", x, y)), 3)
+    case("count(x*y>0.25)", lambda: ctx.region_reduce("count", [k(1)], [fma[0], ("gt_f64", [k(0), 2])], [x, y, 0.25]),
+         lambda: ctx.call("count", ctx.call("gt_f64", ctx.call("mul_f64", x, y), 0.25)), 16 * n)
+    case("min(x*y+z)", lambda: ctx.region_reduce("reduce_min_f64", [k(1)], fma, [x, y, z], raw=True),
+         lambda: ctx.call("reduce_min_f64", ctx.call("add_f64", ctx.call("mul_f64", x, y), z), raw=True), 24 * n)
+    del x, y, z
+    return {"workload": "n=2^%d rand_f64 columns; region_GB/s counts each input read once and the result "
+                        "written once" % (n.bit_length() - 1), **out}
+
+
 def cpu_sum_rates(n):
     """Rows/s (in G) of the oracle port's canonical sum on the hard inputs, one thread."""
     import oracle
@@ -818,6 +871,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--sort-n", type=int, default=1 << 27, help="0 skips the argsort/group-by section")
     ap.add_argument("--scan-n", type=int, default=1 << 28, help="0 skips the float scan section")
+    ap.add_argument("--region-n", type=int, default=1 << 28, help="0 skips the region section")
     ap.add_argument("--hard-sizes", default="26,28",
                     help="log2 sizes of the canonical sums on hard inputs (empty skips the section)")
     ap.add_argument("--batch-arrays", type=int, default=4096, help="0 skips the batched section")
@@ -942,6 +996,7 @@ def main():
         c3 = run_sort_groupby(ctx, args.sort_n, stream, steps=3, warmup=1,
                               digests=digests.get("sort_groupby"))
     c6 = run_f64_scans(ctx, args.scan_n, stream) if args.scan_n > 0 else None
+    c8 = run_regions(ctx, args.region_n, stream) if args.region_n > 0 else None
     hard = [1 << int(v) for v in args.hard_sizes.split(",") if v.strip()]
     c7 = run_canon_adversarial(ctx, hard, stream, no_cpu=args.no_cpu or rank != 0) if hard else None
     c4 = run_batched(ctx, args.batch_arrays) if args.batch_arrays > 0 else None
@@ -971,6 +1026,7 @@ def main():
             "kernels": kernels,
             "sort_groupby": c3,
             "f64_scans": c6,
+            "regions": c8,
             "canon_adversarial": c7,
             "batched": c4,
             "batched_wide": c4w,

@@ -256,6 +256,36 @@ VKC_API vkc_status vkc_elementwise_tile(vkc_ctx *ctx, int id, const vkc_value *a
 VKC_API vkc_status vkc_scan_add_i64_noalloc(int device, const int64_t *in, int64_t *out, int64_t n,
                                             void *stream, char *err, size_t err_len);
 
+/* ------------------------------------------------------------------ regions */
+
+/* A region of the reference's executor (src/exec/region.rs:22-50): elementwise kernels with
+ * array outputs in post-order, each reading region inputs or the outputs of earlier kernels.
+ * A source is an input position i >= 0, or -1 - k for the output of kernel k. */
+typedef struct vkc_region_kernel {
+    int32_t kernel; /* kernel id */
+    int32_t nargs;
+    int32_t args[3];
+} vkc_region_kernel;
+
+/* The value of the region's last kernel, with the values and errors of evaluating every kernel
+ * whole (Tiling::Off). It runs as one pass over the rows with every intermediate value on chip;
+ * a region whose whole evaluation could fail (an operand of the wrong type or kind, arrays of
+ * different lengths, a zero divisor), or that holds more than 12 kernels, 8 inputs or 16 of
+ * both, runs kernel by kernel instead, as the reference falls back to whole evaluation when a
+ * tiled run fails (src/exec/region.rs:137-159). Replaces the tiled run of eval_region. */
+VKC_API vkc_status vkc_region_eval(vkc_ctx *ctx, const vkc_region_kernel *kernels, int nkernels,
+                                   const vkc_value *inputs, int ninputs, vkc_value *out);
+
+/* A fused region (src/exec/region/fused.rs): reduction `root` over arguments `root_args`
+ * (sources as above) whose region arguments are the kernels' outputs. When the region matches
+ * a fused kernel's pattern of the registry (src/kernels/scalar/fused.rs:286-379: dot_T,
+ * sumsq_T, count_<cmp>_T, condsum_<cmp>_T) that kernel runs over the pattern's operands;
+ * otherwise each region argument is evaluated by vkc_region_eval and the root is called once.
+ * Values and errors are those of whole evaluation. Replaces eval_fused. */
+VKC_API vkc_status vkc_region_reduce(vkc_ctx *ctx, int root, const int32_t *root_args, int nroot,
+                                     const vkc_region_kernel *kernels, int nkernels,
+                                     const vkc_value *inputs, int ninputs, vkc_value *out);
+
 /* ------------------------------------------------------------------ batches and graphs */
 
 /* A batch: many arrays of one element type that run the same planned statement. The

@@ -103,6 +103,11 @@ _SIGNATURES = {
                                             _P]),
     "vkc_scan_add_i64_noalloc": (ctypes.c_int, [ctypes.c_int, _P, _P, ctypes.c_int64, _P,
                                                 ctypes.c_char_p, ctypes.c_size_t]),
+    "vkc_region_eval": (ctypes.c_int, [_P, ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(_Value), ctypes.c_int,
+                                       ctypes.POINTER(_Value)]),
+    "vkc_region_reduce": (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(ctypes.c_int32), ctypes.c_int,
+                                         ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(_Value), ctypes.c_int,
+                                         ctypes.POINTER(_Value)]),
     "vkc_batch_new": (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(_P), ctypes.POINTER(_P)]),
     "vkc_batch_free": (None, [_P]),
     "vkc_batch_len": (ctypes.c_int, [_P]),
@@ -116,6 +121,17 @@ _SIGNATURES = {
     "vkc_graph_launch": (ctypes.c_int, [_P, _P]),
     "vkc_graph_free": (None, [_P]),
 }
+
+
+
+class _RegionKernel(ctypes.Structure):
+    _fields_ = [("kernel", ctypes.c_int32), ("nargs", ctypes.c_int32), ("args", ctypes.c_int32 * 3)]
+
+
+def region_kernel(k):
+    """The source naming region kernel k's output."""
+    return -1 - k
+
 
 _lib = None
 
@@ -371,6 +387,38 @@ class Context:
         vals = self._values(args)
         self._check(_lib.vkc_call_into(self.handle, self.kernel_id(name), vals, len(args), out.handle,
                                        int(row)))
+
+    def _region_kernels(self, kernels):
+        ks = (_RegionKernel * max(1, len(kernels)))()
+        for i, (name, srcs) in enumerate(kernels):
+            ks[i].kernel = self.kernel_id(name)
+            ks[i].nargs = len(srcs)
+            for j, a in enumerate(srcs):
+                ks[i].args[j] = a
+        return ks
+
+    def region(self, kernels, inputs, raw=False):
+        """A region (vkc_region_eval): `kernels` in post-order as (name, sources), a source being an
+        input position i >= 0 or region_kernel(k) for kernel k's output; the last kernel's value."""
+        vals = self._values(inputs)
+        out = _Value()
+        self._check(_lib.vkc_region_eval(self.handle, ctypes.cast(self._region_kernels(kernels), ctypes.c_void_p),
+                                         len(kernels), vals, len(inputs), ctypes.byref(out)))
+        if out.kind == 0:
+            return Array(self, out.array)
+        return _scalar_bits_value(out.scalar) if raw else _scalar_from_c(out.scalar)
+
+    def region_reduce(self, root, root_args, kernels, inputs, raw=False):
+        """A fused region (vkc_region_reduce): reduction `root` over `root_args` (sources)."""
+        vals = self._values(inputs)
+        ra = (ctypes.c_int32 * max(1, len(root_args)))(*root_args)
+        out = _Value()
+        self._check(_lib.vkc_region_reduce(self.handle, self.kernel_id(root), ra, len(root_args),
+                                           ctypes.cast(self._region_kernels(kernels), ctypes.c_void_p), len(kernels),
+                                           vals, len(inputs), ctypes.byref(out)))
+        if out.kind == 0:
+            return Array(self, out.array)
+        return _scalar_bits_value(out.scalar) if raw else _scalar_from_c(out.scalar)
 
     def reducer(self, name):
         return Reducer(self, name)

@@ -19,6 +19,7 @@
 #include <type_traits>
 
 #include "reduce_common.h"
+#include "region.h"
 
 namespace vkc {
 
@@ -80,36 +81,38 @@ __device__ __forceinline__ double ew_sqrt(double a) { return __dsqrt_rn(a); }
 __device__ __forceinline__ float ew_sqrt(float a) { return __fsqrt_rn(a); }
 
 // Operation tags: f(a, b) or f(a) on storage type T, giving U.
-#define EW_BIN(NAME, EXPR)                                                                     \
+#define EW_BIN(NAME, EXPR, CODE)                                                               \
     struct NAME {                                                                              \
+        static constexpr int code = CODE;                                                      \
         template <class T, class U> __device__ static U f(T a, T b) { return static_cast<U>(EXPR); } \
     };
-EW_BIN(OpAdd, ew_add(a, b))
-EW_BIN(OpSub, ew_sub(a, b))
-EW_BIN(OpMul, ew_mul(a, b))
-EW_BIN(OpMin, ew_min(a, b))
-EW_BIN(OpMax, ew_max(a, b))
-EW_BIN(OpLt, a < b)
-EW_BIN(OpLe, a <= b)
-EW_BIN(OpGt, a > b)
-EW_BIN(OpGe, a >= b)
-EW_BIN(OpEq, a == b)
-EW_BIN(OpNe, a != b)
-EW_BIN(OpAnd, a & b)
-EW_BIN(OpOr, a | b)
-EW_BIN(OpXor, a ^ b)
-EW_BIN(OpDiv, ew_div(a, b))
+EW_BIN(OpAdd, ew_add(a, b), EF_ADD)
+EW_BIN(OpSub, ew_sub(a, b), EF_SUB)
+EW_BIN(OpMul, ew_mul(a, b), EF_MUL)
+EW_BIN(OpMin, ew_min(a, b), EF_MIN)
+EW_BIN(OpMax, ew_max(a, b), EF_MAX)
+EW_BIN(OpLt, a < b, EF_LT)
+EW_BIN(OpLe, a <= b, EF_LE)
+EW_BIN(OpGt, a > b, EF_GT)
+EW_BIN(OpGe, a >= b, EF_GE)
+EW_BIN(OpEq, a == b, EF_EQ)
+EW_BIN(OpNe, a != b, EF_NE)
+EW_BIN(OpAnd, a & b, EF_AND)
+EW_BIN(OpOr, a | b, EF_OR)
+EW_BIN(OpXor, a ^ b, EF_XOR)
+EW_BIN(OpDiv, ew_div(a, b), EF_DIV)
 #undef EW_BIN
 
-#define EW_UN(NAME, EXPR)                                                                      \
+#define EW_UN(NAME, EXPR, CODE)                                                                \
     struct NAME {                                                                              \
+        static constexpr int code = CODE;                                                      \
         template <class T, class U> __device__ static U f(T a) { return static_cast<U>(EXPR); } \
     };
-EW_UN(OpNeg, ew_neg(a))
-EW_UN(OpAbs, ew_abs(a))
-EW_UN(OpSqrt, ew_sqrt(a))
-EW_UN(OpBitNot, ~a)
-EW_UN(OpBoolNot, a ^ 1u)
+EW_UN(OpNeg, ew_neg(a), EF_NEG)
+EW_UN(OpAbs, ew_abs(a), EF_ABS)
+EW_UN(OpSqrt, ew_sqrt(a), EF_SQRT)
+EW_UN(OpBitNot, ~a, EF_NOT)
+EW_UN(OpBoolNot, a ^ 1u, EF_BNOT)
 #undef EW_UN
 
 // Rust `as` (elementwise.rs:572-613).
@@ -134,6 +137,7 @@ template <class S, class D> struct CastAs {
     }
 };
 template <class S, class D> struct OpCast {
+    static constexpr int code = EF_CAST;
     template <class T, class U> __device__ static U f(T a) { return CastAs<S, D>::f(a); }
 };
 
@@ -162,12 +166,6 @@ __global__ void __launch_bounds__(256) select_kernel(Opnd m, Opnd a, Opnd b, T *
 
 // The divider of an unsigned divisor d of B bits (elementwise.rs:627-666): with l = ceil(log2 d),
 // m = floor(2^B (2^l - d) / d) + 1, t = mulhi(m, n), q = (t + ((n - t) >> min(l, 1))) >> max(l - 1, 0).
-struct Divider {
-    unsigned long long m;
-    int sh1, sh2;
-    unsigned long long dneg;  // signed types: all ones when the divisor is negative
-};
-
 __device__ __forceinline__ unsigned long long div_u(unsigned long long x, const Divider &v, int bits) {
     unsigned long long t;
     if (bits == 64) t = __umul64hi(v.m, x);
@@ -175,24 +173,26 @@ __device__ __forceinline__ unsigned long long div_u(unsigned long long x, const 
     return (t + ((x - t) >> v.sh1)) >> v.sh2;
 }
 
-template <class T>
-__global__ void __launch_bounds__(256) div_const_kernel(Opnd a, Divider v, T *__restrict__ out, int64_t n) {
+template <class T> __device__ __forceinline__ T ew_div_const(T x, const Divider &v) {
     using UT = Wide<T>;
     constexpr int B = 8 * sizeof(T);
-    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
-    for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride) {
-        const T x = get<T>(a, i);
-        if constexpr (std::is_signed<T>::value) {
-            // Magnitudes, then the sign: MIN's magnitude 2^(B-1) divided by 1 reads back as MIN.
-            const UT xneg = static_cast<UT>(x < 0 ? ~UT(0) : UT(0));
-            const UT mag = x < 0 ? static_cast<UT>(UT(0) - static_cast<UT>(x)) : static_cast<UT>(x);
-            const UT q = static_cast<UT>(div_u(mag, v, B));
-            const UT mask = static_cast<UT>(xneg ^ static_cast<UT>(v.dneg));
-            out[i] = static_cast<T>(static_cast<UT>((q ^ mask) - mask));
-        } else {
-            out[i] = static_cast<T>(div_u(static_cast<unsigned long long>(x), v, B));
-        }
+    if constexpr (std::is_signed<T>::value) {
+        // Magnitudes, then the sign: MIN's magnitude 2^(B-1) divided by 1 reads back as MIN.
+        const UT xneg = static_cast<UT>(x < 0 ? ~UT(0) : UT(0));
+        const UT mag = x < 0 ? static_cast<UT>(UT(0) - static_cast<UT>(x)) : static_cast<UT>(x);
+        const UT q = static_cast<UT>(div_u(mag, v, B));
+        const UT mask = static_cast<UT>(xneg ^ static_cast<UT>(v.dneg));
+        return static_cast<T>(static_cast<UT>((q ^ mask) - mask));
+    } else {
+        return static_cast<T>(div_u(static_cast<unsigned long long>(x), v, B));
     }
+}
+
+template <class T>
+__global__ void __launch_bounds__(256) div_const_kernel(Opnd a, Divider v, T *__restrict__ out, int64_t n) {
+    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride)
+        out[i] = ew_div_const<T>(get<T>(a, i), v);
 }
 
 // ------------------------------------------------------------------ entries
@@ -245,18 +245,34 @@ static Divider make_divider(unsigned long long d, int bits) {
     return v;
 }
 
+// The divider of the divisor d of type T (a signed divisor by its magnitude and sign).
+template <class T> static Divider typed_divider(T d) {
+    using UT = Wide<T>;
+    const bool neg = std::is_signed<T>::value && d < 0;
+    const UT mag = neg ? static_cast<UT>(UT(0) - static_cast<UT>(d)) : static_cast<UT>(d);
+    Divider v = make_divider(static_cast<unsigned long long>(mag), 8 * sizeof(T));
+    v.dneg = neg ? ~0ull : 0ull;
+    return v;
+}
+
+bool make_ew_divider(int ty, unsigned long long bits, Divider *out) {
+    switch (ty) {
+    case ET_I64: if (static_cast<long long>(bits) == 0) return false; *out = typed_divider<long long>(static_cast<long long>(bits)); return true;
+    case ET_U64: if (bits == 0) return false; *out = typed_divider<unsigned long long>(bits); return true;
+    case ET_I32: if (static_cast<int>(static_cast<unsigned>(bits)) == 0) return false; *out = typed_divider<int>(static_cast<int>(static_cast<unsigned>(bits))); return true;
+    case ET_U8: if ((bits & 0xff) == 0) return false; *out = typed_divider<unsigned char>(static_cast<unsigned char>(bits)); return true;
+    default: return false;
+    }
+}
+
 template <class T>
 static vkc_status run_div_const(vkc_ctx *ctx, const Arg *args, int nargs, int64_t n, vkc_array *out) {
     if (nargs != 2) return fail(ctx, VKC_RUNTIME, arity_error(2, nargs));
     T d;
     memcpy(&d, &args[1].s.bits, sizeof(T));
     if (d == 0) return fail(ctx, VKC_RUNTIME, "div_const: division by zero");  // elementwise.rs:725-727
-    using UT = Wide<T>;
-    const bool neg = std::is_signed<T>::value && d < 0;
-    const UT mag = neg ? static_cast<UT>(UT(0) - static_cast<UT>(d)) : static_cast<UT>(d);
-    Divider v = make_divider(static_cast<unsigned long long>(mag), 8 * sizeof(T));
-    v.dneg = neg ? ~0ull : 0ull;
-    div_const_kernel<T><<<ew_grid(ctx, n), 256, 0, ctx->stream>>>(opnd(args[0]), v, static_cast<T *>(out->data()), n);
+    div_const_kernel<T><<<ew_grid(ctx, n), 256, 0, ctx->stream>>>(opnd(args[0]), typed_divider<T>(d),
+                                                                   static_cast<T *>(out->data()), n);
     return launched(ctx, "div_const");
 }
 
@@ -286,6 +302,150 @@ static vkc_status iota(vkc_ctx *ctx, const vkc_value *args, int nargs, vkc_value
     return VKC_OK;
 }
 
+// ------------------------------------------------------------------ regions
+//
+// A region's rows pass through its kernels in post-order on chip. Values are 64-bit words
+// holding a type's bytes in their low bytes (bool as u8 0/1); every kernel applies the same row
+// operation as its own entry above, so a region gives the bits of its kernels run one by one.
+
+template <class T> __device__ __forceinline__ T from_word(unsigned long long w) {
+    T v;
+    memcpy(&v, &w, sizeof(T));
+    return v;
+}
+template <class T> __device__ __forceinline__ unsigned long long to_word(T v) {
+    unsigned long long w = 0;
+    memcpy(&w, &v, sizeof(T));
+    return w;
+}
+
+template <class S> __device__ __forceinline__ unsigned long long rg_cast(int dst, S x) {
+    switch (dst) {
+    case ET_F64: return to_word(CastAs<S, double>::f(x));
+    case ET_F32: return to_word(CastAs<S, float>::f(x));
+    case ET_I64: return to_word(CastAs<S, long long>::f(x));
+    case ET_U64: return to_word(CastAs<S, unsigned long long>::f(x));
+    case ET_I32: return to_word(CastAs<S, int>::f(x));
+    default: return to_word(CastAs<S, unsigned char>::f(x));
+    }
+}
+
+template <class T>
+__device__ __forceinline__ unsigned long long rg_typed(const RgOp &o, unsigned long long a, unsigned long long b,
+                                                    unsigned long long c) {
+    constexpr bool FL = std::is_floating_point<T>::value;
+    const T x = from_word<T>(a), y = from_word<T>(b);
+    switch (o.fn) {
+    case EF_ADD: return to_word(ew_add(x, y));
+    case EF_SUB: return to_word(ew_sub(x, y));
+    case EF_MUL: return to_word(ew_mul(x, y));
+    case EF_MIN: return to_word(ew_min(x, y));
+    case EF_MAX: return to_word(ew_max(x, y));
+    case EF_LT: return x < y;
+    case EF_LE: return x <= y;
+    case EF_GT: return x > y;
+    case EF_GE: return x >= y;
+    case EF_EQ: return x == y;
+    case EF_NE: return x != y;
+    case EF_SELECT: return (a & 0xffu) ? b : c;  // select(mask, a, b): the mask is the first operand
+    case EF_CAST: return rg_cast<T>(o.dst, x);
+    case EF_NEG: if constexpr (FL || std::is_signed<T>::value) return to_word(ew_neg(x)); break;
+    case EF_ABS: if constexpr (FL || std::is_signed<T>::value) return to_word(ew_abs(x)); break;
+    case EF_DIV: if constexpr (FL) return to_word(ew_div(x, y)); break;
+    case EF_SQRT: if constexpr (FL) return to_word(ew_sqrt(x)); break;
+    case EF_AND: if constexpr (!FL) return to_word(static_cast<T>(x & y)); break;
+    case EF_OR: if constexpr (!FL) return to_word(static_cast<T>(x | y)); break;
+    case EF_XOR: if constexpr (!FL) return to_word(static_cast<T>(x ^ y)); break;
+    case EF_NOT: if constexpr (!FL) return to_word(static_cast<T>(~x)); break;
+    case EF_BNOT: return a ^ 1u;
+    case EF_DIVC: if constexpr (!FL) return to_word(ew_div_const<T>(x, o.dv)); break;
+    default: break;
+    }
+    return 0;
+}
+
+__device__ __forceinline__ unsigned long long rg_eval(const RgOp &o, unsigned long long a, unsigned long long b,
+                                                      unsigned long long c) {
+    switch (o.ty) {
+    case ET_F64: return rg_typed<double>(o, a, b, c);
+    case ET_F32: return rg_typed<float>(o, a, b, c);
+    case ET_I64: return rg_typed<long long>(o, a, b, c);
+    case ET_U64: return rg_typed<unsigned long long>(o, a, b, c);
+    case ET_I32: return rg_typed<int>(o, a, b, c);
+    default: return rg_typed<unsigned char>(o, a, b, c);
+    }
+}
+
+__device__ __forceinline__ unsigned long long rg_load(const RgIn &in, int64_t i) {
+    switch (in.width) {
+    case 8: return __ldcs(static_cast<const unsigned long long *>(in.p) + i);
+    case 4: return __ldcs(static_cast<const unsigned *>(in.p) + i);
+    default: return __ldcs(static_cast<const unsigned char *>(in.p) + i);
+    }
+}
+
+constexpr int RG_THREADS = 128, RG_ROWS = 4, RG_BLOCK_ROWS = RG_THREADS * RG_ROWS;
+
+// Slots live in shared memory, slot j of local row l at s_w[j * RG_BLOCK_ROWS + l]; a thread
+// touches only its own rows (t, t + 128, ...), so no barrier is needed. Each block takes
+// RG_BLOCK_ROWS rows per step: the inputs' loads of a step are in flight together.
+__global__ void __launch_bounds__(RG_THREADS) region_kernel(const RegionProg P, int64_t n, void *__restrict__ out) {
+    extern __shared__ unsigned long long s_w[];
+    const int t = threadIdx.x;
+    for (int64_t b0 = static_cast<int64_t>(blockIdx.x) * RG_BLOCK_ROWS; b0 < n;
+         b0 += static_cast<int64_t>(gridDim.x) * RG_BLOCK_ROWS) {
+        for (int j = 0; j < P.nin; ++j) {
+            const RgIn in = P.in[j];
+            unsigned long long v[RG_ROWS];
+#pragma unroll
+            for (int r = 0; r < RG_ROWS; ++r) {
+                const int64_t i = b0 + t + r * RG_THREADS;
+                v[r] = !in.arr ? in.s : (i < n ? rg_load(in, i) : 0ull);
+            }
+#pragma unroll
+            for (int r = 0; r < RG_ROWS; ++r) s_w[j * RG_BLOCK_ROWS + t + r * RG_THREADS] = v[r];
+        }
+        for (int k = 0; k < P.nk; ++k) {
+            const RgOp o = P.op[k];
+            unsigned long long *dst = s_w + (P.nin + k) * RG_BLOCK_ROWS + t;
+            const unsigned long long *a0 = s_w + o.a[0] * RG_BLOCK_ROWS + t;
+            const unsigned long long *a1 = s_w + o.a[1] * RG_BLOCK_ROWS + t;
+            const unsigned long long *a2 = s_w + o.a[2] * RG_BLOCK_ROWS + t;
+#pragma unroll
+            for (int r = 0; r < RG_ROWS; ++r)
+                dst[r * RG_THREADS] = rg_eval(o, a0[r * RG_THREADS], a1[r * RG_THREADS], a2[r * RG_THREADS]);
+        }
+        const unsigned long long *res = s_w + (P.nin + P.nk - 1) * RG_BLOCK_ROWS + t;
+#pragma unroll
+        for (int r = 0; r < RG_ROWS; ++r) {
+            const int64_t i = b0 + t + r * RG_THREADS;
+            if (i >= n) break;
+            const unsigned long long w = res[r * RG_THREADS];
+            switch (P.out_width) {
+            case 8: static_cast<unsigned long long *>(out)[i] = w; break;
+            case 4: static_cast<unsigned *>(out)[i] = static_cast<unsigned>(w); break;
+            default: static_cast<unsigned char *>(out)[i] = static_cast<unsigned char>(w); break;
+            }
+        }
+    }
+}
+
+vkc_status launch_region(vkc_ctx *ctx, const RegionProg &p, int64_t n, void *out) {
+    if (n <= 0) return VKC_OK;
+    const size_t smem = static_cast<size_t>(p.nin + p.nk) * RG_BLOCK_ROWS * sizeof(unsigned long long);
+    static std::atomic<unsigned long long> configured{0};
+    once_per_device(configured, ctx->device, [] {
+        cudaFuncSetAttribute(region_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             static_cast<int>(RG_MAX_SLOTS * RG_BLOCK_ROWS * sizeof(unsigned long long)));
+    });
+    // Resident blocks: as many as the slots' shared memory allows, at most 16 a multiprocessor.
+    const int per_sm = std::max(1, std::min(16, static_cast<int>((200u << 10) / smem)));
+    const int64_t blocks = (n + RG_BLOCK_ROWS - 1) / RG_BLOCK_ROWS;
+    const int grid = static_cast<int>(std::min<int64_t>(blocks, static_cast<int64_t>(ctx->sms) * per_sm));
+    region_kernel<<<grid, RG_THREADS, smem, ctx->stream>>>(p, n, out);
+    return launched(ctx, "region");
+}
+
 // ------------------------------------------------------------------ registration
 
 template <class T> struct TypeOf;
@@ -298,12 +458,34 @@ template <> struct TypeOf<unsigned char> { static constexpr vkc_type v = VKC_U8;
 
 static std::string tname(vkc_type t) { return type_name(t); }
 
+template <class T> constexpr int tcode() {
+    return std::is_same<T, double>::value               ? ET_F64
+           : std::is_same<T, float>::value              ? ET_F32
+           : std::is_same<T, long long>::value          ? ET_I64
+           : std::is_same<T, unsigned long long>::value ? ET_U64
+           : std::is_same<T, int>::value                ? ET_I32
+                                                        : ET_U8;
+}
+
+// An elementwise entry with its row operation for the region evaluator.
+struct EwEntry {
+    ElemFn f;
+    int fn, ty, dst;
+};
+template <class T, class U, class F> static EwEntry bin() { return {run_bin<T, U, F>, F::code, tcode<T>(), tcode<U>()}; }
+template <class T, class U, class F> static EwEntry un() { return {run_un<T, U, F>, F::code, tcode<T>(), tcode<U>()}; }
+template <class T> static EwEntry sel() { return {run_select<T>, EF_SELECT, tcode<T>(), tcode<T>()}; }
+template <class T> static EwEntry divc() { return {run_div_const<T>, EF_DIVC, tcode<T>(), tcode<T>()}; }
+
 // KernelDef of an elementwise entry; cost = the row bytes (elementwise.rs:272).
-static void add(std::vector<KernelDef> &t, const std::string &name, std::vector<InSpec> in, vkc_type out, ElemFn f) {
+static void add(std::vector<KernelDef> &t, const std::string &name, std::vector<InSpec> in, vkc_type out, EwEntry e) {
     uint64_t cost = static_cast<uint64_t>(type_width(out));
     for (const InSpec &s : in) cost += static_cast<uint64_t>(type_width(s.type));
     KernelDef d{name, VKC_ELEMENTWISE, std::move(in), true, out, cost};
-    d.elem = f;
+    d.elem = e.f;
+    d.ew_fn = e.fn;
+    d.ew_ty = e.ty;
+    d.ew_dst = e.dst;
     t.push_back(d);
 }
 
@@ -312,38 +494,38 @@ template <class T> static void reg_num(std::vector<KernelDef> &t) {
     const vkc_type ty = TypeOf<T>::v;
     const std::string n = tname(ty);
     const InSpec e{IN_EITHER, ty};
-    add(t, "add_" + n, {e, e}, ty, run_bin<T, T, OpAdd>);
-    add(t, "sub_" + n, {e, e}, ty, run_bin<T, T, OpSub>);
-    add(t, "mul_" + n, {e, e}, ty, run_bin<T, T, OpMul>);
-    add(t, "min_" + n, {e, e}, ty, run_bin<T, T, OpMin>);
-    add(t, "max_" + n, {e, e}, ty, run_bin<T, T, OpMax>);
-    add(t, "lt_" + n, {e, e}, VKC_BOOL, run_bin<T, unsigned char, OpLt>);
-    add(t, "le_" + n, {e, e}, VKC_BOOL, run_bin<T, unsigned char, OpLe>);
-    add(t, "gt_" + n, {e, e}, VKC_BOOL, run_bin<T, unsigned char, OpGt>);
-    add(t, "ge_" + n, {e, e}, VKC_BOOL, run_bin<T, unsigned char, OpGe>);
+    add(t, "add_" + n, {e, e}, ty, bin<T, T, OpAdd>());
+    add(t, "sub_" + n, {e, e}, ty, bin<T, T, OpSub>());
+    add(t, "mul_" + n, {e, e}, ty, bin<T, T, OpMul>());
+    add(t, "min_" + n, {e, e}, ty, bin<T, T, OpMin>());
+    add(t, "max_" + n, {e, e}, ty, bin<T, T, OpMax>());
+    add(t, "lt_" + n, {e, e}, VKC_BOOL, bin<T, unsigned char, OpLt>());
+    add(t, "le_" + n, {e, e}, VKC_BOOL, bin<T, unsigned char, OpLe>());
+    add(t, "gt_" + n, {e, e}, VKC_BOOL, bin<T, unsigned char, OpGt>());
+    add(t, "ge_" + n, {e, e}, VKC_BOOL, bin<T, unsigned char, OpGe>());
 }
 
 // register_signed (:771-775) and register_float (:777-781).
 template <class T> static void reg_signed(std::vector<KernelDef> &t) {
     const vkc_type ty = TypeOf<T>::v;
     const InSpec e{IN_EITHER, ty};
-    add(t, "neg_" + tname(ty), {e}, ty, run_un<T, T, OpNeg>);
-    add(t, "abs_" + tname(ty), {e}, ty, run_un<T, T, OpAbs>);
+    add(t, "neg_" + tname(ty), {e}, ty, un<T, T, OpNeg>());
+    add(t, "abs_" + tname(ty), {e}, ty, un<T, T, OpAbs>());
 }
 template <class T> static void reg_float(std::vector<KernelDef> &t) {
     const vkc_type ty = TypeOf<T>::v;
     const InSpec e{IN_EITHER, ty};
-    add(t, "div_" + tname(ty), {e, e}, ty, run_bin<T, T, OpDiv>);
-    add(t, "sqrt_" + tname(ty), {e}, ty, run_un<T, T, OpSqrt>);
+    add(t, "div_" + tname(ty), {e, e}, ty, bin<T, T, OpDiv>());
+    add(t, "sqrt_" + tname(ty), {e}, ty, un<T, T, OpSqrt>());
 }
 
 // register_any (:789-804): eq, ne, select; `ty` is bool for the bool instantiation on u8.
 template <class T> static void reg_any(std::vector<KernelDef> &t, vkc_type ty) {
     const std::string n = tname(ty);
     const InSpec e{IN_EITHER, ty}, b{IN_EITHER, VKC_BOOL};
-    add(t, "eq_" + n, {e, e}, VKC_BOOL, run_bin<T, unsigned char, OpEq>);
-    add(t, "ne_" + n, {e, e}, VKC_BOOL, run_bin<T, unsigned char, OpNe>);
-    add(t, "select_" + n, {b, e, e}, ty, run_select<T>);
+    add(t, "eq_" + n, {e, e}, VKC_BOOL, bin<T, unsigned char, OpEq>());
+    add(t, "ne_" + n, {e, e}, VKC_BOOL, bin<T, unsigned char, OpNe>());
+    add(t, "select_" + n, {b, e, e}, ty, sel<T>());
 }
 
 // register_bits (:806-813).
@@ -351,28 +533,28 @@ template <class T> static void reg_bits(std::vector<KernelDef> &t) {
     const vkc_type ty = TypeOf<T>::v;
     const std::string n = tname(ty);
     const InSpec e{IN_EITHER, ty};
-    add(t, "and_" + n, {e, e}, ty, run_bin<T, T, OpAnd>);
-    add(t, "or_" + n, {e, e}, ty, run_bin<T, T, OpOr>);
-    add(t, "xor_" + n, {e, e}, ty, run_bin<T, T, OpXor>);
-    add(t, "not_" + n, {e}, ty, run_un<T, T, OpBitNot>);
+    add(t, "and_" + n, {e, e}, ty, bin<T, T, OpAnd>());
+    add(t, "or_" + n, {e, e}, ty, bin<T, T, OpOr>());
+    add(t, "xor_" + n, {e, e}, ty, bin<T, T, OpXor>());
+    add(t, "not_" + n, {e}, ty, un<T, T, OpBitNot>());
 }
 
 // register_div_const (:739-755): the divisor is a scalar.
 template <class T> static void reg_div_const(std::vector<KernelDef> &t) {
     const vkc_type ty = TypeOf<T>::v;
-    add(t, "div_const_" + tname(ty), {InSpec{IN_EITHER, ty}, InSpec{IN_SCALAR, ty}}, ty, run_div_const<T>);
+    add(t, "div_const_" + tname(ty), {InSpec{IN_EITHER, ty}, InSpec{IN_SCALAR, ty}}, ty, divc<T>());
 }
 
 // register_casts (:858-871): one source type to every numeric array type.
 template <class S> static void reg_casts_from(std::vector<KernelDef> &t, vkc_type src) {
     const std::string s = "cast_" + tname(src) + "_";
     const InSpec e{IN_EITHER, src};
-    add(t, s + "f64", {e}, VKC_F64, run_un<S, double, OpCast<S, double>>);
-    add(t, s + "f32", {e}, VKC_F32, run_un<S, float, OpCast<S, float>>);
-    add(t, s + "i64", {e}, VKC_I64, run_un<S, long long, OpCast<S, long long>>);
-    add(t, s + "u64", {e}, VKC_U64, run_un<S, unsigned long long, OpCast<S, unsigned long long>>);
-    add(t, s + "i32", {e}, VKC_I32, run_un<S, int, OpCast<S, int>>);
-    add(t, s + "u8", {e}, VKC_U8, run_un<S, unsigned char, OpCast<S, unsigned char>>);
+    add(t, s + "f64", {e}, VKC_F64, un<S, double, OpCast<S, double>>());
+    add(t, s + "f32", {e}, VKC_F32, un<S, float, OpCast<S, float>>());
+    add(t, s + "i64", {e}, VKC_I64, un<S, long long, OpCast<S, long long>>());
+    add(t, s + "u64", {e}, VKC_U64, un<S, unsigned long long, OpCast<S, unsigned long long>>());
+    add(t, s + "i32", {e}, VKC_I32, un<S, int, OpCast<S, int>>());
+    add(t, s + "u8", {e}, VKC_U8, un<S, unsigned char, OpCast<S, unsigned char>>());
 }
 
 void register_elementwise(std::vector<KernelDef> &t) {
@@ -405,10 +587,10 @@ void register_elementwise(std::vector<KernelDef> &t) {
     reg_bits<unsigned char>(t);
     // register_bool (:815-823): on the 0/1 storage.
     const InSpec be{IN_EITHER, VKC_BOOL};
-    add(t, "and_bool", {be, be}, VKC_BOOL, run_bin<unsigned char, unsigned char, OpAnd>);
-    add(t, "or_bool", {be, be}, VKC_BOOL, run_bin<unsigned char, unsigned char, OpOr>);
-    add(t, "xor_bool", {be, be}, VKC_BOOL, run_bin<unsigned char, unsigned char, OpXor>);
-    add(t, "not_bool", {be}, VKC_BOOL, run_un<unsigned char, unsigned char, OpBoolNot>);
+    add(t, "and_bool", {be, be}, VKC_BOOL, bin<unsigned char, unsigned char, OpAnd>());
+    add(t, "or_bool", {be, be}, VKC_BOOL, bin<unsigned char, unsigned char, OpOr>());
+    add(t, "xor_bool", {be, be}, VKC_BOOL, bin<unsigned char, unsigned char, OpXor>());
+    add(t, "not_bool", {be}, VKC_BOOL, un<unsigned char, unsigned char, OpBoolNot>());
     reg_casts_from<double>(t, VKC_F64);
     reg_casts_from<float>(t, VKC_F32);
     reg_casts_from<long long>(t, VKC_I64);

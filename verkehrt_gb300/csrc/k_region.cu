@@ -1,0 +1,299 @@
+// Regions on the device: the reference's executor runs a region (a subtree of at least two
+// elementwise kernels with array outputs, src/exec/region.rs:22-50) tile by tile, and a fused
+// region (a reduction over such kernels, src/exec/region/fused.rs:1-3) feeds the tiles to the
+// root's accumulator. Here a region is one pass over the rows (region_kernel, every
+// intermediate value on chip), with the values and errors of whole evaluation (Tiling::Off):
+//  * a region that could fail, or could fail differently when fused (an operand of the wrong
+//    type or kind, arrays of different lengths, a kernel without an array operand, a zero
+//    divisor, more kernels or inputs than the evaluator holds), runs whole instead, kernel by
+//    kernel in post-order, which raises the error whole evaluation raises, as the reference
+//    does when its tiled run fails (region.rs:137-159);
+//  * a fused root whose region matches one of the registry's fused patterns
+//    (src/kernels/scalar/fused.rs:286-379: dot_T, sumsq_T, count_<cmp>_T, condsum_<cmp>_T are
+//    declared there as those compositions) runs as that fused reduction over the pattern's
+//    operands; any other root is called once over its arguments, each region argument
+//    evaluated by one pass.
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "region.h"
+#include "registry.h"
+
+namespace vkc {
+
+namespace {
+
+struct Src {
+    bool kernel;  // the output of region kernel i, else region input i
+    int i;
+};
+Src src_of(int32_t a) { return a >= 0 ? Src{false, a} : Src{true, -1 - a}; }
+
+// Sources in range and in post-order, arities that the struct can hold.
+vkc_status check_shape(vkc_ctx *ctx, const vkc_region_kernel *ks, int nk, int nin) {
+    if (nk < 1) return fail(ctx, VKC_USAGE, "a region has at least one kernel");
+    if (nin < 0) return fail(ctx, VKC_USAGE, "negative input count");
+    for (int k = 0; k < nk; ++k) {
+        if (ks[k].nargs < 0 || ks[k].nargs > 3)
+            return fail(ctx, VKC_USAGE, "region kernel " + std::to_string(k) + ": 0 to 3 arguments");
+        for (int j = 0; j < ks[k].nargs; ++j) {
+            const Src s = src_of(ks[k].args[j]);
+            if (s.kernel ? s.i >= k : s.i >= nin)
+                return fail(ctx, VKC_USAGE, "region kernel " + std::to_string(k) + ": argument " + std::to_string(j) +
+                                                " names no earlier kernel or input");
+        }
+    }
+    return VKC_OK;
+}
+
+// The one-pass program of a region whose whole evaluation cannot fail, or false.
+bool plan_region(const vkc_region_kernel *ks, int nk, const vkc_value *in, int nin, RegionProg *p, int64_t *n,
+                 vkc_type *out_type) {
+    if (nk > RG_MAX_K || nin > RG_MAX_IN || nk + nin > RG_MAX_SLOTS) return false;
+    int64_t len = -1;
+    memset(p, 0, sizeof *p);
+    p->nin = nin;
+    p->nk = nk;
+    for (int j = 0; j < nin; ++j) {
+        const vkc_value &v = in[j];
+        if (v.kind == VKC_VALUE_ARRAY) {
+            if (!v.array) return false;
+            if (len >= 0 && v.array->len != len) return false;  // a length mismatch somewhere
+            len = v.array->len;
+            p->in[j] = RgIn{v.array->data(), 0, type_width(v.array->type), 1};
+        } else if (v.kind == VKC_VALUE_SCALAR) {
+            p->in[j] = RgIn{nullptr, v.scalar.bits, type_width(v.scalar.type), 0};
+        } else {
+            return false;
+        }
+    }
+    if (len < 0) return false;
+    std::vector<vkc_type> ty(static_cast<size_t>(nk));
+    for (int k = 0; k < nk; ++k) {
+        const char *name = vkc_kernel_name(ks[k].kernel);
+        const KernelDef *d = name ? kernel_def(name) : nullptr;
+        if (!d || d->cls != VKC_ELEMENTWISE || d->ew_fn < 0) return false;
+        if (static_cast<int>(d->inputs.size()) != ks[k].nargs) return false;
+        bool any_array = false;
+        RgOp &o = p->op[k];
+        o.fn = static_cast<unsigned char>(d->ew_fn);
+        o.ty = static_cast<unsigned char>(d->ew_ty);
+        o.dst = static_cast<unsigned char>(d->ew_dst);
+        for (int j = 0; j < ks[k].nargs; ++j) {
+            const Src s = src_of(ks[k].args[j]);
+            const bool arr = s.kernel || in[s.i].kind == VKC_VALUE_ARRAY;
+            const vkc_type t = s.kernel ? ty[s.i] : (arr ? in[s.i].array->type : in[s.i].scalar.type);
+            const InSpec &spec = d->inputs[static_cast<size_t>(j)];
+            if (t != spec.type || (spec.kind == IN_SCALAR && arr) || (spec.kind == IN_ARRAY && !arr)) return false;
+            any_array |= arr;
+            o.a[j] = static_cast<unsigned char>(s.kernel ? nin + s.i : s.i);
+        }
+        if (!any_array) return false;  // "an array kernel needs an array operand"
+        if (d->ew_fn == EF_DIVC && !make_ew_divider(d->ew_ty, in[src_of(ks[k].args[1]).i].scalar.bits, &o.dv))
+            return false;  // division by zero
+        ty[static_cast<size_t>(k)] = d->out_type;
+    }
+    *out_type = ty.back();
+    p->out_width = type_width(*out_type);
+    *n = len;
+    return true;
+}
+
+void release_values(std::vector<vkc_value> &vals) {
+    for (vkc_value &v : vals)
+        if (v.kind == VKC_VALUE_ARRAY && v.array) vkc_array_release(v.array);
+    vals.clear();
+}
+
+// Whole evaluation: every kernel by vkc_call in post-order.
+vkc_status eval_whole(vkc_ctx *ctx, const vkc_region_kernel *ks, int nk, const vkc_value *in, vkc_value *out) {
+    std::vector<vkc_value> vals;
+    for (int k = 0; k < nk; ++k) {
+        vkc_value args[3];
+        for (int j = 0; j < ks[k].nargs; ++j) {
+            const Src s = src_of(ks[k].args[j]);
+            args[j] = s.kernel ? vals[static_cast<size_t>(s.i)] : in[s.i];
+        }
+        vkc_value v;
+        const vkc_status st = vkc_call(ctx, ks[k].kernel, args, ks[k].nargs, &v);
+        if (st) {
+            release_values(vals);
+            return st;
+        }
+        vals.push_back(v);
+    }
+    *out = vals.back();
+    vals.pop_back();
+    release_values(vals);
+    return VKC_OK;
+}
+
+vkc_status eval_region(vkc_ctx *ctx, const vkc_region_kernel *ks, int nk, const vkc_value *in, int nin,
+                       vkc_value *out) {
+    memset(out, 0, sizeof *out);
+    vkc_status st = check_shape(ctx, ks, nk, nin);
+    if (st) return st;
+    RegionProg p;
+    int64_t n;
+    vkc_type t;
+    if (!plan_region(ks, nk, in, nin, &p, &n, &t)) return eval_whole(ctx, ks, nk, in, out);
+    await_values(ctx, in, nin);
+    vkc_array *o;
+    if ((st = new_array(ctx, t, n, false, &o))) return st;
+    if ((st = launch_region(ctx, p, n, o->data()))) {
+        vkc_array_release(o);
+        return st;
+    }
+    out->kind = VKC_VALUE_ARRAY;
+    out->array = o;
+    return VKC_OK;
+}
+
+// The subtree of kernel k, renumbered in post-order, with the region's inputs.
+std::vector<vkc_region_kernel> subtree(const vkc_region_kernel *ks, int k) {
+    std::vector<char> seen(static_cast<size_t>(k) + 1, 0);
+    // Kernels are in post-order, so the subtree is the marked kernels in index order.
+    seen[static_cast<size_t>(k)] = 1;
+    for (int i = k; i >= 0; --i) {
+        if (!seen[static_cast<size_t>(i)]) continue;
+        for (int j = 0; j < ks[i].nargs; ++j) {
+            const Src s = src_of(ks[i].args[j]);
+            if (s.kernel) seen[static_cast<size_t>(s.i)] = 1;
+        }
+    }
+    std::vector<int> at(static_cast<size_t>(k) + 1, -1);
+    std::vector<vkc_region_kernel> out;
+    for (int i = 0; i <= k; ++i) {
+        if (!seen[static_cast<size_t>(i)]) continue;
+        vkc_region_kernel r = ks[i];
+        for (int j = 0; j < r.nargs; ++j) {
+            const Src s = src_of(r.args[j]);
+            if (s.kernel) r.args[j] = -1 - at[static_cast<size_t>(s.i)];
+        }
+        at[static_cast<size_t>(i)] = static_cast<int>(out.size());
+        out.push_back(r);
+    }
+    return out;
+}
+
+std::string name_of(int id) {
+    const char *s = vkc_kernel_name(id);
+    return s ? s : "";
+}
+
+// The fused.rs patterns over a region that runs fused (so none of its kernels can fail):
+// reduce_add_T(mul_T(x, y)) is dot_T(x, y), or sumsq_T(x) when x and y are one array;
+// count(<cmp>_T(x, c)) is count_<cmp>_T(x, c); reduce_add_T(select_T(<cmp>_T(x, c), x, e)) is
+// condsum_<cmp>_T(x, c, e). Operands are region sources; true when one matched.
+bool fused_pattern(const vkc_region_kernel *ks, const vkc_value *in, int root, const std::vector<Src> &args,
+                   int *root2, std::vector<Src> *args2) {
+    if (args.size() != 1 || !args[0].kernel) return false;
+    const std::string rn = name_of(root);
+    const vkc_region_kernel &k = ks[args[0].i];
+    const std::string kn = name_of(k.kernel);
+    auto is_array = [&](Src s) { return s.kernel || in[s.i].kind == VKC_VALUE_ARRAY; };
+    auto same_array = [&](Src a, Src b) {
+        if (a.kernel || b.kernel) return false;
+        const vkc_value &x = in[a.i], &y = in[b.i];
+        return x.kind == VKC_VALUE_ARRAY && y.kind == VKC_VALUE_ARRAY && x.array->data() == y.array->data() &&
+               x.array->len == y.array->len && x.array->type == y.array->type;
+    };
+    auto scalar_input = [&](Src s) { return !s.kernel && in[s.i].kind == VKC_VALUE_SCALAR; };
+    static const char *const types[] = {"f64", "f32", "i64", "u64", "i32"};
+    static const char *const cmps[] = {"eq", "ne", "lt", "le", "gt", "ge"};
+    for (const char *t : types) {
+        if (rn == std::string("reduce_add_") + t && kn == std::string("mul_") + t) {
+            const Src x = src_of(k.args[0]), y = src_of(k.args[1]);
+            if (!is_array(x) || !is_array(y)) return false;
+            const std::string f = same_array(x, y) ? std::string("sumsq_") + t : std::string("dot_") + t;
+            if ((*root2 = vkc_kernel_lookup(f.c_str())) < 0) return false;
+            *args2 = same_array(x, y) ? std::vector<Src>{x} : std::vector<Src>{x, y};
+            return true;
+        }
+        for (const char *c : cmps) {
+            const std::string cmp = std::string(c) + "_" + t;
+            if (rn == "count" && kn == cmp) {
+                const Src x = src_of(k.args[0]), v = src_of(k.args[1]);
+                if (!is_array(x) || !scalar_input(v)) return false;
+                if ((*root2 = vkc_kernel_lookup(("count_" + cmp).c_str())) < 0) return false;
+                *args2 = {x, v};
+                return true;
+            }
+            if (rn == std::string("reduce_add_") + t && kn == std::string("select_") + t) {
+                const Src m = src_of(k.args[0]), a = src_of(k.args[1]), e = src_of(k.args[2]);
+                if (!m.kernel || name_of(ks[m.i].kernel) != cmp || !scalar_input(e)) continue;
+                const Src x = src_of(ks[m.i].args[0]), v = src_of(ks[m.i].args[1]);
+                if (!same_array(x, a) || !scalar_input(v)) continue;
+                if ((*root2 = vkc_kernel_lookup(("condsum_" + cmp).c_str())) < 0) return false;
+                *args2 = {x, v, e};
+                return true;
+            }
+        }
+    }
+    return false;
+}
+
+}  // namespace
+
+}  // namespace vkc
+
+using namespace vkc;
+
+extern "C" {
+
+vkc_status vkc_region_eval(vkc_ctx *ctx, const vkc_region_kernel *kernels, int nkernels, const vkc_value *inputs,
+                           int ninputs, vkc_value *out) {
+    if (!ctx || !out || (nkernels > 0 && !kernels) || (ninputs > 0 && !inputs)) return VKC_USAGE;
+    return eval_region(ctx, kernels, nkernels, inputs, ninputs, out);
+}
+
+vkc_status vkc_region_reduce(vkc_ctx *ctx, int root, const int32_t *root_args, int nroot,
+                             const vkc_region_kernel *kernels, int nkernels, const vkc_value *inputs, int ninputs,
+                             vkc_value *out) {
+    if (!ctx || !out || (nroot > 0 && !root_args) || (nkernels > 0 && !kernels) || (ninputs > 0 && !inputs))
+        return VKC_USAGE;
+    memset(out, 0, sizeof *out);
+    if (vkc_kernel_class(root) != VKC_REDUCTION || !vkc_kernel_name(root))
+        return fail(ctx, VKC_USAGE, "the root of a fused region is a reduction");
+    vkc_status st = check_shape(ctx, kernels, nkernels, ninputs);
+    if (st) return st;
+    std::vector<Src> args;
+    for (int j = 0; j < nroot; ++j) {
+        const Src s = src_of(root_args[j]);
+        if (s.kernel ? s.i >= nkernels : s.i >= ninputs)
+            return fail(ctx, VKC_USAGE, "root argument " + std::to_string(j) + " names no kernel or input");
+        args.push_back(s);
+    }
+    RegionProg p;
+    int64_t n;
+    vkc_type t;
+    int root2 = root;
+    std::vector<Src> args2 = args;
+    if (!plan_region(kernels, nkernels, inputs, ninputs, &p, &n, &t) ||
+        !fused_pattern(kernels, inputs, root, args, &root2, &args2)) {
+        root2 = root;
+        args2 = args;
+    }
+    // The root's arguments left to right, each region argument by one pass over its subtree.
+    std::vector<vkc_value> temps, call;
+    for (const Src &s : args2) {
+        if (!s.kernel) {
+            call.push_back(inputs[s.i]);
+            continue;
+        }
+        const std::vector<vkc_region_kernel> sub = subtree(kernels, s.i);
+        vkc_value v;
+        if ((st = eval_region(ctx, sub.data(), static_cast<int>(sub.size()), inputs, ninputs, &v))) {
+            release_values(temps);
+            return st;
+        }
+        temps.push_back(v);
+        call.push_back(v);
+    }
+    st = vkc_call(ctx, root2, call.data(), static_cast<int>(call.size()), out);
+    release_values(temps);
+    return st;
+}
+
+}  // extern "C"

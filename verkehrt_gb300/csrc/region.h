@@ -1,0 +1,54 @@
+// The region evaluator: a chain of elementwise kernels (a region of the reference's executor,
+// src/exec/region.rs:22-50) run as one pass over the rows, every intermediate value kept on
+// chip. Shared by k_elementwise.cu (the row operations and the kernel) and k_region.cu (the
+// entries that check a region and fall back to whole evaluation).
+#pragma once
+
+#include "vkc_internal.h"
+
+namespace vkc {
+
+// Row operations of the elementwise kernels.
+enum EwFn {
+    EF_ADD, EF_SUB, EF_MUL, EF_MIN, EF_MAX, EF_LT, EF_LE, EF_GT, EF_GE, EF_EQ, EF_NE,
+    EF_AND, EF_OR, EF_XOR, EF_DIV, EF_NEG, EF_ABS, EF_SQRT, EF_NOT, EF_BNOT, EF_SELECT,
+    EF_DIVC, EF_CAST
+};
+// Storage types (bool is stored as u8 0/1).
+enum EwTy { ET_F64, ET_F32, ET_I64, ET_U64, ET_I32, ET_U8 };
+
+// The truncating division of div_const_T by a scalar (round-up multiply-high constants).
+struct Divider {
+    unsigned long long m;
+    int sh1, sh2;
+    unsigned long long dneg;  // signed types: all ones when the divisor is negative
+};
+// The divider of divisor bits `d` of storage type `ty`; false for a zero divisor.
+bool make_ew_divider(int ty, unsigned long long d, Divider *out);
+
+constexpr int RG_MAX_IN = 8;      // region inputs
+constexpr int RG_MAX_K = 12;      // region kernels
+constexpr int RG_MAX_SLOTS = 16;  // inputs + kernels
+
+struct RgIn {
+    const void *p;          // array rows, or nullptr for a scalar splat
+    unsigned long long s;   // the scalar's bits
+    int width;              // bytes per row
+    int arr;
+};
+// Kernel k of the region writes slot nin + k from the slots a[0..2] (inputs are slots
+// 0..nin-1).
+struct RgOp {
+    unsigned char fn, ty, dst, a[3];
+    Divider dv;
+};
+struct RegionProg {
+    int nin, nk, out_width;
+    RgIn in[RG_MAX_IN];
+    RgOp op[RG_MAX_K];
+};
+
+// Runs `p` over n rows into `out` (the last kernel's rows) on the context's stream.
+vkc_status launch_region(vkc_ctx *ctx, const RegionProg &p, int64_t n, void *out);
+
+}  // namespace vkc

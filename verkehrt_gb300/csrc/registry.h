@@ -73,6 +73,9 @@ struct KernelDef {
     SelectFn sel = nullptr;
     ScanMake scan = nullptr;
     WholeFn whole = nullptr;
+    // Elementwise kernels: the row operation, its operand type and its result type as codes
+    // of the region evaluator (k_elementwise.cu); ew_fn < 0 elsewhere.
+    int ew_fn = -1, ew_ty = 0, ew_dst = 0;
 };
 
 // The table's entry of that name (for entries built from other entries), or nullptr.
