@@ -246,7 +246,8 @@ VKC_API vkc_status vkc_elementwise_tile(vkc_ctx *ctx, int id, const vkc_value *a
  * may be at most 2^28 rows (larger n is rejected with VKC_USAGE and a message), and `in` and
  * `out` must be device (or managed) memory of `device` (NULL or host pointers are rejected with
  * VKC_USAGE). The first call on a device looks up the array's device address (once per device)
- * and keeps it for the life of the process; make that first call before any stream capture.
+ * and keeps it for the life of the process. Every call synchronizes `stream`, so the entry
+ * cannot run inside a stream capture.
  * A device reset (cudaDeviceReset) reloads the library's device image and leaves that address
  * stale, so this entry must not be called after a reset of its device. Every call shares the
  * array: calls that overlap on the GPU race,

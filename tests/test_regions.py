@@ -235,7 +235,7 @@ def test_fused_roots(ctx):
     k = vk.region_kernel
     n = 300_001
     x, y = column("f64", n, 7), column("f64", n, 8)
-    x[:8] = np.abs(x[:8]) + 1.0  # no NaN or inf in the sums below
+    x[:8] = np.arange(8) + 1.0  # no NaN or inf in the sums below
     y[:8] = 1.0
     dx, dy = ctx.upload(x), ctx.upload(y)
 
@@ -246,7 +246,7 @@ def test_fused_roots(ctx):
             vals.append(ctx.call(name, *[inputs[s] if s >= 0 else vals[-1 - s] for s in srcs]))
         args = [inputs[s] if s >= 0 else vals[-1 - s] for s in root_args]
         want = ctx.call(root, *args, raw=True)
-        assert got == want, (root, kernels)
+        assert (got[0], got[2]) == (want[0], want[2]), (root, kernels)  # type and bits
         if want_bits is not None:
             assert got[2] == want_bits
         return got

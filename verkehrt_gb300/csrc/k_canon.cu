@@ -1119,14 +1119,15 @@ __global__ void canon_finish(CanonState *state, int tail_len) {
 // around zero, magnitudes as large as the sum) make the walk resolve most tiles from the rows,
 // one at a time. When the walk falls behind this kernel's pace (WalkClock) it stops, and this
 // kernel runs each stopped lane to the end from its exact state. One warp per lane; each step
-// takes 32 * CH_ROWS of the lane's rows, CH_ROWS consecutive ones per thread, prefetched
-// CH_SLOTS - 1 steps ahead with cp.async into the thread's own row of a shared ring (each thread
-// reads only what it copied). The cost is one warp round per binade crossing, each with CH_ROWS
+// takes 32 * ROWS of the lane's rows, ROWS consecutive ones per thread (the autotuner's
+// canon_chain_rows), prefetched CH_SLOTS - 1 steps ahead with cp.async into the thread's own row
+// of a shared ring (each thread reads only what it copied). The cost is one warp round per
+// binade crossing, each with ROWS
 // dependent IEEE adds (63 cycles each on GB300), so the rows per thread are few (measured at
 // 2^26 mean-centred rows: 8 rows 43 ms, 32 rows 92 ms; eight warps a lane, or 32 rows in four
 // 8-row fallback units, were slower again: every crossing costs a whole round).
 //
-// A thread's CH_ROWS rows act on the state's magnitude S (in ulps u = 2^(E-52) of its binade E) as
+// A thread's ROWS rows act on the state's magnitude S (in ulps u = 2^(E-52) of its binade E) as
 // integer increments, the integer step of seg_tf: +-RNE(|x|/u) by the row's sign relative to
 // the state's, and for a row exactly halfway the even neighbour, which depends on the parity of
 // S at that row; so each thread keeps its increments for both parities of S before its rows,
@@ -1136,10 +1137,7 @@ __global__ void canon_finish(CanonState *state, int tail_len) {
 // exact sum of a downward step above 2^E); the first thread whose rows fail (a crossing, a row
 // not below 2^E or not finite) adds its rows with IEEE adds, the reference's own operation, and
 // the rest are computed again for the new state. So the result is the chain's, bit for bit.
-constexpr int CH_ROWS = 8;                   // lane rows per thread and step
-constexpr int CH_STEP = 32 * CH_ROWS;        // 16-row blocks per step
-constexpr int CH_SLOTS = 8;                  // steps in the shared ring
-constexpr int CH_PITCH = CH_ROWS + 1;        // doubles per thread row (odd: spreads the banks)
+constexpr int CH_SLOTS = 8;  // steps in the shared ring
 
 __device__ __forceinline__ void cp_async8(void *dst, const void *src) {
     asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
@@ -1149,31 +1147,33 @@ template <int N> __device__ __forceinline__ void cp_async_wait() {
     asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 
-template <int OP> constexpr size_t chain_smem() {
-    return static_cast<size_t>(CH_SLOTS) * (OP == ROW_DOT ? 2 : 1) * 32 * CH_PITCH * sizeof(unsigned long long);
+// Doubles per thread row of the ring: ROWS + 1 (odd: spreads the banks).
+template <int OP, int ROWS> constexpr size_t chain_smem() {
+    return static_cast<size_t>(CH_SLOTS) * (OP == ROW_DOT ? 2 : 1) * 32 * (ROWS + 1) * sizeof(unsigned long long);
 }
 
-template <int OP>
+template <int OP, int ROWS>
 __global__ void __launch_bounds__(32) canon_chain_kernel(RowArgs args, int64_t nb, int T, CanonWork wk,
                                                          CanonState *state) {
     extern __shared__ __align__(16) unsigned long long chain_smem_buf[];
     constexpr int NA = OP == ROW_DOT ? 2 : 1;
+    constexpr int STEP = 32 * ROWS, PITCH = ROWS + 1;
     const int L = blockIdx.x, j = threadIdx.x;
     const int t0 = wk.resume[L];
     if (t0 >= T) return;
     const int64_t b0 = static_cast<int64_t>(t0) * CT_BLOCKS;
-    const int64_t steps = (nb - b0 + CH_STEP - 1) / CH_STEP;
+    const int64_t steps = (nb - b0 + STEP - 1) / STEP;
     auto row_at = [&](int64_t k, int a) {
-        return chain_smem_buf + ((k % CH_SLOTS) * NA + a) * (32 * CH_PITCH) + j * CH_PITCH;
+        return chain_smem_buf + ((k % CH_SLOTS) * NA + a) * (32 * PITCH) + j * PITCH;
     };
     // Copies of step k (an empty group past the end keeps the group count uniform).
     auto issue = [&](int64_t k) {
         if (k < steps) {
-            const int64_t bb = b0 + k * CH_STEP + static_cast<int64_t>(j) * CH_ROWS;
+            const int64_t bb = b0 + k * STEP + static_cast<int64_t>(j) * ROWS;
             unsigned long long *dx = row_at(k, 0);
             unsigned long long *dy = row_at(k, NA - 1);
 #pragma unroll 8
-            for (int i = 0; i < CH_ROWS; ++i) {
+            for (int i = 0; i < ROWS; ++i) {
                 if (bb + i < nb) {
                     cp_async8(dx + i, args.x + (bb + i) * 16 + L);
                     if (OP == ROW_DOT) cp_async8(dy + i, args.y + (bb + i) * 16 + L);
@@ -1186,13 +1186,13 @@ __global__ void __launch_bounds__(32) canon_chain_kernel(RowArgs args, int64_t n
     unsigned long long s = state->lanes[L];
     for (int64_t k = 0; k < steps; ++k) {
         cp_async_wait<CH_SLOTS - 2>();  // this thread's copies of step k have landed
-        unsigned long long v[CH_ROWS];
+        unsigned long long v[ROWS];
         {
-            const int64_t bb = b0 + k * CH_STEP + static_cast<int64_t>(j) * CH_ROWS;
+            const int64_t bb = b0 + k * STEP + static_cast<int64_t>(j) * ROWS;
             const unsigned long long *rx = row_at(k, 0);
             const unsigned long long *ry = row_at(k, NA - 1);
 #pragma unroll
-            for (int i = 0; i < CH_ROWS; ++i)
+            for (int i = 0; i < ROWS; ++i)
                 v[i] = bb + i < nb ? row_value<OP>(args, rx[i], OP == ROW_DOT ? ry[i] : 0ull) : 0ull;
         }
         issue(k + CH_SLOTS - 1);  // into the slot of step k - 1, read by the previous step
@@ -1205,7 +1205,7 @@ __global__ void __launch_bounds__(32) canon_chain_kernel(RowArgs args, int64_t n
         // even start, (P1, mn1, mx1) for an odd one.
         unsigned fkey = ~0u;
         long long fP0 = 0, fP1 = 0, fmn0 = 0, fmx0 = 0, fmn1 = 0, fmx1 = 0;
-        bool fok = false;
+        bool fok = false, ftie = false;
         while (cur < 32) {
             const unsigned es = static_cast<unsigned>(s >> 52) & 0x7ffu;
             const unsigned long long neg = s >> 63;
@@ -1217,8 +1217,9 @@ __global__ void __launch_bounds__(32) canon_chain_kernel(RowArgs args, int64_t n
                 fmn0 = fmn1 = LLONG_MAX;
                 fmx0 = fmx1 = LLONG_MIN;
                 fok = true;
+                ftie = false;
 #pragma unroll
-                for (int i = 0; i < CH_ROWS; ++i) {
+                for (int i = 0; i < ROWS; ++i) {
                     const unsigned long long b = v[i];
                     const unsigned ex = static_cast<unsigned>(b >> 52) & 0x7ffu;
                     fok &= ex < es;  // below 2^E and finite
@@ -1230,6 +1231,7 @@ __global__ void __launch_bounds__(32) canon_chain_kernel(RowArgs args, int64_t n
                         const long long qf = q - 1;
                         i0 = qf + ((fP0 + qf) & 1);
                         i1 = qf + ((1 + fP1 + qf) & 1);
+                        ftie = true;
                     }
                     const bool down = ((b >> 63) ^ neg) != 0;  // the row moves the magnitude down
                     fP0 += down ? -i0 : i0;
@@ -1242,22 +1244,35 @@ __global__ void __launch_bounds__(32) canon_chain_kernel(RowArgs args, int64_t n
             }
             const bool live = j >= cur;
             const bool ok = !live || (usable && fok);
-            // Ordered composition of the parity pairs (the state's parity after a function).
-            long long c0 = live ? fP0 : 0, c1 = live ? fP1 : 0;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const long long a0 = __shfl_up_sync(FULL, c0, o), a1 = __shfl_up_sync(FULL, c1, o);
-                if (j >= o) {
-                    const long long n0 = a0 + ((a0 & 1) ? c1 : c0);
-                    const long long n1 = a1 + (((1 + a1) & 1) ? c1 : c0);
-                    c0 = n0;
-                    c1 = n1;
-                }
-            }
-            const long long e0 = __shfl_up_sync(FULL, c0, 1), e1 = __shfl_up_sync(FULL, c1, 1);
             const long long M = static_cast<long long>((s & MANT) | ONE52);
             const long long p0 = M & 1;
-            const long long pre = j == 0 ? 0 : (p0 ? e1 : e0);  // increments before this thread
+            long long c0 = live ? fP0 : 0, c1 = live ? fP1 : 0, pre;
+            if (!__any_sync(FULL, live && ftie)) {
+                // No halfway row: every function is one increment whatever the parity, and the
+                // composition is a plain sum.
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const long long a0 = __shfl_up_sync(FULL, c0, o);
+                    if (j >= o) c0 += a0;
+                }
+                c1 = c0;
+                const long long e0 = __shfl_up_sync(FULL, c0, 1);
+                pre = j == 0 ? 0 : e0;
+            } else {
+                // Ordered composition of the parity pairs (the state's parity after a function).
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const long long a0 = __shfl_up_sync(FULL, c0, o), a1 = __shfl_up_sync(FULL, c1, o);
+                    if (j >= o) {
+                        const long long n0 = a0 + ((a0 & 1) ? c1 : c0);
+                        const long long n1 = a1 + (((1 + a1) & 1) ? c1 : c0);
+                        c0 = n0;
+                        c1 = n1;
+                    }
+                }
+                const long long e0 = __shfl_up_sync(FULL, c0, 1), e1 = __shfl_up_sync(FULL, c1, 1);
+                pre = j == 0 ? 0 : (p0 ? e1 : e0);  // increments before this thread
+            }
             const bool odd = ((p0 + pre) & 1) != 0;
             const long long mn = odd ? fmn1 : fmn0, mx = odd ? fmx1 : fmx0;
             const long long lo = static_cast<long long>(ONE52) + 1, hi = static_cast<long long>(2 * ONE52) - 1;
@@ -1276,7 +1291,7 @@ __global__ void __launch_bounds__(32) canon_chain_kernel(RowArgs args, int64_t n
             if (j == js) {
                 double d = as_f64(s);
 #pragma unroll
-                for (int i = 0; i < CH_ROWS; ++i) d = __dadd_rn(d, as_f64(v[i]));
+                for (int i = 0; i < ROWS; ++i) d = __dadd_rn(d, as_f64(v[i]));
                 r = as_bits(d);
             }
             s = __shfl_sync(FULL, r, js);
@@ -1324,10 +1339,18 @@ static vkc_status launch_canon(vkc_ctx *ctx, const RowArgs &a, int64_t nb, int T
     if constexpr (!RECORD) {
         static std::atomic<unsigned long long> chain_configured{0};
         once_per_device(chain_configured, ctx->device, [] {
-            cudaFuncSetAttribute(canon_chain_kernel<OP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 static_cast<int>(chain_smem<OP>()));
+            cudaFuncSetAttribute(canon_chain_kernel<OP, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 static_cast<int>(chain_smem<OP, 4>()));
+            cudaFuncSetAttribute(canon_chain_kernel<OP, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 static_cast<int>(chain_smem<OP, 8>()));
+            cudaFuncSetAttribute(canon_chain_kernel<OP, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 static_cast<int>(chain_smem<OP, 16>()));
         });
-        canon_chain_kernel<OP><<<16, 32, chain_smem<OP>(), ctx->stream>>>(a, nb, T, wk, state);
+        switch (tune(ctx, TK_CHAIN_ROWS, nb * 16)) {
+        case 4: canon_chain_kernel<OP, 4><<<16, 32, chain_smem<OP, 4>(), ctx->stream>>>(a, nb, T, wk, state); break;
+        case 16: canon_chain_kernel<OP, 16><<<16, 32, chain_smem<OP, 16>(), ctx->stream>>>(a, nb, T, wk, state); break;
+        default: canon_chain_kernel<OP, 8><<<16, 32, chain_smem<OP, 8>(), ctx->stream>>>(a, nb, T, wk, state); break;
+        }
         if ((st = launched(ctx, "canon_chain"))) return st;
     }
     if constexpr (RECORD) {

@@ -4,4 +4,4 @@
 // first table's slots); columns are the size classes n < 2^20, n < 2^24, and larger.
 // Measured on: NVIDIA GB300, 2026-12-03 (median of the runs in tuning_table.json).
 #pragma once
-#define VKC_TUNE_TABLE { {8, 12, 16}, {16, 8, 16}, {1, 2, 1}, {22, 21, 22} }
+#define VKC_TUNE_TABLE { {8, 12, 16}, {16, 8, 16}, {1, 2, 1}, {22, 21, 22}, {8, 8, 8} }
