@@ -50,7 +50,9 @@ def test_every_candidate_gives_the_same_results(ctx):
             "stream_blocks_per_sm": (oracle.count_cmp_f64(x, "gt", 0.5), oracle.reduce_min_f64(x), oracle.argmax_f64(x)),
             "gather_rows_per_thread": oracle.gather(src, idx),
             "group_first_table_log2": oracle.group_id_i64(g),
+            "canon_chain_rows": np.float64(oracle.reduce_add_f64(x - 0.5)).view(np.uint64),
         }
+        dc = ctx.upload(x - 0.5)
         for knob in autotune.KNOBS:
             before = ctx.tune_get(knob, c)
             for v in autotune.CANDIDATES[knob]:
@@ -62,6 +64,8 @@ def test_every_candidate_gives_the_same_results(ctx):
                     assert got == want[knob], (n, v)
                 elif knob == "gather_rows_per_thread":
                     assert np.array_equal(ctx.call("gather_i64", ds, di).numpy(), want[knob]), (n, v)
+                elif knob == "canon_chain_rows":
+                    assert ctx.call("reduce_add_f64", dc, raw=True)[2] == int(want[knob]), (n, v)
                 else:
                     assert np.array_equal(ctx.call("group_id_i64", dg).numpy(), want[knob]), (n, v)
             ctx.tune_set(knob, c, before)

@@ -389,9 +389,13 @@ constexpr int RG_THREADS = 128, RG_ROWS = 4, RG_BLOCK_ROWS = RG_THREADS * RG_ROW
 // Slots live in shared memory, slot j of local row l at s_w[j * RG_BLOCK_ROWS + l]; a thread
 // touches only its own rows (t, t + 128, ...), so no barrier is needed. Each block takes
 // RG_BLOCK_ROWS rows per step: the inputs' loads of a step are in flight together.
+// COUNT: instead of storing the result rows, count the nonzero ones (a region under `count`)
+// into *out (an unsigned 64-bit counter).
+template <bool COUNT>
 __global__ void __launch_bounds__(RG_THREADS) region_kernel(const RegionProg P, int64_t n, void *__restrict__ out) {
     extern __shared__ unsigned long long s_w[];
     const int t = threadIdx.x;
+    unsigned long long nonzero = 0;
     for (int64_t b0 = static_cast<int64_t>(blockIdx.x) * RG_BLOCK_ROWS; b0 < n;
          b0 += static_cast<int64_t>(gridDim.x) * RG_BLOCK_ROWS) {
         for (int j = 0; j < P.nin; ++j) {
@@ -421,6 +425,10 @@ __global__ void __launch_bounds__(RG_THREADS) region_kernel(const RegionProg P, 
             const int64_t i = b0 + t + r * RG_THREADS;
             if (i >= n) break;
             const unsigned long long w = res[r * RG_THREADS];
+            if (COUNT) {
+                nonzero += w != 0;
+                continue;
+            }
             switch (P.out_width) {
             case 8: static_cast<unsigned long long *>(out)[i] = w; break;
             case 4: static_cast<unsigned *>(out)[i] = static_cast<unsigned>(w); break;
@@ -428,21 +436,27 @@ __global__ void __launch_bounds__(RG_THREADS) region_kernel(const RegionProg P, 
             }
         }
     }
+    if (COUNT) {
+        nonzero = warp_sum(nonzero);
+        if ((t & 31) == 0 && nonzero) atomicAdd(static_cast<unsigned long long *>(out), nonzero);
+    }
 }
 
-vkc_status launch_region(vkc_ctx *ctx, const RegionProg &p, int64_t n, void *out) {
+vkc_status launch_region(vkc_ctx *ctx, const RegionProg &p, int64_t n, void *out, bool count) {
     if (n <= 0) return VKC_OK;
     const size_t smem = static_cast<size_t>(p.nin + p.nk) * RG_BLOCK_ROWS * sizeof(unsigned long long);
     static std::atomic<unsigned long long> configured{0};
     once_per_device(configured, ctx->device, [] {
-        cudaFuncSetAttribute(region_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             static_cast<int>(RG_MAX_SLOTS * RG_BLOCK_ROWS * sizeof(unsigned long long)));
+        const int most = static_cast<int>(RG_MAX_SLOTS * RG_BLOCK_ROWS * sizeof(unsigned long long));
+        cudaFuncSetAttribute(region_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, most);
+        cudaFuncSetAttribute(region_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, most);
     });
     // Resident blocks: as many as the slots' shared memory allows, at most 16 a multiprocessor.
     const int per_sm = std::max(1, std::min(16, static_cast<int>((200u << 10) / smem)));
     const int64_t blocks = (n + RG_BLOCK_ROWS - 1) / RG_BLOCK_ROWS;
     const int grid = static_cast<int>(std::min<int64_t>(blocks, static_cast<int64_t>(ctx->sms) * per_sm));
-    region_kernel<<<grid, RG_THREADS, smem, ctx->stream>>>(p, n, out);
+    if (count) region_kernel<true><<<grid, RG_THREADS, smem, ctx->stream>>>(p, n, out);
+    else region_kernel<false><<<grid, RG_THREADS, smem, ctx->stream>>>(p, n, out);
     return launched(ctx, "region");
 }
 

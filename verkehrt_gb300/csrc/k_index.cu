@@ -9,6 +9,9 @@
 
 namespace vkc {
 
+int64_t scan_counts_sum_words(int64_t m);
+void scan_counts(vkc_ctx *ctx, const unsigned *c, int64_t m, unsigned *sums, unsigned *out);
+
 // ------------------------------------------------------------------ gather
 
 template <int W> struct GWord;
@@ -57,52 +60,47 @@ static void launch_gather(vkc_ctx *ctx, int rows, int64_t n, const typename GWor
 // ------------------------------------------------------------------ partitioned gather
 //
 // Random 8-byte reads from a source far larger than L2 each cost a DRAM burst (about 97 DRAM
-// bytes per row on GB300, against 24 algorithmic). For such sources the gather runs as three
+// bytes per row on GB300, against 24 algorithmic). For such sources the gather runs as four
 // passes over tiles of GP_TILE index rows, so that the source is read one region at a time
-// while that region sits in L2, and every other access is a coalesced run. Intermediate arrays
-// are tile-major (tile t owns positions t * GP_TILE ..), so no pass needs a global scan:
-//   partition  per tile, each row's region (GP_NB regions of 2^rb source rows) and its slot in
-//              the tile's region-sorted order; the offsets within the regions go to `part` in
-//              that order, each row's slot to `loc`, and each (region, tile) run's count and
-//              start to `cs`. The bounds check is here: an offending row takes no slot and
-//              records its row number.
-//   region     one block per (region, GP_TPB tiles), region-major, so the blocks in flight read
-//              one or two regions, whose lines stay in L2: vals[p] = src[region base + part[p]]
-//              over the block's runs;
-//   restore    each tile stages its vals in shared memory and writes out[r] = staged[loc[r]] in
-//              row order.
-// DRAM bytes per row: 8 idx + 4 part + 2 loc, then 4 part + 8 vals + about 8 of source
-// lines, then 8 vals + 2 loc + 8 out: about 52 (the one-pass gather: about 97).
+// while that region sits in L2, and every other access is a coalesced run:
+//   count      per tile, the rows that fall in each of the GP_NB source regions (and the bounds
+//              check: an offending row is not counted and records its row number);
+//   partition  after one exclusive scan of the counts (region-major), each row's offset within
+//              its region goes to its tile's run of `part` in that region, and the row's slot in
+//              the tile's region-sorted order goes to `loc`;
+//   region     positions in region order read src[region base + part[p]] into vals[p]; the
+//              blocks in flight cover one or two regions, whose lines stay in L2;
+//   restore    each tile gathers its runs of vals into shared memory in region-sorted order and
+//              writes out[i] = staged[loc[i]] in row order.
+// About 60 DRAM bytes per row, nearly all in runs.
 constexpr int GP_THREADS = 256, GP_ITEMS = 16, GP_TILE = GP_THREADS * GP_ITEMS;
-constexpr int GP_NB = 64;   // source regions
-constexpr int GP_TPB = 64;  // tiles per block of the region pass
-constexpr int GP_UNROLL = 8;
+constexpr int GP_NB = 64;  // source regions
 
-// Warp 0: the exclusive prefix of n <= 64 counts get(b) into s_start[0 .. n - 1], and their
-// total into s_start[n].
-template <class Get> __device__ __forceinline__ void gp_starts(Get get, int n, unsigned *s_start) {
+// Warp 0: the exclusive prefix of GP_NB counts get(b) into s_start[0 .. GP_NB - 1], and their
+// total into s_start[GP_NB].
+template <class Get> __device__ __forceinline__ void gp_starts(Get get, unsigned *s_start) {
     const int lane = threadIdx.x & 31;
     unsigned run = 0;
 #pragma unroll
-    for (int b0 = 0; b0 < 64; b0 += 32) {
-        const unsigned c = b0 + lane < n ? get(b0 + lane) : 0u;
+    for (int b0 = 0; b0 < GP_NB; b0 += 32) {
+        const unsigned c = get(b0 + lane);
         unsigned x = c;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
             const unsigned y = __shfl_up_sync(FULL, x, o);
             if (lane >= o) x += y;
         }
-        if (b0 + lane < n) s_start[b0 + lane] = run + x - c;
+        s_start[b0 + lane] = run + x - c;
         run += __shfl_sync(FULL, x, 31);
     }
-    if (lane == 0) s_start[n] = run;
+    if (lane == 0) s_start[GP_NB] = run;
 }
 
-// The last j with s_start[j] <= v (s_start[0] = 0 <= v < s_start[64]; 64 entries).
-__device__ __forceinline__ int gp_run_of(const unsigned *s_start, unsigned v) {
-    int lo = 0, hi = 64;
+// The last b with s_start[b] <= v (s_start[0] = 0 <= v < s_start[GP_NB]).
+__device__ __forceinline__ int gp_region_of(const unsigned *s_start, unsigned v) {
+    int lo = 0, hi = GP_NB;
 #pragma unroll
-    for (int it = 0; it < 6; ++it) {
+    for (int it = 0; it < 6; ++it) {  // GP_NB = 2^6
         const int mid = (lo + hi) >> 1;
         if (s_start[mid] <= v) lo = mid;
         else hi = mid;
@@ -110,14 +108,38 @@ __device__ __forceinline__ int gp_run_of(const unsigned *s_start, unsigned v) {
     return lo;
 }
 
+__global__ void __launch_bounds__(GP_THREADS) gp_count_kernel(const long long *__restrict__ idx, int64_t n, uint64_t nsrc,
+                                                              int rb, int tiles, unsigned *__restrict__ counts,
+                                                              DevStatus *status) {
+    __shared__ unsigned h[GP_NB];
+    if (threadIdx.x < GP_NB) h[threadIdx.x] = 0;
+    __syncthreads();
+    const int64_t base = static_cast<int64_t>(blockIdx.x) * GP_TILE;
+#pragma unroll
+    for (int j = 0; j < GP_ITEMS; ++j) {
+        const int64_t r = base + j * GP_THREADS + threadIdx.x;
+        if (r < n) {
+            const auto k = static_cast<unsigned long long>(__ldcs(idx + r));
+            if (k < nsrc) atomicAdd(&h[static_cast<unsigned>(k >> rb)], 1u);
+            else atomicMin(&status->first_bad, static_cast<unsigned long long>(r));
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < GP_NB) counts[static_cast<int64_t>(threadIdx.x) * tiles + blockIdx.x] = h[threadIdx.x];
+}
+
 __global__ void __launch_bounds__(GP_THREADS) gp_partition_kernel(const long long *__restrict__ idx, int64_t n,
                                                                   uint64_t nsrc, int rb, int tiles,
+                                                                  const unsigned *__restrict__ offs,
                                                                   unsigned *__restrict__ part,
-                                                                  unsigned short *__restrict__ loc,
-                                                                  unsigned *__restrict__ cs, DevStatus *status) {
-    __shared__ unsigned s_cnt[GP_NB], s_start[GP_NB + 1];
+                                                                  unsigned short *__restrict__ loc) {
+    __shared__ unsigned s_cnt[GP_NB], s_start[GP_NB + 1], s_goff[GP_NB];
     __shared__ unsigned s_part[GP_TILE];
-    if (threadIdx.x < GP_NB) s_cnt[threadIdx.x] = 0;
+    __shared__ unsigned char s_reg[GP_TILE];
+    if (threadIdx.x < GP_NB) {
+        s_cnt[threadIdx.x] = 0;
+        s_goff[threadIdx.x] = offs[static_cast<int64_t>(threadIdx.x) * tiles + blockIdx.x];
+    }
     __syncthreads();
     const int64_t base = static_cast<int64_t>(blockIdx.x) * GP_TILE;
     const unsigned long long mask = (1ull << rb) - 1;
@@ -126,85 +148,86 @@ __global__ void __launch_bounds__(GP_THREADS) gp_partition_kernel(const long lon
 #pragma unroll
     for (int j = 0; j < GP_ITEMS; ++j) {
         const int64_t r = base + j * GP_THREADS + threadIdx.x;
-        k[j] = r < n ? static_cast<unsigned long long>(__ldcs(idx + r)) : ~0ull;  // past the end: no slot
-        if (r < n && k[j] >= nsrc) atomicMin(&status->first_bad, static_cast<unsigned long long>(r));
+        k[j] = r < n ? static_cast<unsigned long long>(__ldcs(idx + r)) : ~0ull;  // past the end: like an offending row
     }
     // Slots within the tile's region runs, in any order: the output does not depend on it.
 #pragma unroll
     for (int j = 0; j < GP_ITEMS; ++j) rk[j] = k[j] < nsrc ? atomicAdd(&s_cnt[static_cast<unsigned>(k[j] >> rb)], 1u) : 0u;
     __syncthreads();
-    if (threadIdx.x < 32) gp_starts([&](int b) { return s_cnt[b]; }, GP_NB, s_start);
+    if (threadIdx.x < 32) gp_starts([&](int b) { return s_cnt[b]; }, s_start);
     __syncthreads();
-    if (threadIdx.x < GP_NB)
-        cs[static_cast<int64_t>(threadIdx.x) * tiles + blockIdx.x] = (s_cnt[threadIdx.x] << 16) | s_start[threadIdx.x];
 #pragma unroll
     for (int j = 0; j < GP_ITEMS; ++j) {
         const int64_t r = base + j * GP_THREADS + threadIdx.x;
         if (r >= n) continue;
         if (k[j] < nsrc) {
-            const unsigned l = s_start[static_cast<unsigned>(k[j] >> rb)] + rk[j];
+            const unsigned b = static_cast<unsigned>(k[j] >> rb);
+            const unsigned l = s_start[b] + rk[j];
             loc[r] = static_cast<unsigned short>(l);
             s_part[l] = static_cast<unsigned>(k[j] & mask);
+            s_reg[l] = static_cast<unsigned char>(b);
         } else {
             loc[r] = 0;  // the call fails; the row's output is never read
         }
     }
     __syncthreads();
     const int rows = static_cast<int>(s_start[GP_NB]);
-    for (int l = threadIdx.x; l < rows; l += GP_THREADS) part[base + l] = s_part[l];
+    for (int l = threadIdx.x; l < rows; l += GP_THREADS) {
+        const unsigned b = s_reg[l];
+        part[s_goff[b] + static_cast<unsigned>(l) - s_start[b]] = s_part[l];
+    }
 }
 
 __global__ void __launch_bounds__(GP_THREADS) gp_region_kernel(const unsigned long long *__restrict__ src,
                                                                const unsigned *__restrict__ part,
-                                                               const unsigned *__restrict__ cs, int tiles, int chunks,
-                                                               int rb, unsigned long long *__restrict__ vals) {
-    __shared__ unsigned s_pre[GP_TPB + 1], s_word[GP_TPB];
-    const int b = blockIdx.x / chunks;
-    const int t0 = (blockIdx.x - b * chunks) * GP_TPB;
-    const int nt = min(GP_TPB, tiles - t0);
-    if (threadIdx.x < nt) s_word[threadIdx.x] = cs[static_cast<int64_t>(b) * tiles + t0 + threadIdx.x];
+                                                               const unsigned *__restrict__ counts,
+                                                               const unsigned *__restrict__ offs, int tiles, int rb,
+                                                               unsigned long long *__restrict__ vals) {
+    __shared__ unsigned s_start[GP_NB + 1];
+    const int64_t last = static_cast<int64_t>(GP_NB) * tiles - 1;
+    // Region b's positions start at the offset of (b, tile 0); the last offset plus its count
+    // is the number of rows in range.
+    if (threadIdx.x <= GP_NB)
+        s_start[threadIdx.x] = threadIdx.x < GP_NB ? offs[static_cast<int64_t>(threadIdx.x) * tiles] : offs[last] + counts[last];
     __syncthreads();
-    if (threadIdx.x < 32) gp_starts([&](int j) { return s_word[j] >> 16; }, nt, s_pre);
-    __syncthreads();
-    const unsigned total = s_pre[nt];
-    if (threadIdx.x > nt && threadIdx.x <= GP_TPB) s_pre[threadIdx.x] = total;  // empty runs past the last tile
-    __syncthreads();
-    const unsigned long long *reg = src + (static_cast<int64_t>(b) << rb);
-    for (unsigned e0 = 0; e0 < total; e0 += GP_THREADS * GP_UNROLL) {
-        int64_t p[GP_UNROLL];
-        unsigned off[GP_UNROLL];
-#pragma unroll
-        for (int u = 0; u < GP_UNROLL; ++u) {
-            const unsigned e = e0 + u * GP_THREADS + threadIdx.x;
-            p[u] = -1;
-            if (e < total) {
-                const int j = gp_run_of(s_pre, e);
-                p[u] = static_cast<int64_t>(t0 + j) * GP_TILE + (s_word[j] & 0xffffu) + (e - s_pre[j]);
-            }
+    const unsigned total = s_start[GP_NB];
+    const int64_t base = static_cast<int64_t>(blockIdx.x) * GP_TILE;
+#pragma unroll 4
+    for (int j = 0; j < GP_ITEMS; ++j) {
+        const int64_t p = base + j * GP_THREADS + threadIdx.x;
+        if (p < total) {
+            const int b = gp_region_of(s_start, static_cast<unsigned>(p));
+            vals[p] = __ldg(src + (static_cast<int64_t>(b) << rb) + __ldcs(part + p));
         }
-#pragma unroll
-        for (int u = 0; u < GP_UNROLL; ++u) off[u] = p[u] >= 0 ? __ldcs(part + p[u]) : 0u;
-        unsigned long long v[GP_UNROLL];
-#pragma unroll
-        for (int u = 0; u < GP_UNROLL; ++u) v[u] = p[u] >= 0 ? __ldg(reg + off[u]) : 0ull;
-#pragma unroll
-        for (int u = 0; u < GP_UNROLL; ++u)
-            if (p[u] >= 0) vals[p[u]] = v[u];
     }
 }
 
 __global__ void __launch_bounds__(GP_THREADS) gp_restore_kernel(const unsigned long long *__restrict__ vals,
-                                                                const unsigned short *__restrict__ loc, int64_t n,
+                                                                const unsigned short *__restrict__ loc,
+                                                                const unsigned *__restrict__ counts,
+                                                                const unsigned *__restrict__ offs, int64_t n, int tiles,
                                                                 unsigned long long *__restrict__ out) {
+    __shared__ unsigned s_start[GP_NB + 1], s_goff[GP_NB];
     __shared__ unsigned long long s_vals[GP_TILE];
-    const int64_t base = static_cast<int64_t>(blockIdx.x) * GP_TILE;
-    const int rows = static_cast<int>(min(static_cast<int64_t>(GP_TILE), n - base));
+    if (threadIdx.x < 32) gp_starts([&](int b) { return counts[static_cast<int64_t>(b) * tiles + blockIdx.x]; }, s_start);
+    if (threadIdx.x < GP_NB) s_goff[threadIdx.x] = offs[static_cast<int64_t>(threadIdx.x) * tiles + blockIdx.x];
+    __syncthreads();
+    const int rows = static_cast<int>(s_start[GP_NB]);
+    unsigned at[GP_ITEMS];
 #pragma unroll
     for (int j = 0; j < GP_ITEMS; ++j) {
-        const int l = threadIdx.x + j * GP_THREADS;
-        if (l < rows) s_vals[l] = __ldcs(vals + base + l);
+        const unsigned l = threadIdx.x + j * GP_THREADS;
+        const int b = l < static_cast<unsigned>(rows) ? gp_region_of(s_start, l) : 0;
+        at[j] = s_goff[b] + l - s_start[b];
     }
+    unsigned long long v[GP_ITEMS];
+#pragma unroll
+    for (int j = 0; j < GP_ITEMS; ++j) v[j] = threadIdx.x + j * GP_THREADS < rows ? __ldcs(vals + at[j]) : 0ull;
+#pragma unroll
+    for (int j = 0; j < GP_ITEMS; ++j)
+        if (threadIdx.x + j * GP_THREADS < rows) s_vals[threadIdx.x + j * GP_THREADS] = v[j];
     __syncthreads();
+    const int64_t base = static_cast<int64_t>(blockIdx.x) * GP_TILE;
 #pragma unroll
     for (int j = 0; j < GP_ITEMS; ++j) {
         const int64_t r = base + j * GP_THREADS + threadIdx.x;
@@ -215,11 +238,11 @@ __global__ void __launch_bounds__(GP_THREADS) gp_restore_kernel(const unsigned l
 // The partitioned path pays when the source is well beyond L2 (2^26 rows, 512 MiB; at 2^25
 // rows the one-pass gather still hits L2 often enough) and the index rows are at least half
 // the source rows, so that each region line fetched into L2 is read about twice (with fewer,
-// the one-pass gather moves fewer DRAM bytes). Offsets within a region are u32 (at most 2^38
-// source rows).
+// the one-pass gather moves fewer DRAM bytes). Measured on GB300 at n = 2^28 index rows into
+// 2^28 source rows: 68 G rows/s against 45 G. Positions are u32: fewer than 2^32 index rows.
 static bool gather_partitions(uint64_t nsrc, int64_t n) {
     return nsrc >= (uint64_t(1) << 26) && nsrc <= (uint64_t(1) << 38) && n >= (int64_t(1) << 22) &&
-           2 * static_cast<uint64_t>(n) >= nsrc && n < (int64_t(1) << 40);
+           2 * static_cast<uint64_t>(n) >= nsrc && n < (int64_t(1) << 32);
 }
 
 static vkc_status gather_partitioned(vkc_ctx *ctx, const unsigned long long *src, uint64_t nsrc, const long long *idx,
@@ -228,22 +251,25 @@ static vkc_status gather_partitioned(vkc_ctx *ctx, const unsigned long long *src
     while ((uint64_t(1) << lg) < nsrc) ++lg;
     const int rb = lg - 6;  // GP_NB = 2^6 regions of 2^rb rows
     const int tiles = static_cast<int>((n + GP_TILE - 1) / GP_TILE);
-    const int chunks = (tiles + GP_TPB - 1) / GP_TPB;
-    const int64_t padded = static_cast<int64_t>(tiles) * GP_TILE;
+    const int64_t m = static_cast<int64_t>(GP_NB) * tiles;
     auto up = [](size_t b) { return (b + 255) & ~size_t(255); };
-    const size_t o_part = up(static_cast<size_t>(GP_NB) * tiles * 4), o_loc = o_part + up(padded * 4);
-    const size_t o_vals = o_loc + up(n * 2), total = o_vals + padded * 8;
+    const size_t o_offs = up(m * 4), o_sums = o_offs + up(m * 4);
+    const size_t o_part = o_sums + up(scan_counts_sum_words(m) * 4), o_loc = o_part + up(n * 4);
+    const size_t o_vals = o_loc + up(n * 2), total = o_vals + n * 8;
     void *p;
     vkc_status st = scratch(ctx, total, &p);
     if (st) return st;
     char *b = static_cast<char *>(p);
-    auto *cs = reinterpret_cast<unsigned *>(b);
+    auto *counts = reinterpret_cast<unsigned *>(b);
+    auto *offs = reinterpret_cast<unsigned *>(b + o_offs);
     auto *part = reinterpret_cast<unsigned *>(b + o_part);
     auto *loc = reinterpret_cast<unsigned short *>(b + o_loc);
     auto *vals = reinterpret_cast<unsigned long long *>(b + o_vals);
-    gp_partition_kernel<<<tiles, GP_THREADS, 0, ctx->stream>>>(idx, n, nsrc, rb, tiles, part, loc, cs, ctx->status);
-    gp_region_kernel<<<GP_NB * chunks, GP_THREADS, 0, ctx->stream>>>(src, part, cs, tiles, chunks, rb, vals);
-    gp_restore_kernel<<<tiles, GP_THREADS, 0, ctx->stream>>>(vals, loc, n, out);
+    gp_count_kernel<<<tiles, GP_THREADS, 0, ctx->stream>>>(idx, n, nsrc, rb, tiles, counts, ctx->status);
+    scan_counts(ctx, counts, m, reinterpret_cast<unsigned *>(b + o_sums), offs);
+    gp_partition_kernel<<<tiles, GP_THREADS, 0, ctx->stream>>>(idx, n, nsrc, rb, tiles, offs, part, loc);
+    gp_region_kernel<<<tiles, GP_THREADS, 0, ctx->stream>>>(src, part, counts, offs, tiles, rb, vals);
+    gp_restore_kernel<<<tiles, GP_THREADS, 0, ctx->stream>>>(vals, loc, counts, offs, n, tiles, out);
     return launched(ctx, "gather_partitioned");
 }
 

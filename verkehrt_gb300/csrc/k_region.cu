@@ -8,6 +8,7 @@
 //    divisor, more kernels or inputs than the evaluator holds), runs whole instead, kernel by
 //    kernel in post-order, which raises the error whole evaluation raises, as the reference
 //    does when its tiled run fails (region.rs:137-159);
+//  * `count` over a region counts the region's true rows as it evaluates them;
 //  * a fused root whose region matches one of the registry's fused patterns
 //    (src/kernels/scalar/fused.rs:286-379: dot_T, sumsq_T, count_<cmp>_T, condsum_<cmp>_T are
 //    declared there as those compositions) runs as that fused reduction over the pattern's
@@ -268,6 +269,23 @@ vkc_status vkc_region_reduce(vkc_ctx *ctx, int root, const int32_t *root_args, i
     RegionProg p;
     int64_t n;
     vkc_type t;
+    if (name_of(root) == "count" && args.size() == 1 && args[0].kernel) {
+        // count over a region: the rows counted as the region is evaluated, nothing stored.
+        const std::vector<vkc_region_kernel> sub = subtree(kernels, args[0].i);
+        if (plan_region(sub.data(), static_cast<int>(sub.size()), inputs, ninputs, &p, &n, &t) && t == VKC_BOOL) {
+            await_values(ctx, inputs, ninputs);
+            vkc_array *c;
+            if ((st = new_array(ctx, VKC_I64, 1, true, &c))) return st;
+            int64_t v = 0;
+            st = launch_region(ctx, p, n, c->data(), true);
+            if (!st) st = vkc_array_download(ctx, c, &v, 1);
+            vkc_array_release(c);
+            if (st) return st;
+            out->kind = VKC_VALUE_SCALAR;
+            out->scalar = scalar_i64(v);
+            return VKC_OK;
+        }
+    }
     int root2 = root;
     std::vector<Src> args2 = args;
     if (!plan_region(kernels, nkernels, inputs, ninputs, &p, &n, &t) ||

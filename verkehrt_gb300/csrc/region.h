@@ -48,7 +48,8 @@ struct RegionProg {
     RgOp op[RG_MAX_K];
 };
 
-// Runs `p` over n rows into `out` (the last kernel's rows) on the context's stream.
-vkc_status launch_region(vkc_ctx *ctx, const RegionProg &p, int64_t n, void *out);
+// Runs `p` over n rows into `out` (the last kernel's rows) on the context's stream; with
+// `count`, adds the number of nonzero result rows to the u64 at `out` instead.
+vkc_status launch_region(vkc_ctx *ctx, const RegionProg &p, int64_t n, void *out, bool count = false);
 
 }  // namespace vkc
