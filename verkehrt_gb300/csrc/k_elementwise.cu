@@ -376,7 +376,7 @@ __device__ __forceinline__ unsigned long long rg_eval(const RgOp &o, unsigned lo
     }
 }
 
-__device__ __forceinline__ unsigned long long rg_load(const RgIn &in, int64_t i) {
+__device__ __forceinline__ unsigned long long rg_load(const RgIn in, int64_t i) {
     switch (in.width) {
     case 8: return __ldcs(static_cast<const unsigned long long *>(in.p) + i);
     case 4: return __ldcs(static_cast<const unsigned *>(in.p) + i);
@@ -386,11 +386,12 @@ __device__ __forceinline__ unsigned long long rg_load(const RgIn &in, int64_t i)
 
 constexpr int RG_THREADS = 128, RG_ROWS = 4, RG_BLOCK_ROWS = RG_THREADS * RG_ROWS;
 
-// Slots live in shared memory, slot j of local row l at s_w[j * RG_BLOCK_ROWS + l]; a thread
-// touches only its own rows (t, t + 128, ...), so no barrier is needed. Each block takes
-// RG_BLOCK_ROWS rows per step: the inputs' loads of a step are in flight together.
-// COUNT: instead of storing the result rows, count the nonzero ones (a region under `count`)
-// into *out (an unsigned 64-bit counter).
+// Each block takes RG_BLOCK_ROWS rows per step, four per thread (t, t + 128, ...). A kernel's
+// operands come from the input arrays (loaded where the kernel needs them: an input that two
+// kernels read is read again from L1), constants, the previous kernel's value in registers, or
+// a shared-memory slot (a value that a kernel after the next one reads; a thread touches only
+// its own rows, so no barrier is needed). COUNT: instead of storing the result rows, count the
+// nonzero ones (a region under `count`) into *out (an unsigned 64-bit counter).
 template <bool COUNT>
 __global__ void __launch_bounds__(RG_THREADS) region_kernel(const RegionProg P, int64_t n, void *__restrict__ out) {
     extern __shared__ unsigned long long s_w[];
@@ -398,33 +399,43 @@ __global__ void __launch_bounds__(RG_THREADS) region_kernel(const RegionProg P, 
     unsigned long long nonzero = 0;
     for (int64_t b0 = static_cast<int64_t>(blockIdx.x) * RG_BLOCK_ROWS; b0 < n;
          b0 += static_cast<int64_t>(gridDim.x) * RG_BLOCK_ROWS) {
-        for (int j = 0; j < P.nin; ++j) {
-            const RgIn in = P.in[j];
-            unsigned long long v[RG_ROWS];
+        unsigned long long prev[RG_ROWS];
+        for (int k = 0; k < P.nk; ++k) {
+            const RgOp &o = P.op[k];
+            unsigned long long a[3][RG_ROWS];
 #pragma unroll
-            for (int r = 0; r < RG_ROWS; ++r) {
-                const int64_t i = b0 + t + r * RG_THREADS;
-                v[r] = !in.arr ? in.s : (i < n ? rg_load(in, i) : 0ull);
+            for (int j = 0; j < 3; ++j) {
+                const int kind = o.kind[j], idx = o.idx[j];
+                if (kind == RK_IN) {
+                    const RgIn in = P.in[idx];
+#pragma unroll
+                    for (int r = 0; r < RG_ROWS; ++r) {
+                        const int64_t i = b0 + t + r * RG_THREADS;
+                        a[j][r] = i < n ? rg_load(in, i) : 0ull;
+                    }
+                } else if (kind == RK_CONST) {
+#pragma unroll
+                    for (int r = 0; r < RG_ROWS; ++r) a[j][r] = o.c[j];
+                } else if (kind == RK_PREV) {
+#pragma unroll
+                    for (int r = 0; r < RG_ROWS; ++r) a[j][r] = prev[r];
+                } else {
+#pragma unroll
+                    for (int r = 0; r < RG_ROWS; ++r) a[j][r] = s_w[idx * RG_BLOCK_ROWS + t + r * RG_THREADS];
+                }
             }
 #pragma unroll
-            for (int r = 0; r < RG_ROWS; ++r) s_w[j * RG_BLOCK_ROWS + t + r * RG_THREADS] = v[r];
-        }
-        for (int k = 0; k < P.nk; ++k) {
-            const RgOp o = P.op[k];
-            unsigned long long *dst = s_w + (P.nin + k) * RG_BLOCK_ROWS + t;
-            const unsigned long long *a0 = s_w + o.a[0] * RG_BLOCK_ROWS + t;
-            const unsigned long long *a1 = s_w + o.a[1] * RG_BLOCK_ROWS + t;
-            const unsigned long long *a2 = s_w + o.a[2] * RG_BLOCK_ROWS + t;
+            for (int r = 0; r < RG_ROWS; ++r) prev[r] = rg_eval(o, a[0][r], a[1][r], a[2][r]);
+            if (o.keep) {
 #pragma unroll
-            for (int r = 0; r < RG_ROWS; ++r)
-                dst[r * RG_THREADS] = rg_eval(o, a0[r * RG_THREADS], a1[r * RG_THREADS], a2[r * RG_THREADS]);
+                for (int r = 0; r < RG_ROWS; ++r) s_w[o.slot * RG_BLOCK_ROWS + t + r * RG_THREADS] = prev[r];
+            }
         }
-        const unsigned long long *res = s_w + (P.nin + P.nk - 1) * RG_BLOCK_ROWS + t;
 #pragma unroll
         for (int r = 0; r < RG_ROWS; ++r) {
             const int64_t i = b0 + t + r * RG_THREADS;
             if (i >= n) break;
-            const unsigned long long w = res[r * RG_THREADS];
+            const unsigned long long w = prev[r];
             if (COUNT) {
                 nonzero += w != 0;
                 continue;
@@ -444,17 +455,18 @@ __global__ void __launch_bounds__(RG_THREADS) region_kernel(const RegionProg P, 
 
 vkc_status launch_region(vkc_ctx *ctx, const RegionProg &p, int64_t n, void *out, bool count) {
     if (n <= 0) return VKC_OK;
-    const size_t smem = static_cast<size_t>(p.nin + p.nk) * RG_BLOCK_ROWS * sizeof(unsigned long long);
+    const size_t smem = static_cast<size_t>(p.nslots) * RG_BLOCK_ROWS * sizeof(unsigned long long);
     static std::atomic<unsigned long long> configured{0};
     once_per_device(configured, ctx->device, [] {
-        const int most = static_cast<int>(RG_MAX_SLOTS * RG_BLOCK_ROWS * sizeof(unsigned long long));
+        const int most = static_cast<int>(RG_MAX_K * RG_BLOCK_ROWS * sizeof(unsigned long long));
         cudaFuncSetAttribute(region_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, most);
         cudaFuncSetAttribute(region_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, most);
     });
-    // Resident blocks: as many as the slots' shared memory allows, at most 16 a multiprocessor.
-    const int per_sm = std::max(1, std::min(16, static_cast<int>((200u << 10) / smem)));
+    int per_sm = 0;
+    if (count) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, region_kernel<true>, RG_THREADS, smem);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, region_kernel<false>, RG_THREADS, smem);
     const int64_t blocks = (n + RG_BLOCK_ROWS - 1) / RG_BLOCK_ROWS;
-    const int grid = static_cast<int>(std::min<int64_t>(blocks, static_cast<int64_t>(ctx->sms) * per_sm));
+    const int grid = static_cast<int>(std::min<int64_t>(blocks, static_cast<int64_t>(ctx->sms) * std::max(1, per_sm)));
     if (count) region_kernel<true><<<grid, RG_THREADS, smem, ctx->stream>>>(p, n, out);
     else region_kernel<false><<<grid, RG_THREADS, smem, ctx->stream>>>(p, n, out);
     return launched(ctx, "region");

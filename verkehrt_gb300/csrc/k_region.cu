@@ -54,7 +54,6 @@ bool plan_region(const vkc_region_kernel *ks, int nk, const vkc_value *in, int n
     if (nk > RG_MAX_K || nin > RG_MAX_IN || nk + nin > RG_MAX_SLOTS) return false;
     int64_t len = -1;
     memset(p, 0, sizeof *p);
-    p->nin = nin;
     p->nk = nk;
     for (int j = 0; j < nin; ++j) {
         const vkc_value &v = in[j];
@@ -62,15 +61,14 @@ bool plan_region(const vkc_region_kernel *ks, int nk, const vkc_value *in, int n
             if (!v.array) return false;
             if (len >= 0 && v.array->len != len) return false;  // a length mismatch somewhere
             len = v.array->len;
-            p->in[j] = RgIn{v.array->data(), 0, type_width(v.array->type), 1};
-        } else if (v.kind == VKC_VALUE_SCALAR) {
-            p->in[j] = RgIn{nullptr, v.scalar.bits, type_width(v.scalar.type), 0};
-        } else {
+            p->in[j] = RgIn{v.array->data(), type_width(v.array->type)};
+        } else if (v.kind != VKC_VALUE_SCALAR) {
             return false;
         }
     }
     if (len < 0) return false;
     std::vector<vkc_type> ty(static_cast<size_t>(nk));
+    std::vector<char> keep(static_cast<size_t>(nk), 0);
     for (int k = 0; k < nk; ++k) {
         const char *name = vkc_kernel_name(ks[k].kernel);
         const KernelDef *d = name ? kernel_def(name) : nullptr;
@@ -81,6 +79,7 @@ bool plan_region(const vkc_region_kernel *ks, int nk, const vkc_value *in, int n
         o.fn = static_cast<unsigned char>(d->ew_fn);
         o.ty = static_cast<unsigned char>(d->ew_ty);
         o.dst = static_cast<unsigned char>(d->ew_dst);
+        for (int j = 0; j < 3; ++j) o.kind[j] = RK_CONST;  // unused operands read 0
         for (int j = 0; j < ks[k].nargs; ++j) {
             const Src s = src_of(ks[k].args[j]);
             const bool arr = s.kernel || in[s.i].kind == VKC_VALUE_ARRAY;
@@ -88,13 +87,34 @@ bool plan_region(const vkc_region_kernel *ks, int nk, const vkc_value *in, int n
             const InSpec &spec = d->inputs[static_cast<size_t>(j)];
             if (t != spec.type || (spec.kind == IN_SCALAR && arr) || (spec.kind == IN_ARRAY && !arr)) return false;
             any_array |= arr;
-            o.a[j] = static_cast<unsigned char>(s.kernel ? nin + s.i : s.i);
+            if (!s.kernel) {
+                o.kind[j] = arr ? RK_IN : RK_CONST;
+                o.idx[j] = static_cast<unsigned char>(s.i);
+                o.c[j] = arr ? 0 : in[s.i].scalar.bits;
+            } else if (s.i == k - 1) {
+                o.kind[j] = RK_PREV;
+            } else {
+                o.kind[j] = RK_SLOT;
+                o.idx[j] = static_cast<unsigned char>(s.i);  // a kernel; its slot below
+                keep[static_cast<size_t>(s.i)] = 1;
+            }
         }
         if (!any_array) return false;  // "an array kernel needs an array operand"
         if (d->ew_fn == EF_DIVC && !make_ew_divider(d->ew_ty, in[src_of(ks[k].args[1]).i].scalar.bits, &o.dv))
             return false;  // division by zero
         ty[static_cast<size_t>(k)] = d->out_type;
     }
+    // Slots of the kept values, in kernel order.
+    std::vector<int> slot(static_cast<size_t>(nk), -1);
+    for (int k = 0; k < nk; ++k)
+        if (keep[static_cast<size_t>(k)]) {
+            slot[static_cast<size_t>(k)] = p->nslots++;
+            p->op[k].keep = 1;
+            p->op[k].slot = static_cast<unsigned char>(slot[static_cast<size_t>(k)]);
+        }
+    for (int k = 0; k < nk; ++k)
+        for (int j = 0; j < 3; ++j)
+            if (p->op[k].kind[j] == RK_SLOT) p->op[k].idx[j] = static_cast<unsigned char>(slot[p->op[k].idx[j]]);
     *out_type = ty.back();
     p->out_width = type_width(*out_type);
     *n = len;

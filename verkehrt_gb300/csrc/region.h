@@ -31,19 +31,24 @@ constexpr int RG_MAX_K = 12;      // region kernels
 constexpr int RG_MAX_SLOTS = 16;  // inputs + kernels
 
 struct RgIn {
-    const void *p;          // array rows, or nullptr for a scalar splat
-    unsigned long long s;   // the scalar's bits
-    int width;              // bytes per row
-    int arr;
+    const void *p;  // array rows
+    int width;      // bytes per row
 };
-// Kernel k of the region writes slot nin + k from the slots a[0..2] (inputs are slots
-// 0..nin-1).
+// Where an operand comes from: an array input (idx), a constant (a scalar input, or an unused
+// operand), the previous kernel's value (held in registers), or the shared-memory slot of an
+// earlier kernel whose value a later kernel reads (idx).
+enum RgKind { RK_IN, RK_CONST, RK_PREV, RK_SLOT };
+// Kernel k of the region: operation, operand type, result type, the three operands, and the
+// slot its value is kept in when a kernel after the next one reads it.
 struct RgOp {
-    unsigned char fn, ty, dst, a[3];
+    unsigned char fn, ty, dst;
+    unsigned char kind[3], idx[3];
+    unsigned char keep, slot;
+    unsigned long long c[3];
     Divider dv;
 };
 struct RegionProg {
-    int nin, nk, out_width;
+    int nk, nslots, out_width;
     RgIn in[RG_MAX_IN];
     RgOp op[RG_MAX_K];
 };
