@@ -386,9 +386,9 @@ __device__ __forceinline__ unsigned long long rg_load(const RgIn in, int64_t i) 
 
 constexpr int RG_THREADS = 128, RG_ROWS = 4, RG_BLOCK_ROWS = RG_THREADS * RG_ROWS;
 
-// Each block takes RG_BLOCK_ROWS rows per step, four per thread (t, t + 128, ...). A kernel's
-// operands come from the input arrays (loaded where the kernel needs them: an input that two
-// kernels read is read again from L1), constants, the previous kernel's value in registers, or
+// Each block takes RG_BLOCK_ROWS rows per step, four per thread (t, t + 128, ...), and loads
+// every array input's rows of the step first. A kernel's operands come from those inputs,
+// constants, the previous kernel's value in registers, or
 // a shared-memory slot (a value that a kernel after the next one reads; a thread touches only
 // its own rows, so no barrier is needed). COUNT: instead of storing the result rows, count the
 // nonzero ones (a region under `count`) into *out (an unsigned 64-bit counter).
@@ -399,6 +399,17 @@ __global__ void __launch_bounds__(RG_THREADS) region_kernel(const RegionProg P, 
     unsigned long long nonzero = 0;
     for (int64_t b0 = static_cast<int64_t>(blockIdx.x) * RG_BLOCK_ROWS; b0 < n;
          b0 += static_cast<int64_t>(gridDim.x) * RG_BLOCK_ROWS) {
+        // Every array input's rows of the step, all loads in flight together.
+        unsigned long long inv[RG_MAX_ARR][RG_ROWS];
+#pragma unroll
+        for (int j = 0; j < RG_MAX_ARR; ++j) {
+            const RgIn in = P.in[j];
+#pragma unroll
+            for (int r = 0; r < RG_ROWS; ++r) {
+                const int64_t i = b0 + t + r * RG_THREADS;
+                inv[j][r] = (in.p && i < n) ? rg_load(in, i) : 0ull;
+            }
+        }
         unsigned long long prev[RG_ROWS];
         for (int k = 0; k < P.nk; ++k) {
             const RgOp &o = P.op[k];
@@ -407,11 +418,14 @@ __global__ void __launch_bounds__(RG_THREADS) region_kernel(const RegionProg P, 
             for (int j = 0; j < 3; ++j) {
                 const int kind = o.kind[j], idx = o.idx[j];
                 if (kind == RK_IN) {
-                    const RgIn in = P.in[idx];
-#pragma unroll
-                    for (int r = 0; r < RG_ROWS; ++r) {
-                        const int64_t i = b0 + t + r * RG_THREADS;
-                        a[j][r] = i < n ? rg_load(in, i) : 0ull;
+                    // A uniform branch per input keeps the register array statically indexed.
+                    switch (idx) {
+#define RG_IN_CASE(q)                                                \
+    case q:                                                          \
+        for (int r = 0; r < RG_ROWS; ++r) a[j][r] = inv[q][r];       \
+        break;
+                        RG_IN_CASE(0) RG_IN_CASE(1) RG_IN_CASE(2) default: RG_IN_CASE(3)
+#undef RG_IN_CASE
                     }
                 } else if (kind == RK_CONST) {
 #pragma unroll

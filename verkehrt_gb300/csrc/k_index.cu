@@ -235,90 +235,6 @@ __global__ void __launch_bounds__(GP_THREADS) gp_restore_kernel(const unsigned l
     }
 }
 
-// Fixed-capacity form: region b owns positions [b * cap, (b + 1) * cap) with cap a little
-// above the region's expected share of the rows, so a tile learns where its runs go from one
-// atomicAdd per region on a fill counter: no count pass and no scan (8 DRAM bytes a row and two
-// launches fewer). A region that would overflow its capacity (indices far from uniform) sets
-// fill[GP_NB]; the host then runs the four-pass form instead. Counts, bounds and offsets are
-// recorded as the count pass and the scan would have.
-__global__ void __launch_bounds__(GP_THREADS) gpf_partition_kernel(const long long *__restrict__ idx, int64_t n,
-                                                                   uint64_t nsrc, int rb, int tiles, unsigned cap,
-                                                                   unsigned *__restrict__ fill,
-                                                                   unsigned *__restrict__ counts,
-                                                                   unsigned *__restrict__ offs,
-                                                                   unsigned *__restrict__ part,
-                                                                   unsigned short *__restrict__ loc,
-                                                                   DevStatus *status) {
-    __shared__ unsigned s_cnt[GP_NB], s_start[GP_NB + 1], s_goff[GP_NB];
-    __shared__ unsigned s_part[GP_TILE];
-    __shared__ unsigned char s_reg[GP_TILE];
-    if (threadIdx.x < GP_NB) s_cnt[threadIdx.x] = 0;
-    __syncthreads();
-    const int64_t base = static_cast<int64_t>(blockIdx.x) * GP_TILE;
-    const unsigned long long mask = (1ull << rb) - 1;
-    unsigned long long k[GP_ITEMS];
-    unsigned rk[GP_ITEMS];
-#pragma unroll
-    for (int j = 0; j < GP_ITEMS; ++j) {
-        const int64_t r = base + j * GP_THREADS + threadIdx.x;
-        k[j] = r < n ? static_cast<unsigned long long>(__ldcs(idx + r)) : ~0ull;  // past the end: no slot
-        if (r < n && k[j] >= nsrc) atomicMin(&status->first_bad, static_cast<unsigned long long>(r));
-    }
-#pragma unroll
-    for (int j = 0; j < GP_ITEMS; ++j) rk[j] = k[j] < nsrc ? atomicAdd(&s_cnt[static_cast<unsigned>(k[j] >> rb)], 1u) : 0u;
-    __syncthreads();
-    if (threadIdx.x < 32) gp_starts([&](int b) { return s_cnt[b]; }, s_start);
-    if (threadIdx.x < GP_NB) {
-        const unsigned c = s_cnt[threadIdx.x];
-        const unsigned at = c ? atomicAdd(&fill[threadIdx.x], c) : 0u;
-        const bool over = at + c > cap;  // at and c are below 2^32 / GP_NB: no wrap
-        if (over) atomicOr(&fill[GP_NB], 1u);
-        s_goff[threadIdx.x] = over ? ~0u : threadIdx.x * cap + at;
-        counts[static_cast<int64_t>(threadIdx.x) * tiles + blockIdx.x] = c;
-        offs[static_cast<int64_t>(threadIdx.x) * tiles + blockIdx.x] = over ? 0u : threadIdx.x * cap + at;
-    }
-    __syncthreads();
-#pragma unroll
-    for (int j = 0; j < GP_ITEMS; ++j) {
-        const int64_t r = base + j * GP_THREADS + threadIdx.x;
-        if (r >= n) continue;
-        if (k[j] < nsrc) {
-            const unsigned b = static_cast<unsigned>(k[j] >> rb);
-            const unsigned l = s_start[b] + rk[j];
-            loc[r] = static_cast<unsigned short>(l);
-            s_part[l] = static_cast<unsigned>(k[j] & mask);
-            s_reg[l] = static_cast<unsigned char>(b);
-        } else {
-            loc[r] = 0;  // the call fails; the row's output is never read
-        }
-    }
-    __syncthreads();
-    const int rows = static_cast<int>(s_start[GP_NB]);
-    for (int l = threadIdx.x; l < rows; l += GP_THREADS) {
-        const unsigned b = s_reg[l];
-        if (s_goff[b] != ~0u) part[s_goff[b] + static_cast<unsigned>(l) - s_start[b]] = s_part[l];
-    }
-}
-
-// Region b's filled positions, one block per GP_TILE of them (bpr blocks per region, region-major).
-__global__ void __launch_bounds__(GP_THREADS) gpf_region_kernel(const unsigned long long *__restrict__ src,
-                                                                const unsigned *__restrict__ part,
-                                                                const unsigned *__restrict__ fill, unsigned cap,
-                                                                int bpr, int rb,
-                                                                unsigned long long *__restrict__ vals) {
-    const int b = blockIdx.x / bpr;
-    const unsigned q0 = static_cast<unsigned>(blockIdx.x - b * bpr) * GP_TILE;
-    const unsigned filled = min(fill[b], cap);
-    if (q0 >= filled) return;
-    const unsigned long long *reg = src + (static_cast<int64_t>(b) << rb);
-    const int64_t p0 = static_cast<int64_t>(b) * cap + q0;
-#pragma unroll 4
-    for (int j = 0; j < GP_ITEMS; ++j) {
-        const unsigned q = q0 + j * GP_THREADS + threadIdx.x;
-        if (q < filled) vals[p0 + j * GP_THREADS + threadIdx.x] = __ldg(reg + __ldcs(part + p0 + j * GP_THREADS + threadIdx.x));
-    }
-}
-
 // The partitioned path pays when the source is well beyond L2 (2^26 rows, 512 MiB; at 2^25
 // rows the one-pass gather still hits L2 often enough) and the index rows are at least half
 // the source rows, so that each region line fetched into L2 is read about twice (with fewer,
@@ -329,55 +245,8 @@ static bool gather_partitions(uint64_t nsrc, int64_t n) {
            2 * static_cast<uint64_t>(n) >= nsrc && n < (int64_t(1) << 32);
 }
 
-// The fixed-capacity form; *fell_back when a region overflowed (nothing written to `out`).
-static vkc_status gather_fixed(vkc_ctx *ctx, const unsigned long long *src, uint64_t nsrc, const long long *idx,
-                               int64_t n, unsigned long long *out, bool *fell_back) {
-    *fell_back = true;
-    int lg = 0;
-    while ((uint64_t(1) << lg) < nsrc) ++lg;
-    const int rb = lg - 6;
-    const int tiles = static_cast<int>((n + GP_TILE - 1) / GP_TILE);
-    const int64_t m = static_cast<int64_t>(GP_NB) * tiles;
-    // A region's expected share is n 2^rb / nsrc rows; 1/16 more, in whole tiles.
-    const double share = static_cast<double>(n) * static_cast<double>(uint64_t(1) << rb) / static_cast<double>(nsrc);
-    const int64_t cap64 = (static_cast<int64_t>(share * 1.0625) / GP_TILE + 2) * GP_TILE;
-    if (cap64 * GP_NB >= (int64_t(1) << 32)) return VKC_OK;  // u32 positions
-    const unsigned cap = static_cast<unsigned>(cap64);
-    const int64_t npos = cap64 * GP_NB;
-    auto up = [](size_t b) { return (b + 255) & ~size_t(255); };
-    const size_t o_offs = up(m * 4), o_fill = o_offs + up(m * 4), o_part = o_fill + up((GP_NB + 1) * 4);
-    const size_t o_loc = o_part + up(npos * 4), o_vals = o_loc + up(n * 2), total = o_vals + npos * 8;
-    void *p;
-    vkc_status st = scratch(ctx, total, &p);
-    if (st) return st;
-    char *b = static_cast<char *>(p);
-    auto *counts = reinterpret_cast<unsigned *>(b);
-    auto *offs = reinterpret_cast<unsigned *>(b + o_offs);
-    auto *fill = reinterpret_cast<unsigned *>(b + o_fill);
-    auto *part = reinterpret_cast<unsigned *>(b + o_part);
-    auto *loc = reinterpret_cast<unsigned short *>(b + o_loc);
-    auto *vals = reinterpret_cast<unsigned long long *>(b + o_vals);
-    VKC_CUDA(ctx, cudaMemsetAsync(fill, 0, (GP_NB + 1) * sizeof(unsigned), ctx->stream));
-    gpf_partition_kernel<<<tiles, GP_THREADS, 0, ctx->stream>>>(idx, n, nsrc, rb, tiles, cap, fill, counts, offs,
-                                                                part, loc, ctx->status);
-    if ((st = launched(ctx, "gather_partition"))) return st;
-    unsigned *h;
-    if ((st = pinned(ctx, sizeof(unsigned), reinterpret_cast<void **>(&h)))) return st;
-    VKC_CUDA(ctx, cudaMemcpyAsync(h, fill + GP_NB, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream));
-    VKC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    if (*h) return VKC_OK;  // a region overflowed
-    *fell_back = false;
-    const int bpr = static_cast<int>(cap64 / GP_TILE);
-    gpf_region_kernel<<<GP_NB * bpr, GP_THREADS, 0, ctx->stream>>>(src, part, fill, cap, bpr, rb, vals);
-    gp_restore_kernel<<<tiles, GP_THREADS, 0, ctx->stream>>>(vals, loc, counts, offs, n, tiles, out);
-    return launched(ctx, "gather_partitioned");
-}
-
 static vkc_status gather_partitioned(vkc_ctx *ctx, const unsigned long long *src, uint64_t nsrc, const long long *idx,
                                      int64_t n, unsigned long long *out) {
-    bool fell_back;
-    vkc_status st = gather_fixed(ctx, src, nsrc, idx, n, out, &fell_back);
-    if (st || !fell_back) return st;
     int lg = 0;
     while ((uint64_t(1) << lg) < nsrc) ++lg;
     const int rb = lg - 6;  // GP_NB = 2^6 regions of 2^rb rows
@@ -388,7 +257,7 @@ static vkc_status gather_partitioned(vkc_ctx *ctx, const unsigned long long *src
     const size_t o_part = o_sums + up(scan_counts_sum_words(m) * 4), o_loc = o_part + up(n * 4);
     const size_t o_vals = o_loc + up(n * 2), total = o_vals + n * 8;
     void *p;
-    st = scratch(ctx, total, &p);
+    vkc_status st = scratch(ctx, total, &p);
     if (st) return st;
     char *b = static_cast<char *>(p);
     auto *counts = reinterpret_cast<unsigned *>(b);

@@ -61,12 +61,20 @@ bool plan_region(const vkc_region_kernel *ks, int nk, const vkc_value *in, int n
             if (!v.array) return false;
             if (len >= 0 && v.array->len != len) return false;  // a length mismatch somewhere
             len = v.array->len;
-            p->in[j] = RgIn{v.array->data(), type_width(v.array->type)};
         } else if (v.kind != VKC_VALUE_SCALAR) {
             return false;
         }
     }
     if (len < 0) return false;
+    // The array inputs in input order, at most RG_MAX_ARR.
+    std::vector<int> arr_no(static_cast<size_t>(nin), -1);
+    int narr = 0;
+    for (int j = 0; j < nin; ++j)
+        if (in[j].kind == VKC_VALUE_ARRAY) {
+            if (narr == RG_MAX_ARR) return false;
+            arr_no[static_cast<size_t>(j)] = narr;
+            p->in[narr++] = RgIn{in[j].array->data(), type_width(in[j].array->type)};
+        }
     std::vector<vkc_type> ty(static_cast<size_t>(nk));
     std::vector<char> keep(static_cast<size_t>(nk), 0);
     for (int k = 0; k < nk; ++k) {
@@ -89,7 +97,7 @@ bool plan_region(const vkc_region_kernel *ks, int nk, const vkc_value *in, int n
             any_array |= arr;
             if (!s.kernel) {
                 o.kind[j] = arr ? RK_IN : RK_CONST;
-                o.idx[j] = static_cast<unsigned char>(s.i);
+                o.idx[j] = static_cast<unsigned char>(arr ? arr_no[static_cast<size_t>(s.i)] : 0);
                 o.c[j] = arr ? 0 : in[s.i].scalar.bits;
             } else if (s.i == k - 1) {
                 o.kind[j] = RK_PREV;

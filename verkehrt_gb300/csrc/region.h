@@ -27,6 +27,7 @@ struct Divider {
 bool make_ew_divider(int ty, unsigned long long d, Divider *out);
 
 constexpr int RG_MAX_IN = 8;      // region inputs
+constexpr int RG_MAX_ARR = 4;     // of which arrays (held in registers, one step's rows each)
 constexpr int RG_MAX_K = 12;      // region kernels
 constexpr int RG_MAX_SLOTS = 16;  // inputs + kernels
 
@@ -34,7 +35,7 @@ struct RgIn {
     const void *p;  // array rows
     int width;      // bytes per row
 };
-// Where an operand comes from: an array input (idx), a constant (a scalar input, or an unused
+// Where an operand comes from: an array input (idx, its number among the arrays), a constant (a scalar input, or an unused
 // operand), the previous kernel's value (held in registers), or the shared-memory slot of an
 // earlier kernel whose value a later kernel reads (idx).
 enum RgKind { RK_IN, RK_CONST, RK_PREV, RK_SLOT };
@@ -49,7 +50,7 @@ struct RgOp {
 };
 struct RegionProg {
     int nk, nslots, out_width;
-    RgIn in[RG_MAX_IN];
+    RgIn in[RG_MAX_ARR];  // the array inputs, numbered in input order
     RgOp op[RG_MAX_K];
 };
 
