@@ -319,60 +319,82 @@ template <class T> __device__ __forceinline__ unsigned long long to_word(T v) {
     return w;
 }
 
-template <class S> __device__ __forceinline__ unsigned long long rg_cast(int dst, S x) {
-    switch (dst) {
-    case ET_F64: return to_word(CastAs<S, double>::f(x));
-    case ET_F32: return to_word(CastAs<S, float>::f(x));
-    case ET_I64: return to_word(CastAs<S, long long>::f(x));
-    case ET_U64: return to_word(CastAs<S, unsigned long long>::f(x));
-    case ET_I32: return to_word(CastAs<S, int>::f(x));
-    default: return to_word(CastAs<S, unsigned char>::f(x));
+constexpr int RG_THREADS = 128, RG_ROWS = 4, RG_BLOCK_ROWS = RG_THREADS * RG_ROWS;
+
+// One kernel of a region over a thread's RG_ROWS rows: the operation is chosen once (uniform
+// branches), then the rows run through it.
+#define RG_EACH(EXPR)                                      \
+    {                                                      \
+        _Pragma("unroll") for (int r = 0; r < RG_ROWS; ++r) { \
+            const T x = from_word<T>(a[0][r]);             \
+            const T y = from_word<T>(a[1][r]);             \
+            (void)x;                                       \
+            (void)y;                                       \
+            out[r] = (EXPR);                               \
+        }                                                  \
+        return;                                            \
     }
-}
 
 template <class T>
-__device__ __forceinline__ unsigned long long rg_typed(const RgOp &o, unsigned long long a, unsigned long long b,
-                                                    unsigned long long c) {
+__device__ __forceinline__ void rg_typed(const RgOp &o, const unsigned long long (&a)[3][RG_ROWS],
+                                         unsigned long long (&out)[RG_ROWS]) {
     constexpr bool FL = std::is_floating_point<T>::value;
-    const T x = from_word<T>(a), y = from_word<T>(b);
+    constexpr bool SG = FL || std::is_signed<T>::value;
     switch (o.fn) {
-    case EF_ADD: return to_word(ew_add(x, y));
-    case EF_SUB: return to_word(ew_sub(x, y));
-    case EF_MUL: return to_word(ew_mul(x, y));
-    case EF_MIN: return to_word(ew_min(x, y));
-    case EF_MAX: return to_word(ew_max(x, y));
-    case EF_LT: return x < y;
-    case EF_LE: return x <= y;
-    case EF_GT: return x > y;
-    case EF_GE: return x >= y;
-    case EF_EQ: return x == y;
-    case EF_NE: return x != y;
-    case EF_SELECT: return (a & 0xffu) ? b : c;  // select(mask, a, b): the mask is the first operand
-    case EF_CAST: return rg_cast<T>(o.dst, x);
-    case EF_NEG: if constexpr (FL || std::is_signed<T>::value) return to_word(ew_neg(x)); break;
-    case EF_ABS: if constexpr (FL || std::is_signed<T>::value) return to_word(ew_abs(x)); break;
-    case EF_DIV: if constexpr (FL) return to_word(ew_div(x, y)); break;
-    case EF_SQRT: if constexpr (FL) return to_word(ew_sqrt(x)); break;
-    case EF_AND: if constexpr (!FL) return to_word(static_cast<T>(x & y)); break;
-    case EF_OR: if constexpr (!FL) return to_word(static_cast<T>(x | y)); break;
-    case EF_XOR: if constexpr (!FL) return to_word(static_cast<T>(x ^ y)); break;
-    case EF_NOT: if constexpr (!FL) return to_word(static_cast<T>(~x)); break;
-    case EF_BNOT: return a ^ 1u;
-    case EF_DIVC: if constexpr (!FL) return to_word(ew_div_const<T>(x, o.dv)); break;
+    case EF_ADD: RG_EACH(to_word(ew_add(x, y)))
+    case EF_SUB: RG_EACH(to_word(ew_sub(x, y)))
+    case EF_MUL: RG_EACH(to_word(ew_mul(x, y)))
+    case EF_MIN: RG_EACH(to_word(ew_min(x, y)))
+    case EF_MAX: RG_EACH(to_word(ew_max(x, y)))
+    case EF_LT: RG_EACH(static_cast<unsigned long long>(x < y))
+    case EF_LE: RG_EACH(static_cast<unsigned long long>(x <= y))
+    case EF_GT: RG_EACH(static_cast<unsigned long long>(x > y))
+    case EF_GE: RG_EACH(static_cast<unsigned long long>(x >= y))
+    case EF_EQ: RG_EACH(static_cast<unsigned long long>(x == y))
+    case EF_NE: RG_EACH(static_cast<unsigned long long>(x != y))
+    // select(mask, a, b): the mask is the first operand.
+    case EF_SELECT: RG_EACH((a[0][r] & 0xffu) ? a[1][r] : a[2][r])
+    case EF_BNOT: RG_EACH(a[0][r] ^ 1u)
+    case EF_CAST:
+        switch (o.dst) {
+        case ET_F64: RG_EACH(to_word(CastAs<T, double>::f(x)))
+        case ET_F32: RG_EACH(to_word(CastAs<T, float>::f(x)))
+        case ET_I64: RG_EACH(to_word(CastAs<T, long long>::f(x)))
+        case ET_U64: RG_EACH(to_word(CastAs<T, unsigned long long>::f(x)))
+        case ET_I32: RG_EACH(to_word(CastAs<T, int>::f(x)))
+        default: RG_EACH(to_word(CastAs<T, unsigned char>::f(x)))
+        }
     default: break;
     }
-    return 0;
+    if constexpr (SG) {
+        if (o.fn == EF_NEG) RG_EACH(to_word(ew_neg(x)))
+        if (o.fn == EF_ABS) RG_EACH(to_word(ew_abs(x)))
+    }
+    if constexpr (FL) {
+        if (o.fn == EF_DIV) RG_EACH(to_word(ew_div(x, y)))
+        if (o.fn == EF_SQRT) RG_EACH(to_word(ew_sqrt(x)))
+    }
+    if constexpr (!FL) {
+        if (o.fn == EF_AND) RG_EACH(to_word(static_cast<T>(x & y)))
+        if (o.fn == EF_OR) RG_EACH(to_word(static_cast<T>(x | y)))
+        if (o.fn == EF_XOR) RG_EACH(to_word(static_cast<T>(x ^ y)))
+        if (o.fn == EF_NOT) RG_EACH(to_word(static_cast<T>(~x)))
+        if (o.fn == EF_DIVC) RG_EACH(to_word(ew_div_const<T>(x, o.dv)))
+    }
+#pragma unroll
+    for (int r = 0; r < RG_ROWS; ++r) out[r] = 0;
 }
+#undef RG_EACH
 
-__device__ __forceinline__ unsigned long long rg_eval(const RgOp &o, unsigned long long a, unsigned long long b,
-                                                      unsigned long long c) {
+__device__ __forceinline__ void rg_eval(const RgOp &o, const unsigned long long (&a)[3][RG_ROWS],
+                                        unsigned long long (&out)[RG_ROWS]) {
     switch (o.ty) {
-    case ET_F64: return rg_typed<double>(o, a, b, c);
-    case ET_F32: return rg_typed<float>(o, a, b, c);
-    case ET_I64: return rg_typed<long long>(o, a, b, c);
-    case ET_U64: return rg_typed<unsigned long long>(o, a, b, c);
-    case ET_I32: return rg_typed<int>(o, a, b, c);
-    default: return rg_typed<unsigned char>(o, a, b, c);
+    case ET_F64: rg_typed<double>(o, a, out); return;
+    case ET_F32: rg_typed<float>(o, a, out); return;
+    case ET_I64: rg_typed<long long>(o, a, out); return;
+    case ET_U64: rg_typed<unsigned long long>(o, a, out); return;
+    case ET_I32: rg_typed<int>(o, a, out); return;
+    default: rg_typed<unsigned char>(o, a, out); return;
     }
 }
 
@@ -383,8 +405,6 @@ __device__ __forceinline__ unsigned long long rg_load(const RgIn in, int64_t i) 
     default: return __ldcs(static_cast<const unsigned char *>(in.p) + i);
     }
 }
-
-constexpr int RG_THREADS = 128, RG_ROWS = 4, RG_BLOCK_ROWS = RG_THREADS * RG_ROWS;
 
 // Each block takes RG_BLOCK_ROWS rows per step, four per thread (t, t + 128, ...), and loads
 // every array input's rows of the step first. A kernel's operands come from those inputs,
@@ -438,8 +458,7 @@ __global__ void __launch_bounds__(RG_THREADS) region_kernel(const RegionProg P, 
                     for (int r = 0; r < RG_ROWS; ++r) a[j][r] = s_w[idx * RG_BLOCK_ROWS + t + r * RG_THREADS];
                 }
             }
-#pragma unroll
-            for (int r = 0; r < RG_ROWS; ++r) prev[r] = rg_eval(o, a[0][r], a[1][r], a[2][r]);
+            rg_eval(o, a, prev);
             if (o.keep) {
 #pragma unroll
                 for (int r = 0; r < RG_ROWS; ++r) s_w[o.slot * RG_BLOCK_ROWS + t + r * RG_THREADS] = prev[r];
