@@ -398,91 +398,120 @@ __device__ __forceinline__ void rg_eval(const RgOp &o, const unsigned long long 
     }
 }
 
-__device__ __forceinline__ unsigned long long rg_load(const RgIn in, int64_t i) {
+// Loads input j's rows of the step (FULL: the step lies inside the array, no row checks).
+template <bool FULL>
+__device__ __forceinline__ void rg_load_rows(const RgIn in, int64_t base, int64_t n, unsigned long long (&v)[RG_ROWS]) {
     switch (in.width) {
-    case 8: return __ldcs(static_cast<const unsigned long long *>(in.p) + i);
-    case 4: return __ldcs(static_cast<const unsigned *>(in.p) + i);
-    default: return __ldcs(static_cast<const unsigned char *>(in.p) + i);
+    case 8: {
+        const unsigned long long *q = static_cast<const unsigned long long *>(in.p) + base;
+#pragma unroll
+        for (int r = 0; r < RG_ROWS; ++r) v[r] = (FULL || base + r * RG_THREADS < n) ? __ldcs(q + r * RG_THREADS) : 0ull;
+        break;
+    }
+    case 4: {
+        const unsigned *q = static_cast<const unsigned *>(in.p) + base;
+#pragma unroll
+        for (int r = 0; r < RG_ROWS; ++r) v[r] = (FULL || base + r * RG_THREADS < n) ? __ldcs(q + r * RG_THREADS) : 0u;
+        break;
+    }
+    default: {
+        const unsigned char *q = static_cast<const unsigned char *>(in.p) + base;
+#pragma unroll
+        for (int r = 0; r < RG_ROWS; ++r) v[r] = (FULL || base + r * RG_THREADS < n) ? __ldcs(q + r * RG_THREADS) : 0u;
+        break;
+    }
+    }
+}
+
+// One step of RG_BLOCK_ROWS rows from row b0: the thread's rows b0 + t + 128 r.
+template <bool COUNT, bool FULL>
+__device__ __forceinline__ void region_step(const RegionProg &P, int64_t b0, int64_t n, void *__restrict__ out,
+                                            unsigned long long *s_w, unsigned long long &nonzero) {
+    const int t = threadIdx.x;
+    const int64_t base = b0 + t;
+    // Every array input's rows of the step, all loads in flight together.
+    unsigned long long inv[RG_MAX_ARR][RG_ROWS];
+#pragma unroll
+    for (int j = 0; j < RG_MAX_ARR; ++j)
+        if (j < P.narr) rg_load_rows<FULL>(P.in[j], base, n, inv[j]);
+    unsigned long long prev[RG_ROWS];
+    for (int k = 0; k < P.nk; ++k) {
+        const RgOp &o = P.op[k];
+        unsigned long long a[3][RG_ROWS];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            const int kind = o.kind[j], idx = o.idx[j];
+            if (kind == RK_IN) {
+                // A uniform branch per input keeps the register array statically indexed.
+                switch (idx) {
+#define RG_IN_CASE(q)                                                          \
+    case q:                                                                    \
+        _Pragma("unroll") for (int r = 0; r < RG_ROWS; ++r) a[j][r] = inv[q][r]; \
+        break;
+                    RG_IN_CASE(0) RG_IN_CASE(1) RG_IN_CASE(2) default: RG_IN_CASE(3)
+#undef RG_IN_CASE
+                }
+            } else if (kind == RK_CONST) {
+#pragma unroll
+                for (int r = 0; r < RG_ROWS; ++r) a[j][r] = o.c[j];
+            } else if (kind == RK_PREV) {
+#pragma unroll
+                for (int r = 0; r < RG_ROWS; ++r) a[j][r] = prev[r];
+            } else {
+#pragma unroll
+                for (int r = 0; r < RG_ROWS; ++r) a[j][r] = s_w[idx * RG_BLOCK_ROWS + t + r * RG_THREADS];
+            }
+        }
+        rg_eval(o, a, prev);
+        if (o.keep) {
+#pragma unroll
+            for (int r = 0; r < RG_ROWS; ++r) s_w[o.slot * RG_BLOCK_ROWS + t + r * RG_THREADS] = prev[r];
+        }
+    }
+    if (COUNT) {
+#pragma unroll
+        for (int r = 0; r < RG_ROWS; ++r)
+            if (FULL || base + r * RG_THREADS < n) nonzero += prev[r] != 0;
+        return;
+    }
+    switch (P.out_width) {
+    case 8:
+#pragma unroll
+        for (int r = 0; r < RG_ROWS; ++r)
+            if (FULL || base + r * RG_THREADS < n) static_cast<unsigned long long *>(out)[base + r * RG_THREADS] = prev[r];
+        break;
+    case 4:
+#pragma unroll
+        for (int r = 0; r < RG_ROWS; ++r)
+            if (FULL || base + r * RG_THREADS < n) static_cast<unsigned *>(out)[base + r * RG_THREADS] = static_cast<unsigned>(prev[r]);
+        break;
+    default:
+#pragma unroll
+        for (int r = 0; r < RG_ROWS; ++r)
+            if (FULL || base + r * RG_THREADS < n)
+                static_cast<unsigned char *>(out)[base + r * RG_THREADS] = static_cast<unsigned char>(prev[r]);
+        break;
     }
 }
 
 // Each block takes RG_BLOCK_ROWS rows per step, four per thread (t, t + 128, ...), and loads
 // every array input's rows of the step first. A kernel's operands come from those inputs,
-// constants, the previous kernel's value in registers, or
-// a shared-memory slot (a value that a kernel after the next one reads; a thread touches only
-// its own rows, so no barrier is needed). COUNT: instead of storing the result rows, count the
-// nonzero ones (a region under `count`) into *out (an unsigned 64-bit counter).
+// constants, the previous kernel's value in registers, or a shared-memory slot (a value that a
+// kernel after the next one reads; a thread touches only its own rows, so no barrier is
+// needed). COUNT: instead of storing the result rows, count the nonzero ones (a region under
+// `count`) into *out (an unsigned 64-bit counter).
 template <bool COUNT>
 __global__ void __launch_bounds__(RG_THREADS) region_kernel(const RegionProg P, int64_t n, void *__restrict__ out) {
     extern __shared__ unsigned long long s_w[];
-    const int t = threadIdx.x;
     unsigned long long nonzero = 0;
     for (int64_t b0 = static_cast<int64_t>(blockIdx.x) * RG_BLOCK_ROWS; b0 < n;
          b0 += static_cast<int64_t>(gridDim.x) * RG_BLOCK_ROWS) {
-        // Every array input's rows of the step, all loads in flight together.
-        unsigned long long inv[RG_MAX_ARR][RG_ROWS];
-#pragma unroll
-        for (int j = 0; j < RG_MAX_ARR; ++j) {
-            const RgIn in = P.in[j];
-#pragma unroll
-            for (int r = 0; r < RG_ROWS; ++r) {
-                const int64_t i = b0 + t + r * RG_THREADS;
-                inv[j][r] = (in.p && i < n) ? rg_load(in, i) : 0ull;
-            }
-        }
-        unsigned long long prev[RG_ROWS];
-        for (int k = 0; k < P.nk; ++k) {
-            const RgOp &o = P.op[k];
-            unsigned long long a[3][RG_ROWS];
-#pragma unroll
-            for (int j = 0; j < 3; ++j) {
-                const int kind = o.kind[j], idx = o.idx[j];
-                if (kind == RK_IN) {
-                    // A uniform branch per input keeps the register array statically indexed.
-                    switch (idx) {
-#define RG_IN_CASE(q)                                                \
-    case q:                                                          \
-        for (int r = 0; r < RG_ROWS; ++r) a[j][r] = inv[q][r];       \
-        break;
-                        RG_IN_CASE(0) RG_IN_CASE(1) RG_IN_CASE(2) default: RG_IN_CASE(3)
-#undef RG_IN_CASE
-                    }
-                } else if (kind == RK_CONST) {
-#pragma unroll
-                    for (int r = 0; r < RG_ROWS; ++r) a[j][r] = o.c[j];
-                } else if (kind == RK_PREV) {
-#pragma unroll
-                    for (int r = 0; r < RG_ROWS; ++r) a[j][r] = prev[r];
-                } else {
-#pragma unroll
-                    for (int r = 0; r < RG_ROWS; ++r) a[j][r] = s_w[idx * RG_BLOCK_ROWS + t + r * RG_THREADS];
-                }
-            }
-            rg_eval(o, a, prev);
-            if (o.keep) {
-#pragma unroll
-                for (int r = 0; r < RG_ROWS; ++r) s_w[o.slot * RG_BLOCK_ROWS + t + r * RG_THREADS] = prev[r];
-            }
-        }
-#pragma unroll
-        for (int r = 0; r < RG_ROWS; ++r) {
-            const int64_t i = b0 + t + r * RG_THREADS;
-            if (i >= n) break;
-            const unsigned long long w = prev[r];
-            if (COUNT) {
-                nonzero += w != 0;
-                continue;
-            }
-            switch (P.out_width) {
-            case 8: static_cast<unsigned long long *>(out)[i] = w; break;
-            case 4: static_cast<unsigned *>(out)[i] = static_cast<unsigned>(w); break;
-            default: static_cast<unsigned char *>(out)[i] = static_cast<unsigned char>(w); break;
-            }
-        }
+        if (b0 + RG_BLOCK_ROWS <= n) region_step<COUNT, true>(P, b0, n, out, s_w, nonzero);
+        else region_step<COUNT, false>(P, b0, n, out, s_w, nonzero);
     }
     if (COUNT) {
         nonzero = warp_sum(nonzero);
-        if ((t & 31) == 0 && nonzero) atomicAdd(static_cast<unsigned long long *>(out), nonzero);
+        if ((threadIdx.x & 31) == 0 && nonzero) atomicAdd(static_cast<unsigned long long *>(out), nonzero);
     }
 }
 

@@ -75,6 +75,7 @@ bool plan_region(const vkc_region_kernel *ks, int nk, const vkc_value *in, int n
             arr_no[static_cast<size_t>(j)] = narr;
             p->in[narr++] = RgIn{in[j].array->data(), type_width(in[j].array->type)};
         }
+    p->narr = narr;
     std::vector<vkc_type> ty(static_cast<size_t>(nk));
     std::vector<char> keep(static_cast<size_t>(nk), 0);
     for (int k = 0; k < nk; ++k) {

@@ -49,7 +49,7 @@ struct RgOp {
     Divider dv;
 };
 struct RegionProg {
-    int nk, nslots, out_width;
+    int nk, nslots, out_width, narr;
     RgIn in[RG_MAX_ARR];  // the array inputs, numbered in input order
     RgOp op[RG_MAX_K];
 };
