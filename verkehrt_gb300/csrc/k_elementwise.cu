@@ -321,6 +321,33 @@ template <class T> __device__ __forceinline__ unsigned long long to_word(T v) {
 
 constexpr int RG_THREADS = 128, RG_ROWS = 4, RG_BLOCK_ROWS = RG_THREADS * RG_ROWS;
 
+// Orderings of f64 rows without the FP64 unit (a region's other operations often keep it busy:
+// GB300 issues about 0.5 T FP64 operations a second): on the bits, with IEEE's answers (a NaN
+// is unordered and unequal, -0 equals +0), with kcommon.cuh's order keys, which rank -0 just
+// below +0. Other types compare as they are.
+__device__ __forceinline__ bool f64_nan(unsigned long long b) { return (b & 0x7fffffffffffffffull) > 0x7ff0000000000000ull; }
+__device__ __forceinline__ bool f64_zeros(unsigned long long a, unsigned long long b) {
+    return ((a | b) & 0x7fffffffffffffffull) == 0;
+}
+template <class T> __device__ __forceinline__ bool rg_less(unsigned long long a, unsigned long long b, T x, T y) {
+    if constexpr (std::is_same<T, double>::value)
+        return !f64_nan(a) && !f64_nan(b) && f64_key(a) < f64_key(b) && !f64_zeros(a, b);
+    else
+        return x < y;
+}
+template <class T> __device__ __forceinline__ bool rg_less_eq(unsigned long long a, unsigned long long b, T x, T y) {
+    if constexpr (std::is_same<T, double>::value)
+        return !f64_nan(a) && !f64_nan(b) && (f64_key(a) <= f64_key(b) || f64_zeros(a, b));
+    else
+        return x <= y;
+}
+template <class T> __device__ __forceinline__ bool rg_equal(unsigned long long a, unsigned long long b, T x, T y) {
+    if constexpr (std::is_same<T, double>::value)
+        return !f64_nan(a) && (a == b || f64_zeros(a, b));
+    else
+        return x == y;
+}
+
 // One kernel of a region over a thread's RG_ROWS rows: the operation is chosen once (uniform
 // branches), then the rows run through it.
 #define RG_EACH(EXPR)                                      \
@@ -346,12 +373,12 @@ __device__ __forceinline__ void rg_typed(const RgOp &o, const unsigned long long
     case EF_MUL: RG_EACH(to_word(ew_mul(x, y)))
     case EF_MIN: RG_EACH(to_word(ew_min(x, y)))
     case EF_MAX: RG_EACH(to_word(ew_max(x, y)))
-    case EF_LT: RG_EACH(static_cast<unsigned long long>(x < y))
-    case EF_LE: RG_EACH(static_cast<unsigned long long>(x <= y))
-    case EF_GT: RG_EACH(static_cast<unsigned long long>(x > y))
-    case EF_GE: RG_EACH(static_cast<unsigned long long>(x >= y))
-    case EF_EQ: RG_EACH(static_cast<unsigned long long>(x == y))
-    case EF_NE: RG_EACH(static_cast<unsigned long long>(x != y))
+    case EF_LT: RG_EACH(static_cast<unsigned long long>(rg_less<T>(a[0][r], a[1][r], x, y)))
+    case EF_LE: RG_EACH(static_cast<unsigned long long>(rg_less_eq<T>(a[0][r], a[1][r], x, y)))
+    case EF_GT: RG_EACH(static_cast<unsigned long long>(rg_less<T>(a[1][r], a[0][r], y, x)))
+    case EF_GE: RG_EACH(static_cast<unsigned long long>(rg_less_eq<T>(a[1][r], a[0][r], y, x)))
+    case EF_EQ: RG_EACH(static_cast<unsigned long long>(rg_equal<T>(a[0][r], a[1][r], x, y)))
+    case EF_NE: RG_EACH(static_cast<unsigned long long>(!rg_equal<T>(a[0][r], a[1][r], x, y)))
     // select(mask, a, b): the mask is the first operand.
     case EF_SELECT: RG_EACH((a[0][r] & 0xffu) ? a[1][r] : a[2][r])
     case EF_BNOT: RG_EACH(a[0][r] ^ 1u)
@@ -398,120 +425,91 @@ __device__ __forceinline__ void rg_eval(const RgOp &o, const unsigned long long 
     }
 }
 
-// Loads input j's rows of the step (FULL: the step lies inside the array, no row checks).
-template <bool FULL>
-__device__ __forceinline__ void rg_load_rows(const RgIn in, int64_t base, int64_t n, unsigned long long (&v)[RG_ROWS]) {
+__device__ __forceinline__ unsigned long long rg_load(const RgIn in, int64_t i) {
     switch (in.width) {
-    case 8: {
-        const unsigned long long *q = static_cast<const unsigned long long *>(in.p) + base;
-#pragma unroll
-        for (int r = 0; r < RG_ROWS; ++r) v[r] = (FULL || base + r * RG_THREADS < n) ? __ldcs(q + r * RG_THREADS) : 0ull;
-        break;
-    }
-    case 4: {
-        const unsigned *q = static_cast<const unsigned *>(in.p) + base;
-#pragma unroll
-        for (int r = 0; r < RG_ROWS; ++r) v[r] = (FULL || base + r * RG_THREADS < n) ? __ldcs(q + r * RG_THREADS) : 0u;
-        break;
-    }
-    default: {
-        const unsigned char *q = static_cast<const unsigned char *>(in.p) + base;
-#pragma unroll
-        for (int r = 0; r < RG_ROWS; ++r) v[r] = (FULL || base + r * RG_THREADS < n) ? __ldcs(q + r * RG_THREADS) : 0u;
-        break;
-    }
-    }
-}
-
-// One step of RG_BLOCK_ROWS rows from row b0: the thread's rows b0 + t + 128 r.
-template <bool COUNT, bool FULL>
-__device__ __forceinline__ void region_step(const RegionProg &P, int64_t b0, int64_t n, void *__restrict__ out,
-                                            unsigned long long *s_w, unsigned long long &nonzero) {
-    const int t = threadIdx.x;
-    const int64_t base = b0 + t;
-    // Every array input's rows of the step, all loads in flight together.
-    unsigned long long inv[RG_MAX_ARR][RG_ROWS];
-#pragma unroll
-    for (int j = 0; j < RG_MAX_ARR; ++j)
-        if (j < P.narr) rg_load_rows<FULL>(P.in[j], base, n, inv[j]);
-    unsigned long long prev[RG_ROWS];
-    for (int k = 0; k < P.nk; ++k) {
-        const RgOp &o = P.op[k];
-        unsigned long long a[3][RG_ROWS];
-#pragma unroll
-        for (int j = 0; j < 3; ++j) {
-            const int kind = o.kind[j], idx = o.idx[j];
-            if (kind == RK_IN) {
-                // A uniform branch per input keeps the register array statically indexed.
-                switch (idx) {
-#define RG_IN_CASE(q)                                                          \
-    case q:                                                                    \
-        _Pragma("unroll") for (int r = 0; r < RG_ROWS; ++r) a[j][r] = inv[q][r]; \
-        break;
-                    RG_IN_CASE(0) RG_IN_CASE(1) RG_IN_CASE(2) default: RG_IN_CASE(3)
-#undef RG_IN_CASE
-                }
-            } else if (kind == RK_CONST) {
-#pragma unroll
-                for (int r = 0; r < RG_ROWS; ++r) a[j][r] = o.c[j];
-            } else if (kind == RK_PREV) {
-#pragma unroll
-                for (int r = 0; r < RG_ROWS; ++r) a[j][r] = prev[r];
-            } else {
-#pragma unroll
-                for (int r = 0; r < RG_ROWS; ++r) a[j][r] = s_w[idx * RG_BLOCK_ROWS + t + r * RG_THREADS];
-            }
-        }
-        rg_eval(o, a, prev);
-        if (o.keep) {
-#pragma unroll
-            for (int r = 0; r < RG_ROWS; ++r) s_w[o.slot * RG_BLOCK_ROWS + t + r * RG_THREADS] = prev[r];
-        }
-    }
-    if (COUNT) {
-#pragma unroll
-        for (int r = 0; r < RG_ROWS; ++r)
-            if (FULL || base + r * RG_THREADS < n) nonzero += prev[r] != 0;
-        return;
-    }
-    switch (P.out_width) {
-    case 8:
-#pragma unroll
-        for (int r = 0; r < RG_ROWS; ++r)
-            if (FULL || base + r * RG_THREADS < n) static_cast<unsigned long long *>(out)[base + r * RG_THREADS] = prev[r];
-        break;
-    case 4:
-#pragma unroll
-        for (int r = 0; r < RG_ROWS; ++r)
-            if (FULL || base + r * RG_THREADS < n) static_cast<unsigned *>(out)[base + r * RG_THREADS] = static_cast<unsigned>(prev[r]);
-        break;
-    default:
-#pragma unroll
-        for (int r = 0; r < RG_ROWS; ++r)
-            if (FULL || base + r * RG_THREADS < n)
-                static_cast<unsigned char *>(out)[base + r * RG_THREADS] = static_cast<unsigned char>(prev[r]);
-        break;
+    case 8: return __ldcs(static_cast<const unsigned long long *>(in.p) + i);
+    case 4: return __ldcs(static_cast<const unsigned *>(in.p) + i);
+    default: return __ldcs(static_cast<const unsigned char *>(in.p) + i);
     }
 }
 
 // Each block takes RG_BLOCK_ROWS rows per step, four per thread (t, t + 128, ...), and loads
 // every array input's rows of the step first. A kernel's operands come from those inputs,
-// constants, the previous kernel's value in registers, or a shared-memory slot (a value that a
-// kernel after the next one reads; a thread touches only its own rows, so no barrier is
-// needed). COUNT: instead of storing the result rows, count the nonzero ones (a region under
-// `count`) into *out (an unsigned 64-bit counter).
+// constants, the previous kernel's value in registers, or
+// a shared-memory slot (a value that a kernel after the next one reads; a thread touches only
+// its own rows, so no barrier is needed). COUNT: instead of storing the result rows, count the
+// nonzero ones (a region under `count`) into *out (an unsigned 64-bit counter).
 template <bool COUNT>
 __global__ void __launch_bounds__(RG_THREADS) region_kernel(const RegionProg P, int64_t n, void *__restrict__ out) {
     extern __shared__ unsigned long long s_w[];
+    const int t = threadIdx.x;
     unsigned long long nonzero = 0;
     for (int64_t b0 = static_cast<int64_t>(blockIdx.x) * RG_BLOCK_ROWS; b0 < n;
          b0 += static_cast<int64_t>(gridDim.x) * RG_BLOCK_ROWS) {
-        if (b0 + RG_BLOCK_ROWS <= n) region_step<COUNT, true>(P, b0, n, out, s_w, nonzero);
-        else region_step<COUNT, false>(P, b0, n, out, s_w, nonzero);
+        // Every array input's rows of the step, all loads in flight together.
+        unsigned long long inv[RG_MAX_ARR][RG_ROWS];
+#pragma unroll
+        for (int j = 0; j < RG_MAX_ARR; ++j) {
+            const RgIn in = P.in[j];
+#pragma unroll
+            for (int r = 0; r < RG_ROWS; ++r) {
+                const int64_t i = b0 + t + r * RG_THREADS;
+                inv[j][r] = (in.p && i < n) ? rg_load(in, i) : 0ull;
+            }
+        }
+        unsigned long long prev[RG_ROWS];
+        for (int k = 0; k < P.nk; ++k) {
+            const RgOp &o = P.op[k];
+            unsigned long long a[3][RG_ROWS];
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                const int kind = o.kind[j], idx = o.idx[j];
+                if (kind == RK_IN) {
+                    // A uniform branch per input keeps the register array statically indexed.
+                    switch (idx) {
+#define RG_IN_CASE(q)                                                \
+    case q:                                                          \
+        for (int r = 0; r < RG_ROWS; ++r) a[j][r] = inv[q][r];       \
+        break;
+                        RG_IN_CASE(0) RG_IN_CASE(1) RG_IN_CASE(2) default: RG_IN_CASE(3)
+#undef RG_IN_CASE
+                    }
+                } else if (kind == RK_CONST) {
+#pragma unroll
+                    for (int r = 0; r < RG_ROWS; ++r) a[j][r] = o.c[j];
+                } else if (kind == RK_PREV) {
+#pragma unroll
+                    for (int r = 0; r < RG_ROWS; ++r) a[j][r] = prev[r];
+                } else {
+#pragma unroll
+                    for (int r = 0; r < RG_ROWS; ++r) a[j][r] = s_w[idx * RG_BLOCK_ROWS + t + r * RG_THREADS];
+                }
+            }
+            rg_eval(o, a, prev);
+            if (o.keep) {
+#pragma unroll
+                for (int r = 0; r < RG_ROWS; ++r) s_w[o.slot * RG_BLOCK_ROWS + t + r * RG_THREADS] = prev[r];
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < RG_ROWS; ++r) {
+            const int64_t i = b0 + t + r * RG_THREADS;
+            if (i >= n) break;
+            const unsigned long long w = prev[r];
+            if (COUNT) {
+                nonzero += w != 0;
+                continue;
+            }
+            switch (P.out_width) {
+            case 8: static_cast<unsigned long long *>(out)[i] = w; break;
+            case 4: static_cast<unsigned *>(out)[i] = static_cast<unsigned>(w); break;
+            default: static_cast<unsigned char *>(out)[i] = static_cast<unsigned char>(w); break;
+            }
+        }
     }
     if (COUNT) {
         nonzero = warp_sum(nonzero);
-        if ((threadIdx.x & 31) == 0 && nonzero) atomicAdd(static_cast<unsigned long long *>(out), nonzero);
+        if ((t & 31) == 0 && nonzero) atomicAdd(static_cast<unsigned long long *>(out), nonzero);
     }
 }
 
