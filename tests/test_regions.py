@@ -268,6 +268,19 @@ def test_fused_roots(ctx):
     i = ctx.upload(column("i32", n, 9))
     check("reduce_add_i32", [k(0)], [("mul_i32", [0, 0])], [i, i])  # sumsq_i32
     check("reduce_max_i32", [k(0)], [("xor_i32", [0, 1])], [i, vk.Scalar("i32", 12345)])
+    # Extremes and the i64 sum folded in the region's pass: NaN rows, -0 and +0, ties.
+    xn = column("f64", n, 17)  # NaN, infinities and signed zeros among the first rows
+    dxn = ctx.upload(xn)
+    for root in ("reduce_min_f64", "reduce_max_f64", "argmin_f64", "argmax_f64"):
+        check(root, [k(0)], [("mul_f64", [0, 1])], [dxn, dy])
+        check(root, [k(0)], [("mul_f64", [0, 1])], [dxn, 0.0])  # every row +-0 or NaN
+        check(root, [k(1)], [("abs_f64", [0]), ("neg_f64", [k(0)])], [dx])
+    ii = ctx.upload(column("i64", n, 19))
+    for root in ("reduce_min_i64", "reduce_max_i64", "argmin_i64", "argmax_i64", "reduce_add_i64"):
+        check(root, [k(0)], [("mul_i64", [0, 1])], [ii, ii])
+        check(root, [k(0)], [("and_i64", [0, 1])], [ii, vk.Scalar("i64", 7)])  # many ties
+    want = oracle.argmin_f64(oracle.ew_binary("mul", "f64", xn, y))
+    assert ctx.region_reduce("argmin_f64", [k(0)], [("mul_f64", [0, 1])], [dxn, dy]) == want
     # dot over two region kernels, and its length mismatch error as whole evaluation gives it.
     check("dot_f64", [k(0), k(1)], [("neg_f64", [0]), ("abs_f64", [1])], [dx, dy])
     short = ctx.upload(column("f64", 10, 3))

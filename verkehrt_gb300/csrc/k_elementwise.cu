@@ -321,32 +321,8 @@ template <class T> __device__ __forceinline__ unsigned long long to_word(T v) {
 
 constexpr int RG_THREADS = 128, RG_ROWS = 4, RG_BLOCK_ROWS = RG_THREADS * RG_ROWS;
 
-// Orderings of f64 rows without the FP64 unit (a region's other operations often keep it busy:
-// GB300 issues about 0.5 T FP64 operations a second): on the bits, with IEEE's answers (a NaN
-// is unordered and unequal, -0 equals +0), with kcommon.cuh's order keys, which rank -0 just
-// below +0. Other types compare as they are.
+// NaN test on the bits (the region folds' NaN rule).
 __device__ __forceinline__ bool f64_nan(unsigned long long b) { return (b & 0x7fffffffffffffffull) > 0x7ff0000000000000ull; }
-__device__ __forceinline__ bool f64_zeros(unsigned long long a, unsigned long long b) {
-    return ((a | b) & 0x7fffffffffffffffull) == 0;
-}
-template <class T> __device__ __forceinline__ bool rg_less(unsigned long long a, unsigned long long b, T x, T y) {
-    if constexpr (std::is_same<T, double>::value)
-        return !f64_nan(a) && !f64_nan(b) && f64_key(a) < f64_key(b) && !f64_zeros(a, b);
-    else
-        return x < y;
-}
-template <class T> __device__ __forceinline__ bool rg_less_eq(unsigned long long a, unsigned long long b, T x, T y) {
-    if constexpr (std::is_same<T, double>::value)
-        return !f64_nan(a) && !f64_nan(b) && (f64_key(a) <= f64_key(b) || f64_zeros(a, b));
-    else
-        return x <= y;
-}
-template <class T> __device__ __forceinline__ bool rg_equal(unsigned long long a, unsigned long long b, T x, T y) {
-    if constexpr (std::is_same<T, double>::value)
-        return !f64_nan(a) && (a == b || f64_zeros(a, b));
-    else
-        return x == y;
-}
 
 // One kernel of a region over a thread's RG_ROWS rows: the operation is chosen once (uniform
 // branches), then the rows run through it.
@@ -373,12 +349,12 @@ __device__ __forceinline__ void rg_typed(const RgOp &o, const unsigned long long
     case EF_MUL: RG_EACH(to_word(ew_mul(x, y)))
     case EF_MIN: RG_EACH(to_word(ew_min(x, y)))
     case EF_MAX: RG_EACH(to_word(ew_max(x, y)))
-    case EF_LT: RG_EACH(static_cast<unsigned long long>(rg_less<T>(a[0][r], a[1][r], x, y)))
-    case EF_LE: RG_EACH(static_cast<unsigned long long>(rg_less_eq<T>(a[0][r], a[1][r], x, y)))
-    case EF_GT: RG_EACH(static_cast<unsigned long long>(rg_less<T>(a[1][r], a[0][r], y, x)))
-    case EF_GE: RG_EACH(static_cast<unsigned long long>(rg_less_eq<T>(a[1][r], a[0][r], y, x)))
-    case EF_EQ: RG_EACH(static_cast<unsigned long long>(rg_equal<T>(a[0][r], a[1][r], x, y)))
-    case EF_NE: RG_EACH(static_cast<unsigned long long>(!rg_equal<T>(a[0][r], a[1][r], x, y)))
+    case EF_LT: RG_EACH(static_cast<unsigned long long>(x < y))
+    case EF_LE: RG_EACH(static_cast<unsigned long long>(x <= y))
+    case EF_GT: RG_EACH(static_cast<unsigned long long>(x > y))
+    case EF_GE: RG_EACH(static_cast<unsigned long long>(x >= y))
+    case EF_EQ: RG_EACH(static_cast<unsigned long long>(x == y))
+    case EF_NE: RG_EACH(static_cast<unsigned long long>(x != y))
     // select(mask, a, b): the mask is the first operand.
     case EF_SELECT: RG_EACH((a[0][r] & 0xffu) ? a[1][r] : a[2][r])
     case EF_BNOT: RG_EACH(a[0][r] ^ 1u)
@@ -439,6 +415,64 @@ __device__ __forceinline__ unsigned long long rg_load(const RgIn in, int64_t i) 
 // a shared-memory slot (a value that a kernel after the next one reads; a thread touches only
 // its own rows, so no barrier is needed). COUNT: instead of storing the result rows, count the
 // nonzero ones (a region under `count`) into *out (an unsigned 64-bit counter).
+// The values of the region's last kernel for the thread's rows of the step from row b0.
+__device__ __forceinline__ void rg_values(const RegionProg &P, int64_t b0, int64_t n, unsigned long long *s_w,
+                                          unsigned long long (&prev)[RG_ROWS]) {
+    const int t = threadIdx.x;
+    // Every array input's rows of the step, all loads in flight together.
+    unsigned long long inv[RG_MAX_ARR][RG_ROWS];
+    const int64_t base = b0 + t;
+#pragma unroll
+    for (int j = 0; j < RG_MAX_ARR; ++j) {
+        if (j >= P.narr) continue;
+        const RgIn in = P.in[j];
+        if (in.width == 8) {
+            const unsigned long long *q = static_cast<const unsigned long long *>(in.p) + base;
+#pragma unroll
+            for (int r = 0; r < RG_ROWS; ++r) inv[j][r] = base + r * RG_THREADS < n ? __ldcs(q + r * RG_THREADS) : 0ull;
+        } else {
+#pragma unroll
+            for (int r = 0; r < RG_ROWS; ++r) {
+                const int64_t i = base + r * RG_THREADS;
+                inv[j][r] = i < n ? rg_load(in, i) : 0ull;
+            }
+        }
+    }
+    for (int k = 0; k < P.nk; ++k) {
+        const RgOp &o = P.op[k];
+        unsigned long long a[3][RG_ROWS];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            const int kind = o.kind[j], idx = o.idx[j];
+            if (kind == RK_IN) {
+                // A uniform branch per input keeps the register array statically indexed.
+                switch (idx) {
+#define RG_IN_CASE(q)                                                \
+    case q:                                                          \
+        for (int r = 0; r < RG_ROWS; ++r) a[j][r] = inv[q][r];       \
+        break;
+                    RG_IN_CASE(0) RG_IN_CASE(1) RG_IN_CASE(2) default: RG_IN_CASE(3)
+#undef RG_IN_CASE
+                }
+            } else if (kind == RK_CONST) {
+#pragma unroll
+                for (int r = 0; r < RG_ROWS; ++r) a[j][r] = o.c[j];
+            } else if (kind == RK_PREV) {
+#pragma unroll
+                for (int r = 0; r < RG_ROWS; ++r) a[j][r] = prev[r];
+            } else {
+#pragma unroll
+                for (int r = 0; r < RG_ROWS; ++r) a[j][r] = s_w[idx * RG_BLOCK_ROWS + t + r * RG_THREADS];
+            }
+        }
+        rg_eval(o, a, prev);
+        if (o.keep) {
+#pragma unroll
+            for (int r = 0; r < RG_ROWS; ++r) s_w[o.slot * RG_BLOCK_ROWS + t + r * RG_THREADS] = prev[r];
+        }
+    }
+}
+
 template <bool COUNT>
 __global__ void __launch_bounds__(RG_THREADS) region_kernel(const RegionProg P, int64_t n, void *__restrict__ out) {
     extern __shared__ unsigned long long s_w[];
@@ -446,51 +480,8 @@ __global__ void __launch_bounds__(RG_THREADS) region_kernel(const RegionProg P, 
     unsigned long long nonzero = 0;
     for (int64_t b0 = static_cast<int64_t>(blockIdx.x) * RG_BLOCK_ROWS; b0 < n;
          b0 += static_cast<int64_t>(gridDim.x) * RG_BLOCK_ROWS) {
-        // Every array input's rows of the step, all loads in flight together.
-        unsigned long long inv[RG_MAX_ARR][RG_ROWS];
-#pragma unroll
-        for (int j = 0; j < RG_MAX_ARR; ++j) {
-            const RgIn in = P.in[j];
-#pragma unroll
-            for (int r = 0; r < RG_ROWS; ++r) {
-                const int64_t i = b0 + t + r * RG_THREADS;
-                inv[j][r] = (in.p && i < n) ? rg_load(in, i) : 0ull;
-            }
-        }
         unsigned long long prev[RG_ROWS];
-        for (int k = 0; k < P.nk; ++k) {
-            const RgOp &o = P.op[k];
-            unsigned long long a[3][RG_ROWS];
-#pragma unroll
-            for (int j = 0; j < 3; ++j) {
-                const int kind = o.kind[j], idx = o.idx[j];
-                if (kind == RK_IN) {
-                    // A uniform branch per input keeps the register array statically indexed.
-                    switch (idx) {
-#define RG_IN_CASE(q)                                                \
-    case q:                                                          \
-        for (int r = 0; r < RG_ROWS; ++r) a[j][r] = inv[q][r];       \
-        break;
-                        RG_IN_CASE(0) RG_IN_CASE(1) RG_IN_CASE(2) default: RG_IN_CASE(3)
-#undef RG_IN_CASE
-                    }
-                } else if (kind == RK_CONST) {
-#pragma unroll
-                    for (int r = 0; r < RG_ROWS; ++r) a[j][r] = o.c[j];
-                } else if (kind == RK_PREV) {
-#pragma unroll
-                    for (int r = 0; r < RG_ROWS; ++r) a[j][r] = prev[r];
-                } else {
-#pragma unroll
-                    for (int r = 0; r < RG_ROWS; ++r) a[j][r] = s_w[idx * RG_BLOCK_ROWS + t + r * RG_THREADS];
-                }
-            }
-            rg_eval(o, a, prev);
-            if (o.keep) {
-#pragma unroll
-                for (int r = 0; r < RG_ROWS; ++r) s_w[o.slot * RG_BLOCK_ROWS + t + r * RG_THREADS] = prev[r];
-            }
-        }
+        rg_values(P, b0, n, s_w, prev);
 #pragma unroll
         for (int r = 0; r < RG_ROWS; ++r) {
             const int64_t i = b0 + t + r * RG_THREADS;
@@ -511,6 +502,96 @@ __global__ void __launch_bounds__(RG_THREADS) region_kernel(const RegionProg P, 
         nonzero = warp_sum(nonzero);
         if ((t & 31) == 0 && nonzero) atomicAdd(static_cast<unsigned long long *>(out), nonzero);
     }
+}
+
+// ------------------------------------------------------------------ region folds
+//
+// A reduction over a region's value in the same pass: reduce_min/max and argmin/argmax on f64
+// and i64 (f64 rows by their order keys, the first NaN row deciding, as the extreme reducers of
+// k_reduce.cu do: src/kernels/scalar/reduce.rs:380-468) and the wrapping i64 sum
+// (reduce.rs:331-377).
+
+__device__ __forceinline__ void rg_fold_take(int kind, RgFold &a, const RgFold &b) {
+    a.nan_idx = min(a.nan_idx, b.nan_idx);
+    a.sum += b.sum;
+    if (b.idx == ~0ull) return;
+    const bool mx = kind == RF_MAX || kind == RF_ARGMAX;
+    const bool better = a.idx == ~0ull || (mx ? b.key > a.key : b.key < a.key) || (b.key == a.key && b.idx < a.idx);
+    if (better) {
+        a.key = b.key;
+        a.idx = b.idx;
+    }
+}
+
+__device__ __forceinline__ RgFold rg_fold_shfl(const RgFold &v, int o) {
+    return RgFold{static_cast<long long>(__shfl_xor_sync(FULL, static_cast<unsigned long long>(v.key), o)),
+                  __shfl_xor_sync(FULL, v.idx, o), __shfl_xor_sync(FULL, v.nan_idx, o), __shfl_xor_sync(FULL, v.sum, o)};
+}
+
+// The block's fold of `v` into thread 0's return value (every thread calls it).
+__device__ __forceinline__ RgFold rg_fold_block(int kind, RgFold v) {
+    __shared__ RgFold s_f[RG_THREADS / 32];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) rg_fold_take(kind, v, rg_fold_shfl(v, o));
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) s_f[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0)
+        for (int w = 1; w < RG_THREADS / 32; ++w) rg_fold_take(kind, v, s_f[w]);
+    return v;
+}
+
+__global__ void __launch_bounds__(RG_THREADS) region_fold_kernel(const RegionProg P, int64_t n, int kind, bool f64,
+                                                                 RgFold *partials, unsigned *done, RgFold *result) {
+    extern __shared__ unsigned long long s_w[];
+    const int t = threadIdx.x;
+    RgFold me{0, ~0ull, ~0ull, 0};
+    for (int64_t b0 = static_cast<int64_t>(blockIdx.x) * RG_BLOCK_ROWS; b0 < n;
+         b0 += static_cast<int64_t>(gridDim.x) * RG_BLOCK_ROWS) {
+        unsigned long long prev[RG_ROWS];
+        rg_values(P, b0, n, s_w, prev);
+#pragma unroll
+        for (int r = 0; r < RG_ROWS; ++r) {
+            const int64_t i = b0 + t + r * RG_THREADS;
+            if (i >= n) break;
+            const unsigned long long w = prev[r];
+            if (kind == RF_SUM) {
+                me.sum += w;
+                continue;
+            }
+            if (f64 && f64_nan(w)) {
+                me.nan_idx = min(me.nan_idx, static_cast<unsigned long long>(i));
+                continue;
+            }
+            rg_fold_take(kind, me, RgFold{f64 ? f64_key(w) : static_cast<long long>(w), static_cast<unsigned long long>(i), ~0ull, 0});
+        }
+    }
+    const RgFold b = rg_fold_block(kind, me);
+    if (t == 0) partials[blockIdx.x] = b;
+    if (last_block(done)) {
+        RgFold v{0, ~0ull, ~0ull, 0};
+        for (unsigned q = t; q < gridDim.x; q += RG_THREADS) rg_fold_take(kind, v, partials[q]);
+        v = rg_fold_block(kind, v);
+        if (t == 0) *result = v;
+    }
+}
+
+vkc_status launch_region_fold(vkc_ctx *ctx, const RegionProg &p, int64_t n, int kind, bool f64, RgFold *work,
+                              unsigned *done) {
+    if (n <= 0) return VKC_OK;
+    const size_t smem = static_cast<size_t>(p.nslots) * RG_BLOCK_ROWS * sizeof(unsigned long long);
+    static std::atomic<unsigned long long> configured{0};
+    once_per_device(configured, ctx->device, [] {
+        cudaFuncSetAttribute(region_fold_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             static_cast<int>(RG_MAX_K * RG_BLOCK_ROWS * sizeof(unsigned long long)));
+    });
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, region_fold_kernel, RG_THREADS, smem);
+    const int64_t blocks = (n + RG_BLOCK_ROWS - 1) / RG_BLOCK_ROWS;
+    int64_t g = std::min<int64_t>(blocks, static_cast<int64_t>(ctx->sms) * std::max(1, per_sm));
+    const int grid = static_cast<int>(std::min<int64_t>(g, RG_FOLD_MAX_GRID));
+    region_fold_kernel<<<grid, RG_THREADS, smem, ctx->stream>>>(p, n, kind, f64, work + 1, done, work);
+    return launched(ctx, "region_fold");
 }
 
 vkc_status launch_region(vkc_ctx *ctx, const RegionProg &p, int64_t n, void *out, bool count) {

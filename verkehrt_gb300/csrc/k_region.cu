@@ -8,7 +8,8 @@
 //    divisor, more kernels or inputs than the evaluator holds), runs whole instead, kernel by
 //    kernel in post-order, which raises the error whole evaluation raises, as the reference
 //    does when its tiled run fails (region.rs:137-159);
-//  * `count` over a region counts the region's true rows as it evaluates them;
+//  * `count` over a region counts the region's true rows as it evaluates them, and the extremes
+//    (reduce_min/max, argmin/argmax on f64 and i64) and the i64 sum fold them in the same pass;
 //  * a fused root whose region matches one of the registry's fused patterns
 //    (src/kernels/scalar/fused.rs:286-379: dot_T, sumsq_T, count_<cmp>_T, condsum_<cmp>_T are
 //    declared there as those compositions) runs as that fused reduction over the pattern's
@@ -18,6 +19,7 @@
 #include <string>
 #include <vector>
 
+#include "kcommon.cuh"
 #include "region.h"
 #include "registry.h"
 
@@ -314,6 +316,47 @@ vkc_status vkc_region_reduce(vkc_ctx *ctx, int root, const int32_t *root_args, i
             out->scalar = scalar_i64(v);
             return VKC_OK;
         }
+    }
+    // Extremes and the i64 sum over a region: folded in the same pass.
+    static const struct {
+        const char *name;
+        int kind;
+        bool f64;
+    } folds[] = {{"reduce_min_f64", RF_MIN, true},     {"reduce_max_f64", RF_MAX, true},
+                 {"argmin_f64", RF_ARGMIN, true},      {"argmax_f64", RF_ARGMAX, true},
+                 {"reduce_min_i64", RF_MIN, false},    {"reduce_max_i64", RF_MAX, false},
+                 {"argmin_i64", RF_ARGMIN, false},     {"argmax_i64", RF_ARGMAX, false},
+                 {"reduce_add_i64", RF_SUM, false}};
+    for (const auto &f : folds) {
+        if (name_of(root) != f.name || args.size() != 1 || !args[0].kernel) continue;
+        const std::vector<vkc_region_kernel> sub = subtree(kernels, args[0].i);
+        if (!plan_region(sub.data(), static_cast<int>(sub.size()), inputs, ninputs, &p, &n, &t) ||
+            t != (f.f64 ? VKC_F64 : VKC_I64) || n == 0)
+            break;  // the root over the materialised value gives the value and the errors
+        await_values(ctx, inputs, ninputs);
+        vkc_array *w;
+        const int64_t words = 4 * (RG_FOLD_MAX_GRID + 1) + 1;
+        if ((st = new_array(ctx, VKC_U64, words, true, &w))) return st;
+        auto *work = static_cast<RgFold *>(w->data());
+        RgFold r{};
+        st = launch_region_fold(ctx, p, n, f.kind, f.f64, work,
+                                reinterpret_cast<unsigned *>(static_cast<unsigned long long *>(w->data()) + words - 1));
+        if (!st) st = vkc_array_download(ctx, w, &r, 4);
+        vkc_array_release(w);
+        if (st) return st;
+        out->kind = VKC_VALUE_SCALAR;
+        const bool arg = f.kind == RF_ARGMIN || f.kind == RF_ARGMAX;
+        if (f.kind == RF_SUM) {
+            out->scalar = scalar_i64(static_cast<int64_t>(r.sum));
+        } else if (arg) {  // reduce.rs:454-467: a NaN row decides
+            out->scalar = scalar_i64(static_cast<int64_t>(f.f64 && r.nan_idx != ~0ull ? r.nan_idx : r.idx));
+        } else if (f.f64) {  // reduce.rs:401-411: any NaN makes the result NaN
+            out->scalar.type = VKC_F64;
+            out->scalar.bits = r.nan_idx != ~0ull ? 0x7ff8000000000000ull : bits_of_key(r.key);
+        } else {
+            out->scalar = scalar_i64(r.key);
+        }
+        return VKC_OK;
     }
     int root2 = root;
     std::vector<Src> args2 = args;

@@ -54,6 +54,20 @@ struct RegionProg {
     RgOp op[RG_MAX_K];
 };
 
+// Region folds: the root reduction over the region's value in the same pass.
+enum RgFoldKind { RF_MIN, RF_MAX, RF_ARGMIN, RF_ARGMAX, RF_SUM };
+struct RgFold {
+    long long key;                // the best order key (f64) or value (i64)
+    unsigned long long idx;       // its first row (~0: no row yet)
+    unsigned long long nan_idx;   // the first NaN row (~0: none)
+    unsigned long long sum;       // RF_SUM: the wrapping sum
+};
+constexpr int RG_FOLD_MAX_GRID = 4096;
+// Folds `p`'s value over n > 0 rows: work[0] gets the result, work[1 ..] holds one partial per
+// block (RG_FOLD_MAX_GRID at most); *done is a zeroed counter.
+vkc_status launch_region_fold(vkc_ctx *ctx, const RegionProg &p, int64_t n, int kind, bool f64, RgFold *work,
+                              unsigned *done);
+
 // Runs `p` over n rows into `out` (the last kernel's rows) on the context's stream; with
 // `count`, adds the number of nonzero result rows to the u64 at `out` instead.
 vkc_status launch_region(vkc_ctx *ctx, const RegionProg &p, int64_t n, void *out, bool count = false);
