@@ -1716,10 +1716,8 @@ static vkc_status scan_add_f64(vkc_ctx *ctx, const vkc_value *args, int, vkc_val
 // scan_by_add_f64: each segment (from a row whose start flag is set, row 0 always, to the next)
 // is scanned with its lanes numbered from its first row. Segment heads are listed in order
 // (a count per 4096-row tile, a scan, an ordered write); one thread scans each segment of at
-// most SB_SHORT rows in registers (the 16 lanes, each block's combine and tail, in the order of
-// the oracle's restatement: the first block's adds from +0.0 in FP64, later blocks by add_bits),
-// its warp moving the rows; longer segments, listed for the host, take the tiled scan above on
-// their rows.
+// most SB_SHORT rows in registers (the 16 lanes, each block's combine and tail); longer
+// segments, listed for the host, take the tiled scan above on their rows.
 constexpr int SB_TILE = 4096;
 constexpr int64_t SB_SHORT = int64_t(1) << 16;
 
@@ -1755,121 +1753,87 @@ __global__ void __launch_bounds__(256) sb_list_kernel(const unsigned char *__res
     }
 }
 
-// Every segment: the short ones here, the long ones listed as (first row, rows) pairs after a
-// count in longs[0]. A warp takes 32 consecutive segments, a thread one segment, 16 rows (one
-// canonical block) a round: the warp loads the round's blocks of its segments into shared
-// memory two segments per instruction (16 lanes on one segment's 128 bytes), each thread runs
-// sb_segment's steps on its block there, and the warp writes the results back the same way, so
-// loads and stores move whole lines where one thread per segment moved 8 bytes at a time.
-constexpr int SBW_WARPS = 4;
-__global__ void __launch_bounds__(32 * SBW_WARPS) sb_segment_kernel(const unsigned long long *__restrict__ x, int64_t n,
-                                                                    const long long *__restrict__ heads,
-                                                                    const unsigned *__restrict__ offs,
-                                                                    const unsigned *__restrict__ counts, int tiles,
-                                                                    unsigned long long *__restrict__ out,
-                                                                    unsigned long long *__restrict__ longs) {
-    __shared__ unsigned long long buf[SBW_WARPS][32][17];
-    __shared__ long long s_b0[SBW_WARPS][32], s_e[SBW_WARPS][32];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    unsigned long long(*bw)[17] = buf[wid];
-    const int64_t G = static_cast<int64_t>(offs[tiles - 1]) + counts[tiles - 1];
-    const int64_t step = static_cast<int64_t>(gridDim.x) * SBW_WARPS * 32;
-    for (int64_t g0 = (static_cast<int64_t>(blockIdx.x) * SBW_WARPS + wid) * 32; g0 < G; g0 += step) {
-        const int64_t g = g0 + lane;
-        int64_t s = 0, e = 0;
-        if (g < G) {
-            s = heads[g];
-            e = g + 1 < G ? heads[g + 1] : n;
+// One segment [s, e) of at most SB_SHORT rows, in the order of the oracle's restatement.
+__device__ void sb_segment(const unsigned long long *__restrict__ x, int64_t s, int64_t e,
+                           unsigned long long *__restrict__ out) {
+    double lane[16];
+#pragma unroll
+    for (int j = 0; j < 16; ++j) lane[j] = 0.0;
+    double base = 0.0;  // the combine of the lanes before the block (+0.0 while all are +0.0)
+    // The first block's adds start from +0.0, where the integer steps never apply: FP64 adds.
+    for (int64_t b0 = s; b0 < e; b0 += 16) {
+        const int64_t cnt = e - b0;
+        if (b0 == s) {
+            double t = 0.0;
+#pragma unroll
+            for (int r = 0; r < 16; ++r) {
+                if (r < cnt) {
+                    const double v = as_f64(x[b0 + r]);
+                    if (r < 15) {
+                        t = __dadd_rn(t, v);
+                        out[b0 + r] = as_bits(t);
+                    }
+                    lane[r] = __dadd_rn(0.0, v);  // used only when the block is whole
+                }
+            }
+            if (cnt >= 16) {
+                double a[16];
+#pragma unroll
+                for (int j = 0; j < 16; ++j) a[j] = lane[j];
+#pragma unroll
+                for (int step = 8; step > 0; step >>= 1)
+#pragma unroll
+                    for (int q = 0; q < step; ++q) a[q] = __dadd_rn(a[q], a[q + step]);
+                base = a[0];
+                out[b0 + 15] = as_bits(base);
+            }
+        } else if (cnt >= 16) {
+            double v[16];
+#pragma unroll
+            for (int j = 0; j < 16; ++j) v[j] = as_f64(x[b0 + j]);
+            unsigned long long t = as_bits(base);
+#pragma unroll
+            for (int r = 0; r < 15; ++r) {
+                t = add_bits(t, as_bits(v[r]));
+                out[b0 + r] = t;
+            }
+            double a[16];
+#pragma unroll
+            for (int j = 0; j < 16; ++j) a[j] = lane[j] = as_f64(add_bits(as_bits(lane[j]), as_bits(v[j])));
+#pragma unroll
+            for (int step = 8; step > 0; step >>= 1)
+#pragma unroll
+                for (int q = 0; q < step; ++q) a[q] = __dadd_rn(a[q], a[q + step]);
+            base = a[0];
+            out[b0 + 15] = as_bits(base);
+        } else {
+            unsigned long long t = as_bits(base);
+            for (int64_t i = b0; i < e; ++i) {
+                t = add_bits(t, x[i]);
+                out[i] = t;
+            }
         }
+    }
+}
+
+// Every segment: the short ones here, the long ones listed as (first row, rows) pairs after a
+// count in longs[0].
+__global__ void __launch_bounds__(128) sb_segment_kernel(const unsigned long long *__restrict__ x, int64_t n,
+                                                         const long long *__restrict__ heads,
+                                                         const unsigned *__restrict__ offs,
+                                                         const unsigned *__restrict__ counts, int tiles,
+                                                         unsigned long long *__restrict__ out,
+                                                         unsigned long long *__restrict__ longs) {
+    const int64_t G = static_cast<int64_t>(offs[tiles - 1]) + counts[tiles - 1];
+    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    for (int64_t g = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; g < G; g += stride) {
+        const int64_t s = heads[g], e = g + 1 < G ? heads[g + 1] : n;
         if (e - s > SB_SHORT) {
             const unsigned long long k = atomicAdd(longs, 1ull);
             longs[1 + 2 * k] = static_cast<unsigned long long>(s);
             longs[2 + 2 * k] = static_cast<unsigned long long>(e - s);
-            e = s;  // scanned by the tiled path
-        }
-        double lanev[16];
-#pragma unroll
-        for (int j = 0; j < 16; ++j) lanev[j] = 0.0;
-        double base = 0.0;  // the combine of the lanes before the block
-        int64_t b0 = s;
-        while (__any_sync(FULL, b0 < e)) {
-            s_b0[wid][lane] = b0;
-            s_e[wid][lane] = e;
-            __syncwarp();
-#pragma unroll 4
-            for (int q = 0; q < 16; ++q) {
-                const int sg = 2 * q + (lane >> 4), j = lane & 15;
-                const int64_t row = s_b0[wid][sg] + j;
-                bw[sg][j] = row < s_e[wid][sg] ? __ldcs(x + row) : 0ull;
-            }
-            __syncwarp();
-            if (b0 < e) {
-                const int64_t cnt = e - b0;
-                unsigned long long v[16];
-#pragma unroll
-                for (int j = 0; j < 16; ++j) v[j] = bw[lane][j];
-                if (b0 == s) {
-                    // The first block's adds start from +0.0, where the integer steps never
-                    // apply: FP64 adds.
-                    double t = 0.0;
-#pragma unroll
-                    for (int r = 0; r < 16; ++r) {
-                        if (r < cnt) {
-                            const double xv = as_f64(v[r]);
-                            if (r < 15) {
-                                t = __dadd_rn(t, xv);
-                                bw[lane][r] = as_bits(t);
-                            }
-                            lanev[r] = __dadd_rn(0.0, xv);  // used only when the block is whole
-                        }
-                    }
-                    if (cnt >= 16) {
-                        double a[16];
-#pragma unroll
-                        for (int j = 0; j < 16; ++j) a[j] = lanev[j];
-#pragma unroll
-                        for (int h = 8; h > 0; h >>= 1)
-#pragma unroll
-                            for (int q = 0; q < h; ++q) a[q] = __dadd_rn(a[q], a[q + h]);
-                        base = a[0];
-                        bw[lane][15] = as_bits(base);
-                    }
-                } else if (cnt >= 16) {
-                    unsigned long long t = as_bits(base);
-#pragma unroll
-                    for (int r = 0; r < 15; ++r) {
-                        t = add_bits(t, v[r]);
-                        bw[lane][r] = t;
-                    }
-                    double a[16];
-#pragma unroll
-                    for (int j = 0; j < 16; ++j) a[j] = lanev[j] = as_f64(add_bits(as_bits(lanev[j]), v[j]));
-#pragma unroll
-                    for (int h = 8; h > 0; h >>= 1)
-#pragma unroll
-                        for (int q = 0; q < h; ++q) a[q] = __dadd_rn(a[q], a[q + h]);
-                    base = a[0];
-                    bw[lane][15] = as_bits(base);
-                } else {
-                    unsigned long long t = as_bits(base);
-#pragma unroll
-                    for (int r = 0; r < 15; ++r) {
-                        if (r < cnt) {
-                            t = add_bits(t, v[r]);
-                            bw[lane][r] = t;
-                        }
-                    }
-                }
-            }
-            __syncwarp();
-#pragma unroll 4
-            for (int q = 0; q < 16; ++q) {
-                const int sg = 2 * q + (lane >> 4), j = lane & 15;
-                const int64_t row = s_b0[wid][sg] + j;
-                if (row < s_e[wid][sg]) out[row] = bw[sg][j];
-            }
-            __syncwarp();
-            b0 += 16;
+        } else {
+            sb_segment(x, s, e, out);
         }
     }
 }
@@ -1930,7 +1894,7 @@ static vkc_status scan_by_add_f64(vkc_ctx *ctx, const vkc_value *args, int, vkc_
     scan_counts(ctx, counts, tiles, sums, offs);
     sb_list_kernel<<<static_cast<unsigned>(tiles), 256, 0, ctx->stream>>>(starts, n, offs, heads);
     if ((st = launched(ctx, "sb_list"))) return done(st);
-    sb_segment_kernel<<<stream_grid(ctx, n, 32 * SBW_WARPS, 16, 256), 32 * SBW_WARPS, 0, ctx->stream>>>(
+    sb_segment_kernel<<<stream_grid(ctx, n, 128, 16, 256), 128, 0, ctx->stream>>>(
         x, n, heads, offs, counts, static_cast<int>(tiles), ov, longs);
     if ((st = launched(ctx, "sb_segment"))) return done(st);
     unsigned long long nlong = 0;
