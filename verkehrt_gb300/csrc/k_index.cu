@@ -73,7 +73,7 @@ static void launch_gather(vkc_ctx *ctx, int rows, int64_t n, const typename GWor
 //   restore    each tile gathers its runs of vals into shared memory in region-sorted order and
 //              writes out[i] = staged[loc[i]] in row order.
 // About 60 DRAM bytes per row, nearly all in runs.
-constexpr int GP_THREADS = 512, GP_ITEMS = 16, GP_TILE = GP_THREADS * GP_ITEMS;
+constexpr int GP_THREADS = 256, GP_ITEMS = 16, GP_TILE = GP_THREADS * GP_ITEMS;
 constexpr int GP_NB = 64;  // source regions
 
 // Warp 0: the exclusive prefix of GP_NB counts get(b) into s_start[0 .. GP_NB - 1], and their
@@ -208,7 +208,7 @@ __global__ void __launch_bounds__(GP_THREADS) gp_restore_kernel(const unsigned l
                                                                 const unsigned *__restrict__ offs, int64_t n, int tiles,
                                                                 unsigned long long *__restrict__ out) {
     __shared__ unsigned s_start[GP_NB + 1], s_goff[GP_NB];
-    extern __shared__ unsigned long long s_vals[];  // GP_TILE rows
+    __shared__ unsigned long long s_vals[GP_TILE];
     if (threadIdx.x < 32) gp_starts([&](int b) { return counts[static_cast<int64_t>(b) * tiles + blockIdx.x]; }, s_start);
     if (threadIdx.x < GP_NB) s_goff[threadIdx.x] = offs[static_cast<int64_t>(threadIdx.x) * tiles + blockIdx.x];
     __syncthreads();
@@ -269,13 +269,7 @@ static vkc_status gather_partitioned(vkc_ctx *ctx, const unsigned long long *src
     scan_counts(ctx, counts, m, reinterpret_cast<unsigned *>(b + o_sums), offs);
     gp_partition_kernel<<<tiles, GP_THREADS, 0, ctx->stream>>>(idx, n, nsrc, rb, tiles, offs, part, loc);
     gp_region_kernel<<<tiles, GP_THREADS, 0, ctx->stream>>>(src, part, counts, offs, tiles, rb, vals);
-    static std::atomic<unsigned long long> configured{0};
-    once_per_device(configured, ctx->device, [] {
-        cudaFuncSetAttribute(gp_restore_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             static_cast<int>(GP_TILE * sizeof(unsigned long long)));
-    });
-    gp_restore_kernel<<<tiles, GP_THREADS, GP_TILE * sizeof(unsigned long long), ctx->stream>>>(vals, loc, counts, offs,
-                                                                                             n, tiles, out);
+    gp_restore_kernel<<<tiles, GP_THREADS, 0, ctx->stream>>>(vals, loc, counts, offs, n, tiles, out);
     return launched(ctx, "gather_partitioned");
 }
 
