@@ -278,11 +278,13 @@ VKC_API vkc_status vkc_region_eval(vkc_ctx *ctx, const vkc_region_kernel *kernel
                                    const vkc_value *inputs, int ninputs, vkc_value *out);
 
 /* A fused region (src/exec/region/fused.rs): reduction `root` over arguments `root_args`
- * (sources as above) whose region arguments are the kernels' outputs. When the region matches
- * a fused kernel's pattern of the registry (src/kernels/scalar/fused.rs:286-379: dot_T,
- * sumsq_T, count_<cmp>_T, condsum_<cmp>_T) that kernel runs over the pattern's operands;
- * otherwise each region argument is evaluated by vkc_region_eval and the root is called once.
- * Values and errors are those of whole evaluation. Replaces eval_fused. */
+ * (sources as above) whose region arguments are the kernels' outputs. `count`, the extremes on
+ * f64 and i64 (reduce_min/max, argmin/argmax) and reduce_add_i64 over one region argument fold
+ * the region's value in its own pass (count(<cmp>_T(x, c)) is count_<cmp>_T); when the region
+ * matches another fused kernel's pattern of the registry (src/kernels/scalar/fused.rs:286-379:
+ * dot_T, sumsq_T, condsum_<cmp>_T) that kernel runs over the pattern's operands; otherwise each
+ * region argument is evaluated by vkc_region_eval and the root is called once. Values and
+ * errors are those of whole evaluation. Replaces eval_fused. */
 VKC_API vkc_status vkc_region_reduce(vkc_ctx *ctx, int root, const int32_t *root_args, int nroot,
                                      const vkc_region_kernel *kernels, int nkernels,
                                      const vkc_value *inputs, int ninputs, vkc_value *out);

@@ -11,8 +11,8 @@
 //  * `count` over a region counts the region's true rows as it evaluates them, and the extremes
 //    (reduce_min/max, argmin/argmax on f64 and i64) and the i64 sum fold them in the same pass;
 //  * a fused root whose region matches one of the registry's fused patterns
-//    (src/kernels/scalar/fused.rs:286-379: dot_T, sumsq_T, count_<cmp>_T, condsum_<cmp>_T are
-//    declared there as those compositions) runs as that fused reduction over the pattern's
+//    (src/kernels/scalar/fused.rs:286-379: dot_T, sumsq_T and condsum_<cmp>_T are declared
+//    there as those compositions) runs as that fused reduction over the pattern's
 //    operands; any other root is called once over its arguments, each region argument
 //    evaluated by one pass.
 #include <cstring>
@@ -216,8 +216,9 @@ std::string name_of(int id) {
 
 // The fused.rs patterns over a region that runs fused (so none of its kernels can fail):
 // reduce_add_T(mul_T(x, y)) is dot_T(x, y), or sumsq_T(x) when x and y are one array;
-// count(<cmp>_T(x, c)) is count_<cmp>_T(x, c); reduce_add_T(select_T(<cmp>_T(x, c), x, e)) is
-// condsum_<cmp>_T(x, c, e). Operands are region sources; true when one matched.
+// reduce_add_T(select_T(<cmp>_T(x, c), x, e)) is condsum_<cmp>_T(x, c, e). (count(<cmp>_T(x, c)),
+// count_<cmp>_T, is counted in the region's own pass.) Operands are region sources; true when one
+// matched.
 bool fused_pattern(const vkc_region_kernel *ks, const vkc_value *in, int root, const std::vector<Src> &args,
                    int *root2, std::vector<Src> *args2) {
     if (args.size() != 1 || !args[0].kernel) return false;
@@ -245,13 +246,6 @@ bool fused_pattern(const vkc_region_kernel *ks, const vkc_value *in, int root, c
         }
         for (const char *c : cmps) {
             const std::string cmp = std::string(c) + "_" + t;
-            if (rn == "count" && kn == cmp) {
-                const Src x = src_of(k.args[0]), v = src_of(k.args[1]);
-                if (!is_array(x) || !scalar_input(v)) return false;
-                if ((*root2 = vkc_kernel_lookup(("count_" + cmp).c_str())) < 0) return false;
-                *args2 = {x, v};
-                return true;
-            }
             if (rn == std::string("reduce_add_") + t && kn == std::string("select_") + t) {
                 const Src m = src_of(k.args[0]), a = src_of(k.args[1]), e = src_of(k.args[2]);
                 if (!m.kernel || name_of(ks[m.i].kernel) != cmp || !scalar_input(e)) continue;
