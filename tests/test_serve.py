@@ -120,3 +120,12 @@ def test_batched_group_sums_equal_the_plain_ones(ctx):
     big = [ctx.upload(np.full(n, i, np.uint8)) for i, n in enumerate([20_000, 8192, 8193, 1])]
     rows = ctx.batch_concat(ctx.batch(big), index=False)
     assert np.array_equal(rows.numpy(), np.concatenate([np.full(n, i, np.uint8) for i, n in enumerate([20_000, 8192, 8193, 1])]))
+    # Four-byte rows, views that start inside their arrays, and an empty batch.
+    src = np.arange(50_000, dtype=np.int32) * 7 - 3
+    whole = ctx.upload(src)
+    views = [whole.slice(5, 20_005), whole.slice(1, 2), whole.slice(30_000, 49_999)]
+    rows, index = ctx.batch_concat(ctx.batch(views))
+    assert np.array_equal(rows.numpy(), np.concatenate([src[5:20_005], src[1:2], src[30_000:49_999]]))
+    assert np.array_equal(index.numpy(), np.repeat(np.arange(3), [20_000, 1, 19_999]))
+    rows, index = ctx.batch_concat(ctx.batch([]))
+    assert len(rows) == 0 and len(index) == 0
