@@ -326,6 +326,12 @@ VKC_API vkc_status vkc_batch_dot_f64(vkc_ctx *ctx, vkc_batch *xs, vkc_batch *ys,
 VKC_API vkc_status vkc_batch_argsort_i64(vkc_ctx *ctx, vkc_batch *keys, const vkc_batch *outs,
                                          unsigned key_digits);
 
+/* Many rand_f64 (type VKC_F64) or rand_i64 (VKC_I64) statements in one launch: outs[i] gets
+ * rand(lens[i], seeds[i]), equal to that call's array (src/kernels/scalar/construct.rs:64-76).
+ * The arrays are views of one allocation. A negative length fails as rand does. */
+VKC_API vkc_status vkc_batch_rand(vkc_ctx *ctx, vkc_type type, int count, const int64_t *lens,
+                                  const int64_t *seeds, vkc_array **outs);
+
 /* The batch's arrays concatenated in the caller's order into a new array `rows` (the batch's
  * element type), and, when `index` is not NULL, a new i64 array naming the array of every row
  * (0 for the rows of the first array, and so on). A statement with no batched entry

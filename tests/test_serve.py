@@ -112,6 +112,12 @@ def test_batched_group_sums_equal_the_plain_ones(ctx):
     for a, b in zip(alone, reqs):
         assert b.batched
         assert np.array_equal(a.result.numpy(), b.result.numpy()), a.n
+    # Batched generators equal their own calls.
+    lens, seeds = [0, 1, 5, 1000, 70_001], [3, 4, 5, 6, 7]
+    for t in ("f64", "i64"):
+        got = ctx.batch_rand(t, lens, seeds)
+        for a, n, sd in zip(got, lens, seeds):
+            assert np.array_equal(a.numpy(), ctx.call("rand_" + t, n, sd).numpy())
     # The concatenation and its index column.
     arrays = [ctx.upload(np.arange(k, dtype=np.int64) * 3) for k in (5, 0, 3)]
     rows, index = ctx.batch_concat(ctx.batch(arrays))

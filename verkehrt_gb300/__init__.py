@@ -116,6 +116,8 @@ _SIGNATURES = {
     "vkc_batch_count_f64": (ctypes.c_int, [_P, _P, ctypes.c_int, ctypes.c_double, _P]),
     "vkc_batch_dot_f64": (ctypes.c_int, [_P, _P, _P, _P]),
     "vkc_batch_concat": (ctypes.c_int, [_P, _P, ctypes.POINTER(_P), ctypes.POINTER(_P)]),
+    "vkc_batch_rand": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int64),
+                                      ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(_P)]),
     "vkc_graph_begin": (ctypes.c_int, [_P]),
     "vkc_graph_end": (ctypes.c_int, [_P, ctypes.POINTER(_P)]),
     "vkc_graph_launch": (ctypes.c_int, [_P, _P]),
@@ -505,6 +507,15 @@ class Context:
     def batch_argsort(self, keys, outs, key_digits=0):
         """outs[i] = argsort_i64(keys[i]) for every array (enqueued)."""
         self._check(_lib.vkc_batch_argsort_i64(self.handle, keys.handle, outs.handle, key_digits))
+
+    def batch_rand(self, type_name, lens, seeds):
+        """rand_f64 / rand_i64 (type_name "f64" or "i64") of every (len, seed) pair, one launch."""
+        k = len(lens)
+        ln = (ctypes.c_int64 * max(1, k))(*[int(v) for v in lens])
+        sd = (ctypes.c_int64 * max(1, k))(*[int(v) for v in seeds])
+        outs = (_P * max(1, k))()
+        self._check(_lib.vkc_batch_rand(self.handle, TYPES[type_name], k, ln, sd, outs))
+        return [Array(self, outs[i]) for i in range(k)]
 
     def batch_concat(self, batch, index=True):
         """The batch's arrays concatenated in order, and (index=True) the i64 column naming each

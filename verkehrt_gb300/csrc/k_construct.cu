@@ -1,5 +1,7 @@
 // Construction kernels: rand_f64, rand_i64 and length_T
 // (src/kernels/scalar/construct.rs:12-17, :64-76, :99-106, :233-251).
+#include <algorithm>
+
 #include "kcommon.cuh"
 #include "registry.h"
 
@@ -81,6 +83,32 @@ static vkc_status rand_i64(vkc_ctx *c, const vkc_value *a, int n, vkc_value *o) 
     return run_rand(c, a, n, o, false);
 }
 
+// ------------------------------------------------------------------ batched generators
+//
+// Many rand_f64/rand_i64 statements (one per request of a batch) in one launch: block row y
+// fills statement y's array, each value the generator's value at its own (seed, row), so every
+// array equals its own rand call. The arrays are views of one allocation, each starting on a
+// 256-byte boundary.
+constexpr int RB_MAX = 512;  // statements per launch
+struct RandBatch {
+    int count;
+    long long start[RB_MAX], len[RB_MAX];
+    unsigned long long seed[RB_MAX];
+};
+
+template <bool F64>
+__global__ void __launch_bounds__(256) batch_rand_kernel(const RandBatch B, unsigned long long *__restrict__ base) {
+    const int sg = blockIdx.y;
+    const int64_t n = B.len[sg];
+    const unsigned long long seed = B.seed[sg];
+    unsigned long long *out = base + B.start[sg];
+    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const unsigned long long a = splitmix64(seed + static_cast<unsigned long long>(i));
+        __stcs(out + i, F64 ? unit53_bits(a) : a);
+    }
+}
+
 // construct.rs:99-106 (run_length): the handle knows its length, no kernel runs.
 static vkc_status length(vkc_ctx *ctx, const vkc_value *args, int nargs, vkc_value *out) {
     if (nargs != 1) return fail(ctx, VKC_USAGE, arity_error(1, nargs));
@@ -108,3 +136,46 @@ void register_construct(std::vector<KernelDef> &t) {
 }
 
 }  // namespace vkc
+
+using namespace vkc;
+
+extern "C" VKC_API vkc_status vkc_batch_rand(vkc_ctx *ctx, vkc_type type, int count, const int64_t *lens,
+                                            const int64_t *seeds, vkc_array **outs) {
+    if (!ctx || count < 0 || (count > 0 && (!lens || !seeds || !outs))) return VKC_USAGE;
+    if (type != VKC_F64 && type != VKC_I64) return fail(ctx, VKC_USAGE, "batch rand: f64 or i64 arrays");
+    for (int i = 0; i < count; ++i) {
+        outs[i] = nullptr;
+        if (lens[i] < 0) return fail(ctx, VKC_RUNTIME, "negative length " + std::to_string(lens[i]));
+    }
+    vkc_status st = VKC_OK;
+    for (int c0 = 0; c0 < count && !st; c0 += RB_MAX) {
+        const int m = std::min(count - c0, RB_MAX);
+        RandBatch B;
+        B.count = m;
+        int64_t total = 0, longest = 0;
+        for (int i = 0; i < m; ++i) {
+            B.start[i] = total;
+            B.len[i] = lens[c0 + i];
+            B.seed[i] = static_cast<unsigned long long>(seeds[c0 + i]);
+            total += (lens[c0 + i] + 31) / 32 * 32;  // 256-byte starts
+            longest = std::max<int64_t>(longest, lens[c0 + i]);
+        }
+        vkc_array *all;
+        if ((st = new_array(ctx, type, total, false, &all))) break;
+        if (longest > 0) {
+            const dim3 grid(static_cast<unsigned>(std::min<int64_t>((longest + 1023) / 1024, 64)), static_cast<unsigned>(m));
+            auto *base = static_cast<unsigned long long *>(all->data());
+            if (type == VKC_F64) batch_rand_kernel<true><<<grid, 256, 0, ctx->stream>>>(B, base);
+            else batch_rand_kernel<false><<<grid, 256, 0, ctx->stream>>>(B, base);
+            st = launched(ctx, "batch_rand");
+        }
+        for (int i = 0; i < m && !st; ++i) st = vkc_array_slice(ctx, all, B.start[i], B.len[i], &outs[c0 + i]);
+        vkc_array_release(all);  // the views hold the allocation
+    }
+    if (st)
+        for (int i = 0; i < count; ++i) {
+            vkc_array_release(outs[i]);
+            outs[i] = nullptr;
+        }
+    return st;
+}

@@ -7,7 +7,8 @@ server keeps the GPU busy with them:
 * every worker owns a context (its own CUDA stream and allocator cache), so the work of
   different workers overlaps on the device;
 * a worker that frees up takes the oldest waiting request's kind and coalesces every waiting
-  small request of that kind into one batched launch (vkc_batch_*), as long as the group fits
+  small request of that kind into one batched launch (vkc_batch_*, the requests' generator
+  statements included), as long as the group fits
   the free part of the device-memory budget; a large request runs alone through the plain
   entries;
 * admission: a request is only started when the bytes it holds at its peak fit the budget left
@@ -103,33 +104,38 @@ def run_one(ctx, r):
 
 
 def run_batch(ctx, reqs):
-    """Same-kind requests as one batched launch (the inputs are generated per request)."""
+    """Same-kind requests as one batched launch; their generator statements are batched too
+    (vkc_batch_rand: one launch for every request's rand call, each array that call's)."""
     kind = reqs[0].kind
+    lens = [r.n for r in reqs]
+    seeds = [r.seed for r in reqs]
+    seeds1 = [r.seed + 1 for r in reqs]
     if kind == "dot":
-        xs = [ctx.call("rand_f64", r.n, r.seed) for r in reqs]
-        ys = [ctx.call("rand_f64", r.n, r.seed + 1) for r in reqs]
+        xs = ctx.batch_rand("f64", lens, seeds)
+        ys = ctx.batch_rand("f64", lens, seeds1)
         sums = ctx.new_array("f64", len(reqs))
         ctx.batch_dot(ctx.batch(xs), ctx.batch(ys), sums)
         out = sums.numpy().view(np.uint64)
         for r, v in zip(reqs, out):
             r.result = int(v)
     elif kind == "filter_len":
-        xs = [ctx.call("rand_f64", r.n, r.seed) for r in reqs]
+        xs = ctx.batch_rand("f64", lens, seeds)
         counts = ctx.new_array("i64", len(reqs))
         ctx.batch_count(ctx.batch(xs), "gt", THRESHOLD, counts)
         for r, v in zip(reqs, counts.numpy()):
             r.result = int(v)
     elif kind == "argsort":
-        ks = [ctx.call("rand_i64", r.n, r.seed) for r in reqs]
+        ks = ctx.batch_rand("i64", lens, seeds)
         outs = [ctx.new_array("i64", r.n) for r in reqs]
         ctx.batch_argsort(ctx.batch(ks), ctx.batch(outs))
         for r, o in zip(reqs, outs):
             r.result = o
     else:
-        keys = [ctx.call("and_i64", ctx.call("rand_i64", r.n, r.seed), KEY_MASK) for r in reqs]
-        vals = [ctx.call("and_i64", ctx.call("rand_i64", r.n, r.seed + 1), KEY_MASK) for r in reqs]
-        kcat, index = ctx.batch_concat(ctx.batch(keys))
-        vcat = ctx.batch_concat(ctx.batch(vals), index=False)
+        # The masks apply row by row, so they run once over the concatenations.
+        kraw, index = ctx.batch_concat(ctx.batch(ctx.batch_rand("i64", lens, seeds)))
+        vraw = ctx.batch_concat(ctx.batch(ctx.batch_rand("i64", lens, seeds1)), index=False)
+        kcat = ctx.call("and_i64", kraw, KEY_MASK)
+        vcat = ctx.call("and_i64", vraw, KEY_MASK)
         g = ctx.call("group_id2_i64_i64", index, kcat)
         nb = ctx.call("reduce_max_i64", g) + 1 if len(g) else 0
         sums = ctx.call("reduce_into_add_i64", g, vcat, nb)
