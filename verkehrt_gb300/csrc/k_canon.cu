@@ -1044,25 +1044,7 @@ __global__ void __launch_bounds__(WK_THREADS) canon_walk_kernel(RowArgs args, in
         }
     }
     __syncthreads();
-    if (t >= 32) {
-        // Warps 1.. prefetch into L2 the lane's rows of the tiles the walk will likely resolve
-        // from the rows: in the mixed chunks held here, tiles with no record or with records in
-        // two binades (their range spans a binade boundary). The walk's loads then hit L2.
-        if (!held) return;
-        const int nm = min(sm.nmixed, WK_MAX_MIXED), lane = t & 31;
-        for (int q = (t >> 5) - 1; q < nm * 32; q += WK_THREADS / 32 - 1) {  // a tile per warp
-            const int slot = q >> 5, j = q & 31;
-            const int tp = sm.chunk_of[slot] * 32 + j;
-            if (tp >= T || (sm.mE[slot][j][0] != NO_E && sm.mE[slot][j][1] == NO_E)) continue;
-            for (int blk = lane; blk < CT_BLOCKS; blk += 32) {
-                const int64_t b = static_cast<int64_t>(tp) * CT_BLOCKS + blk;
-                if (b >= nb) break;
-                asm volatile("prefetch.global.L2 [%0];" ::"l"(args.x + b * 16 + L));
-                if (OP == ROW_DOT) asm volatile("prefetch.global.L2 [%0];" ::"l"(args.y + b * 16 + L));
-            }
-        }
-        return;
-    }
+    if (t >= 32) return;
     const int lane = t;
     unsigned long long s = state->lanes[L];
     int stop = -1;
