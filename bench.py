@@ -609,7 +609,7 @@ def run_batched(ctx, count=4096, lo=10, hi=18, reps=2):
 SERVED_MIXES = {
     "mixed": {"n_lo": 1e3, "n_hi": 1e8, "rates": (500, 1000, 1500, 2000, 2500, 3000, 4000, 6400),
               "p99_bound_ms": 100.0},
-    "small": {"n_lo": 1e3, "n_hi": 1e5, "rates": (1000, 2500, 5000, 10000, 20000, 40000),
+    "small": {"n_lo": 1e3, "n_hi": 1e5, "rates": (1000, 2500, 5000, 10000, 20000, 40000, 60000, 80000, 120000),
               "p99_bound_ms": 20.0},
 }
 
