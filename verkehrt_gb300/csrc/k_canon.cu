@@ -322,8 +322,6 @@ struct CanonWork {
     int *whole = nullptr;                  // scans: [16][C] chunks the walk took whole
     int *resume = nullptr;                 // reductions: [16] tile where the lane chain takes over
                                            // from the walk (T: the walk finished the lane)
-    int *superE = nullptr;                 // reductions: [16][CS] binade of each 32-chunk
-    TF *superD = nullptr;                  // superchunk's transfer function (NO_E: none)
 };
 
 constexpr int CAND_GROUP = 1024;  // tiles per K2 block
@@ -776,39 +774,6 @@ __global__ void __launch_bounds__(256) canon_chunk_kernel(int T, int C, CanonWor
     }
 }
 
-// K4a': per lane and superchunk of 32 chunks (one warp each), the composed transfer function
-// when every chunk of it has one in the same binade (chunks past C are the identity). The walk
-// of a reduction applies these first, so a run of chunks in one binade costs one step per 32
-// superchunks instead of one per 32 chunks.
-__global__ void __launch_bounds__(256) canon_super_kernel(int C, CanonWork wk) {
-    const int lane = threadIdx.x & 31;
-    const int CS = (C + 31) / 32;
-    const int64_t gw = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
-    if (gw >= static_cast<int64_t>(16) * CS) return;
-    const int L = static_cast<int>(gw / CS), sk = static_cast<int>(gw % CS);
-    const int k = sk * 32 + lane;
-    const int E = __shfl_sync(FULL, k < C ? wk.chunkE[static_cast<int64_t>(L) * C + k] : NO_E, 0);
-    TF f{0, 0};
-    bool ok = k >= C;
-    if (k < C && wk.chunkE[static_cast<int64_t>(L) * C + k] == E) {
-        f = wk.chunkD[static_cast<int64_t>(L) * C + k];
-        ok = true;
-    }
-    if (!__all_sync(FULL, ok) || E == NO_E) {
-        if (lane == 0) wk.superE[static_cast<int64_t>(L) * CS + sk] = NO_E;
-        return;
-    }
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        TF other = TF{__shfl_down_sync(FULL, f.d0, o), __shfl_down_sync(FULL, f.d1, o)};
-        if (lane + o < 32) f = compose(f, other);
-    }
-    if (lane == 0) {
-        wk.superE[static_cast<int64_t>(L) * CS + sk] = E;
-        wk.superD[static_cast<int64_t>(L) * CS + sk] = f;
-    }
-}
-
 // The binade of |s| (s normal and finite), NO_E otherwise.
 __device__ __forceinline__ int state_binade(unsigned long long s) {
     const unsigned long long e = (s >> 52) & 0x7ff;
@@ -999,23 +964,6 @@ __device__ __forceinline__ unsigned long long walk_lane(const RowArgs &args, int
         if (!RECORD && clk.slower(k * 32)) {
             *stop = k * 32;
             return s;
-        }
-        if (!RECORD && (k & 31) == 0) {
-            // Whole superchunks k / 32 .. k / 32 + 31.
-            const int CS = (C + 31) / 32, E = state_binade(s), sk = (k >> 5) + lane;
-            int se = NO_E;
-            TF f{0, 0};
-            if (sk < CS) {
-                se = wk.superE[static_cast<int64_t>(L) * CS + sk];
-                if (se != NO_E && se == E) f = wk.superD[static_cast<int64_t>(L) * CS + sk];
-            }
-            unsigned long long r = s;
-            const int m = E == NO_E ? 0 : apply_prefix<SIGNED>(f, sk < CS && se != NO_E && se == E, s, E, &r);
-            if (m > 0) {
-                s = r;
-                k += 32 * m;
-                continue;
-            }
         }
         // Whole chunks k .. k+31.
         const int E = state_binade(s);
@@ -1380,11 +1328,6 @@ static vkc_status launch_canon(vkc_ctx *ctx, const RowArgs &a, int64_t nb, int T
     int warps = 16 * C;
     canon_chunk_kernel<<<(warps + 7) / 8, 256, 0, ctx->stream>>>(T, C, wk);
     if ((st = launched(ctx, "canon_chunk"))) return st;
-    if constexpr (!RECORD) {
-        const int swarps = 16 * ((C + 31) / 32);
-        canon_super_kernel<<<(swarps + 7) / 8, 256, 0, ctx->stream>>>(C, wk);
-        if ((st = launched(ctx, "canon_super"))) return st;
-    }
     static std::atomic<unsigned long long> configured{0};
     once_per_device(configured, ctx->device, [] {
         cudaFuncSetAttribute(canon_walk_kernel<OP, RECORD>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1435,19 +1378,13 @@ static size_t canon_layout(int T, int C, bool scan, char *b, CanonWork *wk, Cano
     const size_t o_wh = o_ts + up(static_cast<size_t>(T + 1) * 16 * sizeof(unsigned long long));
     const size_t o_cs = o_wh + up(c16 * sizeof(int));
     const size_t o_rs = up(o_fl + static_cast<size_t>(2 * T + 2) * sizeof(int));
-    const size_t s16 = static_cast<size_t>((C + 31) / 32) * 16;
-    const size_t o_suE = up(o_rs + 16 * sizeof(int)), o_suD = o_suE + up(s16 * sizeof(int));
-    const size_t total = scan ? o_cs + sizeof(CanonState) : o_suD + s16 * sizeof(TF);
+    const size_t total = scan ? o_cs + sizeof(CanonState) : o_rs + 16 * sizeof(int);
     if (b) {
         *wk = CanonWork{reinterpret_cast<float *>(b), reinterpret_cast<int *>(b + o_cand),
                         reinterpret_cast<int *>(b + o_recE), reinterpret_cast<TF *>(b + o_recD),
                         reinterpret_cast<int *>(b + o_chE), reinterpret_cast<TF *>(b + o_chD),
                         reinterpret_cast<double *>(b + o_gs), reinterpret_cast<int *>(b + o_fl)};
-        if (!scan) {
-            wk->resume = reinterpret_cast<int *>(b + o_rs);
-            wk->superE = reinterpret_cast<int *>(b + o_suE);
-            wk->superD = reinterpret_cast<TF *>(b + o_suD);
-        }
+        if (!scan) wk->resume = reinterpret_cast<int *>(b + o_rs);
         if (scan) {
             wk->tstate = reinterpret_cast<unsigned long long *>(b + o_ts);
             wk->whole = reinterpret_cast<int *>(b + o_wh);
