@@ -126,6 +126,29 @@ class Tree:
         return self.kernel("cast_%s_%s" % (s, t), [self.gen(s, depth - 1)], t)
 
 
+class F64Tree(Tree):
+    """Random regions of f64 arithmetic and comparisons (the f64 evaluator's regions): a
+    comparison feeds a select's mask or is the region's value."""
+
+    def gen(self, t, depth, may_scalar=False):
+        r = self.rng
+        if t == "bool":  # always a comparison (the evaluator's inputs are f64)
+            op = r.choice(["lt", "le", "gt", "ge", "eq", "ne"])
+            d = max(depth - 1, 0)
+            return self.kernel(op + "_f64", [self.gen("f64", d), self.gen("f64", d, True)], "bool")
+        if depth == 0 or len(self.kernels) >= self.max_kernels or r.random() < 0.25:
+            return self.scalar("f64") if may_scalar and r.random() < 0.4 else self.array("f64")
+        c = r.random()
+        if c < 0.5:
+            op = r.choice(["add", "sub", "mul", "div", "min", "max"])
+            return self.kernel(op + "_f64", [self.gen("f64", depth - 1), self.gen("f64", depth - 1, True)], "f64")
+        if c < 0.75:
+            op = r.choice(["neg", "abs", "sqrt"])
+            return self.kernel(op + "_f64", [self.gen("f64", depth - 1)], "f64")
+        return self.kernel("select_f64", [self.gen("bool", depth - 1), self.gen("f64", depth - 1),
+                                          self.gen("f64", depth - 1, True)], "f64")
+
+
 def device_inputs(ctx, tree):
     import verkehrt_gb300 as vk
 
@@ -192,6 +215,25 @@ def test_random_regions_equal_whole_evaluation_and_the_oracle(ctx, n):
         assert same(got.numpy(), oracle_eval(tree), t), (n, case, tree.kernels)
         checked += 1
     assert checked == 40
+
+
+@pytest.mark.parametrize("n", [1, 777, 100_003])
+def test_random_f64_regions(ctx, n):
+    rng = random.Random(7 * n)
+    for case in range(40):
+        tree = F64Tree(rng, n, 100 + case)
+        t = rng.choice(["f64", "f64", "bool"])
+        top = tree.gen(t, depth=rng.randint(1, 4))
+        if top >= 0:  # a leaf (f64 only): make it a region of one kernel
+            top = tree.kernel("add_f64", [top, top], "f64")
+        dev = device_inputs(ctx, tree)
+        got = ctx.region(tree.kernels, dev)
+        assert same(got.numpy(), whole(ctx, tree.kernels, dev).numpy(), t), (n, case, tree.kernels)
+        assert same(got.numpy(), oracle_eval(tree), t), (n, case, tree.kernels)
+        if t == "bool":
+            k = len(tree.kernels) - 1
+            want = int(np.count_nonzero(oracle_eval(tree)))
+            assert ctx.region_reduce("count", [-1 - k], tree.kernels, dev) == want
 
 
 def test_region_errors_are_whole_evaluation_errors(ctx):

@@ -594,6 +594,99 @@ vkc_status launch_region_fold(vkc_ctx *ctx, const RegionProg &p, int64_t n, int 
     return launched(ctx, "region_fold");
 }
 
+// Regions of f64 arithmetic and comparisons over f64 inputs: values held as doubles (a
+// comparison's result as 1.0 or 0.0, read back by select_f64 and by the output as a bool), the
+// same row operations as the kernels' own entries, no type dispatch and no word conversions.
+template <bool COUNT>
+__global__ void __launch_bounds__(RG_THREADS) region_f64_kernel(const RegionProg P, int64_t n, void *__restrict__ out) {
+    extern __shared__ double s_d[];
+    const int t = threadIdx.x;
+    unsigned long long nonzero = 0;
+    for (int64_t b0 = static_cast<int64_t>(blockIdx.x) * RG_BLOCK_ROWS; b0 < n;
+         b0 += static_cast<int64_t>(gridDim.x) * RG_BLOCK_ROWS) {
+        const int64_t base = b0 + t;
+        double inv[RG_MAX_ARR][RG_ROWS];
+#pragma unroll
+        for (int j = 0; j < RG_MAX_ARR; ++j) {
+            const double *q = static_cast<const double *>(P.in[j].p);
+#pragma unroll
+            for (int r = 0; r < RG_ROWS; ++r) inv[j][r] = (q && base + r * RG_THREADS < n) ? __ldcs(q + base + r * RG_THREADS) : 0.0;
+        }
+        double prev[RG_ROWS];
+        for (int k = 0; k < P.nk; ++k) {
+            const RgOp &o = P.op[k];
+            double a[3][RG_ROWS];
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                const int kind = o.kind[j], idx = o.idx[j];
+                if (kind == RK_IN) {
+                    switch (idx) {
+#define RG_IN_CASE(q)                                                          \
+    case q:                                                                    \
+        _Pragma("unroll") for (int r = 0; r < RG_ROWS; ++r) a[j][r] = inv[q][r]; \
+        break;
+                        RG_IN_CASE(0) RG_IN_CASE(1) RG_IN_CASE(2) default: RG_IN_CASE(3)
+#undef RG_IN_CASE
+                    }
+                } else if (kind == RK_CONST) {
+#pragma unroll
+                    for (int r = 0; r < RG_ROWS; ++r) a[j][r] = __longlong_as_double(static_cast<long long>(o.c[j]));
+                } else if (kind == RK_PREV) {
+#pragma unroll
+                    for (int r = 0; r < RG_ROWS; ++r) a[j][r] = prev[r];
+                } else {
+#pragma unroll
+                    for (int r = 0; r < RG_ROWS; ++r) a[j][r] = s_d[idx * RG_BLOCK_ROWS + t + r * RG_THREADS];
+                }
+            }
+#define RG_F(EXPR)                                                                     \
+    {                                                                                  \
+        _Pragma("unroll") for (int r = 0; r < RG_ROWS; ++r) {                          \
+            const double x = a[0][r], y = a[1][r];                                     \
+            (void)y;                                                                   \
+            prev[r] = (EXPR);                                                          \
+        }                                                                              \
+        break;                                                                         \
+    }
+            switch (o.fn) {
+            case EF_ADD: RG_F(ew_add(x, y))
+            case EF_SUB: RG_F(ew_sub(x, y))
+            case EF_MUL: RG_F(ew_mul(x, y))
+            case EF_DIV: RG_F(ew_div(x, y))
+            case EF_MIN: RG_F(ew_min(x, y))
+            case EF_MAX: RG_F(ew_max(x, y))
+            case EF_NEG: RG_F(ew_neg(x))
+            case EF_ABS: RG_F(ew_abs(x))
+            case EF_SQRT: RG_F(ew_sqrt(x))
+            case EF_LT: RG_F(x < y ? 1.0 : 0.0)
+            case EF_LE: RG_F(x <= y ? 1.0 : 0.0)
+            case EF_GT: RG_F(x > y ? 1.0 : 0.0)
+            case EF_GE: RG_F(x >= y ? 1.0 : 0.0)
+            case EF_EQ: RG_F(x == y ? 1.0 : 0.0)
+            case EF_NE: RG_F(x != y ? 1.0 : 0.0)
+            default: RG_F(x != 0.0 ? y : a[2][r])  // EF_SELECT: the mask is 1.0 or 0.0
+            }
+#undef RG_F
+            if (o.keep) {
+#pragma unroll
+                for (int r = 0; r < RG_ROWS; ++r) s_d[o.slot * RG_BLOCK_ROWS + t + r * RG_THREADS] = prev[r];
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < RG_ROWS; ++r) {
+            const int64_t i = base + r * RG_THREADS;
+            if (i >= n) break;
+            if (COUNT) nonzero += prev[r] != 0.0;
+            else if (P.out_width == 8) static_cast<double *>(out)[i] = prev[r];
+            else static_cast<unsigned char *>(out)[i] = prev[r] != 0.0;
+        }
+    }
+    if (COUNT) {
+        nonzero = warp_sum(nonzero);
+        if ((t & 31) == 0 && nonzero) atomicAdd(static_cast<unsigned long long *>(out), nonzero);
+    }
+}
+
 vkc_status launch_region(vkc_ctx *ctx, const RegionProg &p, int64_t n, void *out, bool count) {
     if (n <= 0) return VKC_OK;
     const size_t smem = static_cast<size_t>(p.nslots) * RG_BLOCK_ROWS * sizeof(unsigned long long);
@@ -603,13 +696,27 @@ vkc_status launch_region(vkc_ctx *ctx, const RegionProg &p, int64_t n, void *out
         cudaFuncSetAttribute(region_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, most);
         cudaFuncSetAttribute(region_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, most);
     });
+    static std::atomic<unsigned long long> configured_f64{0};
+    once_per_device(configured_f64, ctx->device, [] {
+        const int most = static_cast<int>(RG_MAX_K * RG_BLOCK_ROWS * sizeof(double));
+        cudaFuncSetAttribute(region_f64_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, most);
+        cudaFuncSetAttribute(region_f64_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, most);
+    });
     int per_sm = 0;
-    if (count) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, region_kernel<true>, RG_THREADS, smem);
-    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, region_kernel<false>, RG_THREADS, smem);
+    const void *kern = p.f64only ? (count ? reinterpret_cast<const void *>(region_f64_kernel<true>)
+                                          : reinterpret_cast<const void *>(region_f64_kernel<false>))
+                                 : (count ? reinterpret_cast<const void *>(region_kernel<true>)
+                                          : reinterpret_cast<const void *>(region_kernel<false>));
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, RG_THREADS, smem);
     const int64_t blocks = (n + RG_BLOCK_ROWS - 1) / RG_BLOCK_ROWS;
     const int grid = static_cast<int>(std::min<int64_t>(blocks, static_cast<int64_t>(ctx->sms) * std::max(1, per_sm)));
-    if (count) region_kernel<true><<<grid, RG_THREADS, smem, ctx->stream>>>(p, n, out);
-    else region_kernel<false><<<grid, RG_THREADS, smem, ctx->stream>>>(p, n, out);
+    if (p.f64only) {
+        if (count) region_f64_kernel<true><<<grid, RG_THREADS, smem, ctx->stream>>>(p, n, out);
+        else region_f64_kernel<false><<<grid, RG_THREADS, smem, ctx->stream>>>(p, n, out);
+    } else {
+        if (count) region_kernel<true><<<grid, RG_THREADS, smem, ctx->stream>>>(p, n, out);
+        else region_kernel<false><<<grid, RG_THREADS, smem, ctx->stream>>>(p, n, out);
+    }
     return launched(ctx, "region");
 }
 

@@ -129,6 +129,24 @@ bool plan_region(const vkc_region_kernel *ks, int nk, const vkc_value *in, int n
     *out_type = ty.back();
     p->out_width = type_width(*out_type);
     *n = len;
+    // f64 arithmetic and comparisons only, over f64 inputs: the f64 evaluator. A comparison's
+    // result may feed only select_f64's mask or be the region's value.
+    bool f64 = true;
+    for (int j = 0; j < nin && f64; ++j)
+        f64 = (in[j].kind == VKC_VALUE_ARRAY ? in[j].array->type : in[j].scalar.type) == VKC_F64;
+    for (int k = 0; k < nk && f64; ++k) {
+        const RgOp &o = p->op[k];
+        const bool cmp = o.fn == EF_LT || o.fn == EF_LE || o.fn == EF_GT || o.fn == EF_GE || o.fn == EF_EQ || o.fn == EF_NE;
+        const bool arith = o.fn == EF_ADD || o.fn == EF_SUB || o.fn == EF_MUL || o.fn == EF_DIV || o.fn == EF_MIN ||
+                           o.fn == EF_MAX || o.fn == EF_NEG || o.fn == EF_ABS || o.fn == EF_SQRT || o.fn == EF_SELECT;
+        f64 = o.ty == ET_F64 && (cmp || arith);
+        for (int k2 = k + 1; k2 < nk && f64 && cmp; ++k2)  // who reads a comparison's value
+            for (int j = 0; j < ks[k2].nargs; ++j) {
+                const Src s = src_of(ks[k2].args[j]);
+                if (s.kernel && s.i == k && !(p->op[k2].fn == EF_SELECT && j == 0)) f64 = false;
+            }
+    }
+    p->f64only = f64;
     return true;
 }
 

@@ -50,6 +50,7 @@ struct RgOp {
 };
 struct RegionProg {
     int nk, nslots, out_width, narr;
+    int f64only;  // every kernel f64 arithmetic or an f64 comparison, every input f64 (region_f64_kernel)
     RgIn in[RG_MAX_ARR];  // the array inputs, numbered in input order
     RgOp op[RG_MAX_K];
 };
