@@ -594,6 +594,40 @@ vkc_status launch_region_fold(vkc_ctx *ctx, const RegionProg &p, int64_t n, int 
     return launched(ctx, "region_fold");
 }
 
+// The IEEE orderings of doubles on their bits (kcommon.cuh's order keys rank -0 just below +0;
+// a NaN is unordered and unequal), so that comparisons leave the FP64 unit to the arithmetic,
+// and a comparison's result as 1.0 or +0.0, tested on its bits.
+__device__ __forceinline__ bool f64_nan_v(double v) {
+    return (static_cast<unsigned long long>(__double_as_longlong(v)) & 0x7fffffffffffffffull) > 0x7ff0000000000000ull;
+}
+__device__ __forceinline__ bool f64_zeros_v(double x, double y) {
+    return ((static_cast<unsigned long long>(__double_as_longlong(x)) | static_cast<unsigned long long>(__double_as_longlong(y))) &
+            0x7fffffffffffffffull) == 0;
+}
+__device__ __forceinline__ bool f64_less(double x, double y) {
+    const unsigned long long a = __double_as_longlong(x), b = __double_as_longlong(y);
+    return !f64_nan_v(x) && !f64_nan_v(y) && f64_key(a) < f64_key(b) && !f64_zeros_v(x, y);
+}
+__device__ __forceinline__ bool f64_less_eq(double x, double y) {
+    const unsigned long long a = __double_as_longlong(x), b = __double_as_longlong(y);
+    return !f64_nan_v(x) && !f64_nan_v(y) && (f64_key(a) <= f64_key(b) || f64_zeros_v(x, y));
+}
+__device__ __forceinline__ bool f64_equal(double x, double y) {
+    return !f64_nan_v(x) && (__double_as_longlong(x) == __double_as_longlong(y) || f64_zeros_v(x, y));
+}
+// ew_min / ew_max with the order keys where no row is a NaN (the key order ranks -0 below +0, as
+// the 754-2019 minimum and maximum do); a NaN row takes ew_min / ew_max itself.
+__device__ __forceinline__ double rg_min(double x, double y) {
+    if (f64_nan_v(x) || f64_nan_v(y)) return ew_min(x, y);
+    return f64_key(__double_as_longlong(x)) <= f64_key(__double_as_longlong(y)) ? x : y;
+}
+__device__ __forceinline__ double rg_max(double x, double y) {
+    if (f64_nan_v(x) || f64_nan_v(y)) return ew_max(x, y);
+    return f64_key(__double_as_longlong(x)) >= f64_key(__double_as_longlong(y)) ? x : y;
+}
+__device__ __forceinline__ double rg_one(bool c) { return __longlong_as_double(c ? 0x3ff0000000000000ll : 0ll); }
+__device__ __forceinline__ bool rg_true(double v) { return __double_as_longlong(v) != 0; }
+
 // Regions of f64 arithmetic and comparisons over f64 inputs: values held as doubles (a
 // comparison's result as 1.0 or 0.0, read back by select_f64 and by the output as a bool), the
 // same row operations as the kernels' own entries, no type dispatch and no word conversions.
@@ -653,18 +687,18 @@ __global__ void __launch_bounds__(RG_THREADS) region_f64_kernel(const RegionProg
             case EF_SUB: RG_F(ew_sub(x, y))
             case EF_MUL: RG_F(ew_mul(x, y))
             case EF_DIV: RG_F(ew_div(x, y))
-            case EF_MIN: RG_F(ew_min(x, y))
-            case EF_MAX: RG_F(ew_max(x, y))
+            case EF_MIN: RG_F(rg_min(x, y))
+            case EF_MAX: RG_F(rg_max(x, y))
             case EF_NEG: RG_F(ew_neg(x))
             case EF_ABS: RG_F(ew_abs(x))
             case EF_SQRT: RG_F(ew_sqrt(x))
-            case EF_LT: RG_F(x < y ? 1.0 : 0.0)
-            case EF_LE: RG_F(x <= y ? 1.0 : 0.0)
-            case EF_GT: RG_F(x > y ? 1.0 : 0.0)
-            case EF_GE: RG_F(x >= y ? 1.0 : 0.0)
-            case EF_EQ: RG_F(x == y ? 1.0 : 0.0)
-            case EF_NE: RG_F(x != y ? 1.0 : 0.0)
-            default: RG_F(x != 0.0 ? y : a[2][r])  // EF_SELECT: the mask is 1.0 or 0.0
+            case EF_LT: RG_F(rg_one(f64_less(x, y)))
+            case EF_LE: RG_F(rg_one(f64_less_eq(x, y)))
+            case EF_GT: RG_F(rg_one(f64_less(y, x)))
+            case EF_GE: RG_F(rg_one(f64_less_eq(y, x)))
+            case EF_EQ: RG_F(rg_one(f64_equal(x, y)))
+            case EF_NE: RG_F(rg_one(!f64_equal(x, y)))
+            default: RG_F(rg_true(x) ? y : a[2][r])  // EF_SELECT: the mask is 1.0 or +0.0
             }
 #undef RG_F
             if (o.keep) {
@@ -676,9 +710,9 @@ __global__ void __launch_bounds__(RG_THREADS) region_f64_kernel(const RegionProg
         for (int r = 0; r < RG_ROWS; ++r) {
             const int64_t i = base + r * RG_THREADS;
             if (i >= n) break;
-            if (COUNT) nonzero += prev[r] != 0.0;
+            if (COUNT) nonzero += rg_true(prev[r]);
             else if (P.out_width == 8) static_cast<double *>(out)[i] = prev[r];
-            else static_cast<unsigned char *>(out)[i] = prev[r] != 0.0;
+            else static_cast<unsigned char *>(out)[i] = rg_true(prev[r]);
         }
     }
     if (COUNT) {
