@@ -864,7 +864,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--n", type=int, default=1 << 28)
-    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--e2e-steps", type=int, default=9)
     ap.add_argument("--cpu-sample", type=int, default=1 << 23)
     ap.add_argument("--cpu-procs", type=int, default=0,
                     help="host processes of the reference arm (0: every core this process may use)")

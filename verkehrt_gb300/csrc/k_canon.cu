@@ -1546,7 +1546,7 @@ __device__ __forceinline__ unsigned long long add_bits(unsigned long long s, uns
 // segments' rows one at a time (add_bits) for the state after every block; a lane whose segments
 // do not all apply (a binade crossing, a negative row or state, the first tile) runs its whole
 // chain in one thread instead. (4) The combines of the states, (5) the tails, in add_bits.
-__global__ void __launch_bounds__(256) canon_scan_kernel(const unsigned long long *__restrict__ x, int64_t n, int64_t nb,
+__global__ void __launch_bounds__(256, 3) canon_scan_kernel(const unsigned long long *__restrict__ x, int64_t n, int64_t nb,
                                                          int T, const unsigned long long *__restrict__ tstate,
                                                          unsigned long long *__restrict__ out) {
     extern __shared__ __align__(16) unsigned char scan_smem[];
@@ -1555,7 +1555,19 @@ __global__ void __launch_bounds__(256) canon_scan_kernel(const unsigned long lon
     const int64_t row0 = static_cast<int64_t>(t) * (CT_BLOCKS * 16);
     const int64_t left = n - row0;
     const int rows = left < CT_BLOCKS * 16 ? static_cast<int>(left) : CT_BLOCKS * 16;
-    for (int i = tid; i < rows; i += 256) sm.v[(i >> 4) * SCAN_PAD + (i & 15)] = x[row0 + i];
+    {  // all 16 loads of a thread in flight before the first store
+        unsigned long long pre[CT_BLOCKS * 16 / 256];
+#pragma unroll
+        for (int q = 0; q < CT_BLOCKS * 16 / 256; ++q) {
+            const int i = tid + q * 256;
+            pre[q] = i < rows ? x[row0 + i] : 0ull;
+        }
+#pragma unroll
+        for (int q = 0; q < CT_BLOCKS * 16 / 256; ++q) {
+            const int i = tid + q * 256;
+            if (i < rows) sm.v[(i >> 4) * SCAN_PAD + (i & 15)] = pre[q];
+        }
+    }
     // The tile's whole blocks (all but a partial last one) feed the lanes.
     const int64_t whole = nb - static_cast<int64_t>(t) * CT_BLOCKS;
     const int fb = whole <= 0 ? 0 : (whole < CT_BLOCKS ? static_cast<int>(whole) : CT_BLOCKS);
@@ -1714,12 +1726,14 @@ static vkc_status scan_add_f64(vkc_ctx *ctx, const vkc_value *args, int, vkc_val
 }
 
 // scan_by_add_f64: each segment (from a row whose start flag is set, row 0 always, to the next)
-// is scanned with its lanes numbered from its first row. Segment heads are listed in order
-// (a count per 4096-row tile, a scan, an ordered write); one thread scans each segment of at
-// most SB_SHORT rows in registers (the 16 lanes, each block's combine and tail); longer
-// segments, listed for the host, take the tiled scan above on their rows.
-constexpr int SB_TILE = 4096;
+// is scanned with its lanes numbered from its first row. Segment heads are listed in order (a
+// count per 1024-row tile, a scan, an ordered write). One block per tile then takes the segments
+// whose heads lie in the tile: consecutive segments packed into runs of at most SBP_CAP rows,
+// staged in shared memory; a segment longer than that in windows of SBP_CAP rows that carry its
+// lane states; segments longer than SB_SHORT are listed for the host and take the tiled scan.
+constexpr int SB_TILE = 1024;
 constexpr int64_t SB_SHORT = int64_t(1) << 16;
+constexpr int SBP_CAP = 1536, SBP_THREADS = 128, SBP_RPT = SBP_CAP / SBP_THREADS;  // 12 rows a thread
 
 __device__ __forceinline__ unsigned sb_heads(const unsigned char *__restrict__ starts, int64_t n, int64_t r0, unsigned *mask) {
     unsigned m = 0;
@@ -1732,16 +1746,16 @@ __device__ __forceinline__ unsigned sb_heads(const unsigned char *__restrict__ s
     return __popc(m);
 }
 
-__global__ void __launch_bounds__(256) sb_count_kernel(const unsigned char *__restrict__ starts, int64_t n,
-                                                       unsigned *__restrict__ counts) {
+__global__ void __launch_bounds__(SB_TILE / 16) sb_count_kernel(const unsigned char *__restrict__ starts, int64_t n,
+                                                                unsigned *__restrict__ counts) {
     unsigned m, total;
     const unsigned c = sb_heads(starts, n, static_cast<int64_t>(blockIdx.x) * SB_TILE + threadIdx.x * 16, &m);
     block_exclusive_sum<unsigned>(c, &total);
     if (threadIdx.x == 0) counts[blockIdx.x] = total;
 }
 
-__global__ void __launch_bounds__(256) sb_list_kernel(const unsigned char *__restrict__ starts, int64_t n,
-                                                      const unsigned *__restrict__ offs, long long *__restrict__ heads) {
+__global__ void __launch_bounds__(SB_TILE / 16) sb_list_kernel(const unsigned char *__restrict__ starts, int64_t n,
+                                                               const unsigned *__restrict__ offs, long long *__restrict__ heads) {
     unsigned m, total;
     const int64_t r0 = static_cast<int64_t>(blockIdx.x) * SB_TILE + threadIdx.x * 16;
     const unsigned c = sb_heads(starts, n, r0, &m);
@@ -1753,88 +1767,212 @@ __global__ void __launch_bounds__(256) sb_list_kernel(const unsigned char *__res
     }
 }
 
-// One segment [s, e) of at most SB_SHORT rows, in the order of the oracle's restatement.
-__device__ void sb_segment(const unsigned long long *__restrict__ x, int64_t s, int64_t e,
-                           unsigned long long *__restrict__ out) {
-    double lane[16];
+// Rows of a pack in shared memory: row i at i ^ ((i >> 4) & 15), so that the threads of a
+// half-warp reading the same position of 16 consecutive 16-row blocks hit different banks.
+__device__ __forceinline__ int sbp(int i) { return i ^ ((i >> 4) & 15); }
+
+struct SbSmem {
+    unsigned long long x[SBP_CAP];    // the pack's rows (bits)
+    unsigned long long out[SBP_CAP];  // the lane states after each whole block at their rows, then the outputs
+    unsigned long long carried[16];   // a long segment: its lane states at the window's first row
+    unsigned long long carried_c;     // and their combine
+    long long tile_end;               // the row after the tile's last segment
+    unsigned bm[SBP_CAP / 32 + 2];    // the pack's segment heads (two words past the end stay 0)
+    unsigned items[SBP_CAP / 16];     // segments with a whole block: first row | blocks << 16
+    int n_items;
+    int warp_max[32];
+    unsigned short hs[SB_TILE];  // the tile's heads, from the tile's first row
+};
+
+// Block-wide exclusive maximum (-1 before the first thread); blockDim.x a multiple of 32.
+__device__ __forceinline__ int sb_exclusive_max(int v, int *warp_max) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    int x = v;
 #pragma unroll
-    for (int j = 0; j < 16; ++j) lane[j] = 0.0;
-    double base = 0.0;  // the combine of the lanes before the block (+0.0 while all are +0.0)
-    // The first block's adds start from +0.0, where the integer steps never apply: FP64 adds.
-    for (int64_t b0 = s; b0 < e; b0 += 16) {
-        const int64_t cnt = e - b0;
-        if (b0 == s) {
-            double t = 0.0;
-#pragma unroll
-            for (int r = 0; r < 16; ++r) {
-                if (r < cnt) {
-                    const double v = as_f64(x[b0 + r]);
-                    if (r < 15) {
-                        t = __dadd_rn(t, v);
-                        out[b0 + r] = as_bits(t);
-                    }
-                    lane[r] = __dadd_rn(0.0, v);  // used only when the block is whole
-                }
-            }
-            if (cnt >= 16) {
-                double a[16];
-#pragma unroll
-                for (int j = 0; j < 16; ++j) a[j] = lane[j];
-#pragma unroll
-                for (int step = 8; step > 0; step >>= 1)
-#pragma unroll
-                    for (int q = 0; q < step; ++q) a[q] = __dadd_rn(a[q], a[q + step]);
-                base = a[0];
-                out[b0 + 15] = as_bits(base);
-            }
-        } else if (cnt >= 16) {
-            double v[16];
-#pragma unroll
-            for (int j = 0; j < 16; ++j) v[j] = as_f64(x[b0 + j]);
-            unsigned long long t = as_bits(base);
-#pragma unroll
-            for (int r = 0; r < 15; ++r) {
-                t = add_bits(t, as_bits(v[r]));
-                out[b0 + r] = t;
-            }
-            double a[16];
-#pragma unroll
-            for (int j = 0; j < 16; ++j) a[j] = lane[j] = as_f64(add_bits(as_bits(lane[j]), as_bits(v[j])));
-#pragma unroll
-            for (int step = 8; step > 0; step >>= 1)
-#pragma unroll
-                for (int q = 0; q < step; ++q) a[q] = __dadd_rn(a[q], a[q + step]);
-            base = a[0];
-            out[b0 + 15] = as_bits(base);
-        } else {
-            unsigned long long t = as_bits(base);
-            for (int64_t i = b0; i < e; ++i) {
-                t = add_bits(t, x[i]);
-                out[i] = t;
-            }
-        }
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(FULL, x, o);
+        if (lane >= o) x = max(x, y);
     }
+    int before = __shfl_up_sync(FULL, x, 1);
+    if (lane == 0) before = -1;
+    if (lane == 31) warp_max[w] = x;
+    __syncthreads();
+    int carry = -1;
+    for (int j = 0; j < w && j < nw; ++j) carry = max(carry, warp_max[j]);
+    __syncthreads();
+    return max(carry, before);
 }
 
-// Every segment: the short ones here, the long ones listed as (first row, rows) pairs after a
-// count in longs[0].
-__global__ void __launch_bounds__(128) sb_segment_kernel(const unsigned long long *__restrict__ x, int64_t n,
-                                                         const long long *__restrict__ heads,
-                                                         const unsigned *__restrict__ offs,
-                                                         const unsigned *__restrict__ counts, int tiles,
-                                                         unsigned long long *__restrict__ out,
-                                                         unsigned long long *__restrict__ longs) {
-    const int64_t G = static_cast<int64_t>(offs[tiles - 1]) + counts[tiles - 1];
-    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
-    for (int64_t g = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; g < G; g += stride) {
-        const int64_t s = heads[g], e = g + 1 < G ? heads[g + 1] : n;
-        if (e - s > SB_SHORT) {
-            const unsigned long long k = atomicAdd(longs, 1ull);
-            longs[1 + 2 * k] = static_cast<unsigned long long>(s);
-            longs[2 + 2 * k] = static_cast<unsigned long long>(e - s);
-        } else {
-            sb_segment(x, s, e, out);
+// One pack: rows [p0, p0 + rows) of x. `window`: a window of one long segment, whose lanes start
+// from `carried` (+0.0 in its first window) and whose first block's tail from `carried_c`;
+// otherwise the consecutive segments m .. m2 - 1 of the tile, each of at most SBP_CAP rows,
+// their lanes and first tails from +0.0. In the order of the oracle's restatement: lane l of a
+// segment adds its rows l, l + 16, ... of the whole blocks (the first add from +0.0 is the FP64
+// add, the rest add_bits, which equals it); the row closing a whole block gets the pairwise
+// combine (+8, +4, +2, +1) of the lane states after it; the other rows of a block are the chain
+// from the combine before the block (+0.0 for the segment's first block).
+__device__ __forceinline__ void sb_pack(SbSmem &sm, const unsigned long long *__restrict__ x,
+                                        unsigned long long *__restrict__ out, int64_t p0, int rows, bool window,
+                                        bool first, int m, int m2, int64_t trow, int cnt) {
+    const int tid = threadIdx.x;
+    unsigned long long v[SBP_RPT];
+#pragma unroll
+    for (int q = 0; q < SBP_RPT; ++q) {
+        const int i = tid + q * SBP_THREADS;
+        v[q] = i < rows ? x[p0 + i] : 0ull;
+    }
+#pragma unroll
+    for (int q = 0; q < SBP_RPT; ++q) {
+        const int i = tid + q * SBP_THREADS;
+        if (i < rows) sm.x[sbp(i)] = v[q];
+    }
+    if (window) {
+        if (first && tid < 16) sm.carried[tid] = 0ull;
+        if (first && tid == 0) sm.carried_c = 0ull;
+        if (tid == 0) {
+            sm.items[0] = static_cast<unsigned>(rows >> 4) << 16;
+            sm.n_items = rows >= 16 ? 1 : 0;
         }
+    } else {
+        for (int j = m + tid; j < m2; j += SBP_THREADS) {
+            const int64_t sj = trow + sm.hs[j];
+            const int64_t ej = j + 1 < cnt ? trow + sm.hs[j + 1] : sm.tile_end;
+            const int off = static_cast<int>(sj - p0);
+            atomicOr(&sm.bm[off >> 5], 1u << (off & 31));
+            const unsigned nb = static_cast<unsigned>((ej - sj) >> 4);
+            if (nb > 0) sm.items[atomicAdd(&sm.n_items, 1)] = static_cast<unsigned>(off) | (nb << 16);
+        }
+    }
+    __syncthreads();
+    // The lane chains: 16 consecutive threads take the 16 lanes of one segment.
+    const int total = 16 * sm.n_items;
+    for (int i = tid; i < total; i += SBP_THREADS) {
+        const unsigned it = sm.items[i >> 4];
+        const int l = i & 15, off = static_cast<int>(it & 0xffffu), nb = static_cast<int>(it >> 16);
+        unsigned long long st = window ? sm.carried[l] : 0ull;
+        for (int b = 0; b < nb; ++b) {
+            const int r = off + l + 16 * b;
+            st = add_bits(st, sm.x[sbp(r)]);
+            sm.out[sbp(r)] = st;
+        }
+        if (window) sm.carried[l] = st;  // read by this thread only, in the next window
+    }
+    // Each thread's rows r0 .. r0 + SBP_RPT - 1 and the segment start before them.
+    const int r0 = tid * SBP_RPT;
+    unsigned mine = 0;
+    int sr0 = 0;
+    if (!window) {
+        const unsigned long long w2 = sm.bm[r0 >> 5] | (static_cast<unsigned long long>(sm.bm[(r0 >> 5) + 1]) << 32);
+        mine = static_cast<unsigned>(w2 >> (r0 & 31)) & ((1u << SBP_RPT) - 1);
+        sr0 = sb_exclusive_max(mine ? r0 + 31 - __clz(mine) : -1, sm.warp_max);  // synchronises the block
+    } else {
+        __syncthreads();
+    }
+    // Each thread's block starts and the one block end (at most one block closes in 16 or fewer
+    // consecutive rows), found first so that a warp runs one combine and the tails side by side.
+    int sr = sr0, rend = -1;
+    unsigned smask = 0;
+#pragma unroll
+    for (int q = 0; q < SBP_RPT; ++q) {
+        const int r = r0 + q;
+        if ((mine >> q) & 1u) sr = r;
+        if (r < rows) {
+            if (((r - sr) & 15) == 0) smask |= 1u << q;
+            if (((r - sr) & 15) == 15) rend = r;
+        }
+    }
+    if (rend >= 0) {
+        double a[16];
+#pragma unroll
+        for (int k = 0; k < 16; ++k) a[k] = as_f64(sm.out[sbp(rend - 15 + k)]);
+#pragma unroll
+        for (int step = 8; step > 0; step >>= 1)
+#pragma unroll
+            for (int k = 0; k < step; ++k) a[k] = __dadd_rn(a[k], a[k + step]);
+        sm.out[sbp(rend)] = as_bits(a[0]);
+    }
+    __syncthreads();
+    // The tails, from each block's first row: the combine before it, +0.0 at a segment's head.
+    while (smask) {
+        const int q = __ffs(smask) - 1;
+        smask &= smask - 1;
+        const int r = r0 + q;
+        const bool head = window ? r == 0 : ((mine >> q) & 1u) != 0;
+        unsigned long long c = head ? (window ? sm.carried_c : 0ull) : sm.out[sbp(r - 1)];
+        // rows r .. r + 14 up to the next head or the pack's end
+        const int b1 = r + 1, sh = b1 & 31;
+        const unsigned next = (sm.bm[b1 >> 5] >> sh) | (sh ? sm.bm[(b1 >> 5) + 1] << (32 - sh) : 0u);
+        const int len = min((next & 0x3fffu) ? __ffs(next & 0x3fffu) : 15, rows - r);
+        for (int k = 0; k < len; ++k) {
+            c = add_bits(c, sm.x[sbp(r + k)]);
+            sm.out[sbp(r + k)] = c;
+        }
+    }
+    __syncthreads();
+    if (window && tid == 0) sm.carried_c = sm.out[sbp(rows - 1)];  // the next window's, when this one is whole
+#pragma unroll
+    for (int q = 0; q < SBP_RPT; ++q) {
+        const int i = tid + q * SBP_THREADS;
+        if (i < rows) out[p0 + i] = sm.out[sbp(i)];
+    }
+    if (!window)
+        for (int i = tid; i < SBP_CAP / 32 + 2; i += SBP_THREADS) sm.bm[i] = 0;
+    if (tid == 0) sm.n_items = 0;
+    __syncthreads();
+}
+
+// One block per tile of SB_TILE rows: the segments whose heads lie in it, the long ones (more
+// than SB_SHORT rows) listed as (first row, rows) pairs after a count in longs[0].
+__global__ void __launch_bounds__(SBP_THREADS, 8) sb_pack_kernel(const unsigned long long *__restrict__ x, int64_t n,
+                                                                 const long long *__restrict__ heads,
+                                                                 const unsigned *__restrict__ offs,
+                                                                 const unsigned *__restrict__ counts, int tiles,
+                                                                 unsigned long long *__restrict__ out,
+                                                                 unsigned long long *__restrict__ longs) {
+    extern __shared__ __align__(16) unsigned char sb_smem[];
+    SbSmem &sm = *reinterpret_cast<SbSmem *>(sb_smem);
+    const int c = blockIdx.x, tid = threadIdx.x;
+    const int cnt = static_cast<int>(counts[c]);
+    if (cnt == 0) return;
+    const int64_t k0 = offs[c];
+    const int64_t G = static_cast<int64_t>(offs[tiles - 1]) + counts[tiles - 1];
+    const int64_t trow = static_cast<int64_t>(c) * SB_TILE;
+    for (int i = tid; i < cnt; i += SBP_THREADS) sm.hs[i] = static_cast<unsigned short>(heads[k0 + i] - trow);
+    for (int i = tid; i < SBP_CAP / 32 + 2; i += SBP_THREADS) sm.bm[i] = 0;
+    if (tid == 0) {
+        sm.tile_end = k0 + cnt < G ? heads[k0 + cnt] : n;
+        sm.n_items = 0;
+    }
+    __syncthreads();
+    const int64_t tile_end = sm.tile_end;
+    auto end_of = [&](int j) { return j + 1 < cnt ? trow + sm.hs[j + 1] : tile_end; };
+    int m = 0;
+    while (m < cnt) {
+        const int64_t s = trow + sm.hs[m], e = end_of(m);
+        if (e - s > SB_SHORT) {
+            if (tid == 0) {
+                const unsigned long long k = atomicAdd(longs, 1ull);
+                longs[1 + 2 * k] = static_cast<unsigned long long>(s);
+                longs[2 + 2 * k] = static_cast<unsigned long long>(e - s);
+            }
+            ++m;
+            continue;
+        }
+        if (e - s > SBP_CAP) {
+            for (int64_t w0 = s; w0 < e; w0 += SBP_CAP)
+                sb_pack(sm, x, out, w0, static_cast<int>(e - w0 < SBP_CAP ? e - w0 : SBP_CAP), true, w0 == s, 0, 0, trow, cnt);
+            ++m;
+            continue;
+        }
+        // The longest run of segments from m within SBP_CAP rows.
+        int lo = m + 1, hi = cnt;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (end_of(mid - 1) - s <= SBP_CAP) lo = mid;
+            else hi = mid - 1;
+        }
+        sb_pack(sm, x, out, s, static_cast<int>(end_of(lo - 1) - s), false, false, m, lo, trow, cnt);
+        m = lo;
     }
 }
 
@@ -1889,14 +2027,18 @@ static vkc_status scan_by_add_f64(vkc_ctx *ctx, const vkc_value *args, int, vkc_
     auto cuda = [&](cudaError_t e, const char *what) { return e == cudaSuccess ? VKC_OK : cuda_fail(ctx, e, what); };
     if ((st = cuda(cudaMemsetAsync(longs, 0, sizeof(unsigned long long), ctx->stream), "cudaMemsetAsync")))
         return done(st);
-    sb_count_kernel<<<static_cast<unsigned>(tiles), 256, 0, ctx->stream>>>(starts, n, counts);
+    sb_count_kernel<<<static_cast<unsigned>(tiles), SB_TILE / 16, 0, ctx->stream>>>(starts, n, counts);
     if ((st = launched(ctx, "sb_count"))) return done(st);
     scan_counts(ctx, counts, tiles, sums, offs);
-    sb_list_kernel<<<static_cast<unsigned>(tiles), 256, 0, ctx->stream>>>(starts, n, offs, heads);
+    sb_list_kernel<<<static_cast<unsigned>(tiles), SB_TILE / 16, 0, ctx->stream>>>(starts, n, offs, heads);
     if ((st = launched(ctx, "sb_list"))) return done(st);
-    sb_segment_kernel<<<stream_grid(ctx, n, 128, 16, 256), 128, 0, ctx->stream>>>(
+    static std::atomic<unsigned long long> configured{0};
+    once_per_device(configured, ctx->device, [] {
+        cudaFuncSetAttribute(sb_pack_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sizeof(SbSmem)));
+    });
+    sb_pack_kernel<<<static_cast<unsigned>(tiles), SBP_THREADS, sizeof(SbSmem), ctx->stream>>>(
         x, n, heads, offs, counts, static_cast<int>(tiles), ov, longs);
-    if ((st = launched(ctx, "sb_segment"))) return done(st);
+    if ((st = launched(ctx, "sb_pack"))) return done(st);
     unsigned long long nlong = 0;
     if ((st = cuda(cudaMemcpyAsync(&nlong, longs, sizeof nlong, cudaMemcpyDeviceToHost, ctx->stream), "cudaMemcpyAsync")) ||
         (st = cuda(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize")))
