@@ -132,6 +132,21 @@ def test_gpu_scan_by_long_segments(ctx):
 
 
 @pytest.mark.gpu
+def test_gpu_scan_by_many_long_segments(ctx):
+    # Many segments beyond 2^16 rows: one block per segment in windows (some starting at rows
+    # that are not 16-byte aligned), rows of mixed sign and magnitude.
+    n = (1 << 22) + 5
+    rng = np.random.default_rng(11)
+    heads = np.cumsum(rng.integers(65_537, 90_000, size=60))
+    heads = heads[heads < n]
+    s = np.zeros(n, dtype=np.uint8)
+    s[heads] = 1
+    for x in (uniform(n, 12) - 0.2, varied(n, 13)):
+        got = ctx.call("scan_by_add_f64", ctx.upload(x), ctx.upload(s.astype(bool))).numpy()
+        assert same(got, oracle.scan_by_add_f64(x, s))
+
+
+@pytest.mark.gpu
 def test_gpu_scan_errors_and_empty(ctx):
     x = ctx.upload(np.array([1.0, 2.0, 3.0]))
     with pytest.raises(Exception, match=r"^expected f64\[\], got i64\[\]$"):

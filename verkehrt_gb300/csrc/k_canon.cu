@@ -40,6 +40,7 @@
 //
 // All of the per-row work is integer arithmetic: GB300 executes FP64 adds at about 1/66 of
 // its integer op rate, so an FP64 tree would be compute-bound well below the HBM roofline.
+#include <algorithm>
 #include <climits>
 #include <cmath>
 
@@ -1976,6 +1977,20 @@ __global__ void __launch_bounds__(SBP_THREADS, 8) sb_pack_kernel(const unsigned 
     }
 }
 
+// One block per listed long segment (first row, rows): the windows of sb_pack in order.
+__global__ void __launch_bounds__(SBP_THREADS, 8) sb_long_kernel(const unsigned long long *__restrict__ x,
+                                                                 const unsigned long long *__restrict__ list,
+                                                                 unsigned long long *__restrict__ out) {
+    extern __shared__ __align__(16) unsigned char sb_smem[];
+    SbSmem &sm = *reinterpret_cast<SbSmem *>(sb_smem);
+    const int64_t s = static_cast<int64_t>(list[2 * blockIdx.x]), e = s + static_cast<int64_t>(list[2 * blockIdx.x + 1]);
+    for (int i = threadIdx.x; i < SBP_CAP / 32 + 2; i += SBP_THREADS) sm.bm[i] = 0;
+    if (threadIdx.x == 0) sm.n_items = 0;
+    __syncthreads();
+    for (int64_t w0 = s; w0 < e; w0 += SBP_CAP)
+        sb_pack(sm, x, out, w0, static_cast<int>(e - w0 < SBP_CAP ? e - w0 : SBP_CAP), true, w0 == s, 0, 0, 0, 0);
+}
+
 static vkc_status scan_by_add_f64(vkc_ctx *ctx, const vkc_value *args, int, vkc_value *out) {
     vkc_status st;
     if (!array_arg(ctx, args[0], VKC_F64, &st) || !array_arg(ctx, args[1], VKC_BOOL, &st)) return st;
@@ -2035,6 +2050,7 @@ static vkc_status scan_by_add_f64(vkc_ctx *ctx, const vkc_value *args, int, vkc_
     static std::atomic<unsigned long long> configured{0};
     once_per_device(configured, ctx->device, [] {
         cudaFuncSetAttribute(sb_pack_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sizeof(SbSmem)));
+        cudaFuncSetAttribute(sb_long_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sizeof(SbSmem)));
     });
     sb_pack_kernel<<<static_cast<unsigned>(tiles), SBP_THREADS, sizeof(SbSmem), ctx->stream>>>(
         x, n, heads, offs, counts, static_cast<int>(tiles), ov, longs);
@@ -2049,8 +2065,21 @@ static vkc_status scan_by_add_f64(vkc_ctx *ctx, const vkc_value *args, int, vkc_
                                        cudaMemcpyDeviceToHost, ctx->stream), "cudaMemcpyAsync")) ||
             (st = cuda(cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize")))
             return done(st);
-        for (unsigned long long k = 0; k < nlong && !st; ++k)
-            st = canon_scan_rows(ctx, x + list[2 * k], static_cast<int64_t>(list[2 * k + 1]), ov + list[2 * k]);
+        // One tiled scan per segment costs about 140 us of launches and waits plus 11 ps a row,
+        // one after another; a block per segment in windows about 5 ns a row, all segments side
+        // by side (figures measured at 2^27 rows). The cheaper of the two takes them all.
+        unsigned long long longest = 0, rows = 0;
+        for (unsigned long long k = 0; k < nlong; ++k) {
+            longest = std::max(longest, list[2 * k + 1]);
+            rows += list[2 * k + 1];
+        }
+        if (static_cast<double>(nlong) * 140e-6 + static_cast<double>(rows) * 11e-12 > static_cast<double>(longest) * 5e-9) {
+            sb_long_kernel<<<static_cast<unsigned>(nlong), SBP_THREADS, sizeof(SbSmem), ctx->stream>>>(x, longs + 1, ov);
+            st = launched(ctx, "sb_long");
+        } else {
+            for (unsigned long long k = 0; k < nlong && !st; ++k)
+                st = canon_scan_rows(ctx, x + list[2 * k], static_cast<int64_t>(list[2 * k + 1]), ov + list[2 * k]);
+        }
     }
     return done(st);
 }
