@@ -1736,12 +1736,24 @@ constexpr int SB_TILE = 1024;
 constexpr int64_t SB_SHORT = int64_t(1) << 16;
 constexpr int SBP_CAP = 1536, SBP_THREADS = 128, SBP_RPT = SBP_CAP / SBP_THREADS;  // 12 rows a thread
 
+// The head bits of rows r0 .. r0 + 15: one 16-byte load where the flags allow it.
 __device__ __forceinline__ unsigned sb_heads(const unsigned char *__restrict__ starts, int64_t n, int64_t r0, unsigned *mask) {
     unsigned m = 0;
+    if (r0 + 16 <= n && (reinterpret_cast<uintptr_t>(starts + r0) & 15) == 0) {
+        const uint4 q = *reinterpret_cast<const uint4 *>(starts + r0);
+        const unsigned w[4] = {q.x, q.y, q.z, q.w};
 #pragma unroll
-    for (int j = 0; j < 16; ++j) {
-        const int64_t i = r0 + j;
-        if (i < n && (i == 0 || starts[i] != 0)) m |= 1u << j;
+        for (int k = 0; k < 4; ++k)
+#pragma unroll
+            for (int b = 0; b < 4; ++b)
+                if ((w[k] >> (8 * b)) & 0xffu) m |= 1u << (4 * k + b);
+        if (r0 == 0) m |= 1u;
+    } else {
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+            const int64_t i = r0 + j;
+            if (i < n && (i == 0 || starts[i] != 0)) m |= 1u << j;
+        }
     }
     *mask = m;
     return __popc(m);
