@@ -132,6 +132,28 @@ def test_gpu_scan_by_long_segments(ctx):
 
 
 @pytest.mark.gpu
+def test_gpu_scan_by_segment_edges(ctx):
+    # Segment lengths at the edges of the 16-row blocks, of the 1024-row head tiles and of the
+    # 1536-row shared-memory runs and windows, and start flags read from views at every offset
+    # modulo 16 (the flags are read 16 bytes at a time only where aligned).
+    lens = [1536, 1537, 1535, 1, 1024, 1023, 3072, 3073, 15, 16, 17, 31, 32, 33, 4608, 2, 1536 * 5 + 7]
+    lens += [1] * 40 + [16] * 20 + [1500, 36, 1537]
+    n = sum(lens)
+    s = np.zeros(n + 16, dtype=np.uint8)
+    at = 0
+    for L in lens:
+        s[at] = 1
+        at += L
+    x = varied(n + 16, 21)
+    dx = ctx.upload(x)
+    ds = ctx.upload(s.astype(bool))
+    for off in range(16):
+        m = n - 16 + off
+        got = ctx.call("scan_by_add_f64", dx.slice(off, off + m), ds.slice(off, off + m)).numpy()
+        assert same(got, oracle.scan_by_add_f64(x[off : off + m], s[off : off + m])), off
+
+
+@pytest.mark.gpu
 def test_gpu_scan_by_many_long_segments(ctx):
     # Many segments beyond 2^16 rows: one block per segment in windows (some starting at rows
     # that are not 16-byte aligned), rows of mixed sign and magnitude.

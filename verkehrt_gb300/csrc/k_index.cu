@@ -115,12 +115,18 @@ __global__ void __launch_bounds__(GP_THREADS) gp_count_kernel(const long long *_
     if (threadIdx.x < GP_NB) h[threadIdx.x] = 0;
     __syncthreads();
     const int64_t base = static_cast<int64_t>(blockIdx.x) * GP_TILE;
+    // All of a thread's loads are issued before its first atomic (the atomics keep the order).
+    unsigned long long k[GP_ITEMS];
+#pragma unroll
+    for (int j = 0; j < GP_ITEMS; ++j) {
+        const int64_t r = base + j * GP_THREADS + threadIdx.x;
+        k[j] = r < n ? static_cast<unsigned long long>(__ldcs(idx + r)) : 0ull;
+    }
 #pragma unroll
     for (int j = 0; j < GP_ITEMS; ++j) {
         const int64_t r = base + j * GP_THREADS + threadIdx.x;
         if (r < n) {
-            const auto k = static_cast<unsigned long long>(__ldcs(idx + r));
-            if (k < nsrc) atomicAdd(&h[static_cast<unsigned>(k >> rb)], 1u);
+            if (k[j] < nsrc) atomicAdd(&h[static_cast<unsigned>(k[j] >> rb)], 1u);
             else atomicMin(&status->first_bad, static_cast<unsigned long long>(r));
         }
     }
@@ -192,13 +198,31 @@ __global__ void __launch_bounds__(GP_THREADS) gp_region_kernel(const unsigned lo
     __syncthreads();
     const unsigned total = s_start[GP_NB];
     const int64_t base = static_cast<int64_t>(blockIdx.x) * GP_TILE;
-#pragma unroll 4
+    if (base >= total) return;
+    // A thread's positions rise, so its region only moves forward from the first one's. The
+    // offsets are loaded first, then every source read is in flight at once; the source reads
+    // skip L1 (each touches one sector of a line that no other read of this block is likely
+    // to use).
+    int b = gp_region_of(s_start, static_cast<unsigned>(base + threadIdx.x < total ? base + threadIdx.x : total - 1));
+    unsigned o[GP_ITEMS];
+#pragma unroll
+    for (int j = 0; j < GP_ITEMS; ++j) {
+        const int64_t p = base + j * GP_THREADS + threadIdx.x;
+        o[j] = p < total ? __ldcs(part + p) : 0u;
+    }
+    unsigned long long v[GP_ITEMS];
+#pragma unroll
     for (int j = 0; j < GP_ITEMS; ++j) {
         const int64_t p = base + j * GP_THREADS + threadIdx.x;
         if (p < total) {
-            const int b = gp_region_of(s_start, static_cast<unsigned>(p));
-            vals[p] = __ldg(src + (static_cast<int64_t>(b) << rb) + __ldcs(part + p));
+            while (static_cast<unsigned>(p) >= s_start[b + 1]) ++b;
+            v[j] = __ldcg(src + (static_cast<int64_t>(b) << rb) + o[j]);
         }
+    }
+#pragma unroll
+    for (int j = 0; j < GP_ITEMS; ++j) {
+        const int64_t p = base + j * GP_THREADS + threadIdx.x;
+        if (p < total) __stcs(vals + p, v[j]);
     }
 }
 
