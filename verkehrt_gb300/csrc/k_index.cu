@@ -134,7 +134,7 @@ __global__ void __launch_bounds__(GP_THREADS) gp_count_kernel(const long long *_
     if (threadIdx.x < GP_NB) counts[static_cast<int64_t>(threadIdx.x) * tiles + blockIdx.x] = h[threadIdx.x];
 }
 
-__global__ void __launch_bounds__(GP_THREADS) gp_partition_kernel(const long long *__restrict__ idx, int64_t n,
+__global__ void __launch_bounds__(GP_THREADS, 4) gp_partition_kernel(const long long *__restrict__ idx, int64_t n,
                                                                   uint64_t nsrc, int rb, int tiles,
                                                                   const unsigned *__restrict__ offs,
                                                                   unsigned *__restrict__ part,
@@ -149,16 +149,21 @@ __global__ void __launch_bounds__(GP_THREADS) gp_partition_kernel(const long lon
     __syncthreads();
     const int64_t base = static_cast<int64_t>(blockIdx.x) * GP_TILE;
     const unsigned long long mask = (1ull << rb) - 1;
-    unsigned long long k[GP_ITEMS];
-    unsigned rk[GP_ITEMS];
+    // Per row: its offset in its region, and its region (bits 16 and up) with its slot among
+    // the tile's rows of that region (the low 16 bits; GP_TILE <= 2^16), or ~0u for an
+    // offending row or one past the end (kept in 32-bit words: fewer registers, more blocks).
+    unsigned off[GP_ITEMS], rk[GP_ITEMS];
 #pragma unroll
     for (int j = 0; j < GP_ITEMS; ++j) {
         const int64_t r = base + j * GP_THREADS + threadIdx.x;
-        k[j] = r < n ? static_cast<unsigned long long>(__ldcs(idx + r)) : ~0ull;  // past the end: like an offending row
+        const unsigned long long k = r < n ? static_cast<unsigned long long>(__ldcs(idx + r)) : ~0ull;
+        off[j] = static_cast<unsigned>(k & mask);
+        rk[j] = k < nsrc ? static_cast<unsigned>(k >> rb) << 16 : ~0u;
     }
     // Slots within the tile's region runs, in any order: the output does not depend on it.
 #pragma unroll
-    for (int j = 0; j < GP_ITEMS; ++j) rk[j] = k[j] < nsrc ? atomicAdd(&s_cnt[static_cast<unsigned>(k[j] >> rb)], 1u) : 0u;
+    for (int j = 0; j < GP_ITEMS; ++j)
+        if (rk[j] != ~0u) rk[j] |= atomicAdd(&s_cnt[rk[j] >> 16], 1u);
     __syncthreads();
     if (threadIdx.x < 32) gp_starts([&](int b) { return s_cnt[b]; }, s_start);
     __syncthreads();
@@ -166,11 +171,11 @@ __global__ void __launch_bounds__(GP_THREADS) gp_partition_kernel(const long lon
     for (int j = 0; j < GP_ITEMS; ++j) {
         const int64_t r = base + j * GP_THREADS + threadIdx.x;
         if (r >= n) continue;
-        if (k[j] < nsrc) {
-            const unsigned b = static_cast<unsigned>(k[j] >> rb);
-            const unsigned l = s_start[b] + rk[j];
+        if (rk[j] != ~0u) {
+            const unsigned b = rk[j] >> 16;
+            const unsigned l = s_start[b] + (rk[j] & 0xffffu);
             loc[r] = static_cast<unsigned short>(l);
-            s_part[l] = static_cast<unsigned>(k[j] & mask);
+            s_part[l] = off[j];
             s_reg[l] = static_cast<unsigned char>(b);
         } else {
             loc[r] = 0;  // the call fails; the row's output is never read
