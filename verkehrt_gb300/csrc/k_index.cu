@@ -136,7 +136,7 @@ __global__ void __launch_bounds__(GP_THREADS) gp_count_kernel(const long long *_
 
 __global__ void __launch_bounds__(GP_THREADS, 4) gp_partition_kernel(const long long *__restrict__ idx, int64_t n,
                                                                   uint64_t nsrc, int rb, int tiles,
-                                                                  const unsigned *__restrict__ offs,
+                                                                  const unsigned *__restrict__ toffs,
                                                                   unsigned *__restrict__ part,
                                                                   unsigned short *__restrict__ loc) {
     __shared__ unsigned s_cnt[GP_NB], s_start[GP_NB + 1], s_goff[GP_NB];
@@ -144,7 +144,7 @@ __global__ void __launch_bounds__(GP_THREADS, 4) gp_partition_kernel(const long 
     __shared__ unsigned char s_reg[GP_TILE];
     if (threadIdx.x < GP_NB) {
         s_cnt[threadIdx.x] = 0;
-        s_goff[threadIdx.x] = offs[static_cast<int64_t>(threadIdx.x) * tiles + blockIdx.x];
+        s_goff[threadIdx.x] = toffs[static_cast<int64_t>(blockIdx.x) * GP_NB + threadIdx.x];
     }
     __syncthreads();
     const int64_t base = static_cast<int64_t>(blockIdx.x) * GP_TILE;
@@ -186,6 +186,30 @@ __global__ void __launch_bounds__(GP_THREADS, 4) gp_partition_kernel(const long 
     for (int l = threadIdx.x; l < rows; l += GP_THREADS) {
         const unsigned b = s_reg[l];
         part[s_goff[b] + static_cast<unsigned>(l) - s_start[b]] = s_part[l];
+    }
+}
+
+// The counts and offsets of every (region, tile), region-major as the scan needs them, copied
+// tile-major (tile t's 64 values in one 256-byte run) for the passes that read one tile's.
+__global__ void __launch_bounds__(256) gp_tables_kernel(const unsigned *__restrict__ counts,
+                                                        const unsigned *__restrict__ offs, int tiles,
+                                                        unsigned *__restrict__ tcounts, unsigned *__restrict__ toffs) {
+    __shared__ unsigned s_c[GP_NB][GP_NB + 1], s_o[GP_NB][GP_NB + 1];
+    const int t0 = blockIdx.x * GP_NB;
+    for (int i = threadIdx.x; i < GP_NB * GP_NB; i += 256) {
+        const int b = i / GP_NB, tt = i % GP_NB;
+        if (t0 + tt < tiles) {
+            s_c[b][tt] = counts[static_cast<int64_t>(b) * tiles + t0 + tt];
+            s_o[b][tt] = offs[static_cast<int64_t>(b) * tiles + t0 + tt];
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < GP_NB * GP_NB; i += 256) {
+        const int tt = i / GP_NB, b = i % GP_NB;
+        if (t0 + tt < tiles) {
+            tcounts[static_cast<int64_t>(t0 + tt) * GP_NB + b] = s_c[b][tt];
+            toffs[static_cast<int64_t>(t0 + tt) * GP_NB + b] = s_o[b][tt];
+        }
     }
 }
 
@@ -233,13 +257,14 @@ __global__ void __launch_bounds__(GP_THREADS) gp_region_kernel(const unsigned lo
 
 __global__ void __launch_bounds__(GP_THREADS) gp_restore_kernel(const unsigned long long *__restrict__ vals,
                                                                 const unsigned short *__restrict__ loc,
-                                                                const unsigned *__restrict__ counts,
-                                                                const unsigned *__restrict__ offs, int64_t n, int tiles,
+                                                                const unsigned *__restrict__ tcounts,
+                                                                const unsigned *__restrict__ toffs, int64_t n,
                                                                 unsigned long long *__restrict__ out) {
     __shared__ unsigned s_start[GP_NB + 1], s_goff[GP_NB];
     __shared__ unsigned long long s_vals[GP_TILE];
-    if (threadIdx.x < 32) gp_starts([&](int b) { return counts[static_cast<int64_t>(b) * tiles + blockIdx.x]; }, s_start);
-    if (threadIdx.x < GP_NB) s_goff[threadIdx.x] = offs[static_cast<int64_t>(threadIdx.x) * tiles + blockIdx.x];
+    const unsigned *tc = tcounts + static_cast<int64_t>(blockIdx.x) * GP_NB;
+    if (threadIdx.x < 32) gp_starts([&](int b) { return tc[b]; }, s_start);
+    if (threadIdx.x < GP_NB) s_goff[threadIdx.x] = toffs[static_cast<int64_t>(blockIdx.x) * GP_NB + threadIdx.x];
     __syncthreads();
     const int rows = static_cast<int>(s_start[GP_NB]);
     unsigned at[GP_ITEMS];
@@ -282,7 +307,7 @@ static vkc_status gather_partitioned(vkc_ctx *ctx, const unsigned long long *src
     const int tiles = static_cast<int>((n + GP_TILE - 1) / GP_TILE);
     const int64_t m = static_cast<int64_t>(GP_NB) * tiles;
     auto up = [](size_t b) { return (b + 255) & ~size_t(255); };
-    const size_t o_offs = up(m * 4), o_sums = o_offs + up(m * 4);
+    const size_t o_offs = up(m * 4), o_tc = o_offs + up(m * 4), o_to = o_tc + up(m * 4), o_sums = o_to + up(m * 4);
     const size_t o_part = o_sums + up(scan_counts_sum_words(m) * 4), o_loc = o_part + up(n * 4);
     const size_t o_vals = o_loc + up(n * 2), total = o_vals + n * 8;
     void *p;
@@ -291,14 +316,17 @@ static vkc_status gather_partitioned(vkc_ctx *ctx, const unsigned long long *src
     char *b = static_cast<char *>(p);
     auto *counts = reinterpret_cast<unsigned *>(b);
     auto *offs = reinterpret_cast<unsigned *>(b + o_offs);
+    auto *tcounts = reinterpret_cast<unsigned *>(b + o_tc);
+    auto *toffs = reinterpret_cast<unsigned *>(b + o_to);
     auto *part = reinterpret_cast<unsigned *>(b + o_part);
     auto *loc = reinterpret_cast<unsigned short *>(b + o_loc);
     auto *vals = reinterpret_cast<unsigned long long *>(b + o_vals);
     gp_count_kernel<<<tiles, GP_THREADS, 0, ctx->stream>>>(idx, n, nsrc, rb, tiles, counts, ctx->status);
     scan_counts(ctx, counts, m, reinterpret_cast<unsigned *>(b + o_sums), offs);
-    gp_partition_kernel<<<tiles, GP_THREADS, 0, ctx->stream>>>(idx, n, nsrc, rb, tiles, offs, part, loc);
+    gp_tables_kernel<<<(tiles + GP_NB - 1) / GP_NB, 256, 0, ctx->stream>>>(counts, offs, tiles, tcounts, toffs);
+    gp_partition_kernel<<<tiles, GP_THREADS, 0, ctx->stream>>>(idx, n, nsrc, rb, tiles, toffs, part, loc);
     gp_region_kernel<<<tiles, GP_THREADS, 0, ctx->stream>>>(src, part, counts, offs, tiles, rb, vals);
-    gp_restore_kernel<<<tiles, GP_THREADS, 0, ctx->stream>>>(vals, loc, counts, offs, n, tiles, out);
+    gp_restore_kernel<<<tiles, GP_THREADS, 0, ctx->stream>>>(vals, loc, tcounts, toffs, n, out);
     return launched(ctx, "gather_partitioned");
 }
 
