@@ -108,7 +108,7 @@ __device__ __forceinline__ int gp_region_of(const unsigned *s_start, unsigned v)
     return lo;
 }
 
-__global__ void __launch_bounds__(GP_THREADS) gp_count_kernel(const long long *__restrict__ idx, int64_t n, uint64_t nsrc,
+__global__ void __launch_bounds__(GP_THREADS, 4) gp_count_kernel(const long long *__restrict__ idx, int64_t n, uint64_t nsrc,
                                                               int rb, int tiles, unsigned *__restrict__ counts,
                                                               DevStatus *status) {
     __shared__ unsigned h[GP_NB];
