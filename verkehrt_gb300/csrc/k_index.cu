@@ -213,7 +213,7 @@ __global__ void __launch_bounds__(256) gp_tables_kernel(const unsigned *__restri
     }
 }
 
-__global__ void __launch_bounds__(GP_THREADS) gp_region_kernel(const unsigned long long *__restrict__ src,
+__global__ void __launch_bounds__(GP_THREADS, 6) gp_region_kernel(const unsigned long long *__restrict__ src,
                                                                const unsigned *__restrict__ part,
                                                                const unsigned *__restrict__ counts,
                                                                const unsigned *__restrict__ offs, int tiles, int rb,
@@ -233,25 +233,30 @@ __global__ void __launch_bounds__(GP_THREADS) gp_region_kernel(const unsigned lo
     // skip L1 (each touches one sector of a line that no other read of this block is likely
     // to use).
     int b = gp_region_of(s_start, static_cast<unsigned>(base + threadIdx.x < total ? base + threadIdx.x : total - 1));
-    unsigned o[GP_ITEMS];
+    // Four quarters of GP_ITEMS / 4 rows: fewer registers, six blocks an SM.
+    constexpr int H = GP_ITEMS / 4;
+#pragma unroll 1
+    for (int h = 0; h < GP_ITEMS / H; ++h) {
+        unsigned o[H];
 #pragma unroll
-    for (int j = 0; j < GP_ITEMS; ++j) {
-        const int64_t p = base + j * GP_THREADS + threadIdx.x;
-        o[j] = p < total ? __ldcs(part + p) : 0u;
-    }
-    unsigned long long v[GP_ITEMS];
-#pragma unroll
-    for (int j = 0; j < GP_ITEMS; ++j) {
-        const int64_t p = base + j * GP_THREADS + threadIdx.x;
-        if (p < total) {
-            while (static_cast<unsigned>(p) >= s_start[b + 1]) ++b;
-            v[j] = __ldcg(src + (static_cast<int64_t>(b) << rb) + o[j]);
+        for (int j = 0; j < H; ++j) {
+            const int64_t p = base + (h * H + j) * GP_THREADS + threadIdx.x;
+            o[j] = p < total ? __ldcs(part + p) : 0u;
         }
-    }
+        unsigned long long v[H];
 #pragma unroll
-    for (int j = 0; j < GP_ITEMS; ++j) {
-        const int64_t p = base + j * GP_THREADS + threadIdx.x;
-        if (p < total) __stcs(vals + p, v[j]);
+        for (int j = 0; j < H; ++j) {
+            const int64_t p = base + (h * H + j) * GP_THREADS + threadIdx.x;
+            if (p < total) {
+                while (static_cast<unsigned>(p) >= s_start[b + 1]) ++b;
+                v[j] = __ldcg(src + (static_cast<int64_t>(b) << rb) + o[j]);
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < H; ++j) {
+            const int64_t p = base + (h * H + j) * GP_THREADS + threadIdx.x;
+            if (p < total) __stcs(vals + p, v[j]);
+        }
     }
 }
 
