@@ -260,7 +260,7 @@ __global__ void __launch_bounds__(GP_THREADS, 6) gp_region_kernel(const unsigned
     }
 }
 
-__global__ void __launch_bounds__(GP_THREADS) gp_restore_kernel(const unsigned long long *__restrict__ vals,
+__global__ void __launch_bounds__(GP_THREADS, 6) gp_restore_kernel(const unsigned long long *__restrict__ vals,
                                                                 const unsigned short *__restrict__ loc,
                                                                 const unsigned *__restrict__ tcounts,
                                                                 const unsigned *__restrict__ toffs, int64_t n,
