@@ -134,6 +134,9 @@ __global__ void __launch_bounds__(GP_THREADS, 4) gp_count_kernel(const long long
     if (threadIdx.x < GP_NB) counts[static_cast<int64_t>(threadIdx.x) * tiles + blockIdx.x] = h[threadIdx.x];
 }
 
+// PACK (regions of at most 2^26 rows): a row's region rides in the top 6 bits of its staged
+// offset, so no byte array of regions is written and read back.
+template <bool PACK>
 __global__ void __launch_bounds__(GP_THREADS, 4) gp_partition_kernel(const long long *__restrict__ idx, int64_t n,
                                                                   uint64_t nsrc, int rb, int tiles,
                                                                   const unsigned *__restrict__ toffs,
@@ -141,7 +144,7 @@ __global__ void __launch_bounds__(GP_THREADS, 4) gp_partition_kernel(const long 
                                                                   unsigned short *__restrict__ loc) {
     __shared__ unsigned s_cnt[GP_NB], s_start[GP_NB + 1], s_goff[GP_NB];
     __shared__ unsigned s_part[GP_TILE];
-    __shared__ unsigned char s_reg[GP_TILE];
+    __shared__ unsigned char s_reg[PACK ? 1 : GP_TILE];
     if (threadIdx.x < GP_NB) {
         s_cnt[threadIdx.x] = 0;
         s_goff[threadIdx.x] = toffs[static_cast<int64_t>(blockIdx.x) * GP_NB + threadIdx.x];
@@ -175,8 +178,12 @@ __global__ void __launch_bounds__(GP_THREADS, 4) gp_partition_kernel(const long 
             const unsigned b = rk[j] >> 16;
             const unsigned l = s_start[b] + (rk[j] & 0xffffu);
             loc[r] = static_cast<unsigned short>(l);
-            s_part[l] = off[j];
-            s_reg[l] = static_cast<unsigned char>(b);
+            if (PACK) {
+                s_part[l] = off[j] | (b << 26);
+            } else {
+                s_part[l] = off[j];
+                s_reg[l] = static_cast<unsigned char>(b);
+            }
         } else {
             loc[r] = 0;  // the call fails; the row's output is never read
         }
@@ -184,8 +191,9 @@ __global__ void __launch_bounds__(GP_THREADS, 4) gp_partition_kernel(const long 
     __syncthreads();
     const int rows = static_cast<int>(s_start[GP_NB]);
     for (int l = threadIdx.x; l < rows; l += GP_THREADS) {
-        const unsigned b = s_reg[l];
-        part[s_goff[b] + static_cast<unsigned>(l) - s_start[b]] = s_part[l];
+        const unsigned v = s_part[l];
+        const unsigned b = PACK ? v >> 26 : s_reg[l];
+        part[s_goff[b] + static_cast<unsigned>(l) - s_start[b]] = PACK ? v & ((1u << 26) - 1) : v;
     }
 }
 
@@ -329,7 +337,10 @@ static vkc_status gather_partitioned(vkc_ctx *ctx, const unsigned long long *src
     gp_count_kernel<<<tiles, GP_THREADS, 0, ctx->stream>>>(idx, n, nsrc, rb, tiles, counts, ctx->status);
     scan_counts(ctx, counts, m, reinterpret_cast<unsigned *>(b + o_sums), offs);
     gp_tables_kernel<<<(tiles + GP_NB - 1) / GP_NB, 256, 0, ctx->stream>>>(counts, offs, tiles, tcounts, toffs);
-    gp_partition_kernel<<<tiles, GP_THREADS, 0, ctx->stream>>>(idx, n, nsrc, rb, tiles, toffs, part, loc);
+    if (rb <= 26)
+        gp_partition_kernel<true><<<tiles, GP_THREADS, 0, ctx->stream>>>(idx, n, nsrc, rb, tiles, toffs, part, loc);
+    else
+        gp_partition_kernel<false><<<tiles, GP_THREADS, 0, ctx->stream>>>(idx, n, nsrc, rb, tiles, toffs, part, loc);
     gp_region_kernel<<<tiles, GP_THREADS, 0, ctx->stream>>>(src, part, counts, offs, tiles, rb, vals);
     gp_restore_kernel<<<tiles, GP_THREADS, 0, ctx->stream>>>(vals, loc, tcounts, toffs, n, out);
     return launched(ctx, "gather_partitioned");
