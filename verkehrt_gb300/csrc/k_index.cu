@@ -275,30 +275,38 @@ __global__ void __launch_bounds__(GP_THREADS, 6) gp_restore_kernel(const unsigne
                                                                 unsigned long long *__restrict__ out) {
     __shared__ unsigned s_start[GP_NB + 1], s_goff[GP_NB];
     __shared__ unsigned long long s_vals[GP_TILE];
+    const int64_t base = static_cast<int64_t>(blockIdx.x) * GP_TILE;
+    // The rows' slots first (two to a register): their loads overlap the tables' and the runs'.
+    unsigned lp[GP_ITEMS / 2];
+#pragma unroll
+    for (int j = 0; j < GP_ITEMS; ++j) {
+        const int64_t r = base + j * GP_THREADS + threadIdx.x;
+        const unsigned lv = r < n ? static_cast<unsigned>(__ldcs(loc + r)) : 0u;
+        lp[j / 2] = (j & 1) ? (lp[j / 2] | (lv << 16)) : lv;
+    }
     const unsigned *tc = tcounts + static_cast<int64_t>(blockIdx.x) * GP_NB;
     if (threadIdx.x < 32) gp_starts([&](int b) { return tc[b]; }, s_start);
     if (threadIdx.x < GP_NB) s_goff[threadIdx.x] = toffs[static_cast<int64_t>(blockIdx.x) * GP_NB + threadIdx.x];
     __syncthreads();
     const int rows = static_cast<int>(s_start[GP_NB]);
-    unsigned at[GP_ITEMS];
+    // The runs straight into shared memory (cp.async: every copy in flight, no registers held).
 #pragma unroll
     for (int j = 0; j < GP_ITEMS; ++j) {
         const unsigned l = threadIdx.x + j * GP_THREADS;
-        const int b = l < static_cast<unsigned>(rows) ? gp_region_of(s_start, l) : 0;
-        at[j] = s_goff[b] + l - s_start[b];
+        if (l < static_cast<unsigned>(rows)) {
+            const int b = gp_region_of(s_start, l);
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(static_cast<unsigned>(__cvta_generic_to_shared(&s_vals[l]))),
+                         "l"(vals + s_goff[b] + l - s_start[b])
+                         : "memory");
+        }
     }
-    unsigned long long v[GP_ITEMS];
-#pragma unroll
-    for (int j = 0; j < GP_ITEMS; ++j) v[j] = threadIdx.x + j * GP_THREADS < rows ? __ldcs(vals + at[j]) : 0ull;
-#pragma unroll
-    for (int j = 0; j < GP_ITEMS; ++j)
-        if (threadIdx.x + j * GP_THREADS < rows) s_vals[threadIdx.x + j * GP_THREADS] = v[j];
+    asm volatile("cp.async.commit_group;" ::: "memory");
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
     __syncthreads();
-    const int64_t base = static_cast<int64_t>(blockIdx.x) * GP_TILE;
 #pragma unroll
     for (int j = 0; j < GP_ITEMS; ++j) {
         const int64_t r = base + j * GP_THREADS + threadIdx.x;
-        if (r < n) out[r] = s_vals[loc[r]];
+        if (r < n) out[r] = s_vals[(lp[j / 2] >> (16 * (j & 1))) & 0xffffu];
     }
 }
 
