@@ -236,10 +236,11 @@ __global__ void __launch_bounds__(GP_THREADS, 6) gp_region_kernel(const unsigned
     const unsigned total = s_start[GP_NB];
     const int64_t base = static_cast<int64_t>(blockIdx.x) * GP_TILE;
     if (base >= total) return;
-    // A thread's positions rise, so its region only moves forward from the first one's. The
-    // offsets are loaded first, then every source read is in flight at once; the source reads
-    // skip L1 (each touches one sector of a line that no other read of this block is likely
-    // to use).
+    // A thread's positions rise, so its region only moves forward from the first one's. In
+    // each quarter the offsets are loaded first, then the quarter's source reads are in flight
+    // together; the source reads skip L1 (each touches one sector of a line that no other read
+    // of this block is likely to use: the same reads as cp.async into shared memory, which
+    // allocates in L1, took 886 us against 310 at 2^26).
     int b = gp_region_of(s_start, static_cast<unsigned>(base + threadIdx.x < total ? base + threadIdx.x : total - 1));
     // Four quarters of GP_ITEMS / 4 rows: fewer registers, six blocks an SM.
     constexpr int H = GP_ITEMS / 4;
