@@ -357,11 +357,16 @@ __global__ void __launch_bounds__(GR_THREADS) gr_count_kernel(const long long *_
     if (threadIdx.x < GR_NB) h[threadIdx.x] = 0;
     __syncthreads();
     const int64_t base = static_cast<int64_t>(blockIdx.x) * GR_TILE;
+    // All of a thread's loads before its first atomic (the atomics keep the program's order).
+    unsigned long long k[GR_ITEMS];
 #pragma unroll
     for (int j = 0; j < GR_ITEMS; ++j) {
         const int64_t r = base + j * GR_THREADS + threadIdx.x;
-        if (r < n) atomicAdd(&h[gr_region(static_cast<unsigned long long>(__ldcs(keys + r)))], 1u);
+        k[j] = r < n ? static_cast<unsigned long long>(__ldcs(keys + r)) : 0ull;
     }
+#pragma unroll
+    for (int j = 0; j < GR_ITEMS; ++j)
+        if (base + j * GR_THREADS + threadIdx.x < n) atomicAdd(&h[gr_region(k[j])], 1u);
     __syncthreads();
     if (threadIdx.x < GR_NB) counts[static_cast<int64_t>(threadIdx.x) * tiles + blockIdx.x] = h[threadIdx.x];
 }

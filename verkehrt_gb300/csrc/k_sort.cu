@@ -53,11 +53,19 @@ __global__ void __launch_bounds__(256) rs_hist_kernel(const long long *__restric
     __shared__ unsigned h[8][RADIX];
     for (int i = threadIdx.x; i < 8 * RADIX; i += blockDim.x) (&h[0][0])[i] = 0;
     __syncthreads();
-    int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
-    for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride) {
-        unsigned long long k = image_of(__ldcs(keys + i));
+    // Eight rows a thread per round, all loaded before the first atomic (the atomics keep the
+    // program's order, so a load after one would wait for it).
+    constexpr int R = 8;
+    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    for (int64_t i0 = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i0 < n; i0 += R * stride) {
+        unsigned long long k[R];
 #pragma unroll
-        for (int p = 0; p < 8; ++p) atomicAdd(&h[p][(k >> (8 * p)) & 0xff], 1u);
+        for (int j = 0; j < R; ++j) k[j] = i0 + j * stride < n ? image_of(__ldcs(keys + i0 + j * stride)) : 0ull;
+#pragma unroll
+        for (int j = 0; j < R; ++j)
+            if (i0 + j * stride < n)
+#pragma unroll
+                for (int p = 0; p < 8; ++p) atomicAdd(&h[p][(k[j] >> (8 * p)) & 0xff], 1u);
     }
     __syncthreads();
     for (int i = threadIdx.x; i < 8 * RADIX; i += blockDim.x) {
@@ -594,7 +602,7 @@ static vkc_status argsort_i64(vkc_ctx *ctx, const vkc_value *args, int nargs, vk
     if ((st = scratch(ctx, 8 * RADIX * sizeof(unsigned), &p))) return release(st);
     auto *hist = static_cast<unsigned *>(p);
     VKC_CUDA(ctx, cudaMemsetAsync(hist, 0, 8 * RADIX * sizeof(unsigned), ctx->stream));
-    rs_hist_kernel<<<stream_grid(ctx, n, 256, 4, 16384), 256, 0, ctx->stream>>>(keys, n, hist);
+    rs_hist_kernel<<<stream_grid(ctx, n, 256, 6, 16384), 256, 0, ctx->stream>>>(keys, n, hist);
     if ((st = launched(ctx, "rs_hist"))) return release(st);
     void *h;
     if ((st = pinned(ctx, 2 * 8 * RADIX * sizeof(unsigned) + 16, &h))) return release(st);
