@@ -173,7 +173,8 @@ VKC_API void vkc_array_release(vkc_array *a);
 /* ------------------------------------------------------------------ kernel table */
 
 /* The kernels with a `cuda` entry, named as in the reference registry (src/kernels.rs:471-482,
- * Registry::new; names from src/kernels/scalar/*::register). Ids are dense, 0..count-1. */
+ * Registry::new; names from the register functions of src/kernels/scalar/). Ids are dense,
+ * 0..count-1. */
 VKC_API int vkc_kernel_count(void);
 VKC_API const char *vkc_kernel_name(int id);
 /* Registry::by_name, src/kernels.rs:620-622: the id, or -1. */

@@ -498,7 +498,7 @@ struct ChainReducer : DevReducer {
         fin(ctx, static_cast<u64 *>(state), tail_len);
         vkc_status st = launched(ctx, "family_chain_finish");
         if (st) return st;
-        u64 r;
+        u64 r = 0;
         if ((st = download(ctx, &r, 8, 32 * 8))) return st;
         *out = word_scalar(in, r);
         return VKC_OK;

@@ -37,7 +37,7 @@ static vkc_status io_buffers(vkc_ctx *ctx, unsigned char **buf) {
 // Reads `bytes` bytes of the open file `fd` to device address `dst`. On a read error, *err
 // gets errno and the call returns VKC_RUNTIME without a message (the caller words it).
 static vkc_status stream_file(vkc_ctx *ctx, int fd, size_t bytes, void *dst, int *err) {
-    unsigned char *buf;
+    unsigned char *buf = nullptr;
     vkc_status st;
     if ((st = io_buffers(ctx, &buf))) return st;
     size_t done = 0;

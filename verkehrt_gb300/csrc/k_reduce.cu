@@ -147,7 +147,7 @@ struct CountReducer : DevReducer {
         return launched(ctx, "count");
     }
     vkc_status finish(vkc_ctx *ctx, vkc_scalar *out) override {
-        unsigned long long v;
+        unsigned long long v = 0;
         vkc_status st = download(ctx, &v, sizeof v);
         if (st) return st;
         *out = scalar_i64(static_cast<int64_t>(v));
@@ -464,7 +464,7 @@ struct IntSumReducer : DevReducer {
         return launched(ctx, "isum");
     }
     vkc_status finish(vkc_ctx *ctx, vkc_scalar *out) override {
-        unsigned long long v;
+        unsigned long long v = 0;
         vkc_status st = download(ctx, &v, sizeof v);
         if (st) return st;
         *out = scalar_i64(static_cast<int64_t>(v));

@@ -865,7 +865,7 @@ vkc_status vkc_call(vkc_ctx *ctx, int id, const vkc_value *args, int nargs, vkc_
         Builder b{ctx, d->out_type, nullptr, 0, 0};
         st = d->sel(ctx, call.data(), nargs, 0, &b);
         if (st) return st;
-        vkc_array *o;
+        vkc_array *o = nullptr;
         st = finish_builder(b, &o);
         if (st) return st;
         out->kind = VKC_VALUE_ARRAY;
