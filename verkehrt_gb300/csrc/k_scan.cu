@@ -18,7 +18,7 @@ namespace vkc {
 constexpr int SC_THREADS = 512;  // compute threads (+ 2 warps)
 constexpr int SC_TILE = 8192;
 constexpr int SC_SLICE = SC_TILE / (SC_THREADS / 32);  // rows per warp
-constexpr int SC_VEC = 4;                              // rows per lane per step (one 32-byte load)
+constexpr int SC_VEC = 2;                              // rows per lane per step (one 16-byte load)
 constexpr int SC_STEPS = SC_SLICE / (32 * SC_VEC);
 constexpr int SC_WINDOW = 4;
 constexpr int SC_SLOTS = 3;   // tile ring: 1 copy in flight
@@ -85,8 +85,9 @@ struct SegRec {
 // A scan as a tile pass. A slot holds the tile's values (scanned in place by the stage) and
 // one byte per row: the start flags of scan_by as copied, then whether a segment starts at or
 // before the row in its warp slice. A compute warp's slice is SC_SLICE consecutive rows, read in
-// SC_STEPS steps of 128 rows; in a step lane l holds rows 4l..4l+3, so global stores are
-// coalesced and row order is (step, lane, item). A tile that is not whole, or not aligned, is
+// SC_STEPS steps of 64 rows; in a step lane l holds rows 2l and 2l + 1, so the lanes' 16-byte
+// reads of the slot meet every bank once (with four rows a lane, 32 bytes apart, each read took
+// two passes), global stores are coalesced and row order is (step, lane, item). A tile that is not whole, or not aligned, is
 // read from global memory instead of the slot.
 template <bool BY> struct ScanPass {
     static constexpr int THREADS = SC_THREADS;
@@ -118,14 +119,11 @@ template <bool BY> struct ScanPass {
                                               unsigned long long (&v)[SC_VEC], unsigned &f) const {
         f = 0;
         if (sm) {
-            const ulonglong2 *p = reinterpret_cast<const ulonglong2 *>(reinterpret_cast<const unsigned long long *>(slot) + j);
-            const ulonglong2 u0 = p[0], u1 = p[1];
+            const ulonglong2 u0 = *reinterpret_cast<const ulonglong2 *>(reinterpret_cast<const unsigned long long *>(slot) + j);
             v[0] = u0.x;
             v[1] = u0.y;
-            v[2] = u1.x;
-            v[3] = u1.y;
             if (BY) {
-                const unsigned m = *reinterpret_cast<const unsigned *>(slot + VAL_BYTES + j);
+                const unsigned m = *reinterpret_cast<const unsigned short *>(slot + VAL_BYTES + j);
 #pragma unroll
                 for (int k = 0; k < SC_VEC; ++k)
                     if ((m >> (8 * k)) & 0xffu) f |= 1u << k;
@@ -201,9 +199,8 @@ template <bool BY> struct ScanPass {
                     if (lane >= o) inc += y;
                 }
                 const unsigned long long pre = carry + inc - v[SC_VEC - 1];
-                ulonglong2 *p = reinterpret_cast<ulonglong2 *>(reinterpret_cast<unsigned long long *>(slot) + j);
-                p[0] = ulonglong2{v[0] + pre, v[1] + pre};
-                p[1] = ulonglong2{v[2] + pre, v[3] + pre};
+                *reinterpret_cast<ulonglong2 *>(reinterpret_cast<unsigned long long *>(slot) + j) =
+                    ulonglong2{v[0] + pre, v[1] + pre};
                 carry += __shfl_sync(FULL, inc, 31);
             }
             return Staged{};
@@ -233,10 +230,8 @@ template <bool BY> struct ScanPass {
                 if (static_cast<unsigned>(k) < first) v[k] += pre.sum;
                 if (static_cast<unsigned>(k) >= first || pre.start) has |= 1u << (8 * k);
             }
-            ulonglong2 *p = reinterpret_cast<ulonglong2 *>(reinterpret_cast<unsigned long long *>(slot) + j);
-            p[0] = ulonglong2{v[0], v[1]};
-            p[1] = ulonglong2{v[2], v[3]};
-            *reinterpret_cast<unsigned *>(slot + VAL_BYTES + j) = has;
+            *reinterpret_cast<ulonglong2 *>(reinterpret_cast<unsigned long long *>(slot) + j) = ulonglong2{v[0], v[1]};
+            *reinterpret_cast<unsigned short *>(slot + VAL_BYTES + j) = static_cast<unsigned short>(has);
             carry = seg_op(carry, SegRec::shfl(inc, 31));
         }
         return Staged{};
@@ -249,11 +244,10 @@ template <bool BY> struct ScanPass {
         for (int s = 0; s < SC_STEPS; ++s) {
             const int j = w * SC_SLICE + s * (32 * SC_VEC) + lane * SC_VEC;
             const int64_t i0 = r0 + j;
-            const ulonglong2 *p = reinterpret_cast<const ulonglong2 *>(reinterpret_cast<const unsigned long long *>(slot) + j);
-            const ulonglong2 u0 = p[0], u1 = p[1];
-            unsigned long long e[4] = {u0.x, u0.y, u1.x, u1.y};
+            const ulonglong2 u0 = *reinterpret_cast<const ulonglong2 *>(reinterpret_cast<const unsigned long long *>(slot) + j);
+            unsigned long long e[SC_VEC] = {u0.x, u0.y};
             if constexpr (BY) {
-                const unsigned has = *reinterpret_cast<const unsigned *>(slot + VAL_BYTES + j);
+                const unsigned has = *reinterpret_cast<const unsigned short *>(slot + VAL_BYTES + j);
 #pragma unroll
                 for (int k = 0; k < SC_VEC; ++k)
                     if (!((has >> (8 * k)) & 0xffu)) e[k] += pre.sum;
@@ -262,12 +256,7 @@ template <bool BY> struct ScanPass {
                 for (int k = 0; k < SC_VEC; ++k) e[k] += pre.sum;
             }
             if (aligned && i0 + SC_VEC <= n) {
-                ulonglong4_32a u;
-                u.x = e[0];
-                u.y = e[1];
-                u.z = e[2];
-                u.w = e[3];
-                *reinterpret_cast<ulonglong4_32a *>(out + i0) = u;
+                *reinterpret_cast<ulonglong2 *>(out + i0) = ulonglong2{e[0], e[1]};
             } else {
 #pragma unroll
                 for (int k = 0; k < SC_VEC; ++k)
