@@ -18,8 +18,6 @@ namespace vkc {
 constexpr int SC_THREADS = 512;  // compute threads (+ 2 warps)
 constexpr int SC_TILE = 8192;
 constexpr int SC_SLICE = SC_TILE / (SC_THREADS / 32);  // rows per warp
-constexpr int SC_VEC = 2;                              // rows per lane per step (one 16-byte load)
-constexpr int SC_STEPS = SC_SLICE / (32 * SC_VEC);
 constexpr int SC_WINDOW = 4;
 constexpr int SC_SLOTS = 3;   // tile ring: 1 copy in flight
 constexpr int SC_BLOCKS = 1;  // blocks per SM
@@ -85,11 +83,16 @@ struct SegRec {
 // A scan as a tile pass. A slot holds the tile's values (scanned in place by the stage) and
 // one byte per row: the start flags of scan_by as copied, then whether a segment starts at or
 // before the row in its warp slice. A compute warp's slice is SC_SLICE consecutive rows, read in
-// SC_STEPS steps of 64 rows; in a step lane l holds rows 2l and 2l + 1, so the lanes' 16-byte
-// reads of the slot meet every bank once (with four rows a lane, 32 bytes apart, each read took
-// two passes), global stores are coalesced and row order is (step, lane, item). A tile that is not whole, or not aligned, is
+// STEPS steps of 32 * VEC rows; in a step lane l holds rows VEC l .. VEC l + VEC - 1, so global
+// stores are coalesced and row order is (step, lane, item). The plain scan takes two rows a lane
+// (one 16-byte read of the slot a step, every bank once: with four rows a lane, 32 bytes apart,
+// each read took two passes; 0.76 against 0.88 ms at 2^28); the segmented scan keeps four,
+// whose fewer warp scans of (sum, start) pairs cost less than the bank passes (0.56 against
+// 0.60 ms at 2^27). A tile that is not whole, or not aligned, is
 // read from global memory instead of the slot.
 template <bool BY> struct ScanPass {
+    static constexpr int VEC = BY ? 4 : 2;  // rows per lane per step
+    static constexpr int STEPS = SC_SLICE / (32 * VEC);
     static constexpr int THREADS = SC_THREADS;
     static constexpr int VAL_BYTES = 8 * SC_TILE;
     static constexpr int SLOT_BYTES = VAL_BYTES + SC_TILE;
@@ -116,21 +119,26 @@ template <bool BY> struct ScanPass {
     // The rows of one step and their start flags (bit k: row 4l + k), from the slot or from
     // global memory. Row 0 of the array starts a segment whatever its byte (scan.rs:300-308).
     __device__ __forceinline__ void load_step(bool sm, const unsigned char *slot, int j, int64_t i0,
-                                              unsigned long long (&v)[SC_VEC], unsigned &f) const {
+                                              unsigned long long (&v)[VEC], unsigned &f) const {
         f = 0;
         if (sm) {
-            const ulonglong2 u0 = *reinterpret_cast<const ulonglong2 *>(reinterpret_cast<const unsigned long long *>(slot) + j);
-            v[0] = u0.x;
-            v[1] = u0.y;
-            if (BY) {
-                const unsigned m = *reinterpret_cast<const unsigned short *>(slot + VAL_BYTES + j);
+            const ulonglong2 *p = reinterpret_cast<const ulonglong2 *>(reinterpret_cast<const unsigned long long *>(slot) + j);
 #pragma unroll
-                for (int k = 0; k < SC_VEC; ++k)
+            for (int c = 0; c < VEC / 2; ++c) {
+                const ulonglong2 u = p[c];
+                v[2 * c] = u.x;
+                v[2 * c + 1] = u.y;
+            }
+            if (BY) {
+                const unsigned m = VEC == 4 ? *reinterpret_cast<const unsigned *>(slot + VAL_BYTES + j)
+                                            : *reinterpret_cast<const unsigned short *>(slot + VAL_BYTES + j);
+#pragma unroll
+                for (int k = 0; k < VEC; ++k)
                     if ((m >> (8 * k)) & 0xffu) f |= 1u << k;
             }
         } else {
 #pragma unroll
-            for (int k = 0; k < SC_VEC; ++k) {
+            for (int k = 0; k < VEC; ++k) {
                 const bool in = i0 + k < n;
                 v[k] = in ? x[i0 + k] : 0ull;
                 if (BY && in && starts[i0 + k]) f |= 1u << k;
@@ -147,31 +155,31 @@ template <bool BY> struct ScanPass {
         const bool sm = whole(tile);
         unsigned long long t = 0;
         unsigned last = 0;  // the last start in the slice, as a position in row order + 1 (0: none)
-        unsigned long long v[SC_STEPS][SC_VEC];
-        unsigned f[SC_STEPS];
+        unsigned long long v[STEPS][VEC];
+        unsigned f[STEPS];
 #pragma unroll
-        for (int s = 0; s < SC_STEPS; ++s) {
-            const int j = w * SC_SLICE + s * (32 * SC_VEC) + lane * SC_VEC;
+        for (int s = 0; s < STEPS; ++s) {
+            const int j = w * SC_SLICE + s * (32 * VEC) + lane * VEC;
             load_step(sm, slot, j, r0 + j, v[s], f[s]);
         }
         if (!BY) {
 #pragma unroll
-            for (int s = 0; s < SC_STEPS; ++s)
+            for (int s = 0; s < STEPS; ++s)
 #pragma unroll
-                for (int k = 0; k < SC_VEC; ++k) t += v[s][k];
+                for (int k = 0; k < VEC; ++k) t += v[s][k];
             return Seg{warp_sum(t), 0};
         }
 #pragma unroll
-        for (int s = 0; s < SC_STEPS; ++s)
+        for (int s = 0; s < STEPS; ++s)
 #pragma unroll
-            for (int k = 0; k < SC_VEC; ++k)
-                if ((f[s] >> k) & 1u) last = (s * 32 + lane) * SC_VEC + k + 1;
+            for (int k = 0; k < VEC; ++k)
+                if ((f[s] >> k) & 1u) last = (s * 32 + lane) * VEC + k + 1;
         last = __reduce_max_sync(FULL, last);
 #pragma unroll
-        for (int s = 0; s < SC_STEPS; ++s)
+        for (int s = 0; s < STEPS; ++s)
 #pragma unroll
-            for (int k = 0; k < SC_VEC; ++k)
-                if (static_cast<unsigned>((s * 32 + lane) * SC_VEC + k + 1) >= last) t += v[s][k];
+            for (int k = 0; k < VEC; ++k)
+                if (static_cast<unsigned>((s * 32 + lane) * VEC + k + 1) >= last) t += v[s][k];
         return Seg{warp_sum(t), last != 0};
     }
 
@@ -185,20 +193,20 @@ template <bool BY> struct ScanPass {
             // Without segments: a plain wrapping add scan of the slice, in place.
             unsigned long long carry = 0;
 #pragma unroll
-            for (int s = 0; s < SC_STEPS; ++s) {
-                const int j = w * SC_SLICE + s * (32 * SC_VEC) + lane * SC_VEC;
-                unsigned long long v[SC_VEC];
+            for (int s = 0; s < STEPS; ++s) {
+                const int j = w * SC_SLICE + s * (32 * VEC) + lane * VEC;
+                unsigned long long v[VEC];
                 unsigned f;
                 load_step(sm, slot, j, r0 + j, v, f);
 #pragma unroll
-                for (int k = 1; k < SC_VEC; ++k) v[k] += v[k - 1];
-                unsigned long long inc = v[SC_VEC - 1];
+                for (int k = 1; k < VEC; ++k) v[k] += v[k - 1];
+                unsigned long long inc = v[VEC - 1];
 #pragma unroll
                 for (int o = 1; o < 32; o <<= 1) {
                     const unsigned long long y = __shfl_up_sync(FULL, inc, o);
                     if (lane >= o) inc += y;
                 }
-                const unsigned long long pre = carry + inc - v[SC_VEC - 1];
+                const unsigned long long pre = carry + inc - v[VEC - 1];
                 *reinterpret_cast<ulonglong2 *>(reinterpret_cast<unsigned long long *>(slot) + j) =
                     ulonglong2{v[0] + pre, v[1] + pre};
                 carry += __shfl_sync(FULL, inc, 31);
@@ -207,15 +215,15 @@ template <bool BY> struct ScanPass {
         }
         Seg carry{0, 0};  // the slice so far
 #pragma unroll
-        for (int s = 0; s < SC_STEPS; ++s) {
-            const int j = w * SC_SLICE + s * (32 * SC_VEC) + lane * SC_VEC;
-            unsigned long long v[SC_VEC];
+        for (int s = 0; s < STEPS; ++s) {
+            const int j = w * SC_SLICE + s * (32 * VEC) + lane * VEC;
+            unsigned long long v[VEC];
             unsigned f;
             load_step(sm, slot, j, r0 + j, v, f);
             // Lane-local inclusive segmented scan of the 4 rows.
             Seg loc{0, 0};
 #pragma unroll
-            for (int k = 0; k < SC_VEC; ++k) {
+            for (int k = 0; k < VEC; ++k) {
                 loc = seg_op(loc, Seg{v[k], (f >> k) & 1u});
                 v[k] = loc.sum;
             }
@@ -223,15 +231,18 @@ template <bool BY> struct ScanPass {
             Seg ex = SegRec::shfl_up(inc, 1);
             if (lane == 0) ex = Seg{0, 0};
             const Seg pre = seg_op(carry, ex);  // the slice before this lane's rows
-            const unsigned first = f ? __ffs(f) - 1 : SC_VEC;
+            const unsigned first = f ? __ffs(f) - 1 : VEC;
             unsigned has = 0;
 #pragma unroll
-            for (int k = 0; k < SC_VEC; ++k) {
+            for (int k = 0; k < VEC; ++k) {
                 if (static_cast<unsigned>(k) < first) v[k] += pre.sum;
                 if (static_cast<unsigned>(k) >= first || pre.start) has |= 1u << (8 * k);
             }
-            *reinterpret_cast<ulonglong2 *>(reinterpret_cast<unsigned long long *>(slot) + j) = ulonglong2{v[0], v[1]};
-            *reinterpret_cast<unsigned short *>(slot + VAL_BYTES + j) = static_cast<unsigned short>(has);
+            ulonglong2 *p = reinterpret_cast<ulonglong2 *>(reinterpret_cast<unsigned long long *>(slot) + j);
+#pragma unroll
+            for (int c = 0; c < VEC / 2; ++c) p[c] = ulonglong2{v[2 * c], v[2 * c + 1]};
+            if constexpr (VEC == 4) *reinterpret_cast<unsigned *>(slot + VAL_BYTES + j) = has;
+            else *reinterpret_cast<unsigned short *>(slot + VAL_BYTES + j) = static_cast<unsigned short>(has);
             carry = seg_op(carry, SegRec::shfl(inc, 31));
         }
         return Staged{};
@@ -241,25 +252,41 @@ template <bool BY> struct ScanPass {
         const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
         const int64_t r0 = static_cast<int64_t>(tile) * SC_TILE;
 #pragma unroll
-        for (int s = 0; s < SC_STEPS; ++s) {
-            const int j = w * SC_SLICE + s * (32 * SC_VEC) + lane * SC_VEC;
+        for (int s = 0; s < STEPS; ++s) {
+            const int j = w * SC_SLICE + s * (32 * VEC) + lane * VEC;
             const int64_t i0 = r0 + j;
-            const ulonglong2 u0 = *reinterpret_cast<const ulonglong2 *>(reinterpret_cast<const unsigned long long *>(slot) + j);
-            unsigned long long e[SC_VEC] = {u0.x, u0.y};
-            if constexpr (BY) {
-                const unsigned has = *reinterpret_cast<const unsigned short *>(slot + VAL_BYTES + j);
+            const ulonglong2 *p = reinterpret_cast<const ulonglong2 *>(reinterpret_cast<const unsigned long long *>(slot) + j);
+            unsigned long long e[VEC];
 #pragma unroll
-                for (int k = 0; k < SC_VEC; ++k)
+            for (int c = 0; c < VEC / 2; ++c) {
+                const ulonglong2 u = p[c];
+                e[2 * c] = u.x;
+                e[2 * c + 1] = u.y;
+            }
+            if constexpr (BY) {
+                const unsigned has = VEC == 4 ? *reinterpret_cast<const unsigned *>(slot + VAL_BYTES + j)
+                                              : *reinterpret_cast<const unsigned short *>(slot + VAL_BYTES + j);
+#pragma unroll
+                for (int k = 0; k < VEC; ++k)
                     if (!((has >> (8 * k)) & 0xffu)) e[k] += pre.sum;
             } else {
 #pragma unroll
-                for (int k = 0; k < SC_VEC; ++k) e[k] += pre.sum;
+                for (int k = 0; k < VEC; ++k) e[k] += pre.sum;
             }
-            if (aligned && i0 + SC_VEC <= n) {
-                *reinterpret_cast<ulonglong2 *>(out + i0) = ulonglong2{e[0], e[1]};
+            if (aligned && i0 + VEC <= n) {
+                if constexpr (VEC == 4) {
+                    ulonglong4_32a u;
+                    u.x = e[0];
+                    u.y = e[1];
+                    u.z = e[2];
+                    u.w = e[3];
+                    *reinterpret_cast<ulonglong4_32a *>(out + i0) = u;
+                } else {
+                    *reinterpret_cast<ulonglong2 *>(out + i0) = ulonglong2{e[0], e[1]};
+                }
             } else {
 #pragma unroll
-                for (int k = 0; k < SC_VEC; ++k)
+                for (int k = 0; k < VEC; ++k)
                     if (i0 + k < n) out[i0 + k] = e[k];
             }
         }
