@@ -53,7 +53,7 @@ __global__ void __launch_bounds__(256) rs_hist_kernel(const long long *__restric
     __shared__ unsigned h[8][RADIX];
     for (int i = threadIdx.x; i < 8 * RADIX; i += blockDim.x) (&h[0][0])[i] = 0;
     __syncthreads();
-    // Eight rows a thread per round, all loaded before the first atomic (the atomics keep the
+    // Eight rows a thread per loop pass, all loaded before the first atomic (the atomics keep the
     // program's order, so a load after one would wait for it).
     constexpr int R = 8;
     const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
