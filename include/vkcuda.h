@@ -113,7 +113,7 @@ VKC_API vkc_status vkc_set_cache_limit(vkc_ctx *ctx, size_t bytes);
 /* Launch shapes chosen per size class (0: n < 2^20, 1: n < 2^24, 2: larger) by the committed
  * autotuner table (the reference fixes its tile sizes per ISA; these are this backend's):
  * "radix_items" (rows per thread of the argsort passes: 8, 12, 16), "stream_blocks_per_sm"
- * (count/min/max/argmin/argmax/integer sums: 2, 4, 8, 16), "gather_rows_per_thread" (1, 2, 4)
+ * (count/min/max/argmin/argmax/integer sums: 2, 4, 5, 6, 8, 12, 16), "gather_rows_per_thread" (1, 2, 4)
  * and "group_first_table_log2" (group_id's first hash table, 18 .. 22). vkc_tune_set
  * overrides one entry for this context (the autotuner measures candidates that way); results
  * never depend on it.

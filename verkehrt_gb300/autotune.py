@@ -35,7 +35,7 @@ KNOBS = ["radix_items", "stream_blocks_per_sm", "gather_rows_per_thread", "group
          "canon_chain_rows"]
 CANDIDATES = {
     "radix_items": [8, 12, 16],
-    "stream_blocks_per_sm": [2, 4, 8, 16],
+    "stream_blocks_per_sm": [2, 4, 5, 6, 8, 12, 16],
     "gather_rows_per_thread": [1, 2, 4],
     "group_first_table_log2": [18, 19, 20, 21, 22],
     "canon_chain_rows": [4, 8, 16],

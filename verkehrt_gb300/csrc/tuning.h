@@ -39,7 +39,7 @@ inline const char *tune_knob_name(int k) {
 inline bool tune_allowed(int k, int v) {
     switch (k) {
     case TK_RADIX_ITEMS: return v == 8 || v == 12 || v == 16;
-    case TK_STREAM_BLOCKS: return v == 2 || v == 4 || v == 8 || v == 16;
+    case TK_STREAM_BLOCKS: return v == 2 || v == 4 || v == 5 || v == 6 || v == 8 || v == 12 || v == 16;
     case TK_GATHER_ROWS: return v == 1 || v == 2 || v == 4;
     case TK_GROUP_FIRST_LOG2: return v >= 18 && v <= 22;
     case TK_CHAIN_ROWS: return v == 4 || v == 8 || v == 16;

@@ -5,4 +5,4 @@
 // size classes n < 2^20, n < 2^24, and larger.
 // Measured on: NVIDIA GB300, 2026-12-04 (median of the runs in tuning_table.json).
 #pragma once
-#define VKC_TUNE_TABLE { {8, 12, 16}, {16, 8, 16}, {1, 2, 1}, {22, 21, 22}, {16, 8, 8} }
+#define VKC_TUNE_TABLE { {8, 12, 16}, {12, 16, 5}, {1, 2, 1}, {22, 21, 22}, {16, 8, 8} }
