@@ -1820,8 +1820,8 @@ __device__ __forceinline__ int sb_exclusive_max(int v, int *warp_max) {
 // from `carried` (+0.0 in its first window) and whose first block's tail from `carried_c`;
 // otherwise the consecutive segments m .. m2 - 1 of the tile, each of at most SBP_CAP rows,
 // their lanes and first tails from +0.0. In the order of the oracle's restatement: lane l of a
-// segment adds its rows l, l + 16, ... of the whole blocks (the first add from +0.0 is the FP64
-// add, the rest add_bits, which equals it); the row closing a whole block gets the pairwise
+// segment adds its rows l, l + 16, ... of the whole blocks (add_bits, which equals the IEEE add
+// and takes the FP64 add itself from +0.0); the row closing a whole block gets the pairwise
 // combine (+8, +4, +2, +1) of the lane states after it; the other rows of a block are the chain
 // from the combine before the block (+0.0 for the segment's first block).
 __device__ __forceinline__ void sb_pack(SbSmem &sm, const unsigned long long *__restrict__ x,
